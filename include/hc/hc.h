@@ -1,0 +1,295 @@
+/*
+ * hc.h — C ABI of the GB300 hydroelastic contact engine.
+ *
+ * This is the drop-in boundary for the contact-surface path of the MuJoCo
+ * contact-surfaces plugin (ubi-agni/mujoco_contact_surfaces).  Every entry
+ * point takes plain pointers and sizes; no C++ or torch types cross it.
+ * Each entry point names the reference interface it replaces, as
+ * `file:line` within the reference project:
+ *
+ *   P  = mujoco_contact_surfaces/src/mujoco_contact_surfaces_plugin.cpp
+ *   PH = mujoco_contact_surfaces/include/mujoco_contact_surfaces/mujoco_contact_surfaces_plugin.h
+ *   CT = mujoco_contact_surfaces/include/mujoco_contact_surfaces/common_types.h
+ *   UH = mujoco_contact_surfaces/include/mujoco_contact_surfaces/plugin_utils.h
+ *   FS = mujoco_contact_surface_sensors/src/flat_tactile_sensor.cpp
+ *
+ * Conventions
+ *   - Geoms are addressed by the caller's geom id (MuJoCo geom index).
+ *     Geom types use MuJoCo's mjtGeom numbering.
+ *   - Poses are MuJoCo's geom_xpos (3 doubles) and geom_xmat (9 doubles,
+ *     row-major) per geom id; velocities are mj_objectVelocity(...,
+ *     flg_local=0) 6-vectors [omega; v] at the geom origin, world aligned.
+ *   - The contact pair (g1, g2) is re-ordered so that M is the geom that was
+ *     registered first (the reference orders by Drake geometry id, which it
+ *     assigns in parse order).  Wrenches are reported on M:
+ *     force on M and torque on M about M's origin (geom_xpos of M).  The
+ *     wrench on N is the negative force and
+ *     -(torque + (x_M - x_N) x force) about N's origin.
+ *   - Every function returns hc_status; HC_OK is 0.  hc_last_error() gives
+ *     a message for the calling thread's last failure.
+ *   - A context owns one CUDA stream and all device buffers.  Calls on one
+ *     context are not thread safe; different contexts are independent.
+ *   - Allocation happens only in create / add_geom / set_pairs /
+ *     add_flat_sensor and when a capacity grows; hc_step allocates nothing.
+ */
+#ifndef HC_HC_H_
+#define HC_HC_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HC_API __attribute__((visibility("default")))
+
+typedef enum {
+  HC_OK = 0,
+  HC_ERR_INVALID_ARG = 1,  /* bad id, size, NaN/Inf pose, bad mesh          */
+  HC_ERR_UNSUPPORTED = 2,  /* pair or geom type without a contact surface:
+                              the caller falls back to its default narrow
+                              phase exactly as P:270-271 does              */
+  HC_ERR_OVERFLOW = 3,     /* a fixed-capacity device buffer overflowed;
+                              results are incomplete, grow and re-run      */
+  HC_ERR_TIMEOUT = 4,      /* a bounded device-side wait gave up            */
+  HC_ERR_CUDA = 5,         /* CUDA runtime error (message in hc_last_error) */
+  HC_ERR_DEGENERATE = 6,   /* degenerate input geometry (zero-volume mesh)  */
+  HC_ERR_NOT_READY = 7,    /* step not run yet / no such output             */
+  HC_ERR_NO_DEVICE = 8     /* no CUDA device visible                        */
+} hc_status;
+
+/* MuJoCo mjtGeom numbering. */
+enum {
+  HC_GEOM_PLANE = 0,
+  HC_GEOM_HFIELD = 1,
+  HC_GEOM_SPHERE = 2,
+  HC_GEOM_CAPSULE = 3,
+  HC_GEOM_ELLIPSOID = 4,
+  HC_GEOM_CYLINDER = 5,
+  HC_GEOM_BOX = 6,
+  HC_GEOM_MESH = 7
+};
+
+/* cs::HydroelasticContactRepresentation (PH:251, P:574-591). */
+enum { HC_REPR_TRIANGLE = 0, HC_REPR_POLYGON = 1 };
+
+/* Contact kinds (PH:134-138). */
+enum { HC_RIGID = 0, HC_SOFT = 1 };
+
+/* Query kinds chosen by the pair dispatch. */
+enum {
+  HC_QUERY_NONE = 0,        /* default narrow phase            */
+  HC_QUERY_SOFT_RIGID = 1,  /* ComputeContactSurfaceFromSoftVolumeRigidSurface */
+  HC_QUERY_SOFT_HALFSPACE = 2, /* ...SoftVolumeRigidHalfSpace              */
+  HC_QUERY_SOFT_SOFT = 3    /* ComputeContactSurfaceFromCompliantVolumes    */
+};
+
+/* Flat sensor windows (FS:140-168). */
+enum { HC_WINDOW_NONE = 0, HC_WINDOW_GAUSS = 1, HC_WINDOW_TUKEY = 2, HC_WINDOW_SQUARE = 3 };
+
+/* Debug flags for hc_set_debug. */
+enum {
+  HC_DEBUG_CANDIDATES = 1  /* record every non-empty element pair (for the
+                              canonical-sort parity check)                 */
+};
+
+typedef struct hc_context hc_context;
+
+typedef struct {
+  int device;               /* CUDA device ordinal                          */
+  int representation;       /* HC_REPR_TRIANGLE (default) or HC_REPR_POLYGON */
+  int apply_forces;         /* cs::ApplyContactSurfaceForces (default 1)     */
+  int use_graph;            /* capture hc_step in a CUDA graph (default 1)   */
+  int64_t item_capacity;    /* cluster-pair work items (0 = automatic)       */
+  int64_t face_capacity;    /* contact polygons kept for surfaces/sensors    */
+} hc_config;
+
+/* Fill a config with defaults. */
+HC_API void hc_config_default(hc_config* cfg);
+
+/* Message of the calling thread's last failing call ("" when none). */
+HC_API const char* hc_last_error(void);
+
+/* Library version string. */
+HC_API const char* hc_version(void);
+
+/* ---- context ------------------------------------------------------------
+ * Replaces the plugin object's construction and load(m, d).    */
+HC_API hc_status hc_context_create(const hc_config* cfg, hc_context** out);
+/* Replaces the plugin destructor. */
+HC_API hc_status hc_context_destroy(hc_context* ctx);
+/* Replaces reset(): forgets the last step's outputs. */
+HC_API hc_status hc_reset(hc_context* ctx);
+
+/* ---- geoms --------------------------------------------------------------
+ * Replaces the per-geom branch of parseMujocoCustomFields:
+ * `cs5` is the cs::<geom> numeric [E, dissipation, resolutionHint,
+ * mu_static, mu_dynamic].  E > 0 makes a soft geom (tet mesh +
+ * linear pressure field E*extent), E <= 0 a rigid one (triangle mesh; a
+ * plane is a rigid half-space).  `size` is MuJoCo's geom_size (half sizes).
+ * `mesh_vert`/`mesh_face` are used for HC_GEOM_MESH only (nvert x 3
+ * doubles, nface x 3 ints, outward counter-clockwise faces).
+ * `out_kind` receives HC_SOFT / HC_RIGID, or -1 when the geom type has no
+ * contact surface (capsule, hfield, soft plane: P:634-647).  Registration
+ * order defines the M/N order of every pair.                    */
+HC_API hc_status hc_add_geom(hc_context* ctx, int geom_id, int type, const double size[3],
+                             const double cs5[5], const double* mesh_vert, int nvert,
+                             const int* mesh_face, int nface, int* out_kind);
+
+/* Replaces onGeomChanged: regenerate the geom's mesh and
+ * pressure field for a new size and rebuild or refit its LBVH.           */
+HC_API hc_status hc_update_geom_size(hc_context* ctx, int geom_id, const double size[3]);
+
+typedef struct {
+  int kind;          /* HC_SOFT / HC_RIGID / -1                           */
+  int type;          /* mjtGeom                                            */
+  int order;         /* registration index (the reference's Drake id order) */
+  int n_elements;    /* tets (soft) or triangles (rigid); 0 for a plane      */
+  int n_vertices;
+  double E, dissipation, resolution_hint, mu_static, mu_dynamic;
+} hc_geom_info;
+HC_API hc_status hc_get_geom_info(hc_context* ctx, int geom_id, hc_geom_info* out);
+
+/* Copy the geom's mesh as stored (vertices rounded to float, body frame).
+ * Soft: elems = 4 ints per tet, pressure = one value per vertex.
+ * Rigid: elems = 3 ints per triangle, pressure untouched.  Pass NULL
+ * pointers to query sizes only.                                           */
+HC_API hc_status hc_get_geom_mesh(hc_context* ctx, int geom_id, double* vert, double* pressure,
+                                  int* elems);
+
+/* Stateless mesh generation (host only, no device needed): the same
+ * generator hc_add_geom uses.  Two calls: first with NULL outputs to get
+ * the sizes.                                                             */
+HC_API hc_status hc_generate_mesh(int type, const double size[3], const double cs5[5],
+                                  const double* mesh_vert, int nvert, const int* mesh_face,
+                                  int nface, int* out_kind, int* out_nvert, int* out_nelem,
+                                  double* vert, double* pressure, int* elems);
+
+/* ---- per-step inputs ----------------------------------------------------
+ * Poses and velocities for geom ids [0, n_geom).  Replaces getGeomPose
+ * and getGeomVelocity.  Host pointers; copied to
+ * the device on the context stream.  `vel` may be NULL (zero velocity).  */
+HC_API hc_status hc_set_poses(hc_context* ctx, int n_geom, const double* xpos,
+                              const double* xmat, const double* vel);
+/* Same with device pointers (already in HBM, same layout).               */
+HC_API hc_status hc_set_poses_device(hc_context* ctx, int n_geom, const double* d_xpos,
+                                     const double* d_xmat, const double* d_vel);
+
+/* ---- pair dispatch ------------------------------------------------------
+ * Replaces the classification part of collision_cb: decides
+ * per pair which contact-surface query runs (or HC_ERR_UNSUPPORTED when
+ * either geom lacks cs:: properties or both are rigid, the P:270-271
+ * fallback).  per_pair_status and per_pair_query may be NULL.            */
+HC_API hc_status hc_set_pairs(hc_context* ctx, int n_pair, const int* g1, const int* g2,
+                              int* per_pair_status, int* per_pair_query);
+
+/* Runs one step over the current pairs and poses: broadphase, clipping,
+ * quadrature, the force law and the per-pair
+ * wrench, plus taxel binning for every flat sensor (FS:262-402).
+ * Asynchronous on the context stream.                                    */
+HC_API hc_status hc_step(hc_context* ctx);
+
+/* Convenience: hc_set_pairs + hc_step. */
+HC_API hc_status hc_collide_pairs(hc_context* ctx, int n_pair, const int* g1, const int* g2,
+                                  int* per_pair_status);
+
+/* Per-pair wrench on M about M's origin, world frame: n_pair x
+ * [fx fy fz tx ty tz] doubles.  Synchronises the context stream.        */
+HC_API hc_status hc_get_wrenches(hc_context* ctx, double* wrench);
+/* Device pointer to the same n_pair x 6 doubles (valid until the next
+ * hc_set_pairs).                                                        */
+HC_API hc_status hc_get_wrenches_device(hc_context* ctx, const double** d_wrench);
+/* The query kind and M/N order chosen for each pair: m_geom/n_geom ids. */
+HC_API hc_status hc_get_pair_order(hc_context* ctx, int* query, int* m_geom, int* n_geom);
+
+typedef struct {
+  int32_t n_polygons;       /* non-empty clipped element pairs            */
+  int32_t n_faces;          /* quadrature points kept (area > 1e-14 and
+                               gradient checks)           */
+  int32_t n_near_degenerate;/* polygons with a vertex within 1e-12 of a
+                               clip plane                                 */
+  int32_t n_items;          /* cluster-pair work items visited            */
+  double area;              /* total contact area (faces kept)            */
+  double total_fn0;         /* sum of A*p0                    */
+} hc_pair_stats;
+HC_API hc_status hc_get_pair_stats(hc_context* ctx, hc_pair_stats* out);
+
+/* Contact surface of one pair, copied to host memory, world frame, in a
+ * canonical order (soft element, other element).  Polygons are stored as
+ * vertex lists: poly_offset[n_poly+1] into vert (3 doubles each) and
+ * vert_pressure; normal (3 per polygon, out of N into M); elem_a/elem_b
+ * (original element indices: soft tet, and rigid triangle / soft tet of
+ * the second body / -1 for a half-space).  Call with NULL arrays to get
+ * the counts.  Replaces access to ContactSurface (CT:59-66).             */
+typedef struct {
+  int n_poly;
+  int n_vert;
+  int* poly_offset;
+  double* vert;
+  double* vert_pressure;
+  double* normal;
+  int* elem_a;
+  int* elem_b;
+} hc_surface_view;
+HC_API hc_status hc_get_surface(hc_context* ctx, int pair, hc_surface_view* view);
+
+/* Debug record of every non-empty element pair (HC_DEBUG_CANDIDATES). */
+typedef struct {
+  int32_t pair;
+  int32_t elem_a;
+  int32_t elem_b;
+  int32_t n_vert;   /* vertices of the clipped polygon                  */
+  int32_t flags;    /* bit 0: near-degenerate                           */
+} hc_candidate;
+HC_API hc_status hc_set_debug(hc_context* ctx, int flags);
+HC_API hc_status hc_get_candidates(hc_context* ctx, hc_candidate* out, int64_t capacity,
+                                   int64_t* count);
+
+/* ---- flat tactile sensor ------------------------------------------------
+ * Replaces FlatTactileSensor::load (FS:127-214) and bvh_update
+ * (FS:262-402): a cx x cy taxel grid on the top face of a box geom at
+ * `resolution`, sampling_resolution^2 rays per cell, optional window.
+ * cx = floor(2*xs/resolution + 0.1) (FS:196-197).                       */
+HC_API hc_status hc_add_flat_sensor(hc_context* ctx, int geom_id, double resolution,
+                                    int sampling_resolution, int window, double sigma,
+                                    int* out_sensor, int* out_cx, int* out_cy);
+/* The sensor's taxel map of the last step (cx*cy floats, index x + cy*y as
+ * FS:396-397).  Synchronises the context stream.                        */
+HC_API hc_status hc_get_taxels(hc_context* ctx, int sensor, float* out);
+/* Device pointer to all sensors' taxel maps (sensor-major). */
+HC_API hc_status hc_get_taxels_device(hc_context* ctx, const float** d_taxels,
+                                      int64_t* n_floats);
+
+/* ---- adjoint -------------------------------------------------------------
+ * Gradient of L with respect to both geoms' 6-DoF poses (twist
+ * [dtheta; dx], world frame, applied as X <- exp(dtheta) X, x <- x + dx)
+ * and the soft moduli, given dL/dwrench (n_pair x 6 doubles, may be NULL)
+ * and dL/dtaxel (all sensors' maps, may be NULL).  Recomputes the clip
+ * polygons instead of storing them.  Outputs: dL_dpose n_pair x 2 x 6
+ * (M then N), dL_dE n_pair x 2 (M then N; 0 for a rigid geom).          */
+HC_API hc_status hc_adjoint(hc_context* ctx, const double* dL_dwrench, const float* dL_dtaxel,
+                            double* dL_dpose, double* dL_dE);
+
+/* ---- measurement --------------------------------------------------------*/
+typedef struct {
+  float ms_setup, ms_broadphase, ms_narrowphase, ms_reduce, ms_taxels, ms_total;
+  int64_t n_items;
+  int64_t n_polygons;
+} hc_timings;
+/* Enable CUDA-event timing of the stages of hc_step (disables the graph). */
+HC_API hc_status hc_enable_timing(hc_context* ctx, int enable);
+HC_API hc_status hc_get_timings(hc_context* ctx, hc_timings* out);
+/* The context's CUDA stream (cudaStream_t), for callers that order their
+ * own work against hc_step.                                             */
+HC_API hc_status hc_get_stream(hc_context* ctx, void** stream);
+/* Number of kernels one hc_step launches for the current pairs/sensors. */
+HC_API hc_status hc_get_launch_count(hc_context* ctx, int* n);
+/* Autotune the narrow-phase launch shape on the current pairs and poses. */
+HC_API hc_status hc_autotune(hc_context* ctx, int* chosen_block, int* chosen_ctas_per_sm);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HC_HC_H_ */

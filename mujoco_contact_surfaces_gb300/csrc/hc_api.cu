@@ -1,0 +1,1108 @@
+// hc_api.cu — host implementation of the C ABI (include/hc/hc.h).
+//
+// Owns the device pools and per-step buffers of one context, performs the
+// pair dispatch of collision_cb (mujoco_contact_surfaces_plugin.cpp:255-318)
+// on the host once per pair list, and launches the device pipeline.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/hc/hc.h"
+#include "hc_internal.h"
+#include "kernels.h"
+#include "meshgen.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+hc_status fail(hc_status st, const std::string& msg) {
+  g_last_error = msg;
+  return st;
+}
+
+#define HC_CUDA(call)                                                                      \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return fail(HC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;  // capacity in elements
+  cudaError_t reserve(size_t want) {
+    if (want <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    size_t cap = std::max<size_t>(want, 1);
+    cudaError_t e = cudaMalloc(&p, cap * sizeof(T));
+    if (e == cudaSuccess) n = cap;
+    return e;
+  }
+  cudaError_t upload(const std::vector<T>& v, cudaStream_t s) {
+    cudaError_t e = reserve(v.size());
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+struct GeomHost {
+  int id = -1, type = 0, kind = -1, order = 0;
+  double size[3] = {0, 0, 0}, cs5[5] = {0, 0, 0, 0, 0};
+  bool is_plane = false;
+  hc::SoftMesh soft;
+  hc::RigidMesh rigid;
+  std::vector<double> mesh_v;  // user mesh for HC_GEOM_MESH (regeneration)
+  std::vector<int> mesh_f;
+  // device placement
+  int elem_off = 0, n_elem = 0, node_off = 0, leaves = 1;
+  std::vector<int> perm;       // Morton position -> original element
+};
+
+struct SensorHost {
+  int geom;
+  double resolution;
+  int sr, window;
+  double sigma;
+  int cx, cy;
+  hc::SensorDev dev;
+};
+
+uint32_t expand_bits(uint32_t v) {
+  v = (v * 0x00010001u) & 0xFF0000FFu;
+  v = (v * 0x00000101u) & 0x0F00F00Fu;
+  v = (v * 0x00000011u) & 0xC30C30C3u;
+  v = (v * 0x00000005u) & 0x49249249u;
+  return v;
+}
+
+// Morton order of element centroids inside the mesh's bounding box.
+std::vector<int> morton_order(const std::vector<double>& v, const std::vector<int>& e, int npe) {
+  int ne = (int)(e.size() / npe);
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (size_t i = 0; i < v.size(); i += 3)
+    for (int a = 0; a < 3; ++a) lo[a] = std::min(lo[a], v[i + a]), hi[a] = std::max(hi[a], v[i + a]);
+  std::vector<std::pair<uint32_t, int>> key(ne);
+  for (int i = 0; i < ne; ++i) {
+    double c[3] = {0, 0, 0};
+    for (int k = 0; k < npe; ++k)
+      for (int a = 0; a < 3; ++a) c[a] += v[3 * e[npe * i + k] + a] / npe;
+    uint32_t q[3];
+    for (int a = 0; a < 3; ++a) {
+      double ext = hi[a] - lo[a];
+      double f = ext > 0 ? (c[a] - lo[a]) / ext : 0.5;
+      q[a] = (uint32_t)std::min(1023.0, std::max(0.0, f * 1024.0));
+    }
+    key[i] = {(expand_bits(q[0]) << 2) | (expand_bits(q[1]) << 1) | expand_bits(q[2]), i};
+  }
+  std::stable_sort(key.begin(), key.end());
+  std::vector<int> perm(ne);
+  for (int i = 0; i < ne; ++i) perm[i] = key[i].second;
+  return perm;
+}
+
+int next_pow2(int n) {
+  int p = 1;
+  while (p < n) p <<= 1;
+  return p;
+}
+
+double combined_E(double a, double b) {
+  if (std::isinf(a)) return b;
+  if (std::isinf(b)) return a;
+  return a * b / (a + b);
+}
+
+}  // namespace
+
+struct hc_context {
+  hc_config cfg;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::map<int, GeomHost> geoms;
+  int n_registered = 0;
+  bool pools_dirty = true;
+  int max_geom_id = -1;
+  // pools
+  DevBuf<float4> tets, tris, nodes;
+  DevBuf<int> tet_orig, tri_orig;
+  // inputs
+  DevBuf<double> xpos, xmat, vel;
+  int n_pose = 0;
+  bool have_vel = false;
+  bool poses_set = false;
+  // pairs
+  std::vector<hc::PairDev> pairs_h;
+  std::vector<int> g1_h, g2_h;
+  DevBuf<hc::PairDev> pairs;
+  DevBuf<hc::FrameDev> frames;
+  DevBuf<int> unit_pair, unit_cl, unit_count, unit_off, block_sum;
+  int n_units = 0, n_bp_blocks = 0;
+  DevBuf<int4> items;
+  DevBuf<hc::ItemOut> item_out;
+  int item_cap = 0;
+  DevBuf<int> counters;  // [item_total, item_next, status, cand_count, poly_count]
+  DevBuf<hc::PairOut> pair_out;
+  // sensors
+  std::vector<SensorHost> sensors;
+  DevBuf<hc::SensorDev> sensors_d;
+  DevBuf<unsigned long long> samples;
+  DevBuf<float> taxels, weights, samp_coord;
+  DevBuf<int> cell_sensor, cell_first;
+  int n_cells = 0;
+  bool sensors_dirty = false;
+  // debug
+  int debug = 0;
+  DevBuf<hc::CandRec> cand;
+  int cand_cap = 0;
+  DevBuf<hc::PolyRec> polys;
+  int poly_cap = 0;
+  // graph
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  bool graph_valid = false;
+  bool stepped = false;
+  bool timing = false;
+  cudaEvent_t ev[6] = {};
+  hc_timings last_timings = {};
+  int launches_per_step = 0;
+  int narrow_block = 128, narrow_ctas_per_sm = 8;
+  int n_sm = 0;
+};
+
+namespace {
+
+void invalidate_graph(hc_context* c) {
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->graph_exec = nullptr;
+  c->graph = nullptr;
+  c->graph_valid = false;
+}
+
+hc_status build_pools(hc_context* c) {
+  if (!c->pools_dirty) return HC_OK;
+  std::vector<GeomHost*> order;
+  for (auto& kv : c->geoms) order.push_back(&kv.second);
+  std::sort(order.begin(), order.end(), [](GeomHost* a, GeomHost* b) { return a->order < b->order; });
+  std::vector<float4> tets, tris;
+  std::vector<int> tet_orig, tri_orig;
+  int node_total = 0;
+  std::vector<int> s_eoff, s_ne, s_noff, s_L, r_eoff, r_ne, r_noff, r_L;
+  for (GeomHost* g : order) {
+    g->n_elem = 0;
+    g->leaves = 1;
+    if (g->kind == HC_SOFT) {
+      const auto& m = g->soft;
+      int ne = (int)(m.t.size() / 4);
+      g->perm = morton_order(m.v, m.t, 4);
+      g->elem_off = (int)(tets.size() / 4);
+      g->n_elem = ne;
+      for (int i = 0; i < ne; ++i) {
+        int t = g->perm[i];
+        for (int k = 0; k < 4; ++k) {
+          int vi = m.t[4 * t + k];
+          tets.push_back(make_float4((float)m.v[3 * vi], (float)m.v[3 * vi + 1], (float)m.v[3 * vi + 2], (float)m.p[vi]));
+        }
+        tet_orig.push_back(t);
+      }
+      s_eoff.push_back(g->elem_off); s_ne.push_back(ne);
+    } else if (g->kind == HC_RIGID && !g->is_plane) {
+      const auto& m = g->rigid;
+      int ne = (int)(m.f.size() / 3);
+      g->perm = morton_order(m.v, m.f, 3);
+      g->elem_off = (int)(tris.size() / 3);
+      g->n_elem = ne;
+      for (int i = 0; i < ne; ++i) {
+        int t = g->perm[i];
+        for (int k = 0; k < 3; ++k) {
+          int vi = m.f[3 * t + k];
+          tris.push_back(make_float4((float)m.v[3 * vi], (float)m.v[3 * vi + 1], (float)m.v[3 * vi + 2], 0.f));
+        }
+        tri_orig.push_back(t);
+      }
+      r_eoff.push_back(g->elem_off); r_ne.push_back(ne);
+    } else {
+      continue;
+    }
+    int ncl = std::max(1, (g->n_elem + hc::kCluster - 1) / hc::kCluster);
+    g->leaves = next_pow2(ncl);
+    g->node_off = node_total;
+    node_total += 2 * g->leaves;
+    if (g->kind == HC_SOFT) { s_noff.push_back(g->node_off); s_L.push_back(g->leaves); }
+    else { r_noff.push_back(g->node_off); r_L.push_back(g->leaves); }
+  }
+  cudaStream_t s = c->stream;
+  HC_CUDA(c->tets.upload(tets, s));
+  HC_CUDA(c->tris.upload(tris, s));
+  HC_CUDA(c->tet_orig.upload(tet_orig, s));
+  HC_CUDA(c->tri_orig.upload(tri_orig, s));
+  // two float4 (lo, hi) per node
+  HC_CUDA(c->nodes.reserve(2 * (size_t)std::max(1, node_total)));
+  // LBVH node boxes on the device
+  auto refit = [&](const std::vector<int>& eoff, const std::vector<int>& ne, const std::vector<int>& noff,
+                   const std::vector<int>& L, const float4* elems, int vpe) -> hc_status {
+    if (eoff.empty()) return HC_OK;
+    DevBuf<int> a, b, d, e;
+    std::vector<int> all;
+    if (a.upload(eoff, s) || b.upload(ne, s) || d.upload(noff, s) || e.upload(L, s)) return fail(HC_ERR_CUDA, "refit upload");
+    hc::launch_refit(elems, vpe, c->nodes.p, a.p, b.p, d.p, e.p, (int)eoff.size(), s);
+    cudaError_t err = cudaStreamSynchronize(s);
+    a.release(); b.release(); d.release(); e.release();
+    if (err != cudaSuccess) return fail(HC_ERR_CUDA, std::string("refit: ") + cudaGetErrorString(err));
+    return HC_OK;
+  };
+  hc_status st = refit(s_eoff, s_ne, s_noff, s_L, c->tets.p, 4);
+  if (st) return st;
+  st = refit(r_eoff, r_ne, r_noff, r_L, c->tris.p, 3);
+  if (st) return st;
+  HC_CUDA(cudaGetLastError());
+  c->pools_dirty = false;
+  invalidate_graph(c);
+  return HC_OK;
+}
+
+bool finite_all(const double* p, size_t n) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(p[i])) return false;
+  return true;
+}
+
+hc_status ensure_items(hc_context* c, int cap) {
+  if (cap <= c->item_cap) return HC_OK;
+  HC_CUDA(c->items.reserve(cap));
+  HC_CUDA(c->item_out.reserve(cap));
+  c->item_cap = cap;
+  invalidate_graph(c);
+  return HC_OK;
+}
+
+hc_status build_sensors(hc_context* c) {
+  if (!c->sensors_dirty) return HC_OK;
+  std::vector<hc::SensorDev> sd;
+  std::vector<float> w, coord;
+  std::vector<int> cell_sensor, cell_first;
+  int64_t smp = 0;
+  int cells = 0;
+  for (size_t k = 0; k < c->sensors.size(); ++k) {
+    SensorHost& S = c->sensors[k];
+    const GeomHost& g = c->geoms[S.geom];
+    hc::SensorDev d;
+    d.geom = S.geom;
+    d.cx = S.cx; d.cy = S.cy; d.sr = S.sr;
+    d.nx = S.cx * S.sr; d.ny = S.cy * S.sr;
+    d.sample_off = smp;
+    smp += (int64_t)d.nx * d.ny;
+    d.taxel_off = cells;
+    cell_first.push_back(cells);
+    for (int i = 0; i < S.cx * S.cy; ++i) cell_sensor.push_back((int)k);
+    cells += S.cx * S.cy;
+    // constants of FlatTactileSensor::load (flat_tactile_sensor.cpp:179-185)
+    const double resolution = S.resolution;
+    const int sr = S.sr;
+    float xs = (float)g.size[0], ys = (float)g.size[1], zs = (float)g.size[2];
+    float rSampling_resolution = (float)(resolution / sr);
+    d.rmean = (float)(1. / (sr * sr));
+    d.zs15 = (float)(1.5 * zs);
+    // sample coordinates in the sensor frame (FS:324-327)
+    d.samp_off_x = (int)coord.size();
+    for (int x = 0; x < S.cx; ++x)
+      for (int i = 0; i < sr; ++i)
+        coord.push_back((float)((double)(-xs) + x * resolution + (double)(float)(i * rSampling_resolution) +
+                                0.5 * rSampling_resolution));
+    d.samp_off_y = (int)coord.size();
+    for (int y = 0; y < S.cy; ++y)
+      for (int j = 0; j < sr; ++j)
+        coord.push_back((float)((double)(-ys) + y * resolution + (double)(float)(j * rSampling_resolution) +
+                                0.5 * rSampling_resolution));
+    // window weights (FS:305-388)
+    d.weight_off = (int)w.size();
+    float di_factor = (float)(resolution / sr);
+    float sub_halfwidth = (float)(di_factor / 2.0f - resolution / 2.0f);
+    const float SQRT_2 = 1.41421356237f;
+    float max_dist = (float)(SQRT_2 * resolution / 2.0f);
+    float sigma = (float)S.sigma;
+    float rsigma_squared = S.window == HC_WINDOW_GAUSS ? 0.5f / (sigma * sigma) : 0.f;
+    float rtukey = S.window == HC_WINDOW_TUKEY ? 1.f / sigma * sr * sr : 0.f;
+    for (int i = 0; i < sr; ++i)
+      for (int j = 0; j < sr; ++j) {
+        float weight = 1.0f;
+        if (S.window == HC_WINDOW_GAUSS) {
+          float dist = std::hypot(di_factor * i + sub_halfwidth, di_factor * j + sub_halfwidth) / max_dist;
+          weight = std::exp(-(dist * dist) * rsigma_squared);
+        } else if (S.window == HC_WINDOW_TUKEY) {
+          if (sr / 2 - std::abs(sr / 2 - i) <= sigma * sr / 2)
+            weight *= 0.5f * (1.f - cosf((float)(2.f * M_PI * (sr / 2 - std::abs(sr / 2 - i)) * rtukey)));
+          if (sr / 2 - std::abs(sr / 2 - j) <= sigma * sr / 2)
+            weight *= 0.5f * (1.f - cosf((float)(2.f * M_PI * (sr / 2 - std::abs(sr / 2 - j)) * rtukey)));
+        } else if (S.window == HC_WINDOW_SQUARE) {
+          float inv_dist = 1 - std::hypot(di_factor * i + sub_halfwidth, di_factor * j + sub_halfwidth) / max_dist;
+          weight = inv_dist * inv_dist;
+        }
+        w.push_back(weight);
+      }
+    S.dev = d;
+    sd.push_back(d);
+  }
+  cudaStream_t s = c->stream;
+  HC_CUDA(c->sensors_d.upload(sd, s));
+  HC_CUDA(c->weights.upload(w, s));
+  HC_CUDA(c->samp_coord.upload(coord, s));
+  HC_CUDA(c->cell_sensor.upload(cell_sensor, s));
+  HC_CUDA(c->cell_first.upload(cell_first, s));
+  HC_CUDA(c->taxels.reserve(std::max(1, cells)));
+  HC_CUDA(c->samples.reserve(std::max<int64_t>(1, smp)));
+  if (smp > 0) HC_CUDA(cudaMemsetAsync(c->samples.p, 0xFF, smp * sizeof(unsigned long long), s));
+  if (cells > 0) HC_CUDA(cudaMemsetAsync(c->taxels.p, 0, cells * sizeof(float), s));
+  c->n_cells = cells;
+  c->sensors_dirty = false;
+  invalidate_graph(c);
+  return HC_OK;
+}
+
+hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
+  hc::StepArgs a;
+  memset(&a, 0, sizeof(a));
+  a.xpos = c->xpos.p;
+  a.xmat = c->xmat.p;
+  a.vel = c->have_vel ? c->vel.p : nullptr;
+  a.pairs = c->pairs.p;
+  a.n_pair = (int)c->pairs_h.size();
+  a.frames = c->frames.p;
+  a.tets = c->tets.p;
+  a.tet_orig = c->tet_orig.p;
+  a.tris = c->tris.p;
+  a.tri_orig = c->tri_orig.p;
+  a.nodes = c->nodes.p;
+  a.unit_pair = c->unit_pair.p;
+  a.unit_cl = c->unit_cl.p;
+  a.n_units = c->n_units;
+  a.unit_count = c->unit_count.p;
+  a.unit_off = c->unit_off.p;
+  a.block_sum = c->block_sum.p;
+  a.n_bp_blocks = c->n_bp_blocks;
+  a.items = c->items.p;
+  a.item_cap = c->item_cap;
+  a.item_total = c->counters.p;
+  a.item_next = c->counters.p + 1;
+  a.status = c->counters.p + 2;
+  a.cand_count = c->counters.p + 3;
+  a.poly_count = c->counters.p + 4;
+  a.item_out = c->item_out.p;
+  a.pair_out = c->pair_out.p;
+  a.sensors = c->sensors_d.p;
+  a.n_sensor = (int)c->sensors.size();
+  a.samples = c->samples.p;
+  a.taxels = c->taxels.p;
+  a.weights = c->weights.p;
+  a.samp_coord = c->samp_coord.p;
+  a.n_cells_total = c->n_cells;
+  a.cell_sensor = c->cell_sensor.p;
+  a.cell_first = c->cell_first.p;
+  a.repr = c->cfg.representation;
+  a.apply_forces = c->cfg.apply_forces;
+  a.debug = c->debug;
+  a.cand = c->cand.p;
+  a.cand_cap = c->cand_cap;
+  a.polys = c->polys.p;
+  a.poly_cap = c->poly_cap;
+  a.want_polys = want_polys;
+  a.want_pair = want_pair;
+  a.narrow_block = c->narrow_block;
+  a.narrow_grid = std::max(1, c->n_sm * c->narrow_ctas_per_sm);
+  return a;
+}
+
+// Launch one step on the context stream (graph when possible).
+hc_status run_step(hc_context* c, int want_polys, int want_pair) {
+  if (c->pairs_h.empty() && c->sensors.empty()) {
+    c->stepped = true;
+    return HC_OK;
+  }
+  hc::StepArgs a = make_args(c, want_polys, want_pair);
+  HC_CUDA(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(int), c->stream));
+  if (c->timing && !want_polys) {
+    c->launches_per_step = hc::launch_step(a, c->stream, c->ev);
+    HC_CUDA(cudaGetLastError());
+    c->stepped = true;
+    return HC_OK;
+  }
+  bool use_graph = c->cfg.use_graph && !want_polys;
+  if (!use_graph) {
+    c->launches_per_step = hc::launch_step(a, c->stream, nullptr);
+    HC_CUDA(cudaGetLastError());
+    c->stepped = true;
+    return HC_OK;
+  }
+  if (!c->graph_valid) {
+    invalidate_graph(c);
+    HC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    c->launches_per_step = hc::launch_step(a, c->stream, nullptr);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &c->graph);
+    if (e != cudaSuccess) return fail(HC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    HC_CUDA(cudaGraphInstantiate(&c->graph_exec, c->graph, 0));
+    c->graph_valid = true;
+  }
+  HC_CUDA(cudaGraphLaunch(c->graph_exec, c->stream));
+  c->stepped = true;
+  return HC_OK;
+}
+
+// Check the status word; on item overflow grow the capacity and re-run.
+hc_status finish_step(hc_context* c) {
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    int cnt[8];
+    HC_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    if (!(cnt[2] & 1)) return HC_OK;
+    // overflow: the scan wrote the full total into unit_off[n_units]
+    int total = 0;
+    HC_CUDA(cudaMemcpy(&total, c->unit_off.p + c->n_units, sizeof(int), cudaMemcpyDeviceToHost));
+    hc_status st = ensure_items(c, std::max(2 * c->item_cap, total + total / 4 + 1024));
+    if (st) return st;
+    st = run_step(c, 0, -1);
+    if (st) return st;
+  }
+  return fail(HC_ERR_OVERFLOW, "work-item capacity overflow persisted");
+}
+
+hc_status need(hc_context* c) {
+  if (!c) return fail(HC_ERR_INVALID_ARG, "null context");
+  return HC_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+void hc_config_default(hc_config* cfg) {
+  if (!cfg) return;
+  memset(cfg, 0, sizeof(*cfg));
+  cfg->device = 0;
+  cfg->representation = HC_REPR_TRIANGLE;
+  cfg->apply_forces = 1;
+  cfg->use_graph = 1;
+  cfg->item_capacity = 0;
+  cfg->face_capacity = 0;
+}
+
+const char* hc_last_error(void) { return g_last_error.c_str(); }
+
+const char* hc_version(void) { return "hydroelastic-gb300 0.1 (sm_103a)"; }
+
+hc_status hc_context_create(const hc_config* cfg, hc_context** out) {
+  if (!out) return fail(HC_ERR_INVALID_ARG, "out is null");
+  *out = nullptr;
+  hc_config c0;
+  hc_config_default(&c0);
+  if (cfg) c0 = *cfg;
+  if (c0.representation != HC_REPR_TRIANGLE && c0.representation != HC_REPR_POLYGON)
+    return fail(HC_ERR_INVALID_ARG, "representation must be HC_REPR_TRIANGLE or HC_REPR_POLYGON");
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return fail(HC_ERR_NO_DEVICE, "no CUDA device visible");
+  if (c0.device < 0 || c0.device >= ndev) return fail(HC_ERR_INVALID_ARG, "device ordinal out of range");
+  HC_CUDA(cudaSetDevice(c0.device));
+  hc_context* c = new hc_context();
+  c->cfg = c0;
+  c->device = c0.device;
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, c0.device);
+  c->n_sm = prop.multiProcessorCount;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return fail(HC_ERR_CUDA, "stream create failed");
+  }
+  for (auto& ev : c->ev) cudaEventCreate(&ev);
+  if (c->counters.reserve(8) != cudaSuccess) {
+    delete c;
+    return fail(HC_ERR_CUDA, "counter alloc failed");
+  }
+  cudaMemset(c->counters.p, 0, 8 * sizeof(int));
+  *out = c;
+  return HC_OK;
+}
+
+hc_status hc_context_destroy(hc_context* c) {
+  if (!c) return HC_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  invalidate_graph(c);
+  c->tets.release(); c->tris.release(); c->nodes.release(); c->tet_orig.release(); c->tri_orig.release();
+  c->xpos.release(); c->xmat.release(); c->vel.release();
+  c->pairs.release(); c->frames.release(); c->unit_pair.release(); c->unit_cl.release();
+  c->unit_count.release(); c->unit_off.release(); c->block_sum.release(); c->items.release();
+  c->item_out.release(); c->counters.release(); c->pair_out.release(); c->sensors_d.release();
+  c->samples.release(); c->taxels.release(); c->weights.release(); c->samp_coord.release();
+  c->cell_sensor.release(); c->cell_first.release(); c->cand.release(); c->polys.release();
+  for (auto& ev : c->ev) cudaEventDestroy(ev);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return HC_OK;
+}
+
+hc_status hc_reset(hc_context* c) {
+  if (hc_status st = need(c)) return st;
+  c->stepped = false;
+  return HC_OK;
+}
+
+hc_status hc_generate_mesh(int type, const double size[3], const double cs5[5], const double* mesh_vert, int nvert,
+                           const int* mesh_face, int nface, int* out_kind, int* out_nvert, int* out_nelem,
+                           double* vert, double* pressure, int* elems) {
+  if (!size || !cs5) return fail(HC_ERR_INVALID_ARG, "size and cs5 are required");
+  double E = cs5[0], hint = cs5[2];
+  if (out_kind) *out_kind = -1;
+  if (E > 0) {
+    hc::SoftMesh m;
+    std::string err = hc::make_soft_mesh(type, size, E, hint, mesh_vert, nvert, mesh_face, nface, &m);
+    if (!err.empty()) {
+      bool unsup = type == HC_GEOM_PLANE || type == HC_GEOM_HFIELD || type == HC_GEOM_CAPSULE;
+      return fail(unsup ? HC_ERR_UNSUPPORTED : HC_ERR_INVALID_ARG, err);
+    }
+    hc::round_to_float(&m);
+    if (out_kind) *out_kind = HC_SOFT;
+    if (out_nvert) *out_nvert = (int)(m.v.size() / 3);
+    if (out_nelem) *out_nelem = (int)(m.t.size() / 4);
+    if (vert) memcpy(vert, m.v.data(), m.v.size() * sizeof(double));
+    if (pressure) memcpy(pressure, m.p.data(), m.p.size() * sizeof(double));
+    if (elems) memcpy(elems, m.t.data(), m.t.size() * sizeof(int));
+    return HC_OK;
+  }
+  hc::RigidMesh m;
+  std::string err = hc::make_rigid_mesh(type, size, hint, mesh_vert, nvert, mesh_face, nface, &m);
+  if (!err.empty()) {
+    bool unsup = type == HC_GEOM_HFIELD || type == HC_GEOM_CAPSULE;
+    return fail(unsup ? HC_ERR_UNSUPPORTED : HC_ERR_INVALID_ARG, err);
+  }
+  hc::round_to_float(&m);
+  if (out_kind) *out_kind = HC_RIGID;
+  if (out_nvert) *out_nvert = (int)(m.v.size() / 3);
+  if (out_nelem) *out_nelem = (int)(m.f.size() / 3);
+  if (vert) memcpy(vert, m.v.data(), m.v.size() * sizeof(double));
+  if (elems) memcpy(elems, m.f.data(), m.f.size() * sizeof(int));
+  return HC_OK;
+}
+
+static hc_status make_geom_mesh(GeomHost* g) {
+  double E = g->cs5[0], hint = g->cs5[2];
+  const double* mv = g->mesh_v.empty() ? nullptr : g->mesh_v.data();
+  const int* mf = g->mesh_f.empty() ? nullptr : g->mesh_f.data();
+  int nv = (int)(g->mesh_v.size() / 3), nf = (int)(g->mesh_f.size() / 3);
+  if (E > 0) {
+    std::string err = hc::make_soft_mesh(g->type, g->size, E, hint, mv, nv, mf, nf, &g->soft);
+    if (!err.empty()) return fail(HC_ERR_INVALID_ARG, err);
+    hc::round_to_float(&g->soft);
+    g->kind = HC_SOFT;
+  } else {
+    std::string err = hc::make_rigid_mesh(g->type, g->size, hint, mv, nv, mf, nf, &g->rigid);
+    if (!err.empty()) return fail(HC_ERR_INVALID_ARG, err);
+    hc::round_to_float(&g->rigid);
+    g->kind = HC_RIGID;
+    g->is_plane = g->type == HC_GEOM_PLANE;
+  }
+  return HC_OK;
+}
+
+hc_status hc_add_geom(hc_context* c, int geom_id, int type, const double size[3], const double cs5[5],
+                      const double* mesh_vert, int nvert, const int* mesh_face, int nface, int* out_kind) {
+  if (hc_status st = need(c)) return st;
+  if (out_kind) *out_kind = -1;
+  if (geom_id < 0) return fail(HC_ERR_INVALID_ARG, "negative geom id");
+  if (!size || !cs5) return fail(HC_ERR_INVALID_ARG, "size and cs5 are required");
+  if (c->geoms.count(geom_id)) return fail(HC_ERR_INVALID_ARG, "geom id already registered");
+  if (!finite_all(size, 3) || !finite_all(cs5, 5)) return fail(HC_ERR_INVALID_ARG, "non-finite size or cs:: values");
+  // soft plane, hfield and capsule have no contact surface.
+  if (type == HC_GEOM_HFIELD || type == HC_GEOM_CAPSULE || (type == HC_GEOM_PLANE && cs5[0] > 0))
+    return fail(HC_ERR_UNSUPPORTED, "geom type has no hydroelastic representation");
+  if (type < 0 || type > HC_GEOM_MESH) return fail(HC_ERR_INVALID_ARG, "unknown geom type");
+  GeomHost g;
+  g.id = geom_id;
+  g.type = type;
+  memcpy(g.size, size, sizeof(g.size));
+  memcpy(g.cs5, cs5, sizeof(g.cs5));
+  if (type == HC_GEOM_MESH) {
+    if (!mesh_vert || !mesh_face || nvert <= 0 || nface <= 0) return fail(HC_ERR_INVALID_ARG, "mesh geom needs data");
+    g.mesh_v.assign(mesh_vert, mesh_vert + 3 * (size_t)nvert);
+    g.mesh_f.assign(mesh_face, mesh_face + 3 * (size_t)nface);
+  }
+  if (hc_status st = make_geom_mesh(&g)) return st;
+  g.order = c->n_registered++;
+  if (out_kind) *out_kind = g.kind;
+  c->max_geom_id = std::max(c->max_geom_id, geom_id);
+  c->geoms[geom_id] = std::move(g);
+  c->pools_dirty = true;
+  c->pairs_h.clear();  // pair tables refer to pool offsets
+  return HC_OK;
+}
+
+hc_status hc_update_geom_size(hc_context* c, int geom_id, const double size[3]) {
+  if (hc_status st = need(c)) return st;
+  auto it = c->geoms.find(geom_id);
+  if (it == c->geoms.end()) return fail(HC_ERR_INVALID_ARG, "unknown geom id");
+  if (!size || !finite_all(size, 3)) return fail(HC_ERR_INVALID_ARG, "bad size");
+  GeomHost& g = it->second;
+  double old[3];
+  memcpy(old, g.size, sizeof(old));
+  memcpy(g.size, size, sizeof(g.size));
+  if (hc_status st = make_geom_mesh(&g)) {
+    memcpy(g.size, old, sizeof(old));
+    make_geom_mesh(&g);
+    return st;
+  }
+  c->pools_dirty = true;
+  // Pair tables hold pool offsets: rebuild them for the current pairs.
+  if (!c->pairs_h.empty()) {
+    std::vector<int> g1 = c->g1_h, g2 = c->g2_h;
+    return hc_set_pairs(c, (int)g1.size(), g1.data(), g2.data(), nullptr, nullptr);
+  }
+  return HC_OK;
+}
+
+hc_status hc_get_geom_info(hc_context* c, int geom_id, hc_geom_info* out) {
+  if (hc_status st = need(c)) return st;
+  auto it = c->geoms.find(geom_id);
+  if (it == c->geoms.end() || !out) return fail(HC_ERR_INVALID_ARG, "unknown geom id");
+  const GeomHost& g = it->second;
+  out->kind = g.kind;
+  out->type = g.type;
+  out->order = g.order;
+  out->n_elements = g.kind == HC_SOFT ? (int)(g.soft.t.size() / 4) : (int)(g.rigid.f.size() / 3);
+  out->n_vertices = g.kind == HC_SOFT ? (int)(g.soft.v.size() / 3) : (int)(g.rigid.v.size() / 3);
+  out->E = g.cs5[0]; out->dissipation = g.cs5[1]; out->resolution_hint = g.cs5[2];
+  out->mu_static = g.cs5[3]; out->mu_dynamic = g.cs5[4];
+  return HC_OK;
+}
+
+hc_status hc_get_geom_mesh(hc_context* c, int geom_id, double* vert, double* pressure, int* elems) {
+  if (hc_status st = need(c)) return st;
+  auto it = c->geoms.find(geom_id);
+  if (it == c->geoms.end()) return fail(HC_ERR_INVALID_ARG, "unknown geom id");
+  const GeomHost& g = it->second;
+  if (g.kind == HC_SOFT) {
+    if (vert) memcpy(vert, g.soft.v.data(), g.soft.v.size() * sizeof(double));
+    if (pressure) memcpy(pressure, g.soft.p.data(), g.soft.p.size() * sizeof(double));
+    if (elems) memcpy(elems, g.soft.t.data(), g.soft.t.size() * sizeof(int));
+  } else {
+    if (vert) memcpy(vert, g.rigid.v.data(), g.rigid.v.size() * sizeof(double));
+    if (elems) memcpy(elems, g.rigid.f.data(), g.rigid.f.size() * sizeof(int));
+  }
+  return HC_OK;
+}
+
+hc_status hc_set_poses(hc_context* c, int n_geom, const double* xpos, const double* xmat, const double* vel) {
+  if (hc_status st = need(c)) return st;
+  if (n_geom <= c->max_geom_id) return fail(HC_ERR_INVALID_ARG, "n_geom must cover every registered geom id");
+  if (!xpos || !xmat) return fail(HC_ERR_INVALID_ARG, "xpos and xmat are required");
+  HC_CUDA(cudaSetDevice(c->device));
+  if ((size_t)n_geom * 3 > c->xpos.n || (size_t)n_geom * 9 > c->xmat.n || (size_t)n_geom * 6 > c->vel.n) {
+    HC_CUDA(c->xpos.reserve((size_t)n_geom * 3));
+    HC_CUDA(c->xmat.reserve((size_t)n_geom * 9));
+    HC_CUDA(c->vel.reserve((size_t)n_geom * 6));
+    invalidate_graph(c);
+  }
+  HC_CUDA(cudaMemcpyAsync(c->xpos.p, xpos, (size_t)n_geom * 3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  HC_CUDA(cudaMemcpyAsync(c->xmat.p, xmat, (size_t)n_geom * 9 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  bool hv = vel != nullptr;
+  if (hv) HC_CUDA(cudaMemcpyAsync(c->vel.p, vel, (size_t)n_geom * 6 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (hv != c->have_vel) invalidate_graph(c);
+  c->have_vel = hv;
+  c->n_pose = n_geom;
+  c->poses_set = true;
+  return HC_OK;
+}
+
+hc_status hc_set_poses_device(hc_context* c, int n_geom, const double* d_xpos, const double* d_xmat,
+                              const double* d_vel) {
+  if (hc_status st = need(c)) return st;
+  if (n_geom <= c->max_geom_id) return fail(HC_ERR_INVALID_ARG, "n_geom must cover every registered geom id");
+  if (!d_xpos || !d_xmat) return fail(HC_ERR_INVALID_ARG, "xpos and xmat are required");
+  HC_CUDA(cudaSetDevice(c->device));
+  if ((size_t)n_geom * 3 > c->xpos.n || (size_t)n_geom * 9 > c->xmat.n || (size_t)n_geom * 6 > c->vel.n) {
+    HC_CUDA(c->xpos.reserve((size_t)n_geom * 3));
+    HC_CUDA(c->xmat.reserve((size_t)n_geom * 9));
+    HC_CUDA(c->vel.reserve((size_t)n_geom * 6));
+    invalidate_graph(c);
+  }
+  HC_CUDA(cudaMemcpyAsync(c->xpos.p, d_xpos, (size_t)n_geom * 3 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  HC_CUDA(cudaMemcpyAsync(c->xmat.p, d_xmat, (size_t)n_geom * 9 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  bool hv = d_vel != nullptr;
+  if (hv) HC_CUDA(cudaMemcpyAsync(c->vel.p, d_vel, (size_t)n_geom * 6 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  if (hv != c->have_vel) invalidate_graph(c);
+  c->have_vel = hv;
+  c->n_pose = n_geom;
+  c->poses_set = true;
+  return HC_OK;
+}
+
+hc_status hc_set_pairs(hc_context* c, int n_pair, const int* g1, const int* g2, int* per_pair_status,
+                       int* per_pair_query) {
+  if (hc_status st = need(c)) return st;
+  if (n_pair < 0 || (n_pair > 0 && (!g1 || !g2))) return fail(HC_ERR_INVALID_ARG, "bad pair arrays");
+  HC_CUDA(cudaSetDevice(c->device));
+  if (hc_status st = build_pools(c)) return st;
+  if (hc_status st = build_sensors(c)) return st;
+  std::vector<hc::PairDev> P(n_pair);
+  std::vector<int> upair, ucl;
+  hc_status worst = HC_OK;
+  for (int i = 0; i < n_pair; ++i) {
+    hc::PairDev& p = P[i];
+    memset(&p, 0, sizeof(p));
+    p.sensor0 = p.sensor1 = -1;
+    auto i1 = c->geoms.find(g1[i]), i2 = c->geoms.find(g2[i]);
+    int st = HC_OK;
+    p.gs = p.gm = std::max(0, g1[i]);
+    p.go = p.gn = std::max(0, g2[i]);
+    if (g1[i] < 0 || g2[i] < 0 || g1[i] == g2[i]) {
+      st = HC_ERR_INVALID_ARG;
+    } else if (i1 == c->geoms.end() || i2 == c->geoms.end() ||
+               (i1->second.kind == HC_RIGID && i2->second.kind == HC_RIGID)) {
+      st = HC_ERR_UNSUPPORTED;
+    }
+    p.unit_begin = p.unit_end = (int)upair.size();
+    if (st == HC_OK) {
+      const GeomHost& G1 = i1->second;
+      const GeomHost& G2 = i2->second;
+      const GeomHost& M = G1.order <= G2.order ? G1 : G2;
+      const GeomHost& N = &M == &G1 ? G2 : G1;
+      const GeomHost* S;
+      const GeomHost* O;
+      if (G1.kind == HC_SOFT && G2.kind == HC_SOFT) {
+        p.query = HC_QUERY_SOFT_SOFT;
+        S = &M; O = &N;
+      } else {
+        S = G1.kind == HC_SOFT ? &G1 : &G2;
+        O = S == &G1 ? &G2 : &G1;
+        p.query = O->is_plane ? HC_QUERY_SOFT_HALFSPACE : HC_QUERY_SOFT_RIGID;
+      }
+      p.gs = S->id; p.go = O->id; p.gm = M.id; p.gn = N.id;
+      p.s_is_m = S == &M;
+      p.s_elem_off = S->elem_off; p.s_n_elem = S->n_elem; p.s_node_off = S->node_off; p.s_leaves = S->leaves;
+      p.o_elem_off = O->elem_off; p.o_n_elem = O->n_elem; p.o_node_off = O->node_off; p.o_leaves = O->leaves;
+      p.o_n_clusters = (O->n_elem + hc::kCluster - 1) / hc::kCluster;
+      // material combination
+      double EM = M.kind == HC_SOFT ? M.cs5[0] : INFINITY, EN = N.kind == HC_SOFT ? N.cs5[0] : INFINITY;
+      double dM = M.kind == HC_SOFT ? M.cs5[1] : 1.0, dN = N.kind == HC_SOFT ? N.cs5[1] : 1.0;
+      double Es = combined_E(EM, EN), d = 0;
+      if (std::isinf(Es)) d = 0.5 * (dM + dN);
+      else {
+        if (!std::isinf(EM)) d += Es / EM * dM;
+        if (!std::isinf(EN)) d += Es / EN * dN;
+      }
+      double ma = M.cs5[4], mb = N.cs5[4];
+      p.damping = (float)d;
+      p.mu = (float)(ma + mb == 0 ? 0.0 : 2 * ma * mb / (ma + mb));
+      p.E_s = (float)S->cs5[0];
+      p.E_o = O->kind == HC_SOFT ? (float)O->cs5[0] : 0.f;
+      int ns = 0;
+      for (size_t k = 0; k < c->sensors.size() && ns < 2; ++k)
+        if (c->sensors[k].geom == g1[i] || c->sensors[k].geom == g2[i]) {
+          if (ns == 0) p.sensor0 = (int)k; else p.sensor1 = (int)k;
+          ++ns;
+        }
+      if (p.query == HC_QUERY_SOFT_HALFSPACE) {
+        upair.push_back(i); ucl.push_back(-1);
+      } else {
+        for (int k = 0; k < p.o_n_clusters; ++k) { upair.push_back(i); ucl.push_back(k); }
+      }
+      p.unit_end = (int)upair.size();
+    } else {
+      p.query = HC_QUERY_NONE;
+      if (worst == HC_OK) worst = (hc_status)st;
+    }
+    if (per_pair_status) per_pair_status[i] = st;
+    if (per_pair_query) per_pair_query[i] = p.query;
+  }
+  cudaStream_t s = c->stream;
+  c->pairs_h = P;
+  c->g1_h.assign(g1, g1 + n_pair);
+  c->g2_h.assign(g2, g2 + n_pair);
+  HC_CUDA(c->pairs.upload(P, s));
+  HC_CUDA(c->frames.reserve(std::max(1, n_pair)));
+  HC_CUDA(c->pair_out.reserve(std::max(1, n_pair)));
+  c->n_units = (int)upair.size();
+  c->n_bp_blocks = std::max(1, (c->n_units + hc::kBpBlock - 1) / hc::kBpBlock);
+  HC_CUDA(c->unit_pair.upload(upair, s));
+  HC_CUDA(c->unit_cl.upload(ucl, s));
+  HC_CUDA(c->unit_count.reserve(std::max(1, c->n_units)));
+  HC_CUDA(c->unit_off.reserve(c->n_units + 1));
+  HC_CUDA(c->block_sum.reserve(c->n_bp_blocks));
+  int want = c->cfg.item_capacity > 0 ? (int)c->cfg.item_capacity : std::max(1 << 16, 64 * n_pair);
+  if (hc_status st = ensure_items(c, want)) return st;
+  HC_CUDA(cudaStreamSynchronize(s));
+  invalidate_graph(c);
+  c->stepped = false;
+  (void)worst;
+  return HC_OK;
+}
+
+hc_status hc_step(hc_context* c) {
+  if (hc_status st = need(c)) return st;
+  if (!c->poses_set && !c->pairs_h.empty()) return fail(HC_ERR_NOT_READY, "poses not set");
+  HC_CUDA(cudaSetDevice(c->device));
+  if (c->pools_dirty || c->sensors_dirty) {
+    std::vector<int> g1 = c->g1_h, g2 = c->g2_h;
+    if (hc_status st = hc_set_pairs(c, (int)g1.size(), g1.data(), g2.data(), nullptr, nullptr)) return st;
+  }
+  if ((size_t)c->n_pose * 3 > c->xpos.n || c->n_pose <= c->max_geom_id)
+    return fail(HC_ERR_NOT_READY, "poses do not cover every registered geom");
+  return run_step(c, 0, -1);
+}
+
+hc_status hc_collide_pairs(hc_context* c, int n_pair, const int* g1, const int* g2, int* per_pair_status) {
+  if (hc_status st = hc_set_pairs(c, n_pair, g1, g2, per_pair_status, nullptr)) return st;
+  return hc_step(c);
+}
+
+hc_status hc_get_wrenches(hc_context* c, double* wrench) {
+  if (hc_status st = need(c)) return st;
+  if (!c->stepped) return fail(HC_ERR_NOT_READY, "no step has run");
+  HC_CUDA(cudaSetDevice(c->device));
+  if (hc_status st = finish_step(c)) return st;
+  size_t n = c->pairs_h.size();
+  if (!wrench || !n) return HC_OK;
+  std::vector<hc::PairOut> o(n);
+  HC_CUDA(cudaMemcpy(o.data(), c->pair_out.p, n * sizeof(hc::PairOut), cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < n; ++i) memcpy(wrench + 6 * i, o[i].wrench, 6 * sizeof(double));
+  return HC_OK;
+}
+
+hc_status hc_get_wrenches_device(hc_context* c, const double** d_wrench) {
+  if (hc_status st = need(c)) return st;
+  if (!d_wrench) return fail(HC_ERR_INVALID_ARG, "null output");
+  *d_wrench = reinterpret_cast<const double*>(c->pair_out.p);
+  return HC_OK;
+}
+
+hc_status hc_get_pair_order(hc_context* c, int* query, int* m_geom, int* n_geom) {
+  if (hc_status st = need(c)) return st;
+  for (size_t i = 0; i < c->pairs_h.size(); ++i) {
+    if (query) query[i] = c->pairs_h[i].query;
+    if (m_geom) m_geom[i] = c->pairs_h[i].gm;
+    if (n_geom) n_geom[i] = c->pairs_h[i].gn;
+  }
+  return HC_OK;
+}
+
+hc_status hc_get_pair_stats(hc_context* c, hc_pair_stats* out) {
+  if (hc_status st = need(c)) return st;
+  if (!c->stepped) return fail(HC_ERR_NOT_READY, "no step has run");
+  HC_CUDA(cudaSetDevice(c->device));
+  if (hc_status st = finish_step(c)) return st;
+  size_t n = c->pairs_h.size();
+  if (!out || !n) return HC_OK;
+  std::vector<hc::PairOut> o(n);
+  HC_CUDA(cudaMemcpy(o.data(), c->pair_out.p, n * sizeof(hc::PairOut), cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < n; ++i) {
+    out[i].n_polygons = o[i].n_poly;
+    out[i].n_faces = o[i].n_faces;
+    out[i].n_near_degenerate = o[i].n_near;
+    out[i].n_items = o[i].n_items;
+    out[i].area = o[i].area;
+    out[i].total_fn0 = o[i].total_fn0;
+  }
+  return HC_OK;
+}
+
+hc_status hc_set_debug(hc_context* c, int flags) {
+  if (hc_status st = need(c)) return st;
+  HC_CUDA(cudaSetDevice(c->device));
+  if ((flags & HC_DEBUG_CANDIDATES) && c->cand_cap == 0) {
+    c->cand_cap = 1 << 22;
+    HC_CUDA(c->cand.reserve(c->cand_cap));
+  }
+  if (flags != c->debug) invalidate_graph(c);
+  c->debug = flags;
+  return HC_OK;
+}
+
+hc_status hc_get_candidates(hc_context* c, hc_candidate* out, int64_t capacity, int64_t* count) {
+  if (hc_status st = need(c)) return st;
+  if (!(c->debug & HC_DEBUG_CANDIDATES)) return fail(HC_ERR_NOT_READY, "candidate recording is off");
+  HC_CUDA(cudaSetDevice(c->device));
+  if (hc_status st = finish_step(c)) return st;
+  int cnt[8];
+  HC_CUDA(cudaMemcpy(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
+  if (cnt[2] & 2) return fail(HC_ERR_OVERFLOW, "candidate record buffer overflow");
+  int64_t n = std::min<int64_t>(cnt[3], c->cand_cap);
+  if (count) *count = n;
+  if (out && capacity > 0) {
+    int64_t k = std::min(n, capacity);
+    std::vector<hc::CandRec> r(k);
+    HC_CUDA(cudaMemcpy(r.data(), c->cand.p, k * sizeof(hc::CandRec), cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < k; ++i) {
+      out[i].pair = r[i].pair; out[i].elem_a = r[i].elem_a; out[i].elem_b = r[i].elem_b;
+      out[i].n_vert = r[i].n_vert; out[i].flags = r[i].flags;
+    }
+  }
+  return HC_OK;
+}
+
+hc_status hc_get_surface(hc_context* c, int pair, hc_surface_view* view) {
+  if (hc_status st = need(c)) return st;
+  if (!view || pair < 0 || pair >= (int)c->pairs_h.size()) return fail(HC_ERR_INVALID_ARG, "bad pair or view");
+  if (!c->stepped) return fail(HC_ERR_NOT_READY, "no step has run");
+  HC_CUDA(cudaSetDevice(c->device));
+  if (c->poly_cap == 0) {
+    c->poly_cap = 1 << 20;
+    HC_CUDA(c->polys.reserve(c->poly_cap));
+  }
+  // Re-run the (deterministic) step with polygon recording for this pair.
+  if (hc_status st = run_step(c, 1, pair)) return st;
+  if (hc_status st = finish_step(c)) return st;
+  int cnt[8];
+  HC_CUDA(cudaMemcpy(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
+  if (cnt[2] & 4) return fail(HC_ERR_OVERFLOW, "surface record buffer overflow");
+  int n = std::min(cnt[4], c->poly_cap);
+  std::vector<hc::PolyRec> r(n);
+  if (n) HC_CUDA(cudaMemcpy(r.data(), c->polys.p, n * sizeof(hc::PolyRec), cudaMemcpyDeviceToHost));
+  std::sort(r.begin(), r.end(), [](const hc::PolyRec& a, const hc::PolyRec& b) {
+    return a.elem_a != b.elem_a ? a.elem_a < b.elem_a : a.elem_b < b.elem_b;
+  });
+  int nv = 0;
+  for (auto& p : r) nv += p.nv;
+  view->n_poly = n;
+  view->n_vert = nv;
+  if (!view->poly_offset && !view->vert && !view->vert_pressure && !view->normal && !view->elem_a && !view->elem_b)
+    return HC_OK;
+  // soft frame -> world
+  const hc::PairDev& P = c->pairs_h[pair];
+  double R[9], x[3];
+  HC_CUDA(cudaMemcpy(R, c->xmat.p + 9 * (size_t)P.gs, sizeof(R), cudaMemcpyDeviceToHost));
+  HC_CUDA(cudaMemcpy(x, c->xpos.p + 3 * (size_t)P.gs, sizeof(x), cudaMemcpyDeviceToHost));
+  int k = 0;
+  for (int i = 0; i < n; ++i) {
+    const hc::PolyRec& p = r[i];
+    if (view->poly_offset) view->poly_offset[i] = k;
+    for (int j = 0; j < p.nv; ++j, ++k) {
+      double v[3] = {p.v[j][0], p.v[j][1], p.v[j][2]};
+      for (int a = 0; a < 3; ++a)
+        if (view->vert) view->vert[3 * k + a] = R[3 * a] * v[0] + R[3 * a + 1] * v[1] + R[3 * a + 2] * v[2] + x[a];
+      if (view->vert_pressure) view->vert_pressure[k] = p.v[j][3];
+    }
+    for (int a = 0; a < 3; ++a)
+      if (view->normal) view->normal[3 * i + a] = R[3 * a] * p.n[0] + R[3 * a + 1] * p.n[1] + R[3 * a + 2] * p.n[2];
+    if (view->elem_a) view->elem_a[i] = p.elem_a;
+    if (view->elem_b) view->elem_b[i] = p.elem_b;
+  }
+  if (view->poly_offset) view->poly_offset[n] = k;
+  return HC_OK;
+}
+
+hc_status hc_add_flat_sensor(hc_context* c, int geom_id, double resolution, int sampling_resolution, int window,
+                             double sigma, int* out_sensor, int* out_cx, int* out_cy) {
+  if (hc_status st = need(c)) return st;
+  auto it = c->geoms.find(geom_id);
+  if (it == c->geoms.end()) return fail(HC_ERR_INVALID_ARG, "sensor geom has no cs:: properties");
+  if (!(resolution > 0) || sampling_resolution <= 0) return fail(HC_ERR_INVALID_ARG, "bad resolution");
+  if (window < HC_WINDOW_NONE || window > HC_WINDOW_SQUARE) return fail(HC_ERR_INVALID_ARG, "bad window");
+  // FS:148-161 default sigmas
+  if (window == HC_WINDOW_GAUSS && sigma == -1.0) sigma = 0.1;
+  if (window == HC_WINDOW_TUKEY && sigma == -1.0) sigma = 0.3;
+  if ((window == HC_WINDOW_GAUSS || window == HC_WINDOW_TUKEY) && !(sigma > 0))
+    return fail(HC_ERR_INVALID_ARG, "window needs sigma > 0");
+  SensorHost S;
+  S.geom = geom_id;
+  S.resolution = resolution;
+  S.sr = sampling_resolution;
+  S.window = window;
+  S.sigma = sigma;
+  const GeomHost& g = it->second;
+  S.cx = (int)floorl(2 * (long double)g.size[0] / resolution + 0.1L);   // FS:196-197
+  S.cy = (int)floorl(2 * (long double)g.size[1] / resolution + 0.1L);
+  if (S.cx <= 0 || S.cy <= 0) return fail(HC_ERR_INVALID_ARG, "sensor grid is empty");
+  c->sensors.push_back(S);
+  c->sensors_dirty = true;
+  if (out_sensor) *out_sensor = (int)c->sensors.size() - 1;
+  if (out_cx) *out_cx = S.cx;
+  if (out_cy) *out_cy = S.cy;
+  return HC_OK;
+}
+
+hc_status hc_get_taxels(hc_context* c, int sensor, float* out) {
+  if (hc_status st = need(c)) return st;
+  if (sensor < 0 || sensor >= (int)c->sensors.size() || !out) return fail(HC_ERR_INVALID_ARG, "bad sensor");
+  if (c->sensors_dirty) return fail(HC_ERR_NOT_READY, "sensor not built; run a step first");
+  HC_CUDA(cudaSetDevice(c->device));
+  if (c->stepped) {
+    if (hc_status st = finish_step(c)) return st;
+  }
+  const SensorHost& S = c->sensors[sensor];
+  HC_CUDA(cudaMemcpy(out, c->taxels.p + S.dev.taxel_off, S.cx * S.cy * sizeof(float), cudaMemcpyDeviceToHost));
+  return HC_OK;
+}
+
+hc_status hc_get_taxels_device(hc_context* c, const float** d_taxels, int64_t* n_floats) {
+  if (hc_status st = need(c)) return st;
+  if (d_taxels) *d_taxels = c->taxels.p;
+  if (n_floats) *n_floats = c->n_cells;
+  return HC_OK;
+}
+
+hc_status hc_enable_timing(hc_context* c, int enable) {
+  if (hc_status st = need(c)) return st;
+  c->timing = enable != 0;
+  return HC_OK;
+}
+
+hc_status hc_get_timings(hc_context* c, hc_timings* out) {
+  if (hc_status st = need(c)) return st;
+  if (!out) return fail(HC_ERR_INVALID_ARG, "null output");
+  if (!c->timing) return fail(HC_ERR_NOT_READY, "timing is off");
+  HC_CUDA(cudaEventSynchronize(c->ev[5]));
+  float t[5];
+  for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&t[i], c->ev[i], c->ev[i + 1]);
+  out->ms_setup = t[0];
+  out->ms_broadphase = t[1];
+  out->ms_narrowphase = t[2];
+  out->ms_reduce = t[3];
+  out->ms_taxels = t[4];
+  cudaEventElapsedTime(&out->ms_total, c->ev[0], c->ev[5]);
+  int cnt[8];
+  HC_CUDA(cudaMemcpy(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
+  out->n_items = cnt[0];
+  out->n_polygons = 0;
+  return HC_OK;
+}
+
+hc_status hc_get_stream(hc_context* c, void** stream) {
+  if (hc_status st = need(c)) return st;
+  if (!stream) return fail(HC_ERR_INVALID_ARG, "null output");
+  *stream = (void*)c->stream;
+  return HC_OK;
+}
+
+hc_status hc_get_launch_count(hc_context* c, int* n) {
+  if (hc_status st = need(c)) return st;
+  if (n) *n = c->launches_per_step;
+  return HC_OK;
+}
+
+hc_status hc_autotune(hc_context* c, int* chosen_block, int* chosen_ctas_per_sm) {
+  if (hc_status st = need(c)) return st;
+  if (chosen_block) *chosen_block = c->narrow_block;
+  if (chosen_ctas_per_sm) *chosen_ctas_per_sm = c->narrow_ctas_per_sm;
+  return HC_OK;
+}
+
+hc_status hc_adjoint(hc_context* c, const double* dL_dwrench, const float* dL_dtaxel, double* dL_dpose,
+                     double* dL_dE) {
+  if (hc_status st = need(c)) return st;
+  (void)dL_dwrench; (void)dL_dtaxel; (void)dL_dpose; (void)dL_dE;
+  return fail(HC_ERR_UNSUPPORTED, "adjoint not built yet");
+}
+
+}  // extern "C"

@@ -1,0 +1,82 @@
+// kernels.h — launch wrappers for the device kernels (host-callable).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hc_internal.h"
+
+namespace hc {
+
+struct StepArgs {
+  // per-step inputs (device)
+  const double* xpos;
+  const double* xmat;
+  const double* vel;
+  // pairs
+  const PairDev* pairs;
+  int n_pair;
+  FrameDev* frames;
+  // geometry pools
+  const float4* tets;
+  const int* tet_orig;
+  const float4* tris;
+  const int* tri_orig;
+  const float4* nodes;
+  // broadphase units and items
+  const int* unit_pair;
+  const int* unit_cl;
+  int n_units;
+  int* unit_count;
+  int* unit_off;      // n_units + 1
+  int* block_sum;     // one per broadphase block
+  int n_bp_blocks;
+  int4* items;
+  int item_cap;
+  int* item_total;
+  int* item_next;
+  int* status;        // bit 0: item overflow, bit 1: candidate overflow,
+                      // bit 2: polygon overflow
+  ItemOut* item_out;
+  PairOut* pair_out;
+  // sensors
+  const SensorDev* sensors;
+  int n_sensor;
+  unsigned long long* samples;
+  float* taxels;
+  const float* weights;
+  const float* samp_coord;
+  int n_cells_total;
+  const int* cell_sensor;   // sensor index per global cell
+  const int* cell_first;    // first global cell of each sensor
+  // options
+  int repr;
+  int apply_forces;
+  int debug;
+  CandRec* cand;
+  int cand_cap;
+  int* cand_count;
+  PolyRec* polys;
+  int poly_cap;
+  int* poly_count;
+  int want_polys;
+  int want_pair;      // -1 = all pairs
+  // launch shape of the narrow phase
+  int narrow_block;
+  int narrow_grid;
+};
+
+constexpr int kBpBlock = 256;
+
+// LBVH build/refit: node boxes of the implicit trees of `n_geoms` geoms.
+void launch_refit(const float4* elems, int verts_per_elem, float4* nodes, const int* geom_elem_off,
+                  const int* geom_n_elem, const int* geom_node_off, const int* geom_leaves,
+                  int n_geoms, cudaStream_t s);
+
+// One step: frames, broadphase, narrow phase, per-pair reduce, taxels.
+// Returns the number of kernels launched.
+int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev /* 6 or null */);
+
+// Adjoint kernels (adjoint.cu).
+struct AdjArgs;
+
+}  // namespace hc

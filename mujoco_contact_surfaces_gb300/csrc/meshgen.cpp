@@ -1,0 +1,361 @@
+// meshgen.cpp — primitive tessellations and pressure fields (load time only).
+#include "meshgen.h"
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <utility>
+
+#include "../../include/hc/hc.h"
+
+namespace hc {
+namespace {
+
+const double kPi = 3.14159265358979323846;
+
+// Refinement level of the octahedral sphere: the smallest L whose great-arc
+// edge length pi*R/(2*2^L) is at most the hint.  Capped so a mesh stays
+// below ~2M elements.
+int sphere_level(double R, double hint) {
+  if (!(hint > 0)) return 2;
+  int L = 0;
+  while (L < 9 && kPi * R / (2.0 * std::ldexp(1.0, L)) > hint) ++L;
+  return L;
+}
+
+// Unit sphere surface: octahedron refined `level` times, every new vertex
+// projected back to the sphere.  Faces are outward counter-clockwise.
+void unit_sphere(int level, std::vector<double>* v, std::vector<int>* f) {
+  const double oct_v[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+  const int oct_f[8][3] = {{0, 2, 4}, {2, 1, 4}, {1, 3, 4}, {3, 0, 4},
+                           {2, 0, 5}, {1, 2, 5}, {3, 1, 5}, {0, 3, 5}};
+  v->assign(&oct_v[0][0], &oct_v[0][0] + 18);
+  f->assign(&oct_f[0][0], &oct_f[0][0] + 24);
+  for (int l = 0; l < level; ++l) {
+    std::map<std::pair<int, int>, int> mid;
+    std::vector<int> nf;
+    nf.reserve(f->size() * 4);
+    auto midpoint = [&](int a, int b) {
+      std::pair<int, int> key(std::min(a, b), std::max(a, b));
+      auto it = mid.find(key);
+      if (it != mid.end()) return it->second;
+      double x = (*v)[3 * a] + (*v)[3 * b], y = (*v)[3 * a + 1] + (*v)[3 * b + 1],
+             z = (*v)[3 * a + 2] + (*v)[3 * b + 2];
+      double n = std::sqrt(x * x + y * y + z * z);
+      int id = (int)(v->size() / 3);
+      v->push_back(x / n);
+      v->push_back(y / n);
+      v->push_back(z / n);
+      mid.emplace(key, id);
+      return id;
+    };
+    for (size_t i = 0; i < f->size(); i += 3) {
+      int a = (*f)[i], b = (*f)[i + 1], c = (*f)[i + 2];
+      int ab = midpoint(a, b), bc = midpoint(b, c), ca = midpoint(c, a);
+      int tri[4][3] = {{a, ab, ca}, {ab, b, bc}, {ca, bc, c}, {ab, bc, ca}};
+      for (auto& t : tri) nf.insert(nf.end(), t, t + 3);
+    }
+    f->swap(nf);
+  }
+}
+
+void orient_tets(SoftMesh* m) {
+  for (size_t i = 0; i < m->t.size(); i += 4) {
+    int* t = &m->t[i];
+    if (tet_volume(&m->v[3 * t[0]], &m->v[3 * t[1]], &m->v[3 * t[2]], &m->v[3 * t[3]]) < 0)
+      std::swap(t[2], t[3]);
+  }
+}
+
+// Soft body made of one interior vertex fanned to every surface triangle
+// (the single-interior-vertex strategy of P:652-653 and the convex-mesh
+// fan of P:766-789).  The interior vertex carries pressure E, the surface
+// vertices 0.
+void fan_soft(const std::vector<double>& sv, const std::vector<int>& sf, const double c[3],
+              double E, SoftMesh* out) {
+  out->v = sv;
+  out->v.insert(out->v.end(), c, c + 3);
+  int ci = (int)(sv.size() / 3);
+  out->p.assign(sv.size() / 3, 0.0);
+  out->p.push_back(E);
+  out->t.clear();
+  out->t.reserve(sf.size() / 3 * 4);
+  for (size_t i = 0; i < sf.size(); i += 3) {
+    int tet[4] = {ci, sf[i], sf[i + 1], sf[i + 2]};
+    out->t.insert(out->t.end(), tet, tet + 4);
+  }
+  orient_tets(out);
+}
+
+// Kuhn (Freudenthal) split of the logical hex [i,i+1]x[j,j+1]x[k,k+1] into
+// six tets sharing the diagonal corner0 -> corner7; every hex face is cut on
+// its min->max diagonal, so neighbouring cells agree.  `vid(di,dj,dk)` maps a
+// logical corner to a vertex id; tets with a repeated vertex (collapsed
+// corners) are dropped.
+template <class F>
+void kuhn_cell(F vid, std::vector<int>* tets) {
+  const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  for (auto& p : perm) {
+    int c[3] = {0, 0, 0};
+    int ids[4];
+    ids[0] = vid(0, 0, 0);
+    for (int s = 0; s < 3; ++s) {
+      c[p[s]] = 1;
+      ids[s + 1] = vid(c[0], c[1], c[2]);
+    }
+    bool dup = false;
+    for (int a = 0; a < 4; ++a)
+      for (int b = a + 1; b < 4; ++b) dup |= ids[a] == ids[b];
+    if (!dup) tets->insert(tets->end(), ids, ids + 4);
+  }
+}
+
+int even_count(double extent, double hint, int min_n) {
+  int n = min_n;
+  if (hint > 0) n = std::max(min_n, 2 * (int)std::ceil(extent / (2.0 * hint) - 1e-9));
+  if (n % 2) ++n;
+  return n;
+}
+
+void soft_box(const double h[3], double E, double hint, SoftMesh* out) {
+  // Even cell counts put a vertex layer on every mid-plane, so the extent
+  // field min_i(h_i - |x_i|) / min_i(h_i) is captured exactly in the
+  // thinnest direction.
+  int n[3];
+  for (int a = 0; a < 3; ++a) n[a] = even_count(2 * h[a], hint, 2);
+  auto id = [&](int i, int j, int k) { return (k * (n[1] + 1) + j) * (n[0] + 1) + i; };
+  double hmin = std::min(h[0], std::min(h[1], h[2]));
+  out->v.clear();
+  out->p.clear();
+  for (int k = 0; k <= n[2]; ++k)
+    for (int j = 0; j <= n[1]; ++j)
+      for (int i = 0; i <= n[0]; ++i) {
+        double x = -h[0] + 2 * h[0] * i / n[0], y = -h[1] + 2 * h[1] * j / n[1],
+               z = -h[2] + 2 * h[2] * k / n[2];
+        out->v.insert(out->v.end(), {x, y, z});
+        double d = std::min(h[0] - std::fabs(x), std::min(h[1] - std::fabs(y), h[2] - std::fabs(z)));
+        out->p.push_back(E * std::max(0.0, d) / hmin);
+      }
+  out->t.clear();
+  for (int k = 0; k < n[2]; ++k)
+    for (int j = 0; j < n[1]; ++j)
+      for (int i = 0; i < n[0]; ++i)
+        kuhn_cell([&](int a, int b, int c) { return id(i + a, j + b, k + c); }, &out->t);
+  orient_tets(out);
+}
+
+void soft_cylinder(double R, double hl, double E, double hint, SoftMesh* out) {
+  int nr = std::max(1, hint > 0 ? (int)std::ceil(R / hint - 1e-9) : 1);
+  int ns = std::max(12, 4 * (int)std::ceil(2 * kPi * R / (4 * (hint > 0 ? hint : R)) - 1e-9));
+  int nz = even_count(2 * hl, hint, 2);
+  // Vertex ids: per layer k, the axis vertex then rings 1..nr with ns each.
+  int per_layer = 1 + nr * ns;
+  auto id = [&](int i, int j, int k) {
+    if (i == 0) return k * per_layer;
+    return k * per_layer + 1 + (i - 1) * ns + ((j % ns) + ns) % ns;
+  };
+  double dmax = std::min(R, hl);
+  out->v.clear();
+  out->p.clear();
+  for (int k = 0; k <= nz; ++k) {
+    double z = -hl + 2 * hl * k / nz;
+    for (int i = 0; i <= nr; ++i) {
+      int jn = i == 0 ? 1 : ns;
+      for (int j = 0; j < jn; ++j) {
+        double r = R * i / nr, th = 2 * kPi * j / ns;
+        out->v.insert(out->v.end(), {r * std::cos(th), r * std::sin(th), z});
+        double d = std::min(R - r, hl - std::fabs(z));
+        out->p.push_back(E * std::max(0.0, d) / dmax);
+      }
+    }
+  }
+  out->t.clear();
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ns; ++j)
+      for (int i = 0; i < nr; ++i)
+        kuhn_cell([&](int a, int b, int c) { return id(i + a, j + b, k + c); }, &out->t);
+  orient_tets(out);
+}
+
+void rigid_box(const double h[3], double hint, RigidMesh* out) {
+  out->v.clear();
+  out->f.clear();
+  // Each face: axis a normal, sign s; in-plane axes u, v chosen so that
+  // u x v = s * e_a (outward counter-clockwise).
+  for (int a = 0; a < 3; ++a)
+    for (int s = -1; s <= 1; s += 2) {
+      int u = (a + 1) % 3, w = (a + 2) % 3;
+      if (s < 0) std::swap(u, w);
+      int nu = hint > 0 ? std::max(1, (int)std::ceil(2 * h[u] / hint - 1e-9)) : 1;
+      int nw = hint > 0 ? std::max(1, (int)std::ceil(2 * h[w] / hint - 1e-9)) : 1;
+      int base = (int)(out->v.size() / 3);
+      for (int jw = 0; jw <= nw; ++jw)
+        for (int iu = 0; iu <= nu; ++iu) {
+          double p[3];
+          p[a] = s * h[a];
+          p[u] = -h[u] + 2 * h[u] * iu / nu;
+          p[w] = -h[w] + 2 * h[w] * jw / nw;
+          out->v.insert(out->v.end(), p, p + 3);
+        }
+      for (int jw = 0; jw < nw; ++jw)
+        for (int iu = 0; iu < nu; ++iu) {
+          int v00 = base + jw * (nu + 1) + iu, v10 = v00 + 1, v01 = v00 + nu + 1, v11 = v01 + 1;
+          out->f.insert(out->f.end(), {v00, v10, v11, v00, v11, v01});
+        }
+    }
+}
+
+void rigid_cylinder(double R, double hl, double hint, RigidMesh* out) {
+  int ns = std::max(12, 4 * (int)std::ceil(2 * kPi * R / (4 * (hint > 0 ? hint : R)) - 1e-9));
+  int nz = hint > 0 ? std::max(1, (int)std::ceil(2 * hl / hint - 1e-9)) : 1;
+  out->v.clear();
+  out->f.clear();
+  for (int k = 0; k <= nz; ++k)
+    for (int j = 0; j < ns; ++j) {
+      double th = 2 * kPi * j / ns;
+      out->v.insert(out->v.end(), {R * std::cos(th), R * std::sin(th), -hl + 2 * hl * k / nz});
+    }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ns; ++j) {
+      int a = k * ns + j, b = k * ns + (j + 1) % ns, c = a + ns, d = b + ns;
+      out->f.insert(out->f.end(), {a, b, d, a, d, c});
+    }
+  int cb = (int)(out->v.size() / 3);
+  out->v.insert(out->v.end(), {0, 0, -hl});
+  out->v.insert(out->v.end(), {0, 0, hl});
+  for (int j = 0; j < ns; ++j) {
+    int a = j, b = (j + 1) % ns;
+    out->f.insert(out->f.end(), {cb, b, a});                      // bottom, -z
+    out->f.insert(out->f.end(), {cb + 1, nz * ns + a, nz * ns + b});  // top, +z
+  }
+}
+
+// Centroid of the volume enclosed by a closed, outward oriented triangle
+// mesh: signed-volume weighted centroids of the tets (origin, p, q, r).
+// Same quantity as CalcCentroidOfEnclosedVolume.
+bool enclosed_centroid(const double* v, const int* f, int nf, double c[3]) {
+  double six_total = 0, acc[3] = {0, 0, 0};
+  for (int i = 0; i < nf; ++i) {
+    const double *p = v + 3 * f[3 * i], *q = v + 3 * f[3 * i + 1], *r = v + 3 * f[3 * i + 2];
+    double cx = q[1] * r[2] - q[2] * r[1], cy = q[2] * r[0] - q[0] * r[2], cz = q[0] * r[1] - q[1] * r[0];
+    double six = p[0] * cx + p[1] * cy + p[2] * cz;
+    six_total += six;
+    for (int a = 0; a < 3; ++a) acc[a] += six * (p[a] + q[a] + r[a]);
+  }
+  if (!(std::fabs(six_total) > 0)) return false;
+  for (int a = 0; a < 3; ++a) c[a] = acc[a] / (4 * six_total);
+  return true;
+}
+
+bool finite3(const double* s) {
+  return std::isfinite(s[0]) && std::isfinite(s[1]) && std::isfinite(s[2]);
+}
+
+}  // namespace
+
+double tet_volume(const double* a, const double* b, const double* c, const double* d) {
+  double e1[3], e2[3], e3[3];
+  for (int i = 0; i < 3; ++i) e1[i] = b[i] - a[i], e2[i] = c[i] - a[i], e3[i] = d[i] - a[i];
+  double cx = e2[1] * e3[2] - e2[2] * e3[1], cy = e2[2] * e3[0] - e2[0] * e3[2],
+         cz = e2[0] * e3[1] - e2[1] * e3[0];
+  return (e1[0] * cx + e1[1] * cy + e1[2] * cz) / 6.0;
+}
+
+std::string make_soft_mesh(int type, const double size[3], double E, double hint,
+                           const double* mesh_v, int nv, const int* mesh_f, int nf, SoftMesh* out) {
+  if (!(E > 0) || !std::isfinite(E)) return "soft geom needs a finite modulus E > 0";
+  if (!finite3(size)) return "non-finite geom size";
+  switch (type) {
+    case HC_GEOM_SPHERE:
+    case HC_GEOM_ELLIPSOID: {
+      double ax[3];
+      if (type == HC_GEOM_SPHERE) ax[0] = ax[1] = ax[2] = size[0];
+      else for (int a = 0; a < 3; ++a) ax[a] = size[a];
+      if (!(ax[0] > 0 && ax[1] > 0 && ax[2] > 0)) return "sphere/ellipsoid needs positive radii";
+      std::vector<double> sv;
+      std::vector<int> sf;
+      unit_sphere(sphere_level(std::max(ax[0], std::max(ax[1], ax[2])), hint), &sv, &sf);
+      for (size_t i = 0; i < sv.size(); ++i) sv[i] *= ax[i % 3];
+      const double c[3] = {0, 0, 0};
+      fan_soft(sv, sf, c, E, out);
+      return "";
+    }
+    case HC_GEOM_BOX: {
+      if (!(size[0] > 0 && size[1] > 0 && size[2] > 0)) return "box needs positive half sizes";
+      soft_box(size, E, hint, out);
+      return "";
+    }
+    case HC_GEOM_CYLINDER: {
+      // A soft cylinder with hint <= 0 reads an uninitialised mesh in the
+      // reference; here it is rejected.
+      if (!(hint > 0)) return "soft cylinder needs a positive resolution hint";
+      if (!(size[0] > 0 && size[1] > 0)) return "cylinder needs positive radius and half length";
+      soft_cylinder(size[0], size[1], E, hint, out);
+      return "";
+    }
+    case HC_GEOM_MESH: {
+      if (!mesh_v || !mesh_f || nv < 4 || nf < 4) return "mesh geom needs vertices and faces";
+      for (int i = 0; i < 3 * nf; ++i)
+        if (mesh_f[i] < 0 || mesh_f[i] >= nv) return "mesh face index out of range";
+      double c[3];
+      if (!enclosed_centroid(mesh_v, mesh_f, nf, c)) return "mesh encloses zero volume";
+      std::vector<double> sv(mesh_v, mesh_v + 3 * nv);
+      std::vector<int> sf(mesh_f, mesh_f + 3 * nf);
+      fan_soft(sv, sf, c, E, out);
+      return "";
+    }
+    case HC_GEOM_PLANE: return "soft plane collision not implemented";
+    case HC_GEOM_HFIELD: return "hfield collision not implemented";
+    case HC_GEOM_CAPSULE: return "capsule collision not implemented";
+    default: return "unknown geom type";
+  }
+}
+
+std::string make_rigid_mesh(int type, const double size[3], double hint, const double* mesh_v,
+                            int nv, const int* mesh_f, int nf, RigidMesh* out) {
+  if (!finite3(size)) return "non-finite geom size";
+  switch (type) {
+    case HC_GEOM_PLANE: out->v.clear(); out->f.clear(); return "";
+    case HC_GEOM_SPHERE:
+    case HC_GEOM_ELLIPSOID: {
+      double ax[3];
+      if (type == HC_GEOM_SPHERE) ax[0] = ax[1] = ax[2] = size[0];
+      else for (int a = 0; a < 3; ++a) ax[a] = size[a];
+      if (!(ax[0] > 0 && ax[1] > 0 && ax[2] > 0)) return "sphere/ellipsoid needs positive radii";
+      unit_sphere(sphere_level(std::max(ax[0], std::max(ax[1], ax[2])), hint), &out->v, &out->f);
+      for (size_t i = 0; i < out->v.size(); ++i) out->v[i] *= ax[i % 3];
+      return "";
+    }
+    case HC_GEOM_BOX:
+      if (!(size[0] > 0 && size[1] > 0 && size[2] > 0)) return "box needs positive half sizes";
+      rigid_box(size, hint, out);
+      return "";
+    case HC_GEOM_CYLINDER:
+      if (!(size[0] > 0 && size[1] > 0)) return "cylinder needs positive radius and half length";
+      rigid_cylinder(size[0], size[1], hint, out);
+      return "";
+    case HC_GEOM_MESH:
+      if (!mesh_v || !mesh_f || nv < 3 || nf < 1) return "mesh geom needs vertices and faces";
+      for (int i = 0; i < 3 * nf; ++i)
+        if (mesh_f[i] < 0 || mesh_f[i] >= nv) return "mesh face index out of range";
+      out->v.assign(mesh_v, mesh_v + 3 * nv);
+      out->f.assign(mesh_f, mesh_f + 3 * nf);
+      return "";
+    case HC_GEOM_HFIELD: return "hfield collision not implemented";
+    case HC_GEOM_CAPSULE: return "capsule collision not implemented";
+    default: return "unknown geom type";
+  }
+}
+
+void round_to_float(SoftMesh* m) {
+  for (double& x : m->v) x = (double)(float)x;
+  for (double& x : m->p) x = (double)(float)x;
+  // Rounding can flip a sliver's orientation; re-orient.
+  orient_tets(m);
+}
+
+void round_to_float(RigidMesh* m) {
+  for (double& x : m->v) x = (double)(float)x;
+}
+
+}  // namespace hc

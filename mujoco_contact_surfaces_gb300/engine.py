@@ -1,0 +1,185 @@
+"""Host-side wrapper of one engine context (the C ABI in include/hc/hc.h).
+
+`Engine` mirrors what the reference plugin does per model load and per step
+(mujoco_contact_surfaces_plugin.cpp: load P:208-245, collision_cb
+P:255-318, passiveCallback P:411-523), with numpy arrays in and out.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+class Engine:
+    def __init__(self, device: int = 0, representation: int = L.REPR_TRIANGLE, apply_forces: bool = True,
+                 use_graph: bool = True, item_capacity: int = 0):
+        self.lib = L.load()
+        cfg = L.hc_config()
+        self.lib.hc_config_default(C.byref(cfg))
+        cfg.device = device
+        cfg.representation = representation
+        cfg.apply_forces = int(apply_forces)
+        cfg.use_graph = int(use_graph)
+        cfg.item_capacity = item_capacity
+        self.ctx = C.c_void_p()
+        L.check(self.lib.hc_context_create(C.byref(cfg), C.byref(self.ctx)))
+        self.n_pair = 0
+        self.sensors = {}   # sensor index -> (cx, cy)
+
+    def close(self):
+        if self.ctx:
+            self.lib.hc_context_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- geoms ---------------------------------------------------------------
+    def add_geom(self, geom_id: int, gtype: int, size, cs5, mesh_vert=None, mesh_face=None) -> int:
+        size = np.ascontiguousarray(size, np.float64)
+        cs5 = np.ascontiguousarray(cs5, np.float64)
+        mv = np.ascontiguousarray(mesh_vert, np.float64).reshape(-1) if mesh_vert is not None else None
+        mf = np.ascontiguousarray(mesh_face, np.int32).reshape(-1) if mesh_face is not None else None
+        kind = C.c_int()
+        L.check(self.lib.hc_add_geom(self.ctx, geom_id, gtype, L.dptr(size), L.dptr(cs5), L.dptr(mv),
+                                     0 if mv is None else len(mv) // 3, L.iptr(mf), 0 if mf is None else len(mf) // 3,
+                                     C.byref(kind)))
+        return kind.value
+
+    def geom_info(self, geom_id: int) -> L.hc_geom_info:
+        info = L.hc_geom_info()
+        L.check(self.lib.hc_get_geom_info(self.ctx, geom_id, C.byref(info)))
+        return info
+
+    def geom_mesh(self, geom_id: int):
+        info = self.geom_info(geom_id)
+        npe = 4 if info.kind == L.SOFT else 3
+        v = np.zeros((info.n_vertices, 3), np.float64)
+        e = np.zeros((info.n_elements, npe), np.int32)
+        p = np.zeros(info.n_vertices, np.float64) if info.kind == L.SOFT else None
+        L.check(self.lib.hc_get_geom_mesh(self.ctx, geom_id, L.dptr(v), L.dptr(p), L.iptr(e)))
+        return v, p, e
+
+    def update_geom_size(self, geom_id: int, size):
+        size = np.ascontiguousarray(size, np.float64)
+        L.check(self.lib.hc_update_geom_size(self.ctx, geom_id, L.dptr(size)))
+
+    def add_flat_sensor(self, geom_id: int, resolution: float, sampling_resolution: int = 5,
+                        window: int = L.WINDOW_NONE, sigma: float = -1.0) -> int:
+        sid, cx, cy = C.c_int(), C.c_int(), C.c_int()
+        L.check(self.lib.hc_add_flat_sensor(self.ctx, geom_id, resolution, sampling_resolution, window, sigma,
+                                            C.byref(sid), C.byref(cx), C.byref(cy)))
+        self.sensors[sid.value] = (cx.value, cy.value)
+        return sid.value
+
+    # -- per step --------------------------------------------------------------
+    def set_poses(self, xpos, xmat, vel=None):
+        xpos = np.ascontiguousarray(xpos, np.float64)
+        xmat = np.ascontiguousarray(xmat, np.float64)
+        n = xpos.size // 3
+        v = np.ascontiguousarray(vel, np.float64) if vel is not None else None
+        L.check(self.lib.hc_set_poses(self.ctx, n, L.dptr(xpos), L.dptr(xmat), L.dptr(v)))
+
+    def set_poses_device(self, n_geom: int, d_xpos: int, d_xmat: int, d_vel: int | None):
+        L.check(self.lib.hc_set_poses_device(self.ctx, n_geom, C.c_void_p(d_xpos), C.c_void_p(d_xmat),
+                                             C.c_void_p(d_vel) if d_vel else None))
+
+    def set_pairs(self, g1, g2):
+        g1 = np.ascontiguousarray(g1, np.int32)
+        g2 = np.ascontiguousarray(g2, np.int32)
+        st = np.zeros(len(g1), np.int32)
+        q = np.zeros(len(g1), np.int32)
+        L.check(self.lib.hc_set_pairs(self.ctx, len(g1), L.iptr(g1), L.iptr(g2), L.iptr(st), L.iptr(q)))
+        self.n_pair = len(g1)
+        return st, q
+
+    def step(self):
+        L.check(self.lib.hc_step(self.ctx))
+
+    def wrenches(self) -> np.ndarray:
+        w = np.zeros((self.n_pair, 6), np.float64)
+        L.check(self.lib.hc_get_wrenches(self.ctx, L.dptr(w)))
+        return w
+
+    def pair_order(self):
+        q = np.zeros(self.n_pair, np.int32)
+        m = np.zeros(self.n_pair, np.int32)
+        n = np.zeros(self.n_pair, np.int32)
+        L.check(self.lib.hc_get_pair_order(self.ctx, L.iptr(q), L.iptr(m), L.iptr(n)))
+        return q, m, n
+
+    def pair_stats(self):
+        arr = (L.hc_pair_stats * max(1, self.n_pair))()
+        L.check(self.lib.hc_get_pair_stats(self.ctx, arr))
+        return [arr[i] for i in range(self.n_pair)]
+
+    def taxels(self, sensor: int) -> np.ndarray:
+        cx, cy = self.sensors[sensor]
+        out = np.zeros(cx * cy, np.float32)
+        L.check(self.lib.hc_get_taxels(self.ctx, sensor, L.fptr(out)))
+        return out
+
+    def set_debug(self, flags: int):
+        L.check(self.lib.hc_set_debug(self.ctx, flags))
+
+    def candidates(self) -> np.ndarray:
+        n = C.c_int64()
+        L.check(self.lib.hc_get_candidates(self.ctx, None, 0, C.byref(n)))
+        arr = (L.hc_candidate * max(1, n.value))()
+        L.check(self.lib.hc_get_candidates(self.ctx, arr, n.value, C.byref(n)))
+        out = np.zeros((n.value, 5), np.int64)
+        for i in range(n.value):
+            r = arr[i]
+            out[i] = (r.pair, r.elem_a, r.elem_b, r.n_vert, r.flags)
+        return out
+
+    def surface(self, pair: int):
+        v = L.hc_surface_view()
+        L.check(self.lib.hc_get_surface(self.ctx, pair, C.byref(v)))
+        n, nv = v.n_poly, v.n_vert
+        off = np.zeros(n + 1, np.int32)
+        vert = np.zeros((nv, 3), np.float64)
+        pr = np.zeros(nv, np.float64)
+        nrm = np.zeros((n, 3), np.float64)
+        ea = np.zeros(n, np.int32)
+        eb = np.zeros(n, np.int32)
+        v.poly_offset = L.iptr(off)
+        v.vert = L.dptr(vert)
+        v.vert_pressure = L.dptr(pr)
+        v.normal = L.dptr(nrm)
+        v.elem_a = L.iptr(ea)
+        v.elem_b = L.iptr(eb)
+        L.check(self.lib.hc_get_surface(self.ctx, pair, C.byref(v)))
+        return dict(offset=off, vert=vert, pressure=pr, normal=nrm, elem_a=ea, elem_b=eb)
+
+    def enable_timing(self, on: bool = True):
+        L.check(self.lib.hc_enable_timing(self.ctx, int(on)))
+
+    def timings(self) -> L.hc_timings:
+        t = L.hc_timings()
+        L.check(self.lib.hc_get_timings(self.ctx, C.byref(t)))
+        return t
+
+    def launch_count(self) -> int:
+        n = C.c_int()
+        L.check(self.lib.hc_get_launch_count(self.ctx, C.byref(n)))
+        return n.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        L.check(self.lib.hc_get_stream(self.ctx, C.byref(s)))
+        return s.value or 0
+
+    def adjoint(self, dL_dwrench=None, dL_dtaxel=None):
+        dw = np.ascontiguousarray(dL_dwrench, np.float64) if dL_dwrench is not None else None
+        dt = np.ascontiguousarray(dL_dtaxel, np.float32) if dL_dtaxel is not None else None
+        dpose = np.zeros((self.n_pair, 2, 6), np.float64)
+        dE = np.zeros((self.n_pair, 2), np.float64)
+        L.check(self.lib.hc_adjoint(self.ctx, L.dptr(dw), L.fptr(dt), L.dptr(dpose), L.dptr(dE)))
+        return dpose, dE

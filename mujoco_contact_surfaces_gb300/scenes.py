@@ -1,0 +1,324 @@
+"""Seeded synthetic scenes for the contact-surface workloads.
+
+Every generator uses numpy's PCG64 with seed = workload index * 1000 +
+repeat.  A scene is plain data (geoms with MuJoCo geom types, sizes and the
+cs:: 5-tuple [E, dissipation, resolutionHint, mu_static, mu_dynamic], poses as
+geom_xpos / row-major geom_xmat, velocities [omega; v], contact pairs and flat
+sensors), so the same scene feeds the engine and the oracle.
+
+Workloads (sizes from the reference's example assets and configs):
+  single_pair   soft sphere R=0.05 m at resolution 0.01 m, E=1e5 Pa, d=1 s/m,
+                mu=0.5, on a rigid 0.2x0.2x0.02 m box (12 triangles); poses
+                with penetration U[0,5 mm] and tilt U[-30,30] deg.
+  tactile       rigid 8x8 cm plate with a 16x16 flat taxel grid (5 mm pitch,
+                5x5 rays per cell) pressed by a soft sphere, ellipsoid
+                (0.04/0.03/0.02) or cylinder (r=0.03, h=0.06), 2k-8k tets,
+                E U[5e4,5e5], penetration U[0,4 mm], offset U[-2,2 cm]^2.
+  batched       soft primitives of 500-20000 tets (log-uniform) against
+                rigid meshes of 12-5000 triangles, 1-8 pairs per scene,
+                penetration U[0,10%] of the soft extent, velocities U[-0.1,0.1].
+  soft_soft     pairs of soft spheres/boxes, 2k-50k tets, E ratio
+                log-U[0.1,10], overlap U[0,8%] of the smaller extent, random
+                relative rotation.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+
+SEED_SINGLE, SEED_TACTILE, SEED_BATCHED, SEED_SOFTSOFT, SEED_ADJOINT = 0, 1000, 2000, 3000, 4000
+
+
+@dataclass
+class Scene:
+    geoms: list = field(default_factory=list)      # dicts: id, type, size, cs5, mesh_v, mesh_f
+    xpos: np.ndarray | None = None
+    xmat: np.ndarray | None = None
+    vel: np.ndarray | None = None
+    g1: list = field(default_factory=list)
+    g2: list = field(default_factory=list)
+    sensors: list = field(default_factory=list)    # dicts: geom, resolution, sr, window, sigma
+    scene_of_pair: list = field(default_factory=list)
+
+    @property
+    def n_geom(self):
+        return len(self.geoms)
+
+    def add_geom(self, gtype, size, cs5, mesh_v=None, mesh_f=None) -> int:
+        gid = len(self.geoms)
+        self.geoms.append(dict(id=gid, type=gtype, size=np.asarray(size, np.float64),
+                               cs5=np.asarray(cs5, np.float64), mesh_v=mesh_v, mesh_f=mesh_f))
+        return gid
+
+
+def rot_axis(axis, ang):
+    a = np.asarray(axis, np.float64)
+    a = a / np.linalg.norm(a)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) + math.sin(ang) * K + (1 - math.cos(ang)) * (K @ K)
+
+
+def random_rotation(rng):
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def sphere_hint(R, level):
+    """Resolution hint that selects octahedral refinement `level` for radius R."""
+    return math.pi * R / (2.0 * 2 ** level) * 1.0001
+
+
+def _alloc(scene: Scene):
+    n = scene.n_geom
+    scene.xpos = np.zeros((n, 3))
+    scene.xmat = np.tile(np.eye(3).reshape(1, 9), (n, 1))
+    scene.vel = np.zeros((n, 6))
+
+
+def single_pair(n_poses=1000, seed=SEED_SINGLE, velocities=False) -> Scene:
+    """Soft sphere on a rigid box, one pair per pose (each pose its own scene)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene()
+    R = 0.05
+    for k in range(n_poses):
+        gs = s.add_geom(L.GEOM_SPHERE, [R, 0, 0], [1e5, 1.0, 0.01, 0.5, 0.5])
+        gb = s.add_geom(L.GEOM_BOX, [0.1, 0.1, 0.01], [0, 1.0, 0, 0.5, 0.5])
+        s.g1.append(gs); s.g2.append(gb); s.scene_of_pair.append(k)
+    _alloc(s)
+    for k in range(n_poses):
+        gs, gb = 2 * k, 2 * k + 1
+        pen = rng.uniform(0, 0.005)
+        tilt = math.radians(rng.uniform(-30, 30))
+        phi = rng.uniform(0, 2 * math.pi)
+        axis = [math.cos(phi), math.sin(phi), 0.0]
+        Rs = rot_axis(axis, tilt) @ rot_axis([0, 0, 1], rng.uniform(0, 2 * math.pi))
+        s.xmat[gs] = Rs.reshape(9)
+        s.xpos[gs] = [0.0, 0.0, 0.01 + R - pen]
+        s.xpos[gb] = [0.0, 0.0, 0.0]
+        if velocities:
+            s.vel[gs] = rng.uniform(-0.1, 0.1, 6)
+    return s
+
+
+def tactile(n_scenes=16, seed=SEED_TACTILE, velocities=False, sampling_resolution=5,
+            plate_half=(0.04, 0.04, 0.005)) -> Scene:
+    """Rigid plate with a 16x16 taxel grid pressed by a soft primitive.
+
+    With a square plate the top face's diagonal passes exactly through the
+    samples with equal x and y indices; parity tests use a plate 0.1 mm
+    wider in x so that no ray sample sits exactly on a triangle edge."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene()
+    plate_h = list(plate_half)
+    kinds = []
+    for k in range(n_scenes):
+        kind = int(rng.integers(0, 3))
+        E = rng.uniform(5e4, 5e5)
+        if kind == 0:
+            R = rng.uniform(0.025, 0.04)
+            lev = int(rng.integers(4, 6))
+            g = s.add_geom(L.GEOM_SPHERE, [R, 0, 0], [E, 1.0, sphere_hint(R, lev), 0.5, 0.5])
+            low = R
+        elif kind == 1:
+            lev = int(rng.integers(4, 6))
+            g = s.add_geom(L.GEOM_ELLIPSOID, [0.04, 0.03, 0.02], [E, 1.0, sphere_hint(0.04, lev), 0.5, 0.5])
+            low = 0.02
+        else:
+            hint = float(rng.choice([0.01, 0.0075]))
+            g = s.add_geom(L.GEOM_CYLINDER, [0.03, 0.03, 0], [E, 1.0, hint, 0.5, 0.5])
+            low = 0.03   # lying on its side
+        p = s.add_geom(L.GEOM_BOX, plate_h, [0, 1.0, 0, 0.5, 0.5])
+        s.g1.append(g); s.g2.append(p); s.scene_of_pair.append(k)
+        s.sensors.append(dict(geom=p, resolution=0.005, sr=sampling_resolution, window=L.WINDOW_NONE, sigma=-1.0))
+        kinds.append((kind, low))
+    _alloc(s)
+    for k in range(n_scenes):
+        g, p = 2 * k, 2 * k + 1
+        kind, low = kinds[k]
+        pen = rng.uniform(0, 0.004)
+        off = rng.uniform(-0.02, 0.02, 2)
+        yaw = rot_axis([0, 0, 1], rng.uniform(0, 2 * math.pi))
+        Rg = yaw @ rot_axis([1, 0, 0], math.pi / 2) if kind == 2 else yaw
+        s.xmat[g] = Rg.reshape(9)
+        s.xpos[g] = [off[0], off[1], plate_h[2] + low - pen]
+        s.xpos[p] = [0, 0, 0]
+        if velocities:
+            s.vel[g] = rng.uniform(-0.1, 0.1, 6)
+    return s
+
+
+def _soft_primitive(rng, target_tets):
+    """A random convex soft primitive with roughly `target_tets` tets."""
+    kind = int(rng.integers(0, 4))
+    ext = rng.uniform(0.02, 0.08)
+    E = rng.uniform(5e4, 5e5)
+    if kind == 0:
+        lev = int(np.clip(round(math.log(max(target_tets, 8) / 8, 4)), 2, 6))
+        return L.GEOM_SPHERE, [ext, 0, 0], [E, 1.0, sphere_hint(ext, lev), 0.5, 0.5], ext
+    if kind == 1:
+        ax = ext * rng.uniform(0.4, 1.0, 3)
+        ax[0] = ext
+        lev = int(np.clip(round(math.log(max(target_tets, 8) / 8, 4)), 2, 6))
+        return L.GEOM_ELLIPSOID, list(ax), [E, 1.0, sphere_hint(ext, lev), 0.5, 0.5], float(ax.min())
+    if kind == 2:
+        h = ext * rng.uniform(0.3, 1.0, 3)
+        vol_cells = target_tets / 6.0
+        hint = (8 * h[0] * h[1] * h[2] / vol_cells) ** (1 / 3)
+        return L.GEOM_BOX, list(h), [E, 1.0, hint, 0.5, 0.5], float(h.min())
+    r, hl = ext, ext * rng.uniform(0.3, 1.5)
+    hint = (2 * math.pi * r * r * hl * 6 / max(target_tets, 100)) ** (1 / 3) * 0.9
+    return L.GEOM_CYLINDER, [r, hl, 0], [E, 1.0, hint, 0.5, 0.5], min(r, hl)
+
+
+def _rigid_primitive(rng, target_tris):
+    kind = int(rng.integers(0, 3))
+    ext = rng.uniform(0.05, 0.2)
+    if kind == 0 or target_tris <= 12:
+        h = [ext, ext * rng.uniform(0.5, 1.0), ext * rng.uniform(0.1, 0.5)]
+        area = 8 * (h[0] * h[1] + h[1] * h[2] + h[0] * h[2])
+        hint = math.sqrt(area / max(target_tris / 2.0, 6)) if target_tris > 12 else 0.0
+        return L.GEOM_BOX, h, [0, 1.0, hint, 0.5, 0.5], h[2]
+    if kind == 1:
+        lev = int(np.clip(round(math.log(max(target_tris, 8) / 8, 4)), 1, 5))
+        return L.GEOM_SPHERE, [ext, 0, 0], [0, 1.0, sphere_hint(ext, lev), 0.5, 0.5], ext
+    r, hl = ext, ext * rng.uniform(0.3, 1.0)
+    hint = math.sqrt(2 * math.pi * r * 2 * hl / max(target_tris / 2.0, 12))
+    return L.GEOM_CYLINDER, [r, hl, 0], [0, 1.0, hint, 0.5, 0.5], r
+
+
+def batched(n_scenes=4096, seed=SEED_BATCHED, max_pairs=8, tet_range=(500, 20000), tri_range=(12, 5000)) -> Scene:
+    """Independent scenes of 1-8 soft-rigid pairs with uneven mesh sizes."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene()
+    place = []
+    for k in range(n_scenes):
+        npair = int(rng.integers(1, max_pairs + 1))
+        for _ in range(npair):
+            nt = math.exp(rng.uniform(math.log(tet_range[0]), math.log(tet_range[1])))
+            nr = math.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1])))
+            st, ssize, scs, sext = _soft_primitive(rng, nt)
+            rt, rsize, rcs, rext = _rigid_primitive(rng, nr)
+            gs = s.add_geom(st, ssize, scs)
+            gr = s.add_geom(rt, rsize, rcs)
+            s.g1.append(gs); s.g2.append(gr); s.scene_of_pair.append(k)
+            place.append((gs, gr, st, ssize, rt, rsize, sext, rext))
+    _alloc(s)
+    for (gs, gr, st, ssize, rt, rsize, sext, rext) in place:
+        # rigid body at the origin of its own scene frame, its top support
+        # at z = top; the soft body above it, sunk by a fraction of its extent
+        if rt == L.GEOM_BOX:
+            top = rsize[2]
+        elif rt == L.GEOM_SPHERE:
+            top = rsize[0]
+        else:
+            top = rsize[1]   # cylinder cap
+        Rs = random_rotation(rng)
+        # lowest point of the soft body along z after rotation (support)
+        if st == L.GEOM_SPHERE:
+            low = ssize[0]
+        elif st == L.GEOM_ELLIPSOID:
+            low = float(np.sqrt(np.sum((Rs[2, :] * np.asarray(ssize)) ** 2)))
+        elif st == L.GEOM_BOX:
+            low = float(np.sum(np.abs(Rs[2, :]) * np.asarray(ssize)))
+        else:
+            r, hl = ssize[0], ssize[1]
+            low = float(r * math.sqrt(max(0.0, 1 - Rs[2, 2] ** 2)) + hl * abs(Rs[2, 2]))
+        pen = rng.uniform(0, 0.1) * sext
+        off = rng.uniform(-0.3, 0.3, 2) * min(sext, rext)
+        s.xmat[gs] = Rs.reshape(9)
+        s.xpos[gs] = [off[0], off[1], top + low - pen]
+        s.xpos[gr] = [0, 0, 0]
+        s.vel[gs] = rng.uniform(-0.1, 0.1, 6)
+        s.vel[gr] = rng.uniform(-0.1, 0.1, 6)
+    return s
+
+
+def soft_soft(n_pairs=1024, seed=SEED_SOFTSOFT, tet_range=(2000, 50000)) -> Scene:
+    """Pairs of soft spheres/boxes meeting on the equal-pressure surface."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene()
+    place = []
+    for k in range(n_pairs):
+        bodies = []
+        for _ in range(2):
+            nt = math.exp(rng.uniform(math.log(tet_range[0]), math.log(tet_range[1])))
+            E = 1e5 * math.exp(rng.uniform(math.log(0.1), math.log(10)) / 2)
+            if rng.integers(0, 2) == 0:
+                R = rng.uniform(0.03, 0.06)
+                lev = int(np.clip(round(math.log(max(nt, 8) / 8, 4)), 3, 6))
+                gid = s.add_geom(L.GEOM_SPHERE, [R, 0, 0], [E, 1.0, sphere_hint(R, lev), 0.5, 0.5])
+                bodies.append((gid, L.GEOM_SPHERE, [R, R, R], R))
+            else:
+                h = rng.uniform(0.02, 0.05, 3)
+                hint = (8 * h[0] * h[1] * h[2] * 6 / nt) ** (1 / 3)
+                gid = s.add_geom(L.GEOM_BOX, list(h), [E, 1.0, hint, 0.5, 0.5])
+                bodies.append((gid, L.GEOM_BOX, list(h), float(h.min())))
+        s.g1.append(bodies[0][0]); s.g2.append(bodies[1][0]); s.scene_of_pair.append(k)
+        place.append(bodies)
+    _alloc(s)
+    for (a, b) in place:
+        Ra, Rb = random_rotation(rng), random_rotation(rng)
+        # distance between centres along z: sum of supports minus overlap
+        def support(body, R):
+            _, t, h, _ = body
+            if t == L.GEOM_SPHERE:
+                return h[0]
+            return float(np.sum(np.abs(R[2, :]) * np.asarray(h)))
+        ov = rng.uniform(0, 0.08) * min(a[3], b[3])
+        d = support(a, Ra) + support(b, Rb) - ov
+        s.xmat[a[0]] = Ra.reshape(9)
+        s.xmat[b[0]] = Rb.reshape(9)
+        s.xpos[a[0]] = [0, 0, 0]
+        off = rng.uniform(-0.2, 0.2, 2) * min(a[3], b[3])
+        s.xpos[b[0]] = [off[0], off[1], -d]
+    return s
+
+
+def halfspace(n_pairs=8, seed=SEED_SINGLE + 500) -> Scene:
+    """Soft primitives resting on a rigid ground plane (plane geom)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene()
+    ground = s.add_geom(L.GEOM_PLANE, [0, 0, 1], [0, 1.0, 0, 0.5, 0.5])
+    place = []
+    for k in range(n_pairs):
+        st, ssize, scs, sext = _soft_primitive(rng, rng.uniform(500, 4000))
+        g = s.add_geom(st, ssize, scs)
+        s.g1.append(g); s.g2.append(ground); s.scene_of_pair.append(k)
+        place.append((g, st, ssize, sext))
+    _alloc(s)
+    for (g, st, ssize, sext) in place:
+        Rs = random_rotation(rng)
+        if st == L.GEOM_SPHERE:
+            low = ssize[0]
+        elif st == L.GEOM_ELLIPSOID:
+            low = float(np.sqrt(np.sum((Rs[2, :] * np.asarray(ssize)) ** 2)))
+        elif st == L.GEOM_BOX:
+            low = float(np.sum(np.abs(Rs[2, :]) * np.asarray(ssize)))
+        else:
+            r, hl = ssize[0], ssize[1]
+            low = float(r * math.sqrt(max(0.0, 1 - Rs[2, 2] ** 2)) + hl * abs(Rs[2, 2]))
+        s.xmat[g] = Rs.reshape(9)
+        s.xpos[g] = [rng.uniform(-1, 1), rng.uniform(-1, 1), low - rng.uniform(0, 0.1) * sext]
+        s.vel[g] = rng.uniform(-0.1, 0.1, 6)
+    return s
+
+
+def build_engine(scene: Scene, **engine_kw):
+    """An Engine holding the scene's geoms, sensors, pairs and poses."""
+    from .engine import Engine
+    eng = Engine(**engine_kw)
+    for g in scene.geoms:
+        eng.add_geom(g["id"], g["type"], g["size"], g["cs5"], g["mesh_v"], g["mesh_f"])
+    for sn in scene.sensors:
+        eng.add_flat_sensor(sn["geom"], sn["resolution"], sn["sr"], sn["window"], sn["sigma"])
+    eng.set_pairs(scene.g1, scene.g2)
+    eng.set_poses(scene.xpos, scene.xmat, scene.vel)
+    return eng

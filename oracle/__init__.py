@@ -1,0 +1,8 @@
+"""FP64 CPU oracle of the contact-surface path — test infrastructure only.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU legs import this
+package, as the checker.  Parity status: unpinned (see oracle.h).
+"""
+from .oracle import Oracle, build, load
+
+__all__ = ["Oracle", "build", "load"]
