@@ -257,6 +257,9 @@ HC_API hc_status hc_add_flat_sensor(hc_context* ctx, int geom_id, double resolut
 /* The sensor's taxel map of the last step (cx*cy floats, index x + cy*y as
  * FS:396-397).  Synchronises the context stream.                        */
 HC_API hc_status hc_get_taxels(hc_context* ctx, int sensor, float* out);
+/* All sensors' taxel maps in one host copy (sensor-major, cx*cy floats
+ * each, in hc_add_flat_sensor order).  n_floats: capacity of `out`. */
+HC_API hc_status hc_get_taxels_all(hc_context* ctx, float* out, int64_t n_floats);
 /* Device pointer to all sensors' taxel maps (sensor-major). */
 HC_API hc_status hc_get_taxels_device(hc_context* ctx, const float** d_taxels,
                                       int64_t* n_floats);

@@ -96,6 +96,7 @@ SIGNATURES = {
     "hc_get_candidates": (C.c_int, [_P, C.POINTER(hc_candidate), C.c_int64, C.POINTER(C.c_int64)]),
     "hc_add_flat_sensor": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double, _ip, _ip, _ip]),
     "hc_get_taxels": (C.c_int, [_P, C.c_int, _fp]),
+    "hc_get_taxels_all": (C.c_int, [_P, _fp, C.c_int64]),
     "hc_get_taxels_device": (C.c_int, [_P, C.POINTER(_P), C.POINTER(C.c_int64)]),
     "hc_adjoint": (C.c_int, [_P, _dp, _fp, _dp, _dp]),
     "hc_enable_timing": (C.c_int, [_P, C.c_int]),

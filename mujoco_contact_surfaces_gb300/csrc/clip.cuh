@@ -15,12 +15,18 @@
 // Faces whose normal makes an angle above 5*pi/8 with the soft pressure
 // gradient are culled (the method's back-face test).
 //
-// Precision: every sign decision is first taken in FP32 with a conservative
-// error margin.  When any FP32 value falls inside its margin the whole
-// element pair is recomputed in FP64 from the stored FP32 inputs and the
-// FP64 frames, so decisions equal an FP64 evaluation.  In FP64 a value
-// within 1e-12 (metres, or cosine units for the normal test) of its
-// threshold marks the pair near-degenerate.
+// Precision.  The section function values s_k of the four tet vertices
+// (signed distance to the triangle plane / plane, or p_A - p_B) are
+// evaluated in FP64: they set the penetration, to which area and force are
+// most sensitive.  Section vertices are interpolated from the edge endpoint
+// nearest the plane and kept in coordinates relative to the tet vertex
+// nearest the plane, so FP32 carries only the small offsets.  Clip-plane
+// distances are carried per vertex and interpolated with the positions.
+// Every FP32 sign decision has a conservative margin; when a value falls
+// inside it the element pair is recomputed in FP64 from the stored FP32
+// inputs and the FP64 frames, so decisions equal an FP64 evaluation.  In
+// FP64 a value within 1e-12 (metres, or cosine units for the normal test)
+// of its threshold marks the pair near-degenerate.
 #pragma once
 #include "geom_math.cuh"
 #include "hc_internal.h"
@@ -28,33 +34,35 @@
 namespace hc {
 
 constexpr float kFilt = 3.0e-6f;            // FP32 margin factor (~50 ulp)
+constexpr float kFiltRel = 1.0e-6f;         // margin of interpolated values
 constexpr double kNearTol = 1.0e-12;        // near-degenerate threshold
-constexpr float kCosAlphaF = -0.38268343236508978f;   // cos(5*pi/8)
-constexpr double kCosAlphaD = -0.38268343236508978;
+constexpr double kCosAlphaD = -0.38268343236508978;   // cos(5*pi/8)
 
-// Polygon vertex: position, pressure, and a bound on its position error
-// (metres; FP32 pass only).
-template <class R>
-struct PVx {
-  R x, y, z, p, e;
+// Polygon vertex: position (relative to an anchor), pressure and the
+// distances to up to ND clip planes.
+template <class R, int ND>
+struct PV {
+  R x, y, z, p;
+  R d[ND];
 };
 
-template <class R>
-__device__ __forceinline__ PVx<R> pv_lerp(const PVx<R>& a, const PVx<R>& b, R t) {
-  PVx<R> o;
+template <class R, int ND>
+__device__ __forceinline__ PV<R, ND> pv_lerp(const PV<R, ND>& a, const PV<R, ND>& b, R t) {
+  PV<R, ND> o;
   o.x = a.x + t * (b.x - a.x);
   o.y = a.y + t * (b.y - a.y);
   o.z = a.z + t * (b.z - a.z);
   o.p = a.p + t * (b.p - a.p);
-  o.e = a.e > b.e ? a.e : b.e;
+#pragma unroll
+  for (int j = 0; j < ND; ++j) o.d[j] = a.d[j] + t * (b.d[j] - a.d[j]);
   return o;
 }
 
-template <class R>
-__device__ __forceinline__ V3<R> pv_pos(const PVx<R>& a) { return mk(a.x, a.y, a.z); }
+template <class R, int ND>
+__device__ __forceinline__ V3<R> pv_pos(const PV<R, ND>& a) { return mk(a.x, a.y, a.z); }
 
-// Uncertainty bookkeeping: FP32 passes set `unc` when a decision is inside
-// its margin; FP64 passes set `near` when a value is within kNearTol.
+// FP32 passes set `unc` when a decision is inside its margin; FP64 passes
+// set `near` when a value is within kNearTol.
 struct Decide {
   bool unc = false;
   bool near = false;
@@ -69,32 +77,33 @@ __device__ __forceinline__ void check(Decide& dc, R v, R tol) {
   }
 }
 
-// Section of tet (vertices tv[0..3], values s[0..3]) by s = 0.  Output is a
-// triangle or quad in cyclic order (marching-tetrahedron pattern).
-// tol_s: margin of the s values (FP32 only).
-template <class R>
-__device__ __forceinline__ int tet_section(const PVx<R> tv[4], const R s[4], R tol_s, Decide& dc,
-                                           PVx<R> out[kMaxPolyV]) {
+// Section of a tet by s = 0 (s given in FP64 for the four vertices).
+// Output: triangle or quad in cyclic order (marching-tetrahedron pattern),
+// each vertex interpolated from the endpoint with the smaller |s|.
+template <class R, int ND>
+__device__ __forceinline__ int tet_section(const PV<R, ND> tv[4], const double s[4], Decide& dc, PV<R, ND> out[4]) {
   int pos = 0;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    check(dc, s[k], tol_s);
-    pos |= (s[k] > (R)0) << k;
+    if (fabs(s[k]) < kNearTol) {
+      if (sizeof(R) == 4) dc.unc = true;
+      else dc.near = true;
+    }
+    pos |= (s[k] > 0.0) << k;
   }
-  int np = __popc(pos);
+  const int np = __popc(pos);
   if (np == 0 || np == 4) return 0;
   int ea[4], eb[4], n;
   if (np == 1 || np == 3) {
-    int single = np == 1 ? __ffs(pos) - 1 : __ffs(~pos & 0xF) - 1;
+    const int single = np == 1 ? __ffs(pos) - 1 : __ffs(~pos & 0xF) - 1;
     n = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k)
       if (k != single) { ea[n] = single; eb[n] = k; ++n; }
-    n = 3;
   } else {
-    int a = __ffs(pos) - 1, b = __ffs(pos & ~(1 << a)) - 1;
-    int neg = ~pos & 0xF;
-    int c = __ffs(neg) - 1, d = __ffs(neg & ~(1 << c)) - 1;
+    const int a = __ffs(pos) - 1, b = __ffs(pos & ~(1 << a)) - 1;
+    const int neg = ~pos & 0xF;
+    const int c = __ffs(neg) - 1, d = __ffs(neg & ~(1 << c)) - 1;
     ea[0] = a; eb[0] = c;
     ea[1] = a; eb[1] = d;
     ea[2] = b; eb[2] = d;
@@ -104,31 +113,23 @@ __device__ __forceinline__ int tet_section(const PVx<R> tv[4], const R s[4], R t
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     if (i < n) {
-      const int a = ea[i], b = eb[i];
-      R sa = s[a], sb = s[b];
-      R t = sa / (sa - sb);
-      out[i] = pv_lerp(tv[a], tv[b], t);
-      if (sizeof(R) == 4) {
-        V3<R> d = pv_pos(tv[b]) - pv_pos(tv[a]);
-        out[i].e = amax(d) * ((R)2 * tol_s / abs_r(sa - sb) + (R)4e-7) + (tv[a].e > tv[b].e ? tv[a].e : tv[b].e);
-      }
+      int a = ea[i], b = eb[i];
+      if (fabs(s[a]) > fabs(s[b])) { int t = a; a = b; b = t; }
+      const R sa = (R)s[a], sb = (R)s[b];
+      out[i] = pv_lerp(tv[a], tv[b], sa / (sa - sb));
     }
   }
   return n;
 }
 
-// Sutherland-Hodgman clip of a convex polygon by n.x - o >= 0.
-// tol_p: margin of the plane evaluation itself (FP32 only).
-template <class R>
-__device__ __forceinline__ int clip_plane(const PVx<R>* in, int n, V3<R> pn, R po, R tol_p, Decide& dc,
-                                          PVx<R>* out) {
-  R d[kMaxPolyV];
+// Sutherland-Hodgman clip of a convex polygon by d_j >= 0 (carried
+// distances).  tol: FP32 margin of the plane distances.
+template <class R, int ND>
+__device__ __forceinline__ int clip_dist(const PV<R, ND>* in, int n, int j, R tol, Decide& dc, PV<R, ND>* out) {
   bool all_in = true;
   for (int i = 0; i < n; ++i) {
-    d[i] = dot(pn, pv_pos(in[i])) - po;
-    R tol = tol_p + (R)2 * in[i].e;
-    check(dc, d[i], tol);
-    all_in &= d[i] >= (R)0;
+    check(dc, in[i].d[j], tol);
+    all_in &= in[i].d[j] >= (R)0;
   }
   if (all_in) {
     for (int i = 0; i < n; ++i) out[i] = in[i];
@@ -136,24 +137,18 @@ __device__ __forceinline__ int clip_plane(const PVx<R>* in, int n, V3<R> pn, R p
   }
   int m = 0;
   for (int i = 0; i < n; ++i) {
-    int j = i + 1 == n ? 0 : i + 1;
-    bool ii = d[i] >= (R)0, ij = d[j] >= (R)0;
+    const int k = i + 1 == n ? 0 : i + 1;
+    const R di = in[i].d[j], dk = in[k].d[j];
+    const bool ii = di >= (R)0, ik = dk >= (R)0;
     if (ii && m < kMaxPolyV) out[m++] = in[i];
-    if (ii != ij && m < kMaxPolyV) {
-      R t = d[i] / (d[i] - d[j]);
-      PVx<R> v = pv_lerp(in[i], in[j], t);
-      if (sizeof(R) == 4) {
-        V3<R> dd = pv_pos(in[j]) - pv_pos(in[i]);
-        R ti = tol_p + (R)2 * in[i].e, tj = tol_p + (R)2 * in[j].e;
-        v.e = (in[i].e > in[j].e ? in[i].e : in[j].e) + amax(dd) * ((ti + tj) / abs_r(d[i] - d[j]) + (R)4e-7);
-      }
-      out[m++] = v;
+    if (ii != ik && m < kMaxPolyV) {
+      out[m++] = abs_r(di) <= abs_r(dk) ? pv_lerp(in[i], in[k], di / (di - dk)) : pv_lerp(in[k], in[i], dk / (dk - di));
     }
   }
   return m;
 }
 
-// Linear field of a tet from its vertex values: p(x) = g.x + c.  Also the
+// Linear field of a tet from its vertex values: p(x) = g.x + c; also the
 // tet's minimum height (for conditioning-based margins).
 template <class R>
 __device__ __forceinline__ void tet_field(const V3<R> X[4], const R P[4], V3<R>& g, R& c, R& hmin) {
@@ -170,7 +165,6 @@ __device__ __forceinline__ void tet_field(const V3<R> X[4], const R P[4], V3<R>&
   R inv = (R)1 / det;
   g = (c23 * d1 + c31 * d2 + c12 * d3) * inv;
   c = P[0] - dot(g, X[0]);
-  // face areas*2: |c23| (face opposite 0), |c31|, |c12|, |(e2-e1)x(e3-e1)|
   V3<R> f0 = cross(e2 - e1, e3 - e1);
   R amax_ = norm(c23);
   R t1 = norm(c31), t2 = norm(c12), t3 = norm(f0);
@@ -195,6 +189,11 @@ __device__ __forceinline__ void tet_planes(const V3<R> X[4], V3<R> n[4], R o[4])
     n[k] = nn;
     o[k] = dot(nn, X[i0]);
   }
+}
+
+// FP64 signed value n.x - o of a float point.
+__device__ __forceinline__ double plane64(const double* n, double o, float x, float y, float z) {
+  return fma(n[2], (double)z, fma(n[1], (double)y, n[0] * (double)x)) - o;
 }
 
 }  // namespace hc

@@ -310,623 +310,7 @@ __global__ void bp_emit_kernel(StepArgs a) {
   });
 }
 
-// ---------------------------------------------------------------------------
-// narrow phase
-// ---------------------------------------------------------------------------
-struct Acc {
-  float F[3], T[3], area, fn0;
-  int n_poly, n_faces, n_near;
-};
-
-struct PairCtx {
-  const PairDev* P;
-  const FrameDev* F;
-  int pair;
-};
-
-// One quadrature point (mujoco_contact_surfaces_plugin.cpp:345-404) and the
-// force law in the soft frame.
-__device__ __forceinline__ void point_force(Acc& ac, const FrameDev& F, float damping, float mu, int apply, float A,
-                                            V3<float> p, V3<float> n, float gM, float gN, float p0) {
-  if (!(A > 1.0e-14f)) return;
-  if (gM < 1.0e-14f || gN < 1.0e-14f) return;
-  float g = 1.0f / (1.0f / gM + 1.0f / gN);
-  float fn0 = A * p0;
-  float k = A * g;
-  ac.area += A;
-  ac.fn0 += fn0;
-  ac.n_faces += 1;
-  V3<float> lin = mk(F.lin[0], F.lin[1], F.lin[2]), ang = mk(F.ang[0], F.ang[1], F.ang[2]);
-  V3<float> v = lin + cross(ang, p);
-  float vn = dot(v, n);
-  float fn = fmaxf(0.f, 1.f - damping * vn) * (fn0 - 0.001f * k * vn);
-  if (!apply) return;
-  V3<float> vt = v - n * vn;
-  const float eps = (1.0e-4f * 1.0e-2f) * (1.0e-4f * 1.0e-2f);
-  float v_slip = sqrtf(dot(vt, vt) + eps);
-  float s = v_slip / 1.0e-4f;
-  float mu_reg = s < 1.f ? mu * s * (2.f - s) : mu;
-  V3<float> f = vt * (-mu_reg * fn / v_slip) + n * fn;
-  V3<float> tq = cross(p, f);
-  ac.F[0] += f.x; ac.F[1] += f.y; ac.F[2] += f.z;
-  ac.T[0] += tq.x; ac.T[1] += tq.y; ac.T[2] += tq.z;
-}
-
-// Ray hits of one fan triangle (soft frame) on a sensor's sample grid: the
-// sensor's rays are parallel to its -z axis, start 1.5*zs above its centre
-// (+1e-8) and accept 0 < t < 1.5*zs (flat_tactile_sensor.cpp:324-346); the
-// triangle test follows the Moeller-Trumbore acceptance rules of
-// bvh.cpp:49-74 in the sensor frame.  Each sample keeps the smallest t,
-// packed with the pressure at the hit, by a 64-bit atomicMin.
-__device__ void raster_tri(const StepArgs& a, int sid, const float* Rl, const float* tl, V3<float> A, V3<float> B,
-                           V3<float> C, float pa, float pb, float pc) {
-  const SensorDev S = a.sensors[sid];
-  V3<float> la = mat_mul<float>(Rl, A) + mk(tl[0], tl[1], tl[2]);
-  V3<float> lb = mat_mul<float>(Rl, B) + mk(tl[0], tl[1], tl[2]);
-  V3<float> lc = mat_mul<float>(Rl, C) + mk(tl[0], tl[1], tl[2]);
-  float e1x = lb.x - la.x, e1y = lb.y - la.y, e2x = lc.x - la.x, e2y = lc.y - la.y;
-  float det = e1x * e2y - e1y * e2x;
-  if (fabsf(det) < 1e-10f) return;
-  const float* sx = a.samp_coord + S.samp_off_x;
-  const float* sy = a.samp_coord + S.samp_off_y;
-  float x0 = sx[0], dx = S.nx > 1 ? sx[1] - sx[0] : 1.f;
-  float y0 = sy[0], dy = S.ny > 1 ? sy[1] - sy[0] : 1.f;
-  float mnx = fminf(la.x, fminf(lb.x, lc.x)), mxx = fmaxf(la.x, fmaxf(lb.x, lc.x));
-  float mny = fminf(la.y, fminf(lb.y, lc.y)), mxy = fmaxf(la.y, fmaxf(lb.y, lc.y));
-  int X0 = max(0, (int)floorf((mnx - x0) / dx) - 1), X1 = min(S.nx - 1, (int)ceilf((mxx - x0) / dx) + 1);
-  int Y0 = max(0, (int)floorf((mny - y0) / dy) - 1), Y1 = min(S.ny - 1, (int)ceilf((mxy - y0) / dy) + 1);
-  if (X0 > X1 || Y0 > Y1) return;
-  float inv = 1.f / det;
-  unsigned long long* smp = a.samples + S.sample_off;
-  for (int X = X0; X <= X1; ++X) {
-    float wx = sx[X] - la.x;
-    for (int Y = Y0; Y <= Y1; ++Y) {
-      float wy = sy[Y] - la.y;
-      float u = (wx * e2y - wy * e2x) * inv;
-      if (u < 0.f || u > 1.f) continue;
-      float v = (e1x * wy - e1y * wx) * inv;
-      if (v < 0.f || u + v > 1.f) continue;
-      float z = la.z + u * (lb.z - la.z) + v * (lc.z - la.z);
-      float t = (S.zs15 + 1e-8f) - z;
-      if (!(t > 0.f && t < S.zs15)) continue;
-      float pr = (1.f - u - v) * pa + u * pb + v * pc;
-      unsigned long long key =
-          ((unsigned long long)__float_as_uint(t) << 32) | (unsigned long long)__float_as_uint(pr);
-      atomicMin(&smp[(size_t)X * S.ny + Y], key);
-    }
-  }
-}
-
-// Quadrature of one polygon (float, soft frame) and its contribution to the
-// forces and to the sensors.  n: contact normal out of N into M.
-__device__ void integrate_polygon(const StepArgs& a, const PairCtx& pc, Acc& ac, const PVx<float>* v, int nv,
-                                  V3<float> n, float gM, float gN) {
-  const FrameDev& F = *pc.F;
-  const PairDev& P = *pc.P;
-  // area-weighted centroid by a fan from vertex 0
-  float A = 0.f, pcen = 0.f;
-  V3<float> c = mk(0.f, 0.f, 0.f);
-  V3<float> v0 = pv_pos(v[0]);
-  for (int i = 1; i + 1 < nv; ++i) {
-    V3<float> vi = pv_pos(v[i]), vj = pv_pos(v[i + 1]);
-    float ai = 0.5f * dot(cross(vi - v0, vj - v0), n);
-    A += ai;
-    c = c + (v0 + vi + vj) * (ai * (1.f / 3.f));
-    pcen += ai * (v[0].p + v[i].p + v[i + 1].p) * (1.f / 3.f);
-  }
-  if (A != 0.f) {
-    c = c * (1.f / A);
-    pcen /= A;
-  } else {
-    c = mk(0.f, 0.f, 0.f);
-    pcen = 0.f;
-    for (int i = 0; i < nv; ++i) {
-      c = c + pv_pos(v[i]) * (1.f / nv);
-      pcen += v[i].p / nv;
-    }
-  }
-  if (a.repr == 1) {
-    point_force(ac, F, P.damping, P.mu, a.apply_forces, fabsf(A), c, n, gM, gN, pcen);
-  } else {
-    for (int i = 0; i < nv; ++i) {
-      int j = i + 1 == nv ? 0 : i + 1;
-      V3<float> vi = pv_pos(v[i]), vj = pv_pos(v[j]);
-      float Ai = 0.5f * norm(cross(vi - c, vj - c));
-      V3<float> cen = (c + vi + vj) * (1.f / 3.f);
-      float p0 = pcen / 3.f + v[i].p / 3.f + v[j].p / 3.f;
-      point_force(ac, F, P.damping, P.mu, a.apply_forces, Ai, cen, n, gM, gN, p0);
-    }
-  }
-  for (int q = 0; q < 2; ++q) {
-    int sid = q == 0 ? P.sensor0 : P.sensor1;
-    if (sid < 0) continue;
-    const float* Rl = q == 0 ? F.Rl : F.Rl1;
-    const float* tl = q == 0 ? F.tl : F.tl1;
-    for (int i = 0; i < nv; ++i) {
-      int j = i + 1 == nv ? 0 : i + 1;
-      raster_tri(a, sid, Rl, tl, pv_pos(v[i]), pv_pos(v[j]), c, v[i].p, v[j].p, pcen);
-    }
-  }
-}
-
-__device__ void record(const StepArgs& a, const PairCtx& pc, const PVx<float>* v, int nv, V3<float> n, int ea,
-                       int eb, int flags) {
-  if (a.debug & 1) {
-    int k = atomicAdd(a.cand_count, 1);
-    if (k < a.cand_cap) {
-      CandRec r;
-      r.pair = pc.pair; r.elem_a = ea; r.elem_b = eb; r.n_vert = nv; r.flags = flags;
-      a.cand[k] = r;
-    } else {
-      atomicOr(a.status, 2);
-    }
-  }
-  if (a.want_polys && (a.want_pair < 0 || a.want_pair == pc.pair)) {
-    int k = atomicAdd(a.poly_count, 1);
-    if (k < a.poly_cap) {
-      PolyRec& r = a.polys[k];
-      r.pair = pc.pair; r.elem_a = ea; r.elem_b = eb; r.nv = nv;
-      r.n[0] = n.x; r.n[1] = n.y; r.n[2] = n.z; r.n[3] = 0.f;
-      for (int i = 0; i < kMaxPolyV; ++i) {
-        bool in = i < nv;
-        r.v[i][0] = in ? v[i].x : 0.f;
-        r.v[i][1] = in ? v[i].y : 0.f;
-        r.v[i][2] = in ? v[i].z : 0.f;
-        r.v[i][3] = in ? v[i].p : 0.f;
-      }
-    } else {
-      atomicOr(a.status, 4);
-    }
-  }
-}
-
-// --- soft-rigid element pair ------------------------------------------------
-struct TriData {
-  float Y[3][3];     // vertices, soft frame
-  float n[3];        // unit normal (out of the rigid body)
-  float o;           // n . Y0
-  float en[3][3];    // in-plane inward edge normals
-  float eo[3];
-  float lo[3], hi[3];
-  float M, h, Lt;    // magnitude, min altitude, max edge
-  int orig;
-  int valid;
-};
-
-template <class R>
-struct TetIn {
-  V3<R> X[4];
-  R P[4];
-  V3<R> g;
-  R c, gl, hmin, kappa, xmax, pmax;
-};
-
-template <class R>
-__device__ __forceinline__ void tet_prepare(TetIn<R>& t) {
-  tet_field(t.X, t.P, t.g, t.c, t.hmin);
-  t.gl = norm(t.g);
-  R lmax = 0, xm = 0, pm = 0;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    xm = fmax(xm, amax(t.X[i]));
-    pm = fmax(pm, abs_r(t.P[i]));
-#pragma unroll
-    for (int j = i + 1; j < 4; ++j) lmax = fmax(lmax, norm(t.X[j] - t.X[i]));
-  }
-  t.xmax = xm;
-  t.pmax = pm;
-  t.kappa = t.hmin > (R)0 ? lmax / t.hmin : (R)1e30;
-}
-
-// Soft-rigid polygon of tet `t` and triangle (Y, n, o, en, eo).
-// Returns vertex count (0 when empty or culled).
-template <class R>
-__device__ int sr_polygon(const TetIn<R>& t, const V3<R> Y[3], V3<R> n, R o, const V3<R> en[3], const R eo[3], R M,
-                          R h, R Lt, Decide& dc, PVx<R>* out, PVx<R>* tmp) {
-  if (!(t.gl > (R)0)) return 0;
-  R cg = dot(n, t.g) / t.gl;
-  R tol_c = (R)kFilt * ((R)1 + M / h + t.kappa);
-  check(dc, cg - (R)kCosAlphaD, tol_c);
-  if (!dc.unc && !(cg > (R)kCosAlphaD)) return 0;
-  R D = 0;
-  R s[4];
-  PVx<R> tv[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    s[k] = dot(n, t.X[k]) - o;
-    D = fmax(D, amax(t.X[k] - Y[0]));
-    tv[k].x = t.X[k].x; tv[k].y = t.X[k].y; tv[k].z = t.X[k].z; tv[k].p = t.P[k]; tv[k].e = 0;
-  }
-  R tol_s = (R)kFilt * (M * ((R)1 + D / h) + D);
-  int nv = tet_section(tv, s, tol_s, dc, out);
-  if (nv == 0) return 0;
-  R tol_p = (R)kFilt * (M * ((R)1 + (D + Lt) / h) + D + Lt);
-  PVx<R>* src = out;
-  PVx<R>* dst = tmp;
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    nv = clip_plane(src, nv, en[j], eo[j], tol_p, dc, dst);
-    PVx<R>* sw = src; src = dst; dst = sw;
-    if (nv == 0) return 0;
-  }
-  if (src != out)
-    for (int i = 0; i < nv; ++i) out[i] = src[i];
-  return nv;
-}
-
-template <class R>
-__device__ __forceinline__ void tri_prepare(const V3<R> Yin[3], V3<R> Y[3], V3<R>& n, R& o, V3<R> en[3], R eo[3],
-                                            R& h, R& Lt, bool& valid) {
-  for (int k = 0; k < 3; ++k) Y[k] = Yin[k];
-  V3<R> N = cross(Y[1] - Y[0], Y[2] - Y[0]);
-  R ln = norm(N);
-  valid = ln > (R)0;
-  n = valid ? N * ((R)1 / ln) : mk<R>(0, 0, 1);
-  o = dot(n, Y[0]);
-  R le = 0;
-  for (int j = 0; j < 3; ++j) {
-    V3<R> e = Y[j == 2 ? 0 : j + 1] - Y[j];
-    le = fmax(le, norm(e));
-    V3<R> m = cross(n, e);
-    R lm = norm(m);
-    en[j] = lm > (R)0 ? m * ((R)1 / lm) : m;
-    eo[j] = dot(en[j], Y[j]);
-  }
-  Lt = le;
-  h = le > (R)0 ? ln / le : (R)0;
-}
-
-// --- half-space element --------------------------------------------------------
-template <class R>
-__device__ int hs_polygon(const TetIn<R>& t, V3<R> n, R o, Decide& dc, PVx<R>* out) {
-  if (!(t.gl > (R)0)) return 0;
-  R cg = dot(n, t.g) / t.gl;
-  R tol_c = (R)kFilt * ((R)1 + t.kappa);
-  check(dc, cg - (R)kCosAlphaD, tol_c);
-  if (!dc.unc && !(cg > (R)kCosAlphaD)) return 0;
-  R s[4];
-  PVx<R> tv[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    s[k] = dot(n, t.X[k]) - o;
-    tv[k].x = t.X[k].x; tv[k].y = t.X[k].y; tv[k].z = t.X[k].z; tv[k].p = t.P[k]; tv[k].e = 0;
-  }
-  R tol_s = (R)kFilt * (t.xmax + abs_r(o));
-  return tet_section(tv, s, tol_s, dc, out);
-}
-
-// --- soft-soft element pair -----------------------------------------------------
-struct TetB {
-  float Y[4][3];
-  float P[4];
-  float g[3], c, gl;
-  float pn[4][3], po[4];
-  float lo[3], hi[3];
-  float M, h, kappa;
-  int orig;
-  int valid;
-};
-
-template <class R>
-__device__ int ss_polygon(const TetIn<R>& ta, V3<R> gb, R cb, R glb, const V3<R> pn[4], const R po[4], R Mb, R hb,
-                          R kb, Decide& dc, PVx<R>* out, PVx<R>* tmp, V3<R>& nrm) {
-  V3<R> m = ta.g - gb;
-  R lm = norm(m);
-  if (!(lm > (R)0) || !(ta.gl > (R)0) || !(glb > (R)0)) return 0;
-  nrm = m * ((R)1 / lm);
-  R cond = (((R)1 + ta.kappa) * ta.gl + ((R)1 + kb + Mb / hb) * glb) / lm;
-  R tol_c = (R)kFilt * cond;
-  R ca = dot(nrm, ta.g) / ta.gl;
-  R cbb = -dot(nrm, gb) / glb;
-  check(dc, ca - (R)kCosAlphaD, tol_c);
-  check(dc, cbb - (R)kCosAlphaD, tol_c);
-  if (!dc.unc && !(ca > (R)kCosAlphaD && cbb > (R)kCosAlphaD)) return 0;
-  R s[4];
-  PVx<R> tv[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    s[k] = (ta.P[k] - (dot(gb, ta.X[k]) + cb)) / lm;
-    tv[k].x = ta.X[k].x; tv[k].y = ta.X[k].y; tv[k].z = ta.X[k].z; tv[k].p = ta.P[k]; tv[k].e = 0;
-  }
-  R tol_s = (R)kFilt * (ta.pmax + glb * (ta.xmax + Mb) * ((R)1 + Mb / hb) + abs_r(cb)) / lm;
-  int nv = tet_section(tv, s, tol_s, dc, out);
-  if (nv == 0) return 0;
-  R D = ta.xmax + Mb;
-  R tol_p = (R)kFilt * (Mb * ((R)1 + D / hb) + D);
-  PVx<R>* src = out;
-  PVx<R>* dst = tmp;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    nv = clip_plane(src, nv, pn[j], po[j], tol_p, dc, dst);
-    PVx<R>* sw = src; src = dst; dst = sw;
-    if (nv == 0) return 0;
-  }
-  if (src != out)
-    for (int i = 0; i < nv; ++i) out[i] = src[i];
-  return nv;
-}
-
-__device__ __forceinline__ bool aabb_overlap(const float* alo, const float* ahi, const float* blo, const float* bhi) {
-  return alo[0] <= bhi[0] && ahi[0] >= blo[0] && alo[1] <= bhi[1] && ahi[1] >= blo[1] && alo[2] <= bhi[2] &&
-         ahi[2] >= blo[2];
-}
-
-template <class R>
-__device__ __forceinline__ void load_tet(const float4* tets, int idx, TetIn<R>& t) {
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    float4 v = tets[4 * (size_t)idx + k];
-    t.X[k] = mk<R>(v.x, v.y, v.z);
-    t.P[k] = v.w;
-  }
-}
-
-template <class R>
-__device__ __forceinline__ PVx<float> to_f(const PVx<R>& v) {
-  PVx<float> o;
-  o.x = (float)v.x; o.y = (float)v.y; o.z = (float)v.z; o.p = (float)v.p; o.e = 0.f;
-  return o;
-}
-
-constexpr int kNarrowWarps = 4;
-
-__global__ void __launch_bounds__(128) narrow_kernel(StepArgs a) {
-  __shared__ union Stage {
-    TriData tri[kCluster];
-    TetB tetb[kCluster];
-  } s_stage[kNarrowWarps];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int n_items = *a.item_total;
-  while (true) {
-    int item = 0;
-    if (lane == 0) item = atomicAdd(a.item_next, 1);
-    item = __shfl_sync(0xffffffffu, item, 0);
-    if (item >= n_items) break;
-    const int4 it = a.items[item];
-    PairCtx pc;
-    pc.pair = it.x;
-    pc.P = &a.pairs[it.x];
-    pc.F = &a.frames[it.x];
-    const PairDev& P = *pc.P;
-    const FrameDev& F = *pc.F;
-    Acc ac;
-    for (int i = 0; i < 3; ++i) ac.F[i] = ac.T[i] = 0.f;
-    ac.area = ac.fn0 = 0.f;
-    ac.n_poly = ac.n_faces = ac.n_near = 0;
-    const int sl = it.y, oc = it.z;
-    const int ti = sl * kCluster + lane;
-    const bool tvalid = ti < P.s_n_elem;
-    TetIn<float> t;
-    float tlo[3], thi[3];
-    if (tvalid) {
-      load_tet(a.tets, P.s_elem_off + ti, t);
-      tet_prepare(t);
-      for (int i = 0; i < 3; ++i) {
-        float lo = fminf(fminf((&t.X[0].x)[i], (&t.X[1].x)[i]), fminf((&t.X[2].x)[i], (&t.X[3].x)[i]));
-        float hi = fmaxf(fmaxf((&t.X[0].x)[i], (&t.X[1].x)[i]), fmaxf((&t.X[2].x)[i], (&t.X[3].x)[i]));
-        float pad = 1e-5f * (fabsf(lo) + fabsf(hi)) + 1e-7f;
-        tlo[i] = lo - pad;
-        thi[i] = hi + pad;
-      }
-    }
-    const int torig = tvalid ? a.tet_orig[P.s_elem_off + ti] : -1;
-    const float sgn = P.s_is_m ? 1.f : -1.f;
-    PVx<float> poly[kMaxPolyV], tmp[kMaxPolyV];
-    if (P.query == 1) {
-      // ---- stage the rigid triangles of cluster oc (soft frame) ----
-      const int tj = oc * kCluster + lane;
-      TriData& S = s_stage[wid].tri[lane];
-      S.valid = 0;
-      if (tj < P.o_n_elem && F.valid) {
-        V3<float> Yin[3], Y[3], n, en[3];
-        float o, eo[3], h, Lt, M = 0.f;
-        bool ok;
-        for (int k = 0; k < 3; ++k) {
-          float4 r = a.tris[3 * (size_t)(P.o_elem_off + tj) + k];
-          V3<float> rv = mk(r.x, r.y, r.z);
-          M = fmaxf(M, amax(rv));
-          Yin[k] = mat_mul<float>(F.Rf, rv) + mk(F.tf[0], F.tf[1], F.tf[2]);
-        }
-        M = fmaxf(M, fmaxf(fabsf(F.tf[0]), fmaxf(fabsf(F.tf[1]), fabsf(F.tf[2]))));
-        tri_prepare(Yin, Y, n, o, en, eo, h, Lt, ok);
-        for (int k = 0; k < 3; ++k) {
-          S.Y[k][0] = Y[k].x; S.Y[k][1] = Y[k].y; S.Y[k][2] = Y[k].z;
-          S.en[k][0] = en[k].x; S.en[k][1] = en[k].y; S.en[k][2] = en[k].z;
-          S.eo[k] = eo[k];
-        }
-        S.n[0] = n.x; S.n[1] = n.y; S.n[2] = n.z; S.o = o;
-        for (int i = 0; i < 3; ++i) {
-          float lo = fminf(fminf((&Y[0].x)[i], (&Y[1].x)[i]), (&Y[2].x)[i]);
-          float hi = fmaxf(fmaxf((&Y[0].x)[i], (&Y[1].x)[i]), (&Y[2].x)[i]);
-          float pad = 1e-5f * (M + Lt) + 1e-7f;
-          S.lo[i] = lo - pad;
-          S.hi[i] = hi + pad;
-        }
-        S.M = M; S.h = h; S.Lt = Lt;
-        S.orig = a.tri_orig[P.o_elem_off + tj];
-        S.valid = ok && h > 0.f ? 1 : 0;
-      }
-      __syncwarp();
-      const int n_o = min(kCluster, P.o_n_elem - oc * kCluster);
-      for (int j = 0; j < n_o; ++j) {
-        const TriData& T = s_stage[wid].tri[j];
-        if (!tvalid || !T.valid || !aabb_overlap(tlo, thi, T.lo, T.hi)) continue;
-        V3<float> Y[3] = {mk(T.Y[0][0], T.Y[0][1], T.Y[0][2]), mk(T.Y[1][0], T.Y[1][1], T.Y[1][2]),
-                          mk(T.Y[2][0], T.Y[2][1], T.Y[2][2])};
-        V3<float> en[3] = {mk(T.en[0][0], T.en[0][1], T.en[0][2]), mk(T.en[1][0], T.en[1][1], T.en[1][2]),
-                           mk(T.en[2][0], T.en[2][1], T.en[2][2])};
-        V3<float> n = mk(T.n[0], T.n[1], T.n[2]);
-        float M = fmaxf(T.M, t.xmax);
-        Decide dc;
-        int nv = sr_polygon<float>(t, Y, n, T.o, en, T.eo, M, T.h, T.Lt, dc, poly, tmp);
-        float gint = dot(t.g, n);
-        int flags = 0;
-        if (dc.unc) {
-          // exact-decision fallback in FP64 from the stored inputs
-          TetIn<double> td;
-          load_tet(a.tets, P.s_elem_off + ti, td);
-          tet_prepare(td);
-          V3<double> Yd[3], Ydp[3], nd, end[3];
-          double od, eod[3], hd, Ltd;
-          bool okd;
-          for (int k = 0; k < 3; ++k) {
-            float4 r = a.tris[3 * (size_t)(P.o_elem_off + oc * kCluster + j) + k];
-            Yd[k] = mat_mul<double>(F.R, mk<double>(r.x, r.y, r.z)) + mk(F.t[0], F.t[1], F.t[2]);
-          }
-          tri_prepare(Yd, Ydp, nd, od, end, eod, hd, Ltd, okd);
-          Decide dd;
-          PVx<double> pd[kMaxPolyV], td2[kMaxPolyV];
-          nv = okd ? sr_polygon<double>(td, Ydp, nd, od, end, eod, 0.0, 1.0, 0.0, dd, pd, td2) : 0;
-          for (int i = 0; i < nv; ++i) poly[i] = to_f(pd[i]);
-          if (dd.near) flags |= 1;
-          gint = (float)dot(td.g, nd);
-        }
-        if (nv >= 3) {
-          V3<float> nc = n * sgn;
-          float gM = P.s_is_m ? gint : INFINITY;
-          float gN = P.s_is_m ? INFINITY : gint;
-          ac.n_poly += 1;
-          ac.n_near += flags & 1;
-          integrate_polygon(a, pc, ac, poly, nv, nc, gM, gN);
-          record(a, pc, poly, nv, nc, torig, T.orig, flags);
-        }
-      }
-      __syncwarp();
-    } else if (P.query == 2) {
-      if (tvalid && F.valid) {
-        V3<float> n = mk(F.Rf[2], F.Rf[5], F.Rf[8]);
-        float o = (float)(F.R[2] * F.t[0] + F.R[5] * F.t[1] + F.R[8] * F.t[2]);
-        Decide dc;
-        int nv = hs_polygon<float>(t, n, o, dc, poly);
-        float gint = dot(t.g, n);
-        int flags = 0;
-        if (dc.unc) {
-          TetIn<double> td;
-          load_tet(a.tets, P.s_elem_off + ti, td);
-          tet_prepare(td);
-          V3<double> nd = mk(F.R[2], F.R[5], F.R[8]);
-          double od = F.R[2] * F.t[0] + F.R[5] * F.t[1] + F.R[8] * F.t[2];
-          Decide dd;
-          PVx<double> pd[kMaxPolyV];
-          nv = hs_polygon<double>(td, nd, od, dd, pd);
-          for (int i = 0; i < nv; ++i) poly[i] = to_f(pd[i]);
-          if (dd.near) flags |= 1;
-          gint = (float)dot(td.g, nd);
-        }
-        if (nv >= 3) {
-          V3<float> nc = n * sgn;
-          float gM = P.s_is_m ? gint : INFINITY;
-          float gN = P.s_is_m ? INFINITY : gint;
-          ac.n_poly += 1;
-          ac.n_near += flags & 1;
-          integrate_polygon(a, pc, ac, poly, nv, nc, gM, gN);
-          record(a, pc, poly, nv, nc, torig, -1, flags);
-        }
-      }
-    } else if (P.query == 3) {
-      // ---- stage the B tets of cluster oc in A's (soft) frame ----
-      const int tj = oc * kCluster + lane;
-      TetB& S = s_stage[wid].tetb[lane];
-      S.valid = 0;
-      if (tj < P.o_n_elem && F.valid) {
-        TetIn<float> tb;
-        float M = 0.f;
-        for (int k = 0; k < 4; ++k) {
-          float4 r = a.tets[4 * (size_t)(P.o_elem_off + tj) + k];
-          V3<float> rv = mk(r.x, r.y, r.z);
-          M = fmaxf(M, amax(rv));
-          tb.X[k] = mat_mul<float>(F.Rf, rv) + mk(F.tf[0], F.tf[1], F.tf[2]);
-          tb.P[k] = r.w;
-        }
-        M = fmaxf(M, fmaxf(fabsf(F.tf[0]), fmaxf(fabsf(F.tf[1]), fabsf(F.tf[2]))));
-        tet_prepare(tb);
-        V3<float> pn[4];
-        float po[4];
-        tet_planes(tb.X, pn, po);
-        for (int k = 0; k < 4; ++k) {
-          S.Y[k][0] = tb.X[k].x; S.Y[k][1] = tb.X[k].y; S.Y[k][2] = tb.X[k].z;
-          S.P[k] = tb.P[k];
-          S.pn[k][0] = pn[k].x; S.pn[k][1] = pn[k].y; S.pn[k][2] = pn[k].z;
-          S.po[k] = po[k];
-        }
-        S.g[0] = tb.g.x; S.g[1] = tb.g.y; S.g[2] = tb.g.z; S.c = tb.c; S.gl = tb.gl;
-        for (int i = 0; i < 3; ++i) {
-          float lo = fminf(fminf((&tb.X[0].x)[i], (&tb.X[1].x)[i]), fminf((&tb.X[2].x)[i], (&tb.X[3].x)[i]));
-          float hi = fmaxf(fmaxf((&tb.X[0].x)[i], (&tb.X[1].x)[i]), fmaxf((&tb.X[2].x)[i], (&tb.X[3].x)[i]));
-          float pad = 1e-5f * M + 1e-7f;
-          S.lo[i] = lo - pad;
-          S.hi[i] = hi + pad;
-        }
-        S.M = M; S.h = tb.hmin; S.kappa = tb.kappa;
-        S.orig = a.tet_orig[P.o_elem_off + tj];
-        S.valid = tb.hmin > 0.f ? 1 : 0;
-      }
-      __syncwarp();
-      const int n_o = min(kCluster, P.o_n_elem - oc * kCluster);
-      for (int j = 0; j < n_o; ++j) {
-        const TetB& B = s_stage[wid].tetb[j];
-        if (!tvalid || !B.valid || !aabb_overlap(tlo, thi, B.lo, B.hi)) continue;
-        V3<float> pn[4] = {mk(B.pn[0][0], B.pn[0][1], B.pn[0][2]), mk(B.pn[1][0], B.pn[1][1], B.pn[1][2]),
-                           mk(B.pn[2][0], B.pn[2][1], B.pn[2][2]), mk(B.pn[3][0], B.pn[3][1], B.pn[3][2])};
-        V3<float> gb = mk(B.g[0], B.g[1], B.g[2]);
-        Decide dc;
-        V3<float> nrm;
-        int nv = ss_polygon<float>(t, gb, B.c, B.gl, pn, B.po, B.M, B.h, B.kappa, dc, poly, tmp, nrm);
-        float gM = dot(t.g, nrm), gN = -dot(gb, nrm);
-        int flags = 0;
-        if (dc.unc) {
-          TetIn<double> td, tbd;
-          load_tet(a.tets, P.s_elem_off + ti, td);
-          tet_prepare(td);
-          for (int k = 0; k < 4; ++k) {
-            float4 r = a.tets[4 * (size_t)(P.o_elem_off + oc * kCluster + j) + k];
-            tbd.X[k] = mat_mul<double>(F.R, mk<double>(r.x, r.y, r.z)) + mk(F.t[0], F.t[1], F.t[2]);
-            tbd.P[k] = r.w;
-          }
-          tet_prepare(tbd);
-          V3<double> pnd[4];
-          double pod[4];
-          tet_planes(tbd.X, pnd, pod);
-          Decide dd;
-          PVx<double> pd[kMaxPolyV], td2[kMaxPolyV];
-          V3<double> nrmd;
-          nv = tbd.hmin > 0.0 ? ss_polygon<double>(td, tbd.g, tbd.c, tbd.gl, pnd, pod, 0.0, 1.0, 0.0, dd, pd, td2, nrmd)
-                              : 0;
-          for (int i = 0; i < nv; ++i) poly[i] = to_f(pd[i]);
-          if (dd.near) flags |= 1;
-          if (nv >= 3) {
-            nrm = mk((float)nrmd.x, (float)nrmd.y, (float)nrmd.z);
-            gM = (float)dot(td.g, nrmd);
-            gN = (float)-dot(tbd.g, nrmd);
-          }
-        }
-        if (nv >= 3) {
-          ac.n_poly += 1;
-          ac.n_near += flags & 1;
-          integrate_polygon(a, pc, ac, poly, nv, nrm, gM, gN);
-          record(a, pc, poly, nv, nrm, torig, B.orig, flags);
-        }
-      }
-      __syncwarp();
-    }
-    // ---- deterministic warp reduction (FP64 butterfly) ----
-    double v[8] = {ac.F[0], ac.F[1], ac.F[2], ac.T[0], ac.T[1], ac.T[2], ac.area, ac.fn0};
-    int c3[3] = {ac.n_poly, ac.n_faces, ac.n_near};
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) {
-#pragma unroll
-      for (int i = 0; i < 8; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) c3[i] += __shfl_xor_sync(0xffffffffu, c3[i], o);
-    }
-    if (lane == 0) {
-      ItemOut r;
-      for (int i = 0; i < 8; ++i) r.v[i] = v[i];
-      r.n_poly = c3[0]; r.n_faces = c3[1]; r.n_near = c3[2]; r.pad = 0;
-      a.item_out[item] = r;
-    }
-  }
-}
+#include "narrow.cuh"
 
 // ---------------------------------------------------------------------------
 // per-pair reduction (fixed order, FP64) and the world-frame wrench

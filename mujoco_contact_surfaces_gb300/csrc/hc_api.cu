@@ -433,15 +433,12 @@ hc_status run_step(hc_context* c, int want_polys, int want_pair) {
   }
   hc::StepArgs a = make_args(c, want_polys, want_pair);
   HC_CUDA(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(int), c->stream));
-  if (c->timing && !want_polys) {
-    c->launches_per_step = hc::launch_step(a, c->stream, c->ev);
-    HC_CUDA(cudaGetLastError());
-    c->stepped = true;
-    return HC_OK;
-  }
+  // With timing on, event records between the stages are part of the
+  // launch sequence (and of the captured graph).
+  cudaEvent_t* ev = c->timing && !want_polys ? c->ev : nullptr;
   bool use_graph = c->cfg.use_graph && !want_polys;
   if (!use_graph) {
-    c->launches_per_step = hc::launch_step(a, c->stream, nullptr);
+    c->launches_per_step = hc::launch_step(a, c->stream, ev);
     HC_CUDA(cudaGetLastError());
     c->stepped = true;
     return HC_OK;
@@ -449,7 +446,7 @@ hc_status run_step(hc_context* c, int want_polys, int want_pair) {
   if (!c->graph_valid) {
     invalidate_graph(c);
     HC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    c->launches_per_step = hc::launch_step(a, c->stream, nullptr);
+    c->launches_per_step = hc::launch_step(a, c->stream, ev);
     cudaError_t e = cudaStreamEndCapture(c->stream, &c->graph);
     if (e != cudaSuccess) return fail(HC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
     HC_CUDA(cudaGraphInstantiate(&c->graph_exec, c->graph, 0));
@@ -1045,6 +1042,19 @@ hc_status hc_get_taxels(hc_context* c, int sensor, float* out) {
   return HC_OK;
 }
 
+hc_status hc_get_taxels_all(hc_context* c, float* out, int64_t n_floats) {
+  if (hc_status st = need(c)) return st;
+  if (!out || n_floats < c->n_cells) return fail(HC_ERR_INVALID_ARG, "output too small");
+  if (c->sensors_dirty) return fail(HC_ERR_NOT_READY, "sensors not built; run a step first");
+  HC_CUDA(cudaSetDevice(c->device));
+  if (c->stepped) {
+    if (hc_status st = finish_step(c)) return st;
+  }
+  if (c->n_cells)
+    HC_CUDA(cudaMemcpy(out, c->taxels.p, (size_t)c->n_cells * sizeof(float), cudaMemcpyDeviceToHost));
+  return HC_OK;
+}
+
 hc_status hc_get_taxels_device(hc_context* c, const float** d_taxels, int64_t* n_floats) {
   if (hc_status st = need(c)) return st;
   if (d_taxels) *d_taxels = c->taxels.p;
@@ -1054,6 +1064,7 @@ hc_status hc_get_taxels_device(hc_context* c, const float** d_taxels, int64_t* n
 
 hc_status hc_enable_timing(hc_context* c, int enable) {
   if (hc_status st = need(c)) return st;
+  if ((enable != 0) != c->timing) invalidate_graph(c);
   c->timing = enable != 0;
   return HC_OK;
 }

@@ -125,6 +125,12 @@ class Engine:
         L.check(self.lib.hc_get_taxels(self.ctx, sensor, L.fptr(out)))
         return out
 
+    def all_taxels(self) -> np.ndarray:
+        n = sum(cx * cy for cx, cy in self.sensors.values())
+        out = np.zeros(n, np.float32)
+        L.check(self.lib.hc_get_taxels_all(self.ctx, L.fptr(out), n))
+        return out
+
     def set_debug(self, flags: int):
         L.check(self.lib.hc_set_debug(self.ctx, flags))
 

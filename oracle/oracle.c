@@ -514,6 +514,8 @@ static void soft_soft(const or_ctx* c, int ga, int gb, const double* xpos, const
        * rotation leaves the dot products unchanged */
       pg->gM = v_dot(ga_, nrm);
       pg->gN = -v_dot(gb_, nrm);
+      if (fabs(pg->gM) < 1e-9 * v_norm(ga_)) pg->gM = 0.0;
+      if (fabs(pg->gN) < 1e-9 * v_norm(gb_)) pg->gN = 0.0;
       pg->elem_a = ta; pg->elem_b = tb; pg->flags = flags;
     }
   }
@@ -535,9 +537,13 @@ static void finish_polygon(poly* pg, const double* R, const double* x, int query
   memcpy(pg->n, nw, sizeof(nw));
   memcpy(pg->grad, gw, sizeof(gw));
   if (query != 3) {
+    /* gradient into the soft body along the normal; a component below
+     * 1e-9 of the gradient's magnitude is rounding noise of a gradient
+     * perpendicular to the face and counts as zero (face skipped) */
     double gs = v_dot(gw, nw);
+    if (fabs(gs) < 1e-9 * v_norm(gw)) gs = 0.0;
     if (s_is_m) { pg->gM = gs; pg->gN = INFINITY; }
-    else { pg->gM = INFINITY; pg->gN = -gs; }
+    else { pg->gM = INFINITY; pg->gN = gs == 0.0 ? 0.0 : -gs; }
   }
   /* area-weighted centroid by a fan from vertex 0 */
   double A = 0, c[3] = {0, 0, 0}, pc = 0;
