@@ -387,11 +387,11 @@ __global__ void taxel_kernel(StepArgs a) {
 // ---------------------------------------------------------------------------
 int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   int n = 0;
-  if (ev) cudaEventRecord(ev[0], s);
+  if (ev) cudaEventRecordWithFlags(ev[0], s, cudaEventRecordExternal);
   if (a.n_pair > 0) {
     frames_kernel<<<(a.n_pair + 127) / 128, 128, 0, s>>>(a); ++n;
   }
-  if (ev) cudaEventRecord(ev[1], s);
+  if (ev) cudaEventRecordWithFlags(ev[1], s, cudaEventRecordExternal);
   if (a.n_units > 0) {
     bp_count_kernel<<<a.n_bp_blocks, kBpBlock, 0, s>>>(a); ++n;
   }
@@ -399,19 +399,19 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   if (a.n_units > 0) {
     bp_emit_kernel<<<a.n_bp_blocks, kBpBlock, 0, s>>>(a); ++n;
   }
-  if (ev) cudaEventRecord(ev[2], s);
+  if (ev) cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal);
   if (a.n_pair > 0) {
     narrow_kernel<<<a.narrow_grid, a.narrow_block, 0, s>>>(a); ++n;
   }
-  if (ev) cudaEventRecord(ev[3], s);
+  if (ev) cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal);
   if (a.n_pair > 0) {
     reduce_kernel<<<(a.n_pair * 32 + 127) / 128, 128, 0, s>>>(a); ++n;
   }
-  if (ev) cudaEventRecord(ev[4], s);
+  if (ev) cudaEventRecordWithFlags(ev[4], s, cudaEventRecordExternal);
   if (a.n_cells_total > 0) {
     taxel_kernel<<<(a.n_cells_total + 127) / 128, 128, 0, s>>>(a); ++n;
   }
-  if (ev) cudaEventRecord(ev[5], s);
+  if (ev) cudaEventRecordWithFlags(ev[5], s, cudaEventRecordExternal);
   return n;
 }
 
