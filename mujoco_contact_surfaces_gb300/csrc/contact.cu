@@ -283,7 +283,7 @@ __global__ void bp_scan_kernel(StepArgs a) {
       total = a.item_cap;
     }
     *a.item_total = total;
-    *a.item_next = 0;
+    a.item_next[0] = a.item_next[1] = a.item_next[2] = 0;
     a.unit_off[a.n_units] = carry;
   }
 }
@@ -400,8 +400,14 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
     bp_emit_kernel<<<a.n_bp_blocks, kBpBlock, 0, s>>>(a); ++n;
   }
   if (ev) cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal);
-  if (a.n_pair > 0) {
-    narrow_kernel<<<a.narrow_grid, a.narrow_block, 0, s>>>(a); ++n;
+  if (a.type_unit_end[0] > a.type_unit_begin[0]) {
+    narrow_sr_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
+  }
+  if (a.type_unit_end[1] > a.type_unit_begin[1]) {
+    narrow_hs_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
+  }
+  if (a.type_unit_end[2] > a.type_unit_begin[2]) {
+    narrow_ss_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
   }
   if (ev) cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal);
   if (a.n_pair > 0) {

@@ -113,6 +113,13 @@ std::vector<int> morton_order(const std::vector<double>& v, const std::vector<in
   return perm;
 }
 
+// Device counter words of a context.
+constexpr int kCntTotal = 0;   // work items of the step (clamped to capacity)
+constexpr int kCntStatus = 1;  // bit 0 item overflow, 1 candidate, 2 polygon
+constexpr int kCntCand = 2;    // candidate records written
+constexpr int kCntPoly = 3;    // polygon records written
+constexpr int kCntNext = 4;    // three work counters, one per query type
+
 int next_pow2(int n) {
   int p = 1;
   while (p < n) p <<= 1;
@@ -153,7 +160,10 @@ struct hc_context {
   DevBuf<int4> items;
   DevBuf<hc::ItemOut> item_out;
   int item_cap = 0;
-  DevBuf<int> counters;  // [item_total, item_next, status, cand_count, poly_count]
+  DevBuf<int> counters;  // see kCnt* below
+  int type_units[3][2] = {{0, 0}, {0, 0}, {0, 0}};  // unit ranges per query type
+  DevBuf<double4> tri_plane;
+  DevBuf<float4> tri_meta;
   DevBuf<hc::PairOut> pair_out;
   // sensors
   std::vector<SensorHost> sensors;
@@ -197,7 +207,8 @@ hc_status build_pools(hc_context* c) {
   std::vector<GeomHost*> order;
   for (auto& kv : c->geoms) order.push_back(&kv.second);
   std::sort(order.begin(), order.end(), [](GeomHost* a, GeomHost* b) { return a->order < b->order; });
-  std::vector<float4> tets, tris;
+  std::vector<float4> tets, tris, tri_meta;
+  std::vector<double4> tri_plane;
   std::vector<int> tet_orig, tri_orig;
   int node_total = 0;
   std::vector<int> s_eoff, s_ne, s_noff, s_L, r_eoff, r_ne, r_noff, r_L;
@@ -227,11 +238,33 @@ hc_status build_pools(hc_context* c) {
       g->n_elem = ne;
       for (int i = 0; i < ne; ++i) {
         int t = g->perm[i];
+        const double* r[3];
         for (int k = 0; k < 3; ++k) {
           int vi = m.f[3 * t + k];
+          r[k] = &m.v[3 * vi];
           tris.push_back(make_float4((float)m.v[3 * vi], (float)m.v[3 * vi + 1], (float)m.v[3 * vi + 2], 0.f));
         }
         tri_orig.push_back(t);
+        // FP64 plane of the triangle in its body frame (from the stored
+        // float vertices), min altitude, max edge and coordinate magnitude
+        double e1[3], e2[3], N[3];
+        for (int a = 0; a < 3; ++a) e1[a] = r[1][a] - r[0][a], e2[a] = r[2][a] - r[0][a];
+        N[0] = e1[1] * e2[2] - e1[2] * e2[1];
+        N[1] = e1[2] * e2[0] - e1[0] * e2[2];
+        N[2] = e1[0] * e2[1] - e1[1] * e2[0];
+        double ln = std::sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+        double le = 0, mag = 0;
+        for (int k = 0; k < 3; ++k) {
+          const double* p0 = r[k];
+          const double* p1 = r[(k + 1) % 3];
+          double d2 = 0;
+          for (int a = 0; a < 3; ++a) d2 += (p1[a] - p0[a]) * (p1[a] - p0[a]), mag = std::max(mag, std::fabs(p0[a]));
+          le = std::max(le, std::sqrt(d2));
+        }
+        double n[3] = {0, 0, 1};
+        if (ln > 0) n[0] = N[0] / ln, n[1] = N[1] / ln, n[2] = N[2] / ln;
+        tri_plane.push_back(make_double4(n[0], n[1], n[2], n[0] * r[0][0] + n[1] * r[0][1] + n[2] * r[0][2]));
+        tri_meta.push_back(make_float4(ln > 0 && le > 0 ? (float)(ln / le) : 0.f, (float)le, (float)mag, 0.f));
       }
       r_eoff.push_back(g->elem_off); r_ne.push_back(ne);
     } else {
@@ -249,6 +282,8 @@ hc_status build_pools(hc_context* c) {
   HC_CUDA(c->tris.upload(tris, s));
   HC_CUDA(c->tet_orig.upload(tet_orig, s));
   HC_CUDA(c->tri_orig.upload(tri_orig, s));
+  HC_CUDA(c->tri_plane.upload(tri_plane, s));
+  HC_CUDA(c->tri_meta.upload(tri_meta, s));
   // two float4 (lo, hi) per node
   HC_CUDA(c->nodes.reserve(2 * (size_t)std::max(1, node_total)));
   // LBVH node boxes on the device
@@ -395,11 +430,17 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
   a.n_bp_blocks = c->n_bp_blocks;
   a.items = c->items.p;
   a.item_cap = c->item_cap;
-  a.item_total = c->counters.p;
-  a.item_next = c->counters.p + 1;
-  a.status = c->counters.p + 2;
-  a.cand_count = c->counters.p + 3;
-  a.poly_count = c->counters.p + 4;
+  a.item_total = c->counters.p + kCntTotal;
+  a.status = c->counters.p + kCntStatus;
+  a.cand_count = c->counters.p + kCntCand;
+  a.poly_count = c->counters.p + kCntPoly;
+  a.item_next = c->counters.p + kCntNext;
+  for (int q = 0; q < 3; ++q) {
+    a.type_unit_begin[q] = c->type_units[q][0];
+    a.type_unit_end[q] = c->type_units[q][1];
+  }
+  a.tri_plane = c->tri_plane.p;
+  a.tri_meta = c->tri_meta.p;
   a.item_out = c->item_out.p;
   a.pair_out = c->pair_out.p;
   a.sensors = c->sensors_d.p;
@@ -463,7 +504,7 @@ hc_status finish_step(hc_context* c) {
     int cnt[8];
     HC_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
     HC_CUDA(cudaStreamSynchronize(c->stream));
-    if (!(cnt[2] & 1)) return HC_OK;
+    if (!(cnt[kCntStatus] & 1)) return HC_OK;
     // overflow: the scan wrote the full total into unit_off[n_units]
     int total = 0;
     HC_CUDA(cudaMemcpy(&total, c->unit_off.p + c->n_units, sizeof(int), cudaMemcpyDeviceToHost));
@@ -539,6 +580,7 @@ hc_status hc_context_destroy(hc_context* c) {
   cudaStreamSynchronize(c->stream);
   invalidate_graph(c);
   c->tets.release(); c->tris.release(); c->nodes.release(); c->tet_orig.release(); c->tri_orig.release();
+  c->tri_plane.release(); c->tri_meta.release();
   c->xpos.release(); c->xmat.release(); c->vel.release();
   c->pairs.release(); c->frames.release(); c->unit_pair.release(); c->unit_cl.release();
   c->unit_count.release(); c->unit_off.release(); c->block_sum.release(); c->items.release();
@@ -810,18 +852,31 @@ hc_status hc_set_pairs(hc_context* c, int n_pair, const int* g1, const int* g2, 
           if (ns == 0) p.sensor0 = (int)k; else p.sensor1 = (int)k;
           ++ns;
         }
-      if (p.query == HC_QUERY_SOFT_HALFSPACE) {
-        upair.push_back(i); ucl.push_back(-1);
-      } else {
-        for (int k = 0; k < p.o_n_clusters; ++k) { upair.push_back(i); ucl.push_back(k); }
-      }
-      p.unit_end = (int)upair.size();
     } else {
       p.query = HC_QUERY_NONE;
       if (worst == HC_OK) worst = (hc_status)st;
     }
     if (per_pair_status) per_pair_status[i] = st;
     if (per_pair_query) per_pair_query[i] = p.query;
+  }
+  // Broadphase units ordered by query type, then pair: each narrow-phase
+  // kernel works one contiguous item range; each pair's units (and items)
+  // stay contiguous for the per-pair reduction.
+  const int qorder[3] = {HC_QUERY_SOFT_RIGID, HC_QUERY_SOFT_HALFSPACE, HC_QUERY_SOFT_SOFT};
+  for (int qi = 0; qi < 3; ++qi) {
+    c->type_units[qi][0] = (int)upair.size();
+    for (int i = 0; i < n_pair; ++i) {
+      hc::PairDev& p = P[i];
+      if (p.query != qorder[qi]) continue;
+      p.unit_begin = (int)upair.size();
+      if (p.query == HC_QUERY_SOFT_HALFSPACE) {
+        upair.push_back(i); ucl.push_back(-1);
+      } else {
+        for (int k = 0; k < p.o_n_clusters; ++k) { upair.push_back(i); ucl.push_back(k); }
+      }
+      p.unit_end = (int)upair.size();
+    }
+    c->type_units[qi][1] = (int)upair.size();
   }
   cudaStream_t s = c->stream;
   c->pairs_h = P;
@@ -933,8 +988,8 @@ hc_status hc_get_candidates(hc_context* c, hc_candidate* out, int64_t capacity, 
   if (hc_status st = finish_step(c)) return st;
   int cnt[8];
   HC_CUDA(cudaMemcpy(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
-  if (cnt[2] & 2) return fail(HC_ERR_OVERFLOW, "candidate record buffer overflow");
-  int64_t n = std::min<int64_t>(cnt[3], c->cand_cap);
+  if (cnt[kCntStatus] & 2) return fail(HC_ERR_OVERFLOW, "candidate record buffer overflow");
+  int64_t n = std::min<int64_t>(cnt[kCntCand], c->cand_cap);
   if (count) *count = n;
   if (out && capacity > 0) {
     int64_t k = std::min(n, capacity);
@@ -962,8 +1017,8 @@ hc_status hc_get_surface(hc_context* c, int pair, hc_surface_view* view) {
   if (hc_status st = finish_step(c)) return st;
   int cnt[8];
   HC_CUDA(cudaMemcpy(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
-  if (cnt[2] & 4) return fail(HC_ERR_OVERFLOW, "surface record buffer overflow");
-  int n = std::min(cnt[4], c->poly_cap);
+  if (cnt[kCntStatus] & 4) return fail(HC_ERR_OVERFLOW, "surface record buffer overflow");
+  int n = std::min(cnt[kCntPoly], c->poly_cap);
   std::vector<hc::PolyRec> r(n);
   if (n) HC_CUDA(cudaMemcpy(r.data(), c->polys.p, n * sizeof(hc::PolyRec), cudaMemcpyDeviceToHost));
   std::sort(r.begin(), r.end(), [](const hc::PolyRec& a, const hc::PolyRec& b) {
@@ -1084,7 +1139,7 @@ hc_status hc_get_timings(hc_context* c, hc_timings* out) {
   cudaEventElapsedTime(&out->ms_total, c->ev[0], c->ev[5]);
   int cnt[8];
   HC_CUDA(cudaMemcpy(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
-  out->n_items = cnt[0];
+  out->n_items = cnt[kCntTotal];
   out->n_polygons = 0;
   return HC_OK;
 }

@@ -20,6 +20,8 @@ struct StepArgs {
   const float4* tets;
   const int* tet_orig;
   const float4* tris;
+  const double4* tri_plane;   // body-frame unit normal and offset (FP64)
+  const float4* tri_meta;     // (min altitude, max edge, max |vertex|, 0)
   const int* tri_orig;
   const float4* nodes;
   // broadphase units and items
@@ -32,8 +34,10 @@ struct StepArgs {
   int n_bp_blocks;
   int4* items;
   int item_cap;
+  int type_unit_begin[3];    // unit range of each query type
+  int type_unit_end[3];      // (soft-rigid, half-space, soft-soft)
   int* item_total;
-  int* item_next;
+  int* item_next;     // one work counter per query type
   int* status;        // bit 0: item overflow, bit 1: candidate overflow,
                       // bit 2: polygon overflow
   ItemOut* item_out;

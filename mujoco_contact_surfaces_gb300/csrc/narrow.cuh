@@ -1,25 +1,29 @@
-// narrow.cuh — the narrow-phase kernel (included by contact.cu inside
+// narrow.cuh — the narrow-phase kernels (included by contact.cu inside
 // namespace hc).
 //
-// One warp per work item (soft leaf cluster x other cluster), items taken
-// from a global counter.  The other cluster's 32 elements are staged in
-// shared memory in the soft frame (with FP64 planes / fields); each lane
-// owns one soft tet and walks the staged elements.  Per non-empty polygon:
-// centroid quadrature (mujoco_contact_surfaces_plugin.cpp:320-409),
-// Hunt-Crossley damping and regularised friction, and the
-// flat-sensor ray binning (flat_tactile_sensor.cpp:316-392).  The warp's
-// sums are reduced in FP64 in a fixed order.
+// One kernel per query type, each over the contiguous range of work items
+// of its type (units are ordered by query type).  One warp per item (soft
+// leaf cluster x other cluster); items are taken from a per-type counter.
+// Per item the warp stages the soft tets and the other elements in shared
+// memory (soft frame), builds a queue of candidate element pairs with cheap
+// conservative tests (AABB overlap and an FP32 plane test with an error
+// margin), and then works the queue with all 32 lanes.  Per non-empty
+// polygon: centroid quadrature (mujoco_contact_surfaces_plugin.cpp:320-409),
+// Hunt-Crossley damping and regularised friction, and flat-sensor
+// ray binning (flat_tactile_sensor.cpp:316-392).  The warp's sums are reduced
+// in FP64 in a fixed order.
 
 struct Acc {
   float F[3], T[3], area, fn0;
   int n_poly, n_faces, n_near;
 };
 
-struct PairCtx {
-  const PairDev* P;
-  const FrameDev* F;
-  int pair;
-};
+__device__ __forceinline__ void acc_zero(Acc& ac) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) ac.F[i] = ac.T[i] = 0.f;
+  ac.area = ac.fn0 = 0.f;
+  ac.n_poly = ac.n_faces = ac.n_near = 0;
+}
 
 // One quadrature point and the force law, soft frame.
 __device__ __forceinline__ void point_force(Acc& ac, const FrameDev& F, float damping, float mu, int apply, float A,
@@ -48,46 +52,77 @@ __device__ __forceinline__ void point_force(Acc& ac, const FrameDev& F, float da
   ac.T[0] += tq.x; ac.T[1] += tq.y; ac.T[2] += tq.z;
 }
 
-// Ray hits of one fan triangle (soft frame) on a sensor's sample grid.  The
-// sensor's rays are parallel to its -z axis, start 1.5*zs (+1e-8) above its
-// centre and accept 0 < t < 1.5*zs (flat_tactile_sensor.cpp:324-346); the
-// triangle test follows the acceptance rules of the Moeller-Trumbore test in
-// bvh.cpp:49-74 (|det| < 1e-10 rejects, u in [0,1], v >= 0, u+v <= 1), here
-// in the sensor frame.  Each sample keeps the smallest t, packed with the
-// pressure at the hit, by a 64-bit atomicMin (order independent).
-__device__ void raster_tri(const StepArgs& a, int sid, const float* Rl, const float* tl, V3<float> A, V3<float> B,
-                           V3<float> C, float pa, float pb, float pc) {
+// Ray samples of a flat sensor hit by one contact polygon.  The sensor's
+// rays are parallel to its -z axis, start 1.5*zs (+1e-8) above its centre and
+// accept 0 < t < 1.5*zs (flat_tactile_sensor.cpp:324-346).  The reference
+// casts them against the polygon's fan triangles (Moeller-Trumbore,
+// bvh.cpp:49-74) and evaluates the pressure barycentrically; a ray through
+// the convex polygon hits exactly one fan triangle and, the field being
+// linear on the polygon, the pressure at the hit is the polygon's linear
+// field there.  Polygons whose projection is degenerate (|2A| < 1e-10, the
+// test's parallel threshold) are skipped.  Each sample keeps the smallest t
+// packed with the pressure by a 64-bit atomicMin (order independent).
+template <int ND>
+__device__ void raster_polygon(const StepArgs& a, int sid, const float* Rl, const float* tl, const PV<float, ND>* v,
+                               int nv, V3<float> anc, V3<float> g_soft) {
   const SensorDev S = a.sensors[sid];
   const V3<float> T = mk(tl[0], tl[1], tl[2]);
-  const V3<float> la = mat_mul<float>(Rl, A) + T, lb = mat_mul<float>(Rl, B) + T, lc = mat_mul<float>(Rl, C) + T;
-  const float e1x = lb.x - la.x, e1y = lb.y - la.y, e2x = lc.x - la.x, e2y = lc.y - la.y;
-  const float det = e1x * e2y - e1y * e2x;
-  if (fabsf(det) < 1e-10f) return;
+  float lx[kMaxPolyV], ly[kMaxPolyV], lz[kMaxPolyV];
+  float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY, A2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < kMaxPolyV; ++i) {
+    if (i < nv) {
+      const V3<float> l = mat_mul<float>(Rl, anc + pv_pos(v[i])) + T;
+      lx[i] = l.x; ly[i] = l.y; lz[i] = l.z;
+      mnx = fminf(mnx, l.x); mxx = fmaxf(mxx, l.x);
+      mny = fminf(mny, l.y); mxy = fmaxf(mxy, l.y);
+    }
+  }
+#pragma unroll
+  for (int i = 1; i + 1 < kMaxPolyV; ++i)
+    if (i + 1 < nv) A2 += (lx[i] - lx[0]) * (ly[i + 1] - ly[0]) - (ly[i] - ly[0]) * (lx[i + 1] - lx[0]);
+  if (!(fabsf(A2) >= 1e-10f)) return;
+  const float sgn = A2 > 0.f ? 1.f : -1.f;
+  // plane of the polygon and the pressure gradient, sensor frame
+  const V3<float> e1 = mk(lx[1] - lx[0], ly[1] - ly[0], lz[1] - lz[0]);
+  V3<float> nn = mk(0.f, 0.f, 0.f);
+#pragma unroll
+  for (int i = 2; i < kMaxPolyV; ++i)
+    if (i < nv) nn = nn + cross(e1, mk(lx[i] - lx[0], ly[i] - ly[0], lz[i] - lz[0]));
+  if (!(fabsf(nn.z) > 0.f)) return;
+  const float zx = -nn.x / nn.z, zy = -nn.y / nn.z;  // dz/dx, dz/dy on the plane
+  const V3<float> gl = mat_mul<float>(Rl, g_soft);
+  const float px = gl.x + gl.z * zx, py = gl.y + gl.z * zy;  // dp/dx, dp/dy on the plane
   const float* sx = a.samp_coord + S.samp_off_x;
   const float* sy = a.samp_coord + S.samp_off_y;
   const float x0 = sx[0], dx = S.nx > 1 ? sx[1] - sx[0] : 1.f;
   const float y0 = sy[0], dy = S.ny > 1 ? sy[1] - sy[0] : 1.f;
-  const float mnx = fminf(la.x, fminf(lb.x, lc.x)), mxx = fmaxf(la.x, fmaxf(lb.x, lc.x));
-  const float mny = fminf(la.y, fminf(lb.y, lc.y)), mxy = fmaxf(la.y, fmaxf(lb.y, lc.y));
-  const float fx0 = floorf((mnx - x0) / dx) - 1.f, fx1 = ceilf((mxx - x0) / dx) + 1.f;
-  const float fy0 = floorf((mny - y0) / dy) - 1.f, fy1 = ceilf((mxy - y0) / dy) + 1.f;
+  const float fx0 = ceilf((mnx - x0) / dx - 1e-3f), fx1 = floorf((mxx - x0) / dx + 1e-3f);
+  const float fy0 = ceilf((mny - y0) / dy - 1e-3f), fy1 = floorf((mxy - y0) / dy + 1e-3f);
   if (!(fx1 >= 0.f && fy1 >= 0.f && fx0 <= (float)(S.nx - 1) && fy0 <= (float)(S.ny - 1))) return;
   const int X0 = max(0, (int)fx0), X1 = min(S.nx - 1, (int)fx1);
   const int Y0 = max(0, (int)fy0), Y1 = min(S.ny - 1, (int)fy1);
-  const float inv = 1.f / det;
   unsigned long long* smp = a.samples + S.sample_off;
+  const float p0 = v[0].p;
   for (int X = X0; X <= X1; ++X) {
-    const float wx = sx[X] - la.x;
+    const float qx = sx[X];
     for (int Y = Y0; Y <= Y1; ++Y) {
-      const float wy = sy[Y] - la.y;
-      const float u = (wx * e2y - wy * e2x) * inv;
-      if (u < 0.f || u > 1.f) continue;
-      const float v = (e1x * wy - e1y * wx) * inv;
-      if (v < 0.f || u + v > 1.f) continue;
-      const float z = la.z + u * (lb.z - la.z) + v * (lc.z - la.z);
+      const float qy = sy[Y];
+      bool in = true;
+#pragma unroll
+      for (int i = 0; i < kMaxPolyV; ++i) {
+        if (i < nv) {
+          const int k = i + 1 == nv ? 0 : i + 1;
+          const float ex = (lx[k] - lx[i]) * (qy - ly[i]) - (ly[k] - ly[i]) * (qx - lx[i]);
+          in &= sgn * ex >= 0.f;
+        }
+      }
+      if (!in) continue;
+      const float ddx = qx - lx[0], ddy = qy - ly[0];
+      const float z = lz[0] + zx * ddx + zy * ddy;
       const float t = (S.zs15 + 1e-8f) - z;
       if (!(t > 0.f && t < S.zs15)) continue;
-      const float pr = (1.f - u - v) * pa + u * pb + v * pc;
+      const float pr = p0 + px * ddx + py * ddy;
       const unsigned long long key =
           ((unsigned long long)__float_as_uint(t) << 32) | (unsigned long long)__float_as_uint(pr);
       atomicMin(&smp[(size_t)X * S.ny + Y], key);
@@ -96,13 +131,12 @@ __device__ void raster_tri(const StepArgs& a, int sid, const float* Rl, const fl
 }
 
 // Quadrature of one polygon (vertices relative to `anc`, soft frame) and its
-// contribution to forces and sensors.  n: contact normal out of N into M.
+// contribution to forces and sensors.  n: contact normal out of N into M;
+// g: the soft (M-side for soft-soft) pressure gradient, soft frame.
 template <int ND>
-__device__ void integrate_polygon(const StepArgs& a, const PairCtx& pc, Acc& ac, const PV<float, ND>* v, int nv,
-                                  V3<float> anc, V3<float> n, float gM, float gN) {
-  const FrameDev& F = *pc.F;
-  const PairDev& P = *pc.P;
-  // area-weighted centroid by a fan from vertex 0 (local coordinates)
+__device__ void integrate_polygon(const StepArgs& a, const PairDev& P, const FrameDev& F, Acc& ac,
+                                  const PV<float, ND>* v, int nv, V3<float> anc, V3<float> n, float gM, float gN,
+                                  V3<float> g) {
   float A = 0.f, pcen = 0.f;
   V3<float> c = mk(0.f, 0.f, 0.f);
   const V3<float> v0 = pv_pos(v[0]);
@@ -136,37 +170,28 @@ __device__ void integrate_polygon(const StepArgs& a, const PairCtx& pc, Acc& ac,
       point_force(ac, F, P.damping, P.mu, a.apply_forces, Ai, cen, n, gM, gN, p0);
     }
   }
-  for (int q = 0; q < 2; ++q) {
-    const int sid = q == 0 ? P.sensor0 : P.sensor1;
-    if (sid < 0) continue;
-    const float* Rl = q == 0 ? F.Rl : F.Rl1;
-    const float* tl = q == 0 ? F.tl : F.tl1;
-    const V3<float> ca = anc + c;
-    for (int i = 0; i < nv; ++i) {
-      const int j = i + 1 == nv ? 0 : i + 1;
-      raster_tri(a, sid, Rl, tl, anc + pv_pos(v[i]), anc + pv_pos(v[j]), ca, v[i].p, v[j].p, pcen);
-    }
-  }
+  if (P.sensor0 >= 0) raster_polygon<ND>(a, P.sensor0, F.Rl, F.tl, v, nv, anc, g);
+  if (P.sensor1 >= 0) raster_polygon<ND>(a, P.sensor1, F.Rl1, F.tl1, v, nv, anc, g);
 }
 
 template <int ND>
-__device__ void record(const StepArgs& a, const PairCtx& pc, const PV<float, ND>* v, int nv, V3<float> anc,
-                       V3<float> n, int ea, int eb, int flags) {
+__device__ void record(const StepArgs& a, int pair, const PV<float, ND>* v, int nv, V3<float> anc, V3<float> n,
+                       int ea, int eb, int flags) {
   if (a.debug & 1) {
     const int k = atomicAdd(a.cand_count, 1);
     if (k < a.cand_cap) {
       CandRec r;
-      r.pair = pc.pair; r.elem_a = ea; r.elem_b = eb; r.n_vert = nv; r.flags = flags;
+      r.pair = pair; r.elem_a = ea; r.elem_b = eb; r.n_vert = nv; r.flags = flags;
       a.cand[k] = r;
     } else {
       atomicOr(a.status, 2);
     }
   }
-  if (a.want_polys && (a.want_pair < 0 || a.want_pair == pc.pair)) {
+  if (a.want_polys && (a.want_pair < 0 || a.want_pair == pair)) {
     const int k = atomicAdd(a.poly_count, 1);
     if (k < a.poly_cap) {
       PolyRec& r = a.polys[k];
-      r.pair = pc.pair; r.elem_a = ea; r.elem_b = eb; r.nv = nv;
+      r.pair = pair; r.elem_a = ea; r.elem_b = eb; r.nv = nv;
       r.n[0] = n.x; r.n[1] = n.y; r.n[2] = n.z; r.n[3] = 0.f;
       for (int i = 0; i < kMaxPolyV; ++i) {
         const bool in = i < nv;
@@ -217,6 +242,52 @@ __device__ __forceinline__ void load_tet(const float4* tets, int idx, TetIn<R>& 
   }
 }
 
+// Soft tet staged in shared memory (soft frame).
+struct TetStage {
+  float X[4][3];
+  float P[4];
+  float g[3];
+  float gl, kappa, xmax, pmax;
+  float lo[3], hi[3];
+  int orig, valid;
+};
+
+__device__ __forceinline__ void stage_tet(const StepArgs& a, const PairDev& P, int ti, TetStage& S) {
+  S.valid = 0;
+  if (ti >= P.s_n_elem) return;
+  TetIn<float> t;
+  load_tet(a.tets, P.s_elem_off + ti, t);
+  tet_prepare(t);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    S.X[k][0] = t.X[k].x; S.X[k][1] = t.X[k].y; S.X[k][2] = t.X[k].z;
+    S.P[k] = t.P[k];
+  }
+  S.g[0] = t.g.x; S.g[1] = t.g.y; S.g[2] = t.g.z;
+  S.gl = t.gl; S.kappa = t.kappa; S.xmax = t.xmax; S.pmax = t.pmax;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float lo = fminf(fminf(S.X[0][i], S.X[1][i]), fminf(S.X[2][i], S.X[3][i]));
+    const float hi = fmaxf(fmaxf(S.X[0][i], S.X[1][i]), fmaxf(S.X[2][i], S.X[3][i]));
+    const float pad = 1e-5f * (fabsf(lo) + fabsf(hi)) + 1e-7f;
+    S.lo[i] = lo - pad;
+    S.hi[i] = hi + pad;
+  }
+  S.orig = a.tet_orig[P.s_elem_off + ti];
+  S.valid = t.hmin > 0.f ? 1 : 0;
+}
+
+__device__ __forceinline__ void unstage_tet(const TetStage& S, TetIn<float>& t) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    t.X[k] = mk(S.X[k][0], S.X[k][1], S.X[k][2]);
+    t.P[k] = S.P[k];
+  }
+  t.g = mk(S.g[0], S.g[1], S.g[2]);
+  t.gl = S.gl; t.kappa = S.kappa; t.xmax = S.xmax; t.pmax = S.pmax;
+  t.c = 0.f; t.hmin = 0.f;
+}
+
 // Index of the tet vertex nearest the section plane.
 __device__ __forceinline__ int nearest_vertex(const double s[4]) {
   int k = 0;
@@ -237,48 +308,149 @@ __device__ __forceinline__ void tet_local(const TetIn<R>& t, int anc, PV<R, ND> 
   }
 }
 
-// Rigid triangle in the soft frame.
-struct TriData {
-  double n64[3], o64;  // FP64 plane (unit normal, offset)
-  float Y[3][3];       // vertices
-  float n[3];          // unit normal (out of the rigid body)
-  float en[3][3];      // in-plane inward edge normals
+// Conservative FP32 test: all four vertices certainly on one side of
+// n.x = o (margin covers float rounding of n, o and the dot products).
+__device__ __forceinline__ bool one_sided32(const float X[4][3], const float* n, float o, float margin) {
+  int pos = 0, neg = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float s = n[0] * X[k][0] + n[1] * X[k][1] + n[2] * X[k][2] - o;
+    pos += s > margin;
+    neg += s < -margin;
+  }
+  return pos == 4 || neg == 4;
+}
+
+// Gradient component along a face normal (P:356-359).  A component below
+// 1e-9 of |g| is rounding noise of a gradient perpendicular to the face and
+// counts as zero, so the face is skipped (P:361-368) deterministically; an
+// FP32 value within 1e-5 |g| of zero is re-evaluated in FP64 for that test.
+__device__ __forceinline__ float grad_noise_rule(double gi, double gl) {
+  return fabs(gi) < 1e-9 * gl ? 0.f : (float)gi;
+}
+
+__device__ __noinline__ float grad_along64(const StepArgs& a, int tet_idx, double n0, double n1, double n2) {
+  TetIn<double> td;
+  load_tet(a.tets, tet_idx, td);
+  tet_prepare(td);
+  return grad_noise_rule(td.g.x * n0 + td.g.y * n1 + td.g.z * n2, td.gl);
+}
+
+__device__ __forceinline__ bool aabb_overlap(const float* alo, const float* ahi, const float* blo, const float* bhi) {
+  return alo[0] <= bhi[0] && ahi[0] >= blo[0] && alo[1] <= bhi[1] && ahi[1] >= blo[1] && alo[2] <= bhi[2] &&
+         ahi[2] >= blo[2];
+}
+
+template <int ND>
+__device__ __forceinline__ void to_f(const PV<double, ND>* in, int n, PV<float, ND>* out) {
+  for (int i = 0; i < n; ++i) {
+    out[i].x = (float)in[i].x; out[i].y = (float)in[i].y; out[i].z = (float)in[i].z; out[i].p = (float)in[i].p;
+#pragma unroll
+    for (int j = 0; j < ND; ++j) out[i].d[j] = (float)in[i].d[j];
+  }
+}
+
+__device__ __forceinline__ void warp_reduce_store(const StepArgs& a, const Acc& ac, int item, int lane) {
+  double v[8] = {ac.F[0], ac.F[1], ac.F[2], ac.T[0], ac.T[1], ac.T[2], ac.area, ac.fn0};
+  int c3[3] = {ac.n_poly, ac.n_faces, ac.n_near};
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) c3[i] += __shfl_xor_sync(0xffffffffu, c3[i], o);
+  }
+  if (lane == 0) {
+    ItemOut r;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) r.v[i] = v[i];
+    r.n_poly = c3[0]; r.n_faces = c3[1]; r.n_near = c3[2]; r.pad = 0;
+    a.item_out[item] = r;
+  }
+}
+
+// Item range of query type q and the next item for this warp.
+__device__ __forceinline__ int next_item(const StepArgs& a, int q, int lane, int& ie) {
+  const int total = *a.item_total;
+  const int ib = min(a.unit_off[a.type_unit_begin[q]], total);
+  ie = min(a.unit_off[a.type_unit_end[q]], total);
+  int item = 0;
+  if (lane == 0) item = atomicAdd(a.item_next + q, 1);
+  return ib + __shfl_sync(0xffffffffu, item, 0);
+}
+
+// Compact the warp's candidate masks (bit j of lane i: element pair (i, j))
+// into a queue of (i | j << 5) entries in lane-major order.
+__device__ __forceinline__ int build_queue(unsigned mask, unsigned short* q, int lane) {
+  const int cnt = __popc(mask);
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  int w = incl - cnt;
+  while (mask) {
+    const int j = __ffs(mask) - 1;
+    mask &= mask - 1;
+    q[w++] = (unsigned short)(lane | (j << 5));
+  }
+  return __shfl_sync(0xffffffffu, incl, 31);
+}
+
+constexpr int kNarrowWarps = 4;
+
+// ============================================================================
+// soft-rigid
+// ============================================================================
+struct TriStage {
+  double n64[3], o64;  // FP64 plane (unit normal out of the rigid body, offset)
+  float n[3], o;       // float copies
+  float en[3][3];      // in-plane inward edge normals (FP32)
   float eo[3];
   float lo[3], hi[3];
   float M, h, Lt;      // coordinate magnitude, min altitude, max edge
-  int orig;
-  int valid;
+  int orig, valid;
 };
 
-template <class R>
-__device__ __forceinline__ void tri_planes(const V3<R> Y[3], V3<R>& n, R& o, V3<R> en[3], R eo[3], R& h, R& Lt,
-                                           bool& valid) {
-  const V3<R> N = cross(Y[1] - Y[0], Y[2] - Y[0]);
-  const R ln = norm(N);
-  valid = ln > (R)0;
-  n = valid ? N * ((R)1 / ln) : mk<R>(0, 0, 1);
-  o = dot(n, Y[0]);
-  R le = 0;
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    const V3<R> e = Y[j == 2 ? 0 : j + 1] - Y[j];
-    le = fmax(le, norm(e));
-    const V3<R> m = cross(n, e);
-    const R lm = norm(m);
-    en[j] = lm > (R)0 ? m * ((R)1 / lm) : m;
-    eo[j] = dot(en[j], Y[j]);
-  }
-  Lt = le;
-  h = le > (R)0 ? ln / le : (R)0;
-}
-
-// FP64 triangle in the soft frame from its stored rigid-frame vertices.
-__device__ __forceinline__ void tri_fp64(const StepArgs& a, const FrameDev& F, int idx, V3<double> Y[3]) {
+__device__ __forceinline__ void stage_tri(const StepArgs& a, const PairDev& P, const FrameDev& F, int tj,
+                                          TriStage& S) {
+  S.valid = 0;
+  if (tj >= P.o_n_elem) return;
+  const int idx = P.o_elem_off + tj;
+  const double4 pl = a.tri_plane[idx];
+  const float4 meta = a.tri_meta[idx];
+  // plane: n = R n_body, o = o_body + n . t (FP64)
+  const V3<double> nd = mat_mul<double>(F.R, mk(pl.x, pl.y, pl.z));
+  const double od = pl.w + nd.x * F.t[0] + nd.y * F.t[1] + nd.z * F.t[2];
+  S.n64[0] = nd.x; S.n64[1] = nd.y; S.n64[2] = nd.z; S.o64 = od;
+  const V3<float> n = mk((float)nd.x, (float)nd.y, (float)nd.z);
+  S.n[0] = n.x; S.n[1] = n.y; S.n[2] = n.z; S.o = (float)od;
+  V3<float> Y[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const float4 r = a.tris[3 * (size_t)idx + k];
-    Y[k] = mat_mul<double>(F.R, mk<double>(r.x, r.y, r.z)) + mk(F.t[0], F.t[1], F.t[2]);
+    Y[k] = mat_mul<float>(F.Rf, mk(r.x, r.y, r.z)) + mk(F.tf[0], F.tf[1], F.tf[2]);
   }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const V3<float> e = Y[j == 2 ? 0 : j + 1] - Y[j];
+    V3<float> m = cross(n, e);
+    const float lm = norm(m);
+    m = lm > 0.f ? m * (1.f / lm) : m;
+    S.en[j][0] = m.x; S.en[j][1] = m.y; S.en[j][2] = m.z;
+    S.eo[j] = dot(m, Y[j]);
+  }
+  const float M = fmaxf(meta.z, fmaxf(fabsf(F.tf[0]), fmaxf(fabsf(F.tf[1]), fabsf(F.tf[2]))));
+  const float pad = 1e-5f * (M + meta.y) + 1e-7f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    S.lo[i] = fminf(fminf((&Y[0].x)[i], (&Y[1].x)[i]), (&Y[2].x)[i]) - pad;
+    S.hi[i] = fmaxf(fmaxf((&Y[0].x)[i], (&Y[1].x)[i]), (&Y[2].x)[i]) + pad;
+  }
+  S.M = M; S.h = meta.x; S.Lt = meta.y;
+  S.orig = a.tri_orig[idx];
+  S.valid = meta.x > 0.f ? 1 : 0;
 }
 
 // Soft-rigid polygon: tet section by the triangle plane (FP64 values s),
@@ -319,7 +491,128 @@ __device__ int sr_polygon(const TetIn<R>& t, const double s[4], V3<R> n, const V
   return nv;
 }
 
-// Half-space polygon: tet section by the plane (FP64 values s).
+// Exact-decision fallback of one soft-rigid element pair in FP64 from the
+// stored inputs; returns the vertex count and sets near/gint.
+__device__ __noinline__ int sr_fp64(const StepArgs& a, const PairDev& P, const FrameDev& F, const TriStage& T,
+                                    int tet_idx, int tri_idx, const double s[4], int& anc, PV<float, 3>* poly,
+                                    bool& near, float& gint) {
+  TetIn<double> td;
+  load_tet(a.tets, tet_idx, td);
+  tet_prepare(td);
+  V3<double> Y[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float4 r = a.tris[3 * (size_t)tri_idx + k];
+    Y[k] = mat_mul<double>(F.R, mk<double>(r.x, r.y, r.z)) + mk(F.t[0], F.t[1], F.t[2]);
+  }
+  const V3<double> n = mk(T.n64[0], T.n64[1], T.n64[2]);
+  V3<double> en[3];
+  double eo[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const V3<double> m = cross(n, Y[j == 2 ? 0 : j + 1] - Y[j]);
+    const double lm = norm(m);
+    en[j] = lm > 0.0 ? m * (1.0 / lm) : m;
+    eo[j] = dot(en[j], Y[j]);
+  }
+  Decide dd;
+  PV<double, 3> pd[kMaxPolyV], tmp[kMaxPolyV];
+  const int nv = sr_polygon<double>(td, s, n, en, eo, 0.0, 1.0, 0.0, dd, anc, pd, tmp);
+  to_f(pd, nv, poly);
+  near = dd.near;
+  gint = grad_noise_rule(dot(td.g, n), td.gl);
+  return nv;
+}
+
+__global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
+  __shared__ TriStage s_tri[kNarrowWarps][kCluster];
+  __shared__ TetStage s_tet[kNarrowWarps][kCluster];
+  __shared__ unsigned short s_q[kNarrowWarps][kCluster * kCluster];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  while (true) {
+    int ie;
+    const int item = next_item(a, 0, lane, ie);
+    if (item >= ie) break;
+    const int4 it = a.items[item];
+    const PairDev& P = a.pairs[it.x];
+    const FrameDev& F = a.frames[it.x];
+    Acc ac;
+    acc_zero(ac);
+    const int sl = it.y, oc = it.z;
+    if (F.valid) {
+      stage_tri(a, P, F, oc * kCluster + lane, s_tri[wid][lane]);
+      stage_tet(a, P, sl * kCluster + lane, s_tet[wid][lane]);
+    } else {
+      s_tri[wid][lane].valid = 0;
+      s_tet[wid][lane].valid = 0;
+    }
+    __syncwarp();
+    // candidate queue
+    unsigned mask = 0;
+    const TetStage& me = s_tet[wid][lane];
+    if (me.valid) {
+      const int n_o = min(kCluster, P.o_n_elem - oc * kCluster);
+      for (int j = 0; j < n_o; ++j) {
+        const TriStage& T = s_tri[wid][j];
+        if (!T.valid || !aabb_overlap(me.lo, me.hi, T.lo, T.hi)) continue;
+        const float margin = 4e-6f * (me.xmax + fabsf(T.o) + T.Lt);
+        if (one_sided32(me.X, T.n, T.o, margin)) continue;
+        mask |= 1u << j;
+      }
+    }
+    const int total = build_queue(mask, s_q[wid], lane);
+    __syncwarp();
+    const float sgn = P.s_is_m ? 1.f : -1.f;
+    for (int base = 0; base < total; base += 32) {
+      const int k = base + lane;
+      if (k >= total) continue;
+      const int e = s_q[wid][k];
+      const int i = e & 31, j = e >> 5;
+      const TetStage& TS = s_tet[wid][i];
+      const TriStage& T = s_tri[wid][j];
+      double s[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) s[q] = plane64(T.n64, T.o64, TS.X[q][0], TS.X[q][1], TS.X[q][2]);
+      const bool allp = s[0] > kNearTol && s[1] > kNearTol && s[2] > kNearTol && s[3] > kNearTol;
+      const bool alln = s[0] < -kNearTol && s[1] < -kNearTol && s[2] < -kNearTol && s[3] < -kNearTol;
+      if (allp || alln) continue;
+      TetIn<float> t;
+      unstage_tet(TS, t);
+      const V3<float> n = mk(T.n[0], T.n[1], T.n[2]);
+      const V3<float> en[3] = {mk(T.en[0][0], T.en[0][1], T.en[0][2]), mk(T.en[1][0], T.en[1][1], T.en[1][2]),
+                               mk(T.en[2][0], T.en[2][1], T.en[2][2])};
+      PV<float, 3> poly[kMaxPolyV], tmp[kMaxPolyV];
+      Decide dc;
+      int anc = 0;
+      int nv = sr_polygon<float>(t, s, n, en, T.eo, fmaxf(T.M, t.xmax), T.h, T.Lt, dc, anc, poly, tmp);
+      const int tet_idx = P.s_elem_off + sl * kCluster + i;
+      float gint = 0.f;
+      int flags = 0;
+      if (dc.unc) {
+        bool near;
+        nv = sr_fp64(a, P, F, T, tet_idx, P.o_elem_off + oc * kCluster + j, s, anc, poly, near, gint);
+        flags = near ? 1 : 0;
+      } else if (nv >= 3) {
+        gint = dot(t.g, n);
+        if (fabsf(gint) <= 1e-5f * t.gl) gint = grad_along64(a, tet_idx, T.n64[0], T.n64[1], T.n64[2]);
+      }
+      if (nv < 3) continue;
+      ac.n_poly += 1;
+      ac.n_near += flags;
+      const V3<float> nc = n * sgn;
+      const float gM = P.s_is_m ? gint : INFINITY;
+      const float gN = P.s_is_m ? INFINITY : gint;
+      integrate_polygon<3>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN, t.g);
+      record<3>(a, it.x, poly, nv, t.X[anc], nc, TS.orig, T.orig, flags);
+    }
+    __syncwarp();
+    warp_reduce_store(a, ac, item, lane);
+  }
+}
+
+// ============================================================================
+// soft vs rigid half-space
+// ============================================================================
 template <class R>
 __device__ int hs_polygon(const TetIn<R>& t, const double s[4], V3<R> n, Decide& dc, int& anc, PV<R, 1>* out) {
   if (!(t.gl > (R)0)) return 0;
@@ -334,16 +627,101 @@ __device__ int hs_polygon(const TetIn<R>& t, const double s[4], V3<R> n, Decide&
   return tet_section(tv, s, dc, out);
 }
 
-// Soft tet of body B in A's frame.
-struct TetB {
-  double g64[3], c64;  // FP64 field in A's frame
-  float Y[4][3];
+__device__ __noinline__ int hs_fp64(const StepArgs& a, const FrameDev& F, int tet_idx, const double s[4], int& anc,
+                                    PV<float, 1>* poly, bool& near, float& gint) {
+  TetIn<double> td;
+  load_tet(a.tets, tet_idx, td);
+  tet_prepare(td);
+  const V3<double> nd = mk(F.R[2], F.R[5], F.R[8]);
+  Decide dd;
+  PV<double, 1> pd[kMaxPolyV];
+  const int nv = hs_polygon<double>(td, s, nd, dd, anc, pd);
+  to_f(pd, nv, poly);
+  near = dd.near;
+  gint = grad_noise_rule(dot(td.g, nd), td.gl);
+  return nv;
+}
+
+__global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
+  __shared__ TetStage s_tet[kNarrowWarps][kCluster];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  while (true) {
+    int ie;
+    const int item = next_item(a, 1, lane, ie);
+    if (item >= ie) break;
+    const int4 it = a.items[item];
+    const PairDev& P = a.pairs[it.x];
+    const FrameDev& F = a.frames[it.x];
+    Acc ac;
+    acc_zero(ac);
+    const int sl = it.y;
+    if (F.valid) stage_tet(a, P, sl * kCluster + lane, s_tet[wid][lane]);
+    else s_tet[wid][lane].valid = 0;
+    const double n64[3] = {F.R[2], F.R[5], F.R[8]};
+    const double o64 = F.R[2] * F.t[0] + F.R[5] * F.t[1] + F.R[8] * F.t[2];
+    const float nf[3] = {F.Rf[2], F.Rf[5], F.Rf[8]};
+    const float of = (float)o64;
+    // crossing tets, compacted
+    bool cand = false;
+    {
+      const TetStage& me = s_tet[wid][lane];
+      cand = me.valid && !one_sided32(me.X, nf, of, 4e-6f * (me.xmax + fabsf(of)));
+    }
+    const unsigned ballot = __ballot_sync(0xffffffffu, cand);
+    const int total = __popc(ballot);
+    const float sgn = P.s_is_m ? 1.f : -1.f;
+    if (lane < total) {
+      // the lane-th set bit of the ballot
+      unsigned m = ballot;
+      for (int r = 0; r < lane; ++r) m &= m - 1;
+      const int i = __ffs(m) - 1;
+      const TetStage& TS = s_tet[wid][i];
+      double s[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) s[q] = plane64(n64, o64, TS.X[q][0], TS.X[q][1], TS.X[q][2]);
+      TetIn<float> t;
+      unstage_tet(TS, t);
+      const V3<float> n = mk(nf[0], nf[1], nf[2]);
+      PV<float, 1> poly[kMaxPolyV];
+      Decide dc;
+      int anc = 0;
+      int nv = hs_polygon<float>(t, s, n, dc, anc, poly);
+      const int tet_idx = P.s_elem_off + sl * kCluster + i;
+      float gint = 0.f;
+      int flags = 0;
+      if (dc.unc) {
+        bool near;
+        nv = hs_fp64(a, F, tet_idx, s, anc, poly, near, gint);
+        flags = near ? 1 : 0;
+      } else if (nv >= 3) {
+        gint = dot(t.g, n);
+        if (fabsf(gint) <= 1e-5f * t.gl) gint = grad_along64(a, tet_idx, n64[0], n64[1], n64[2]);
+      }
+      if (nv >= 3) {
+        ac.n_poly += 1;
+        ac.n_near += flags;
+        const V3<float> nc = n * sgn;
+        const float gM = P.s_is_m ? gint : INFINITY;
+        const float gN = P.s_is_m ? INFINITY : gint;
+        integrate_polygon<1>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN, t.g);
+        record<1>(a, it.x, poly, nv, t.X[anc], nc, TS.orig, -1, flags);
+      }
+    }
+    __syncwarp();
+    warp_reduce_store(a, ac, item, lane);
+  }
+}
+
+// ============================================================================
+// soft-soft
+// ============================================================================
+struct TetBStage {
+  double g64[3], c64;  // FP64 field of the B tet in A's frame
   float g[3], gl;
   float pn[4][3], po[4];
   float lo[3], hi[3];
   float M, h, kappa;
-  int orig;
-  int valid;
+  int orig, valid;
 };
 
 // FP64 tet of B in A's frame with its field.
@@ -355,6 +733,45 @@ __device__ __forceinline__ void tetb_fp64(const StepArgs& a, const FrameDev& F, 
     t.P[k] = r.w;
   }
   tet_prepare(t);
+}
+
+__device__ __forceinline__ void stage_tetb(const StepArgs& a, const PairDev& P, const FrameDev& F, int tj,
+                                           TetBStage& S) {
+  S.valid = 0;
+  if (tj >= P.o_n_elem) return;
+  const int idx = P.o_elem_off + tj;
+  TetIn<double> bd;
+  tetb_fp64(a, F, idx, bd);
+  TetIn<float> tb;
+  float M = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float4 r = a.tets[4 * (size_t)idx + k];
+    M = fmaxf(M, amax(mk(r.x, r.y, r.z)));
+    tb.X[k] = mk((float)bd.X[k].x, (float)bd.X[k].y, (float)bd.X[k].z);
+    tb.P[k] = r.w;
+  }
+  M = fmaxf(M, fmaxf(fabsf(F.tf[0]), fmaxf(fabsf(F.tf[1]), fabsf(F.tf[2]))));
+  tet_prepare(tb);
+  V3<float> pn[4];
+  float po[4];
+  tet_planes(tb.X, pn, po);
+  S.g64[0] = bd.g.x; S.g64[1] = bd.g.y; S.g64[2] = bd.g.z; S.c64 = bd.c;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    S.pn[k][0] = pn[k].x; S.pn[k][1] = pn[k].y; S.pn[k][2] = pn[k].z;
+    S.po[k] = po[k];
+  }
+  S.g[0] = tb.g.x; S.g[1] = tb.g.y; S.g[2] = tb.g.z; S.gl = tb.gl;
+  const float pad = 1e-5f * M + 1e-7f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    S.lo[i] = fminf(fminf((&tb.X[0].x)[i], (&tb.X[1].x)[i]), fminf((&tb.X[2].x)[i], (&tb.X[3].x)[i])) - pad;
+    S.hi[i] = fmaxf(fmaxf((&tb.X[0].x)[i], (&tb.X[1].x)[i]), fmaxf((&tb.X[2].x)[i], (&tb.X[3].x)[i])) + pad;
+  }
+  S.M = M; S.h = tb.hmin; S.kappa = tb.kappa;
+  S.orig = a.tet_orig[idx];
+  S.valid = tb.hmin > 0.f && bd.hmin > 0.0 ? 1 : 0;
 }
 
 // Soft-soft polygon: tet A's section by p_A - p_B = 0 (FP64 values s),
@@ -398,326 +815,116 @@ __device__ int ss_polygon(const TetIn<R>& ta, const double s[4], V3<R> gb, R glb
   return nv;
 }
 
-// Gradient component along a face normal (P:356-359).  A component below
-// 1e-9 of |g| is rounding noise of a gradient perpendicular to the face and
-// counts as zero, so the face is skipped (P:361-368) deterministically; an
-// FP32 value within 1e-5 |g| of zero is re-evaluated in FP64 for that test.
-__device__ __forceinline__ float grad_noise_rule(double gi, double gl) {
-  return fabs(gi) < 1e-9 * gl ? 0.f : (float)gi;
-}
-
-__device__ __forceinline__ float grad_along(const StepArgs& a, int tet_idx, float g32, float gl32, const double* n64) {
-  if (fabsf(g32) > 1e-5f * gl32) return g32;
-  TetIn<double> td;
-  load_tet(a.tets, tet_idx, td);
+// FP64 pass of one soft-soft element pair: the exact-decision fallback
+// (`full`) or only the gradient components near zero.
+__device__ __noinline__ int ss_fp64(const StepArgs& a, const FrameDev& F, int ta_idx, int tb_idx, const double s[4],
+                                    bool full, int& anc, PV<float, 4>* poly, bool& near, V3<float>& nrm, float& gM,
+                                    float& gN, int nv_in) {
+  TetIn<double> td, tbd;
+  load_tet(a.tets, ta_idx, td);
   tet_prepare(td);
-  return grad_noise_rule(td.g.x * n64[0] + td.g.y * n64[1] + td.g.z * n64[2], td.gl);
-}
-
-__device__ __forceinline__ bool aabb_overlap(const float* alo, const float* ahi, const float* blo, const float* bhi) {
-  return alo[0] <= bhi[0] && ahi[0] >= blo[0] && alo[1] <= bhi[1] && ahi[1] >= blo[1] && alo[2] <= bhi[2] &&
-         ahi[2] >= blo[2];
-}
-
-template <int ND>
-__device__ __forceinline__ void to_f(const PV<double, ND>* in, int n, PV<float, ND>* out) {
-  for (int i = 0; i < n; ++i) {
-    out[i].x = (float)in[i].x; out[i].y = (float)in[i].y; out[i].z = (float)in[i].z; out[i].p = (float)in[i].p;
-#pragma unroll
-    for (int j = 0; j < ND; ++j) out[i].d[j] = (float)in[i].d[j];
+  tetb_fp64(a, F, tb_idx, tbd);
+  const V3<double> md = td.g - tbd.g;
+  const double lmd = norm(md);
+  near = false;
+  if (!(lmd > 0.0)) return 0;
+  const V3<double> nrmd = md * (1.0 / lmd);
+  int nv = nv_in;
+  if (full) {
+    V3<double> pnd[4];
+    double pod[4];
+    tet_planes(tbd.X, pnd, pod);
+    Decide dd;
+    PV<double, 4> pd[kMaxPolyV], tmp[kMaxPolyV];
+    nv = ss_polygon<double>(td, s, tbd.g, tbd.gl, nrmd, lmd, pnd, pod, 0.0, 1.0, 0.0, dd, anc, pd, tmp);
+    to_f(pd, nv, poly);
+    near = dd.near;
+    nrm = mk((float)nrmd.x, (float)nrmd.y, (float)nrmd.z);
   }
+  gM = grad_noise_rule(dot(td.g, nrmd), td.gl);
+  gN = grad_noise_rule(-dot(tbd.g, nrmd), tbd.gl);
+  return nv;
 }
 
-constexpr int kNarrowWarps = 4;
-
-__global__ void __launch_bounds__(128) narrow_kernel(StepArgs a) {
-  __shared__ union Stage {
-    TriData tri[kCluster];
-    TetB tetb[kCluster];
-  } s_stage[kNarrowWarps];
+__global__ void __launch_bounds__(128, 4) narrow_ss_kernel(StepArgs a) {
+  __shared__ TetBStage s_tb[kNarrowWarps][kCluster];
+  __shared__ TetStage s_tet[kNarrowWarps][kCluster];
+  __shared__ unsigned short s_q[kNarrowWarps][kCluster * kCluster];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int n_items = *a.item_total;
   while (true) {
-    int item = 0;
-    if (lane == 0) item = atomicAdd(a.item_next, 1);
-    item = __shfl_sync(0xffffffffu, item, 0);
-    if (item >= n_items) break;
+    int ie;
+    const int item = next_item(a, 2, lane, ie);
+    if (item >= ie) break;
     const int4 it = a.items[item];
-    PairCtx pc;
-    pc.pair = it.x;
-    pc.P = &a.pairs[it.x];
-    pc.F = &a.frames[it.x];
-    const PairDev& P = *pc.P;
-    const FrameDev& F = *pc.F;
+    const PairDev& P = a.pairs[it.x];
+    const FrameDev& F = a.frames[it.x];
     Acc ac;
-    for (int i = 0; i < 3; ++i) ac.F[i] = ac.T[i] = 0.f;
-    ac.area = ac.fn0 = 0.f;
-    ac.n_poly = ac.n_faces = ac.n_near = 0;
+    acc_zero(ac);
     const int sl = it.y, oc = it.z;
-    const int ti = sl * kCluster + lane;
-    const bool tvalid = ti < P.s_n_elem && F.valid;
-    TetIn<float> t;
-    float tlo[3], thi[3];
-    if (tvalid) {
-      load_tet(a.tets, P.s_elem_off + ti, t);
-      tet_prepare(t);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        const float lo = fminf(fminf((&t.X[0].x)[i], (&t.X[1].x)[i]), fminf((&t.X[2].x)[i], (&t.X[3].x)[i]));
-        const float hi = fmaxf(fmaxf((&t.X[0].x)[i], (&t.X[1].x)[i]), fmaxf((&t.X[2].x)[i], (&t.X[3].x)[i]));
-        const float pad = 1e-5f * (fabsf(lo) + fabsf(hi)) + 1e-7f;
-        tlo[i] = lo - pad;
-        thi[i] = hi + pad;
-      }
+    if (F.valid) {
+      stage_tetb(a, P, F, oc * kCluster + lane, s_tb[wid][lane]);
+      stage_tet(a, P, sl * kCluster + lane, s_tet[wid][lane]);
+    } else {
+      s_tb[wid][lane].valid = 0;
+      s_tet[wid][lane].valid = 0;
     }
-    const int torig = tvalid ? a.tet_orig[P.s_elem_off + ti] : -1;
-    const float sgn = P.s_is_m ? 1.f : -1.f;
-    if (P.query == 1) {
-      PV<float, 3> poly[kMaxPolyV], tmp[kMaxPolyV];
-      // ---- stage the rigid triangles of cluster oc in the soft frame ----
-      const int tj = oc * kCluster + lane;
-      TriData& S = s_stage[wid].tri[lane];
-      S.valid = 0;
-      if (tj < P.o_n_elem && F.valid) {
-        V3<double> Yd[3], nd, end[3];
-        double od, eod[3], hd, Ltd;
-        bool okd;
-        tri_fp64(a, F, P.o_elem_off + tj, Yd);
-        tri_planes(Yd, nd, od, end, eod, hd, Ltd, okd);
-        V3<float> Y[3], n, en[3];
-        float o, eo[3], h, Lt, M = 0.f;
-        bool ok;
-        for (int k = 0; k < 3; ++k) {
-          const float4 r = a.tris[3 * (size_t)(P.o_elem_off + tj) + k];
-          M = fmaxf(M, amax(mk(r.x, r.y, r.z)));
-          Y[k] = mk((float)Yd[k].x, (float)Yd[k].y, (float)Yd[k].z);
-        }
-        M = fmaxf(M, fmaxf(fabsf(F.tf[0]), fmaxf(fabsf(F.tf[1]), fabsf(F.tf[2]))));
-        tri_planes(Y, n, o, en, eo, h, Lt, ok);
-        S.n64[0] = nd.x; S.n64[1] = nd.y; S.n64[2] = nd.z; S.o64 = od;
-        for (int k = 0; k < 3; ++k) {
-          S.Y[k][0] = Y[k].x; S.Y[k][1] = Y[k].y; S.Y[k][2] = Y[k].z;
-          S.en[k][0] = en[k].x; S.en[k][1] = en[k].y; S.en[k][2] = en[k].z;
-          S.eo[k] = eo[k];
-        }
-        S.n[0] = n.x; S.n[1] = n.y; S.n[2] = n.z;
-        const float pad = 1e-5f * (M + Lt) + 1e-7f;
-        for (int i = 0; i < 3; ++i) {
-          S.lo[i] = fminf(fminf((&Y[0].x)[i], (&Y[1].x)[i]), (&Y[2].x)[i]) - pad;
-          S.hi[i] = fmaxf(fmaxf((&Y[0].x)[i], (&Y[1].x)[i]), (&Y[2].x)[i]) + pad;
-        }
-        S.M = M; S.h = h; S.Lt = Lt;
-        S.orig = a.tri_orig[P.o_elem_off + tj];
-        S.valid = okd && ok && h > 0.f ? 1 : 0;
-      }
-      __syncwarp();
+    __syncwarp();
+    unsigned mask = 0;
+    const TetStage& me = s_tet[wid][lane];
+    if (me.valid) {
       const int n_o = min(kCluster, P.o_n_elem - oc * kCluster);
       for (int j = 0; j < n_o; ++j) {
-        const TriData& T = s_stage[wid].tri[j];
-        if (!tvalid || !T.valid || !aabb_overlap(tlo, thi, T.lo, T.hi)) continue;
-        double s[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) s[k] = plane64(T.n64, T.o64, t.X[k].x, t.X[k].y, t.X[k].z);
-        // all four vertices strictly on one side: no section
-        const bool allp = s[0] > kNearTol && s[1] > kNearTol && s[2] > kNearTol && s[3] > kNearTol;
-        const bool alln = s[0] < -kNearTol && s[1] < -kNearTol && s[2] < -kNearTol && s[3] < -kNearTol;
-        if (allp || alln) continue;
-        const V3<float> n = mk(T.n[0], T.n[1], T.n[2]);
-        const V3<float> en[3] = {mk(T.en[0][0], T.en[0][1], T.en[0][2]), mk(T.en[1][0], T.en[1][1], T.en[1][2]),
-                                 mk(T.en[2][0], T.en[2][1], T.en[2][2])};
-        Decide dc;
-        int anc = 0;
-        int nv = sr_polygon<float>(t, s, n, en, T.eo, fmaxf(T.M, t.xmax), T.h, T.Lt, dc, anc, poly, tmp);
-        float gint = nv >= 3 ? grad_along(a, P.s_elem_off + ti, dot(t.g, n), t.gl, T.n64) : 0.f;
-        int flags = 0;
-        if (dc.unc) {
-          // exact-decision fallback in FP64 from the stored inputs
-          TetIn<double> td;
-          load_tet(a.tets, P.s_elem_off + ti, td);
-          tet_prepare(td);
-          V3<double> Yd[3], nd, end[3];
-          double od, eod[3], hd, Ltd;
-          bool okd;
-          tri_fp64(a, F, P.o_elem_off + oc * kCluster + j, Yd);
-          tri_planes(Yd, nd, od, end, eod, hd, Ltd, okd);
-          Decide dd;
-          PV<double, 3> pd[kMaxPolyV], td2[kMaxPolyV];
-          nv = okd ? sr_polygon<double>(td, s, nd, end, eod, 0.0, 1.0, 0.0, dd, anc, pd, td2) : 0;
-          to_f(pd, nv, poly);
-          if (dd.near) flags |= 1;
-          gint = grad_noise_rule(dot(td.g, nd), td.gl);
-        }
-        if (nv >= 3) {
-          ac.n_poly += 1;
-          ac.n_near += flags & 1;
-          const V3<float> nc = n * sgn;
-          const float gM = P.s_is_m ? gint : INFINITY;
-          const float gN = P.s_is_m ? INFINITY : gint;
-          integrate_polygon<3>(a, pc, ac, poly, nv, t.X[anc], nc, gM, gN);
-          record<3>(a, pc, poly, nv, t.X[anc], nc, torig, T.orig, flags);
-        }
+        const TetBStage& B = s_tb[wid][j];
+        if (B.valid && aabb_overlap(me.lo, me.hi, B.lo, B.hi)) mask |= 1u << j;
       }
-      __syncwarp();
-    } else if (P.query == 2) {
-      if (tvalid) {
-        PV<float, 1> poly[kMaxPolyV];
-        const double n64[3] = {F.R[2], F.R[5], F.R[8]};
-        const double o64 = F.R[2] * F.t[0] + F.R[5] * F.t[1] + F.R[8] * F.t[2];
-        double s[4];
+    }
+    const int total = build_queue(mask, s_q[wid], lane);
+    __syncwarp();
+    for (int base = 0; base < total; base += 32) {
+      const int k = base + lane;
+      if (k >= total) continue;
+      const int e = s_q[wid][k];
+      const int i = e & 31, j = e >> 5;
+      const TetStage& TS = s_tet[wid][i];
+      const TetBStage& B = s_tb[wid][j];
+      TetIn<float> t;
+      unstage_tet(TS, t);
+      const V3<float> gb = mk(B.g[0], B.g[1], B.g[2]);
+      const V3<float> m = t.g - gb;
+      const float lm = norm(m);
+      if (!(lm > 0.f) || !(t.gl > 0.f) || !(B.gl > 0.f)) continue;
+      double s[4];
+      const double il = 1.0 / (double)lm;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) s[k] = plane64(n64, o64, t.X[k].x, t.X[k].y, t.X[k].z);
-        const V3<float> n = mk(F.Rf[2], F.Rf[5], F.Rf[8]);
-        Decide dc;
-        int anc = 0;
-        int nv = hs_polygon<float>(t, s, n, dc, anc, poly);
-        float gint = nv >= 3 ? grad_along(a, P.s_elem_off + ti, dot(t.g, n), t.gl, n64) : 0.f;
-        int flags = 0;
-        if (dc.unc) {
-          TetIn<double> td;
-          load_tet(a.tets, P.s_elem_off + ti, td);
-          tet_prepare(td);
-          const V3<double> nd = mk(F.R[2], F.R[5], F.R[8]);
-          Decide dd;
-          PV<double, 1> pd[kMaxPolyV];
-          nv = hs_polygon<double>(td, s, nd, dd, anc, pd);
-          to_f(pd, nv, poly);
-          if (dd.near) flags |= 1;
-          gint = grad_noise_rule(dot(td.g, nd), td.gl);
-        }
-        if (nv >= 3) {
-          ac.n_poly += 1;
-          ac.n_near += flags & 1;
-          const V3<float> nc = n * sgn;
-          const float gM = P.s_is_m ? gint : INFINITY;
-          const float gN = P.s_is_m ? INFINITY : gint;
-          integrate_polygon<1>(a, pc, ac, poly, nv, t.X[anc], nc, gM, gN);
-          record<1>(a, pc, poly, nv, t.X[anc], nc, torig, -1, flags);
-        }
-      }
-    } else if (P.query == 3) {
+      for (int q = 0; q < 4; ++q)
+        s[q] = ((double)t.P[q] - (fma(B.g64[2], (double)t.X[q].z,
+                                      fma(B.g64[1], (double)t.X[q].y, B.g64[0] * (double)t.X[q].x)) +
+                                  B.c64)) * il;
+      const bool allp = s[0] > kNearTol && s[1] > kNearTol && s[2] > kNearTol && s[3] > kNearTol;
+      const bool alln = s[0] < -kNearTol && s[1] < -kNearTol && s[2] < -kNearTol && s[3] < -kNearTol;
+      if (allp || alln) continue;
+      const V3<float> pn[4] = {mk(B.pn[0][0], B.pn[0][1], B.pn[0][2]), mk(B.pn[1][0], B.pn[1][1], B.pn[1][2]),
+                               mk(B.pn[2][0], B.pn[2][1], B.pn[2][2]), mk(B.pn[3][0], B.pn[3][1], B.pn[3][2])};
+      V3<float> nrm = m * (1.f / lm);
       PV<float, 4> poly[kMaxPolyV], tmp[kMaxPolyV];
-      // ---- stage the B tets of cluster oc in A's (soft) frame ----
-      const int tj = oc * kCluster + lane;
-      TetB& S = s_stage[wid].tetb[lane];
-      S.valid = 0;
-      if (tj < P.o_n_elem && F.valid) {
-        TetIn<double> bd;
-        tetb_fp64(a, F, P.o_elem_off + tj, bd);
-        TetIn<float> tb;
-        float M = 0.f;
-        for (int k = 0; k < 4; ++k) {
-          const float4 r = a.tets[4 * (size_t)(P.o_elem_off + tj) + k];
-          M = fmaxf(M, amax(mk(r.x, r.y, r.z)));
-          tb.X[k] = mk((float)bd.X[k].x, (float)bd.X[k].y, (float)bd.X[k].z);
-          tb.P[k] = r.w;
-        }
-        M = fmaxf(M, fmaxf(fabsf(F.tf[0]), fmaxf(fabsf(F.tf[1]), fabsf(F.tf[2]))));
-        tet_prepare(tb);
-        V3<float> pn[4];
-        float po[4];
-        tet_planes(tb.X, pn, po);
-        S.g64[0] = bd.g.x; S.g64[1] = bd.g.y; S.g64[2] = bd.g.z; S.c64 = bd.c;
-        for (int k = 0; k < 4; ++k) {
-          S.Y[k][0] = tb.X[k].x; S.Y[k][1] = tb.X[k].y; S.Y[k][2] = tb.X[k].z;
-          S.pn[k][0] = pn[k].x; S.pn[k][1] = pn[k].y; S.pn[k][2] = pn[k].z;
-          S.po[k] = po[k];
-        }
-        S.g[0] = tb.g.x; S.g[1] = tb.g.y; S.g[2] = tb.g.z; S.gl = tb.gl;
-        const float pad = 1e-5f * M + 1e-7f;
-        for (int i = 0; i < 3; ++i) {
-          S.lo[i] = fminf(fminf((&tb.X[0].x)[i], (&tb.X[1].x)[i]), fminf((&tb.X[2].x)[i], (&tb.X[3].x)[i])) - pad;
-          S.hi[i] = fmaxf(fmaxf((&tb.X[0].x)[i], (&tb.X[1].x)[i]), fmaxf((&tb.X[2].x)[i], (&tb.X[3].x)[i])) + pad;
-        }
-        S.M = M; S.h = tb.hmin; S.kappa = tb.kappa;
-        S.orig = a.tet_orig[P.o_elem_off + tj];
-        S.valid = tb.hmin > 0.f && bd.hmin > 0.0 ? 1 : 0;
+      Decide dc;
+      int anc = 0;
+      int nv = ss_polygon<float>(t, s, gb, B.gl, nrm, lm, pn, B.po, B.M, B.h, B.kappa, dc, anc, poly, tmp);
+      float gM = dot(t.g, nrm), gN = -dot(gb, nrm);
+      int flags = 0;
+      const int ta_idx = P.s_elem_off + sl * kCluster + i, tb_idx = P.o_elem_off + oc * kCluster + j;
+      if (dc.unc || (nv >= 3 && (fabsf(gM) <= 1e-5f * t.gl || fabsf(gN) <= 1e-5f * B.gl))) {
+        bool near;
+        nv = ss_fp64(a, F, ta_idx, tb_idx, s, dc.unc, anc, poly, near, nrm, gM, gN, nv);
+        flags = near ? 1 : 0;
       }
-      __syncwarp();
-      const int n_o = min(kCluster, P.o_n_elem - oc * kCluster);
-      for (int j = 0; j < n_o; ++j) {
-        const TetB& B = s_stage[wid].tetb[j];
-        if (!tvalid || !B.valid || !aabb_overlap(tlo, thi, B.lo, B.hi)) continue;
-        const V3<float> gb = mk(B.g[0], B.g[1], B.g[2]);
-        const V3<float> m = t.g - gb;
-        const float lm = norm(m);
-        if (!(lm > 0.f) || !(t.gl > 0.f) || !(B.gl > 0.f)) continue;
-        double s[4];
-        const double il = 1.0 / (double)lm;
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-          s[k] = ((double)t.P[k] - (fma(B.g64[2], (double)t.X[k].z, fma(B.g64[1], (double)t.X[k].y,
-                                                                          B.g64[0] * (double)t.X[k].x)) +
-                                    B.c64)) * il;
-        const bool allp = s[0] > kNearTol && s[1] > kNearTol && s[2] > kNearTol && s[3] > kNearTol;
-        const bool alln = s[0] < -kNearTol && s[1] < -kNearTol && s[2] < -kNearTol && s[3] < -kNearTol;
-        if (allp || alln) continue;
-        const V3<float> pn[4] = {mk(B.pn[0][0], B.pn[0][1], B.pn[0][2]), mk(B.pn[1][0], B.pn[1][1], B.pn[1][2]),
-                                 mk(B.pn[2][0], B.pn[2][1], B.pn[2][2]), mk(B.pn[3][0], B.pn[3][1], B.pn[3][2])};
-        V3<float> nrm = m * (1.f / lm);
-        Decide dc;
-        int anc = 0;
-        int nv = ss_polygon<float>(t, s, gb, B.gl, nrm, lm, pn, B.po, B.M, B.h, B.kappa, dc, anc, poly, tmp);
-        float gM = dot(t.g, nrm), gN = -dot(gb, nrm);
-        int flags = 0;
-        if (!dc.unc && nv >= 3 && (fabsf(gM) <= 1e-5f * t.gl || fabsf(gN) <= 1e-5f * B.gl)) {
-          TetIn<double> td, tbd;
-          load_tet(a.tets, P.s_elem_off + ti, td);
-          tet_prepare(td);
-          tetb_fp64(a, F, P.o_elem_off + oc * kCluster + j, tbd);
-          const V3<double> md = td.g - tbd.g;
-          const V3<double> nrmd = md * (1.0 / norm(md));
-          gM = grad_noise_rule(dot(td.g, nrmd), td.gl);
-          gN = grad_noise_rule(-dot(tbd.g, nrmd), tbd.gl);
-        }
-        if (dc.unc) {
-          TetIn<double> td, tbd;
-          load_tet(a.tets, P.s_elem_off + ti, td);
-          tet_prepare(td);
-          tetb_fp64(a, F, P.o_elem_off + oc * kCluster + j, tbd);
-          V3<double> pnd[4];
-          double pod[4];
-          tet_planes(tbd.X, pnd, pod);
-          const V3<double> md = td.g - tbd.g;
-          const double lmd = norm(md);
-          Decide dd;
-          PV<double, 4> pd[kMaxPolyV], td2[kMaxPolyV];
-          nv = 0;
-          if (lmd > 0.0) {
-            const V3<double> nrmd = md * (1.0 / lmd);
-            nv = ss_polygon<double>(td, s, tbd.g, tbd.gl, nrmd, lmd, pnd, pod, 0.0, 1.0, 0.0, dd, anc, pd, td2);
-            if (nv >= 3) {
-              nrm = mk((float)nrmd.x, (float)nrmd.y, (float)nrmd.z);
-              gM = grad_noise_rule(dot(td.g, nrmd), td.gl);
-              gN = grad_noise_rule(-dot(tbd.g, nrmd), tbd.gl);
-            }
-          }
-          to_f(pd, nv, poly);
-          if (dd.near) flags |= 1;
-        }
-        if (nv >= 3) {
-          ac.n_poly += 1;
-          ac.n_near += flags & 1;
-          integrate_polygon<4>(a, pc, ac, poly, nv, t.X[anc], nrm, gM, gN);
-          record<4>(a, pc, poly, nv, t.X[anc], nrm, torig, B.orig, flags);
-        }
-      }
-      __syncwarp();
+      if (nv < 3) continue;
+      ac.n_poly += 1;
+      ac.n_near += flags;
+      integrate_polygon<4>(a, P, F, ac, poly, nv, t.X[anc], nrm, gM, gN, t.g);
+      record<4>(a, it.x, poly, nv, t.X[anc], nrm, TS.orig, B.orig, flags);
     }
-    // ---- deterministic warp reduction (FP64 butterfly) ----
-    double v[8] = {ac.F[0], ac.F[1], ac.F[2], ac.T[0], ac.T[1], ac.T[2], ac.area, ac.fn0};
-    int c3[3] = {ac.n_poly, ac.n_faces, ac.n_near};
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) {
-#pragma unroll
-      for (int i = 0; i < 8; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) c3[i] += __shfl_xor_sync(0xffffffffu, c3[i], o);
-    }
-    if (lane == 0) {
-      ItemOut r;
-      for (int i = 0; i < 8; ++i) r.v[i] = v[i];
-      r.n_poly = c3[0]; r.n_faces = c3[1]; r.n_near = c3[2]; r.pad = 0;
-      a.item_out[item] = r;
-    }
+    __syncwarp();
+    warp_reduce_store(a, ac, item, lane);
   }
 }
