@@ -385,6 +385,10 @@ __global__ void taxel_kernel(StepArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+cudaError_t init_kernel_attributes() {
+  return cudaFuncSetAttribute(narrow_sr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
+}
+
 int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   int n = 0;
   if (ev) cudaEventRecordWithFlags(ev[0], s, cudaEventRecordExternal);
@@ -401,7 +405,7 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   }
   if (ev) cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal);
   if (a.type_unit_end[0] > a.type_unit_begin[0]) {
-    narrow_sr_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
+    narrow_sr_kernel<<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a); ++n;
   }
   if (a.type_unit_end[1] > a.type_unit_begin[1]) {
     narrow_hs_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;

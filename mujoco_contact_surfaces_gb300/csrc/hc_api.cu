@@ -162,7 +162,7 @@ struct hc_context {
   int item_cap = 0;
   DevBuf<int> counters;  // see kCnt* below
   int type_units[3][2] = {{0, 0}, {0, 0}, {0, 0}};  // unit ranges per query type
-  DevBuf<double4> tri_plane;
+  DevBuf<hc::Dbl4> tri_plane, tri_edges;
   DevBuf<float4> tri_meta;
   DevBuf<hc::PairOut> pair_out;
   // sensors
@@ -208,7 +208,7 @@ hc_status build_pools(hc_context* c) {
   for (auto& kv : c->geoms) order.push_back(&kv.second);
   std::sort(order.begin(), order.end(), [](GeomHost* a, GeomHost* b) { return a->order < b->order; });
   std::vector<float4> tets, tris, tri_meta;
-  std::vector<double4> tri_plane;
+  std::vector<hc::Dbl4> tri_plane, tri_edges;
   std::vector<int> tet_orig, tri_orig;
   int node_total = 0;
   std::vector<int> s_eoff, s_ne, s_noff, s_L, r_eoff, r_ne, r_noff, r_L;
@@ -263,7 +263,17 @@ hc_status build_pools(hc_context* c) {
         }
         double n[3] = {0, 0, 1};
         if (ln > 0) n[0] = N[0] / ln, n[1] = N[1] / ln, n[2] = N[2] / ln;
-        tri_plane.push_back(make_double4(n[0], n[1], n[2], n[0] * r[0][0] + n[1] * r[0][1] + n[2] * r[0][2]));
+        tri_plane.push_back(hc::Dbl4{n[0], n[1], n[2], n[0] * r[0][0] + n[1] * r[0][1] + n[2] * r[0][2]});
+        // in-plane inward edge planes: unit n x (r_{j+1} - r_j), offset at r_j
+        for (int j = 0; j < 3; ++j) {
+          const double* a0 = r[j];
+          const double* a1 = r[(j + 1) % 3];
+          double e[3] = {a1[0] - a0[0], a1[1] - a0[1], a1[2] - a0[2]};
+          double m[3] = {n[1] * e[2] - n[2] * e[1], n[2] * e[0] - n[0] * e[2], n[0] * e[1] - n[1] * e[0]};
+          double lm = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+          if (lm > 0) m[0] /= lm, m[1] /= lm, m[2] /= lm;
+          tri_edges.push_back(hc::Dbl4{m[0], m[1], m[2], m[0] * a0[0] + m[1] * a0[1] + m[2] * a0[2]});
+        }
         tri_meta.push_back(make_float4(ln > 0 && le > 0 ? (float)(ln / le) : 0.f, (float)le, (float)mag, 0.f));
       }
       r_eoff.push_back(g->elem_off); r_ne.push_back(ne);
@@ -283,6 +293,7 @@ hc_status build_pools(hc_context* c) {
   HC_CUDA(c->tet_orig.upload(tet_orig, s));
   HC_CUDA(c->tri_orig.upload(tri_orig, s));
   HC_CUDA(c->tri_plane.upload(tri_plane, s));
+  HC_CUDA(c->tri_edges.upload(tri_edges, s));
   HC_CUDA(c->tri_meta.upload(tri_meta, s));
   // two float4 (lo, hi) per node
   HC_CUDA(c->nodes.reserve(2 * (size_t)std::max(1, node_total)));
@@ -440,6 +451,7 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
     a.type_unit_end[q] = c->type_units[q][1];
   }
   a.tri_plane = c->tri_plane.p;
+  a.tri_edges = c->tri_edges.p;
   a.tri_meta = c->tri_meta.p;
   a.item_out = c->item_out.p;
   a.pair_out = c->pair_out.p;
@@ -554,6 +566,7 @@ hc_status hc_context_create(const hc_config* cfg, hc_context** out) {
   if (e != cudaSuccess || ndev == 0) return fail(HC_ERR_NO_DEVICE, "no CUDA device visible");
   if (c0.device < 0 || c0.device >= ndev) return fail(HC_ERR_INVALID_ARG, "device ordinal out of range");
   HC_CUDA(cudaSetDevice(c0.device));
+  HC_CUDA(hc::init_kernel_attributes());
   hc_context* c = new hc_context();
   c->cfg = c0;
   c->device = c0.device;
@@ -580,7 +593,7 @@ hc_status hc_context_destroy(hc_context* c) {
   cudaStreamSynchronize(c->stream);
   invalidate_graph(c);
   c->tets.release(); c->tris.release(); c->nodes.release(); c->tet_orig.release(); c->tri_orig.release();
-  c->tri_plane.release(); c->tri_meta.release();
+  c->tri_plane.release(); c->tri_edges.release(); c->tri_meta.release();
   c->xpos.release(); c->xmat.release(); c->vel.release();
   c->pairs.release(); c->frames.release(); c->unit_pair.release(); c->unit_cl.release();
   c->unit_count.release(); c->unit_off.release(); c->block_sum.release(); c->items.release();

@@ -16,6 +16,11 @@
 
 namespace hc {
 
+// Four doubles, 32-byte aligned (one 32 B load).
+struct alignas(32) Dbl4 {
+  double x, y, z, w;
+};
+
 constexpr int kCluster = 32;       // elements per leaf cluster (one warp)
 constexpr int kMaxPolyV = 8;       // max vertices of a clipped polygon
 

@@ -20,7 +20,8 @@ struct StepArgs {
   const float4* tets;
   const int* tet_orig;
   const float4* tris;
-  const double4* tri_plane;   // body-frame unit normal and offset (FP64)
+  const Dbl4* tri_plane;   // body-frame unit normal and offset (FP64)
+  const Dbl4* tri_edges;   // 3 per triangle: body-frame edge planes (FP64)
   const float4* tri_meta;     // (min altitude, max edge, max |vertex|, 0)
   const int* tri_orig;
   const float4* nodes;
@@ -75,6 +76,9 @@ constexpr int kBpBlock = 256;
 void launch_refit(const float4* elems, int verts_per_elem, float4* nodes, const int* geom_elem_off,
                   const int* geom_n_elem, const int* geom_node_off, const int* geom_leaves,
                   int n_geoms, cudaStream_t s);
+
+// Kernel attributes (large dynamic shared memory); once per device.
+cudaError_t init_kernel_attributes();
 
 // One step: frames, broadphase, narrow phase, per-pair reduce, taxels.
 // Returns the number of kernels launched.

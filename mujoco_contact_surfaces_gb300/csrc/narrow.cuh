@@ -405,8 +405,10 @@ constexpr int kNarrowWarps = 4;
 // ============================================================================
 struct TriStage {
   double n64[3], o64;  // FP64 plane (unit normal out of the rigid body, offset)
+  double en64[3][3];   // FP64 in-plane inward edge planes
+  double eo64[3];
   float n[3], o;       // float copies
-  float en[3][3];      // in-plane inward edge normals (FP32)
+  float en[3][3];
   float eo[3];
   float lo[3], hi[3];
   float M, h, Lt;      // coordinate magnitude, min altitude, max edge
@@ -418,7 +420,7 @@ __device__ __forceinline__ void stage_tri(const StepArgs& a, const PairDev& P, c
   S.valid = 0;
   if (tj >= P.o_n_elem) return;
   const int idx = P.o_elem_off + tj;
-  const double4 pl = a.tri_plane[idx];
+  const Dbl4 pl = a.tri_plane[idx];
   const float4 meta = a.tri_meta[idx];
   // plane: n = R n_body, o = o_body + n . t (FP64)
   const V3<double> nd = mat_mul<double>(F.R, mk(pl.x, pl.y, pl.z));
@@ -432,14 +434,14 @@ __device__ __forceinline__ void stage_tri(const StepArgs& a, const PairDev& P, c
     const float4 r = a.tris[3 * (size_t)idx + k];
     Y[k] = mat_mul<float>(F.Rf, mk(r.x, r.y, r.z)) + mk(F.tf[0], F.tf[1], F.tf[2]);
   }
+  // edge planes: en = R en_body, eo = eo_body + en . t (FP64)
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
-    const V3<float> e = Y[j == 2 ? 0 : j + 1] - Y[j];
-    V3<float> m = cross(n, e);
-    const float lm = norm(m);
-    m = lm > 0.f ? m * (1.f / lm) : m;
-    S.en[j][0] = m.x; S.en[j][1] = m.y; S.en[j][2] = m.z;
-    S.eo[j] = dot(m, Y[j]);
+    const Dbl4 ep = a.tri_edges[3 * (size_t)idx + j];
+    const V3<double> m = mat_mul<double>(F.R, mk(ep.x, ep.y, ep.z));
+    const double eo = ep.w + m.x * F.t[0] + m.y * F.t[1] + m.z * F.t[2];
+    S.en64[j][0] = m.x; S.en64[j][1] = m.y; S.en64[j][2] = m.z; S.eo64[j] = eo;
+    S.en[j][0] = (float)m.x; S.en[j][1] = (float)m.y; S.en[j][2] = (float)m.z; S.eo[j] = (float)eo;
   }
   const float M = fmaxf(meta.z, fmaxf(fabsf(F.tf[0]), fmaxf(fabsf(F.tf[1]), fabsf(F.tf[2]))));
   const float pad = 1e-5f * (M + meta.y) + 1e-7f;
@@ -454,35 +456,58 @@ __device__ __forceinline__ void stage_tri(const StepArgs& a, const PairDev& P, c
 }
 
 // Soft-rigid polygon: tet section by the triangle plane (FP64 values s),
-// clipped by the three edge planes.
+// clipped by the three edge planes.  In FP32 an edge plane whose four tet
+// distances are all certainly positive is inactive (no clip); an active
+// plane's distances are evaluated in FP64 (its position matters to the
+// area), then carried in FP32 and interpolated with the vertices.
 template <class R>
-__device__ int sr_polygon(const TetIn<R>& t, const double s[4], V3<R> n, const V3<R> en[3], const R eo[3], R M,
-                          R h, R Lt, Decide& dc, int& anc, PV<R, 3>* out, PV<R, 3>* tmp) {
+__device__ int sr_polygon(const TetIn<R>& t, const double s[4], const TriStage& T, V3<R> n, R M, Decide& dc,
+                          int& anc, PV<R, 3>* out, PV<R, 3>* tmp) {
   if (!(t.gl > (R)0)) return 0;
   const R cg = dot(n, t.g) / t.gl;
-  check(dc, cg - (R)kCosAlphaD, (R)kFilt * ((R)1 + M / h + t.kappa));
+  check(dc, cg - (R)kCosAlphaD, (R)kFilt * ((R)1 + M / (R)T.h + t.kappa));
   if (!dc.unc && !(cg > (R)kCosAlphaD)) return 0;
   anc = nearest_vertex(s);
   PV<R, 3> tv[4];
   tet_local(t, anc, tv);
-  R dmax[3] = {0, 0, 0}, D = 0;
+  bool active[3];
+  R dmax[3];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    D = fmax(D, amax(t.X[k]));
+  for (int j = 0; j < 3; ++j) {
+    active[j] = true;
+    if (sizeof(R) == 4) {
+      const float tol = 4e-6f * ((float)t.xmax + fabsf(T.eo[j]));
+      bool all_in = true, all_out = true;
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      tv[k].d[j] = dot(en[j], t.X[k]) - eo[j];
-      dmax[j] = fmax(dmax[j], abs_r(tv[k].d[j]));
+      for (int k = 0; k < 4; ++k) {
+        const float d = T.en[j][0] * (float)t.X[k].x + T.en[j][1] * (float)t.X[k].y + T.en[j][2] * (float)t.X[k].z -
+                        T.eo[j];
+        tv[k].d[j] = (R)d;
+        all_in &= d > tol;
+        all_out &= d < -tol;
+      }
+      if (all_out) return 0;
+      active[j] = !all_in;
+    }
+    dmax[j] = 0;
+    if (active[j]) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        tv[k].d[j] = (R)(fma(T.en64[j][2], (double)t.X[k].z,
+                             fma(T.en64[j][1], (double)t.X[k].y, T.en64[j][0] * (double)t.X[k].x)) -
+                         T.eo64[j]);
+        dmax[j] = fmax(dmax[j], abs_r(tv[k].d[j]));
+      }
     }
   }
   int nv = tet_section(tv, s, dc, out);
   if (nv == 0) return 0;
-  const R tol_p = (R)kFilt * (M * ((R)1 + (D + Lt) / h) + D + Lt);
   PV<R, 3>* src = out;
   PV<R, 3>* dst = tmp;
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
-    nv = clip_dist(src, nv, j, tol_p + (R)kFiltRel * dmax[j], dc, dst);
+    if (!active[j]) continue;
+    nv = clip_dist(src, nv, j, (R)kFiltRel * dmax[j], dc, dst);
     PV<R, 3>* sw = src; src = dst; dst = sw;
     if (nv == 0) return 0;
   }
@@ -493,42 +518,32 @@ __device__ int sr_polygon(const TetIn<R>& t, const double s[4], V3<R> n, const V
 
 // Exact-decision fallback of one soft-rigid element pair in FP64 from the
 // stored inputs; returns the vertex count and sets near/gint.
-__device__ __noinline__ int sr_fp64(const StepArgs& a, const PairDev& P, const FrameDev& F, const TriStage& T,
-                                    int tet_idx, int tri_idx, const double s[4], int& anc, PV<float, 3>* poly,
-                                    bool& near, float& gint) {
+__device__ __noinline__ int sr_fp64(const StepArgs& a, const TriStage& T, int tet_idx, const double s[4], int& anc,
+                                    PV<float, 3>* poly, bool& near, float& gint) {
   TetIn<double> td;
   load_tet(a.tets, tet_idx, td);
   tet_prepare(td);
-  V3<double> Y[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float4 r = a.tris[3 * (size_t)tri_idx + k];
-    Y[k] = mat_mul<double>(F.R, mk<double>(r.x, r.y, r.z)) + mk(F.t[0], F.t[1], F.t[2]);
-  }
   const V3<double> n = mk(T.n64[0], T.n64[1], T.n64[2]);
-  V3<double> en[3];
-  double eo[3];
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    const V3<double> m = cross(n, Y[j == 2 ? 0 : j + 1] - Y[j]);
-    const double lm = norm(m);
-    en[j] = lm > 0.0 ? m * (1.0 / lm) : m;
-    eo[j] = dot(en[j], Y[j]);
-  }
   Decide dd;
   PV<double, 3> pd[kMaxPolyV], tmp[kMaxPolyV];
-  const int nv = sr_polygon<double>(td, s, n, en, eo, 0.0, 1.0, 0.0, dd, anc, pd, tmp);
+  const int nv = sr_polygon<double>(td, s, T, n, 0.0, dd, anc, pd, tmp);
   to_f(pd, nv, poly);
   near = dd.near;
   gint = grad_noise_rule(dot(td.g, n), td.gl);
   return nv;
 }
 
+// shared memory of one warp of the soft-rigid kernel
+struct SrWarpSmem {
+  TriStage tri[kCluster];
+  TetStage tet[kCluster];
+  unsigned short q[kCluster * kCluster];
+};
+
 __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
-  __shared__ TriStage s_tri[kNarrowWarps][kCluster];
-  __shared__ TetStage s_tet[kNarrowWarps][kCluster];
-  __shared__ unsigned short s_q[kNarrowWarps][kCluster * kCluster];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  SrWarpSmem& W = reinterpret_cast<SrWarpSmem*>(smem_raw)[wid];
   while (true) {
     int ie;
     const int item = next_item(a, 0, lane, ie);
@@ -540,36 +555,36 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
     acc_zero(ac);
     const int sl = it.y, oc = it.z;
     if (F.valid) {
-      stage_tri(a, P, F, oc * kCluster + lane, s_tri[wid][lane]);
-      stage_tet(a, P, sl * kCluster + lane, s_tet[wid][lane]);
+      stage_tri(a, P, F, oc * kCluster + lane, W.tri[lane]);
+      stage_tet(a, P, sl * kCluster + lane, W.tet[lane]);
     } else {
-      s_tri[wid][lane].valid = 0;
-      s_tet[wid][lane].valid = 0;
+      W.tri[lane].valid = 0;
+      W.tet[lane].valid = 0;
     }
     __syncwarp();
     // candidate queue
     unsigned mask = 0;
-    const TetStage& me = s_tet[wid][lane];
+    const TetStage& me = W.tet[lane];
     if (me.valid) {
       const int n_o = min(kCluster, P.o_n_elem - oc * kCluster);
       for (int j = 0; j < n_o; ++j) {
-        const TriStage& T = s_tri[wid][j];
+        const TriStage& T = W.tri[j];
         if (!T.valid || !aabb_overlap(me.lo, me.hi, T.lo, T.hi)) continue;
         const float margin = 4e-6f * (me.xmax + fabsf(T.o) + T.Lt);
         if (one_sided32(me.X, T.n, T.o, margin)) continue;
         mask |= 1u << j;
       }
     }
-    const int total = build_queue(mask, s_q[wid], lane);
+    const int total = build_queue(mask, W.q, lane);
     __syncwarp();
     const float sgn = P.s_is_m ? 1.f : -1.f;
     for (int base = 0; base < total; base += 32) {
       const int k = base + lane;
       if (k >= total) continue;
-      const int e = s_q[wid][k];
+      const int e = W.q[k];
       const int i = e & 31, j = e >> 5;
-      const TetStage& TS = s_tet[wid][i];
-      const TriStage& T = s_tri[wid][j];
+      const TetStage& TS = W.tet[i];
+      const TriStage& T = W.tri[j];
       double s[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) s[q] = plane64(T.n64, T.o64, TS.X[q][0], TS.X[q][1], TS.X[q][2]);
@@ -579,18 +594,16 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
       TetIn<float> t;
       unstage_tet(TS, t);
       const V3<float> n = mk(T.n[0], T.n[1], T.n[2]);
-      const V3<float> en[3] = {mk(T.en[0][0], T.en[0][1], T.en[0][2]), mk(T.en[1][0], T.en[1][1], T.en[1][2]),
-                               mk(T.en[2][0], T.en[2][1], T.en[2][2])};
       PV<float, 3> poly[kMaxPolyV], tmp[kMaxPolyV];
       Decide dc;
       int anc = 0;
-      int nv = sr_polygon<float>(t, s, n, en, T.eo, fmaxf(T.M, t.xmax), T.h, T.Lt, dc, anc, poly, tmp);
+      int nv = sr_polygon<float>(t, s, T, n, fmaxf(T.M, t.xmax), dc, anc, poly, tmp);
       const int tet_idx = P.s_elem_off + sl * kCluster + i;
       float gint = 0.f;
       int flags = 0;
       if (dc.unc) {
         bool near;
-        nv = sr_fp64(a, P, F, T, tet_idx, P.o_elem_off + oc * kCluster + j, s, anc, poly, near, gint);
+        nv = sr_fp64(a, T, tet_idx, s, anc, poly, near, gint);
         flags = near ? 1 : 0;
       } else if (nv >= 3) {
         gint = dot(t.g, n);
@@ -609,6 +622,9 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
     warp_reduce_store(a, ac, item, lane);
   }
 }
+
+constexpr size_t kSrSmemBytes = sizeof(SrWarpSmem) * kNarrowWarps;
+
 
 // ============================================================================
 // soft vs rigid half-space
