@@ -273,6 +273,17 @@ HC_API hc_status hc_get_taxels_device(hc_context* ctx, const float** d_taxels,
  * (M then N), dL_dE n_pair x 2 (M then N; 0 for a rigid geom).          */
 HC_API hc_status hc_adjoint(hc_context* ctx, const double* dL_dwrench, const float* dL_dtaxel,
                             double* dL_dpose, double* dL_dE);
+/* Keep each step's ray-sample hits for a following taxel adjoint (without
+ * this, hc_adjoint with dL_dtaxel re-runs the step once to recover them).  */
+HC_API hc_status hc_set_adjoint_mode(hc_context* ctx, int on);
+/* hc_adjoint on device buffers, asynchronous on the context stream.  The
+ * result is n_pair x 14 doubles: [dL/dtwist M (6), N (6), dL/dE_M, dL/dE_N],
+ * valid until the next adjoint.  A taxel adjoint needs adjoint mode on
+ * before the step.  Covers soft-rigid and half-space pairs.                */
+HC_API hc_status hc_adjoint_device(hc_context* ctx, const double* d_dL_dwrench, const float* d_dL_dtaxel,
+                                   const double** d_grad);
+/* Kernels the last adjoint launched. */
+HC_API hc_status hc_get_adjoint_launch_count(hc_context* ctx, int* n);
 
 /* ---- measurement --------------------------------------------------------*/
 typedef struct {

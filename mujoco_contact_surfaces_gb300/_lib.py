@@ -99,6 +99,9 @@ SIGNATURES = {
     "hc_get_taxels_all": (C.c_int, [_P, _fp, C.c_int64]),
     "hc_get_taxels_device": (C.c_int, [_P, C.POINTER(_P), C.POINTER(C.c_int64)]),
     "hc_adjoint": (C.c_int, [_P, _dp, _fp, _dp, _dp]),
+    "hc_set_adjoint_mode": (C.c_int, [_P, C.c_int]),
+    "hc_adjoint_device": (C.c_int, [_P, _P, _P, C.POINTER(_P)]),
+    "hc_get_adjoint_launch_count": (C.c_int, [_P, _ip]),
     "hc_enable_timing": (C.c_int, [_P, C.c_int]),
     "hc_get_timings": (C.c_int, [_P, C.POINTER(hc_timings)]),
     "hc_get_stream": (C.c_int, [_P, C.POINTER(_P)]),

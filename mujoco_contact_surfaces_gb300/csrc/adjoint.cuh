@@ -1,0 +1,631 @@
+// adjoint.cuh — reverse pass of the soft-rigid and half-space contact path
+// (included by contact.cu inside namespace hc, after narrow.cuh).
+//
+// The adjoint recomputes each item's contact polygons instead of storing
+// them.  Per polygon the geometry is differentiated forward-mode with six
+// tangents: the twist xi = (w, v) of the other body's points in the soft
+// frame (dY = w x Y + v).  The force law and the velocity field are
+// differentiated reverse-mode by hand.  Per lane the contributions to
+// dL/dxi, dL/dlin, dL/dang (the relative velocity field v = lin + ang x p of
+// the soft frame) and the taxel part of dL/dE are accumulated and reduced
+// per item in FP64, then per pair, where the chain rule maps them to the
+// world twists of both bodies.
+
+struct D6 {
+  float v;
+  float d[6];
+};
+
+__device__ __forceinline__ D6 d6c(float x) {
+  D6 r;
+  r.v = x;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) r.d[i] = 0.f;
+  return r;
+}
+__device__ __forceinline__ D6 operator+(const D6& a, const D6& b) {
+  D6 r;
+  r.v = a.v + b.v;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+__device__ __forceinline__ D6 operator-(const D6& a, const D6& b) {
+  D6 r;
+  r.v = a.v - b.v;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+__device__ __forceinline__ D6 operator-(const D6& a) {
+  D6 r;
+  r.v = -a.v;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) r.d[i] = -a.d[i];
+  return r;
+}
+__device__ __forceinline__ D6 operator*(const D6& a, const D6& b) {
+  D6 r;
+  r.v = a.v * b.v;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  return r;
+}
+__device__ __forceinline__ D6 operator*(const D6& a, float s) {
+  D6 r;
+  r.v = a.v * s;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) r.d[i] = a.d[i] * s;
+  return r;
+}
+__device__ __forceinline__ D6 operator/(const D6& a, const D6& b) {
+  D6 r;
+  const float ib = 1.f / b.v;
+  r.v = a.v * ib;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+  return r;
+}
+__device__ __forceinline__ D6 d6sqrt(const D6& a) {
+  D6 r;
+  r.v = sqrtf(a.v);
+  const float h = r.v > 0.f ? 0.5f / r.v : 0.f;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) r.d[i] = a.d[i] * h;
+  return r;
+}
+// a + t (b - a)
+__device__ __forceinline__ D6 d6lerp(const D6& a, const D6& b, const D6& t) { return a + t * (b - a); }
+
+struct V6 {
+  D6 x, y, z;
+};
+__device__ __forceinline__ V6 v6c(V3<float> a) { return V6{d6c(a.x), d6c(a.y), d6c(a.z)}; }
+__device__ __forceinline__ V6 operator+(const V6& a, const V6& b) { return V6{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V6 operator-(const V6& a, const V6& b) { return V6{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V6 operator*(const V6& a, const D6& s) { return V6{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ V6 operator*(const V6& a, float s) { return V6{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ D6 dot6(const V6& a, const V6& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V6 cross6(const V6& a, const V6& b) {
+  return V6{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ V3<float> val(const V6& a) { return mk(a.x.v, a.y.v, a.z.v); }
+
+// Polygon vertex with tangents: position (relative to the anchor), pressure
+// and up to three carried plane distances.
+struct PD {
+  V6 x;
+  D6 p;
+  D6 d[3];
+};
+
+__device__ __forceinline__ PD pd_lerp(const PD& a, const PD& b, const D6& t, int nd) {
+  PD o;
+  o.x = a.x + (b.x - a.x) * t;
+  o.p = d6lerp(a.p, b.p, t);
+  for (int j = 0; j < nd; ++j) o.d[j] = d6lerp(a.d[j], b.d[j], t);
+  return o;
+}
+
+// Section of a tet by s = 0 with tangents (signs from the FP64 values).
+__device__ __forceinline__ int tet_section_d(const PD tv[4], const double s64[4], const D6 s[4], int nd, PD* out) {
+  int pos = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) pos |= (s64[k] > 0.0) << k;
+  const int np = __popc(pos);
+  if (np == 0 || np == 4) return 0;
+  int ea[4], eb[4], n;
+  if (np == 1 || np == 3) {
+    const int single = np == 1 ? __ffs(pos) - 1 : __ffs(~pos & 0xF) - 1;
+    n = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k != single) { ea[n] = single; eb[n] = k; ++n; }
+  } else {
+    const int a = __ffs(pos) - 1, b = __ffs(pos & ~(1 << a)) - 1;
+    const int neg = ~pos & 0xF;
+    const int c = __ffs(neg) - 1, d = __ffs(neg & ~(1 << c)) - 1;
+    ea[0] = a; eb[0] = c;
+    ea[1] = a; eb[1] = d;
+    ea[2] = b; eb[2] = d;
+    ea[3] = b; eb[3] = c;
+    n = 4;
+  }
+  for (int i = 0; i < n; ++i) {
+    int a = ea[i], b = eb[i];
+    if (fabs(s64[a]) > fabs(s64[b])) { int t = a; a = b; b = t; }
+    out[i] = pd_lerp(tv[a], tv[b], s[a] / (s[a] - s[b]), nd);
+  }
+  return n;
+}
+
+__device__ __forceinline__ int clip_dist_d(const PD* in, int n, int j, int nd, PD* out) {
+  bool all_in = true;
+  for (int i = 0; i < n; ++i) all_in &= in[i].d[j].v >= 0.f;
+  if (all_in) {
+    for (int i = 0; i < n; ++i) out[i] = in[i];
+    return n;
+  }
+  int m = 0;
+  for (int i = 0; i < n; ++i) {
+    const int k = i + 1 == n ? 0 : i + 1;
+    const D6 di = in[i].d[j], dk = in[k].d[j];
+    const bool ii = di.v >= 0.f, ik = dk.v >= 0.f;
+    if (ii && m < kMaxPolyV) out[m++] = in[i];
+    if (ii != ik && m < kMaxPolyV)
+      out[m++] = fabsf(di.v) <= fabsf(dk.v) ? pd_lerp(in[i], in[k], di / (di - dk), nd)
+                                           : pd_lerp(in[k], in[i], dk / (dk - di), nd);
+  }
+  return m;
+}
+
+// Reverse of one quadrature point: accumulates into gx[6] the tangent
+// contraction of L = fbar . f (fbar = gF + gT x p) and into glin/gang the
+// velocity-field adjoints.  P.damping, P.mu as the forward.
+__device__ __forceinline__ void adj_zero(AdjAcc& g) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i) g.gx[i] = 0.f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) g.glin[i] = g.gang[i] = 0.f;
+  g.gE = 0.f;
+}
+
+__device__ void point_adjoint(AdjAcc& G, const FrameDev& F, float damping, float mu, const float* gF,
+                              const float* gT, const D6& A, const V6& p, const V6& n, const D6& gM, const D6& gN,
+                              const D6& p0) {
+  if (!(A.v > 1.0e-14f)) return;
+  if (gM.v < 1.0e-14f || gN.v < 1.0e-14f) return;
+  // forward values
+  const float gMv = gM.v, gNv = gN.v;
+  const float g = 1.0f / (1.0f / gMv + 1.0f / gNv);
+  const float fn0 = A.v * p0.v, k = A.v * g;
+  const V3<float> pv = val(p), nv = val(n);
+  const V3<float> lin = mk(F.lin[0], F.lin[1], F.lin[2]), ang = mk(F.ang[0], F.ang[1], F.ang[2]);
+  const V3<float> v = lin + cross(ang, pv);
+  const float vn = dot(v, nv);
+  const float h = 1.f - damping * vn, hp = fmaxf(0.f, h);
+  const float fnb = fn0 - 0.001f * k * vn;
+  const float fn = hp * fnb;
+  const V3<float> vt = v - nv * vn;
+  const float eps = (1.0e-4f * 1.0e-2f) * (1.0e-4f * 1.0e-2f);
+  const float vs = sqrtf(dot(vt, vt) + eps);
+  const float s = vs / 1.0e-4f;
+  const float mur = s < 1.f ? mu * s * (2.f - s) : mu;
+  const V3<float> u = vt * (1.f / vs);
+  const V3<float> q = nv - u * mur;
+  const V3<float> f = q * fn;
+  // upstream: fbar = gF + gT x p ; torque p x f also depends on p
+  const V3<float> gFv = mk(gF[0], gF[1], gF[2]), gTv = mk(gT[0], gT[1], gT[2]);
+  const V3<float> fbar = gFv + cross(gTv, pv);
+  // reverse
+  const float Lfn = dot(fbar, q);
+  const V3<float> qbar = fbar * fn;
+  V3<float> nbar = qbar;
+  const float murbar = -dot(qbar, u);
+  const V3<float> ubar = qbar * (-mur);
+  V3<float> vtbar = ubar * (1.f / vs);
+  float vsbar = -dot(ubar, vt) / (vs * vs);
+  vsbar += murbar * (s < 1.f ? mu * (2.f - 2.f * s) / 1.0e-4f : 0.f);
+  vtbar = vtbar + vt * (vsbar / vs);
+  // vt = v - n vn
+  V3<float> vbar = vtbar;
+  float vnbar = -dot(vtbar, nv);
+  nbar = nbar - vtbar * vn;
+  // fn = hp * (fn0 - 0.001 k vn)
+  const float hbar = h > 0.f ? Lfn * fnb : 0.f;
+  const float fn0bar = Lfn * hp;
+  const float kbar = -Lfn * hp * 0.001f * vn;
+  vnbar += -Lfn * hp * 0.001f * k - damping * hbar;
+  // vn = v . n
+  vbar = vbar + nv * vnbar;
+  nbar = nbar + v * vnbar;
+  // k = A g, fn0 = A p0
+  const float Abar = kbar * g + fn0bar * p0.v;
+  const float gbar = kbar * A.v;
+  const float p0bar = fn0bar * A.v;
+  const float gMbar = gbar * (g / gMv) * (g / gMv);
+  const float gNbar = gbar * (g / gNv) * (g / gNv);
+  // v = lin + ang x p
+  G.glin[0] += vbar.x; G.glin[1] += vbar.y; G.glin[2] += vbar.z;
+  const V3<float> angbar = cross(pv, vbar);
+  G.gang[0] += angbar.x; G.gang[1] += angbar.y; G.gang[2] += angbar.z;
+  V3<float> pbar = cross(vbar, ang) + cross(f, gTv);
+  // contraction with the geometric tangents
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    G.gx[i] += Abar * A.d[i] + p0bar * p0.d[i] + gMbar * gM.d[i] + gNbar * gN.d[i] + pbar.x * p.x.d[i] +
+               pbar.y * p.y.d[i] + pbar.z * p.z.d[i] + nbar.x * n.x.d[i] + nbar.y * n.y.d[i] + nbar.z * n.z.d[i];
+  }
+}
+
+// Quadrature of a tangent polygon with its reverse.
+__device__ void integrate_adjoint(AdjAcc& G, const StepArgs& a, const PairDev& P, const FrameDev& F, const float* gF,
+                                  const float* gT, const PD* v, int nv, V3<float> anc, const V6& n, const D6& gM,
+                                  const D6& gN) {
+  D6 A = d6c(0.f), pc = d6c(0.f);
+  V6 c = v6c(mk(0.f, 0.f, 0.f));
+  for (int i = 1; i + 1 < nv; ++i) {
+    const D6 ai = dot6(cross6(v[i].x - v[0].x, v[i + 1].x - v[0].x), n) * 0.5f;
+    A = A + ai;
+    c = c + (v[0].x + v[i].x + v[i + 1].x) * (ai * (1.f / 3.f));
+    pc = pc + ai * (v[0].p + v[i].p + v[i + 1].p) * (1.f / 3.f);
+  }
+  if (A.v == 0.f) return;
+  c = c * (d6c(1.f) / A);
+  pc = pc / A;
+  const V6 ancv = v6c(anc);
+  if (a.repr == 1) {
+    D6 Aabs = A.v < 0.f ? -A : A;
+    point_adjoint(G, F, P.damping, P.mu, gF, gT, Aabs, ancv + c, n, gM, gN, pc);
+  } else {
+    for (int i = 0; i < nv; ++i) {
+      const int j = i + 1 == nv ? 0 : i + 1;
+      const V6 cr = cross6(v[i].x - c, v[j].x - c);
+      const D6 Ai = d6sqrt(dot6(cr, cr)) * 0.5f;
+      const V6 cen = ancv + (c + v[i].x + v[j].x) * (1.f / 3.f);
+      const D6 p0 = pc * (1.f / 3.f) + v[i].p * (1.f / 3.f) + v[j].p * (1.f / 3.f);
+      point_adjoint(G, F, P.damping, P.mu, gF, gT, Ai, cen, n, gM, gN, p0);
+    }
+  }
+}
+
+__device__ __forceinline__ void adj_reduce_store(const StepArgs& a, const AdjAcc& G, int item, int lane) {
+  double v[13];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) v[i] = G.gx[i];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) v[6 + i] = G.glin[i], v[9 + i] = G.gang[i];
+  v[12] = G.gE;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1)
+#pragma unroll
+    for (int i = 0; i < 13; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+  if (lane == 0)
+#pragma unroll
+    for (int i = 0; i < 13; ++i) a.adj_item[(size_t)item * 16 + i] = v[i];
+}
+
+// Tangent plane distances of a tet vertex X to the plane (n, o) moving with
+// the other body: ds/dw = n x X, ds/dv = -n.
+__device__ __forceinline__ D6 plane_d6(float sval, V3<float> n, V3<float> X) {
+  D6 r;
+  r.v = sval;
+  const V3<float> c = cross(n, X);
+  r.d[0] = c.x; r.d[1] = c.y; r.d[2] = c.z;
+  r.d[3] = -n.x; r.d[4] = -n.y; r.d[5] = -n.z;
+  return r;
+}
+
+// Direction that rotates with the other body: d/dw_i = e_i x n.
+__device__ __forceinline__ V6 rot_dir6(V3<float> n) {
+  V6 r = v6c(n);
+  // e_0 x n = (0, -nz, ny); e_1 x n = (nz, 0, -nx); e_2 x n = (-ny, nx, 0)
+  r.x.d[1] = n.z; r.x.d[2] = -n.y;
+  r.y.d[0] = -n.z; r.y.d[2] = n.x;
+  r.z.d[0] = n.y; r.z.d[1] = -n.x;
+  return r;
+}
+
+__global__ void __launch_bounds__(128, 2) adjoint_sr_kernel(StepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  SrWarpSmem& W = reinterpret_cast<SrWarpSmem*>(smem_raw)[wid];
+  while (true) {
+    int ie;
+    const int item = next_item(a, 0, lane, ie);
+    if (item >= ie) break;
+    const int4 it = a.items[item];
+    const PairDev& P = a.pairs[it.x];
+    const FrameDev& F = a.frames[it.x];
+    const float* gF = a.adj_pair + 8 * (size_t)it.x;
+    const float* gT = gF + 3;
+    AdjAcc G;
+    adj_zero(G);
+    const int sl = it.y, oc = it.z;
+    if (F.valid) {
+      stage_tri(a, P, F, oc * kCluster + lane, W.tri[lane]);
+      stage_tet(a, P, sl * kCluster + lane, W.tet[lane]);
+    } else {
+      W.tri[lane].valid = 0;
+      W.tet[lane].valid = 0;
+    }
+    __syncwarp();
+    unsigned mask = 0;
+    const TetStage& me = W.tet[lane];
+    if (me.valid) {
+      const int n_o = min(kCluster, P.o_n_elem - oc * kCluster);
+      for (int j = 0; j < n_o; ++j) {
+        const TriStage& T = W.tri[j];
+        if (!T.valid || !aabb_overlap(me.lo, me.hi, T.lo, T.hi)) continue;
+        const float margin = 4e-6f * (me.xmax + fabsf(T.o) + T.Lt);
+        if (one_sided32(me.X, T.n, T.o, margin)) continue;
+        mask |= 1u << j;
+      }
+    }
+    const int total = build_queue(mask, W.q, lane);
+    __syncwarp();
+    const float sgn = P.s_is_m ? 1.f : -1.f;
+    for (int base = 0; base < total; base += 32) {
+      const int k = base + lane;
+      if (k >= total) continue;
+      const int e = W.q[k];
+      const int i = e & 31, j = e >> 5;
+      const TetStage& TS = W.tet[i];
+      const TriStage& T = W.tri[j];
+      double s[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) s[q] = plane64(T.n64, T.o64, TS.X[q][0], TS.X[q][1], TS.X[q][2]);
+      const bool allp = s[0] > kNearTol && s[1] > kNearTol && s[2] > kNearTol && s[3] > kNearTol;
+      const bool alln = s[0] < -kNearTol && s[1] < -kNearTol && s[2] < -kNearTol && s[3] < -kNearTol;
+      if (allp || alln) continue;
+      TetIn<float> t;
+      unstage_tet(TS, t);
+      const V3<float> n = mk(T.n[0], T.n[1], T.n[2]);
+      // forward polygon (the taxel keys must equal the forward's)
+      PV<float, 3> poly[kMaxPolyV];
+      Decide dc;
+      int anc = 0;
+      int nv = sr_poly_f(t, s, T, n, fmaxf(T.M, t.xmax), dc, anc, poly);
+      const int tet_idx = P.s_elem_off + sl * kCluster + i;
+      float gint = 0.f;
+      if (dc.unc) {
+        bool near;
+        nv = sr_fp64(a, T, tet_idx, s, anc, poly, near, gint);
+      } else if (nv >= 3) {
+        gint = dot(t.g, n);
+        if (fabsf(gint) <= 1e-5f * t.gl) gint = grad_along64(a, tet_idx, T.n64[0], T.n64[1], T.n64[2]);
+      }
+      if (nv < 3) continue;
+      // taxel adjoint on the forward polygon
+      if (a.adj_taxel) {
+        if (P.sensor0 >= 0)
+          raster_keys<3>(a, P.sensor0, F.Rl, F.tl, poly, nv, t.X[anc], t.g, n, a.sensors[P.sensor0].geom == P.gs,
+                         &G);
+        if (P.sensor1 >= 0)
+          raster_keys<3>(a, P.sensor1, F.Rl1, F.tl1, poly, nv, t.X[anc], t.g, n, a.sensors[P.sensor1].geom == P.gs,
+                         &G);
+      }
+      if (!a.adj_wrench || !a.apply_forces) continue;
+      // tangent polygon: section values and edge distances with tangents
+      D6 sd[4];
+      PD tv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        sd[q] = plane_d6((float)s[q], n, t.X[q]);
+        tv[q].x = v6c(t.X[q] - t.X[anc]);
+        tv[q].p = d6c(t.P[q]);
+      }
+      bool active[3];
+#pragma unroll
+      for (int jj = 0; jj < 3; ++jj) {
+        const V3<float> en = mk(T.en[jj][0], T.en[jj][1], T.en[jj][2]);
+        const float tol = 4e-6f * (t.xmax + fabsf(T.eo[jj]));
+        bool all_in = true;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const double d64 = fma(T.en64[jj][2], (double)t.X[q].z,
+                                 fma(T.en64[jj][1], (double)t.X[q].y, T.en64[jj][0] * (double)t.X[q].x)) -
+                             T.eo64[jj];
+          tv[q].d[jj] = plane_d6((float)d64, en, t.X[q]);
+          all_in &= en.x * t.X[q].x + en.y * t.X[q].y + en.z * t.X[q].z - T.eo[jj] > tol;
+        }
+        active[jj] = !all_in;
+      }
+      PD pa[kMaxPolyV], pb[kMaxPolyV];
+      int m = tet_section_d(tv, s, sd, 3, pa);
+      PD* src = pa;
+      PD* dst = pb;
+      for (int jj = 0; jj < 3 && m > 0; ++jj) {
+        if (!active[jj]) continue;
+        m = clip_dist_d(src, m, jj, 3, dst);
+        PD* sw = src; src = dst; dst = sw;
+      }
+      if (m < 3) continue;
+      const V6 nc = rot_dir6(n * sgn);
+      // gint = g . n_tri: d/dw = n x g
+      D6 gi = d6c(gint);
+      if (gint != 0.f) {
+        const V3<float> ng = cross(n, t.g);
+        gi.d[0] = ng.x; gi.d[1] = ng.y; gi.d[2] = ng.z;
+      }
+      const D6 inf = d6c(INFINITY);
+      integrate_adjoint(G, a, P, F, gF, gT, src, m, t.X[anc], nc, P.s_is_m ? gi : inf, P.s_is_m ? inf : gi);
+    }
+    __syncwarp();
+    adj_reduce_store(a, G, item, lane);
+  }
+}
+
+__global__ void __launch_bounds__(128, 4) adjoint_hs_kernel(StepArgs a) {
+  __shared__ TetStage s_tet[kNarrowWarps][kCluster];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  while (true) {
+    int ie;
+    const int item = next_item(a, 1, lane, ie);
+    if (item >= ie) break;
+    const int4 it = a.items[item];
+    const PairDev& P = a.pairs[it.x];
+    const FrameDev& F = a.frames[it.x];
+    const float* gF = a.adj_pair + 8 * (size_t)it.x;
+    const float* gT = gF + 3;
+    AdjAcc G;
+    adj_zero(G);
+    const int sl = it.y;
+    if (F.valid) stage_tet(a, P, sl * kCluster + lane, s_tet[wid][lane]);
+    else s_tet[wid][lane].valid = 0;
+    const double n64[3] = {F.R[2], F.R[5], F.R[8]};
+    const double o64 = F.R[2] * F.t[0] + F.R[5] * F.t[1] + F.R[8] * F.t[2];
+    const float nf[3] = {F.Rf[2], F.Rf[5], F.Rf[8]};
+    const float of = (float)o64;
+    bool cand;
+    {
+      const TetStage& me = s_tet[wid][lane];
+      cand = me.valid && !one_sided32(me.X, nf, of, 4e-6f * (me.xmax + fabsf(of)));
+    }
+    const unsigned ballot = __ballot_sync(0xffffffffu, cand);
+    const int total = __popc(ballot);
+    const float sgn = P.s_is_m ? 1.f : -1.f;
+    if (lane < total) {
+      unsigned msk = ballot;
+      for (int r = 0; r < lane; ++r) msk &= msk - 1;
+      const int i = __ffs(msk) - 1;
+      const TetStage& TS = s_tet[wid][i];
+      double s[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) s[q] = plane64(n64, o64, TS.X[q][0], TS.X[q][1], TS.X[q][2]);
+      TetIn<float> t;
+      unstage_tet(TS, t);
+      const V3<float> n = mk(nf[0], nf[1], nf[2]);
+      PV<float, 1> poly[kMaxPolyV];
+      Decide dc;
+      int anc = 0;
+      int nv = hs_poly_f(t, s, n, dc, anc, poly);
+      const int tet_idx = P.s_elem_off + sl * kCluster + i;
+      float gint = 0.f;
+      if (dc.unc) {
+        bool near;
+        nv = hs_fp64(a, F, tet_idx, s, anc, poly, near, gint);
+      } else if (nv >= 3) {
+        gint = dot(t.g, n);
+        if (fabsf(gint) <= 1e-5f * t.gl) gint = grad_along64(a, tet_idx, n64[0], n64[1], n64[2]);
+      }
+      if (nv >= 3) {
+        if (a.adj_taxel) {
+          if (P.sensor0 >= 0)
+            raster_keys<1>(a, P.sensor0, F.Rl, F.tl, poly, nv, t.X[anc], t.g, n,
+                           a.sensors[P.sensor0].geom == P.gs, &G);
+          if (P.sensor1 >= 0)
+            raster_keys<1>(a, P.sensor1, F.Rl1, F.tl1, poly, nv, t.X[anc], t.g, n,
+                           a.sensors[P.sensor1].geom == P.gs, &G);
+        }
+        if (a.adj_wrench && a.apply_forces) {
+          D6 sd[4];
+          PD tv[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            sd[q] = plane_d6((float)s[q], n, t.X[q]);
+            tv[q].x = v6c(t.X[q] - t.X[anc]);
+            tv[q].p = d6c(t.P[q]);
+          }
+          PD pa[4];
+          const int m = tet_section_d(tv, s, sd, 0, pa);
+          if (m >= 3) {
+            const V6 nc = rot_dir6(n * sgn);
+            D6 gi = d6c(gint);
+            if (gint != 0.f) {
+              const V3<float> ng = cross(n, t.g);
+              gi.d[0] = ng.x; gi.d[1] = ng.y; gi.d[2] = ng.z;
+            }
+            const D6 inf = d6c(INFINITY);
+            integrate_adjoint(G, a, P, F, gF, gT, pa, m, t.X[anc], nc, P.s_is_m ? gi : inf, P.s_is_m ? inf : gi);
+          }
+        }
+      }
+    }
+    __syncwarp();
+    adj_reduce_store(a, G, item, lane);
+  }
+}
+
+// Per pair: upstream adjoints of the soft-frame sums from dL/dwrench
+// (wrench = [R_S F_S ; R_S T_S + (x_S - x_M) x R_S F_S]).
+__global__ void adjoint_setup_kernel(StepArgs a) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.n_pair) return;
+  const FrameDev& F = a.frames[p];
+  float* o = a.adj_pair + 8 * (size_t)p;
+  if (!a.adj_wrench || !F.valid) {
+    for (int i = 0; i < 8; ++i) o[i] = 0.f;
+    return;
+  }
+  const double* w = a.adj_wrench + 6 * (size_t)p;
+  const V3<double> aF = mk(w[0], w[1], w[2]), aT = mk(w[3], w[4], w[5]);
+  const V3<double> r = mk(F.xS[0] - F.xM[0], F.xS[1] - F.xM[1], F.xS[2] - F.xM[2]);
+  const V3<double> gF = mat_tmul<double>(F.RS, aF + cross(aT, r));
+  const V3<double> gT = mat_tmul<double>(F.RS, aT);
+  o[0] = (float)gF.x; o[1] = (float)gF.y; o[2] = (float)gF.z;
+  o[3] = (float)gT.x; o[4] = (float)gT.y; o[5] = (float)gT.z;
+  o[6] = o[7] = 0.f;
+}
+
+// Per pair: sum of the item gradients (fixed order, FP64) and the chain rule
+// to the world twists of M and N, plus dL/dE.
+__global__ void adjoint_reduce_kernel(StepArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (p >= a.n_pair) return;
+  const PairDev& P = a.pairs[p];
+  const int total = *a.item_total;
+  const int b = min(a.unit_off[P.unit_begin], total), e = min(a.unit_off[P.unit_end], total);
+  double v[13];
+#pragma unroll
+  for (int k = 0; k < 13; ++k) v[k] = 0.0;
+  for (int i = b + lane; i < e; i += 32)
+#pragma unroll
+    for (int k = 0; k < 13; ++k) v[k] += a.adj_item[(size_t)i * 16 + k];
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < 13; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  if (lane) return;
+  double* out = a.adj_out + 14 * (size_t)p;   // [M twist 6, N twist 6, dE_M, dE_N]
+  for (int k = 0; k < 14; ++k) out[k] = 0.0;
+  const FrameDev& F = a.frames[p];
+  if (!F.valid || P.query == 0) return;
+  const V3<double> Gw = mk(v[0], v[1], v[2]), Gv = mk(v[3], v[4], v[5]);
+  const V3<double> Glin = mk(v[6], v[7], v[8]), Gang = mk(v[9], v[10], v[11]);
+  const V3<double> t = mk(F.t[0], F.t[1], F.t[2]);
+  // relative pose (other body in the soft frame)
+  V3<double> thO = mat_mul<double>(F.RS, Gw - cross(t, Gv));
+  V3<double> xO = mat_mul<double>(F.RS, Gv);
+  V3<double> thS = mat_mul<double>(F.RS, Gw) * -1.0;
+  V3<double> xS = xO * -1.0;
+  // velocity field: lin = R_S^T (c + w x x_S), ang = R_S^T w
+  const V3<double> lin = mk((double)F.lin[0], (double)F.lin[1], (double)F.lin[2]);
+  const V3<double> ang = mk((double)F.ang[0], (double)F.ang[1], (double)F.ang[2]);
+  thS = thS - mat_mul<double>(F.RS, cross(lin, Glin) + cross(ang, Gang));
+  const V3<double> RGl = mat_mul<double>(F.RS, Glin);
+  V3<double> wM = mk(0.0, 0.0, 0.0), wN = wM;
+  if (a.vel) {
+    wM = mk(a.vel[6 * (size_t)P.gm], a.vel[6 * (size_t)P.gm + 1], a.vel[6 * (size_t)P.gm + 2]);
+    wN = mk(a.vel[6 * (size_t)P.gn], a.vel[6 * (size_t)P.gn + 1], a.vel[6 * (size_t)P.gn + 2]);
+  }
+  const V3<double> w = wM - wN;
+  xS = xS + cross(RGl, w);
+  V3<double> xM = cross(wM, RGl);
+  V3<double> xN = cross(RGl, wN);
+  // world wrench transform
+  if (a.adj_wrench) {
+    const double* aw = a.adj_wrench + 6 * (size_t)p;
+    const V3<double> aF = mk(aw[0], aw[1], aw[2]), aT = mk(aw[3], aw[4], aw[5]);
+    const PairOut& po = a.pair_out[p];
+    const V3<double> FW = mk(po.wrench[0], po.wrench[1], po.wrench[2]);
+    const V3<double> TW = mk(po.wrench[3], po.wrench[4], po.wrench[5]);
+    const V3<double> r = mk(F.xS[0] - F.xM[0], F.xS[1] - F.xM[1], F.xS[2] - F.xM[2]);
+    const V3<double> TWs = TW - cross(r, FW);
+    thS = thS + cross(FW, aF) + cross(TWs, aT) + cross(FW, cross(aT, r));
+    xS = xS + cross(FW, aT);
+    xM = xM + cross(aT, FW);
+  }
+  // assemble per body (M first)
+  double* gm = out;
+  double* gn = out + 6;
+  const bool sm = P.s_is_m;
+  double* gs = sm ? gm : gn;
+  double* go = sm ? gn : gm;
+  gs[0] += thS.x; gs[1] += thS.y; gs[2] += thS.z; gs[3] += xS.x; gs[4] += xS.y; gs[5] += xS.z;
+  go[0] += thO.x; go[1] += thO.y; go[2] += thO.z; go[3] += xO.x; go[4] += xO.y; go[5] += xO.z;
+  gm[3] += xM.x; gm[4] += xM.y; gm[5] += xM.z;
+  gn[3] += xN.x; gn[4] += xN.y; gn[5] += xN.z;
+  // modulus: soft-rigid / half-space wrench and taxels are linear in E_s
+  if (P.query != 3 && P.E_s > 0.f) {
+    double dE = v[12];
+    if (a.adj_wrench) {
+      const double* aw = a.adj_wrench + 6 * (size_t)p;
+      const PairOut& po = a.pair_out[p];
+      for (int k = 0; k < 6; ++k) dE += aw[k] * po.wrench[k];
+    }
+    dE /= (double)P.E_s;
+    out[12 + (sm ? 0 : 1)] = dE;
+  }
+}

@@ -311,6 +311,7 @@ __global__ void bp_emit_kernel(StepArgs a) {
 }
 
 #include "narrow.cuh"
+#include "adjoint.cuh"
 
 // ---------------------------------------------------------------------------
 // per-pair reduction (fixed order, FP64) and the world-frame wrench
@@ -377,7 +378,7 @@ __global__ void taxel_kernel(StepArgs a) {
         float pr = __uint_as_float((unsigned)(k & 0xffffffffu));
         float raw = pr * S.rmean;
         avg += w[i * S.sr + j] * raw;
-        smp[(size_t)X * S.ny + Y] = ~0ull;
+        if (!a.keep_samples) smp[(size_t)X * S.ny + Y] = ~0ull;
       }
     }
   }
@@ -386,7 +387,29 @@ __global__ void taxel_kernel(StepArgs a) {
 
 // ---------------------------------------------------------------------------
 cudaError_t init_kernel_attributes() {
-  return cudaFuncSetAttribute(narrow_sr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
+  cudaError_t e = cudaFuncSetAttribute(narrow_sr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(adjoint_sr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
+}
+
+// Work counters of the adjoint pass reuse the narrow-phase ones.
+__global__ void reset_next_kernel(StepArgs a) {
+  if (threadIdx.x < 3) a.item_next[threadIdx.x] = 0;
+}
+
+int launch_adjoint(const StepArgs& a, cudaStream_t s) {
+  int n = 0;
+  if (a.n_pair <= 0) return 0;
+  reset_next_kernel<<<1, 32, 0, s>>>(a); ++n;
+  adjoint_setup_kernel<<<(a.n_pair + 127) / 128, 128, 0, s>>>(a); ++n;
+  if (a.type_unit_end[0] > a.type_unit_begin[0]) {
+    adjoint_sr_kernel<<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a); ++n;
+  }
+  if (a.type_unit_end[1] > a.type_unit_begin[1]) {
+    adjoint_hs_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
+  }
+  adjoint_reduce_kernel<<<(a.n_pair * 32 + 127) / 128, 128, 0, s>>>(a); ++n;
+  return n;
 }
 
 int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {

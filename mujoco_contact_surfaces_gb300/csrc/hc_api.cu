@@ -190,6 +190,12 @@ struct hc_context {
   int launches_per_step = 0;
   int narrow_block = 128, narrow_ctas_per_sm = 8;
   int n_sm = 0;
+  // adjoint
+  bool adjoint_mode = false;   // steps keep the won taxel samples
+  bool samples_dirty = false;  // the sample buffer holds a kept step's hits
+  DevBuf<float> adj_pair, adj_taxel;
+  DevBuf<double> adj_item, adj_out, adj_wrench;
+  int adj_launches = 0;
 };
 
 namespace {
@@ -475,6 +481,7 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
   a.want_pair = want_pair;
   a.narrow_block = c->narrow_block;
   a.narrow_grid = std::max(1, c->n_sm * c->narrow_ctas_per_sm);
+  a.keep_samples = c->adjoint_mode ? 1 : 0;
   return a;
 }
 
@@ -486,6 +493,12 @@ hc_status run_step(hc_context* c, int want_polys, int want_pair) {
   }
   hc::StepArgs a = make_args(c, want_polys, want_pair);
   HC_CUDA(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(int), c->stream));
+  // samples kept by an earlier step and not consumed by an adjoint
+  if (c->samples_dirty && c->samples.n) {
+    HC_CUDA(cudaMemsetAsync(c->samples.p, 0xFF, c->samples.n * sizeof(unsigned long long), c->stream));
+    c->samples_dirty = false;
+  }
+  if (c->adjoint_mode && c->n_cells > 0) c->samples_dirty = true;
   // With timing on, event records between the stages are part of the
   // launch sequence (and of the captured graph).
   cudaEvent_t* ev = c->timing && !want_polys ? c->ev : nullptr;
@@ -600,6 +613,8 @@ hc_status hc_context_destroy(hc_context* c) {
   c->item_out.release(); c->counters.release(); c->pair_out.release(); c->sensors_d.release();
   c->samples.release(); c->taxels.release(); c->weights.release(); c->samp_coord.release();
   c->cell_sensor.release(); c->cell_first.release(); c->cand.release(); c->polys.release();
+  c->adj_pair.release(); c->adj_taxel.release(); c->adj_item.release(); c->adj_out.release();
+  c->adj_wrench.release();
   for (auto& ev : c->ev) cudaEventDestroy(ev);
   cudaStreamDestroy(c->stream);
   delete c;
@@ -1177,11 +1192,102 @@ hc_status hc_autotune(hc_context* c, int* chosen_block, int* chosen_ctas_per_sm)
   return HC_OK;
 }
 
+hc_status hc_set_adjoint_mode(hc_context* c, int on) {
+  if (hc_status st = need(c)) return st;
+  if ((on != 0) != c->adjoint_mode) invalidate_graph(c);
+  c->adjoint_mode = on != 0;
+  return HC_OK;
+}
+
+// Launch the adjoint on device inputs; leaves n_pair x 14 doubles in adj_out.
+static hc_status adjoint_launch(hc_context* c, const double* d_dw, const float* d_dt) {
+  for (const auto& p : c->pairs_h)
+    if (p.query == HC_QUERY_SOFT_SOFT) return fail(HC_ERR_UNSUPPORTED, "the adjoint covers soft-rigid and half-space pairs");
+  if (!c->stepped) return fail(HC_ERR_NOT_READY, "no step has run");
+  HC_CUDA(cudaSetDevice(c->device));
+  const int n_pair = (int)c->pairs_h.size();
+  HC_CUDA(c->adj_pair.reserve(8 * (size_t)std::max(1, n_pair)));
+  HC_CUDA(c->adj_out.reserve(14 * (size_t)std::max(1, n_pair)));
+  HC_CUDA(c->adj_item.reserve(16 * (size_t)std::max(1, c->item_cap)));
+  hc::StepArgs a = make_args(c, 0, -1);
+  a.adj_wrench = d_dw;
+  a.adj_taxel = d_dt && c->n_cells > 0 ? d_dt : nullptr;
+  a.adj_pair = c->adj_pair.p;
+  a.adj_item = c->adj_item.p;
+  a.adj_out = c->adj_out.p;
+  c->adj_launches = hc::launch_adjoint(a, c->stream);
+  HC_CUDA(cudaGetLastError());
+  // the taxel adjoint claims (and clears) every won sample
+  if (a.adj_taxel) c->samples_dirty = false;
+  return HC_OK;
+}
+
+// Make sure the last step's won samples are available for a taxel adjoint.
+static hc_status ensure_kept_samples(hc_context* c) {
+  if (hc_status st = finish_step(c)) return st;
+  if (c->samples_dirty || c->n_cells == 0) return HC_OK;
+  bool was = c->adjoint_mode;
+  c->adjoint_mode = true;
+  invalidate_graph(c);
+  hc_status st = run_step(c, 0, -1);
+  c->adjoint_mode = was;
+  invalidate_graph(c);
+  if (st) return st;
+  return finish_step(c);
+}
+
 hc_status hc_adjoint(hc_context* c, const double* dL_dwrench, const float* dL_dtaxel, double* dL_dpose,
                      double* dL_dE) {
   if (hc_status st = need(c)) return st;
-  (void)dL_dwrench; (void)dL_dtaxel; (void)dL_dpose; (void)dL_dE;
-  return fail(HC_ERR_UNSUPPORTED, "adjoint not built yet");
+  if (!c->stepped) return fail(HC_ERR_NOT_READY, "no step has run");
+  HC_CUDA(cudaSetDevice(c->device));
+  const int n_pair = (int)c->pairs_h.size();
+  if (dL_dtaxel) {
+    if (hc_status st = ensure_kept_samples(c)) return st;
+  } else if (hc_status st = finish_step(c)) {
+    return st;
+  }
+  const double* d_dw = nullptr;
+  const float* d_dt = nullptr;
+  if (dL_dwrench && n_pair) {
+    HC_CUDA(c->adj_wrench.reserve(6 * (size_t)n_pair));
+    HC_CUDA(cudaMemcpyAsync(c->adj_wrench.p, dL_dwrench, 6 * (size_t)n_pair * sizeof(double), cudaMemcpyHostToDevice,
+                            c->stream));
+    d_dw = c->adj_wrench.p;
+  }
+  if (dL_dtaxel && c->n_cells) {
+    HC_CUDA(c->adj_taxel.reserve(c->n_cells));
+    HC_CUDA(cudaMemcpyAsync(c->adj_taxel.p, dL_dtaxel, (size_t)c->n_cells * sizeof(float), cudaMemcpyHostToDevice,
+                            c->stream));
+    d_dt = c->adj_taxel.p;
+  }
+  if (hc_status st = adjoint_launch(c, d_dw, d_dt)) return st;
+  std::vector<double> out(14 * (size_t)std::max(1, n_pair));
+  if (n_pair)
+    HC_CUDA(cudaMemcpyAsync(out.data(), c->adj_out.p, 14 * (size_t)n_pair * sizeof(double), cudaMemcpyDeviceToHost,
+                            c->stream));
+  HC_CUDA(cudaStreamSynchronize(c->stream));
+  for (int p = 0; p < n_pair; ++p) {
+    if (dL_dpose) memcpy(dL_dpose + 12 * (size_t)p, &out[14 * (size_t)p], 12 * sizeof(double));
+    if (dL_dE) dL_dE[2 * p] = out[14 * (size_t)p + 12], dL_dE[2 * p + 1] = out[14 * (size_t)p + 13];
+  }
+  return HC_OK;
+}
+
+hc_status hc_adjoint_device(hc_context* c, const double* d_dL_dwrench, const float* d_dL_dtaxel,
+                            const double** d_grad) {
+  if (hc_status st = need(c)) return st;
+  if (d_dL_dtaxel && !c->samples_dirty && c->n_cells > 0)
+    return fail(HC_ERR_NOT_READY, "taxel adjoint needs hc_set_adjoint_mode(ctx, 1) before the step");
+  if (hc_status st = adjoint_launch(c, d_dL_dwrench, d_dL_dtaxel)) return st;
+  if (d_grad) *d_grad = c->adj_out.p;
+  return HC_OK;
+}
+
+hc_status hc_get_adjoint_launch_count(hc_context* c, int* n) {
+  if (hc_status st = need(c)) return st;
+  if (n) *n = c->adj_launches;
+  return HC_OK;
 }
 
 }  // extern "C"

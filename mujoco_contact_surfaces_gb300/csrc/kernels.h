@@ -68,6 +68,13 @@ struct StepArgs {
   // launch shape of the narrow phase
   int narrow_block;
   int narrow_grid;
+  // adjoint
+  int keep_samples;          // taxel pass leaves the won samples for the adjoint
+  const double* adj_wrench;  // dL/dwrench, n_pair x 6 (device) or null
+  const float* adj_taxel;    // dL/dtaxel, all cells (device) or null
+  float* adj_pair;           // per pair: dL/dF_S, dL/dT_S in the soft frame (8 floats)
+  double* adj_item;          // per item: 13 gradient sums (stride 16)
+  double* adj_out;           // per pair: [dL/dtwist M (6), N (6), dL/dE_M, dL/dE_N]
 };
 
 constexpr int kBpBlock = 256;
@@ -84,7 +91,8 @@ cudaError_t init_kernel_attributes();
 // Returns the number of kernels launched.
 int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev /* 6 or null */);
 
-// Adjoint kernels (adjoint.cu).
-struct AdjArgs;
+// Adjoint of the last step (soft-rigid and half-space pairs).  Returns the
+// number of kernels launched.
+int launch_adjoint(const StepArgs& a, cudaStream_t s);
 
 }  // namespace hc

@@ -62,9 +62,21 @@ __device__ __forceinline__ void point_force(Acc& ac, const FrameDev& F, float da
 // field there.  Polygons whose projection is degenerate (|2A| < 1e-10, the
 // test's parallel threshold) are skipped.  Each sample keeps the smallest t
 // packed with the pressure by a 64-bit atomicMin (order independent).
+//
+// The same compiled function serves the adjoint (G != null): a sample this
+// polygon won in the forward pass (bit-identical key) is claimed with a CAS
+// that also clears it, and dL/dp at the hit is added to G.
+struct AdjAcc {
+  float gx[6];     // dL/dxi: twist (w, v) of the other body in the soft frame
+  float glin[3];   // dL/dlin of the velocity field v = lin + ang x p
+  float gang[3];   // dL/dang
+  float gE;        // sum of dL/dp * p over won samples (taxel part of dL/dE * E)
+};
+
 template <int ND>
-__device__ void raster_polygon(const StepArgs& a, int sid, const float* Rl, const float* tl, const PV<float, ND>* v,
-                               int nv, V3<float> anc, V3<float> g_soft) {
+__device__ __noinline__ void raster_keys(const StepArgs& a, int sid, const float* Rl, const float* tl,
+                                         const PV<float, ND>* v, int nv, V3<float> anc, V3<float> g_soft,
+                                         V3<float> n_tri, int soft_is_sensor, AdjAcc* G) {
   const SensorDev S = a.sensors[sid];
   const V3<float> T = mk(tl[0], tl[1], tl[2]);
   float lx[kMaxPolyV], ly[kMaxPolyV], lz[kMaxPolyV];
@@ -125,7 +137,34 @@ __device__ void raster_polygon(const StepArgs& a, int sid, const float* Rl, cons
       const float pr = p0 + px * ddx + py * ddy;
       const unsigned long long key =
           ((unsigned long long)__float_as_uint(t) << 32) | (unsigned long long)__float_as_uint(pr);
-      atomicMin(&smp[(size_t)X * S.ny + Y], key);
+      const size_t si = (size_t)X * S.ny + Y;
+      if (!G) {
+        atomicMin(&smp[si], key);
+        continue;
+      }
+      if (atomicCAS(&smp[si], key, ~0ull) != key) continue;
+      // dL/dp at this sample: cell (X / sr, Y / sr), window weight of (X % sr, Y % sr)
+      const float w = a.weights[S.weight_off + (X % S.sr) * S.sr + (Y % S.sr)];
+      const float pbar = a.adj_taxel[S.taxel_off + X / S.sr + S.cy * (Y / S.sr)] * w * S.rmean;
+      if (pbar == 0.f) continue;
+      G->gE += pbar * pr;
+      const V3<float> xs = mat_tmul<float>(Rl, mk(qx, qy, z) - T);   // hit point, soft frame
+      if (!soft_is_sensor) {
+        // rays and plane move with the other body: dp = g . (w x x + v)
+        const V3<float> wx = cross(xs, g_soft);
+        G->gx[0] += pbar * wx.x; G->gx[1] += pbar * wx.y; G->gx[2] += pbar * wx.z;
+        G->gx[3] += pbar * g_soft.x; G->gx[4] += pbar * g_soft.y; G->gx[5] += pbar * g_soft.z;
+      } else {
+        // rays fixed in the soft frame, plane n.x = o moving: dx = dt D,
+        // dt = -(w.(n x x) - n.v) / (n.D), D = -(sensor z) in the soft frame
+        const V3<float> D = mk(-Rl[6], -Rl[7], -Rl[8]);
+        const float nD = dot(n_tri, D);
+        if (!(fabsf(nD) > 0.f)) continue;
+        const float r = -dot(g_soft, D) / nD;
+        const V3<float> nx = cross(n_tri, xs);
+        G->gx[0] += pbar * r * nx.x; G->gx[1] += pbar * r * nx.y; G->gx[2] += pbar * r * nx.z;
+        G->gx[3] -= pbar * r * n_tri.x; G->gx[4] -= pbar * r * n_tri.y; G->gx[5] -= pbar * r * n_tri.z;
+      }
     }
   }
 }
@@ -170,8 +209,8 @@ __device__ void integrate_polygon(const StepArgs& a, const PairDev& P, const Fra
       point_force(ac, F, P.damping, P.mu, a.apply_forces, Ai, cen, n, gM, gN, p0);
     }
   }
-  if (P.sensor0 >= 0) raster_polygon<ND>(a, P.sensor0, F.Rl, F.tl, v, nv, anc, g);
-  if (P.sensor1 >= 0) raster_polygon<ND>(a, P.sensor1, F.Rl1, F.tl1, v, nv, anc, g);
+  if (P.sensor0 >= 0) raster_keys<ND>(a, P.sensor0, F.Rl, F.tl, v, nv, anc, g, n, 0, nullptr);
+  if (P.sensor1 >= 0) raster_keys<ND>(a, P.sensor1, F.Rl1, F.tl1, v, nv, anc, g, n, 0, nullptr);
 }
 
 template <int ND>
@@ -252,7 +291,9 @@ struct TetStage {
   int orig, valid;
 };
 
-__device__ __forceinline__ void stage_tet(const StepArgs& a, const PairDev& P, int ti, TetStage& S) {
+// (not inlined: the forward and adjoint kernels share one compiled body, so
+// the staged values are bit-identical in both)
+__device__ __noinline__ void stage_tet(const StepArgs& a, const PairDev& P, int ti, TetStage& S) {
   S.valid = 0;
   if (ti >= P.s_n_elem) return;
   TetIn<float> t;
@@ -415,7 +456,7 @@ struct TriStage {
   int orig, valid;
 };
 
-__device__ __forceinline__ void stage_tri(const StepArgs& a, const PairDev& P, const FrameDev& F, int tj,
+__device__ __noinline__ void stage_tri(const StepArgs& a, const PairDev& P, const FrameDev& F, int tj,
                                           TriStage& S) {
   S.valid = 0;
   if (tj >= P.o_n_elem) return;
@@ -533,6 +574,14 @@ __device__ __noinline__ int sr_fp64(const StepArgs& a, const TriStage& T, int te
   return nv;
 }
 
+// FP32 soft-rigid polygon: one compiled body shared by the forward and the
+// adjoint kernels (bit-identical polygons, hence identical taxel keys).
+__device__ __noinline__ int sr_poly_f(const TetIn<float>& t, const double* s, const TriStage& T, V3<float> n,
+                                      float M, Decide& dc, int& anc, PV<float, 3>* out) {
+  PV<float, 3> tmp[kMaxPolyV];
+  return sr_polygon<float>(t, s, T, n, M, dc, anc, out, tmp);
+}
+
 // shared memory of one warp of the soft-rigid kernel
 struct SrWarpSmem {
   TriStage tri[kCluster];
@@ -594,10 +643,10 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
       TetIn<float> t;
       unstage_tet(TS, t);
       const V3<float> n = mk(T.n[0], T.n[1], T.n[2]);
-      PV<float, 3> poly[kMaxPolyV], tmp[kMaxPolyV];
+      PV<float, 3> poly[kMaxPolyV];
       Decide dc;
       int anc = 0;
-      int nv = sr_polygon<float>(t, s, T, n, fmaxf(T.M, t.xmax), dc, anc, poly, tmp);
+      int nv = sr_poly_f(t, s, T, n, fmaxf(T.M, t.xmax), dc, anc, poly);
       const int tet_idx = P.s_elem_off + sl * kCluster + i;
       float gint = 0.f;
       int flags = 0;
@@ -641,6 +690,11 @@ __device__ int hs_polygon(const TetIn<R>& t, const double s[4], V3<R> n, Decide&
 #pragma unroll
   for (int k = 0; k < 4; ++k) tv[k].d[0] = 0;
   return tet_section(tv, s, dc, out);
+}
+
+__device__ __noinline__ int hs_poly_f(const TetIn<float>& t, const double* s, V3<float> n, Decide& dc, int& anc,
+                                      PV<float, 1>* out) {
+  return hs_polygon<float>(t, s, n, dc, anc, out);
 }
 
 __device__ __noinline__ int hs_fp64(const StepArgs& a, const FrameDev& F, int tet_idx, const double s[4], int& anc,
@@ -701,7 +755,7 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
       PV<float, 1> poly[kMaxPolyV];
       Decide dc;
       int anc = 0;
-      int nv = hs_polygon<float>(t, s, n, dc, anc, poly);
+      int nv = hs_poly_f(t, s, n, dc, anc, poly);
       const int tet_idx = P.s_elem_off + sl * kCluster + i;
       float gint = 0.f;
       int flags = 0;

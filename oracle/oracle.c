@@ -861,6 +861,80 @@ static void sensor_update(or_sensor* sn, const double* xpos, const double* xmat,
   free(cnt); free(fill); free(items); free(lo_hi);
 }
 
+/* The same ray sampling evaluated in FP64 throughout (sample origins, ray
+ * test, pressure and sums), for central-difference gradient checks; the
+ * fan triangles come from the FP64 polygons. */
+typedef struct { double v0[3], v1[3], v2[3]; double e0, e1, e2; } dtri;
+
+static void sensor_update64(or_sensor* sn, const double* xpos, const double* xmat, const dtri* tr, int nt) {
+  int cx = sn->cx, cy = sn->cy, sr = sn->sampling_resolution;
+  double* out = sn->taxels64;
+  for (int i = 0; i < cx * cy; ++i) out[i] = 0.0;
+  const int id = sn->geom;
+  const double xs = sn->size[0], ys = sn->size[1], zs = sn->size[2], res = sn->resolution;
+  const double rsr = res / sr, rmean = 1.0 / (sr * sr);
+  const double* rot = xmat + 9 * id;
+  const double D[3] = {-rot[2], -rot[5], -rot[8]};
+  const double di = res / sr, sub = di / 2.0 - res / 2.0, max_dist = sqrt(2.0) * res / 2.0;
+  for (int x = 0; x < cx; ++x)
+    for (int y = 0; y < cy; ++y) {
+      double acc = 0;
+      for (int i = 0; i < sr; ++i)
+        for (int j = 0; j < sr; ++j) {
+          double pos[3] = {-xs + x * res + (i + 0.5) * rsr, -ys + y * res + (j + 0.5) * rsr, 1.5 * zs}, O[3];
+          m_mul(rot, pos, O);
+          for (int a = 0; a < 3; ++a) O[a] += xpos[3 * id + a];
+          double tb = 1e300, ub = 0, vb = 0;
+          int hb = -1;
+          for (int k = 0; k < nt; ++k) {
+            double e1[3], e2[3], h[3], s[3], q[3];
+            v_sub(tr[k].v1, tr[k].v0, e1);
+            v_sub(tr[k].v2, tr[k].v0, e2);
+            v_cross(D, e2, h);
+            double a = v_dot(e1, h);
+            if (fabs(a) < 1e-10) continue;
+            double f = 1.0 / a;
+            v_sub(O, tr[k].v0, s);
+            double u = f * v_dot(s, h);
+            if (u < 0 || u > 1) continue;
+            v_cross(s, e1, q);
+            double v = f * v_dot(D, q);
+            if (v < 0 || u + v > 1) continue;
+            double t = f * v_dot(e2, q);
+            if (t < tb && t > 0) { tb = t; ub = u; vb = v; hb = k; }
+          }
+          if (hb < 0 || !(tb < 1.5 * zs && tb > 0)) continue;
+          double p = (1 - ub - vb) * tr[hb].e0 + ub * tr[hb].e1 + vb * tr[hb].e2;
+          double w = 1.0;
+          double dist = hypot(di * i + sub, di * j + sub) / max_dist;
+          if (sn->window == 1) w = exp(-(dist * dist) * 0.5 / (sn->sigma * sn->sigma));
+          else if (sn->window == 3) w = (1 - dist) * (1 - dist);
+          else if (sn->window == 2) {
+            double rt = 1.0 / sn->sigma * sr * sr;
+            if (sr / 2 - abs(sr / 2 - i) <= sn->sigma * sr / 2) w *= 0.5 * (1 - cos(2 * M_PI * (sr / 2 - abs(sr / 2 - i)) * rt));
+            if (sr / 2 - abs(sr / 2 - j) <= sn->sigma * sr / 2) w *= 0.5 * (1 - cos(2 * M_PI * (sr / 2 - abs(sr / 2 - j)) * rt));
+          }
+          acc += w * p * rmean;
+        }
+      out[x + cy * y] = acc;
+    }
+}
+
+static void push_fan64(dtri** t, int* n, int* cap, const poly* pg) {
+  for (int i = 0; i < pg->nv; ++i) {
+    if (*n == *cap) {
+      *cap = *cap ? 2 * *cap : 256;
+      *t = (dtri*)realloc(*t, sizeof(dtri) * *cap);
+    }
+    dtri* d = &(*t)[(*n)++];
+    int j = (i + 1) % pg->nv;
+    memcpy(d->v0, pg->x[i], sizeof(d->v0));
+    memcpy(d->v1, pg->x[j], sizeof(d->v1));
+    memcpy(d->v2, pg->c, sizeof(d->v2));
+    d->e0 = pg->pr[i]; d->e1 = pg->pr[j]; d->e2 = pg->pc;
+  }
+}
+
 /* kTriangle fan of a polygon as float world triangles with the field
  * values at their vertices (the tri_e_MN the sensor evaluates). */
 static void push_fan(ftrilist* tl, const poly* pg) {
@@ -943,6 +1017,16 @@ int or_collide(or_ctx* c, const double* xpos, const double* xmat, const double* 
     }
     sensor_update(sn, xpos, xmat, &tl);
     free(tl.t);
+    if (sn->taxels64) {
+      dtri* dt = NULL;
+      int nd = 0, cap = 0;
+      for (int i = 0; i < n_pair; ++i) {
+        if (!out[i].query || (g1[i] != sn->geom && g2[i] != sn->geom)) continue;
+        for (int k = 0; k < lists[i].n; ++k) push_fan64(&dt, &nd, &cap, &lists[i].p[k]);
+      }
+      sensor_update64(sn, xpos, xmat, dt, nd);
+      free(dt);
+    }
   }
   for (int i = 0; i < n_pair; ++i) free(lists[i].p);
   free(lists);

@@ -61,6 +61,8 @@ typedef struct {
   double size[3];         /* geom half sizes                                  */
   int cx, cy;             /* filled by or_collide                             */
   float* taxels;          /* cx*cy output, caller-owned (may be NULL)         */
+  double* taxels64;       /* cx*cy output of the same sampling evaluated in
+                             FP64 (gradient checks), may be NULL             */
 } or_sensor;
 
 typedef struct or_ctx or_ctx;

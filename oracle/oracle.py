@@ -50,7 +50,7 @@ class or_candidate(C.Structure):
 class or_sensor(C.Structure):
     _fields_ = [("geom", C.c_int), ("resolution", C.c_double), ("sampling_resolution", C.c_int),
                 ("window", C.c_int), ("sigma", C.c_double), ("size", C.c_double * 3), ("cx", C.c_int),
-                ("cy", C.c_int), ("taxels", C.POINTER(C.c_float))]
+                ("cy", C.c_int), ("taxels", C.POINTER(C.c_float)), ("taxels64", C.POINTER(C.c_double))]
 
 
 _lib = None
@@ -126,7 +126,7 @@ class Oracle:
             pass
 
     def collide(self, representation=0, apply_forces=1, n_threads=0, candidates=False, pairs=None, xpos=None,
-                xmat=None, vel=None, sensors=True):
+                xmat=None, vel=None, sensors=True, taxels64=False):
         s = self.scene
         xpos = np.ascontiguousarray(s.xpos if xpos is None else xpos, np.float64)
         xmat = np.ascontiguousarray(s.xmat if xmat is None else xmat, np.float64)
@@ -141,7 +141,7 @@ class Oracle:
         out = (or_pair_result * max(1, npair))()
         opt = or_options(representation, apply_forces, n_threads)
         sens = (or_sensor * max(1, len(s.sensors)))()
-        taxels = []
+        taxels, t64 = [], []
         if sensors:
             for k, sn in enumerate(s.sensors):
                 size = s.geoms[sn["geom"]]["size"]
@@ -159,6 +159,10 @@ class Oracle:
                 for a in range(3):
                     o.size[a] = size[a]
                 o.taxels = t.ctypes.data_as(C.POINTER(C.c_float))
+                if taxels64:
+                    d = np.zeros(cx.value * cy.value, np.float64)
+                    t64.append(d)
+                    o.taxels64 = d.ctypes.data_as(C.POINTER(C.c_double))
         ncand = C.c_int64()
         cand = None
         cap = 0
@@ -181,6 +185,7 @@ class Oracle:
             area=np.array([out[i].area for i in range(npair)]),
             total_fn0=np.array([out[i].total_fn0 for i in range(npair)]),
             taxels=taxels,
+            taxels64=t64,
         )
         if candidates:
             c = np.zeros((ncand.value, 5), np.int64)

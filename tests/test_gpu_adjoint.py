@@ -1,0 +1,129 @@
+"""Adjoint (C ABI, GPU) vs central finite differences of the FP64 oracle.
+
+The gradient of L = dL/dwrench . wrench + dL/dtaxel . taxels with respect to
+both geoms' world twists [dtheta; dx] (R <- exp(dtheta) R, x <- x + dx) and
+the soft modulus.  Reference: central differences of the FP64 oracle at step
+1e-6 (taxels from its FP64 evaluation of the same ray sampling).  Bar: 1e-3
+relative error per pair (norm of the 12-vector of both twists).
+"""
+import numpy as np
+import pytest
+
+from mujoco_contact_surfaces_gb300 import scenes
+from mujoco_contact_surfaces_gb300.scenes import rot_axis
+from oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+GRAD_RTOL = 1e-3
+
+
+def perturb(xpos, xmat, g, comp, h):
+    xp, xm = xpos.copy(), xmat.copy()
+    if comp < 3:
+        ax = np.zeros(3)
+        ax[comp] = 1.0
+        xm[g] = (rot_axis(ax, h) @ xm[g].reshape(3, 3)).reshape(9)
+    else:
+        xp[g, comp - 3] += h
+    return xp, xm
+
+
+def fd_gradient(orc, s, p, dLdw, dLdt, h=1e-6):
+    """Central differences of L for pair p: 12 components (M then N)."""
+    m, n = orc.collide(pairs=[p], sensors=False)["m"][0], orc.collide(pairs=[p], sensors=False)["n"][0]
+
+    def L(xp, xm):
+        r = orc.collide(pairs=[p], xpos=xp, xmat=xm, sensors=dLdt is not None, taxels64=dLdt is not None)
+        v = float(np.dot(dLdw[p], r["wrench"][0]))
+        if dLdt is not None:
+            v += sum(float(np.dot(dLdt[k], r["taxels64"][k])) for k in range(len(s.sensors)))
+        return v
+
+    g = np.zeros(12)
+    for b, geom in enumerate((m, n)):
+        for c in range(6):
+            xp, xm = perturb(s.xpos, s.xmat, geom, c, h)
+            lp = L(xp, xm)
+            xp, xm = perturb(s.xpos, s.xmat, geom, c, -h)
+            lm = L(xp, xm)
+            g[6 * b + c] = (lp - lm) / (2 * h)
+    return g
+
+
+def run_adjoint(s, dLdw, dLdt, adjoint_mode=True):
+    eng = scenes.build_engine(s)
+    if adjoint_mode:
+        eng.lib.hc_set_adjoint_mode(eng.ctx, 1)
+    eng.step()
+    w = eng.wrenches()
+    tax = eng.all_taxels() if s.sensors else None
+    dt = np.concatenate(dLdt).astype(np.float32) if dLdt is not None else None
+    dpose, dE = eng.adjoint(dLdw, dt)
+    eng.close()
+    return w, tax, dpose, dE
+
+
+def test_wrench_gradient_single_pair(gpu):
+    s = scenes.single_pair(6, velocities=True)
+    rng = np.random.default_rng(7)
+    dLdw = rng.normal(size=(len(s.g1), 6))
+    w, _, dpose, dE = run_adjoint(s, dLdw, None)
+    orc = Oracle(s)
+    for p in range(len(s.g1)):
+        ref = fd_gradient(orc, s, p, dLdw, None)
+        got = dpose[p].reshape(12)
+        err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
+        assert err <= GRAD_RTOL, f"pair {p}: rel err {err:.2e}\n{got}\n{ref}"
+
+
+def test_wrench_and_taxel_gradient_tactile(gpu):
+    s = scenes.tactile(4, velocities=True, plate_half=(0.0401, 0.04, 0.005))
+    rng = np.random.default_rng(11)
+    dLdw = rng.normal(size=(len(s.g1), 6))
+    dLdt = [rng.normal(size=256) * 1e-3 for _ in s.sensors]
+    w, tax, dpose, dE = run_adjoint(s, dLdw, dLdt)
+    orc = Oracle(s)
+    for p in range(len(s.g1)):
+        ref = fd_gradient(orc, s, p, dLdw, dLdt)
+        got = dpose[p].reshape(12)
+        err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
+        assert err <= GRAD_RTOL, f"pair {p}: rel err {err:.2e}\n{got}\n{ref}"
+
+
+def test_taxel_gradient_without_adjoint_mode(gpu):
+    # the adjoint re-runs the step to recover the ray hits
+    s = scenes.tactile(2, velocities=False, plate_half=(0.0401, 0.04, 0.005))
+    rng = np.random.default_rng(3)
+    dLdw = np.zeros((len(s.g1), 6))
+    dLdt = [rng.normal(size=256) for _ in s.sensors]
+    _, _, d1, _ = run_adjoint(s, dLdw, dLdt, adjoint_mode=False)
+    _, _, d2, _ = run_adjoint(s, dLdw, dLdt, adjoint_mode=True)
+    np.testing.assert_allclose(d1, d2, rtol=1e-6, atol=1e-9)
+
+
+def test_modulus_gradient_is_linear_response(gpu):
+    # soft-rigid wrench and taxels are proportional to E: dL/dE = L_E / E
+    s = scenes.tactile(3, velocities=True, plate_half=(0.0401, 0.04, 0.005))
+    rng = np.random.default_rng(5)
+    dLdw = rng.normal(size=(len(s.g1), 6))
+    dLdt = [rng.normal(size=256) for _ in s.sensors]
+    w, tax, dpose, dE = run_adjoint(s, dLdw, dLdt)
+    orc = Oracle(s)
+    r = orc.collide(taxels64=True)
+    for p in range(len(s.g1)):
+        E = s.geoms[s.g1[p]]["cs5"][0]
+        ref = (np.dot(dLdw[p], r["wrench"][p]) + np.dot(dLdt[p], r["taxels64"][p])) / E
+        # the soft body is M (registered first)
+        assert dE[p, 1] == 0.0
+        assert abs(dE[p, 0] - ref) <= 1e-4 * abs(ref) + 1e-12, (dE[p], ref)
+
+
+def test_adjoint_is_deterministic(gpu):
+    s = scenes.tactile(8, velocities=True)
+    rng = np.random.default_rng(1)
+    dLdw = rng.normal(size=(len(s.g1), 6))
+    dLdt = [rng.normal(size=256) for _ in s.sensors]
+    a = run_adjoint(s, dLdw, dLdt)
+    b = run_adjoint(s, dLdw, dLdt)
+    assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3])
