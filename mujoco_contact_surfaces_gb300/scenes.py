@@ -83,8 +83,11 @@ def _alloc(scene: Scene):
     scene.vel = np.zeros((n, 6))
 
 
-def single_pair(n_poses=1000, seed=SEED_SINGLE, velocities=False) -> Scene:
-    """Soft sphere on a rigid box, one pair per pose (each pose its own scene)."""
+def single_pair(n_poses=1000, seed=SEED_SINGLE, velocities=False, min_pen=0.0) -> Scene:
+    """Soft sphere on a rigid box, one pair per pose (each pose its own scene).
+
+    min_pen > 0 draws the penetration from U[min_pen, 5 mm] (finite-difference
+    checks need the contact to stay away from first touch within the step)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     s = Scene()
     R = 0.05
@@ -95,7 +98,7 @@ def single_pair(n_poses=1000, seed=SEED_SINGLE, velocities=False) -> Scene:
     _alloc(s)
     for k in range(n_poses):
         gs, gb = 2 * k, 2 * k + 1
-        pen = rng.uniform(0, 0.005)
+        pen = rng.uniform(min_pen, 0.005)
         tilt = math.radians(rng.uniform(-30, 30))
         phi = rng.uniform(0, 2 * math.pi)
         axis = [math.cos(phi), math.sin(phi), 0.0]
@@ -109,7 +112,7 @@ def single_pair(n_poses=1000, seed=SEED_SINGLE, velocities=False) -> Scene:
 
 
 def tactile(n_scenes=16, seed=SEED_TACTILE, velocities=False, sampling_resolution=5,
-            plate_half=(0.04, 0.04, 0.005)) -> Scene:
+            plate_half=(0.04, 0.04, 0.005), min_pen=0.0) -> Scene:
     """Rigid plate with a 16x16 taxel grid pressed by a soft primitive.
 
     With a square plate the top face's diagonal passes exactly through the
@@ -143,7 +146,7 @@ def tactile(n_scenes=16, seed=SEED_TACTILE, velocities=False, sampling_resolutio
     for k in range(n_scenes):
         g, p = 2 * k, 2 * k + 1
         kind, low = kinds[k]
-        pen = rng.uniform(0, 0.004)
+        pen = rng.uniform(min_pen, 0.004)
         off = rng.uniform(-0.02, 0.02, 2)
         yaw = rot_axis([0, 0, 1], rng.uniform(0, 2 * math.pi))
         Rg = yaw @ rot_axis([1, 0, 0], math.pi / 2) if kind == 2 else yaw

@@ -5,6 +5,12 @@ both geoms' world twists [dtheta; dx] (R <- exp(dtheta) R, x <- x + dx) and
 the soft modulus.  Reference: central differences of the FP64 oracle at step
 1e-6 (taxels from its FP64 evaluation of the same ray sampling).  Bar: 1e-3
 relative error per pair (norm of the 12-vector of both twists).
+
+Central differences only measure the derivative where the function is smooth
+across the step: poses keep at least 1 mm of penetration (the force grows
+with the square of the penetration near first touch), and the taxel maps,
+piecewise linear in the pose with kinks where a ray crosses a tet face, are
+differenced at 1e-7 so that few of the 6400 rays per sensor straddle a kink.
 """
 import numpy as np
 import pytest
@@ -65,7 +71,7 @@ def run_adjoint(s, dLdw, dLdt, adjoint_mode=True):
 
 
 def test_wrench_gradient_single_pair(gpu):
-    s = scenes.single_pair(6, velocities=True)
+    s = scenes.single_pair(6, velocities=True, min_pen=1e-3)
     rng = np.random.default_rng(7)
     dLdw = rng.normal(size=(len(s.g1), 6))
     w, _, dpose, dE = run_adjoint(s, dLdw, None)
@@ -78,14 +84,14 @@ def test_wrench_gradient_single_pair(gpu):
 
 
 def test_wrench_and_taxel_gradient_tactile(gpu):
-    s = scenes.tactile(4, velocities=True, plate_half=(0.0401, 0.04, 0.005))
+    s = scenes.tactile(4, velocities=True, plate_half=(0.0401, 0.04, 0.005), min_pen=1e-3)
     rng = np.random.default_rng(11)
     dLdw = rng.normal(size=(len(s.g1), 6))
     dLdt = [rng.normal(size=256) * 1e-3 for _ in s.sensors]
     w, tax, dpose, dE = run_adjoint(s, dLdw, dLdt)
     orc = Oracle(s)
     for p in range(len(s.g1)):
-        ref = fd_gradient(orc, s, p, dLdw, dLdt)
+        ref = fd_gradient(orc, s, p, dLdw, dLdt, h=1e-7)
         got = dpose[p].reshape(12)
         err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
         assert err <= GRAD_RTOL, f"pair {p}: rel err {err:.2e}\n{got}\n{ref}"
