@@ -1,18 +1,22 @@
-"""Benchmark of the batched hydroelastic contact step on GB300.
+"""Benchmark of the batched hydroelastic contact step (forward + adjoint) on GB300.
 
 python bench.py --gpus N --steps K --warmup W [--impl reference]
 
-Workload: 4096 independent tactile scenes (rigid 8x8 cm plate with a 16x16
-taxel grid pressed by a soft sphere / ellipsoid / cylinder of 2k-8k tets, E in
-5e4-5e5 Pa, penetration 0-4 mm, in-plane offset +-2 cm, velocities U[-0.1,0.1])
-per GPU: the distribution the differentiable batched workload is defined on.
-One step = the pair dispatch frames, LBVH broadphase, clipping, quadrature,
-Hunt-Crossley + friction, per-pair wrench, taxel binning for all scenes, and
-(when built) the adjoint.  Synthetic seeded inputs (no dataset exists).
+Workload: 4096 independent tactile scenes per GPU (rigid 8x8 cm plate with a
+16x16 taxel grid, 5x5 rays per cell, pressed by a soft sphere / ellipsoid /
+cylinder of 2k-8k tets, E in 5e4-5e5 Pa, penetration 0-4 mm, in-plane offset
++-2 cm, velocities U[-0.1,0.1]): the differentiable batched workload.  One
+step = pair frames, LBVH broadphase, clipping, quadrature, Hunt-Crossley +
+friction, per-pair wrenches, taxel binning, then the adjoint of the wrenches
+and taxel maps with respect to both bodies' poses and the modulus (seeded
+upstream gradients).  Synthetic seeded inputs: no dataset exists.
 
-The default arm runs the engine through its C ABI; `--impl reference` times
-the CPU path (the FP64 restatement in oracle/, OpenMP over pairs) on a
-bounded sample of the same workload.
+`value` is timed with inputs resident in HBM; `e2e` goes through the C ABI
+with host buffers (poses and upstream gradients in, wrenches, taxel maps and
+gradients out every step).  The plain path (one scene per launch sequence,
+no graph) is timed on a sample for the batched/plain ratio.  `--impl
+reference` times the CPU path (the FP64 restatement in oracle/, OpenMP over
+pairs, all host threads) on a bounded sample of the same workload.
 """
 from __future__ import annotations
 
@@ -40,15 +44,15 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scenes", type=int, default=4096)
     ap.add_argument("--cpu-sample", type=int, default=256, help="scenes in the CPU baseline sample")
+    ap.add_argument("--plain-sample", type=int, default=64, help="scenes timed on the plain path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
     return ap.parse_args()
 
 
 def dist_info():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
 
 
 def workload(n_scenes, rank):
@@ -56,9 +60,15 @@ def workload(n_scenes, rank):
     return scenes.tactile(n_scenes, seed=scenes.SEED_ADJOINT + rank, velocities=True)
 
 
+def upstream(s, seed=17):
+    """Seeded dL/dwrench (n_pair x 6) and dL/dtaxel (all maps)."""
+    rng = np.random.default_rng(seed)
+    return rng.normal(size=(len(s.g1), 6)), rng.normal(size=256 * len(s.sensors)).astype(np.float32) * 1e-3
+
+
 def config_dict(args, world, extra=None):
-    c = {"workload": "tactile batched: 4096 scenes/GPU, rigid 8x8 cm plate + 16x16 taxels (5x5 rays/cell) "
-                     "vs soft sphere/ellipsoid/cylinder 2k-8k tets",
+    c = {"workload": f"tactile batched fwd+adjoint: {args.scenes} scenes/GPU, rigid 8x8 cm plate + 16x16 taxels "
+                     "(5x5 rays/cell) vs soft sphere/ellipsoid/cylinder 2k-8k tets",
          "scenes_per_gpu": args.scenes, "pairs_per_scene": 1, "representation": "kTriangle",
          "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"scene shards x{world}"}
     if extra:
@@ -67,11 +77,12 @@ def config_dict(args, world, extra=None):
 
 
 def cpu_baseline(n_sample, rank, reps=3):
-    """FP64 oracle, OpenMP over pairs, all host cores, on a bounded sample."""
+    """FP64 oracle, OpenMP over pairs, all host cores, on a bounded sample
+    (forward only: the reference has no adjoint)."""
     import oracle
     s = workload(n_sample, rank)
     o = oracle.Oracle(s)
-    o.collide()  # warm
+    o.collide()
     ts = []
     for _ in range(reps):
         t0 = time.perf_counter()
@@ -80,7 +91,8 @@ def cpu_baseline(n_sample, rank, reps=3):
     o.close()
     t = statistics.median(ts)
     return {"value": n_sample / t, "unit": "pairs/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{n_sample} scenes of the same workload (1 pair + 1 sensor each), median of {reps}"}
+            "sample": f"{n_sample} scenes of the same workload, forward only (the reference path has no "
+                      f"adjoint), median of {reps}"}
 
 
 class Clocks:
@@ -130,18 +142,63 @@ class Clocks:
 
 
 def algorithmic_bytes(eng, n_pair, n_sensor_pairs):
-    """Sec. 8(d) bytes of one forward step: 80 B per distinct soft tet and 48 B
-    per distinct rigid triangle with a non-empty polygon, 96 B of poses and
-    48 B of wrench per pair, 1024 B of taxels per sensor pair."""
+    """Bytes per step by the per-pair formula: forward 80 B per distinct soft
+    tet and 48 B per distinct rigid triangle with a non-empty polygon, 96 B of
+    poses, 48 B of wrench, 1024 B of taxels per sensor pair; the adjoint reads
+    the same elements again plus 48 B of dL/dwrench and 1024 B of dL/dtaxel
+    and writes 104 B of gradients."""
     eng.set_debug(1)
     eng.step()
     cand = eng.candidates()
     eng.set_debug(0)
     tets = len({(int(r[0]), int(r[1])) for r in cand})
     tris = len({(int(r[0]), int(r[2])) for r in cand if r[2] >= 0})
-    narrow = 80 * tets + 48 * tris
-    step = narrow + (96 + 48) * n_pair + 1024 * n_sensor_pairs
-    return narrow, step, tets, tris, len(cand)
+    elem = 80 * tets + 48 * tris
+    fwd = elem + (96 + 48) * n_pair + 1024 * n_sensor_pairs
+    adj = fwd + (48 + 104) * n_pair + 1024 * n_sensor_pairs
+    return dict(elem=elem, fwd=fwd, adj=adj, tets=tets, tris=tris, polygons=len(cand))
+
+
+def plain_path(s_full, n_sample, dLdw, dLdt, local):
+    """One scene per launch sequence, no graph: its own context per scene,
+    fwd + adjoint, timed sequentially."""
+    import torch
+    from mujoco_contact_surfaces_gb300 import scenes
+    sub = scenes.Scene()
+    # the first n_sample scenes (pair k = scene k, geoms 2k, 2k+1)
+    engines = []
+    for k in range(n_sample):
+        sc = scenes.Scene()
+        for g in (s_full.geoms[2 * k], s_full.geoms[2 * k + 1]):
+            sc.add_geom(g["type"], g["size"], g["cs5"], g["mesh_v"], g["mesh_f"])
+        sc.xpos = s_full.xpos[2 * k:2 * k + 2].copy()
+        sc.xmat = s_full.xmat[2 * k:2 * k + 2].copy()
+        sc.vel = s_full.vel[2 * k:2 * k + 2].copy()
+        sc.g1, sc.g2 = [0], [1]
+        sn = dict(s_full.sensors[k])
+        sn["geom"] = 1
+        sc.sensors = [sn]
+        e = scenes.build_engine(sc, device=local, use_graph=False)
+        e.set_adjoint_mode(True)
+        engines.append((e, sc, dLdw[k:k + 1], dLdt[256 * k:256 * (k + 1)]))
+    del sub
+    for e, sc, dw, dt in engines[:2]:
+        e.step()
+        e.wrenches()
+        e.adjoint(dw, dt)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for e, sc, dw, dt in engines:
+        e.set_poses(sc.xpos, sc.xmat, sc.vel)
+        e.step()
+        e.wrenches()
+        e.taxels(0)
+        e.adjoint(dw, dt)
+    t = time.perf_counter() - t0
+    launches = engines[0][0].launch_count() + engines[0][0].adjoint_launch_count()
+    for e, *_ in engines:
+        e.close()
+    return n_sample / t, launches
 
 
 def run_gb300(args):
@@ -157,18 +214,23 @@ def run_gb300(args):
     if os.path.exists(pk):
         peaks = json.load(open(pk))
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
 
     s = workload(args.scenes, rank)
     n_pair = len(s.g1)
     eng = scenes.build_engine(s, device=local)
     eng.enable_timing(True)
-    narrow_bytes, step_bytes, n_tets, n_tris, n_poly = algorithmic_bytes(eng, n_pair, len(s.sensors))
+    ab = algorithmic_bytes(eng, n_pair, len(s.sensors))
+    eng.set_adjoint_mode(True)
+    dLdw_h, dLdt_h = upstream(s)
 
     stream = torch.cuda.ExternalStream(eng.stream(), device=local)
     dev = torch.device("cuda", local)
     xpos = torch.tensor(s.xpos, dtype=torch.float64, device=dev)
     xmat = torch.tensor(s.xmat, dtype=torch.float64, device=dev)
     vel = torch.tensor(s.vel, dtype=torch.float64, device=dev)
+    dLdw = torch.tensor(dLdw_h, dtype=torch.float64, device=dev)
+    dLdt = torch.tensor(dLdt_h, dtype=torch.float32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     n_geom = s.n_geom
     torch.cuda.synchronize()
@@ -176,6 +238,7 @@ def run_gb300(args):
     def device_step():
         eng.set_poses_device(n_geom, xpos.data_ptr(), xmat.data_ptr(), vel.data_ptr())
         eng.step()
+        eng.adjoint_device(dLdw.data_ptr(), dLdt.data_ptr())
 
     for _ in range(args.warmup):
         device_step()
@@ -186,19 +249,23 @@ def run_gb300(args):
 
     clocks = Clocks(local)
     clocks.start()
-    step_ms, narrow_ms = [], []
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    step_ms, narrow_ms, adj_ms = [], [], []
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.fill_(1)
             e0.record(stream)
-        device_step()
+        eng.set_poses_device(n_geom, xpos.data_ptr(), xmat.data_ptr(), vel.data_ptr())
+        eng.step()
         with torch.cuda.stream(stream):
             e1.record(stream)
-        e1.synchronize()
-        step_ms.append(e0.elapsed_time(e1))
-        tm = eng.timings()
-        narrow_ms.append(tm.ms_narrowphase)
+        eng.adjoint_device(dLdw.data_ptr(), dLdt.data_ptr())
+        with torch.cuda.stream(stream):
+            e2.record(stream)
+        e2.synchronize()
+        step_ms.append(e0.elapsed_time(e2))
+        adj_ms.append(e1.elapsed_time(e2))
+        narrow_ms.append(eng.timings().ms_narrowphase)
     torch.cuda.synchronize()
     clk = clocks.stop()
     t_step = sum(step_ms) / len(step_ms)
@@ -207,14 +274,16 @@ def run_gb300(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         t_step = float(t[0])
     value = n_pair * world / (t_step * 1e-3)
+    launches = eng.launch_count() + eng.adjoint_launch_count()
 
-    # end to end through the C ABI with host buffers: H2D poses from pinned
-    # memory, the step, D2H wrenches and taxel maps, every step
+    # end to end through the C ABI with host buffers every step
     hx = torch.tensor(s.xpos, dtype=torch.float64).pin_memory().numpy()
     hm = torch.tensor(s.xmat, dtype=torch.float64).pin_memory().numpy()
     hv = torch.tensor(s.vel, dtype=torch.float64).pin_memory().numpy()
-    h2d = hx.nbytes + hm.nbytes + hv.nbytes
-    d2h = n_pair * 6 * 8 + len(s.sensors) * 256 * 4
+    hw = torch.tensor(dLdw_h, dtype=torch.float64).pin_memory().numpy()
+    ht = torch.tensor(dLdt_h, dtype=torch.float32).pin_memory().numpy()
+    h2d = hx.nbytes + hm.nbytes + hv.nbytes + hw.nbytes + ht.nbytes
+    d2h = n_pair * 6 * 8 + len(s.sensors) * 256 * 4 + n_pair * 14 * 8
     e2e_ms = []
     for _ in range(max(3, args.steps // 2)):
         with torch.cuda.stream(stream):
@@ -223,28 +292,41 @@ def run_gb300(args):
         t0 = time.perf_counter()
         eng.set_poses(hx, hm, hv)
         eng.step()
-        w = eng.wrenches()
-        tx = eng.all_taxels()
+        eng.wrenches()
+        eng.all_taxels()
+        eng.adjoint(hw, ht)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e = n_pair * world / (statistics.median(e2e_ms) * 1e-3)
-    launches = eng.launch_count()
 
     narrow_avg = sum(narrow_ms) / len(narrow_ms)
-    achieved = narrow_bytes / (narrow_avg * 1e-3) / 1e9
+    adj_avg = sum(adj_ms) / len(adj_ms)
+    # dominant kernel: the adjoint's soft-rigid kernel when it is the larger
+    if adj_avg > narrow_avg:
+        kname, kms, kbytes = "adjoint_sr_kernel (adjoint pass)", adj_avg, ab["elem"] + (48 + 1024 + 104) * n_pair
+    else:
+        kname, kms, kbytes = "narrow_sr_kernel", narrow_avg, ab["elem"]
+    achieved = kbytes / (kms * 1e-3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (fp64 section values and wrench sums)", "data": "synthetic",
-        "config": config_dict(args, world, {"pairs": n_pair, "polygons": n_poly, "tets_touched": n_tets,
-                                            "tris_touched": n_tris, "adjoint": "not built"}),
+        "vs_baseline": None, "dtype": "f32 (fp64 section values, plane offsets and wrench sums)",
+        "data": "synthetic (seeded PCG64 scenes; no dataset exists)",
+        "config": config_dict(args, world, {"pairs": n_pair, "polygons": ab["polygons"], "tets_touched": ab["tets"],
+                                            "tris_touched": ab["tris"], "ms_forward": t_step - adj_avg,
+                                            "ms_adjoint": adj_avg, "ms_narrow_kernel": narrow_avg}),
         "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None, "kernel": "narrow_kernel",
-                     "kernel_ms": narrow_avg, "algorithmic_bytes": narrow_bytes,
-                     "step_algorithmic_bytes": step_bytes},
+                     "frac": achieved / hbm_peak, "traffic": None, "kernel": kname, "kernel_ms": kms,
+                     "algorithmic_bytes": kbytes, "step_algorithmic_bytes": ab["adj"],
+                     "step_achieved_gbs": ab["adj"] / (t_step * 1e-3) / 1e9, "peak_source": peak_src},
         "clocks": clk,
     }
+    if rank == 0 and not args.no_plain:
+        pv, pl = plain_path(s, min(args.plain_sample, len(s.g1)), dLdw_h, dLdt_h, local)
+        line["config"]["plain_pairs_per_s"] = pv
+        line["config"]["batched_over_plain"] = value / world / pv
+        line["config"]["plain_launches_per_scene"] = pl
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample, rank)
     eng.close()
@@ -274,8 +356,9 @@ def run_reference(args):
     v = n / t
     line = {"metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": config_dict(args, world, {"scenes_per_step": n}),
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64 scenes)", "impl": "reference",
+            "config": config_dict(args, world, {"scenes_per_step": n, "pass": "forward only (the reference path "
+                                                                            "has no adjoint)"}),
             "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": os.cpu_count(), "kind": "port",
                              "sample": f"{n} scenes of the workload per step (FP64 oracle, OpenMP over pairs)"},
             "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

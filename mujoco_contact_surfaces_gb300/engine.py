@@ -182,6 +182,22 @@ class Engine:
         L.check(self.lib.hc_get_stream(self.ctx, C.byref(s)))
         return s.value or 0
 
+    def set_adjoint_mode(self, on: bool = True):
+        L.check(self.lib.hc_set_adjoint_mode(self.ctx, int(on)))
+
+    def adjoint_device(self, d_dL_dwrench: int | None, d_dL_dtaxel: int | None) -> int:
+        """Asynchronous adjoint on device buffers; returns the device pointer
+        of the n_pair x 14 result ([twist M, twist N, dE_M, dE_N])."""
+        out = C.c_void_p()
+        L.check(self.lib.hc_adjoint_device(self.ctx, C.c_void_p(d_dL_dwrench) if d_dL_dwrench else None,
+                                           C.c_void_p(d_dL_dtaxel) if d_dL_dtaxel else None, C.byref(out)))
+        return out.value or 0
+
+    def adjoint_launch_count(self) -> int:
+        n = C.c_int()
+        L.check(self.lib.hc_get_adjoint_launch_count(self.ctx, C.byref(n)))
+        return n.value
+
     def adjoint(self, dL_dwrench=None, dL_dtaxel=None):
         dw = np.ascontiguousarray(dL_dwrench, np.float64) if dL_dwrench is not None else None
         dt = np.ascontiguousarray(dL_dtaxel, np.float32) if dL_dtaxel is not None else None
