@@ -91,72 +91,82 @@ __device__ __forceinline__ V6 cross6(const V6& a, const V6& b) {
 }
 __device__ __forceinline__ V3<float> val(const V6& a) { return mk(a.x.v, a.y.v, a.z.v); }
 
-// Polygon vertex with tangents: position (relative to the anchor), pressure
-// and up to three carried plane distances.
-struct PD {
+// Polygon vertex with tangents: position relative to the anchor, pressure.
+struct QD {
   V6 x;
   D6 p;
-  D6 d[3];
 };
 
-__device__ __forceinline__ PD pd_lerp(const PD& a, const PD& b, const D6& t, int nd) {
-  PD o;
-  o.x = a.x + (b.x - a.x) * t;
-  o.p = d6lerp(a.p, b.p, t);
-  for (int j = 0; j < nd; ++j) o.d[j] = d6lerp(a.d[j], b.d[j], t);
-  return o;
+// Tangents dx/dxi of a polygon vertex x (absolute, soft frame) that lies on
+// the section plane n.x = o (moving with the other body) and on the two
+// constraints of its label: tet faces (fixed in the soft frame) or clip
+// planes (moving).  For a moving plane (m, o): m.dx = m.v - w.(m x x);
+// for a fixed one: c.dx = 0.  Solved with the 3x3 inverse by cross products.
+__device__ __forceinline__ void vertex_tangent(V3<float> x, V3<float> n, int lab, const V3<float>* face,
+                                               const V3<float>* clipn, V3<float> dx[6]) {
+  const int l0 = lab & 15, l1 = lab >> 4;
+  const V3<float> r0 = n;
+  const V3<float> r1 = l0 < 4 ? face[l0] : clipn[l0 - 4];
+  const V3<float> r2 = l1 < 4 ? face[l1] : clipn[l1 - 4];
+  const V3<float> a0 = cross(r1, r2), a1 = cross(r2, r0), a2 = cross(r0, r1);
+  const float det = dot(r0, a0);
+  const float sc = norm(r0) * norm(r1) * norm(r2);
+  if (!(fabsf(det) > 1e-12f * sc)) {
+#pragma unroll
+    for (int i = 0; i < 6; ++i) dx[i] = mk(0.f, 0.f, 0.f);
+    return;
+  }
+  const float id = 1.f / det;
+  const V3<float> c0 = cross(r0, x);
+  const V3<float> c1 = cross(r1, x), c2 = cross(r2, x);
+  const bool m1 = l0 >= 4, m2 = l1 >= 4;
+  // rotation generators w = e_i: rhs_row = -(r x x)_i for moving rows
+  const float w0[3] = {-c0.x, -c0.y, -c0.z};
+  const float w1[3] = {m1 ? -c1.x : 0.f, m1 ? -c1.y : 0.f, m1 ? -c1.z : 0.f};
+  const float w2[3] = {m2 ? -c2.x : 0.f, m2 ? -c2.y : 0.f, m2 ? -c2.z : 0.f};
+  // translation generators v = e_i: rhs_row = r_i for moving rows
+  const float v0[3] = {r0.x, r0.y, r0.z};
+  const float v1[3] = {m1 ? r1.x : 0.f, m1 ? r1.y : 0.f, m1 ? r1.z : 0.f};
+  const float v2[3] = {m2 ? r2.x : 0.f, m2 ? r2.y : 0.f, m2 ? r2.z : 0.f};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    dx[i] = (a0 * w0[i] + a1 * w1[i] + a2 * w2[i]) * id;
+    dx[3 + i] = (a0 * v0[i] + a1 * v1[i] + a2 * v2[i]) * id;
+  }
 }
 
-// Section of a tet by s = 0 with tangents (signs from the FP64 values).
-__device__ __forceinline__ int tet_section_d(const PD tv[4], const double s64[4], const D6 s[4], int nd, PD* out) {
-  int pos = 0;
+// Unnormalised normals of the four faces of a tet (face k opposite vertex k).
+__device__ __forceinline__ void tet_face_normals(const V3<float> X[4], V3<float> face[4]) {
 #pragma unroll
-  for (int k = 0; k < 4; ++k) pos |= (s64[k] > 0.0) << k;
-  const int np = __popc(pos);
-  if (np == 0 || np == 4) return 0;
-  int ea[4], eb[4], n;
-  if (np == 1 || np == 3) {
-    const int single = np == 1 ? __ffs(pos) - 1 : __ffs(~pos & 0xF) - 1;
-    n = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-      if (k != single) { ea[n] = single; eb[n] = k; ++n; }
-  } else {
-    const int a = __ffs(pos) - 1, b = __ffs(pos & ~(1 << a)) - 1;
-    const int neg = ~pos & 0xF;
-    const int c = __ffs(neg) - 1, d = __ffs(neg & ~(1 << c)) - 1;
-    ea[0] = a; eb[0] = c;
-    ea[1] = a; eb[1] = d;
-    ea[2] = b; eb[2] = d;
-    ea[3] = b; eb[3] = c;
-    n = 4;
+  for (int k = 0; k < 4; ++k) {
+    const int i0 = k == 0 ? 1 : 0;
+    const int i1 = k <= 1 ? 2 : 1;
+    const int i2 = k <= 2 ? 3 : 2;
+    face[k] = cross(X[i1] - X[i0], X[i2] - X[i0]);
   }
-  for (int i = 0; i < n; ++i) {
-    int a = ea[i], b = eb[i];
-    if (fabs(s64[a]) > fabs(s64[b])) { int t = a; a = b; b = t; }
-    out[i] = pd_lerp(tv[a], tv[b], s[a] / (s[a] - s[b]), nd);
-  }
-  return n;
 }
 
-__device__ __forceinline__ int clip_dist_d(const PD* in, int n, int j, int nd, PD* out) {
-  bool all_in = true;
-  for (int i = 0; i < n; ++i) all_in &= in[i].d[j].v >= 0.f;
-  if (all_in) {
-    for (int i = 0; i < n; ++i) out[i] = in[i];
-    return n;
+// Tangent polygon from the float polygon (positions relative to anc).
+template <int ND>
+__device__ __forceinline__ void tangent_polygon(const PV<float, ND>* poly, int nv, V3<float> anc, V3<float> n,
+                                                const V3<float>* face, const V3<float>* clipn, V3<float> g,
+                                                QD* out) {
+  for (int i = 0; i < nv; ++i) {
+    const V3<float> loc = pv_pos(poly[i]);
+    V3<float> dx[6];
+    vertex_tangent(anc + loc, n, poly[i].lab, face, clipn, dx);
+    QD q;
+    q.x = v6c(loc);
+    q.p = d6c(poly[i].p);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      q.x.x.d[k] = dx[k].x;
+      q.x.y.d[k] = dx[k].y;
+      q.x.z.d[k] = dx[k].z;
+      q.p.d[k] = dot(g, dx[k]);
+    }
+    out[i] = q;
   }
-  int m = 0;
-  for (int i = 0; i < n; ++i) {
-    const int k = i + 1 == n ? 0 : i + 1;
-    const D6 di = in[i].d[j], dk = in[k].d[j];
-    const bool ii = di.v >= 0.f, ik = dk.v >= 0.f;
-    if (ii && m < kMaxPolyV) out[m++] = in[i];
-    if (ii != ik && m < kMaxPolyV)
-      out[m++] = fabsf(di.v) <= fabsf(dk.v) ? pd_lerp(in[i], in[k], di / (di - dk), nd)
-                                           : pd_lerp(in[k], in[i], dk / (dk - di), nd);
-  }
-  return m;
 }
 
 // Reverse of one quadrature point: accumulates into gx[6] the tangent
@@ -239,9 +249,9 @@ __device__ void point_adjoint(AdjAcc& G, const FrameDev& F, float damping, float
 }
 
 // Quadrature of a tangent polygon with its reverse.
-__device__ void integrate_adjoint(AdjAcc& G, const StepArgs& a, const PairDev& P, const FrameDev& F, const float* gF,
-                                  const float* gT, const PD* v, int nv, V3<float> anc, const V6& n, const D6& gM,
-                                  const D6& gN) {
+__device__ __noinline__ void integrate_adjoint(AdjAcc& G, const StepArgs& a, const PairDev& P, const FrameDev& F,
+                                               const float* gF, const float* gT, const QD* v, int nv, V3<float> anc,
+                                               const V6& n, const D6& gM, const D6& gN) {
   D6 A = d6c(0.f), pc = d6c(0.f);
   V6 c = v6c(mk(0.f, 0.f, 0.f));
   for (int i = 1; i + 1 < nv; ++i) {
@@ -386,41 +396,14 @@ __global__ void __launch_bounds__(128, 2) adjoint_sr_kernel(StepArgs a) {
                          &G);
       }
       if (!a.adj_wrench || !a.apply_forces) continue;
-      // tangent polygon: section values and edge distances with tangents
-      D6 sd[4];
-      PD tv[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        sd[q] = plane_d6((float)s[q], n, t.X[q]);
-        tv[q].x = v6c(t.X[q] - t.X[anc]);
-        tv[q].p = d6c(t.P[q]);
-      }
-      bool active[3];
-#pragma unroll
-      for (int jj = 0; jj < 3; ++jj) {
-        const V3<float> en = mk(T.en[jj][0], T.en[jj][1], T.en[jj][2]);
-        const float tol = 4e-6f * (t.xmax + fabsf(T.eo[jj]));
-        bool all_in = true;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const double d64 = fma(T.en64[jj][2], (double)t.X[q].z,
-                                 fma(T.en64[jj][1], (double)t.X[q].y, T.en64[jj][0] * (double)t.X[q].x)) -
-                             T.eo64[jj];
-          tv[q].d[jj] = plane_d6((float)d64, en, t.X[q]);
-          all_in &= en.x * t.X[q].x + en.y * t.X[q].y + en.z * t.X[q].z - T.eo[jj] > tol;
-        }
-        active[jj] = !all_in;
-      }
-      PD pa[kMaxPolyV], pb[kMaxPolyV];
-      int m = tet_section_d(tv, s, sd, 3, pa);
-      PD* src = pa;
-      PD* dst = pb;
-      for (int jj = 0; jj < 3 && m > 0; ++jj) {
-        if (!active[jj]) continue;
-        m = clip_dist_d(src, m, jj, 3, dst);
-        PD* sw = src; src = dst; dst = sw;
-      }
-      if (m < 3) continue;
+      // tangent polygon: each vertex as the intersection of the triangle
+      // plane with its two labelled constraints
+      V3<float> face[4];
+      tet_face_normals(t.X, face);
+      const V3<float> clipn[3] = {mk(T.en[0][0], T.en[0][1], T.en[0][2]), mk(T.en[1][0], T.en[1][1], T.en[1][2]),
+                                  mk(T.en[2][0], T.en[2][1], T.en[2][2])};
+      QD qv[kMaxPolyV];
+      tangent_polygon<3>(poly, nv, t.X[anc], n, face, clipn, t.g, qv);
       const V6 nc = rot_dir6(n * sgn);
       // gint = g . n_tri: d/dw = n x g
       D6 gi = d6c(gint);
@@ -429,7 +412,7 @@ __global__ void __launch_bounds__(128, 2) adjoint_sr_kernel(StepArgs a) {
         gi.d[0] = ng.x; gi.d[1] = ng.y; gi.d[2] = ng.z;
       }
       const D6 inf = d6c(INFINITY);
-      integrate_adjoint(G, a, P, F, gF, gT, src, m, t.X[anc], nc, P.s_is_m ? gi : inf, P.s_is_m ? inf : gi);
+      integrate_adjoint(G, a, P, F, gF, gT, qv, nv, t.X[anc], nc, P.s_is_m ? gi : inf, P.s_is_m ? inf : gi);
     }
     __syncwarp();
     adj_reduce_store(a, G, item, lane);
@@ -499,26 +482,18 @@ __global__ void __launch_bounds__(128, 4) adjoint_hs_kernel(StepArgs a) {
                            a.sensors[P.sensor1].geom == P.gs, &G);
         }
         if (a.adj_wrench && a.apply_forces) {
-          D6 sd[4];
-          PD tv[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            sd[q] = plane_d6((float)s[q], n, t.X[q]);
-            tv[q].x = v6c(t.X[q] - t.X[anc]);
-            tv[q].p = d6c(t.P[q]);
+          V3<float> face[4];
+          tet_face_normals(t.X, face);
+          QD qv[kMaxPolyV];
+          tangent_polygon<1>(poly, nv, t.X[anc], n, face, face, t.g, qv);
+          const V6 nc = rot_dir6(n * sgn);
+          D6 gi = d6c(gint);
+          if (gint != 0.f) {
+            const V3<float> ng = cross(n, t.g);
+            gi.d[0] = ng.x; gi.d[1] = ng.y; gi.d[2] = ng.z;
           }
-          PD pa[4];
-          const int m = tet_section_d(tv, s, sd, 0, pa);
-          if (m >= 3) {
-            const V6 nc = rot_dir6(n * sgn);
-            D6 gi = d6c(gint);
-            if (gint != 0.f) {
-              const V3<float> ng = cross(n, t.g);
-              gi.d[0] = ng.x; gi.d[1] = ng.y; gi.d[2] = ng.z;
-            }
-            const D6 inf = d6c(INFINITY);
-            integrate_adjoint(G, a, P, F, gF, gT, pa, m, t.X[anc], nc, P.s_is_m ? gi : inf, P.s_is_m ? inf : gi);
-          }
+          const D6 inf = d6c(INFINITY);
+          integrate_adjoint(G, a, P, F, gF, gT, qv, nv, t.X[anc], nc, P.s_is_m ? gi : inf, P.s_is_m ? inf : gi);
         }
       }
     }

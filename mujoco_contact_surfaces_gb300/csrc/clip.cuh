@@ -38,12 +38,16 @@ constexpr float kFiltRel = 1.0e-6f;         // margin of interpolated values
 constexpr double kNearTol = 1.0e-12;        // near-degenerate threshold
 constexpr double kCosAlphaD = -0.38268343236508978;   // cos(5*pi/8)
 
-// Polygon vertex: position (relative to an anchor), pressure and the
-// distances to up to ND clip planes.
+// Polygon vertex: position (relative to an anchor), pressure, the
+// distances to up to ND clip planes, and the two constraints the vertex lies
+// on besides the section plane (lab = c0 | c1 << 4; 0-3: the tet face
+// opposite vertex k, 4 + j: clip plane j).  The adjoint differentiates each
+// vertex as the intersection of those three planes.
 template <class R, int ND>
 struct PV {
   R x, y, z, p;
   R d[ND];
+  int lab;
 };
 
 template <class R, int ND>
@@ -55,7 +59,14 @@ __device__ __forceinline__ PV<R, ND> pv_lerp(const PV<R, ND>& a, const PV<R, ND>
   o.p = a.p + t * (b.p - a.p);
 #pragma unroll
   for (int j = 0; j < ND; ++j) o.d[j] = a.d[j] + t * (b.d[j] - a.d[j]);
+  o.lab = a.lab;
   return o;
+}
+
+// The constraint shared by two consecutive vertices (the polygon edge's).
+__device__ __forceinline__ int shared_label(int la, int lb) {
+  const int a0 = la & 15, a1 = la >> 4, b0 = lb & 15, b1 = lb >> 4;
+  return (a0 == b0 || a0 == b1) ? a0 : a1;
 }
 
 template <class R, int ND>
@@ -114,9 +125,13 @@ __device__ __forceinline__ int tet_section(const PV<R, ND> tv[4], const double s
   for (int i = 0; i < 4; ++i) {
     if (i < n) {
       int a = ea[i], b = eb[i];
+      // the tet edge (a, b) lies on the faces opposite the two other vertices
+      const int other = 0xF & ~((1 << a) | (1 << b));
+      const int c = __ffs(other) - 1, d = __ffs(other & ~(1 << c)) - 1;
       if (fabs(s[a]) > fabs(s[b])) { int t = a; a = b; b = t; }
       const R sa = (R)s[a], sb = (R)s[b];
       out[i] = pv_lerp(tv[a], tv[b], sa / (sa - sb));
+      out[i].lab = c | (d << 4);
     }
   }
   return n;
@@ -142,7 +157,9 @@ __device__ __forceinline__ int clip_dist(const PV<R, ND>* in, int n, int j, R to
     const bool ii = di >= (R)0, ik = dk >= (R)0;
     if (ii && m < kMaxPolyV) out[m++] = in[i];
     if (ii != ik && m < kMaxPolyV) {
-      out[m++] = abs_r(di) <= abs_r(dk) ? pv_lerp(in[i], in[k], di / (di - dk)) : pv_lerp(in[k], in[i], dk / (dk - di));
+      out[m] = abs_r(di) <= abs_r(dk) ? pv_lerp(in[i], in[k], di / (di - dk)) : pv_lerp(in[k], in[i], dk / (dk - di));
+      out[m].lab = shared_label(in[i].lab, in[k].lab) | ((4 + j) << 4);
+      ++m;
     }
   }
   return m;

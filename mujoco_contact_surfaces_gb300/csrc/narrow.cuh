@@ -386,6 +386,7 @@ template <int ND>
 __device__ __forceinline__ void to_f(const PV<double, ND>* in, int n, PV<float, ND>* out) {
   for (int i = 0; i < n; ++i) {
     out[i].x = (float)in[i].x; out[i].y = (float)in[i].y; out[i].z = (float)in[i].z; out[i].p = (float)in[i].p;
+    out[i].lab = in[i].lab;
 #pragma unroll
     for (int j = 0; j < ND; ++j) out[i].d[j] = (float)in[i].d[j];
   }
