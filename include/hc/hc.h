@@ -197,8 +197,11 @@ HC_API hc_status hc_collide_pairs(hc_context* ctx, int n_pair, const int* g1, co
 /* Per-pair wrench on M about M's origin, world frame: n_pair x
  * [fx fy fz tx ty tz] doubles.  Synchronises the context stream.        */
 HC_API hc_status hc_get_wrenches(hc_context* ctx, double* wrench);
-/* Device pointer to the same n_pair x 6 doubles (valid until the next
- * hc_set_pairs).                                                        */
+/* Device pointer to the per-pair records of the last step (valid until the
+ * next hc_set_pairs): n_pair records of HC_PAIR_RECORD_DOUBLES doubles each,
+ * the wrench (as hc_get_wrenches) in the first 6, then area and total fn0
+ * (hc_pair_stats), then the four int32 counters of hc_pair_stats.        */
+#define HC_PAIR_RECORD_DOUBLES 10
 HC_API hc_status hc_get_wrenches_device(hc_context* ctx, const double** d_wrench);
 /* The query kind and M/N order chosen for each pair: m_geom/n_geom ids. */
 HC_API hc_status hc_get_pair_order(hc_context* ctx, int* query, int* m_geom, int* n_geom);
@@ -291,7 +294,8 @@ typedef struct {
   int64_t n_items;
   int64_t n_polygons;
 } hc_timings;
-/* Enable CUDA-event timing of the stages of hc_step (disables the graph). */
+/* Enable CUDA-event timing of the stages of hc_step (the event records
+ * become part of the captured graph).                                    */
 HC_API hc_status hc_enable_timing(hc_context* ctx, int enable);
 HC_API hc_status hc_get_timings(hc_context* ctx, hc_timings* out);
 /* The context's CUDA stream (cudaStream_t), for callers that order their

@@ -17,8 +17,9 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libhc.so")
 
-SOURCES = ["contact.cu", "adjoint.cu", "hc_api.cu", "meshgen.cpp", "plugin_shim.cpp"]
-HEADERS = ["clip.cuh", "geom_math.cuh", "hc_internal.h", "kernels.h", "meshgen.h", "plugin_shim.h"]
+SOURCES = ["contact.cu", "hc_api.cu", "noalloc.cu", "meshgen.cpp", "plugin_shim.cpp"]
+HEADERS = ["clip.cuh", "geom_math.cuh", "narrow.cuh", "adjoint.cuh", "hc_internal.h", "kernels.h", "meshgen.h",
+           "noalloc.h", "plugin_shim.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

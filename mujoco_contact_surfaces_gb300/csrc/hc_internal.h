@@ -72,6 +72,7 @@ struct PairOut {
   double area, total_fn0;
   int n_poly, n_faces, n_near, n_items;
 };
+static_assert(sizeof(PairOut) == 10 * sizeof(double), "PairOut is the 10-double public pair record");
 
 // Flat sensor (device).
 struct SensorDev {
