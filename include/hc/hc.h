@@ -306,6 +306,48 @@ HC_API hc_status hc_get_launch_count(hc_context* ctx, int* n);
 /* Autotune the narrow-phase launch shape on the current pairs and poses. */
 HC_API hc_status hc_autotune(hc_context* ctx, int* chosen_block, int* chosen_ctas_per_sm);
 
+/* ---- step without device allocation -------------------------------------
+ * No counterpart in the reference: the plugin has no such call.
+ *
+ * hc_step keeps its working buffers (per-pair frames and sums, broadphase
+ * counts and offsets, the cluster-pair work items and their partial sums,
+ * the ray-sample keys of the sensors) in device memory that the context
+ * allocates, and grows the work-item buffers when a step needs more.  Some
+ * callers cannot have device memory allocated while they run: a real-time
+ * control loop that fixes its memory at start-up and must not stall in the
+ * allocator, a process whose device memory is owned by another framework's
+ * pool allocator, or code running where the CUDA allocator may not be
+ * called.  hc_step_noalloc runs the same forward step with all of that
+ * working memory inside one static device array of HC_NOALLOC_SCRATCH_BYTES
+ * (32 MiB) compiled into the library, and calls no allocating routine.
+ *
+ *   n_geom, d_xpos, d_xmat, d_vel: device poses and velocities for geom ids
+ *       [0, n_geom), in the layout of hc_set_poses (d_vel may be NULL);
+ *   d_wrench: device output, n_pair x 6 doubles, as hc_get_wrenches;
+ *   d_taxels: device output, all sensors' taxel maps, as
+ *       hc_get_taxels_device (NULL allowed when the context has no sensor);
+ *   stream: the cudaStream_t to run on, or NULL for the context's stream.
+ *
+ * The context must be ready: hc_set_pairs called after the last change of
+ * geoms or sensors (that call allocates; this one then does not).  The step
+ * reads the context's geometry but writes nothing in it, so hc_get_*,
+ * hc_get_surface and hc_adjoint keep referring to the last hc_step.  The
+ * call is synchronous: it waits for the stream to read back the step's
+ * status word.  A step whose working set does not fit in the array fails
+ * with HC_ERR_OVERFLOW and a message giving the pair, sample or work-item
+ * count that did not fit; its outputs are then incomplete.
+ * The first call on each device looks up the array's device address with
+ * that device current (cudaGetSymbolAddress, once per device); make that
+ * first call before any stream capture.  All calls, from every context and
+ * thread, share the one array, and each call leaves its contents behind: the
+ * call clears what must start cleared, but two calls whose work overlaps on
+ * the GPU race on the array and give wrong results, so serialise them (one
+ * stream, or events between streams).                                       */
+#define HC_NOALLOC_SCRATCH_BYTES (32u << 20)
+HC_API hc_status hc_step_noalloc(hc_context* ctx, int n_geom, const double* d_xpos,
+                                 const double* d_xmat, const double* d_vel, double* d_wrench,
+                                 float* d_taxels, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -107,6 +107,7 @@ SIGNATURES = {
     "hc_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "hc_get_launch_count": (C.c_int, [_P, _ip]),
     "hc_autotune": (C.c_int, [_P, _ip, _ip]),
+    "hc_step_noalloc": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P]),
 }
 
 _lib = None

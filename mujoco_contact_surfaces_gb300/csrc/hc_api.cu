@@ -16,6 +16,7 @@
 #include "hc_internal.h"
 #include "kernels.h"
 #include "meshgen.h"
+#include "noalloc.h"
 
 namespace {
 
@@ -1291,3 +1292,25 @@ hc_status hc_get_adjoint_launch_count(hc_context* c, int* n) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Read-only view of a context for hc_step_noalloc (noalloc.cu).
+namespace hc {
+
+hc_status set_last_error(hc_status st, const char* msg) { return fail(st, msg); }
+
+hc_status noalloc_view(hc_context* c, NoallocView* v) {
+  if (hc_status st = need(c)) return st;
+  if (c->pools_dirty || c->sensors_dirty)
+    return fail(HC_ERR_NOT_READY, "geoms or sensors changed since hc_set_pairs: call hc_set_pairs first");
+  v->args = make_args(c, 0, -1);
+  v->device = c->device;
+  v->stream = c->stream;
+  v->max_geom_id = c->max_geom_id;
+  size_t n = 0;
+  for (const SensorHost& S : c->sensors) n += (size_t)S.cx * S.sr * S.cy * S.sr;
+  v->n_samples = n;
+  return HC_OK;
+}
+
+}  // namespace hc
