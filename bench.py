@@ -55,6 +55,18 @@ def dist_info():
         os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(x: float, world: int) -> float:
+    """The largest per-rank value (the slowest rank's step time); a gloo
+    all-reduce on the host, no device collective."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
 def workload(n_scenes, rank):
     from mujoco_contact_surfaces_gb300 import scenes
     return scenes.tactile(n_scenes, seed=scenes.SEED_ADJOINT + rank, velocities=True)
@@ -268,11 +280,7 @@ def run_gb300(args):
         narrow_ms.append(eng.timings().ms_narrowphase)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    t_step = sum(step_ms) / len(step_ms)
-    if world > 1:
-        t = torch.tensor([t_step], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(t[0])
+    t_step = max_over_ranks(sum(step_ms) / len(step_ms), world)
     value = n_pair * world / (t_step * 1e-3)
     launches = eng.launch_count() + eng.adjoint_launch_count()
 
@@ -296,7 +304,7 @@ def run_gb300(args):
         eng.all_taxels()
         eng.adjoint(hw, ht)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e = n_pair * world / (statistics.median(e2e_ms) * 1e-3)
+    e2e = n_pair * world / (max_over_ranks(statistics.median(e2e_ms), world) * 1e-3)
 
     narrow_avg = sum(narrow_ms) / len(narrow_ms)
     adj_avg = sum(adj_ms) / len(adj_ms)
@@ -327,7 +335,7 @@ def run_gb300(args):
         line["config"]["plain_pairs_per_s"] = pv
         line["config"]["batched_over_plain"] = value / world / pv
         line["config"]["plain_launches_per_scene"] = pl
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample, rank)
     eng.close()
     if rank == 0:
