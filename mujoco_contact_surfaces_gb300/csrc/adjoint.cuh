@@ -11,185 +11,25 @@
 // per item in FP64, then per pair, where the chain rule maps them to the
 // world twists of both bodies.
 
-struct D6 {
-  float v;
-  float d[6];
+// Reverse of the force law at one quadrature point: the
+// velocity-field adjoints are added to G; the adjoints of the point's inputs
+// (area, position, normal, pressure, gM, gN) are returned in `b`.  Returns
+// false (and no contribution) where the forward skips the point (P:345,
+// P:361-368).  upstream: fbar = gF + gT x p (force and torque about the soft
+// origin).
+struct PointBar {
+  float A, p0, gM, gN;
+  V3<float> p, n;
 };
 
-__device__ __forceinline__ D6 d6c(float x) {
-  D6 r;
-  r.v = x;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) r.d[i] = 0.f;
-  return r;
-}
-__device__ __forceinline__ D6 operator+(const D6& a, const D6& b) {
-  D6 r;
-  r.v = a.v + b.v;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) r.d[i] = a.d[i] + b.d[i];
-  return r;
-}
-__device__ __forceinline__ D6 operator-(const D6& a, const D6& b) {
-  D6 r;
-  r.v = a.v - b.v;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) r.d[i] = a.d[i] - b.d[i];
-  return r;
-}
-__device__ __forceinline__ D6 operator-(const D6& a) {
-  D6 r;
-  r.v = -a.v;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) r.d[i] = -a.d[i];
-  return r;
-}
-__device__ __forceinline__ D6 operator*(const D6& a, const D6& b) {
-  D6 r;
-  r.v = a.v * b.v;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
-  return r;
-}
-__device__ __forceinline__ D6 operator*(const D6& a, float s) {
-  D6 r;
-  r.v = a.v * s;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) r.d[i] = a.d[i] * s;
-  return r;
-}
-__device__ __forceinline__ D6 operator/(const D6& a, const D6& b) {
-  D6 r;
-  const float ib = 1.f / b.v;
-  r.v = a.v * ib;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
-  return r;
-}
-__device__ __forceinline__ D6 d6sqrt(const D6& a) {
-  D6 r;
-  r.v = sqrtf(a.v);
-  const float h = r.v > 0.f ? 0.5f / r.v : 0.f;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) r.d[i] = a.d[i] * h;
-  return r;
-}
-// a + t (b - a)
-__device__ __forceinline__ D6 d6lerp(const D6& a, const D6& b, const D6& t) { return a + t * (b - a); }
-
-struct V6 {
-  D6 x, y, z;
-};
-__device__ __forceinline__ V6 v6c(V3<float> a) { return V6{d6c(a.x), d6c(a.y), d6c(a.z)}; }
-__device__ __forceinline__ V6 operator+(const V6& a, const V6& b) { return V6{a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ V6 operator-(const V6& a, const V6& b) { return V6{a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ V6 operator*(const V6& a, const D6& s) { return V6{a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ V6 operator*(const V6& a, float s) { return V6{a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ D6 dot6(const V6& a, const V6& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ V6 cross6(const V6& a, const V6& b) {
-  return V6{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
-}
-__device__ __forceinline__ V3<float> val(const V6& a) { return mk(a.x.v, a.y.v, a.z.v); }
-
-// Polygon vertex with tangents: position relative to the anchor, pressure.
-struct QD {
-  V6 x;
-  D6 p;
-};
-
-// Tangents dx/dxi of a polygon vertex x (absolute, soft frame) that lies on
-// the section plane n.x = o (moving with the other body) and on the two
-// constraints of its label: tet faces (fixed in the soft frame) or clip
-// planes (moving).  For a moving plane (m, o): m.dx = m.v - w.(m x x);
-// for a fixed one: c.dx = 0.  Solved with the 3x3 inverse by cross products.
-__device__ __forceinline__ void vertex_tangent(V3<float> x, V3<float> n, int lab, const V3<float>* face,
-                                               const V3<float>* clipn, V3<float> dx[6]) {
-  const int l0 = lab & 15, l1 = lab >> 4;
-  const V3<float> r0 = n;
-  const V3<float> r1 = l0 < 4 ? face[l0] : clipn[l0 - 4];
-  const V3<float> r2 = l1 < 4 ? face[l1] : clipn[l1 - 4];
-  const V3<float> a0 = cross(r1, r2), a1 = cross(r2, r0), a2 = cross(r0, r1);
-  const float det = dot(r0, a0);
-  const float sc = norm(r0) * norm(r1) * norm(r2);
-  if (!(fabsf(det) > 1e-12f * sc)) {
-#pragma unroll
-    for (int i = 0; i < 6; ++i) dx[i] = mk(0.f, 0.f, 0.f);
-    return;
-  }
-  const float id = 1.f / det;
-  const V3<float> c0 = cross(r0, x);
-  const V3<float> c1 = cross(r1, x), c2 = cross(r2, x);
-  const bool m1 = l0 >= 4, m2 = l1 >= 4;
-  // rotation generators w = e_i: rhs_row = -(r x x)_i for moving rows
-  const float w0[3] = {-c0.x, -c0.y, -c0.z};
-  const float w1[3] = {m1 ? -c1.x : 0.f, m1 ? -c1.y : 0.f, m1 ? -c1.z : 0.f};
-  const float w2[3] = {m2 ? -c2.x : 0.f, m2 ? -c2.y : 0.f, m2 ? -c2.z : 0.f};
-  // translation generators v = e_i: rhs_row = r_i for moving rows
-  const float v0[3] = {r0.x, r0.y, r0.z};
-  const float v1[3] = {m1 ? r1.x : 0.f, m1 ? r1.y : 0.f, m1 ? r1.z : 0.f};
-  const float v2[3] = {m2 ? r2.x : 0.f, m2 ? r2.y : 0.f, m2 ? r2.z : 0.f};
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    dx[i] = (a0 * w0[i] + a1 * w1[i] + a2 * w2[i]) * id;
-    dx[3 + i] = (a0 * v0[i] + a1 * v1[i] + a2 * v2[i]) * id;
-  }
-}
-
-// Unnormalised normals of the four faces of a tet (face k opposite vertex k).
-__device__ __forceinline__ void tet_face_normals(const V3<float> X[4], V3<float> face[4]) {
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int i0 = k == 0 ? 1 : 0;
-    const int i1 = k <= 1 ? 2 : 1;
-    const int i2 = k <= 2 ? 3 : 2;
-    face[k] = cross(X[i1] - X[i0], X[i2] - X[i0]);
-  }
-}
-
-// Tangent polygon from the float polygon (positions relative to anc).
-template <int ND>
-__device__ __forceinline__ void tangent_polygon(const PV<float, ND>* poly, int nv, V3<float> anc, V3<float> n,
-                                                const V3<float>* face, const V3<float>* clipn, V3<float> g,
-                                                QD* out) {
-  for (int i = 0; i < nv; ++i) {
-    const V3<float> loc = pv_pos(poly[i]);
-    V3<float> dx[6];
-    vertex_tangent(anc + loc, n, poly[i].lab, face, clipn, dx);
-    QD q;
-    q.x = v6c(loc);
-    q.p = d6c(poly[i].p);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      q.x.x.d[k] = dx[k].x;
-      q.x.y.d[k] = dx[k].y;
-      q.x.z.d[k] = dx[k].z;
-      q.p.d[k] = dot(g, dx[k]);
-    }
-    out[i] = q;
-  }
-}
-
-// Reverse of one quadrature point: accumulates into gx[6] the tangent
-// contraction of L = fbar . f (fbar = gF + gT x p) and into glin/gang the
-// velocity-field adjoints.  P.damping, P.mu as the forward.
-__device__ __forceinline__ void adj_zero(AdjAcc& g) {
-#pragma unroll
-  for (int i = 0; i < 6; ++i) g.gx[i] = 0.f;
-#pragma unroll
-  for (int i = 0; i < 3; ++i) g.glin[i] = g.gang[i] = 0.f;
-  g.gE = 0.f;
-}
-
-__device__ void point_adjoint(AdjAcc& G, const FrameDev& F, float damping, float mu, const float* gF,
-                              const float* gT, const D6& A, const V6& p, const V6& n, const D6& gM, const D6& gN,
-                              const D6& p0) {
-  if (!(A.v > 1.0e-14f)) return;
-  if (gM.v < 1.0e-14f || gN.v < 1.0e-14f) return;
+__device__ __forceinline__ bool point_reverse(AdjAcc& G, const FrameDev& F, float damping, float mu, V3<float> gFv,
+                                              V3<float> gTv, float A, V3<float> pv, V3<float> nv, float gMv,
+                                              float gNv, float p0, PointBar& b) {
+  if (!(A > 1.0e-14f)) return false;
+  if (gMv < 1.0e-14f || gNv < 1.0e-14f) return false;
   // forward values
-  const float gMv = gM.v, gNv = gN.v;
   const float g = 1.0f / (1.0f / gMv + 1.0f / gNv);
-  const float fn0 = A.v * p0.v, k = A.v * g;
-  const V3<float> pv = val(p), nv = val(n);
+  const float fn0 = A * p0, k = A * g;
   const V3<float> lin = mk(F.lin[0], F.lin[1], F.lin[2]), ang = mk(F.ang[0], F.ang[1], F.ang[2]);
   const V3<float> v = lin + cross(ang, pv);
   const float vn = dot(v, nv);
@@ -204,8 +44,6 @@ __device__ void point_adjoint(AdjAcc& G, const FrameDev& F, float damping, float
   const V3<float> u = vt * (1.f / vs);
   const V3<float> q = nv - u * mur;
   const V3<float> f = q * fn;
-  // upstream: fbar = gF + gT x p ; torque p x f also depends on p
-  const V3<float> gFv = mk(gF[0], gF[1], gF[2]), gTv = mk(gT[0], gT[1], gT[2]);
   const V3<float> fbar = gFv + cross(gTv, pv);
   // reverse
   const float Lfn = dot(fbar, q);
@@ -221,7 +59,7 @@ __device__ void point_adjoint(AdjAcc& G, const FrameDev& F, float damping, float
   V3<float> vbar = vtbar;
   float vnbar = -dot(vtbar, nv);
   nbar = nbar - vtbar * vn;
-  // fn = hp * (fn0 - 0.001 k vn)
+  // fn = hp (fn0 - 0.001 k vn)
   const float hbar = h > 0.f ? Lfn * fnb : 0.f;
   const float fn0bar = Lfn * hp;
   const float kbar = -Lfn * hp * 0.001f * vn;
@@ -229,53 +67,167 @@ __device__ void point_adjoint(AdjAcc& G, const FrameDev& F, float damping, float
   // vn = v . n
   vbar = vbar + nv * vnbar;
   nbar = nbar + v * vnbar;
-  // k = A g, fn0 = A p0
-  const float Abar = kbar * g + fn0bar * p0.v;
-  const float gbar = kbar * A.v;
-  const float p0bar = fn0bar * A.v;
-  const float gMbar = gbar * (g / gMv) * (g / gMv);
-  const float gNbar = gbar * (g / gNv) * (g / gNv);
+  // k = A g, fn0 = A p0, g = 1 / (1/gM + 1/gN)
+  b.A = kbar * g + fn0bar * p0;
+  const float gbar = kbar * A;
+  b.p0 = fn0bar * A;
+  b.gM = gbar * (g / gMv) * (g / gMv);
+  b.gN = gbar * (g / gNv) * (g / gNv);
   // v = lin + ang x p
   G.glin[0] += vbar.x; G.glin[1] += vbar.y; G.glin[2] += vbar.z;
   const V3<float> angbar = cross(pv, vbar);
   G.gang[0] += angbar.x; G.gang[1] += angbar.y; G.gang[2] += angbar.z;
-  V3<float> pbar = cross(vbar, ang) + cross(f, gTv);
-  // contraction with the geometric tangents
-#pragma unroll
-  for (int i = 0; i < 6; ++i) {
-    G.gx[i] += Abar * A.d[i] + p0bar * p0.d[i] + gMbar * gM.d[i] + gNbar * gN.d[i] + pbar.x * p.x.d[i] +
-               pbar.y * p.y.d[i] + pbar.z * p.z.d[i] + nbar.x * n.x.d[i] + nbar.y * n.y.d[i] + nbar.z * n.z.d[i];
-  }
+  b.p = cross(vbar, ang) + cross(f, gTv);
+  b.n = nbar;
+  return true;
 }
 
-// Quadrature of a tangent polygon with its reverse.
-__device__ __noinline__ void integrate_adjoint(AdjAcc& G, const StepArgs& a, const PairDev& P, const FrameDev& F,
-                                               const float* gF, const float* gT, const QD* v, int nv, V3<float> anc,
-                                               const V6& n, const D6& gM, const D6& gN) {
-  D6 A = d6c(0.f), pc = d6c(0.f);
-  V6 c = v6c(mk(0.f, 0.f, 0.f));
-  for (int i = 1; i + 1 < nv; ++i) {
-    const D6 ai = dot6(cross6(v[i].x - v[0].x, v[i + 1].x - v[0].x), n) * 0.5f;
-    A = A + ai;
-    c = c + (v[0].x + v[i].x + v[i + 1].x) * (ai * (1.f / 3.f));
-    pc = pc + ai * (v[0].p + v[i].p + v[i + 1].p) * (1.f / 3.f);
+__device__ __forceinline__ void adj_zero(AdjAcc& g) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i) g.gx[i] = 0.f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) g.glin[i] = g.gang[i] = 0.f;
+  g.gE = 0.f;
+}
+
+// Wrench adjoint of one contact polygon.  The quadrature and the
+// force law are reversed by hand to per-vertex adjoints xbar_v, pbar_v, the
+// normal's nbar and the gradient term's gbar; those are then contracted with
+// the geometric tangents under the twist xi = (w, v) of the other body in the
+// soft frame:
+//   vertex x_v: on the section plane (moving) and its two labelled
+//     constraints (tet faces fixed, clip planes moving); with the rows r_k and
+//     the 3x3 inverse by cross products a_k / det, b_k = xbar.a_k / det and
+//     B = sum over moving rows of b_k r_k give dL/dv += B, dL/dw += x_v x B;
+//   pressure p_v = g . x_v + c: pbar_v adds pbar_v g to xbar_v;
+//   normal ns (rotates with the other body): dL/dw += ns x nbar;
+//   gint = g . n (n rotates): dL/dw += gbar (n x g).
+// poly: the forward polygon relative to anc; n: the section normal (soft
+// frame); sgn: +1 when the soft geom is M (normal out of N into M);
+// face: unnormalised tet face normals; clipn: clip-plane normals.
+template <int ND>
+__device__ __noinline__ void wrench_adjoint(AdjAcc& G, const StepArgs& a, const PairDev& P, const FrameDev& F,
+                                            const float* gF, const float* gT, const PV<float, ND>* poly, int nv,
+                                            V3<float> anc, V3<float> n, float sgn, const V3<float>* face,
+                                            const V3<float>* clipn, V3<float> g, float gint) {
+  V3<float> x[kMaxPolyV], xb[kMaxPolyV];
+  float pv[kMaxPolyV], pb[kMaxPolyV];
+  for (int i = 0; i < nv; ++i) {
+    x[i] = pv_pos(poly[i]);
+    pv[i] = poly[i].p;
+    xb[i] = mk(0.f, 0.f, 0.f);
+    pb[i] = 0.f;
   }
-  if (A.v == 0.f) return;
-  c = c * (d6c(1.f) / A);
-  pc = pc / A;
-  const V6 ancv = v6c(anc);
+  const V3<float> ns = n * sgn;
+  const V3<float> gFv = mk(gF[0], gF[1], gF[2]), gTv = mk(gT[0], gT[1], gT[2]);
+  // forward fan sums
+  float A = 0.f, Sp = 0.f;
+  V3<float> Sc = mk(0.f, 0.f, 0.f);
+  for (int i = 1; i + 1 < nv; ++i) {
+    const float ai = 0.5f * dot(cross(x[i] - x[0], x[i + 1] - x[0]), ns);
+    A += ai;
+    Sc = Sc + (x[0] + x[i] + x[i + 1]) * (ai * (1.f / 3.f));
+    Sp += ai * (pv[0] + pv[i] + pv[i + 1]) * (1.f / 3.f);
+  }
+  if (A == 0.f) return;
+  const float iA = 1.f / A;
+  const V3<float> c = Sc * iA;
+  const float pc = Sp * iA;
+  const float inf = INFINITY;
+  const float gMv = P.s_is_m ? gint : inf, gNv = P.s_is_m ? inf : gint;
+  V3<float> nbar = mk(0.f, 0.f, 0.f), cbar = mk(0.f, 0.f, 0.f);
+  float gbar = 0.f, pcbar = 0.f, Abar = 0.f;
+  PointBar b;
   if (a.repr == 1) {
-    D6 Aabs = A.v < 0.f ? -A : A;
-    point_adjoint(G, F, P.damping, P.mu, gF, gT, Aabs, ancv + c, n, gM, gN, pc);
+    if (point_reverse(G, F, P.damping, P.mu, gFv, gTv, fabsf(A), anc + c, ns, gMv, gNv, pc, b)) {
+      Abar += A < 0.f ? -b.A : b.A;
+      cbar = cbar + b.p;
+      pcbar += b.p0;
+      nbar = nbar + b.n;
+      gbar += P.s_is_m ? b.gM : b.gN;
+    }
   } else {
     for (int i = 0; i < nv; ++i) {
       const int j = i + 1 == nv ? 0 : i + 1;
-      const V6 cr = cross6(v[i].x - c, v[j].x - c);
-      const D6 Ai = d6sqrt(dot6(cr, cr)) * 0.5f;
-      const V6 cen = ancv + (c + v[i].x + v[j].x) * (1.f / 3.f);
-      const D6 p0 = pc * (1.f / 3.f) + v[i].p * (1.f / 3.f) + v[j].p * (1.f / 3.f);
-      point_adjoint(G, F, P.damping, P.mu, gF, gT, Ai, cen, n, gM, gN, p0);
+      const V3<float> u = x[i] - c, w = x[j] - c;
+      const V3<float> cr = cross(u, w);
+      const float len = norm(cr);
+      const V3<float> cen = anc + (c + x[i] + x[j]) * (1.f / 3.f);
+      const float p0 = pc / 3.f + pv[i] / 3.f + pv[j] / 3.f;
+      if (!point_reverse(G, F, P.damping, P.mu, gFv, gTv, 0.5f * len, cen, ns, gMv, gNv, p0, b)) continue;
+      nbar = nbar + b.n;
+      gbar += P.s_is_m ? b.gM : b.gN;
+      if (len > 0.f) {   // A_e = |u x w| / 2
+        const V3<float> crb = cr * (0.5f * b.A / len);
+        const V3<float> ub = cross(w, crb), wb = cross(crb, u);
+        xb[i] = xb[i] + ub;
+        xb[j] = xb[j] + wb;
+        cbar = cbar - ub - wb;
+      }
+      const V3<float> c3 = b.p * (1.f / 3.f);
+      cbar = cbar + c3;
+      xb[i] = xb[i] + c3;
+      xb[j] = xb[j] + c3;
+      const float p3 = b.p0 * (1.f / 3.f);
+      pcbar += p3;
+      pb[i] += p3;
+      pb[j] += p3;
     }
+  }
+  // c = Sc / A, pc = Sp / A
+  const V3<float> Scb = cbar * iA;
+  const float Spb = pcbar * iA;
+  Abar -= (dot(cbar, c) + pcbar * pc) * iA;
+  for (int i = 1; i + 1 < nv; ++i) {
+    const V3<float> e1 = x[i] - x[0], e2 = x[i + 1] - x[0];
+    const V3<float> cr = cross(e1, e2);
+    const float ai = 0.5f * dot(cr, ns);
+    const float aib = Abar + dot(Scb, x[0] + x[i] + x[i + 1]) * (1.f / 3.f) +
+                      Spb * (pv[0] + pv[i] + pv[i + 1]) * (1.f / 3.f);
+    const V3<float> sx = Scb * (ai * (1.f / 3.f));
+    const float sp = Spb * ai * (1.f / 3.f);
+    xb[0] = xb[0] + sx; xb[i] = xb[i] + sx; xb[i + 1] = xb[i + 1] + sx;
+    pb[0] += sp; pb[i] += sp; pb[i + 1] += sp;
+    // a_i = n . (e1 x e2) / 2
+    nbar = nbar + cr * (0.5f * aib);
+    const V3<float> e1b = cross(e2, ns) * (0.5f * aib), e2b = cross(ns, e1) * (0.5f * aib);
+    xb[i] = xb[i] + e1b;
+    xb[i + 1] = xb[i + 1] + e2b;
+    xb[0] = xb[0] - e1b - e2b;
+  }
+  // contraction with the tangents
+  V3<float> rot = cross(ns, nbar), tr = mk(0.f, 0.f, 0.f);
+  if (gint != 0.f) rot = rot + cross(n, g) * gbar;
+  for (int v = 0; v < nv; ++v) {
+    const V3<float> xe = xb[v] + g * pb[v];
+    const V3<float> X = anc + x[v];
+    const int l0 = poly[v].lab & 15, l1 = poly[v].lab >> 4;
+    const V3<float> r0 = n;
+    const V3<float> r1 = l0 < 4 ? face[l0] : clipn[l0 - 4];
+    const V3<float> r2 = l1 < 4 ? face[l1] : clipn[l1 - 4];
+    const V3<float> a0 = cross(r1, r2), a1 = cross(r2, r0), a2 = cross(r0, r1);
+    const float det = dot(r0, a0);
+    const float sc = norm(r0) * norm(r1) * norm(r2);
+    if (!(fabsf(det) > 1e-12f * sc)) continue;
+    const float id = 1.f / det;
+    V3<float> B = r0 * (dot(xe, a0) * id);
+    if (l0 >= 4) B = B + r1 * (dot(xe, a1) * id);
+    if (l1 >= 4) B = B + r2 * (dot(xe, a2) * id);
+    tr = tr + B;
+    rot = rot + cross(X, B);
+  }
+  G.gx[0] += rot.x; G.gx[1] += rot.y; G.gx[2] += rot.z;
+  G.gx[3] += tr.x; G.gx[4] += tr.y; G.gx[5] += tr.z;
+}
+
+// Unnormalised normals of the four faces of a tet (face k opposite vertex k).
+__device__ __forceinline__ void tet_face_normals(const V3<float> X[4], V3<float> face[4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int i0 = k == 0 ? 1 : 0;
+    const int i1 = k <= 1 ? 2 : 1;
+    const int i2 = k <= 2 ? 3 : 2;
+    face[k] = cross(X[i1] - X[i0], X[i2] - X[i0]);
   }
 }
 
@@ -295,28 +247,7 @@ __device__ __forceinline__ void adj_reduce_store(const StepArgs& a, const AdjAcc
     for (int i = 0; i < 13; ++i) a.adj_item[(size_t)item * 16 + i] = v[i];
 }
 
-// Tangent plane distances of a tet vertex X to the plane (n, o) moving with
-// the other body: ds/dw = n x X, ds/dv = -n.
-__device__ __forceinline__ D6 plane_d6(float sval, V3<float> n, V3<float> X) {
-  D6 r;
-  r.v = sval;
-  const V3<float> c = cross(n, X);
-  r.d[0] = c.x; r.d[1] = c.y; r.d[2] = c.z;
-  r.d[3] = -n.x; r.d[4] = -n.y; r.d[5] = -n.z;
-  return r;
-}
-
-// Direction that rotates with the other body: d/dw_i = e_i x n.
-__device__ __forceinline__ V6 rot_dir6(V3<float> n) {
-  V6 r = v6c(n);
-  // e_0 x n = (0, -nz, ny); e_1 x n = (nz, 0, -nx); e_2 x n = (-ny, nx, 0)
-  r.x.d[1] = n.z; r.x.d[2] = -n.y;
-  r.y.d[0] = -n.z; r.y.d[2] = n.x;
-  r.z.d[0] = n.y; r.z.d[1] = -n.x;
-  return r;
-}
-
-__global__ void __launch_bounds__(128, 2) adjoint_sr_kernel(StepArgs a) {
+__global__ void __launch_bounds__(128, 4) adjoint_sr_kernel(StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   SrWarpSmem& W = reinterpret_cast<SrWarpSmem*>(smem_raw)[wid];
@@ -396,23 +327,11 @@ __global__ void __launch_bounds__(128, 2) adjoint_sr_kernel(StepArgs a) {
                          &G);
       }
       if (!a.adj_wrench || !a.apply_forces) continue;
-      // tangent polygon: each vertex as the intersection of the triangle
-      // plane with its two labelled constraints
       V3<float> face[4];
       tet_face_normals(t.X, face);
       const V3<float> clipn[3] = {mk(T.en[0][0], T.en[0][1], T.en[0][2]), mk(T.en[1][0], T.en[1][1], T.en[1][2]),
                                   mk(T.en[2][0], T.en[2][1], T.en[2][2])};
-      QD qv[kMaxPolyV];
-      tangent_polygon<3>(poly, nv, t.X[anc], n, face, clipn, t.g, qv);
-      const V6 nc = rot_dir6(n * sgn);
-      // gint = g . n_tri: d/dw = n x g
-      D6 gi = d6c(gint);
-      if (gint != 0.f) {
-        const V3<float> ng = cross(n, t.g);
-        gi.d[0] = ng.x; gi.d[1] = ng.y; gi.d[2] = ng.z;
-      }
-      const D6 inf = d6c(INFINITY);
-      integrate_adjoint(G, a, P, F, gF, gT, qv, nv, t.X[anc], nc, P.s_is_m ? gi : inf, P.s_is_m ? inf : gi);
+      wrench_adjoint<3>(G, a, P, F, gF, gT, poly, nv, t.X[anc], n, sgn, face, clipn, t.g, gint);
     }
     __syncwarp();
     adj_reduce_store(a, G, item, lane);
@@ -484,16 +403,7 @@ __global__ void __launch_bounds__(128, 4) adjoint_hs_kernel(StepArgs a) {
         if (a.adj_wrench && a.apply_forces) {
           V3<float> face[4];
           tet_face_normals(t.X, face);
-          QD qv[kMaxPolyV];
-          tangent_polygon<1>(poly, nv, t.X[anc], n, face, face, t.g, qv);
-          const V6 nc = rot_dir6(n * sgn);
-          D6 gi = d6c(gint);
-          if (gint != 0.f) {
-            const V3<float> ng = cross(n, t.g);
-            gi.d[0] = ng.x; gi.d[1] = ng.y; gi.d[2] = ng.z;
-          }
-          const D6 inf = d6c(INFINITY);
-          integrate_adjoint(G, a, P, F, gF, gT, qv, nv, t.X[anc], nc, P.s_is_m ? gi : inf, P.s_is_m ? inf : gi);
+          wrench_adjoint<1>(G, a, P, F, gF, gT, poly, nv, t.X[anc], n, sgn, face, face, t.g, gint);
         }
       }
     }
