@@ -102,7 +102,10 @@ typedef struct {
   int apply_forces;         /* cs::ApplyContactSurfaceForces (default 1)     */
   int use_graph;            /* capture hc_step in a CUDA graph (default 1)   */
   int64_t item_capacity;    /* cluster-pair work items (0 = automatic)       */
-  int64_t face_capacity;    /* contact polygons kept for surfaces/sensors    */
+  int64_t face_capacity;    /* initial capacity of contact polygons kept by
+                               steps in adjoint mode (0 = automatic; grows
+                               after an overflow, whose step's adjoint then
+                               recomputes the polygons)                     */
 } hc_config;
 
 /* Fill a config with defaults. */

@@ -220,17 +220,6 @@ __device__ __noinline__ void wrench_adjoint(AdjAcc& G, const StepArgs& a, const 
   G.gx[3] += tr.x; G.gx[4] += tr.y; G.gx[5] += tr.z;
 }
 
-// Unnormalised normals of the four faces of a tet (face k opposite vertex k).
-__device__ __forceinline__ void tet_face_normals(const V3<float> X[4], V3<float> face[4]) {
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int i0 = k == 0 ? 1 : 0;
-    const int i1 = k <= 1 ? 2 : 1;
-    const int i2 = k <= 2 ? 3 : 2;
-    face[k] = cross(X[i1] - X[i0], X[i2] - X[i0]);
-  }
-}
-
 __device__ __forceinline__ void adj_reduce_store(const StepArgs& a, const AdjAcc& G, int item, int lane) {
   double v[13];
 #pragma unroll
@@ -247,7 +236,13 @@ __device__ __forceinline__ void adj_reduce_store(const StepArgs& a, const AdjAcc
     for (int i = 0; i < 13; ++i) a.adj_item[(size_t)item * 16 + i] = v[i];
 }
 
+// True when the forward kept every polygon of the step as an adjoint record.
+__device__ __forceinline__ bool recs_valid(const StepArgs& a) { return a.use_recs && !(*a.status & 8); }
+
+// Recompute path (no records kept, or the record buffer overflowed): one warp
+// per item repeats the forward's staging and clipping.
 __global__ void __launch_bounds__(128, 4) adjoint_sr_kernel(StepArgs a) {
+  if (recs_valid(a)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   SrWarpSmem& W = reinterpret_cast<SrWarpSmem*>(smem_raw)[wid];
@@ -339,6 +334,7 @@ __global__ void __launch_bounds__(128, 4) adjoint_sr_kernel(StepArgs a) {
 }
 
 __global__ void __launch_bounds__(128, 4) adjoint_hs_kernel(StepArgs a) {
+  if (recs_valid(a)) return;
   __shared__ TetStage s_tet[kNarrowWarps][kCluster];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   while (true) {
@@ -412,6 +408,119 @@ __global__ void __launch_bounds__(128, 4) adjoint_hs_kernel(StepArgs a) {
   }
 }
 
+// ---- record path ------------------------------------------------------------
+// Records are kept in the order warps reached the counter; their gradients
+// are stored in pair order (items are ordered by pair): slot = first record
+// of the item (exclusive scan of the items' polygon counts) + sequence number.
+// Soft-soft items keep no records and are left out of the scan.
+__device__ __forceinline__ int rec_items_end(const StepArgs& a) {
+  const int total = *a.item_total;
+  return min(a.unit_off[a.type_unit_begin[2]], total);
+}
+
+__global__ void poly_count_kernel(StepArgs a) {
+  if (!recs_valid(a)) return;
+  const int end = rec_items_end(a);
+  if ((int)(blockIdx.x * blockDim.x) >= end) {
+    if (threadIdx.x == 0) a.poly_block_sum[blockIdx.x] = 0;
+    return;
+  }
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = i < end ? a.item_out[i].n_poly : 0;
+  __shared__ int tot;
+  block_excl_scan(v, &tot);
+  if (threadIdx.x == 0) a.poly_block_sum[blockIdx.x] = tot;
+}
+
+__global__ void poly_scan_kernel(StepArgs a) {
+  if (!recs_valid(a)) return;
+  __shared__ int carry;
+  __shared__ int tot;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < a.n_item_blocks; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const int v = i < a.n_item_blocks ? a.poly_block_sum[i] : 0;
+    const int ex = block_excl_scan(v, &tot);
+    if (i < a.n_item_blocks) a.poly_block_sum[i] = ex + carry;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    // items from rec_items_end on (soft-soft) start at the total
+    const int total = *a.item_total, end = rec_items_end(a);
+    for (int i = end; i <= total; ++i) a.item_poly_off[i] = carry;
+  }
+}
+
+__global__ void poly_emit_kernel(StepArgs a) {
+  if (!recs_valid(a)) return;
+  const int end = rec_items_end(a);
+  if ((int)(blockIdx.x * blockDim.x) >= end) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = i < end ? a.item_out[i].n_poly : 0;
+  __shared__ int tot;
+  const int ex = block_excl_scan(v, &tot) + a.poly_block_sum[blockIdx.x];
+  if (i < end) a.item_poly_off[i] = ex;
+}
+
+// Adjoint of one kept polygon: the taxel part (the forward's raster
+// function on the same values re-identifies the won samples) and the wrench
+// part.
+template <int ND>
+__device__ __forceinline__ void rec_adjoint(const StepArgs& a, const AdjPoly& R, AdjAcc& G) {
+  const PairDev& P = a.pairs[R.pair];
+  const FrameDev& F = a.frames[R.pair];
+  PV<float, ND> poly[kMaxPolyV];
+  const int nv = R.nv;
+  for (int i = 0; i < nv; ++i) {
+    const float4 v = *reinterpret_cast<const float4*>(R.v[i]);
+    poly[i].x = v.x; poly[i].y = v.y; poly[i].z = v.z; poly[i].p = v.w;
+#pragma unroll
+    for (int j = 0; j < ND; ++j) poly[i].d[j] = 0.f;
+    poly[i].lab = (i < 4 ? R.lab0 >> (8 * i) : R.lab1 >> (8 * (i - 4))) & 0xFF;
+  }
+  const V3<float> anc = mk(R.anc[0], R.anc[1], R.anc[2]);
+  const V3<float> n = mk(R.n[0], R.n[1], R.n[2]);
+  const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
+  if (a.adj_taxel) {
+    if (P.sensor0 >= 0)
+      raster_keys<ND>(a, P.sensor0, F.Rl, F.tl, poly, nv, anc, g, n, a.sensors[P.sensor0].geom == P.gs, &G);
+    if (P.sensor1 >= 0)
+      raster_keys<ND>(a, P.sensor1, F.Rl1, F.tl1, poly, nv, anc, g, n, a.sensors[P.sensor1].geom == P.gs, &G);
+  }
+  if (a.adj_wrench && a.apply_forces) {
+    V3<float> face[4], clipn[3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) face[k] = mk(R.face[k][0], R.face[k][1], R.face[k][2]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) clipn[j] = mk(R.clip[j][0], R.clip[j][1], R.clip[j][2]);
+    const float* gF = a.adj_pair + 8 * (size_t)R.pair;
+    wrench_adjoint<ND>(G, a, P, F, gF, gF + 3, poly, nv, anc, n, P.s_is_m ? 1.f : -1.f, face, clipn, g, R.gint);
+  }
+}
+
+__global__ void __launch_bounds__(128, 4) adjoint_rec_kernel(StepArgs a) {
+  if (!recs_valid(a)) return;
+  const int n = min(*a.rec_count, a.rec_cap);
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const AdjPoly& R = a.recs[r];
+    const int2 key = a.rec_key[r];
+    const int dst = a.item_poly_off[key.x] + key.y;
+    if (dst < 0 || dst >= a.rec_cap) continue;
+    AdjAcc G;
+    adj_zero(G);
+    if (R.kind == 0) rec_adjoint<3>(a, R, G);
+    else rec_adjoint<1>(a, R, G);
+    float4* o = reinterpret_cast<float4*>(a.rec_grad + 16 * (size_t)dst);
+    o[0] = make_float4(G.gx[0], G.gx[1], G.gx[2], G.gx[3]);
+    o[1] = make_float4(G.gx[4], G.gx[5], G.glin[0], G.glin[1]);
+    o[2] = make_float4(G.glin[2], G.gang[0], G.gang[1], G.gang[2]);
+    o[3] = make_float4(G.gE, 0.f, 0.f, 0.f);
+  }
+}
+
 // Per pair: upstream adjoints of the soft-frame sums from dL/dwrench
 // (wrench = [R_S F_S ; R_S T_S + (x_S - x_M) x R_S F_S]).
 __global__ void adjoint_setup_kernel(StepArgs a) {
@@ -445,9 +554,22 @@ __global__ void adjoint_reduce_kernel(StepArgs a) {
   double v[13];
 #pragma unroll
   for (int k = 0; k < 13; ++k) v[k] = 0.0;
-  for (int i = b + lane; i < e; i += 32)
+  if (recs_valid(a)) {
+    // the pair's records, in pair order
+    const int rb = a.item_poly_off[b], re = a.item_poly_off[e];
+    for (int i = rb + lane; i < re; i += 32) {
+      const float4* g = reinterpret_cast<const float4*>(a.rec_grad + 16 * (size_t)i);
+      const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3];
+      v[0] += g0.x; v[1] += g0.y; v[2] += g0.z; v[3] += g0.w;
+      v[4] += g1.x; v[5] += g1.y; v[6] += g1.z; v[7] += g1.w;
+      v[8] += g2.x; v[9] += g2.y; v[10] += g2.z; v[11] += g2.w;
+      v[12] += g3.x;
+    }
+  } else {
+    for (int i = b + lane; i < e; i += 32)
 #pragma unroll
-    for (int k = 0; k < 13; ++k) v[k] += a.adj_item[(size_t)i * 16 + k];
+      for (int k = 0; k < 13; ++k) v[k] += a.adj_item[(size_t)i * 16 + k];
+  }
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1)
 #pragma unroll

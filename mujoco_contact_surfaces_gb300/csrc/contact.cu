@@ -402,6 +402,13 @@ int launch_adjoint(const StepArgs& a, cudaStream_t s) {
   if (a.n_pair <= 0) return 0;
   reset_next_kernel<<<1, 32, 0, s>>>(a); ++n;
   adjoint_setup_kernel<<<(a.n_pair + 127) / 128, 128, 0, s>>>(a); ++n;
+  if (a.use_recs) {
+    // kept polygons (each kernel returns at once if the records overflowed)
+    poly_count_kernel<<<a.n_item_blocks, kBpBlock, 0, s>>>(a); ++n;
+    poly_scan_kernel<<<1, kBpBlock, 0, s>>>(a); ++n;
+    poly_emit_kernel<<<a.n_item_blocks, kBpBlock, 0, s>>>(a); ++n;
+    adjoint_rec_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
+  }
   if (a.type_unit_end[0] > a.type_unit_begin[0]) {
     adjoint_sr_kernel<<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a); ++n;
   }

@@ -120,6 +120,7 @@ constexpr int kCntStatus = 1;  // bit 0 item overflow, 1 candidate, 2 polygon
 constexpr int kCntCand = 2;    // candidate records written
 constexpr int kCntPoly = 3;    // polygon records written
 constexpr int kCntNext = 4;    // three work counters, one per query type
+constexpr int kCntRec = 7;     // adjoint records kept (may exceed the capacity)
 
 int next_pow2(int n) {
   int p = 1;
@@ -197,6 +198,13 @@ struct hc_context {
   DevBuf<float> adj_pair, adj_taxel;
   DevBuf<double> adj_item, adj_out, adj_wrench;
   int adj_launches = 0;
+  // adjoint records (polygons kept by steps in adjoint mode)
+  DevBuf<hc::AdjPoly> recs;
+  DevBuf<int2> rec_key;
+  DevBuf<float> rec_grad;
+  DevBuf<int> item_poly_off, poly_block_sum;
+  int rec_cap = 0;
+  bool recs_step = false;  // the last step kept its polygons
 };
 
 namespace {
@@ -342,6 +350,17 @@ hc_status ensure_items(hc_context* c, int cap) {
   return HC_OK;
 }
 
+// Capacity of the adjoint records (polygons kept by a step in adjoint mode).
+hc_status ensure_recs(hc_context* c, int cap) {
+  if (cap <= c->rec_cap) return HC_OK;
+  HC_CUDA(c->recs.reserve(cap));
+  HC_CUDA(c->rec_key.reserve(cap));
+  HC_CUDA(c->rec_grad.reserve(16 * (size_t)cap));
+  c->rec_cap = cap;
+  invalidate_graph(c);
+  return HC_OK;
+}
+
 hc_status build_sensors(hc_context* c) {
   if (!c->sensors_dirty) return HC_OK;
   std::vector<hc::SensorDev> sd;
@@ -483,6 +502,12 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
   a.narrow_block = c->narrow_block;
   a.narrow_grid = std::max(1, c->n_sm * c->narrow_ctas_per_sm);
   a.keep_samples = c->adjoint_mode ? 1 : 0;
+  a.rec_count = c->counters.p + kCntRec;
+  if (c->adjoint_mode && c->rec_cap > 0) {
+    a.recs = c->recs.p;
+    a.rec_key = c->rec_key.p;
+    a.rec_cap = c->rec_cap;
+  }
   return a;
 }
 
@@ -493,6 +518,7 @@ hc_status run_step(hc_context* c, int want_polys, int want_pair) {
     return HC_OK;
   }
   hc::StepArgs a = make_args(c, want_polys, want_pair);
+  c->recs_step = a.recs != nullptr;
   HC_CUDA(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(int), c->stream));
   // samples kept by an earlier step and not consumed by an adjoint
   if (c->samples_dirty && c->samples.n) {
@@ -530,6 +556,12 @@ hc_status finish_step(hc_context* c) {
     int cnt[8];
     HC_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
     HC_CUDA(cudaStreamSynchronize(c->stream));
+    if (cnt[kCntStatus] & 8) {
+      // too many polygons for the records: this step's adjoint recomputes
+      // them; later steps keep them in the larger buffer
+      const int want = std::max(2 * c->rec_cap, cnt[kCntRec] + cnt[kCntRec] / 4 + 1024);
+      if (hc_status st = ensure_recs(c, want)) return st;
+    }
     if (!(cnt[kCntStatus] & 1)) return HC_OK;
     // overflow: the scan wrote the full total into unit_off[n_units]
     int total = 0;
@@ -1197,6 +1229,12 @@ hc_status hc_set_adjoint_mode(hc_context* c, int on) {
   if (hc_status st = need(c)) return st;
   if ((on != 0) != c->adjoint_mode) invalidate_graph(c);
   c->adjoint_mode = on != 0;
+  if (on) {
+    HC_CUDA(cudaSetDevice(c->device));
+    const int want = c->cfg.face_capacity > 0 ? (int)std::min<int64_t>(c->cfg.face_capacity, 1 << 30)
+                                              : std::max(1 << 15, 4 * c->item_cap);
+    if (hc_status st = ensure_recs(c, want)) return st;
+  }
   return HC_OK;
 }
 
@@ -1216,6 +1254,18 @@ static hc_status adjoint_launch(hc_context* c, const double* d_dw, const float* 
   a.adj_pair = c->adj_pair.p;
   a.adj_item = c->adj_item.p;
   a.adj_out = c->adj_out.p;
+  if (c->recs_step) {
+    a.n_item_blocks = std::max(1, (c->item_cap + hc::kBpBlock - 1) / hc::kBpBlock);
+    HC_CUDA(c->item_poly_off.reserve((size_t)c->item_cap + 1));
+    HC_CUDA(c->poly_block_sum.reserve((size_t)a.n_item_blocks));
+    a.use_recs = 1;
+    a.recs = c->recs.p;
+    a.rec_key = c->rec_key.p;
+    a.rec_cap = c->rec_cap;
+    a.item_poly_off = c->item_poly_off.p;
+    a.poly_block_sum = c->poly_block_sum.p;
+    a.rec_grad = c->rec_grad.p;
+  }
   c->adj_launches = hc::launch_adjoint(a, c->stream);
   HC_CUDA(cudaGetLastError());
   // the taxel adjoint claims (and clears) every won sample

@@ -99,4 +99,19 @@ struct PolyRec {
   float v[kMaxPolyV][4];       // vertices (x, y, z, pressure), soft frame
 };
 
+// Contact polygon kept by a forward step in adjoint mode, with what its
+// reverse pass needs (soft frame).  272 B.
+struct alignas(16) AdjPoly {
+  float v[kMaxPolyV][4];       // vertices relative to anc: x, y, z, pressure
+  float anc[3], gint;          // anchor (a tet vertex); gradient along n
+  float n[3];                  // section normal (triangle / plane normal)
+  int lab0;                    // constraint labels of vertices 0-3 (8 bits each)
+  float g[3];                  // soft pressure gradient
+  int lab1;                    // labels of vertices 4-7
+  float face[4][3];            // unnormalised tet face normals
+  float clip[3][3];            // clip-plane normals (soft-rigid)
+  int pair, nv, kind;          // kind: 0 soft-rigid, 1 half-space
+};
+static_assert(sizeof(AdjPoly) == 272, "AdjPoly layout");
+
 }  // namespace hc

@@ -40,7 +40,7 @@ struct StepArgs {
   int* item_total;
   int* item_next;     // one work counter per query type
   int* status;        // bit 0: item overflow, bit 1: candidate overflow,
-                      // bit 2: polygon overflow
+                      // bit 2: polygon overflow, bit 3: adjoint record overflow
   ItemOut* item_out;
   PairOut* pair_out;
   // sensors
@@ -75,6 +75,16 @@ struct StepArgs {
   float* adj_pair;           // per pair: dL/dF_S, dL/dT_S in the soft frame (8 floats)
   double* adj_item;          // per item: 13 gradient sums (stride 16)
   double* adj_out;           // per pair: [dL/dtwist M (6), N (6), dL/dE_M, dL/dE_N]
+  // adjoint records: polygons kept by the forward (null: none kept)
+  AdjPoly* recs;
+  int2* rec_key;             // (item, sequence number within the item)
+  int rec_cap;
+  int* rec_count;
+  int use_recs;              // the adjoint reads the kept polygons (when none overflowed)
+  int* item_poly_off;        // per item: first record of the item in pair order (item_cap + 1)
+  int* poly_block_sum;       // one per kBpBlock items
+  int n_item_blocks;         // item_cap / kBpBlock rounded up
+  float* rec_grad;           // per record in pair order: 13 gradient terms (stride 16)
 };
 
 constexpr int kBpBlock = 256;

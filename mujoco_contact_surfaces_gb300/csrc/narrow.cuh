@@ -440,6 +440,70 @@ __device__ __forceinline__ int build_queue(unsigned mask, unsigned short* q, int
   return __shfl_sync(0xffffffffu, incl, 31);
 }
 
+// Unnormalised normals of the four faces of a tet (face k opposite vertex k).
+__device__ __forceinline__ void tet_face_normals(const V3<float> X[4], V3<float> face[4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int i0 = k == 0 ? 1 : 0;
+    const int i1 = k <= 1 ? 2 : 1;
+    const int i2 = k <= 2 ? 3 : 2;
+    face[k] = cross(X[i1] - X[i0], X[i2] - X[i0]);
+  }
+}
+
+// Keeps this lane's polygon as an adjoint record.  All lanes of the warp
+// call it together once per round (`have` marks a polygon); the record's key
+// is (item, seq), seq being the polygon's rank among the item's polygons in
+// processing order (rounds, then lanes), so the keys do not depend on the
+// order in which warps reach the counter.
+template <int ND>
+__device__ __forceinline__ void keep_polygon(const StepArgs& a, bool have, int item, int& seq, int lane, int pair,
+                                             int kind, const PV<float, ND>* poly, int nv, V3<float> anc,
+                                             V3<float> n, V3<float> g, float gint, const V3<float>* X,
+                                             const float (*clip)[3]) {
+  const unsigned b = __ballot_sync(0xffffffffu, have);
+  if (!b) return;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(a.rec_count, __popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  const int rank = __popc(b & ((1u << lane) - 1u));
+  const int seq0 = seq;
+  seq += __popc(b);
+  if (!have) return;
+  const int r = base + rank;
+  if (r >= a.rec_cap) {
+    atomicOr(a.status, 8);
+    return;
+  }
+  a.rec_key[r] = make_int2(item, seq0 + rank);
+  AdjPoly& R = a.recs[r];
+  int l0 = 0, l1 = 0;
+  for (int i = 0; i < kMaxPolyV; ++i) {
+    const bool in = i < nv;
+    *reinterpret_cast<float4*>(R.v[i]) =
+        in ? make_float4(poly[i].x, poly[i].y, poly[i].z, poly[i].p) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int lb = in ? (poly[i].lab & 0xFF) : 0;
+    if (i < 4) l0 |= lb << (8 * i);
+    else l1 |= lb << (8 * (i - 4));
+  }
+  R.anc[0] = anc.x; R.anc[1] = anc.y; R.anc[2] = anc.z; R.gint = gint;
+  R.n[0] = n.x; R.n[1] = n.y; R.n[2] = n.z; R.lab0 = l0;
+  R.g[0] = g.x; R.g[1] = g.y; R.g[2] = g.z; R.lab1 = l1;
+  V3<float> face[4];
+  tet_face_normals(X, face);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    R.face[k][0] = face[k].x; R.face[k][1] = face[k].y; R.face[k][2] = face[k].z;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) R.clip[j][c] = clip ? clip[j][c] : 0.f;
+  R.pair = pair;
+  R.nv = nv;
+  R.kind = kind;
+}
+
 constexpr int kNarrowWarps = 4;
 
 // ============================================================================
@@ -628,45 +692,55 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
     const int total = build_queue(mask, W.q, lane);
     __syncwarp();
     const float sgn = P.s_is_m ? 1.f : -1.f;
+    int seq = 0;
     for (int base = 0; base < total; base += 32) {
       const int k = base + lane;
-      if (k >= total) continue;
-      const int e = W.q[k];
-      const int i = e & 31, j = e >> 5;
-      const TetStage& TS = W.tet[i];
-      const TriStage& T = W.tri[j];
-      double s[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) s[q] = plane64(T.n64, T.o64, TS.X[q][0], TS.X[q][1], TS.X[q][2]);
-      const bool allp = s[0] > kNearTol && s[1] > kNearTol && s[2] > kNearTol && s[3] > kNearTol;
-      const bool alln = s[0] < -kNearTol && s[1] < -kNearTol && s[2] < -kNearTol && s[3] < -kNearTol;
-      if (allp || alln) continue;
-      TetIn<float> t;
-      unstage_tet(TS, t);
-      const V3<float> n = mk(T.n[0], T.n[1], T.n[2]);
+      bool have = false;
       PV<float, 3> poly[kMaxPolyV];
-      Decide dc;
-      int anc = 0;
-      int nv = sr_poly_f(t, s, T, n, fmaxf(T.M, t.xmax), dc, anc, poly);
-      const int tet_idx = P.s_elem_off + sl * kCluster + i;
+      TetIn<float> t;
+      V3<float> n = mk(0.f, 0.f, 0.f);
+      int nv = 0, anc = 0, jt = 0;
       float gint = 0.f;
-      int flags = 0;
-      if (dc.unc) {
-        bool near;
-        nv = sr_fp64(a, T, tet_idx, s, anc, poly, near, gint);
-        flags = near ? 1 : 0;
-      } else if (nv >= 3) {
-        gint = dot(t.g, n);
-        if (fabsf(gint) <= 1e-5f * t.gl) gint = grad_along64(a, tet_idx, T.n64[0], T.n64[1], T.n64[2]);
-      }
-      if (nv < 3) continue;
-      ac.n_poly += 1;
-      ac.n_near += flags;
-      const V3<float> nc = n * sgn;
-      const float gM = P.s_is_m ? gint : INFINITY;
-      const float gN = P.s_is_m ? INFINITY : gint;
-      integrate_polygon<3>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN, t.g);
-      record<3>(a, it.x, poly, nv, t.X[anc], nc, TS.orig, T.orig, flags);
+      do {
+        if (k >= total) break;
+        const int e = W.q[k];
+        const int i = e & 31, j = e >> 5;
+        jt = j;
+        const TetStage& TS = W.tet[i];
+        const TriStage& T = W.tri[j];
+        double s[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s[q] = plane64(T.n64, T.o64, TS.X[q][0], TS.X[q][1], TS.X[q][2]);
+        const bool allp = s[0] > kNearTol && s[1] > kNearTol && s[2] > kNearTol && s[3] > kNearTol;
+        const bool alln = s[0] < -kNearTol && s[1] < -kNearTol && s[2] < -kNearTol && s[3] < -kNearTol;
+        if (allp || alln) break;
+        unstage_tet(TS, t);
+        n = mk(T.n[0], T.n[1], T.n[2]);
+        Decide dc;
+        nv = sr_poly_f(t, s, T, n, fmaxf(T.M, t.xmax), dc, anc, poly);
+        const int tet_idx = P.s_elem_off + sl * kCluster + i;
+        int flags = 0;
+        if (dc.unc) {
+          bool near;
+          nv = sr_fp64(a, T, tet_idx, s, anc, poly, near, gint);
+          flags = near ? 1 : 0;
+        } else if (nv >= 3) {
+          gint = dot(t.g, n);
+          if (fabsf(gint) <= 1e-5f * t.gl) gint = grad_along64(a, tet_idx, T.n64[0], T.n64[1], T.n64[2]);
+        }
+        if (nv < 3) break;
+        ac.n_poly += 1;
+        ac.n_near += flags;
+        const V3<float> nc = n * sgn;
+        const float gM = P.s_is_m ? gint : INFINITY;
+        const float gN = P.s_is_m ? INFINITY : gint;
+        integrate_polygon<3>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN, t.g);
+        record<3>(a, it.x, poly, nv, t.X[anc], nc, TS.orig, T.orig, flags);
+        have = true;
+      } while (0);
+      if (a.recs)
+        keep_polygon<3>(a, have, item, seq, lane, it.x, 0, poly, nv, t.X[have ? anc : 0], n, t.g, gint, t.X,
+                        W.tri[jt].en);
     }
     __syncwarp();
     warp_reduce_store(a, ac, item, lane);
@@ -741,6 +815,12 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
     const unsigned ballot = __ballot_sync(0xffffffffu, cand);
     const int total = __popc(ballot);
     const float sgn = P.s_is_m ? 1.f : -1.f;
+    bool have = false;
+    PV<float, 1> poly[kMaxPolyV];
+    TetIn<float> t;
+    const V3<float> n = mk(nf[0], nf[1], nf[2]);
+    int nv = 0, anc = 0;
+    float gint = 0.f;
     if (lane < total) {
       // the lane-th set bit of the ballot
       unsigned m = ballot;
@@ -750,15 +830,10 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
       double s[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) s[q] = plane64(n64, o64, TS.X[q][0], TS.X[q][1], TS.X[q][2]);
-      TetIn<float> t;
       unstage_tet(TS, t);
-      const V3<float> n = mk(nf[0], nf[1], nf[2]);
-      PV<float, 1> poly[kMaxPolyV];
       Decide dc;
-      int anc = 0;
-      int nv = hs_poly_f(t, s, n, dc, anc, poly);
+      nv = hs_poly_f(t, s, n, dc, anc, poly);
       const int tet_idx = P.s_elem_off + sl * kCluster + i;
-      float gint = 0.f;
       int flags = 0;
       if (dc.unc) {
         bool near;
@@ -776,7 +851,12 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
         const float gN = P.s_is_m ? INFINITY : gint;
         integrate_polygon<1>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN, t.g);
         record<1>(a, it.x, poly, nv, t.X[anc], nc, TS.orig, -1, flags);
+        have = true;
       }
+    }
+    if (a.recs) {
+      int seq = 0;
+      keep_polygon<1>(a, have, item, seq, lane, it.x, 1, poly, nv, t.X[have ? anc : 0], n, t.g, gint, t.X, nullptr);
     }
     __syncwarp();
     warp_reduce_store(a, ac, item, lane);

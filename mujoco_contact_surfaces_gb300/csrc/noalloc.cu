@@ -63,7 +63,7 @@ struct Carve {
 };
 
 // Word layout of the counter block (the same meaning as hc_step's).
-constexpr int kWTotal = 0, kWStatus = 1, kWCand = 2, kWPoly = 3, kWNext = 4, kWords = 8;
+constexpr int kWTotal = 0, kWStatus = 1, kWCand = 2, kWPoly = 3, kWNext = 4, kWRec = 7, kWords = 8;
 
 // The wrench part of the per-pair records, to the caller's n_pair x 6 array.
 __global__ void wrench_out_kernel(const hc::PairOut* __restrict__ po, int n_pair, double* __restrict__ w) {
@@ -147,6 +147,10 @@ extern "C" HC_API hc_status hc_step_noalloc(hc_context* ctx, int n_geom, const d
   a.want_polys = 0;
   a.want_pair = -1;
   a.keep_samples = 0;
+  a.recs = nullptr;
+  a.rec_key = nullptr;
+  a.rec_cap = 0;
+  a.rec_count = words + kWRec;
 
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : v.stream;
   // The array keeps the previous call's contents: the counter words must

@@ -15,7 +15,8 @@ from . import _lib as L
 
 class Engine:
     def __init__(self, device: int = 0, representation: int = L.REPR_TRIANGLE, apply_forces: bool = True,
-                 use_graph: bool = True, item_capacity: int = 0):
+                 use_graph: bool = True, item_capacity: int = 0,
+                 face_capacity: int = 0):
         self.lib = L.load()
         cfg = L.hc_config()
         self.lib.hc_config_default(C.byref(cfg))
@@ -24,6 +25,7 @@ class Engine:
         cfg.apply_forces = int(apply_forces)
         cfg.use_graph = int(use_graph)
         cfg.item_capacity = item_capacity
+        cfg.face_capacity = face_capacity
         self.ctx = C.c_void_p()
         L.check(self.lib.hc_context_create(C.byref(cfg), C.byref(self.ctx)))
         self.n_pair = 0

@@ -97,15 +97,48 @@ def test_wrench_and_taxel_gradient_tactile(gpu):
         assert err <= GRAD_RTOL, f"pair {p}: rel err {err:.2e}\n{got}\n{ref}"
 
 
+def _close_per_pair(d1, d2, rtol):
+    for p in range(d1.shape[0]):
+        a, b = d1[p].ravel(), d2[p].ravel()
+        assert np.linalg.norm(a - b) <= rtol * max(np.linalg.norm(b), 1e-30), (p, a, b)
+
+
 def test_taxel_gradient_without_adjoint_mode(gpu):
-    # the adjoint re-runs the step to recover the ray hits
+    # without adjoint mode the adjoint re-runs the step to recover the ray
+    # hits and recomputes the polygons; in adjoint mode it reads the polygons
+    # the step kept.  The two paths agree to float rounding.
     s = scenes.tactile(2, velocities=False, plate_half=(0.0401, 0.04, 0.005))
     rng = np.random.default_rng(3)
     dLdw = np.zeros((len(s.g1), 6))
     dLdt = [rng.normal(size=256) for _ in s.sensors]
     _, _, d1, _ = run_adjoint(s, dLdw, dLdt, adjoint_mode=False)
     _, _, d2, _ = run_adjoint(s, dLdw, dLdt, adjoint_mode=True)
-    np.testing.assert_allclose(d1, d2, rtol=1e-6, atol=1e-9)
+    _close_per_pair(d1, d2, 1e-5)
+
+
+def test_kept_polygons_match_recompute_and_overflow_falls_back(gpu):
+    # a record capacity of 16 polygons overflows on the first step: that
+    # step's adjoint recomputes the polygons; the capacity then grows and the
+    # next step's adjoint reads the kept polygons
+    s = scenes.tactile(6, velocities=True, plate_half=(0.0401, 0.04, 0.005))
+    rng = np.random.default_rng(9)
+    dLdw = rng.normal(size=(len(s.g1), 6))
+    dt = np.concatenate([rng.normal(size=256) * 1e-3 for _ in s.sensors]).astype(np.float32)
+    ref = scenes.build_engine(s)
+    ref.set_adjoint_mode(True)
+    ref.step()
+    d_ref, e_ref = ref.adjoint(dLdw, dt)
+    ref.close()
+    eng = scenes.build_engine(s, face_capacity=16)
+    eng.set_adjoint_mode(True)
+    eng.step()
+    d1, e1 = eng.adjoint(dLdw, dt)        # overflowed: recompute path
+    eng.step()
+    d2, e2 = eng.adjoint(dLdw, dt)        # grown: kept polygons
+    eng.close()
+    _close_per_pair(d1, d_ref, 1e-5)
+    _close_per_pair(e1, e_ref, 1e-5)
+    assert np.array_equal(d2, d_ref) and np.array_equal(e2, e_ref)
 
 
 def test_modulus_gradient_is_linear_response(gpu):
