@@ -467,57 +467,90 @@ __global__ void poly_emit_kernel(StepArgs a) {
 
 // Adjoint of one kept polygon: the taxel part (the forward's raster
 // function on the same values re-identifies the won samples) and the wrench
-// part.
+// part, as two phases that the warp enters together.
 template <int ND>
-__device__ __forceinline__ void rec_adjoint(const StepArgs& a, const AdjPoly& R, AdjAcc& G) {
-  const PairDev& P = a.pairs[R.pair];
-  const FrameDev& F = a.frames[R.pair];
-  PV<float, ND> poly[kMaxPolyV];
-  const int nv = R.nv;
-  for (int i = 0; i < nv; ++i) {
+__device__ __forceinline__ void rec_unpack(const AdjPoly& R, PV<float, ND>* poly) {
+  for (int i = 0; i < R.nv; ++i) {
     const float4 v = *reinterpret_cast<const float4*>(R.v[i]);
     poly[i].x = v.x; poly[i].y = v.y; poly[i].z = v.z; poly[i].p = v.w;
 #pragma unroll
     for (int j = 0; j < ND; ++j) poly[i].d[j] = 0.f;
     poly[i].lab = (i < 4 ? R.lab0 >> (8 * i) : R.lab1 >> (8 * (i - 4))) & 0xFF;
   }
+}
+
+template <int ND>
+__device__ __noinline__ void rec_taxel(const StepArgs& a, const AdjPoly& R, AdjAcc& G) {
+  const PairDev& P = a.pairs[R.pair];
+  const FrameDev& F = a.frames[R.pair];
+  PV<float, ND> poly[kMaxPolyV];
+  rec_unpack<ND>(R, poly);
   const V3<float> anc = mk(R.anc[0], R.anc[1], R.anc[2]);
   const V3<float> n = mk(R.n[0], R.n[1], R.n[2]);
   const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
-  if (a.adj_taxel) {
-    if (P.sensor0 >= 0)
-      raster_keys<ND>(a, P.sensor0, F.Rl, F.tl, poly, nv, anc, g, n, a.sensors[P.sensor0].geom == P.gs, &G);
-    if (P.sensor1 >= 0)
-      raster_keys<ND>(a, P.sensor1, F.Rl1, F.tl1, poly, nv, anc, g, n, a.sensors[P.sensor1].geom == P.gs, &G);
-  }
-  if (a.adj_wrench && a.apply_forces) {
-    V3<float> face[4], clipn[3];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) face[k] = mk(R.face[k][0], R.face[k][1], R.face[k][2]);
-#pragma unroll
-    for (int j = 0; j < 3; ++j) clipn[j] = mk(R.clip[j][0], R.clip[j][1], R.clip[j][2]);
-    const float* gF = a.adj_pair + 8 * (size_t)R.pair;
-    wrench_adjoint<ND>(G, a, P, F, gF, gF + 3, poly, nv, anc, n, P.s_is_m ? 1.f : -1.f, face, clipn, g, R.gint);
-  }
+  if (P.sensor0 >= 0)
+    raster_keys<ND>(a, P.sensor0, F.Rl, F.tl, poly, R.nv, anc, g, n, a.sensors[P.sensor0].geom == P.gs, &G);
+  if (P.sensor1 >= 0)
+    raster_keys<ND>(a, P.sensor1, F.Rl1, F.tl1, poly, R.nv, anc, g, n, a.sensors[P.sensor1].geom == P.gs, &G);
 }
 
+template <int ND>
+__device__ __noinline__ void rec_wrench(const StepArgs& a, const AdjPoly& R, AdjAcc& G) {
+  const PairDev& P = a.pairs[R.pair];
+  const FrameDev& F = a.frames[R.pair];
+  PV<float, ND> poly[kMaxPolyV];
+  rec_unpack<ND>(R, poly);
+  const V3<float> anc = mk(R.anc[0], R.anc[1], R.anc[2]);
+  const V3<float> n = mk(R.n[0], R.n[1], R.n[2]);
+  const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
+  V3<float> face[4], clipn[3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) face[k] = mk(R.face[k][0], R.face[k][1], R.face[k][2]);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) clipn[j] = mk(R.clip[j][0], R.clip[j][1], R.clip[j][2]);
+  const float* gF = a.adj_pair + 8 * (size_t)R.pair;
+  wrench_adjoint<ND>(G, a, P, F, gF, gF + 3, poly, R.nv, anc, n, P.s_is_m ? 1.f : -1.f, face, clipn, g, R.gint);
+}
+
+// Warp-uniform loop over the records (every lane runs every iteration, so the
+// phases can end with a full-warp reconvergence).
 __global__ void __launch_bounds__(128, 4) adjoint_rec_kernel(StepArgs a) {
   if (!recs_valid(a)) return;
   const int n = min(*a.rec_count, a.rec_cap);
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-    const AdjPoly& R = a.recs[r];
-    const int2 key = a.rec_key[r];
-    const int dst = a.item_poly_off[key.x] + key.y;
-    if (dst < 0 || dst >= a.rec_cap) continue;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n_warps = (gridDim.x * blockDim.x) >> 5;
+  const bool taxel = a.adj_taxel != nullptr, wrench = a.adj_wrench != nullptr && a.apply_forces;
+  for (int base = warp * 32; base < n; base += n_warps * 32) {
+    const int r = base + lane;
+    const bool ok = r < n;
+    const AdjPoly& R = a.recs[ok ? r : base];
+    int dst = -1;
+    if (ok) {
+      const int2 key = a.rec_key[r];
+      dst = a.item_poly_off[key.x] + key.y;
+    }
+    const bool on = ok && dst >= 0 && dst < a.rec_cap;
+    const int kind = on ? R.kind : 0;
     AdjAcc G;
     adj_zero(G);
-    if (R.kind == 0) rec_adjoint<3>(a, R, G);
-    else rec_adjoint<1>(a, R, G);
-    float4* o = reinterpret_cast<float4*>(a.rec_grad + 16 * (size_t)dst);
-    o[0] = make_float4(G.gx[0], G.gx[1], G.gx[2], G.gx[3]);
-    o[1] = make_float4(G.gx[4], G.gx[5], G.glin[0], G.glin[1]);
-    o[2] = make_float4(G.glin[2], G.gang[0], G.gang[1], G.gang[2]);
-    o[3] = make_float4(G.gE, 0.f, 0.f, 0.f);
+    if (taxel && on) {
+      if (kind == 0) rec_taxel<3>(a, R, G);
+      else rec_taxel<1>(a, R, G);
+    }
+    __syncwarp();
+    if (wrench && on) {
+      if (kind == 0) rec_wrench<3>(a, R, G);
+      else rec_wrench<1>(a, R, G);
+    }
+    __syncwarp();
+    if (on) {
+      float4* o = reinterpret_cast<float4*>(a.rec_grad + 16 * (size_t)dst);
+      o[0] = make_float4(G.gx[0], G.gx[1], G.gx[2], G.gx[3]);
+      o[1] = make_float4(G.gx[4], G.gx[5], G.glin[0], G.glin[1]);
+      o[2] = make_float4(G.glin[2], G.gang[0], G.gang[1], G.gang[2]);
+      o[3] = make_float4(G.gE, 0.f, 0.f, 0.f);
+    }
   }
 }
 

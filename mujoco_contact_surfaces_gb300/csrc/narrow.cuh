@@ -170,12 +170,10 @@ __device__ __noinline__ void raster_keys(const StepArgs& a, int sid, const float
 }
 
 // Quadrature of one polygon (vertices relative to `anc`, soft frame) and its
-// contribution to forces and sensors.  n: contact normal out of N into M;
-// g: the soft (M-side for soft-soft) pressure gradient, soft frame.
+// forces.  n: contact normal out of N into M.
 template <int ND>
-__device__ void integrate_polygon(const StepArgs& a, const PairDev& P, const FrameDev& F, Acc& ac,
-                                  const PV<float, ND>* v, int nv, V3<float> anc, V3<float> n, float gM, float gN,
-                                  V3<float> g) {
+__device__ void integrate_forces(const StepArgs& a, const PairDev& P, const FrameDev& F, Acc& ac,
+                                 const PV<float, ND>* v, int nv, V3<float> anc, V3<float> n, float gM, float gN) {
   float A = 0.f, pcen = 0.f;
   V3<float> c = mk(0.f, 0.f, 0.f);
   const V3<float> v0 = pv_pos(v[0]);
@@ -209,8 +207,24 @@ __device__ void integrate_polygon(const StepArgs& a, const PairDev& P, const Fra
       point_force(ac, F, P.damping, P.mu, a.apply_forces, Ai, cen, n, gM, gN, p0);
     }
   }
+}
+
+// Ray binning of one polygon for the flat sensors of the pair.  g: the soft
+// (M-side for soft-soft) pressure gradient, soft frame.
+template <int ND>
+__device__ __forceinline__ void raster_polygon(const StepArgs& a, const PairDev& P, const FrameDev& F,
+                                               const PV<float, ND>* v, int nv, V3<float> anc, V3<float> n,
+                                               V3<float> g) {
   if (P.sensor0 >= 0) raster_keys<ND>(a, P.sensor0, F.Rl, F.tl, v, nv, anc, g, n, 0, nullptr);
   if (P.sensor1 >= 0) raster_keys<ND>(a, P.sensor1, F.Rl1, F.tl1, v, nv, anc, g, n, 0, nullptr);
+}
+
+template <int ND>
+__device__ void integrate_polygon(const StepArgs& a, const PairDev& P, const FrameDev& F, Acc& ac,
+                                  const PV<float, ND>* v, int nv, V3<float> anc, V3<float> n, float gM, float gN,
+                                  V3<float> g) {
+  integrate_forces<ND>(a, P, F, ac, v, nv, anc, n, gM, gN);
+  raster_polygon<ND>(a, P, F, v, nv, anc, n, g);
 }
 
 template <int ND>
@@ -699,7 +713,7 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
       PV<float, 3> poly[kMaxPolyV];
       TetIn<float> t;
       V3<float> n = mk(0.f, 0.f, 0.f);
-      int nv = 0, anc = 0, jt = 0;
+      int nv = 0, anc = 0, jt = 0, orig_a = 0, orig_b = 0, flags = 0;
       float gint = 0.f;
       do {
         if (k >= total) break;
@@ -719,7 +733,6 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
         Decide dc;
         nv = sr_poly_f(t, s, T, n, fmaxf(T.M, t.xmax), dc, anc, poly);
         const int tet_idx = P.s_elem_off + sl * kCluster + i;
-        int flags = 0;
         if (dc.unc) {
           bool near;
           nv = sr_fp64(a, T, tet_idx, s, anc, poly, near, gint);
@@ -731,13 +744,22 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
         if (nv < 3) break;
         ac.n_poly += 1;
         ac.n_near += flags;
-        const V3<float> nc = n * sgn;
-        const float gM = P.s_is_m ? gint : INFINITY;
-        const float gN = P.s_is_m ? INFINITY : gint;
-        integrate_polygon<3>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN, t.g);
-        record<3>(a, it.x, poly, nv, t.X[anc], nc, TS.orig, T.orig, flags);
+        orig_a = TS.orig;
+        orig_b = T.orig;
         have = true;
       } while (0);
+      // forces, records and rays as separate phases the warp enters together
+      __syncwarp();
+      const V3<float> nc = n * sgn;
+      if (have) {
+        const float gM = P.s_is_m ? gint : INFINITY;
+        const float gN = P.s_is_m ? INFINITY : gint;
+        integrate_forces<3>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN);
+        record<3>(a, it.x, poly, nv, t.X[anc], nc, orig_a, orig_b, flags);
+      }
+      __syncwarp();
+      if (have) raster_polygon<3>(a, P, F, poly, nv, t.X[anc], nc, t.g);
+      __syncwarp();
       if (a.recs)
         keep_polygon<3>(a, have, item, seq, lane, it.x, 0, poly, nv, t.X[have ? anc : 0], n, t.g, gint, t.X,
                         W.tri[jt].en);
@@ -819,7 +841,7 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
     PV<float, 1> poly[kMaxPolyV];
     TetIn<float> t;
     const V3<float> n = mk(nf[0], nf[1], nf[2]);
-    int nv = 0, anc = 0;
+    int nv = 0, anc = 0, orig_a = 0, flags = 0;
     float gint = 0.f;
     if (lane < total) {
       // the lane-th set bit of the ballot
@@ -834,7 +856,6 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
       Decide dc;
       nv = hs_poly_f(t, s, n, dc, anc, poly);
       const int tet_idx = P.s_elem_off + sl * kCluster + i;
-      int flags = 0;
       if (dc.unc) {
         bool near;
         nv = hs_fp64(a, F, tet_idx, s, anc, poly, near, gint);
@@ -846,14 +867,22 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
       if (nv >= 3) {
         ac.n_poly += 1;
         ac.n_near += flags;
-        const V3<float> nc = n * sgn;
-        const float gM = P.s_is_m ? gint : INFINITY;
-        const float gN = P.s_is_m ? INFINITY : gint;
-        integrate_polygon<1>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN, t.g);
-        record<1>(a, it.x, poly, nv, t.X[anc], nc, TS.orig, -1, flags);
+        orig_a = TS.orig;
         have = true;
       }
     }
+    // forces, records and rays as separate phases the warp enters together
+    __syncwarp();
+    const V3<float> nc = n * sgn;
+    if (have) {
+      const float gM = P.s_is_m ? gint : INFINITY;
+      const float gN = P.s_is_m ? INFINITY : gint;
+      integrate_forces<1>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN);
+      record<1>(a, it.x, poly, nv, t.X[anc], nc, orig_a, -1, flags);
+    }
+    __syncwarp();
+    if (have) raster_polygon<1>(a, P, F, poly, nv, t.X[anc], nc, t.g);
+    __syncwarp();
     if (a.recs) {
       int seq = 0;
       keep_polygon<1>(a, have, item, seq, lane, it.x, 1, poly, nv, t.X[have ? anc : 0], n, t.g, gint, t.X, nullptr);
