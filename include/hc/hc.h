@@ -102,10 +102,11 @@ typedef struct {
   int apply_forces;         /* cs::ApplyContactSurfaceForces (default 1)     */
   int use_graph;            /* capture hc_step in a CUDA graph (default 1)   */
   int64_t item_capacity;    /* cluster-pair work items (0 = automatic)       */
-  int64_t face_capacity;    /* initial capacity of contact polygons kept by
-                               steps in adjoint mode (0 = automatic; grows
-                               after an overflow, whose step's adjoint then
-                               recomputes the polygons)                     */
+  int64_t face_capacity;    /* initial capacity of the contact polygons a
+                               step keeps when sensors are attached or in
+                               adjoint mode (0 = automatic; on overflow the
+                               next synchronising call grows it and re-runs
+                               the step)                                    */
 } hc_config;
 
 /* Fill a config with defaults. */

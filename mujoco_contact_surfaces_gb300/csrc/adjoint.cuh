@@ -512,6 +512,32 @@ __device__ __noinline__ void rec_wrench(const StepArgs& a, const AdjPoly& R, Adj
   wrench_adjoint<ND>(G, a, P, F, gF, gF + 3, poly, R.nv, anc, n, P.s_is_m ? 1.f : -1.f, face, clipn, g, R.gint);
 }
 
+// Forward ray binning of the kept polygons, one thread per polygon (the
+// same raster function and inputs as the adjoint's, so keys are identical).
+template <int ND>
+__device__ __noinline__ void rec_raster(const StepArgs& a, const AdjPoly& R) {
+  const PairDev& P = a.pairs[R.pair];
+  const FrameDev& F = a.frames[R.pair];
+  PV<float, ND> poly[kMaxPolyV];
+  rec_unpack<ND>(R, poly);
+  const V3<float> anc = mk(R.anc[0], R.anc[1], R.anc[2]);
+  const V3<float> n = mk(R.n[0], R.n[1], R.n[2]);
+  const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
+  raster_polygon<ND>(a, P, F, poly, R.nv, anc, n, g);
+}
+
+__global__ void __launch_bounds__(128, 4) raster_rec_kernel(StepArgs a) {
+  if (*a.status & 8) return;   // records incomplete: the step is re-run after growth
+  const int n = min(*a.rec_count, a.rec_cap);
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const AdjPoly& R = a.recs[r];
+    const PairDev& P = a.pairs[R.pair];
+    if (P.sensor0 < 0 && P.sensor1 < 0) continue;
+    if (R.kind == 0) rec_raster<3>(a, R);
+    else rec_raster<1>(a, R);
+  }
+}
+
 // Warp-uniform loop over the records (every lane runs every iteration, so the
 // phases can end with a full-warp reconvergence).
 __global__ void __launch_bounds__(128, 4) adjoint_rec_kernel(StepArgs a) {

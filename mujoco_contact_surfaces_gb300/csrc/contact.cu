@@ -443,6 +443,9 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   if (a.type_unit_end[2] > a.type_unit_begin[2]) {
     narrow_ss_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
   }
+  if (a.recs && a.n_sensor > 0 && a.type_unit_end[1] > a.type_unit_begin[0]) {
+    raster_rec_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
+  }
   if (ev) cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal);
   if (a.n_pair > 0) {
     reduce_kernel<<<(a.n_pair * 32 + 127) / 128, 128, 0, s>>>(a); ++n;

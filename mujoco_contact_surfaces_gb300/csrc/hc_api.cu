@@ -350,7 +350,13 @@ hc_status ensure_items(hc_context* c, int cap) {
   return HC_OK;
 }
 
-// Capacity of the adjoint records (polygons kept by a step in adjoint mode).
+// Capacity of the polygon records (kept by steps with sensors or in adjoint
+// mode).
+int initial_rec_cap(const hc_context* c) {
+  return c->cfg.face_capacity > 0 ? (int)std::min<int64_t>(c->cfg.face_capacity, 1 << 30)
+                                  : std::max(1 << 15, 4 * c->item_cap);
+}
+
 hc_status ensure_recs(hc_context* c, int cap) {
   if (cap <= c->rec_cap) return HC_OK;
   HC_CUDA(c->recs.reserve(cap));
@@ -503,7 +509,9 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
   a.narrow_grid = std::max(1, c->n_sm * c->narrow_ctas_per_sm);
   a.keep_samples = c->adjoint_mode ? 1 : 0;
   a.rec_count = c->counters.p + kCntRec;
-  if (c->adjoint_mode && c->rec_cap > 0) {
+  // polygons are kept as records (rays cast from them, adjoint reads them)
+  // in adjoint mode and whenever sensors are attached
+  if ((c->adjoint_mode || c->n_cells > 0) && c->rec_cap > 0) {
     a.recs = c->recs.p;
     a.rec_key = c->rec_key.p;
     a.rec_cap = c->rec_cap;
@@ -556,22 +564,21 @@ hc_status finish_step(hc_context* c) {
     int cnt[8];
     HC_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
     HC_CUDA(cudaStreamSynchronize(c->stream));
+    if (!(cnt[kCntStatus] & 9)) return HC_OK;
     if (cnt[kCntStatus] & 8) {
-      // too many polygons for the records: this step's adjoint recomputes
-      // them; later steps keep them in the larger buffer
+      // too many polygons for the records (rays and adjoint): grow, re-run
       const int want = std::max(2 * c->rec_cap, cnt[kCntRec] + cnt[kCntRec] / 4 + 1024);
       if (hc_status st = ensure_recs(c, want)) return st;
     }
-    if (!(cnt[kCntStatus] & 1)) return HC_OK;
-    // overflow: the scan wrote the full total into unit_off[n_units]
-    int total = 0;
-    HC_CUDA(cudaMemcpy(&total, c->unit_off.p + c->n_units, sizeof(int), cudaMemcpyDeviceToHost));
-    hc_status st = ensure_items(c, std::max(2 * c->item_cap, total + total / 4 + 1024));
-    if (st) return st;
-    st = run_step(c, 0, -1);
-    if (st) return st;
+    if (cnt[kCntStatus] & 1) {
+      // item overflow: the scan wrote the full total into unit_off[n_units]
+      int total = 0;
+      HC_CUDA(cudaMemcpy(&total, c->unit_off.p + c->n_units, sizeof(int), cudaMemcpyDeviceToHost));
+      if (hc_status st = ensure_items(c, std::max(2 * c->item_cap, total + total / 4 + 1024))) return st;
+    }
+    if (hc_status st = run_step(c, 0, -1)) return st;
   }
-  return fail(HC_ERR_OVERFLOW, "work-item capacity overflow persisted");
+  return fail(HC_ERR_OVERFLOW, "work-item or polygon-record capacity overflow persisted");
 }
 
 hc_status need(hc_context* c) {
@@ -955,6 +962,8 @@ hc_status hc_set_pairs(hc_context* c, int n_pair, const int* g1, const int* g2, 
   HC_CUDA(c->block_sum.reserve(c->n_bp_blocks));
   int want = c->cfg.item_capacity > 0 ? (int)c->cfg.item_capacity : std::max(1 << 16, 64 * n_pair);
   if (hc_status st = ensure_items(c, want)) return st;
+  if (c->n_cells > 0 || c->adjoint_mode)
+    if (hc_status st = ensure_recs(c, initial_rec_cap(c))) return st;
   HC_CUDA(cudaStreamSynchronize(s));
   invalidate_graph(c);
   c->stepped = false;
@@ -1231,9 +1240,7 @@ hc_status hc_set_adjoint_mode(hc_context* c, int on) {
   c->adjoint_mode = on != 0;
   if (on) {
     HC_CUDA(cudaSetDevice(c->device));
-    const int want = c->cfg.face_capacity > 0 ? (int)std::min<int64_t>(c->cfg.face_capacity, 1 << 30)
-                                              : std::max(1 << 15, 4 * c->item_cap);
-    if (hc_status st = ensure_recs(c, want)) return st;
+    if (hc_status st = ensure_recs(c, initial_rec_cap(c))) return st;
   }
   return HC_OK;
 }

@@ -116,6 +116,16 @@ __device__ __noinline__ void raster_keys(const StepArgs& a, int sid, const float
   const int Y0 = max(0, (int)fy0), Y1 = min(S.ny - 1, (int)fy1);
   unsigned long long* smp = a.samples + S.sample_off;
   const float p0 = v[0].p;
+  // edge vectors (vertex i to its successor), static indices only
+  float ex[kMaxPolyV], ey[kMaxPolyV];
+#pragma unroll
+  for (int i = 0; i < kMaxPolyV; ++i) {
+    const bool last = i + 1 >= nv;
+    const float nx = last ? lx[0] : lx[i + 1 < kMaxPolyV ? i + 1 : 0];
+    const float ny = last ? ly[0] : ly[i + 1 < kMaxPolyV ? i + 1 : 0];
+    ex[i] = nx - lx[i];
+    ey[i] = ny - ly[i];
+  }
   for (int X = X0; X <= X1; ++X) {
     const float qx = sx[X];
     for (int Y = Y0; Y <= Y1; ++Y) {
@@ -124,9 +134,8 @@ __device__ __noinline__ void raster_keys(const StepArgs& a, int sid, const float
 #pragma unroll
       for (int i = 0; i < kMaxPolyV; ++i) {
         if (i < nv) {
-          const int k = i + 1 == nv ? 0 : i + 1;
-          const float ex = (lx[k] - lx[i]) * (qy - ly[i]) - (ly[k] - ly[i]) * (qx - lx[i]);
-          in &= sgn * ex >= 0.f;
+          const float e = ex[i] * (qy - ly[i]) - ey[i] * (qx - lx[i]);
+          in &= sgn * e >= 0.f;
         }
       }
       if (!in) continue;
@@ -435,6 +444,19 @@ __device__ __forceinline__ int next_item(const StepArgs& a, int q, int lane, int
   return ib + __shfl_sync(0xffffffffu, item, 0);
 }
 
+// The next chunk of kChunk consecutive items of query type q for this warp
+// (consecutive items usually share their pair and other cluster, whose
+// staged elements the warp then keeps).
+constexpr int kChunk = 4;
+__device__ __forceinline__ int next_chunk(const StepArgs& a, int q, int lane, int& ie) {
+  const int total = *a.item_total;
+  const int ib = min(a.unit_off[a.type_unit_begin[q]], total);
+  ie = min(a.unit_off[a.type_unit_end[q]], total);
+  int c = 0;
+  if (lane == 0) c = atomicAdd(a.item_next + q, kChunk);
+  return ib + __shfl_sync(0xffffffffu, c, 0);
+}
+
 // Compact the warp's candidate masks (bit j of lane i: element pair (i, j))
 // into a queue of (i | j << 5) entries in lane-major order.
 __device__ __forceinline__ int build_queue(unsigned mask, unsigned short* q, int lane) {
@@ -672,22 +694,31 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   SrWarpSmem& W = reinterpret_cast<SrWarpSmem*>(smem_raw)[wid];
+  int staged_pair = -1, staged_oc = -1;   // other cluster held in W.tri
   while (true) {
     int ie;
-    const int item = next_item(a, 0, lane, ie);
-    if (item >= ie) break;
+    const int c0 = next_chunk(a, 0, lane, ie);
+    if (c0 >= ie) break;
+    const int c1 = min(c0 + kChunk, ie);
+  for (int item = c0; item < c1; ++item) {
     const int4 it = a.items[item];
     const PairDev& P = a.pairs[it.x];
     const FrameDev& F = a.frames[it.x];
     Acc ac;
     acc_zero(ac);
     const int sl = it.y, oc = it.z;
+    __syncwarp();
     if (F.valid) {
-      stage_tri(a, P, F, oc * kCluster + lane, W.tri[lane]);
+      if (it.x != staged_pair || oc != staged_oc) {
+        stage_tri(a, P, F, oc * kCluster + lane, W.tri[lane]);
+        staged_pair = it.x;
+        staged_oc = oc;
+      }
       stage_tet(a, P, sl * kCluster + lane, W.tet[lane]);
     } else {
       W.tri[lane].valid = 0;
       W.tet[lane].valid = 0;
+      staged_pair = -1;
     }
     __syncwarp();
     // candidate queue
@@ -758,7 +789,8 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
         record<3>(a, it.x, poly, nv, t.X[anc], nc, orig_a, orig_b, flags);
       }
       __syncwarp();
-      if (have) raster_polygon<3>(a, P, F, poly, nv, t.X[anc], nc, t.g);
+      // with kept polygons the rays are cast by raster_rec_kernel
+      if (have && !a.recs) raster_polygon<3>(a, P, F, poly, nv, t.X[anc], nc, t.g);
       __syncwarp();
       if (a.recs)
         keep_polygon<3>(a, have, item, seq, lane, it.x, 0, poly, nv, t.X[have ? anc : 0], n, t.g, gint, t.X,
@@ -766,6 +798,7 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
     }
     __syncwarp();
     warp_reduce_store(a, ac, item, lane);
+  }
   }
 }
 
@@ -881,7 +914,7 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
       record<1>(a, it.x, poly, nv, t.X[anc], nc, orig_a, -1, flags);
     }
     __syncwarp();
-    if (have) raster_polygon<1>(a, P, F, poly, nv, t.X[anc], nc, t.g);
+    if (have && !a.recs) raster_polygon<1>(a, P, F, poly, nv, t.X[anc], nc, t.g);
     __syncwarp();
     if (a.recs) {
       int seq = 0;

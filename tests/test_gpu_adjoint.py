@@ -116,10 +116,22 @@ def test_taxel_gradient_without_adjoint_mode(gpu):
     _close_per_pair(d1, d2, 1e-5)
 
 
+def _device_doubles(ptr, shape):
+    import torch
+
+    class _View:
+        __cuda_array_interface__ = {"shape": shape, "typestr": "<f8", "data": (ptr, False), "version": 2}
+
+    return torch.as_tensor(_View(), device="cuda").cpu().numpy().copy()
+
+
 def test_kept_polygons_match_recompute_and_overflow_falls_back(gpu):
-    # a record capacity of 16 polygons overflows on the first step: that
-    # step's adjoint recomputes the polygons; the capacity then grows and the
-    # next step's adjoint reads the kept polygons
+    # A record capacity of 16 polygons overflows.  In a device-only flow
+    # (step, then the device adjoint, no synchronisation) nothing re-runs the
+    # step, so its wrench adjoint recomputes the polygons; a host call
+    # re-runs the step with a grown capacity and the adjoint reads the kept
+    # polygons, bit-identical to an engine that never overflowed.
+    torch = pytest.importorskip("torch")
     s = scenes.tactile(6, velocities=True, plate_half=(0.0401, 0.04, 0.005))
     rng = np.random.default_rng(9)
     dLdw = rng.normal(size=(len(s.g1), 6))
@@ -128,16 +140,21 @@ def test_kept_polygons_match_recompute_and_overflow_falls_back(gpu):
     ref.set_adjoint_mode(True)
     ref.step()
     d_ref, e_ref = ref.adjoint(dLdw, dt)
+    ref.step()
+    dw_ref, ew_ref = ref.adjoint(dLdw, None)
     ref.close()
     eng = scenes.build_engine(s, face_capacity=16)
     eng.set_adjoint_mode(True)
     eng.step()
-    d1, e1 = eng.adjoint(dLdw, dt)        # overflowed: recompute path
+    d_dw = torch.tensor(dLdw, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    g = _device_doubles(eng.adjoint_device(d_dw.data_ptr(), None), (len(s.g1), 14))
+    torch.cuda.synchronize()
+    _close_per_pair(g[:, :12].reshape(-1, 2, 6), dw_ref, 1e-5)
+    _close_per_pair(g[:, 12:], ew_ref, 1e-5)
     eng.step()
-    d2, e2 = eng.adjoint(dLdw, dt)        # grown: kept polygons
+    d2, e2 = eng.adjoint(dLdw, dt)       # re-run after growth: kept polygons
     eng.close()
-    _close_per_pair(d1, d_ref, 1e-5)
-    _close_per_pair(e1, e_ref, 1e-5)
     assert np.array_equal(d2, d_ref) and np.array_equal(e2, e_ref)
 
 
