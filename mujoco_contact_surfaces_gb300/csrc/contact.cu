@@ -327,7 +327,7 @@ __global__ void reduce_kernel(StepArgs a) {
   int c[3] = {0, 0, 0};
   for (int i = b + lane; i < e; i += 32) {
     const ItemOut& r = a.item_out[i];
-    for (int k = 0; k < 8; ++k) v[k] += r.v[k];
+    for (int k = 0; k < 8; ++k) v[k] += (double)r.hi[k] + (double)r.lo[k];
     c[0] += r.n_poly; c[1] += r.n_faces; c[2] += r.n_near;
   }
 #pragma unroll

@@ -61,8 +61,9 @@ struct FrameDev {
 
 // Per-item outputs (one item = soft leaf cluster x other cluster).
 struct ItemOut {
-  double v[8];          // F(3), T(3) about the soft origin in the soft frame,
-                        // area, total fn0
+  float hi[8], lo[8];   // F(3), T(3) about the soft origin in the soft frame,
+                        // area, total fn0; each the unevaluated sum hi + lo
+                        // of a double-float warp reduction (~48-bit)
   int n_poly, n_faces, n_near, pad;
 };
 

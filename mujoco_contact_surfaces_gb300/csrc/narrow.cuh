@@ -415,20 +415,47 @@ __device__ __forceinline__ void to_f(const PV<double, ND>* in, int n, PV<float, 
   }
 }
 
+// Error-free float addition (Knuth's TwoSum) and double-float accumulation;
+// the _rn intrinsics keep the compiler from contracting or reassociating.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void df_add(float& hi, float& lo, float h2, float l2) {
+  float s, e;
+  two_sum(hi, h2, s, e);
+  e = __fadd_rn(e, __fadd_rn(lo, l2));
+  hi = __fadd_rn(s, e);
+  lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
+
+// Fixed-order butterfly of the lanes' sums in double-float arithmetic (on
+// the FP32 pipe; FP64 runs at 1/64 of the FP32 rate on this part); lane 0
+// stores the item's (hi, lo) pairs.
 __device__ __forceinline__ void warp_reduce_store(const StepArgs& a, const Acc& ac, int item, int lane) {
-  double v[8] = {ac.F[0], ac.F[1], ac.F[2], ac.T[0], ac.T[1], ac.T[2], ac.area, ac.fn0};
+  float hi[8] = {ac.F[0], ac.F[1], ac.F[2], ac.T[0], ac.T[1], ac.T[2], ac.area, ac.fn0};
+  float lo[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   int c3[3] = {ac.n_poly, ac.n_faces, ac.n_near};
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    for (int i = 0; i < 8; ++i) {
+      const float h2 = __shfl_xor_sync(0xffffffffu, hi[i], o);
+      const float l2 = __shfl_xor_sync(0xffffffffu, lo[i], o);
+      df_add(hi[i], lo[i], h2, l2);
+    }
 #pragma unroll
     for (int i = 0; i < 3; ++i) c3[i] += __shfl_xor_sync(0xffffffffu, c3[i], o);
   }
   if (lane == 0) {
     ItemOut r;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) r.v[i] = v[i];
+    for (int i = 0; i < 8; ++i) {
+      r.hi[i] = hi[i];
+      r.lo[i] = lo[i];
+    }
     r.n_poly = c3[0]; r.n_faces = c3[1]; r.n_near = c3[2]; r.pad = 0;
     a.item_out[item] = r;
   }
