@@ -307,8 +307,11 @@ HC_API hc_status hc_get_timings(hc_context* ctx, hc_timings* out);
 HC_API hc_status hc_get_stream(hc_context* ctx, void** stream);
 /* Number of kernels one hc_step launches for the current pairs/sensors. */
 HC_API hc_status hc_get_launch_count(hc_context* ctx, int* n);
-/* Autotune the narrow-phase launch shape on the current pairs and poses. */
-HC_API hc_status hc_autotune(hc_context* ctx, int* chosen_block, int* chosen_ctas_per_sm);
+/* Autotune the launch shape on the current pairs and poses: the grid of the
+ * persistent kernels (CTAs per SM, 2-8) and the soft-rigid work-queue chunk
+ * (consecutive work items a warp takes, 1-8), timed over three steps each;
+ * the fastest is kept for later steps.  Outputs may be NULL.              */
+HC_API hc_status hc_autotune(hc_context* ctx, int* chosen_ctas_per_sm, int* chosen_chunk);
 
 /* ---- step without device allocation -------------------------------------
  * No counterpart in the reference: the plugin has no such call.

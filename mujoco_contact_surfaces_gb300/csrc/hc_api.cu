@@ -190,7 +190,7 @@ struct hc_context {
   cudaEvent_t ev[6] = {};
   hc_timings last_timings = {};
   int launches_per_step = 0;
-  int narrow_block = 128, narrow_ctas_per_sm = 8;
+  int narrow_block = 128, narrow_ctas_per_sm = 8, narrow_chunk = 4;
   int n_sm = 0;
   // adjoint
   bool adjoint_mode = false;   // steps keep the won taxel samples
@@ -507,6 +507,7 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
   a.want_pair = want_pair;
   a.narrow_block = c->narrow_block;
   a.narrow_grid = std::max(1, c->n_sm * c->narrow_ctas_per_sm);
+  a.chunk = std::max(1, c->narrow_chunk);
   a.keep_samples = c->adjoint_mode ? 1 : 0;
   a.rec_count = c->counters.p + kCntRec;
   // polygons are kept as records (rays cast from them, adjoint reads them)
@@ -1227,10 +1228,61 @@ hc_status hc_get_launch_count(hc_context* c, int* n) {
   return HC_OK;
 }
 
-hc_status hc_autotune(hc_context* c, int* chosen_block, int* chosen_ctas_per_sm) {
+// Sweep of the persistent kernels' grid (CTAs per SM) and the soft-rigid
+// work-queue chunk on the current pairs and poses: each shape is warmed up
+// (graph captured) and timed over three steps with the stage events; the
+// fastest step wins.  Results do not depend on the shape (per-item sums are
+// deterministic and reduced in a fixed order).
+hc_status hc_autotune(hc_context* c, int* chosen_ctas_per_sm, int* chosen_chunk) {
   if (hc_status st = need(c)) return st;
-  if (chosen_block) *chosen_block = c->narrow_block;
-  if (chosen_ctas_per_sm) *chosen_ctas_per_sm = c->narrow_ctas_per_sm;
+  if (!c->poses_set || c->pairs_h.empty()) return fail(HC_ERR_NOT_READY, "set pairs and poses before autotuning");
+  HC_CUDA(cudaSetDevice(c->device));
+  if (hc_status st = hc_step(c)) return st;
+  if (hc_status st = finish_step(c)) return st;
+  const bool was_timing = c->timing;
+  const int old_ctas = c->narrow_ctas_per_sm, old_chunk = c->narrow_chunk;
+  c->timing = true;
+  static const int kCtas[] = {2, 3, 4, 6, 8};
+  static const int kChunks[] = {1, 2, 4, 8};
+  float best = INFINITY;
+  int best_ctas = old_ctas, best_chunk = old_chunk;
+  for (int ct : kCtas) {
+    for (int ch : kChunks) {
+      c->narrow_ctas_per_sm = ct;
+      c->narrow_chunk = ch;
+      invalidate_graph(c);
+      hc_status st = run_step(c, 0, -1);
+      if (!st) st = finish_step(c);
+      float tot = 0.f;
+      for (int r = 0; r < 3 && !st; ++r) {
+        st = run_step(c, 0, -1);
+        if (st) break;
+        cudaError_t e = cudaEventSynchronize(c->ev[5]);
+        if (e != cudaSuccess) { st = fail(HC_ERR_CUDA, cudaGetErrorString(e)); break; }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[0], c->ev[5]);
+        tot += ms;
+      }
+      if (st) {
+        c->narrow_ctas_per_sm = old_ctas;
+        c->narrow_chunk = old_chunk;
+        c->timing = was_timing;
+        invalidate_graph(c);
+        return st;
+      }
+      if (tot < best) {
+        best = tot;
+        best_ctas = ct;
+        best_chunk = ch;
+      }
+    }
+  }
+  c->narrow_ctas_per_sm = best_ctas;
+  c->narrow_chunk = best_chunk;
+  c->timing = was_timing;
+  invalidate_graph(c);
+  if (chosen_ctas_per_sm) *chosen_ctas_per_sm = best_ctas;
+  if (chosen_chunk) *chosen_chunk = best_chunk;
   return HC_OK;
 }
 

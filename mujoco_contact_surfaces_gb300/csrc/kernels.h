@@ -68,6 +68,7 @@ struct StepArgs {
   // launch shape of the narrow phase
   int narrow_block;
   int narrow_grid;
+  int chunk;          // consecutive items a soft-rigid warp takes at once
   // adjoint
   int keep_samples;          // taxel pass leaves the won samples for the adjoint
   const double* adj_wrench;  // dL/dwrench, n_pair x 6 (device) or null

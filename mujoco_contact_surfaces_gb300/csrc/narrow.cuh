@@ -471,16 +471,15 @@ __device__ __forceinline__ int next_item(const StepArgs& a, int q, int lane, int
   return ib + __shfl_sync(0xffffffffu, item, 0);
 }
 
-// The next chunk of kChunk consecutive items of query type q for this warp
+// The next chunk of a.chunk consecutive items of query type q for this warp
 // (consecutive items usually share their pair and other cluster, whose
 // staged elements the warp then keeps).
-constexpr int kChunk = 4;
 __device__ __forceinline__ int next_chunk(const StepArgs& a, int q, int lane, int& ie) {
   const int total = *a.item_total;
   const int ib = min(a.unit_off[a.type_unit_begin[q]], total);
   ie = min(a.unit_off[a.type_unit_end[q]], total);
   int c = 0;
-  if (lane == 0) c = atomicAdd(a.item_next + q, kChunk);
+  if (lane == 0) c = atomicAdd(a.item_next + q, a.chunk);
   return ib + __shfl_sync(0xffffffffu, c, 0);
 }
 
@@ -726,7 +725,7 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
     int ie;
     const int c0 = next_chunk(a, 0, lane, ie);
     if (c0 >= ie) break;
-    const int c1 = min(c0 + kChunk, ie);
+    const int c1 = min(c0 + a.chunk, ie);
   for (int item = c0; item < c1; ++item) {
     const int4 it = a.items[item];
     const PairDev& P = a.pairs[it.x];

@@ -174,6 +174,13 @@ class Engine:
         L.check(self.lib.hc_get_timings(self.ctx, C.byref(t)))
         return t
 
+    def autotune(self):
+        """Pick the persistent kernels' grid and the work-queue chunk on the
+        current pairs and poses; returns (ctas_per_sm, chunk)."""
+        ct, ch = C.c_int(), C.c_int()
+        L.check(self.lib.hc_autotune(self.ctx, C.byref(ct), C.byref(ch)))
+        return ct.value, ch.value
+
     def launch_count(self) -> int:
         n = C.c_int()
         L.check(self.lib.hc_get_launch_count(self.ctx, C.byref(n)))

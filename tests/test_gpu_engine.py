@@ -1,0 +1,114 @@
+"""Engine properties on the GPU: determinism, graph vs eager launches, the
+autotuner, capacity regrowth, non-finite poses, unsupported pairs and geom
+resizing.  Each compares the C-ABI outputs of two runs that must agree
+bit for bit."""
+import numpy as np
+import pytest
+
+from mujoco_contact_surfaces_gb300 import _lib as L
+from mujoco_contact_surfaces_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _outputs(eng, scene):
+    eng.step()
+    w = eng.wrenches()
+    t = eng.all_taxels() if scene.sensors else np.zeros(0, np.float32)
+    st = eng.pair_stats()
+    return w, t, np.array([x.n_polygons for x in st]), np.array([x.area for x in st])
+
+
+def _same(a, b):
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_step_is_deterministic_and_graph_matches_eager(gpu):
+    s = scenes.tactile(16, velocities=True)
+    e1 = scenes.build_engine(s)
+    e2 = scenes.build_engine(s, use_graph=False)
+    a, b = _outputs(e1, s), _outputs(e2, s)
+    c = _outputs(e1, s)
+    e1.close(); e2.close()
+    assert a[2].sum() > 0
+    _same(a, b)
+    _same(a, c)
+
+
+def test_autotune_keeps_results(gpu):
+    s = scenes.tactile(64, velocities=True)
+    eng = scenes.build_engine(s)
+    ref = _outputs(eng, s)
+    ct, ch = eng.autotune()
+    assert ct in (2, 3, 4, 6, 8) and ch in (1, 2, 4, 8)
+    _same(ref, _outputs(eng, s))
+    eng.close()
+
+
+def test_item_and_record_overflow_regrow(gpu):
+    s = scenes.batched(12, tet_range=(500, 4000), tri_range=(12, 600))
+    ref_eng = scenes.build_engine(s)
+    ref = _outputs(ref_eng, s)
+    ref_eng.close()
+    eng = scenes.build_engine(s, item_capacity=16, face_capacity=8)
+    got = _outputs(eng, s)
+    eng.close()
+    assert ref[2].sum() > 0
+    _same(ref, got)
+
+
+def test_nonfinite_pose_zeroes_its_pairs_only(gpu):
+    s = scenes.single_pair(6, velocities=True)
+    eng = scenes.build_engine(s)
+    ref = _outputs(eng, s)
+    xp = s.xpos.copy()
+    xp[s.g2[2], 1] = np.nan
+    eng.set_poses(xp, s.xmat, s.vel)
+    w, _, npoly, _ = _outputs(eng, s)
+    eng.close()
+    assert np.all(w[2] == 0.0) and npoly[2] == 0
+    keep = [p for p in range(len(s.g1)) if p != 2]
+    assert np.array_equal(w[keep], ref[0][keep])
+
+
+def test_unsupported_pairs_are_reported_and_skipped(gpu):
+    s = scenes.single_pair(2)
+    eng = scenes.build_engine(s)
+    ref = _outputs(eng, s)
+    # a rigid-rigid pair and a capsule (no contact surface) next to the real ones
+    k1 = eng.add_geom(100, L.GEOM_BOX, [0.1, 0.1, 0.1], [0, 1, 0, 0.5, 0.5])
+    assert k1 == L.RIGID
+    with pytest.raises(L.HCError) as ei:   # no capsule surface
+        eng.add_geom(101, L.GEOM_CAPSULE, [0.02, 0.05, 0], [1e5, 1, 0, 0.5, 0.5])
+    assert ei.value.status == L.HC_ERR_UNSUPPORTED
+    g1 = list(s.g1) + [100, 101]
+    g2 = list(s.g2) + [s.g2[0], s.g1[0]]
+    st, q = eng.set_pairs(g1, g2)
+    assert list(st[-2:]) == [L.HC_ERR_UNSUPPORTED, L.HC_ERR_UNSUPPORTED] and list(q[-2:]) == [0, 0]
+    xp = np.concatenate([s.xpos, np.zeros((102 - s.n_geom, 3))])
+    xm = np.concatenate([s.xmat, np.tile(np.eye(3).reshape(1, 9), (102 - s.n_geom, 1))])
+    v = np.concatenate([s.vel, np.zeros((102 - s.n_geom, 6))])
+    eng.set_poses(xp, xm, v)
+    eng.step()
+    w = eng.wrenches()
+    eng.close()
+    assert np.all(w[-2:] == 0.0)
+    assert np.array_equal(w[:-2], ref[0])
+
+
+def test_update_geom_size_matches_fresh_engine(gpu):
+    s = scenes.single_pair(3)
+    eng = scenes.build_engine(s)
+    _outputs(eng, s)
+    soft = s.g1[0]
+    new = list(s.geoms[soft]["size"])
+    new[0] *= 1.05
+    eng.update_geom_size(soft, new)
+    got = _outputs(eng, s)
+    eng.close()
+    s.geoms[soft]["size"] = new
+    fresh = scenes.build_engine(s)
+    ref = _outputs(fresh, s)
+    fresh.close()
+    _same(ref, got)
