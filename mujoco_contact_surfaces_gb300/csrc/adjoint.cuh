@@ -236,8 +236,10 @@ __device__ __forceinline__ void adj_reduce_store(const StepArgs& a, const AdjAcc
     for (int i = 0; i < 13; ++i) a.adj_item[(size_t)item * 16 + i] = v[i];
 }
 
-// True when the forward kept every polygon of the step as an adjoint record.
-__device__ __forceinline__ bool recs_valid(const StepArgs& a) { return a.use_recs && !(*a.status & 8); }
+// True when the step keeps its polygons as records and none overflowed.
+__device__ __forceinline__ bool rec_ok(const StepArgs& a) { return a.recs != nullptr && !(*a.status & 8); }
+// True when the adjoint can read the polygons the forward kept.
+__device__ __forceinline__ bool recs_valid(const StepArgs& a) { return a.use_recs && rec_ok(a); }
 
 // Recompute path (no records kept, or the record buffer overflowed): one warp
 // per item repeats the forward's staging and clipping.
@@ -419,7 +421,7 @@ __device__ __forceinline__ int rec_items_end(const StepArgs& a) {
 }
 
 __global__ void poly_count_kernel(StepArgs a) {
-  if (!recs_valid(a)) return;
+  if (!rec_ok(a)) return;
   const int end = rec_items_end(a);
   if ((int)(blockIdx.x * blockDim.x) >= end) {
     if (threadIdx.x == 0) a.poly_block_sum[blockIdx.x] = 0;
@@ -433,7 +435,7 @@ __global__ void poly_count_kernel(StepArgs a) {
 }
 
 __global__ void poly_scan_kernel(StepArgs a) {
-  if (!recs_valid(a)) return;
+  if (!rec_ok(a)) return;
   __shared__ int carry;
   __shared__ int tot;
   if (threadIdx.x == 0) carry = 0;
@@ -455,7 +457,7 @@ __global__ void poly_scan_kernel(StepArgs a) {
 }
 
 __global__ void poly_emit_kernel(StepArgs a) {
-  if (!recs_valid(a)) return;
+  if (!rec_ok(a)) return;
   const int end = rec_items_end(a);
   if ((int)(blockIdx.x * blockDim.x) >= end) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -512,10 +514,12 @@ __device__ __noinline__ void rec_wrench(const StepArgs& a, const AdjPoly& R, Adj
   wrench_adjoint<ND>(G, a, P, F, gF, gF + 3, poly, R.nv, anc, n, P.s_is_m ? 1.f : -1.f, face, clipn, g, R.gint);
 }
 
-// Forward ray binning of the kept polygons, one thread per polygon (the
-// same raster function and inputs as the adjoint's, so keys are identical).
+// Forward pass over the kept polygons, one thread per polygon: quadrature
+// and forces into the polygon's pair-ordered slot, and the sensors' rays
+// (the same raster function and inputs as the adjoint's, so keys are
+// identical).
 template <int ND>
-__device__ __noinline__ void rec_raster(const StepArgs& a, const AdjPoly& R) {
+__device__ __noinline__ void rec_forward(const StepArgs& a, const AdjPoly& R, RecOut& o) {
   const PairDev& P = a.pairs[R.pair];
   const FrameDev& F = a.frames[R.pair];
   PV<float, ND> poly[kMaxPolyV];
@@ -523,18 +527,29 @@ __device__ __noinline__ void rec_raster(const StepArgs& a, const AdjPoly& R) {
   const V3<float> anc = mk(R.anc[0], R.anc[1], R.anc[2]);
   const V3<float> n = mk(R.n[0], R.n[1], R.n[2]);
   const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
-  raster_polygon<ND>(a, P, F, poly, R.nv, anc, n, g);
+  const V3<float> nc = n * (P.s_is_m ? 1.f : -1.f);
+  Acc ac;
+  acc_zero(ac);
+  integrate_forces<ND>(a, P, F, ac, poly, R.nv, anc, nc, P.s_is_m ? R.gint : INFINITY, P.s_is_m ? INFINITY : R.gint);
+  o.F[0] = ac.F[0]; o.F[1] = ac.F[1]; o.F[2] = ac.F[2];
+  o.T[0] = ac.T[0]; o.T[1] = ac.T[1]; o.T[2] = ac.T[2];
+  o.area = ac.area; o.fn0 = ac.fn0; o.n_faces = ac.n_faces;
+  o.pad[0] = o.pad[1] = o.pad[2] = 0;
+  raster_polygon<ND>(a, P, F, poly, R.nv, anc, nc, g);
 }
 
-__global__ void __launch_bounds__(128, 4) raster_rec_kernel(StepArgs a) {
-  if (*a.status & 8) return;   // records incomplete: the step is re-run after growth
+__global__ void __launch_bounds__(128, 4) rec_forward_kernel(StepArgs a) {
+  if (!rec_ok(a)) return;   // records incomplete: the step is re-run after growth
   const int n = min(*a.rec_count, a.rec_cap);
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
     const AdjPoly& R = a.recs[r];
-    const PairDev& P = a.pairs[R.pair];
-    if (P.sensor0 < 0 && P.sensor1 < 0) continue;
-    if (R.kind == 0) rec_raster<3>(a, R);
-    else rec_raster<1>(a, R);
+    const int2 key = a.rec_key[r];
+    const int dst = a.item_poly_off[key.x] + key.y;
+    if (dst < 0 || dst >= a.rec_cap) continue;
+    RecOut o;
+    if (R.kind == 0) rec_forward<3>(a, R, o);
+    else rec_forward<1>(a, R, o);
+    a.rec_out[dst] = o;
   }
 }
 

@@ -330,6 +330,17 @@ __global__ void reduce_kernel(StepArgs a) {
     for (int k = 0; k < 8; ++k) v[k] += (double)r.hi[k] + (double)r.lo[k];
     c[0] += r.n_poly; c[1] += r.n_faces; c[2] += r.n_near;
   }
+  if (rec_ok(a)) {
+    // forces of the kept polygons, in pair order
+    const int rb = a.item_poly_off[b], re = a.item_poly_off[e];
+    for (int i = rb + lane; i < re; i += 32) {
+      const RecOut& r = a.rec_out[i];
+      v[0] += r.F[0]; v[1] += r.F[1]; v[2] += r.F[2];
+      v[3] += r.T[0]; v[4] += r.T[1]; v[5] += r.T[2];
+      v[6] += r.area; v[7] += r.fn0;
+      c[1] += r.n_faces;
+    }
+  }
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) {
 #pragma unroll
@@ -403,10 +414,8 @@ int launch_adjoint(const StepArgs& a, cudaStream_t s) {
   reset_next_kernel<<<1, 32, 0, s>>>(a); ++n;
   adjoint_setup_kernel<<<(a.n_pair + 127) / 128, 128, 0, s>>>(a); ++n;
   if (a.use_recs) {
-    // kept polygons (each kernel returns at once if the records overflowed)
-    poly_count_kernel<<<a.n_item_blocks, kBpBlock, 0, s>>>(a); ++n;
-    poly_scan_kernel<<<1, kBpBlock, 0, s>>>(a); ++n;
-    poly_emit_kernel<<<a.n_item_blocks, kBpBlock, 0, s>>>(a); ++n;
+    // kept polygons, in the slots the forward assigned (returns at once if
+    // the records overflowed)
     adjoint_rec_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
   }
   if (a.type_unit_end[0] > a.type_unit_begin[0]) {
@@ -443,8 +452,12 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   if (a.type_unit_end[2] > a.type_unit_begin[2]) {
     narrow_ss_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
   }
-  if (a.recs && a.n_sensor > 0 && a.type_unit_end[1] > a.type_unit_begin[0]) {
-    raster_rec_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
+  if (a.recs && a.type_unit_end[1] > a.type_unit_begin[0]) {
+    // kept polygons: pair-ordered slots, then forces and rays per polygon
+    poly_count_kernel<<<a.n_item_blocks, kBpBlock, 0, s>>>(a); ++n;
+    poly_scan_kernel<<<1, kBpBlock, 0, s>>>(a); ++n;
+    poly_emit_kernel<<<a.n_item_blocks, kBpBlock, 0, s>>>(a); ++n;
+    rec_forward_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
   }
   if (ev) cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal);
   if (a.n_pair > 0) {

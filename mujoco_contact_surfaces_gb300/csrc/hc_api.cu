@@ -201,6 +201,7 @@ struct hc_context {
   // adjoint records (polygons kept by steps in adjoint mode)
   DevBuf<hc::AdjPoly> recs;
   DevBuf<int2> rec_key;
+  DevBuf<hc::RecOut> rec_out;
   DevBuf<float> rec_grad;
   DevBuf<int> item_poly_off, poly_block_sum;
   int rec_cap = 0;
@@ -341,13 +342,15 @@ bool finite_all(const double* p, size_t n) {
   return true;
 }
 
+hc_status ensure_rec_offsets(hc_context* c);
+
 hc_status ensure_items(hc_context* c, int cap) {
   if (cap <= c->item_cap) return HC_OK;
   HC_CUDA(c->items.reserve(cap));
   HC_CUDA(c->item_out.reserve(cap));
   c->item_cap = cap;
   invalidate_graph(c);
-  return HC_OK;
+  return ensure_rec_offsets(c);
 }
 
 // Capacity of the polygon records (kept by steps with sensors or in adjoint
@@ -357,14 +360,27 @@ int initial_rec_cap(const hc_context* c) {
                                   : std::max(1 << 15, 4 * c->item_cap);
 }
 
-hc_status ensure_recs(hc_context* c, int cap) {
-  if (cap <= c->rec_cap) return HC_OK;
-  HC_CUDA(c->recs.reserve(cap));
-  HC_CUDA(c->rec_key.reserve(cap));
-  HC_CUDA(c->rec_grad.reserve(16 * (size_t)cap));
-  c->rec_cap = cap;
+// Per-item record offsets: item_cap + 1 ints and one block sum per kBpBlock items.
+hc_status ensure_rec_offsets(hc_context* c) {
+  if (c->rec_cap == 0) return HC_OK;
+  const size_t blocks = (size_t)std::max(1, (c->item_cap + hc::kBpBlock - 1) / hc::kBpBlock);
+  if ((size_t)c->item_cap + 1 <= c->item_poly_off.n && blocks <= c->poly_block_sum.n) return HC_OK;
+  HC_CUDA(c->item_poly_off.reserve((size_t)c->item_cap + 1));
+  HC_CUDA(c->poly_block_sum.reserve(blocks));
   invalidate_graph(c);
   return HC_OK;
+}
+
+hc_status ensure_recs(hc_context* c, int cap) {
+  if (cap > c->rec_cap) {
+    HC_CUDA(c->recs.reserve(cap));
+    HC_CUDA(c->rec_key.reserve(cap));
+    HC_CUDA(c->rec_out.reserve(cap));
+    HC_CUDA(c->rec_grad.reserve(16 * (size_t)cap));
+    c->rec_cap = cap;
+    invalidate_graph(c);
+  }
+  return ensure_rec_offsets(c);
 }
 
 hc_status build_sensors(hc_context* c) {
@@ -516,6 +532,10 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
     a.recs = c->recs.p;
     a.rec_key = c->rec_key.p;
     a.rec_cap = c->rec_cap;
+    a.rec_out = c->rec_out.p;
+    a.item_poly_off = c->item_poly_off.p;
+    a.poly_block_sum = c->poly_block_sum.p;
+    a.n_item_blocks = std::max(1, (c->item_cap + hc::kBpBlock - 1) / hc::kBpBlock);
   }
   return a;
 }
@@ -1314,16 +1334,20 @@ static hc_status adjoint_launch(hc_context* c, const double* d_dw, const float* 
   a.adj_item = c->adj_item.p;
   a.adj_out = c->adj_out.p;
   if (c->recs_step) {
+    // the polygons the last step kept, in the slots it assigned
     a.n_item_blocks = std::max(1, (c->item_cap + hc::kBpBlock - 1) / hc::kBpBlock);
-    HC_CUDA(c->item_poly_off.reserve((size_t)c->item_cap + 1));
-    HC_CUDA(c->poly_block_sum.reserve((size_t)a.n_item_blocks));
     a.use_recs = 1;
     a.recs = c->recs.p;
     a.rec_key = c->rec_key.p;
     a.rec_cap = c->rec_cap;
+    a.rec_out = c->rec_out.p;
     a.item_poly_off = c->item_poly_off.p;
     a.poly_block_sum = c->poly_block_sum.p;
     a.rec_grad = c->rec_grad.p;
+  } else {
+    a.recs = nullptr;
+    a.rec_key = nullptr;
+    a.rec_cap = 0;
   }
   c->adj_launches = hc::launch_adjoint(a, c->stream);
   HC_CUDA(cudaGetLastError());

@@ -115,4 +115,10 @@ struct alignas(16) AdjPoly {
 };
 static_assert(sizeof(AdjPoly) == 272, "AdjPoly layout");
 
+// Forces of one kept polygon (soft frame), in the pair-ordered record slot.
+struct alignas(16) RecOut {
+  float F[3], T[3], area, fn0;
+  int n_faces, pad[3];
+};
+
 }  // namespace hc

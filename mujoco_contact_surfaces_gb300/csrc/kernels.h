@@ -86,6 +86,7 @@ struct StepArgs {
   int* poly_block_sum;       // one per kBpBlock items
   int n_item_blocks;         // item_cap / kBpBlock rounded up
   float* rec_grad;           // per record in pair order: 13 gradient terms (stride 16)
+  RecOut* rec_out;           // per record in pair order: forces (forward)
 };
 
 constexpr int kBpBlock = 256;

@@ -701,9 +701,9 @@ __device__ __noinline__ int sr_fp64(const StepArgs& a, const TriStage& T, int te
   return nv;
 }
 
-// FP32 soft-rigid polygon: one compiled body shared by the forward and the
-// adjoint kernels (bit-identical polygons, hence identical taxel keys).
-__device__ __noinline__ int sr_poly_f(const TetIn<float>& t, const double* s, const TriStage& T, V3<float> n,
+// FP32 soft-rigid polygon (inlined: its inputs and outputs stay out of
+// local memory where the compiler can keep them in registers).
+__device__ __forceinline__ int sr_poly_f(const TetIn<float>& t, const double* s, const TriStage& T, V3<float> n,
                                       float M, Decide& dc, int& anc, PV<float, 3>* out) {
   PV<float, 3> tmp[kMaxPolyV];
   return sr_polygon<float>(t, s, T, n, M, dc, anc, out, tmp);
@@ -811,11 +811,12 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
       if (have) {
         const float gM = P.s_is_m ? gint : INFINITY;
         const float gN = P.s_is_m ? INFINITY : gint;
-        integrate_forces<3>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN);
+        // with kept polygons the forces are integrated by rec_forward_kernel
+        if (!a.recs) integrate_forces<3>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN);
         record<3>(a, it.x, poly, nv, t.X[anc], nc, orig_a, orig_b, flags);
       }
       __syncwarp();
-      // with kept polygons the rays are cast by raster_rec_kernel
+      // with kept polygons the rays are cast by rec_forward_kernel
       if (have && !a.recs) raster_polygon<3>(a, P, F, poly, nv, t.X[anc], nc, t.g);
       __syncwarp();
       if (a.recs)
@@ -936,7 +937,7 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
     if (have) {
       const float gM = P.s_is_m ? gint : INFINITY;
       const float gN = P.s_is_m ? INFINITY : gint;
-      integrate_forces<1>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN);
+      if (!a.recs) integrate_forces<1>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN);
       record<1>(a, it.x, poly, nv, t.X[anc], nc, orig_a, -1, flags);
     }
     __syncwarp();
