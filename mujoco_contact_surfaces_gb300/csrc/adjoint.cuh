@@ -467,130 +467,334 @@ __global__ void poly_emit_kernel(StepArgs a) {
   if (i < end) a.item_poly_off[i] = ex;
 }
 
-// Adjoint of one kept polygon: the taxel part (the forward's raster
-// function on the same values re-identifies the won samples) and the wrench
-// part, as two phases that the warp enters together.
-template <int ND>
-__device__ __forceinline__ void rec_unpack(const AdjPoly& R, PV<float, ND>* poly) {
-  for (int i = 0; i < R.nv; ++i) {
-    const float4 v = *reinterpret_cast<const float4*>(R.v[i]);
-    poly[i].x = v.x; poly[i].y = v.y; poly[i].z = v.z; poly[i].p = v.w;
+// ---- record kernels: a group of kGroup lanes per kept polygon -------------
+// The lanes of a group share the polygon's work: its quadrature points
+// (kTriangle: one fan triangle per lane), its ray samples (strided over the
+// bounding box), and in the adjoint one vertex per lane.  Group sums use a
+// fixed shuffle order, so results are deterministic.
+constexpr int kGroup = 8;
+
+__device__ __forceinline__ float gsum(float v) {
+  v += __shfl_xor_sync(0xffffffffu, v, 4);
+  v += __shfl_xor_sync(0xffffffffu, v, 2);
+  v += __shfl_xor_sync(0xffffffffu, v, 1);
+  return v;
+}
+__device__ __forceinline__ V3<float> gsum3(V3<float> v) { return mk(gsum(v.x), gsum(v.y), gsum(v.z)); }
+
+__device__ __forceinline__ float4 rec_vtx(const AdjPoly& R, int i) { return *reinterpret_cast<const float4*>(R.v[i]); }
+__device__ __forceinline__ V3<float> rec_pos(const AdjPoly& R, int i) {
+  const float4 v = rec_vtx(R, i);
+  return mk(v.x, v.y, v.z);
+}
+
+// Polygon sums of the quadrature: signed area A, the
+// area-weighted centroid c and the pressure pc there (every lane of the
+// group computes them).
+__device__ __forceinline__ void rec_fan(const AdjPoly& R, int nv, V3<float> n, float& A, V3<float>& c, float& pc) {
+  A = 0.f;
+  pc = 0.f;
+  c = mk(0.f, 0.f, 0.f);
+  const float4 v0 = rec_vtx(R, 0);
+  const V3<float> x0 = mk(v0.x, v0.y, v0.z);
 #pragma unroll
-    for (int j = 0; j < ND; ++j) poly[i].d[j] = 0.f;
-    poly[i].lab = (i < 4 ? R.lab0 >> (8 * i) : R.lab1 >> (8 * (i - 4))) & 0xFF;
+  for (int i = 1; i + 1 < kMaxPolyV; ++i) {
+    if (i + 1 < nv) {
+      const float4 vi = rec_vtx(R, i), vj = rec_vtx(R, i + 1);
+      const V3<float> xi = mk(vi.x, vi.y, vi.z), xj = mk(vj.x, vj.y, vj.z);
+      const float ai = 0.5f * dot(cross(xi - x0, xj - x0), n);
+      A += ai;
+      c = c + (x0 + xi + xj) * (ai * (1.f / 3.f));
+      pc += ai * (v0.w + vi.w + vj.w) * (1.f / 3.f);
+    }
   }
 }
 
-template <int ND>
-__device__ __noinline__ void rec_taxel(const StepArgs& a, const AdjPoly& R, AdjAcc& G) {
+// The lane's share of a kept polygon's forces (its quadrature point).
+__device__ __forceinline__ void rec_forces_part(const StepArgs& a, const AdjPoly& R, int sub, Acc& ac) {
   const PairDev& P = a.pairs[R.pair];
   const FrameDev& F = a.frames[R.pair];
-  PV<float, ND> poly[kMaxPolyV];
-  rec_unpack<ND>(R, poly);
+  const int nv = R.nv;
   const V3<float> anc = mk(R.anc[0], R.anc[1], R.anc[2]);
-  const V3<float> n = mk(R.n[0], R.n[1], R.n[2]);
+  const V3<float> nc = mk(R.n[0], R.n[1], R.n[2]) * (P.s_is_m ? 1.f : -1.f);
+  const float gM = P.s_is_m ? R.gint : INFINITY, gN = P.s_is_m ? INFINITY : R.gint;
+  float A, pcen;
+  V3<float> c;
+  rec_fan(R, nv, nc, A, c, pcen);
+  if (A != 0.f) {
+    c = c * (1.f / A);
+    pcen /= A;
+  } else {
+    c = mk(0.f, 0.f, 0.f);
+    pcen = 0.f;
+    for (int i = 0; i < nv; ++i) {
+      c = c + rec_pos(R, i) * (1.f / nv);
+      pcen += rec_vtx(R, i).w / nv;
+    }
+  }
+  if (a.repr == 1) {
+    if (sub == 0) point_force(ac, F, P.damping, P.mu, a.apply_forces, fabsf(A), anc + c, nc, gM, gN, pcen);
+  } else if (sub < nv) {
+    const int j = sub + 1 == nv ? 0 : sub + 1;
+    const float4 vi = rec_vtx(R, sub), vj = rec_vtx(R, j);
+    const V3<float> xi = mk(vi.x, vi.y, vi.z), xj = mk(vj.x, vj.y, vj.z);
+    const float Ai = 0.5f * norm(cross(xi - c, xj - c));
+    const V3<float> cen = anc + (c + xi + xj) * (1.f / 3.f);
+    const float p0 = pcen / 3.f + vi.w / 3.f + vj.w / 3.f;
+    point_force(ac, F, P.damping, P.mu, a.apply_forces, Ai, cen, nc, gM, gN, p0);
+  }
+}
+
+// The lane's share of a kept polygon's ray samples on one sensor (side 0:
+// the pair's sensor0, 1: sensor1): binning with slot keys (G null; lane 0
+// also stores the polygon's pressure model for the taxel pass) or the
+// adjoint of the samples it won.
+__device__ __forceinline__ void rec_rays_part(const StepArgs& a, const AdjPoly& R, int dst, int side, int sid,
+                                              const float* Rl, const float* tl, int soft_is_sensor, int sub,
+                                              AdjAcc* G) {
+  const SensorDev S = a.sensors[sid];
+  const V3<float> anc = mk(R.anc[0], R.anc[1], R.anc[2]);
   const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
+  RasterPoly rp;
+  if (!raster_prepare(a, S, Rl, tl, R.nv, anc, g, [&](int i) { return rec_vtx(R, i); }, rp)) return;
+  if (!G && sub == 0) {
+    a.slot_press[4 * (size_t)dst + 2 * side] = make_float4(rp.lx[0], rp.ly[0], rp.p0, rp.px);
+    a.slot_press[4 * (size_t)dst + 2 * side + 1] = make_float4(rp.py, 0.f, 0.f, 0.f);
+  }
+  unsigned long long* smp = a.samples + S.sample_off;
+  const float* sx = a.samp_coord + S.samp_off_x;
+  const float* sy = a.samp_coord + S.samp_off_y;
+  const int nY = rp.Y1 - rp.Y0 + 1;
+  const int cnt = (rp.X1 - rp.X0 + 1) * nY;
+  for (int idx = sub; idx < cnt; idx += kGroup) {
+    const int X = rp.X0 + idx / nY, Y = rp.Y0 + idx % nY;
+    float t, z, pr;
+    if (!raster_probe(rp, S, sx[X], sy[Y], t, z, pr)) continue;
+    const unsigned long long key = key_slot(t, dst, side);
+    const size_t si = (size_t)X * S.ny + Y;
+    if (!G) {
+      atomicMin(&smp[si], key);
+      continue;
+    }
+    if (smp[si] != key) continue;   // won by another polygon (keys are unique)
+    sample_adjoint(a, S, Rl, tl, sx[X], sy[Y], z, pr, X, Y, g, mk(R.n[0], R.n[1], R.n[2]), soft_is_sensor, *G);
+  }
+}
+
+__device__ __forceinline__ void rec_rays(const StepArgs& a, const AdjPoly& R, int dst, int sub, AdjAcc* G) {
+  const PairDev& P = a.pairs[R.pair];
+  const FrameDev& F = a.frames[R.pair];
   if (P.sensor0 >= 0)
-    raster_keys<ND>(a, P.sensor0, F.Rl, F.tl, poly, R.nv, anc, g, n, a.sensors[P.sensor0].geom == P.gs, &G);
+    rec_rays_part(a, R, dst, 0, P.sensor0, F.Rl, F.tl, a.sensors[P.sensor0].geom == P.gs, sub, G);
   if (P.sensor1 >= 0)
-    raster_keys<ND>(a, P.sensor1, F.Rl1, F.tl1, poly, R.nv, anc, g, n, a.sensors[P.sensor1].geom == P.gs, &G);
+    rec_rays_part(a, R, dst, 1, P.sensor1, F.Rl1, F.tl1, a.sensors[P.sensor1].geom == P.gs, sub, G);
 }
 
-template <int ND>
-__device__ __noinline__ void rec_wrench(const StepArgs& a, const AdjPoly& R, AdjAcc& G) {
-  const PairDev& P = a.pairs[R.pair];
-  const FrameDev& F = a.frames[R.pair];
-  PV<float, ND> poly[kMaxPolyV];
-  rec_unpack<ND>(R, poly);
-  const V3<float> anc = mk(R.anc[0], R.anc[1], R.anc[2]);
-  const V3<float> n = mk(R.n[0], R.n[1], R.n[2]);
-  const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
-  V3<float> face[4], clipn[3];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) face[k] = mk(R.face[k][0], R.face[k][1], R.face[k][2]);
-#pragma unroll
-  for (int j = 0; j < 3; ++j) clipn[j] = mk(R.clip[j][0], R.clip[j][1], R.clip[j][2]);
-  const float* gF = a.adj_pair + 8 * (size_t)R.pair;
-  wrench_adjoint<ND>(G, a, P, F, gF, gF + 3, poly, R.nv, anc, n, P.s_is_m ? 1.f : -1.f, face, clipn, g, R.gint);
-}
-
-// Forward pass over the kept polygons, one thread per polygon: quadrature
-// and forces into the polygon's pair-ordered slot, and the sensors' rays
-// (the same raster function and inputs as the adjoint's, so keys are
-// identical).
-template <int ND>
-__device__ __noinline__ void rec_forward(const StepArgs& a, const AdjPoly& R, RecOut& o) {
-  const PairDev& P = a.pairs[R.pair];
-  const FrameDev& F = a.frames[R.pair];
-  PV<float, ND> poly[kMaxPolyV];
-  rec_unpack<ND>(R, poly);
-  const V3<float> anc = mk(R.anc[0], R.anc[1], R.anc[2]);
-  const V3<float> n = mk(R.n[0], R.n[1], R.n[2]);
-  const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
-  const V3<float> nc = n * (P.s_is_m ? 1.f : -1.f);
-  Acc ac;
-  acc_zero(ac);
-  integrate_forces<ND>(a, P, F, ac, poly, R.nv, anc, nc, P.s_is_m ? R.gint : INFINITY, P.s_is_m ? INFINITY : R.gint);
-  o.F[0] = ac.F[0]; o.F[1] = ac.F[1]; o.F[2] = ac.F[2];
-  o.T[0] = ac.T[0]; o.T[1] = ac.T[1]; o.T[2] = ac.T[2];
-  o.area = ac.area; o.fn0 = ac.fn0; o.n_faces = ac.n_faces;
-  o.pad[0] = o.pad[1] = o.pad[2] = 0;
-  raster_polygon<ND>(a, P, F, poly, R.nv, anc, nc, g);
-}
-
+// Forward pass over the kept polygons: forces into the polygon's pair-ordered
+// slot, then the sensors' rays.
 __global__ void __launch_bounds__(128, 4) rec_forward_kernel(StepArgs a) {
   if (!rec_ok(a)) return;   // records incomplete: the step is re-run after growth
   const int n = min(*a.rec_count, a.rec_cap);
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-    const AdjPoly& R = a.recs[r];
-    const int2 key = a.rec_key[r];
-    const int dst = a.item_poly_off[key.x] + key.y;
-    if (dst < 0 || dst >= a.rec_cap) continue;
-    RecOut o;
-    if (R.kind == 0) rec_forward<3>(a, R, o);
-    else rec_forward<1>(a, R, o);
-    a.rec_out[dst] = o;
-  }
-}
-
-// Warp-uniform loop over the records (every lane runs every iteration, so the
-// phases can end with a full-warp reconvergence).
-__global__ void __launch_bounds__(128, 4) adjoint_rec_kernel(StepArgs a) {
-  if (!recs_valid(a)) return;
-  const int n = min(*a.rec_count, a.rec_cap);
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, sub = lane & (kGroup - 1), grp = lane / kGroup;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
-  const bool taxel = a.adj_taxel != nullptr, wrench = a.adj_wrench != nullptr && a.apply_forces;
-  for (int base = warp * 32; base < n; base += n_warps * 32) {
-    const int r = base + lane;
-    const bool ok = r < n;
-    const AdjPoly& R = a.recs[ok ? r : base];
+  constexpr int kPer = 32 / kGroup;
+  for (int base = warp * kPer; base < n; base += n_warps * kPer) {
+    const int r = base + grp;
     int dst = -1;
-    if (ok) {
+    if (r < n) {
       const int2 key = a.rec_key[r];
       dst = a.item_poly_off[key.x] + key.y;
     }
-    const bool on = ok && dst >= 0 && dst < a.rec_cap;
-    const int kind = on ? R.kind : 0;
+    const bool on = r < n && dst >= 0 && dst < a.rec_cap;
+    const AdjPoly& R = a.recs[on ? r : base];
+    Acc ac;
+    acc_zero(ac);
+    if (on) rec_forces_part(a, R, sub, ac);
+    float v[9] = {ac.F[0], ac.F[1], ac.F[2], ac.T[0], ac.T[1], ac.T[2], ac.area, ac.fn0, (float)ac.n_faces};
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v[k] = gsum(v[k]);
+    if (on && sub == 0) {
+      RecOut o;
+      o.F[0] = v[0]; o.F[1] = v[1]; o.F[2] = v[2];
+      o.T[0] = v[3]; o.T[1] = v[4]; o.T[2] = v[5];
+      o.area = v[6]; o.fn0 = v[7]; o.n_faces = (int)v[8];
+      o.pad[0] = o.pad[1] = o.pad[2] = 0;
+      a.rec_out[dst] = o;
+    }
+    if (on) rec_rays(a, R, dst, sub, nullptr);
+  }
+}
+
+// Wrench adjoint of one kept polygon, distributed over the group (the
+// serial form is wrench_adjoint): lane k reverses the quadrature point of
+// fan triangle k, lane v owns vertex v for the fan reverse and the
+// constraint contraction.  Every lane of the warp calls it (shuffles).
+__device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPoly& R, bool on, int lane, int sub,
+                                                 AdjAcc& G) {
+  const int nv = on ? R.nv : 0;
+  const int pair = on ? R.pair : 0;
+  const PairDev& P = a.pairs[pair];
+  const FrameDev& F = a.frames[pair];
+  const float sgn = P.s_is_m ? 1.f : -1.f;
+  const V3<float> n = mk(R.n[0], R.n[1], R.n[2]), ns = n * sgn;
+  const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
+  const V3<float> anc = mk(R.anc[0], R.anc[1], R.anc[2]);
+  const float gint = R.gint;
+  const float* gF = a.adj_pair + 8 * (size_t)pair;
+  const V3<float> gFv = mk(gF[0], gF[1], gF[2]), gTv = mk(gF[3], gF[4], gF[5]);
+  float A = 0.f, pc = 0.f;
+  V3<float> c = mk(0.f, 0.f, 0.f);
+  if (on) rec_fan(R, nv, ns, A, c, pc);
+  const bool live = on && A != 0.f;
+  const float iA = live ? 1.f / A : 0.f;
+  c = c * iA;
+  pc = pc * iA;
+  const float gMv = P.s_is_m ? gint : INFINITY, gNv = P.s_is_m ? INFINITY : gint;
+  // quadrature points
+  V3<float> xbi = mk(0.f, 0.f, 0.f), xbj = xbi, nbar = xbi, cbar = xbi;
+  float pbi = 0.f, pbj = 0.f, gbar = 0.f, pcbar = 0.f, Abar = 0.f;
+  PointBar b;
+  if (live) {
+    if (a.repr == 1) {
+      if (sub == 0 && point_reverse(G, F, P.damping, P.mu, gFv, gTv, fabsf(A), anc + c, ns, gMv, gNv, pc, b)) {
+        Abar += A < 0.f ? -b.A : b.A;
+        cbar = cbar + b.p;
+        pcbar += b.p0;
+        nbar = nbar + b.n;
+        gbar += P.s_is_m ? b.gM : b.gN;
+      }
+    } else if (sub < nv) {
+      const int j = sub + 1 == nv ? 0 : sub + 1;
+      const float4 vi = rec_vtx(R, sub), vj = rec_vtx(R, j);
+      const V3<float> xi = mk(vi.x, vi.y, vi.z), xj = mk(vj.x, vj.y, vj.z);
+      const V3<float> u = xi - c, w = xj - c;
+      const V3<float> cr = cross(u, w);
+      const float len = norm(cr);
+      const V3<float> cen = anc + (c + xi + xj) * (1.f / 3.f);
+      const float p0 = pc / 3.f + vi.w / 3.f + vj.w / 3.f;
+      if (point_reverse(G, F, P.damping, P.mu, gFv, gTv, 0.5f * len, cen, ns, gMv, gNv, p0, b)) {
+        nbar = nbar + b.n;
+        gbar += P.s_is_m ? b.gM : b.gN;
+        if (len > 0.f) {   // A_e = |u x w| / 2
+          const V3<float> crb = cr * (0.5f * b.A / len);
+          const V3<float> ub = cross(w, crb), wb = cross(crb, u);
+          xbi = xbi + ub;
+          xbj = xbj + wb;
+          cbar = cbar - ub - wb;
+        }
+        const V3<float> c3 = b.p * (1.f / 3.f);
+        cbar = cbar + c3;
+        xbi = xbi + c3;
+        xbj = xbj + c3;
+        const float p3 = b.p0 * (1.f / 3.f);
+        pcbar += p3;
+        pbi += p3;
+        pbj += p3;
+      }
+    }
+  }
+  nbar = gsum3(nbar);
+  cbar = gsum3(cbar);
+  gbar = gsum(gbar);
+  pcbar = gsum(pcbar);
+  Abar = gsum(Abar);
+  // vertex v collects its share as "i" (own lane) and as "j" (lane v - 1)
+  const int src = (lane & ~(kGroup - 1)) | (sub == 0 ? (nv > 0 ? nv - 1 : 0) : sub - 1);
+  V3<float> xb = xbi + mk(__shfl_sync(0xffffffffu, xbj.x, src), __shfl_sync(0xffffffffu, xbj.y, src),
+                          __shfl_sync(0xffffffffu, xbj.z, src));
+  float pb = pbi + __shfl_sync(0xffffffffu, pbj, src);
+  // c = Sc / A, pc = Sp / A
+  const V3<float> Scb = cbar * iA;
+  const float Spb = pcbar * iA;
+  Abar -= (dot(cbar, c) + pcbar * pc) * iA;
+  if (live) {
+    const float4 v0 = rec_vtx(R, 0);
+    const V3<float> x0 = mk(v0.x, v0.y, v0.z);
+#pragma unroll
+    for (int i = 1; i + 1 < kMaxPolyV; ++i) {
+      if (i + 1 < nv) {
+        const float4 vi = rec_vtx(R, i), vj = rec_vtx(R, i + 1);
+        const V3<float> xi = mk(vi.x, vi.y, vi.z), xj = mk(vj.x, vj.y, vj.z);
+        const V3<float> e1 = xi - x0, e2 = xj - x0;
+        const V3<float> cr = cross(e1, e2);
+        const float ai = 0.5f * dot(cr, ns);
+        const float aib = Abar + dot(Scb, x0 + xi + xj) * (1.f / 3.f) + Spb * (v0.w + vi.w + vj.w) * (1.f / 3.f);
+        const V3<float> sx = Scb * (ai * (1.f / 3.f));
+        const float sp = Spb * ai * (1.f / 3.f);
+        // a_i = n . (e1 x e2) / 2
+        nbar = nbar + cr * (0.5f * aib);
+        const V3<float> e1b = cross(e2, ns) * (0.5f * aib), e2b = cross(ns, e1) * (0.5f * aib);
+        if (sub == 0) { xb = xb + sx - e1b - e2b; pb += sp; }
+        if (sub == i) { xb = xb + sx + e1b; pb += sp; }
+        if (sub == i + 1) { xb = xb + sx + e2b; pb += sp; }
+      }
+    }
+  }
+  // contraction with the tangents of the lane's vertex
+  V3<float> rot = mk(0.f, 0.f, 0.f), tr = rot;
+  if (live && sub < nv) {
+    const V3<float> xe = xb + g * pb;
+    const V3<float> X = anc + rec_pos(R, sub);
+    const int lab = (sub < 4 ? R.lab0 >> (8 * sub) : R.lab1 >> (8 * (sub - 4))) & 0xFF;
+    const int l0 = lab & 15, l1 = lab >> 4;
+    const V3<float> r0 = n;
+    const V3<float> r1 = l0 < 4 ? mk(R.face[l0][0], R.face[l0][1], R.face[l0][2])
+                                : mk(R.clip[l0 - 4][0], R.clip[l0 - 4][1], R.clip[l0 - 4][2]);
+    const V3<float> r2 = l1 < 4 ? mk(R.face[l1][0], R.face[l1][1], R.face[l1][2])
+                                : mk(R.clip[l1 - 4][0], R.clip[l1 - 4][1], R.clip[l1 - 4][2]);
+    const V3<float> a0 = cross(r1, r2), a1 = cross(r2, r0), a2 = cross(r0, r1);
+    const float det = dot(r0, a0);
+    const float sc = norm(r0) * norm(r1) * norm(r2);
+    if (fabsf(det) > 1e-12f * sc) {
+      const float id = 1.f / det;
+      V3<float> B = r0 * (dot(xe, a0) * id);
+      if (l0 >= 4) B = B + r1 * (dot(xe, a1) * id);
+      if (l1 >= 4) B = B + r2 * (dot(xe, a2) * id);
+      tr = B;
+      rot = cross(X, B);
+    }
+  }
+  if (live && sub == 0) {
+    rot = rot + cross(ns, nbar);
+    if (gint != 0.f) rot = rot + cross(n, g) * gbar;
+  }
+  G.gx[0] += rot.x; G.gx[1] += rot.y; G.gx[2] += rot.z;
+  G.gx[3] += tr.x; G.gx[4] += tr.y; G.gx[5] += tr.z;
+}
+
+__global__ void __launch_bounds__(128, 4) adjoint_rec_kernel(StepArgs a) {
+  if (!recs_valid(a)) return;
+  const int n = min(*a.rec_count, a.rec_cap);
+  const int lane = threadIdx.x & 31, sub = lane & (kGroup - 1), grp = lane / kGroup;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n_warps = (gridDim.x * blockDim.x) >> 5;
+  constexpr int kPer = 32 / kGroup;
+  const bool taxel = a.adj_taxel != nullptr, wrench = a.adj_wrench != nullptr && a.apply_forces;
+  for (int base = warp * kPer; base < n; base += n_warps * kPer) {
+    const int r = base + grp;
+    int dst = -1;
+    if (r < n) {
+      const int2 key = a.rec_key[r];
+      dst = a.item_poly_off[key.x] + key.y;
+    }
+    const bool on = r < n && dst >= 0 && dst < a.rec_cap;
+    const AdjPoly& R = a.recs[on ? r : base];
     AdjAcc G;
     adj_zero(G);
-    if (taxel && on) {
-      if (kind == 0) rec_taxel<3>(a, R, G);
-      else rec_taxel<1>(a, R, G);
-    }
+    if (taxel && on) rec_rays(a, R, dst, sub, &G);
     __syncwarp();
-    if (wrench && on) {
-      if (kind == 0) rec_wrench<3>(a, R, G);
-      else rec_wrench<1>(a, R, G);
-    }
-    __syncwarp();
-    if (on) {
+    if (wrench) rec_wrench_group(a, R, on, lane, sub, G);
+    float v[13] = {G.gx[0], G.gx[1], G.gx[2], G.gx[3], G.gx[4], G.gx[5], G.glin[0], G.glin[1], G.glin[2],
+                   G.gang[0], G.gang[1], G.gang[2], G.gE};
+#pragma unroll
+    for (int k = 0; k < 13; ++k) v[k] = gsum(v[k]);
+    if (on && sub == 0) {
       float4* o = reinterpret_cast<float4*>(a.rec_grad + 16 * (size_t)dst);
-      o[0] = make_float4(G.gx[0], G.gx[1], G.gx[2], G.gx[3]);
-      o[1] = make_float4(G.gx[4], G.gx[5], G.glin[0], G.glin[1]);
-      o[2] = make_float4(G.glin[2], G.gang[0], G.gang[1], G.gang[2]);
-      o[3] = make_float4(G.gE, 0.f, 0.f, 0.f);
+      o[0] = make_float4(v[0], v[1], v[2], v[3]);
+      o[1] = make_float4(v[4], v[5], v[6], v[7]);
+      o[2] = make_float4(v[8], v[9], v[10], v[11]);
+      o[3] = make_float4(v[12], 0.f, 0.f, 0.f);
     }
   }
 }

@@ -386,7 +386,17 @@ __global__ void taxel_kernel(StepArgs a) {
       const int Y = y * S.sr + j;
       unsigned long long k = smp[(size_t)X * S.ny + Y];
       if (k != ~0ull) {
-        float pr = __uint_as_float((unsigned)(k & 0xffffffffu));
+        const unsigned lo = (unsigned)(k & 0xffffffffu);
+        float pr = __uint_as_float(lo);
+        if (lo & kSlotTag) {
+          // won by a kept polygon: its pressure model for this sensor
+          const int slot = (int)(lo & ~(kSlotTag | kSideBit));
+          const int side = (lo & kSideBit) ? 1 : 0;
+          const float4 m0 = a.slot_press[4 * (size_t)slot + 2 * side];
+          const float4 m1 = a.slot_press[4 * (size_t)slot + 2 * side + 1];
+          pr = raster_pressure(m0.x, m0.y, m0.z, m0.w, m1.x, a.samp_coord[S.samp_off_x + X],
+                               a.samp_coord[S.samp_off_y + Y]);
+        }
         float raw = pr * S.rmean;
         avg += w[i * S.sr + j] * raw;
         if (!a.keep_samples) smp[(size_t)X * S.ny + Y] = ~0ull;

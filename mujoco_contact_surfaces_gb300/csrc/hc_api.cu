@@ -202,6 +202,7 @@ struct hc_context {
   DevBuf<hc::AdjPoly> recs;
   DevBuf<int2> rec_key;
   DevBuf<hc::RecOut> rec_out;
+  DevBuf<float4> slot_press;
   DevBuf<float> rec_grad;
   DevBuf<int> item_poly_off, poly_block_sum;
   int rec_cap = 0;
@@ -372,10 +373,12 @@ hc_status ensure_rec_offsets(hc_context* c) {
 }
 
 hc_status ensure_recs(hc_context* c, int cap) {
+  cap = std::min(cap, 1 << 30);   // record slots are 30-bit fields of the sample keys
   if (cap > c->rec_cap) {
     HC_CUDA(c->recs.reserve(cap));
     HC_CUDA(c->rec_key.reserve(cap));
     HC_CUDA(c->rec_out.reserve(cap));
+    HC_CUDA(c->slot_press.reserve(4 * (size_t)cap));
     HC_CUDA(c->rec_grad.reserve(16 * (size_t)cap));
     c->rec_cap = cap;
     invalidate_graph(c);
@@ -533,6 +536,7 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
     a.rec_key = c->rec_key.p;
     a.rec_cap = c->rec_cap;
     a.rec_out = c->rec_out.p;
+    a.slot_press = c->slot_press.p;
     a.item_poly_off = c->item_poly_off.p;
     a.poly_block_sum = c->poly_block_sum.p;
     a.n_item_blocks = std::max(1, (c->item_cap + hc::kBpBlock - 1) / hc::kBpBlock);
@@ -1351,8 +1355,7 @@ static hc_status adjoint_launch(hc_context* c, const double* d_dw, const float* 
   }
   c->adj_launches = hc::launch_adjoint(a, c->stream);
   HC_CUDA(cudaGetLastError());
-  // the taxel adjoint claims (and clears) every won sample
-  if (a.adj_taxel) c->samples_dirty = false;
+  // the samples stay as the step left them (the next step clears them)
   return HC_OK;
 }
 

@@ -87,6 +87,8 @@ struct StepArgs {
   int n_item_blocks;         // item_cap / kBpBlock rounded up
   float* rec_grad;           // per record in pair order: 13 gradient terms (stride 16)
   RecOut* rec_out;           // per record in pair order: forces (forward)
+  float4* slot_press;        // per record slot and sensor side (2): the linear
+                             // pressure model (lx0, ly0, p0, px), (py, -, -, -)
 };
 
 constexpr int kBpBlock = 256;

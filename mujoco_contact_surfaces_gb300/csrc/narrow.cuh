@@ -73,107 +73,198 @@ struct AdjAcc {
   float gE;        // sum of dL/dp * p over won samples (taxel part of dL/dE * E)
 };
 
+// One polygon prepared for ray binning on one sensor (sensor frame): vertex
+// x, y, edge vectors, the plane z(x, y) and the linear pressure p(x, y), and
+// the range of sample indices its bounding box covers.  All arithmetic uses
+// explicitly rounded intrinsics, so every kernel that inlines these
+// functions computes bit-identical keys (the adjoint re-identifies the
+// forward's winning samples by their keys).
+struct RasterPoly {
+  float lx[kMaxPolyV], ly[kMaxPolyV], ex[kMaxPolyV], ey[kMaxPolyV];
+  float lz0, zx, zy, px, py, p0;
+  bool pos;           // orientation of the projected polygon
+  int nv, X0, X1, Y0, Y1;
+};
+
+__device__ __forceinline__ float dot3_rn(const float* r, float x, float y, float z) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(r[0], x), __fmul_rn(r[1], y)), __fmul_rn(r[2], z));
+}
+
+// vtx(i) -> float4 (x, y, z relative to anc, pressure).  Returns false when
+// the polygon projects degenerately (|2A| < 1e-10, the ray test's parallel
+// threshold) or misses the sample grid.
+template <class Vtx>
+__device__ __forceinline__ bool raster_prepare(const StepArgs& a, const SensorDev& S, const float* Rl,
+                                               const float* tl, int nv, V3<float> anc, V3<float> g_soft, Vtx vtx,
+                                               RasterPoly& rp) {
+  float lz[kMaxPolyV];
+  float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
+#pragma unroll
+  for (int i = 0; i < kMaxPolyV; ++i) {
+    rp.lx[i] = rp.ly[i] = lz[i] = 0.f;
+    if (i < nv) {
+      const float4 v = vtx(i);
+      const float X = __fadd_rn(anc.x, v.x), Y = __fadd_rn(anc.y, v.y), Z = __fadd_rn(anc.z, v.z);
+      rp.lx[i] = __fadd_rn(dot3_rn(Rl, X, Y, Z), tl[0]);
+      rp.ly[i] = __fadd_rn(dot3_rn(Rl + 3, X, Y, Z), tl[1]);
+      lz[i] = __fadd_rn(dot3_rn(Rl + 6, X, Y, Z), tl[2]);
+      mnx = fminf(mnx, rp.lx[i]); mxx = fmaxf(mxx, rp.lx[i]);
+      mny = fminf(mny, rp.ly[i]); mxy = fmaxf(mxy, rp.ly[i]);
+      if (i == 0) rp.p0 = v.w;
+    }
+  }
+  float A2 = 0.f;
+#pragma unroll
+  for (int i = 1; i + 1 < kMaxPolyV; ++i)
+    if (i + 1 < nv)
+      A2 = __fadd_rn(A2, __fsub_rn(__fmul_rn(__fsub_rn(rp.lx[i], rp.lx[0]), __fsub_rn(rp.ly[i + 1], rp.ly[0])),
+                                   __fmul_rn(__fsub_rn(rp.ly[i], rp.ly[0]), __fsub_rn(rp.lx[i + 1], rp.lx[0]))));
+  if (!(fabsf(A2) >= 1e-10f)) return false;
+  rp.pos = A2 > 0.f;
+  // plane of the polygon and the pressure gradient, sensor frame
+  const float e1x = __fsub_rn(rp.lx[1], rp.lx[0]), e1y = __fsub_rn(rp.ly[1], rp.ly[0]), e1z = __fsub_rn(lz[1], lz[0]);
+  float nx = 0.f, ny = 0.f, nz = 0.f;
+#pragma unroll
+  for (int i = 2; i < kMaxPolyV; ++i) {
+    if (i < nv) {
+      const float fx = __fsub_rn(rp.lx[i], rp.lx[0]), fy = __fsub_rn(rp.ly[i], rp.ly[0]), fz = __fsub_rn(lz[i], lz[0]);
+      nx = __fadd_rn(nx, __fsub_rn(__fmul_rn(e1y, fz), __fmul_rn(e1z, fy)));
+      ny = __fadd_rn(ny, __fsub_rn(__fmul_rn(e1z, fx), __fmul_rn(e1x, fz)));
+      nz = __fadd_rn(nz, __fsub_rn(__fmul_rn(e1x, fy), __fmul_rn(e1y, fx)));
+    }
+  }
+  if (!(fabsf(nz) > 0.f)) return false;
+  rp.zx = __fdiv_rn(-nx, nz);   // dz/dx, dz/dy on the plane
+  rp.zy = __fdiv_rn(-ny, nz);
+  const float glx = dot3_rn(Rl, g_soft.x, g_soft.y, g_soft.z);
+  const float gly = dot3_rn(Rl + 3, g_soft.x, g_soft.y, g_soft.z);
+  const float glz = dot3_rn(Rl + 6, g_soft.x, g_soft.y, g_soft.z);
+  rp.px = __fadd_rn(glx, __fmul_rn(glz, rp.zx));   // dp/dx, dp/dy on the plane
+  rp.py = __fadd_rn(gly, __fmul_rn(glz, rp.zy));
+  rp.lz0 = lz[0];
+  const float* sx = a.samp_coord + S.samp_off_x;
+  const float* sy = a.samp_coord + S.samp_off_y;
+  const float x0 = sx[0], dx = S.nx > 1 ? __fsub_rn(sx[1], sx[0]) : 1.f;
+  const float y0 = sy[0], dy = S.ny > 1 ? __fsub_rn(sy[1], sy[0]) : 1.f;
+  const float fx0 = ceilf(__fsub_rn(__fdiv_rn(__fsub_rn(mnx, x0), dx), 1e-3f));
+  const float fx1 = floorf(__fadd_rn(__fdiv_rn(__fsub_rn(mxx, x0), dx), 1e-3f));
+  const float fy0 = ceilf(__fsub_rn(__fdiv_rn(__fsub_rn(mny, y0), dy), 1e-3f));
+  const float fy1 = floorf(__fadd_rn(__fdiv_rn(__fsub_rn(mxy, y0), dy), 1e-3f));
+  if (!(fx1 >= 0.f && fy1 >= 0.f && fx0 <= (float)(S.nx - 1) && fy0 <= (float)(S.ny - 1))) return false;
+  rp.X0 = max(0, (int)fx0); rp.X1 = min(S.nx - 1, (int)fx1);
+  rp.Y0 = max(0, (int)fy0); rp.Y1 = min(S.ny - 1, (int)fy1);
+  rp.nv = nv;
+#pragma unroll
+  for (int i = 0; i < kMaxPolyV; ++i) {
+    const bool last = i + 1 >= nv;
+    const float nxv = last ? rp.lx[0] : rp.lx[i + 1 < kMaxPolyV ? i + 1 : 0];
+    const float nyv = last ? rp.ly[0] : rp.ly[i + 1 < kMaxPolyV ? i + 1 : 0];
+    rp.ex[i] = __fsub_rn(nxv, rp.lx[i]);
+    rp.ey[i] = __fsub_rn(nyv, rp.ly[i]);
+  }
+  return true;
+}
+
+// Sample keys (64-bit, smallest wins): the ray parameter t in the high word
+// (positive floats order as their bits), a tie-break in the low word: the
+// hit pressure (clamped to +0, so bit 31 is clear) when the polygon is cast
+// inline, or, when it is cast from the kept records, bit 31 set, the sensor
+// side of its pair in bit 30 and its pair-ordered record slot below (the
+// taxel pass then evaluates the winner's pressure from its stored linear
+// model, and the adjoint recognises its samples by the key alone).
+constexpr unsigned kSlotTag = 0x80000000u, kSideBit = 0x40000000u;
+__device__ __forceinline__ unsigned long long key_pressure(float t, float pr) {
+  return ((unsigned long long)__float_as_uint(t) << 32) | (unsigned long long)__float_as_uint(pr > 0.f ? pr : 0.f);
+}
+__device__ __forceinline__ unsigned long long key_slot(float t, int slot, int side) {
+  return ((unsigned long long)__float_as_uint(t) << 32) |
+         (unsigned long long)(kSlotTag | (side ? kSideBit : 0u) | (unsigned)slot);
+}
+
+// Pressure of a prepared polygon's linear model at (qx, qy).
+__device__ __forceinline__ float raster_pressure(float lx0, float ly0, float p0, float px, float py, float qx,
+                                                 float qy) {
+  const float ddx = __fsub_rn(qx, lx0), ddy = __fsub_rn(qy, ly0);
+  return __fadd_rn(__fadd_rn(p0, __fmul_rn(px, ddx)), __fmul_rn(py, ddy));
+}
+
+// Sample (qx, qy) against a prepared polygon: false when the ray misses the
+// polygon or its hit lies outside 0 < t < 1.5 zs; else t, the hit height z
+// and the pressure there.
+__device__ __forceinline__ bool raster_probe(const RasterPoly& rp, const SensorDev& S, float qx, float qy,
+                                             float& t, float& z, float& pr) {
+  bool in = true;
+#pragma unroll
+  for (int i = 0; i < kMaxPolyV; ++i) {
+    if (i < rp.nv) {
+      const float e = __fsub_rn(__fmul_rn(rp.ex[i], __fsub_rn(qy, rp.ly[i])),
+                                __fmul_rn(rp.ey[i], __fsub_rn(qx, rp.lx[i])));
+      in &= rp.pos ? e >= 0.f : e <= 0.f;
+    }
+  }
+  if (!in) return false;
+  const float ddx = __fsub_rn(qx, rp.lx[0]), ddy = __fsub_rn(qy, rp.ly[0]);
+  z = __fadd_rn(__fadd_rn(rp.lz0, __fmul_rn(rp.zx, ddx)), __fmul_rn(rp.zy, ddy));
+  t = __fsub_rn(__fadd_rn(S.zs15, 1e-8f), z);
+  if (!(t > 0.f && t < S.zs15)) return false;
+  pr = raster_pressure(rp.lx[0], rp.ly[0], rp.p0, rp.px, rp.py, qx, qy);
+  return true;
+}
+
+// Adjoint of one won sample: dL/dp = pbar at the hit (qx, qy, z) of the
+// sensor frame.
+__device__ __forceinline__ void sample_adjoint(const StepArgs& a, const SensorDev& S, const float* Rl,
+                                               const float* tl, float qx, float qy, float z, float pr, int X, int Y,
+                                               V3<float> g_soft, V3<float> n_tri, int soft_is_sensor, AdjAcc& G) {
+  // dL/dp at this sample: cell (X / sr, Y / sr), window weight of (X % sr, Y % sr)
+  const float w = a.weights[S.weight_off + (X % S.sr) * S.sr + (Y % S.sr)];
+  const float pbar = a.adj_taxel[S.taxel_off + X / S.sr + S.cy * (Y / S.sr)] * w * S.rmean;
+  if (pbar == 0.f) return;
+  G.gE += pbar * pr;
+  const V3<float> xs = mat_tmul<float>(Rl, mk(qx, qy, z) - mk(tl[0], tl[1], tl[2]));   // hit point, soft frame
+  if (!soft_is_sensor) {
+    // rays and plane move with the other body: dp = g . (w x x + v)
+    const V3<float> wx = cross(xs, g_soft);
+    G.gx[0] += pbar * wx.x; G.gx[1] += pbar * wx.y; G.gx[2] += pbar * wx.z;
+    G.gx[3] += pbar * g_soft.x; G.gx[4] += pbar * g_soft.y; G.gx[5] += pbar * g_soft.z;
+  } else {
+    // rays fixed in the soft frame, plane n.x = o moving: dx = dt D,
+    // dt = -(w.(n x x) - n.v) / (n.D), D = -(sensor z) in the soft frame
+    const V3<float> D = mk(-Rl[6], -Rl[7], -Rl[8]);
+    const float nD = dot(n_tri, D);
+    if (!(fabsf(nD) > 0.f)) return;
+    const float r = -dot(g_soft, D) / nD;
+    const V3<float> nx = cross(n_tri, xs);
+    G.gx[0] += pbar * r * nx.x; G.gx[1] += pbar * r * nx.y; G.gx[2] += pbar * r * nx.z;
+    G.gx[3] -= pbar * r * n_tri.x; G.gx[4] -= pbar * r * n_tri.y; G.gx[5] -= pbar * r * n_tri.z;
+  }
+}
+
 template <int ND>
 __device__ __noinline__ void raster_keys(const StepArgs& a, int sid, const float* Rl, const float* tl,
                                          const PV<float, ND>* v, int nv, V3<float> anc, V3<float> g_soft,
                                          V3<float> n_tri, int soft_is_sensor, AdjAcc* G) {
   const SensorDev S = a.sensors[sid];
-  const V3<float> T = mk(tl[0], tl[1], tl[2]);
-  float lx[kMaxPolyV], ly[kMaxPolyV], lz[kMaxPolyV];
-  float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY, A2 = 0.f;
-#pragma unroll
-  for (int i = 0; i < kMaxPolyV; ++i) {
-    if (i < nv) {
-      const V3<float> l = mat_mul<float>(Rl, anc + pv_pos(v[i])) + T;
-      lx[i] = l.x; ly[i] = l.y; lz[i] = l.z;
-      mnx = fminf(mnx, l.x); mxx = fmaxf(mxx, l.x);
-      mny = fminf(mny, l.y); mxy = fmaxf(mxy, l.y);
-    }
-  }
-#pragma unroll
-  for (int i = 1; i + 1 < kMaxPolyV; ++i)
-    if (i + 1 < nv) A2 += (lx[i] - lx[0]) * (ly[i + 1] - ly[0]) - (ly[i] - ly[0]) * (lx[i + 1] - lx[0]);
-  if (!(fabsf(A2) >= 1e-10f)) return;
-  const float sgn = A2 > 0.f ? 1.f : -1.f;
-  // plane of the polygon and the pressure gradient, sensor frame
-  const V3<float> e1 = mk(lx[1] - lx[0], ly[1] - ly[0], lz[1] - lz[0]);
-  V3<float> nn = mk(0.f, 0.f, 0.f);
-#pragma unroll
-  for (int i = 2; i < kMaxPolyV; ++i)
-    if (i < nv) nn = nn + cross(e1, mk(lx[i] - lx[0], ly[i] - ly[0], lz[i] - lz[0]));
-  if (!(fabsf(nn.z) > 0.f)) return;
-  const float zx = -nn.x / nn.z, zy = -nn.y / nn.z;  // dz/dx, dz/dy on the plane
-  const V3<float> gl = mat_mul<float>(Rl, g_soft);
-  const float px = gl.x + gl.z * zx, py = gl.y + gl.z * zy;  // dp/dx, dp/dy on the plane
+  RasterPoly rp;
+  if (!raster_prepare(a, S, Rl, tl, nv, anc, g_soft,
+                      [&](int i) { return make_float4(v[i].x, v[i].y, v[i].z, v[i].p); }, rp))
+    return;
+  unsigned long long* smp = a.samples + S.sample_off;
   const float* sx = a.samp_coord + S.samp_off_x;
   const float* sy = a.samp_coord + S.samp_off_y;
-  const float x0 = sx[0], dx = S.nx > 1 ? sx[1] - sx[0] : 1.f;
-  const float y0 = sy[0], dy = S.ny > 1 ? sy[1] - sy[0] : 1.f;
-  const float fx0 = ceilf((mnx - x0) / dx - 1e-3f), fx1 = floorf((mxx - x0) / dx + 1e-3f);
-  const float fy0 = ceilf((mny - y0) / dy - 1e-3f), fy1 = floorf((mxy - y0) / dy + 1e-3f);
-  if (!(fx1 >= 0.f && fy1 >= 0.f && fx0 <= (float)(S.nx - 1) && fy0 <= (float)(S.ny - 1))) return;
-  const int X0 = max(0, (int)fx0), X1 = min(S.nx - 1, (int)fx1);
-  const int Y0 = max(0, (int)fy0), Y1 = min(S.ny - 1, (int)fy1);
-  unsigned long long* smp = a.samples + S.sample_off;
-  const float p0 = v[0].p;
-  // edge vectors (vertex i to its successor), static indices only
-  float ex[kMaxPolyV], ey[kMaxPolyV];
-#pragma unroll
-  for (int i = 0; i < kMaxPolyV; ++i) {
-    const bool last = i + 1 >= nv;
-    const float nx = last ? lx[0] : lx[i + 1 < kMaxPolyV ? i + 1 : 0];
-    const float ny = last ? ly[0] : ly[i + 1 < kMaxPolyV ? i + 1 : 0];
-    ex[i] = nx - lx[i];
-    ey[i] = ny - ly[i];
-  }
-  for (int X = X0; X <= X1; ++X) {
+  for (int X = rp.X0; X <= rp.X1; ++X) {
     const float qx = sx[X];
-    for (int Y = Y0; Y <= Y1; ++Y) {
-      const float qy = sy[Y];
-      bool in = true;
-#pragma unroll
-      for (int i = 0; i < kMaxPolyV; ++i) {
-        if (i < nv) {
-          const float e = ex[i] * (qy - ly[i]) - ey[i] * (qx - lx[i]);
-          in &= sgn * e >= 0.f;
-        }
-      }
-      if (!in) continue;
-      const float ddx = qx - lx[0], ddy = qy - ly[0];
-      const float z = lz[0] + zx * ddx + zy * ddy;
-      const float t = (S.zs15 + 1e-8f) - z;
-      if (!(t > 0.f && t < S.zs15)) continue;
-      const float pr = p0 + px * ddx + py * ddy;
-      const unsigned long long key =
-          ((unsigned long long)__float_as_uint(t) << 32) | (unsigned long long)__float_as_uint(pr);
+    for (int Y = rp.Y0; Y <= rp.Y1; ++Y) {
+      float t, z, pr;
+      if (!raster_probe(rp, S, qx, sy[Y], t, z, pr)) continue;
+      const unsigned long long key = key_pressure(t, pr);
       const size_t si = (size_t)X * S.ny + Y;
       if (!G) {
         atomicMin(&smp[si], key);
         continue;
       }
       if (atomicCAS(&smp[si], key, ~0ull) != key) continue;
-      // dL/dp at this sample: cell (X / sr, Y / sr), window weight of (X % sr, Y % sr)
-      const float w = a.weights[S.weight_off + (X % S.sr) * S.sr + (Y % S.sr)];
-      const float pbar = a.adj_taxel[S.taxel_off + X / S.sr + S.cy * (Y / S.sr)] * w * S.rmean;
-      if (pbar == 0.f) continue;
-      G->gE += pbar * pr;
-      const V3<float> xs = mat_tmul<float>(Rl, mk(qx, qy, z) - T);   // hit point, soft frame
-      if (!soft_is_sensor) {
-        // rays and plane move with the other body: dp = g . (w x x + v)
-        const V3<float> wx = cross(xs, g_soft);
-        G->gx[0] += pbar * wx.x; G->gx[1] += pbar * wx.y; G->gx[2] += pbar * wx.z;
-        G->gx[3] += pbar * g_soft.x; G->gx[4] += pbar * g_soft.y; G->gx[5] += pbar * g_soft.z;
-      } else {
-        // rays fixed in the soft frame, plane n.x = o moving: dx = dt D,
-        // dt = -(w.(n x x) - n.v) / (n.D), D = -(sensor z) in the soft frame
-        const V3<float> D = mk(-Rl[6], -Rl[7], -Rl[8]);
-        const float nD = dot(n_tri, D);
-        if (!(fabsf(nD) > 0.f)) continue;
-        const float r = -dot(g_soft, D) / nD;
-        const V3<float> nx = cross(n_tri, xs);
-        G->gx[0] += pbar * r * nx.x; G->gx[1] += pbar * r * nx.y; G->gx[2] += pbar * r * nx.z;
-        G->gx[3] -= pbar * r * n_tri.x; G->gx[4] -= pbar * r * n_tri.y; G->gx[5] -= pbar * r * n_tri.z;
-      }
+      sample_adjoint(a, S, Rl, tl, qx, sy[Y], z, pr, X, Y, g_soft, n_tri, soft_is_sensor, *G);
     }
   }
 }
