@@ -295,6 +295,8 @@ HC_API hc_status hc_get_adjoint_launch_count(hc_context* ctx, int* n);
 /* ---- measurement --------------------------------------------------------*/
 typedef struct {
   float ms_setup, ms_broadphase, ms_narrowphase, ms_reduce, ms_taxels, ms_total;
+  float ms_kept_polygons;   /* forces and rays of the kept polygons (part of
+                               the narrow-phase stage, not of ms_narrowphase) */
   int64_t n_items;
   int64_t n_polygons;
 } hc_timings;

@@ -61,7 +61,7 @@ class hc_candidate(C.Structure):
 class hc_timings(C.Structure):
     _fields_ = [("ms_setup", C.c_float), ("ms_broadphase", C.c_float), ("ms_narrowphase", C.c_float),
                 ("ms_reduce", C.c_float), ("ms_taxels", C.c_float), ("ms_total", C.c_float),
-                ("n_items", C.c_int64), ("n_polygons", C.c_int64)]
+                ("ms_kept_polygons", C.c_float), ("n_items", C.c_int64), ("n_polygons", C.c_int64)]
 
 
 _P = C.c_void_p

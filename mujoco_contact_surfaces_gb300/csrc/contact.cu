@@ -462,6 +462,7 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   if (a.type_unit_end[2] > a.type_unit_begin[2]) {
     narrow_ss_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
   }
+  if (ev) cudaEventRecordWithFlags(ev[6], s, cudaEventRecordExternal);
   if (a.recs && a.type_unit_end[1] > a.type_unit_begin[0]) {
     // kept polygons: pair-ordered slots, then forces and rays per polygon
     poly_count_kernel<<<a.n_item_blocks, kBpBlock, 0, s>>>(a); ++n;

@@ -187,7 +187,7 @@ struct hc_context {
   bool graph_valid = false;
   bool stepped = false;
   bool timing = false;
-  cudaEvent_t ev[6] = {};
+  cudaEvent_t ev[7] = {};   // stage boundaries; ev[6]: narrow kernels | kept polygons
   hc_timings last_timings = {};
   int launches_per_step = 0;
   int narrow_block = 128, narrow_ctas_per_sm = 8, narrow_chunk = 4;
@@ -1226,9 +1226,17 @@ hc_status hc_get_timings(hc_context* c, hc_timings* out) {
   HC_CUDA(cudaEventSynchronize(c->ev[5]));
   float t[5];
   for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&t[i], c->ev[i], c->ev[i + 1]);
+  // the narrow-phase stage splits at ev[6] into the narrow kernels and the
+  // pass over the kept polygons (zero when none are kept)
+  float t_narrow = t[2], t_kept = 0.f;
+  if (cudaEventElapsedTime(&t_narrow, c->ev[2], c->ev[6]) == cudaSuccess)
+    cudaEventElapsedTime(&t_kept, c->ev[6], c->ev[3]);
+  else
+    t_narrow = t[2];
   out->ms_setup = t[0];
   out->ms_broadphase = t[1];
-  out->ms_narrowphase = t[2];
+  out->ms_narrowphase = t_narrow;
+  out->ms_kept_polygons = t_kept;
   out->ms_reduce = t[3];
   out->ms_taxels = t[4];
   cudaEventElapsedTime(&out->ms_total, c->ev[0], c->ev[5]);

@@ -103,7 +103,7 @@ cudaError_t init_kernel_attributes();
 
 // One step: frames, broadphase, narrow phase, per-pair reduce, taxels.
 // Returns the number of kernels launched.
-int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev /* 6 or null */);
+int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev /* 7 or null */);
 
 // Adjoint of the last step (soft-rigid and half-space pairs).  Returns the
 // number of kernels launched.
