@@ -271,6 +271,34 @@ HC_API hc_status hc_get_taxels_all(hc_context* ctx, float* out, int64_t n_floats
 HC_API hc_status hc_get_taxels_device(hc_context* ctx, const float** d_taxels,
                                       int64_t* n_floats);
 
+/* ---- taxel-point sensor -------------------------------------------------
+ * Replaces TaxelSensor::load / internal_update (mujoco_contact_surface_
+ * sensors/src/taxel_sensor.cpp:46-156, 158-478): n_taxels points fixed in the
+ * geom's frame (n x 3 doubles), each valued from samples of the contact
+ * surfaces that involve the geom (in collision order, each polygon fanned
+ * about its area-weighted centroid): `method` HC_TAXEL_CLOSEST, _WEIGHTED,
+ * _MEAN, _SQUARED; `sample_method` HC_SAMPLE_DEFAULT (barycentric grid at
+ * `sample_resolution`) or HC_SAMPLE_AREA_IMPORTANCE (`sample_resolution` of
+ * each surface's area per sample, the reference's default-seeded
+ * minstd_rand0 stream); `include_margin` in metres.  The reference's
+ * quirks are kept: weighted and mean fall through into squared; closest
+ * reports 0 inside the margin unless `visualize` is set (its else binds to
+ * the visualisation test); taxels with no sample inside the margin keep
+ * their value.  Soft-rigid and half-space contacts; at most 1024 contact
+ * polygons per sensor geom per step (else HC_ERR_OVERFLOW from the read).   */
+enum { HC_TAXEL_CLOSEST = 0, HC_TAXEL_WEIGHTED = 1, HC_TAXEL_MEAN = 2, HC_TAXEL_SQUARED = 3 };
+enum { HC_SAMPLE_DEFAULT = 0, HC_SAMPLE_AREA_IMPORTANCE = 1 };
+HC_API hc_status hc_add_taxel_sensor(hc_context* ctx, int geom_id, int n_taxels, const double* taxels, int method,
+                                     double include_margin, double sample_resolution, int sample_method,
+                                     int visualize, int* out_sensor);
+/* Whether the next steps update the sensor (the update-rate gate of
+ * TactileSensorBase::update, tactile_sensor_base.cpp:89-120): a disabled
+ * sensor keeps its values.                                                */
+HC_API hc_status hc_set_taxel_sensor_enabled(hc_context* ctx, int sensor, int on);
+/* The sensor's values after the last step (n_taxels floats, taxel order).
+ * Synchronises the context stream.                                        */
+HC_API hc_status hc_get_taxel_sensor_values(hc_context* ctx, int sensor, float* out);
+
 /* ---- adjoint -------------------------------------------------------------
  * Gradient of L with respect to both geoms' 6-DoF poses (twist
  * [dtheta; dx], world frame, applied as X <- exp(dtheta) X, x <- x + dx)

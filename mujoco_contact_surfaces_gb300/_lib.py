@@ -26,6 +26,8 @@ HC_ERR_NO_DEVICE = 8
 GEOM_PLANE, GEOM_HFIELD, GEOM_SPHERE, GEOM_CAPSULE, GEOM_ELLIPSOID, GEOM_CYLINDER, GEOM_BOX, GEOM_MESH = range(8)
 REPR_TRIANGLE, REPR_POLYGON = 0, 1
 RIGID, SOFT = 0, 1
+TAXEL_CLOSEST, TAXEL_WEIGHTED, TAXEL_MEAN, TAXEL_SQUARED = range(4)
+SAMPLE_DEFAULT, SAMPLE_AREA_IMPORTANCE = 0, 1
 QUERY_NONE, QUERY_SOFT_RIGID, QUERY_SOFT_HALFSPACE, QUERY_SOFT_SOFT = 0, 1, 2, 3
 WINDOW_NONE, WINDOW_GAUSS, WINDOW_TUKEY, WINDOW_SQUARE = 0, 1, 2, 3
 
@@ -108,6 +110,10 @@ SIGNATURES = {
     "hc_get_launch_count": (C.c_int, [_P, _ip]),
     "hc_autotune": (C.c_int, [_P, _ip, _ip]),
     "hc_step_noalloc": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P]),
+    "hc_add_taxel_sensor": (C.c_int, [_P, C.c_int, C.c_int, _dp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
+                                      _ip]),
+    "hc_set_taxel_sensor_enabled": (C.c_int, [_P, C.c_int, C.c_int]),
+    "hc_get_taxel_sensor_values": (C.c_int, [_P, C.c_int, _fp]),
 }
 
 _lib = None

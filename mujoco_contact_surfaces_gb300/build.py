@@ -49,7 +49,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
-    common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden",
+    # host code without FMA contraction: its FP64 transforms (surfaces) match
+    # the device's explicitly rounded ones on every host architecture
+    common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
               "-I", os.path.join(ROOT, "include")]
 
     def compile_one(src):

@@ -615,6 +615,7 @@ __global__ void __launch_bounds__(128, 4) rec_forward_kernel(StepArgs a) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) v[k] = gsum(v[k]);
     if (on && sub == 0) {
+      a.rec_perm[dst] = r;
       RecOut o;
       o.F[0] = v[0]; o.F[1] = v[1]; o.F[2] = v[2];
       o.T[0] = v[3]; o.T[1] = v[4]; o.T[2] = v[5];

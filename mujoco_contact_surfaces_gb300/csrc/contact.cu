@@ -312,6 +312,7 @@ __global__ void bp_emit_kernel(StepArgs a) {
 
 #include "narrow.cuh"
 #include "adjoint.cuh"
+#include "taxel_sensor.cuh"
 
 // ---------------------------------------------------------------------------
 // per-pair reduction (fixed order, FP64) and the world-frame wrench
@@ -410,6 +411,8 @@ __global__ void taxel_kernel(StepArgs a) {
 cudaError_t init_kernel_attributes() {
   cudaError_t e = cudaFuncSetAttribute(narrow_sr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(taxel_sensor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTaxelSmemBytes);
+  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(adjoint_sr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
 }
 
@@ -469,6 +472,9 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
     poly_scan_kernel<<<1, kBpBlock, 0, s>>>(a); ++n;
     poly_emit_kernel<<<a.n_item_blocks, kBpBlock, 0, s>>>(a); ++n;
     rec_forward_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
+    if (a.n_tsens > 0) {
+      taxel_sensor_kernel<<<a.n_tsens, kTaxThreads, kTaxelSmemBytes, s>>>(a); ++n;
+    }
   }
   if (ev) cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal);
   if (a.n_pair > 0) {

@@ -72,6 +72,13 @@ struct GeomHost {
   std::vector<int> perm;       // Morton position -> original element
 };
 
+struct TaxelHost {
+  int geom;
+  int method, sample_method, visualize;
+  double margin, res;
+  std::vector<float4> taxels;   // geom frame
+};
+
 struct SensorHost {
   int geom;
   double resolution;
@@ -203,6 +210,15 @@ struct hc_context {
   DevBuf<int2> rec_key;
   DevBuf<hc::RecOut> rec_out;
   DevBuf<float4> slot_press;
+  DevBuf<int> rec_perm;
+  // taxel-point sensors
+  std::vector<TaxelHost> tsens_h;
+  std::vector<int> tsens_enabled_h;
+  DevBuf<hc::TaxelSensorDev> tsens;
+  DevBuf<int> tsens_pairs, tsens_enabled;
+  DevBuf<float4> taxel_pos;
+  DevBuf<float> taxel_val;
+  int n_taxel_total = 0;
   DevBuf<float> rec_grad;
   DevBuf<int> item_poly_off, poly_block_sum;
   int rec_cap = 0;
@@ -379,6 +395,7 @@ hc_status ensure_recs(hc_context* c, int cap) {
     HC_CUDA(c->rec_key.reserve(cap));
     HC_CUDA(c->rec_out.reserve(cap));
     HC_CUDA(c->slot_press.reserve(4 * (size_t)cap));
+    HC_CUDA(c->rec_perm.reserve(cap));
     HC_CUDA(c->rec_grad.reserve(16 * (size_t)cap));
     c->rec_cap = cap;
     invalidate_graph(c);
@@ -529,17 +546,24 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
   a.chunk = std::max(1, c->narrow_chunk);
   a.keep_samples = c->adjoint_mode ? 1 : 0;
   a.rec_count = c->counters.p + kCntRec;
-  // polygons are kept as records (rays cast from them, adjoint reads them)
-  // in adjoint mode and whenever sensors are attached
-  if ((c->adjoint_mode || c->n_cells > 0) && c->rec_cap > 0) {
+  // polygons are kept as records (rays cast and taxels sampled from them,
+  // the adjoint reads them) in adjoint mode and whenever sensors are attached
+  if ((c->adjoint_mode || c->n_cells > 0 || !c->tsens_h.empty()) && c->rec_cap > 0) {
     a.recs = c->recs.p;
     a.rec_key = c->rec_key.p;
     a.rec_cap = c->rec_cap;
     a.rec_out = c->rec_out.p;
     a.slot_press = c->slot_press.p;
+    a.rec_perm = c->rec_perm.p;
     a.item_poly_off = c->item_poly_off.p;
     a.poly_block_sum = c->poly_block_sum.p;
     a.n_item_blocks = std::max(1, (c->item_cap + hc::kBpBlock - 1) / hc::kBpBlock);
+    a.tsens = c->tsens.p;
+    a.n_tsens = (int)c->tsens_h.size();
+    a.tsens_pairs = c->tsens_pairs.p;
+    a.tsens_enabled = c->tsens_enabled.p;
+    a.taxel_pos = c->taxel_pos.p;
+    a.taxel_val = c->taxel_val.p;
   }
   return a;
 }
@@ -987,8 +1011,44 @@ hc_status hc_set_pairs(hc_context* c, int n_pair, const int* g1, const int* g2, 
   HC_CUDA(c->block_sum.reserve(c->n_bp_blocks));
   int want = c->cfg.item_capacity > 0 ? (int)c->cfg.item_capacity : std::max(1 << 16, 64 * n_pair);
   if (hc_status st = ensure_items(c, want)) return st;
-  if (c->n_cells > 0 || c->adjoint_mode)
+  if (c->n_cells > 0 || c->adjoint_mode || !c->tsens_h.empty())
     if (hc_status st = ensure_recs(c, initial_rec_cap(c))) return st;
+  // taxel-point sensors: the soft-rigid and half-space pairs of each sensor
+  // geom, in pair order
+  if (!c->tsens_h.empty()) {
+    std::vector<hc::TaxelSensorDev> td;
+    std::vector<int> tp;
+    std::vector<float4> pos;
+    for (const TaxelHost& h : c->tsens_h) {
+      hc::TaxelSensorDev d;
+      d.geom = h.geom;
+      d.n_taxels = (int)h.taxels.size();
+      d.taxel_off = (int)pos.size();
+      d.method = h.method;
+      d.sample_method = h.sample_method;
+      d.visualize = h.visualize;
+      d.margin = h.margin;
+      d.res = h.res;
+      d.pair_off = (int)tp.size();
+      for (int i = 0; i < n_pair; ++i)
+        if ((P[i].query == HC_QUERY_SOFT_RIGID || P[i].query == HC_QUERY_SOFT_HALFSPACE) &&
+            (g1[i] == h.geom || g2[i] == h.geom))
+          tp.push_back(i);
+      d.n_pairs = (int)tp.size() - d.pair_off;
+      pos.insert(pos.end(), h.taxels.begin(), h.taxels.end());
+      td.push_back(d);
+    }
+    HC_CUDA(c->tsens.upload(td, s));
+    if (tp.empty()) tp.push_back(0);
+    HC_CUDA(c->tsens_pairs.upload(tp, s));
+    HC_CUDA(c->tsens_enabled.upload(c->tsens_enabled_h, s));
+    HC_CUDA(c->taxel_pos.upload(pos, s));
+    if ((int)pos.size() != c->n_taxel_total) {
+      HC_CUDA(c->taxel_val.reserve(pos.size()));
+      HC_CUDA(cudaMemsetAsync(c->taxel_val.p, 0, pos.size() * sizeof(float), s));
+      c->n_taxel_total = (int)pos.size();
+    }
+  }
   HC_CUDA(cudaStreamSynchronize(s));
   invalidate_graph(c);
   c->stepped = false;
@@ -1146,6 +1206,63 @@ hc_status hc_get_surface(hc_context* c, int pair, hc_surface_view* view) {
     if (view->elem_b) view->elem_b[i] = p.elem_b;
   }
   if (view->poly_offset) view->poly_offset[n] = k;
+  return HC_OK;
+}
+
+hc_status hc_add_taxel_sensor(hc_context* c, int geom_id, int n_taxels, const double* taxels, int method,
+                              double include_margin, double sample_resolution, int sample_method, int visualize,
+                              int* out_sensor) {
+  if (hc_status st = need(c)) return st;
+  if (!c->geoms.count(geom_id)) return fail(HC_ERR_INVALID_ARG, "sensor geom has no cs:: properties");
+  if (n_taxels <= 0 || n_taxels > 1024 || !taxels) return fail(HC_ERR_INVALID_ARG, "1 to 1024 taxels are needed");
+  if (method < HC_TAXEL_CLOSEST || method > HC_TAXEL_SQUARED) return fail(HC_ERR_INVALID_ARG, "bad taxel method");
+  if (sample_method != HC_SAMPLE_DEFAULT && sample_method != HC_SAMPLE_AREA_IMPORTANCE)
+    return fail(HC_ERR_INVALID_ARG, "bad sample method");
+  if (!(include_margin > 0) || !(sample_resolution > 0) || !finite_all(taxels, 3 * (size_t)n_taxels))
+    return fail(HC_ERR_INVALID_ARG, "bad margin, resolution or taxel position");
+  TaxelHost h;
+  h.geom = geom_id;
+  h.method = method;
+  h.sample_method = sample_method;
+  h.visualize = visualize ? 1 : 0;
+  h.margin = include_margin;
+  h.res = sample_resolution;
+  for (int i = 0; i < n_taxels; ++i)
+    h.taxels.push_back(make_float4((float)taxels[3 * i], (float)taxels[3 * i + 1], (float)taxels[3 * i + 2], 0.f));
+  c->tsens_h.push_back(h);
+  c->tsens_enabled_h.push_back(1);
+  c->sensors_dirty = true;   // pairs are dispatched again before the next step
+  if (out_sensor) *out_sensor = (int)c->tsens_h.size() - 1;
+  return HC_OK;
+}
+
+hc_status hc_set_taxel_sensor_enabled(hc_context* c, int sensor, int on) {
+  if (hc_status st = need(c)) return st;
+  if (sensor < 0 || sensor >= (int)c->tsens_h.size()) return fail(HC_ERR_INVALID_ARG, "bad taxel sensor");
+  c->tsens_enabled_h[sensor] = on ? 1 : 0;
+  if (c->tsens_enabled.n >= c->tsens_enabled_h.size()) {
+    HC_CUDA(cudaSetDevice(c->device));
+    HC_CUDA(cudaMemcpyAsync(c->tsens_enabled.p + sensor, &c->tsens_enabled_h[sensor], sizeof(int),
+                            cudaMemcpyHostToDevice, c->stream));
+  }
+  return HC_OK;
+}
+
+hc_status hc_get_taxel_sensor_values(hc_context* c, int sensor, float* out) {
+  if (hc_status st = need(c)) return st;
+  if (sensor < 0 || sensor >= (int)c->tsens_h.size() || !out) return fail(HC_ERR_INVALID_ARG, "bad taxel sensor");
+  if (!c->stepped) return fail(HC_ERR_NOT_READY, "no step has run");
+  HC_CUDA(cudaSetDevice(c->device));
+  if (hc_status st = finish_step(c)) return st;
+  int cnt[8];
+  HC_CUDA(cudaMemcpy(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
+  if (cnt[kCntStatus] & 16)
+    return fail(HC_ERR_OVERFLOW, "a taxel sensor's geom had more than 1024 contact polygons in the last step");
+  int off = 0;
+  for (int k = 0; k < sensor; ++k) off += (int)c->tsens_h[k].taxels.size();
+  const size_t n = c->tsens_h[sensor].taxels.size();
+  if (c->taxel_val.n < (size_t)off + n) return fail(HC_ERR_NOT_READY, "taxel sensor not set up (call hc_set_pairs)");
+  HC_CUDA(cudaMemcpy(out, c->taxel_val.p + off, n * sizeof(float), cudaMemcpyDeviceToHost));
   return HC_OK;
 }
 

@@ -112,8 +112,21 @@ struct alignas(16) AdjPoly {
   float face[4][3];            // unnormalised tet face normals
   float clip[3][3];            // clip-plane normals (soft-rigid)
   int pair, nv, kind;          // kind: 0 soft-rigid, 1 half-space
+  int elem_a, elem_b;          // original soft tet, other element (-1: half-space)
 };
-static_assert(sizeof(AdjPoly) == 272, "AdjPoly layout");
+static_assert(sizeof(AdjPoly) == 288, "AdjPoly layout");
+
+// Taxel-point sensor (device): taxels at given points of a geom, valued from
+// samples of the contact surfaces that involve the geom.
+struct TaxelSensorDev {
+  int geom;
+  int n_taxels, taxel_off;     // taxel positions (geom frame) and values
+  int method;                  // 0 closest, 1 weighted, 2 mean, 3 squared
+  int sample_method;           // 0 default grid, 1 area importance
+  int visualize;
+  int pair_off, n_pairs;       // the pairs that involve the geom, in pair order
+  double margin, res;          // as given (the sample counts use res in double)
+};
 
 // Forces of one kept polygon (soft frame), in the pair-ordered record slot.
 struct alignas(16) RecOut {

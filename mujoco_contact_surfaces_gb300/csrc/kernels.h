@@ -89,6 +89,14 @@ struct StepArgs {
   RecOut* rec_out;           // per record in pair order: forces (forward)
   float4* slot_press;        // per record slot and sensor side (2): the linear
                              // pressure model (lx0, ly0, p0, px), (py, -, -, -)
+  int* rec_perm;             // per record slot: the record index
+  // taxel-point sensors
+  const TaxelSensorDev* tsens;
+  int n_tsens;
+  const int* tsens_pairs;
+  const int* tsens_enabled;  // per sensor: update in this step
+  const float4* taxel_pos;   // geom frame
+  float* taxel_val;          // values (kept between updates)
 };
 
 constexpr int kBpBlock = 256;

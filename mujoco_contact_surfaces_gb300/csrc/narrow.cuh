@@ -613,7 +613,7 @@ template <int ND>
 __device__ __forceinline__ void keep_polygon(const StepArgs& a, bool have, int item, int& seq, int lane, int pair,
                                              int kind, const PV<float, ND>* poly, int nv, V3<float> anc,
                                              V3<float> n, V3<float> g, float gint, const V3<float>* X,
-                                             const float (*clip)[3]) {
+                                             const float (*clip)[3], int elem_a, int elem_b) {
   const unsigned b = __ballot_sync(0xffffffffu, have);
   if (!b) return;
   int base = 0;
@@ -655,6 +655,8 @@ __device__ __forceinline__ void keep_polygon(const StepArgs& a, bool have, int i
   R.pair = pair;
   R.nv = nv;
   R.kind = kind;
+  R.elem_a = elem_a;
+  R.elem_b = elem_b;
 }
 
 constexpr int kNarrowWarps = 4;
@@ -912,7 +914,7 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
       __syncwarp();
       if (a.recs)
         keep_polygon<3>(a, have, item, seq, lane, it.x, 0, poly, nv, t.X[have ? anc : 0], n, t.g, gint, t.X,
-                        W.tri[jt].en);
+                        W.tri[jt].en, orig_a, orig_b);
     }
     __syncwarp();
     warp_reduce_store(a, ac, item, lane);
@@ -1036,7 +1038,8 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
     __syncwarp();
     if (a.recs) {
       int seq = 0;
-      keep_polygon<1>(a, have, item, seq, lane, it.x, 1, poly, nv, t.X[have ? anc : 0], n, t.g, gint, t.X, nullptr);
+      keep_polygon<1>(a, have, item, seq, lane, it.x, 1, poly, nv, t.X[have ? anc : 0], n, t.g, gint, t.X, nullptr,
+                      orig_a, -1);
     }
     __syncwarp();
     warp_reduce_store(a, ac, item, lane);

@@ -30,6 +30,7 @@ class Engine:
         L.check(self.lib.hc_context_create(C.byref(cfg), C.byref(self.ctx)))
         self.n_pair = 0
         self.sensors = {}   # sensor index -> (cx, cy)
+        self.taxel_sensors = {}   # taxel sensor index -> number of taxels
 
     def close(self):
         if self.ctx:
@@ -79,6 +80,24 @@ class Engine:
                                             C.byref(sid), C.byref(cx), C.byref(cy)))
         self.sensors[sid.value] = (cx.value, cy.value)
         return sid.value
+
+    def add_taxel_sensor(self, geom_id: int, taxels, method: int, include_margin: float, sample_resolution: float,
+                         sample_method: int = 0, visualize: bool = False) -> int:
+        t = np.ascontiguousarray(taxels, np.float64).reshape(-1, 3)
+        sid = C.c_int()
+        L.check(self.lib.hc_add_taxel_sensor(self.ctx, geom_id, t.shape[0], L.dptr(t), int(method),
+                                             float(include_margin), float(sample_resolution), int(sample_method),
+                                             int(visualize), C.byref(sid)))
+        self.taxel_sensors[sid.value] = t.shape[0]
+        return sid.value
+
+    def set_taxel_sensor_enabled(self, sensor: int, on: bool = True):
+        L.check(self.lib.hc_set_taxel_sensor_enabled(self.ctx, sensor, int(on)))
+
+    def taxel_sensor_values(self, sensor: int) -> np.ndarray:
+        out = np.zeros(self.taxel_sensors[sensor], np.float32)
+        L.check(self.lib.hc_get_taxel_sensor_values(self.ctx, sensor, L.fptr(out)))
+        return out
 
     # -- per step --------------------------------------------------------------
     def set_poses(self, xpos, xmat, vel=None):

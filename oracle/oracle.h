@@ -85,6 +85,27 @@ int or_surface(or_ctx* c, const double* xpos, const double* xmat, int g1, int g2
 /* Flat-sensor grid size as FlatTactileSensor::load computes it. */
 void or_sensor_grid(double xs, double ys, double resolution, int* cx, int* cy);
 
+/* Taxel-point sensor update (taxel.c; TaxelSensor::internal_update,
+ * mujoco_contact_surface_sensors/src/taxel_sensor.cpp:158-478). */
+typedef struct {
+  int n_taxels;
+  const double* taxels;     /* world positions, 3 per taxel                  */
+  int method;               /* 0 closest, 1 weighted, 2 mean, 3 squared      */
+  double include_margin;
+  double sample_resolution;
+  int sample_method;        /* 0 default grid, 1 area importance             */
+  int visualize;            /* changes the closest method's values (:311-327) */
+} or_taxel_cfg;
+/* Surfaces in collision order: surf_poly_off[n_surf+1] into polygons,
+ * poly_vert_off[n_poly+1] into vert (3 doubles, world) / vert_p; normal: 3
+ * per polygon.  values: n_taxels, in/out (kept where nothing is sampled
+ * within the margin).                                                      */
+void or_taxel_sensor(const or_taxel_cfg* cfg, int n_surf, const int* surf_poly_off, const int* poly_vert_off,
+                     const double* vert, const double* vert_p, const double* normal, double* values);
+/* Known-answer hooks of the sensor's random stream. */
+uint64_t or_minstd_nth(int n);
+double or_uniform_nth(int n);
+
 #ifdef __cplusplus
 }
 #endif

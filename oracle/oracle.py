@@ -17,12 +17,18 @@ LIB = os.path.join(HERE, "_build", "liboracle.so")
 
 
 def build(force: bool = False) -> str:
-    src = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "oracle.h")]
+    src = [os.path.join(HERE, f) for f in ("oracle.c", "taxel.c", "oracle.h", "Makefile")]
     if force or not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in src):
         r = subprocess.run(["make", "-s", "-C", HERE, "-B" if force else "-s"], capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
     return LIB
+
+
+class or_taxel_cfg(C.Structure):
+    _fields_ = [("n_taxels", C.c_int), ("taxels", C.POINTER(C.c_double)), ("method", C.c_int),
+                ("include_margin", C.c_double), ("sample_resolution", C.c_double), ("sample_method", C.c_int),
+                ("visualize", C.c_int)]
 
 
 class or_geom(C.Structure):
@@ -70,6 +76,11 @@ def load():
                                    C.POINTER(or_candidate), C.c_int64, C.POINTER(C.c_int64)]
         lib.or_surface.argtypes = [C.c_void_p, dp, dp, C.c_int, C.c_int, ip, ip, ip, dp, dp, dp, ip, ip]
         lib.or_sensor_grid.argtypes = [C.c_double, C.c_double, C.c_double, ip, ip]
+        lib.or_taxel_sensor.argtypes = [C.POINTER(or_taxel_cfg), C.c_int, ip, ip, dp, dp, dp, dp]
+        lib.or_minstd_nth.restype = C.c_uint64
+        lib.or_minstd_nth.argtypes = [C.c_int]
+        lib.or_uniform_nth.restype = C.c_double
+        lib.or_uniform_nth.argtypes = [C.c_int]
         _lib = lib
     return _lib
 
@@ -211,3 +222,34 @@ class Oracle:
         self.lib.or_surface(self.ctx, _dp(xpos), _dp(xmat), g1, g2, C.byref(npoly), C.byref(nv), _ip(off),
                             _dp(vert), _dp(pr), _dp(nrm), _ip(ea), _ip(eb))
         return dict(offset=off, vert=vert, pressure=pr, normal=nrm, elem_a=ea, elem_b=eb)
+
+
+def taxel_sensor(taxels_world, method, include_margin, sample_resolution, sample_method, visualize, surfaces,
+                 values=None):
+    """Taxel-point sensor update (or_taxel_sensor) on given contact surfaces.
+
+    surfaces: list, in collision order, of dicts with 'poly_offset' (n+1),
+    'vert' (k x 3, world), 'vert_pressure' (k), 'normal' (n x 3).  values:
+    the previous values (kept where nothing is sampled within the margin)."""
+    lib = load()
+    tx = np.ascontiguousarray(taxels_world, np.float64).reshape(-1, 3)
+    n = tx.shape[0]
+    out = np.zeros(n) if values is None else np.array(values, np.float64, copy=True)
+    surf_off, vert_off, verts, vps, nrms = [0], [0], [], [], []
+    for srf in surfaces:
+        po = np.asarray(srf["poly_offset"], np.int64)
+        for k in range(len(po) - 1):
+            vert_off.append(vert_off[-1] + int(po[k + 1] - po[k]))
+        surf_off.append(surf_off[-1] + len(po) - 1)
+        verts.append(np.asarray(srf["vert"], np.float64).reshape(-1, 3))
+        vps.append(np.asarray(srf["vert_pressure"], np.float64).reshape(-1))
+        nrms.append(np.asarray(srf["normal"], np.float64).reshape(-1, 3))
+    so = np.asarray(surf_off, np.int32)
+    vo = np.asarray(vert_off, np.int32)
+    V = np.ascontiguousarray(np.concatenate(verts) if verts else np.zeros((0, 3)))
+    P = np.ascontiguousarray(np.concatenate(vps) if vps else np.zeros(0))
+    N = np.ascontiguousarray(np.concatenate(nrms) if nrms else np.zeros((0, 3)))
+    cfg = or_taxel_cfg(n, _dp(tx), int(method), float(include_margin), float(sample_resolution), int(sample_method),
+                       int(visualize))
+    lib.or_taxel_sensor(C.byref(cfg), len(surfaces), _ip(so), _ip(vo), _dp(V), _dp(P), _dp(N), _dp(out))
+    return out

@@ -169,3 +169,29 @@ def test_no_contact_and_unsupported_pairs():
     s.g1, s.g2 = [a], [b]
     s.xpos = np.zeros((2, 3)); s.xmat = np.tile(np.eye(3).reshape(1, 9), (2, 1)); s.vel = np.zeros((2, 6))
     assert Oracle(s).collide()["query"][0] == 0   # rigid-rigid: default narrow phase
+
+
+def test_taxel_sensor_kat():
+    """Taxel-point sensor restatement (taxel_sensor.cpp:158-478): the random
+    stream, the closest method's visualisation quirk, the fall-through of
+    weighted and mean into squared, kept values and the empty case."""
+    import oracle
+    lib = oracle.load()
+    # C++ [rand.predef]: the 10000th draw of a default-constructed minstd_rand0
+    assert lib.or_minstd_nth(10000) == 1043618065
+    R = 2147483646.0
+    d1, d2 = 16807, 16807 * 16807 % 2147483647
+    assert lib.or_uniform_nth(1) == ((d1 - 1) + (d2 - 1) * R) / (R * R)
+    sq = dict(poly_offset=[0, 4], vert=[[0, 0, 0], [0.01, 0, 0], [0.01, 0.01, 0], [0, 0.01, 0]],
+              vert_pressure=[2, 2, 2, 2], normal=[[0, 0, 1]])
+    tx = [[0.005, 0.005, 0.0], [0.005, 0.005, 0.001], [0.5, 0.5, 0.5]]
+    prev = [7.0, 7.0, 7.0]
+    for sm, res in ((0, 0.001), (1, 0.01)):
+        v = oracle.taxel_sensor(tx, 0, 0.002, res, sm, 1, [sq], values=prev)
+        assert list(v) == [2.0, 2.0, 7.0]           # pressure inside, kept outside
+        v = oracle.taxel_sensor(tx, 0, 0.002, res, sm, 0, [sq], values=prev)
+        assert list(v) == [0.0, 0.0, 7.0]           # the else binds to the visualisation test
+        w = [oracle.taxel_sensor(tx, m, 0.002, res, sm, 0, [sq], values=prev) for m in (1, 2, 3)]
+        assert np.array_equal(w[0], w[1]) and np.array_equal(w[1], w[2])   # fall-through
+        assert w[2][0] > w[2][1] > 0 and w[2][2] == 7.0
+    assert list(oracle.taxel_sensor(tx, 3, 0.002, 0.001, 0, 0, [], values=prev)) == [0.0, 0.0, 0.0]
