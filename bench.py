@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--plain-sample", type=int, default=64, help="scenes timed on the plain path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--taxel-sensors", type=int, default=0,
+                    help="K: also attach a taxel-point sensor with a KxK taxel grid to every plate")
     return ap.parse_args()
 
 
@@ -236,6 +238,17 @@ def run_gb300(args):
     s = workload(args.scenes, rank)
     n_pair = len(s.g1)
     eng = scenes.build_engine(s, device=local)
+    extra = {}
+    if args.taxel_sensors > 0:
+        from mujoco_contact_surfaces_gb300 import _lib as L
+        k = args.taxel_sensors
+        g = np.linspace(-0.035, 0.035, k)
+        grid = np.array([[x, y, 0.005] for x in g for y in g])
+        for sn in s.sensors:
+            eng.add_taxel_sensor(sn["geom"], grid, L.TAXEL_SQUARED, 0.002, 0.0015, L.SAMPLE_DEFAULT, False)
+        eng.set_pairs(s.g1, s.g2)
+        extra["taxel_sensors"] = {"per_plate": k * k, "method": "squared", "include_margin": 0.002,
+                                  "sample_resolution": 0.0015, "sample_method": "default"}
     eng.set_adjoint_mode(True)
     tuned_ctas, tuned_chunk = eng.autotune()       # launch shape, before any timing
     eng.enable_timing(True)
@@ -300,6 +313,7 @@ def run_gb300(args):
     ht = torch.tensor(dLdt_h, dtype=torch.float32).pin_memory().numpy()
     h2d = hx.nbytes + hm.nbytes + hv.nbytes + hw.nbytes + ht.nbytes
     d2h = n_pair * 6 * 8 + len(s.sensors) * 256 * 4 + n_pair * 14 * 8
+    d2h += len(s.sensors) * args.taxel_sensors ** 2 * 4
     e2e_ms = []
     for _ in range(max(3, args.steps // 2)):
         with torch.cuda.stream(stream):
@@ -310,6 +324,8 @@ def run_gb300(args):
         eng.step()
         eng.wrenches()
         eng.all_taxels()
+        if args.taxel_sensors > 0:
+            eng.all_taxel_sensor_values()
         eng.adjoint(hw, ht)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e = n_pair * world / (max_over_ranks(statistics.median(e2e_ms), world) * 1e-3)
@@ -332,7 +348,8 @@ def run_gb300(args):
                                             "tris_touched": ab["tris"], "ms_forward": t_step - adj_avg,
                                             "ms_adjoint": adj_avg, "ms_narrow_kernel": narrow_avg,
                                             "ms_kept_polygons_pass": kept_avg,
-                                            "autotuned": {"ctas_per_sm": tuned_ctas, "chunk": tuned_chunk}}),
+                                            "autotuned": {"ctas_per_sm": tuned_ctas, "chunk": tuned_chunk},
+                                            **extra}),
         "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",

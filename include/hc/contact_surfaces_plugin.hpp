@@ -13,6 +13,7 @@
 //   SurfacePlugin::update              mujoco_contact_surfaces/include/mujoco_contact_surfaces/plugin_utils.h:94
 //   TactileSensorBase::update          mujoco_contact_surface_sensors/src/tactile_sensor_base.cpp:89-120
 //   FlatTactileSensor::load            mujoco_contact_surface_sensors/src/flat_tactile_sensor.cpp:127-214
+//   TaxelSensor::load                  mujoco_contact_surface_sensors/src/taxel_sensor.cpp:46-156
 //
 // The class is a template over an `Api` traits type that names the MuJoCo
 // types and the four MuJoCo calls the plugin needs, so it compiles against
@@ -40,6 +41,7 @@
 #define HC_CONTACT_SURFACES_PLUGIN_HPP_
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <memory>
 #include <string>
@@ -117,6 +119,9 @@ class SurfacePlugin {
   virtual ~SurfacePlugin() = default;
   virtual bool load(const typename Api::Model* m, typename Api::Data* d, hc_context* ctx) = 0;
   virtual void reset() {}
+  // Called before the step that update() will report (d->time is the
+  // step's time): a plugin whose device work is gated can switch it here.
+  virtual void before_step(const typename Api::Model*, typename Api::Data*) {}
   virtual void update(const typename Api::Model* m, typename Api::Data* d, const StepView& step) = 0;
 };
 
@@ -183,6 +188,113 @@ class FlatTactileSensor : public SurfacePlugin<Api> {
   FlatSensorConfig cfg_;
   hc_context* ctx_ = nullptr;
   int geom_id_ = -1, sensor_ = -1, cx_ = 0, cy_ = 0, n_updates_ = 0;
+  double period_ = 0.0, last_update_ = -1e300;
+  std::vector<float> values_;
+};
+
+// Maps points (x, y, z triples) by the inverse of the pose (p, unit
+// quaternion q = w, x, y, z): t <- R(q)^T (t - p), the mju_negPose /
+// mju_quat2Mat product of taxel_sensor.cpp:130-140.  The identity pose leaves
+// the points as they are.
+inline void apply_inverse_pose(const double p[3], const double q[4], std::vector<double>& t) {
+  if (p[0] == 0 && p[1] == 0 && p[2] == 0 && q[0] == 1 && q[1] == 0 && q[2] == 0 && q[3] == 0) return;
+  const double w = q[0], x = q[1], y = q[2], z = q[3];
+  const double Rq[9] = {1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+                        2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                        2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)};
+  double R[9], o[3];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) R[3 * r + c] = Rq[3 * c + r];
+  for (int r = 0; r < 3; ++r) o[r] = -(R[3 * r] * p[0] + R[3 * r + 1] * p[1] + R[3 * r + 2] * p[2]);
+  for (size_t i = 0; i + 2 < t.size(); i += 3) {
+    const double a0 = t[i], a1 = t[i + 1], a2 = t[i + 2];
+    for (int r = 0; r < 3; ++r) t[i + r] = R[3 * r] * a0 + R[3 * r + 1] * a1 + R[3 * r + 2] * a2 + o[r];
+  }
+}
+
+// Taxel-point sensor (taxel_sensor.cpp:46-156 load, 158-478 update): taxels
+// at points of the geom's frame, valued on the device from samples of the
+// contact surfaces; the update-rate gate switches the device update on for
+// the steps it reports.  For a mesh geom with a local pose (Api::kGeomLocalPose
+// and a non-identity geom_pos / geom_quat) the taxels are moved by the
+// inverse of that pose, as the reference does (taxel_sensor.cpp:121-147).
+struct TaxelSensorConfig {
+  std::string sensor_name;
+  std::string geom_name;
+  double update_rate = 100.0;
+  std::vector<std::array<double, 3>> taxels;
+  std::string method = "closest";          // closest, weighted, mean, squared
+  double include_margin = 0.0;
+  double sample_resolution = 0.0;
+  std::string sample_method = "default";   // default, area_importance
+  bool visualize = false;
+};
+
+template <class Api>
+class TaxelSensor : public SurfacePlugin<Api> {
+ public:
+  explicit TaxelSensor(TaxelSensorConfig cfg) : cfg_(std::move(cfg)) {}
+
+  bool load(const typename Api::Model* m, typename Api::Data*, hc_context* ctx) override {
+    ctx_ = ctx;
+    const int g = Api::name2id(m, Api::kObjGeom, cfg_.geom_name.c_str());
+    if (g < 0 || cfg_.taxels.empty() || cfg_.update_rate <= 0) return false;
+    int method = -1, sample = -1;
+    if (cfg_.method == "closest") method = HC_TAXEL_CLOSEST;
+    else if (cfg_.method == "weighted") method = HC_TAXEL_WEIGHTED;
+    else if (cfg_.method == "mean") method = HC_TAXEL_MEAN;
+    else if (cfg_.method == "squared") method = HC_TAXEL_SQUARED;
+    if (cfg_.sample_method == "default") sample = HC_SAMPLE_DEFAULT;
+    else if (cfg_.sample_method == "area_importance") sample = HC_SAMPLE_AREA_IMPORTANCE;
+    if (method < 0 || sample < 0) return false;
+    std::vector<double> t;
+    for (const auto& p : cfg_.taxels) t.insert(t.end(), p.begin(), p.end());
+    move_to_geom_frame(m, g, t);
+    if (hc_add_taxel_sensor(ctx, g, (int)cfg_.taxels.size(), t.data(), method, cfg_.include_margin,
+                            cfg_.sample_resolution, sample, cfg_.visualize ? 1 : 0, &sensor_) != HC_OK)
+      return false;
+    values_.assign(cfg_.taxels.size(), 0.f);
+    period_ = 1.0 / cfg_.update_rate;
+    last_update_ = -1e300;
+    return true;
+  }
+
+  void reset() override { last_update_ = -1e300; }
+
+  void before_step(const typename Api::Model*, typename Api::Data* d) override {
+    due_ = d->time < last_update_ || d->time - last_update_ >= period_;
+    hc_set_taxel_sensor_enabled(ctx_, sensor_, due_ ? 1 : 0);
+  }
+
+  void update(const typename Api::Model*, typename Api::Data* d, const StepView&) override {
+    if (!due_) return;
+    last_update_ = d->time;
+    if (hc_get_taxel_sensor_values(ctx_, sensor_, values_.data()) == HC_OK) ++n_updates_;
+  }
+
+  const std::vector<float>& values() const { return values_; }
+  const std::string& name() const { return cfg_.sensor_name; }
+  int n_updates() const { return n_updates_; }
+
+ private:
+  template <class A = Api>
+  static auto local_pose(const typename A::Model* m, int g, double p[3], double q[4])
+      -> decltype(A::kGeomLocalPose, void()) {
+    for (int k = 0; k < 3; ++k) p[k] = m->geom_pos[3 * g + k];
+    for (int k = 0; k < 4; ++k) q[k] = m->geom_quat[4 * g + k];
+  }
+  static void local_pose(...) {}
+
+  void move_to_geom_frame(const typename Api::Model* m, int g, std::vector<double>& t) const {
+    double p[3] = {0, 0, 0}, q[4] = {1, 0, 0, 0};
+    local_pose(m, g, p, q);
+    if (m->geom_type[g] == HC_GEOM_MESH) apply_inverse_pose(p, q, t);
+  }
+
+  TaxelSensorConfig cfg_;
+  hc_context* ctx_ = nullptr;
+  int sensor_ = -1, n_updates_ = 0;
+  bool due_ = false;
   double period_ = 0.0, last_update_ = -1e300;
   std::vector<float> values_;
 };
@@ -288,6 +400,7 @@ class MujocoContactSurfacesPlugin {
         if (step_ok_ && hc_get_pair_order(ctx_, nullptr, m_geom_.data(), n_geom_.data()) != HC_OK) step_ok_ = false;
       }
       if (step_ok_ && hc_set_poses(ctx_, m->ngeom, d->geom_xpos, d->geom_xmat, vel_.data()) != HC_OK) step_ok_ = false;
+      for (SurfacePlugin<Api>* p : ready_) p->before_step(m, d);
       if (step_ok_ && hc_step(ctx_) != HC_OK) step_ok_ = false;
       wrench_.assign(6 * (size_t)n, 0.0);
       if (step_ok_ && n > 0 && hc_get_wrenches(ctx_, wrench_.data()) != HC_OK) step_ok_ = false;

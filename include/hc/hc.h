@@ -284,8 +284,10 @@ HC_API hc_status hc_get_taxels_device(hc_context* ctx, const float** d_taxels,
  * quirks are kept: weighted and mean fall through into squared; closest
  * reports 0 inside the margin unless `visualize` is set (its else binds to
  * the visualisation test); taxels with no sample inside the margin keep
- * their value.  Soft-rigid and half-space contacts; at most 1024 contact
- * polygons per sensor geom per step (else HC_ERR_OVERFLOW from the read).   */
+ * their value.  Soft-rigid and half-space contacts; 1 to 2^20 taxels; any
+ * number of contact polygons.  A triangle side of more than 4096 grid
+ * steps, or more than 2^20 samples in one fan triangle, makes the next read
+ * return HC_ERR_OVERFLOW (the resolution is too fine for the contact).      */
 enum { HC_TAXEL_CLOSEST = 0, HC_TAXEL_WEIGHTED = 1, HC_TAXEL_MEAN = 2, HC_TAXEL_SQUARED = 3 };
 enum { HC_SAMPLE_DEFAULT = 0, HC_SAMPLE_AREA_IMPORTANCE = 1 };
 HC_API hc_status hc_add_taxel_sensor(hc_context* ctx, int geom_id, int n_taxels, const double* taxels, int method,
@@ -298,6 +300,10 @@ HC_API hc_status hc_set_taxel_sensor_enabled(hc_context* ctx, int sensor, int on
 /* The sensor's values after the last step (n_taxels floats, taxel order).
  * Synchronises the context stream.                                        */
 HC_API hc_status hc_get_taxel_sensor_values(hc_context* ctx, int sensor, float* out);
+/* Every taxel sensor's values after the last step, sensor after sensor in
+ * the order they were added, in one copy (`capacity` floats at `out`; it
+ * must hold the total taxel count).  Synchronises the context stream.      */
+HC_API hc_status hc_get_all_taxel_sensor_values(hc_context* ctx, float* out, size_t capacity);
 
 /* ---- adjoint -------------------------------------------------------------
  * Gradient of L with respect to both geoms' 6-DoF poses (twist

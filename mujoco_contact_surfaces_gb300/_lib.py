@@ -114,6 +114,7 @@ SIGNATURES = {
                                       _ip]),
     "hc_set_taxel_sensor_enabled": (C.c_int, [_P, C.c_int, C.c_int]),
     "hc_get_taxel_sensor_values": (C.c_int, [_P, C.c_int, _fp]),
+    "hc_get_all_taxel_sensor_values": (C.c_int, [_P, _fp, C.c_size_t]),
 }
 
 _lib = None

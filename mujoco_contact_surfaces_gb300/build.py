@@ -17,9 +17,9 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libhc.so")
 
-SOURCES = ["contact.cu", "hc_api.cu", "noalloc.cu", "meshgen.cpp", "plugin_shim.cpp"]
+SOURCES = ["contact.cu", "hc_api.cu", "noalloc.cu", "meshgen.cpp"]
 HEADERS = ["clip.cuh", "geom_math.cuh", "narrow.cuh", "adjoint.cuh", "hc_internal.h", "kernels.h", "meshgen.h",
-           "noalloc.h", "plugin_shim.h"]
+           "noalloc.h", "taxel_sensor.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -31,7 +31,7 @@ def _nvcc() -> str:
 
 
 def _sources():
-    return [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
+    return list(SOURCES)
 
 
 def _stale() -> bool:

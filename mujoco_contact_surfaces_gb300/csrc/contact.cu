@@ -473,6 +473,9 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
     poly_emit_kernel<<<a.n_item_blocks, kBpBlock, 0, s>>>(a); ++n;
     rec_forward_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
     if (a.n_tsens > 0) {
+      if (a.n_tpairs > 0) {
+        taxel_order_kernel<<<a.n_tpairs, kTaxThreads, 0, s>>>(a); ++n;
+      }
       taxel_sensor_kernel<<<a.n_tsens, kTaxThreads, kTaxelSmemBytes, s>>>(a); ++n;
     }
   }

@@ -218,6 +218,9 @@ struct hc_context {
   DevBuf<int> tsens_pairs, tsens_enabled;
   DevBuf<float4> taxel_pos;
   DevBuf<float> taxel_val;
+  DevBuf<int> tpairs, tsort, tidx;   // taxel-sensor pairs; polygon order per record slot
+  DevBuf<unsigned long long> tkey;
+  int n_tpairs = 0;
   int n_taxel_total = 0;
   DevBuf<float> rec_grad;
   DevBuf<int> item_poly_off, poly_block_sum;
@@ -400,6 +403,12 @@ hc_status ensure_recs(hc_context* c, int cap) {
     c->rec_cap = cap;
     invalidate_graph(c);
   }
+  if (!c->tsens_h.empty() && c->tsort.n < (size_t)c->rec_cap) {
+    HC_CUDA(c->tsort.reserve(c->rec_cap));
+    HC_CUDA(c->tidx.reserve(c->rec_cap));
+    HC_CUDA(c->tkey.reserve(c->rec_cap));
+    invalidate_graph(c);
+  }
   return ensure_rec_offsets(c);
 }
 
@@ -564,6 +573,11 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
     a.tsens_enabled = c->tsens_enabled.p;
     a.taxel_pos = c->taxel_pos.p;
     a.taxel_val = c->taxel_val.p;
+    a.tpairs = c->tpairs.p;
+    a.n_tpairs = c->n_tpairs;
+    a.tsort = c->tsort.p;
+    a.tkey = c->tkey.p;
+    a.tidx = c->tidx.p;
   }
   return a;
 }
@@ -1039,6 +1053,12 @@ hc_status hc_set_pairs(hc_context* c, int n_pair, const int* g1, const int* g2, 
       td.push_back(d);
     }
     HC_CUDA(c->tsens.upload(td, s));
+    std::vector<int> up(tp);
+    std::sort(up.begin(), up.end());
+    up.erase(std::unique(up.begin(), up.end()), up.end());
+    c->n_tpairs = (int)up.size();
+    if (up.empty()) up.push_back(0);
+    HC_CUDA(c->tpairs.upload(up, s));
     if (tp.empty()) tp.push_back(0);
     HC_CUDA(c->tsens_pairs.upload(tp, s));
     HC_CUDA(c->tsens_enabled.upload(c->tsens_enabled_h, s));
@@ -1214,7 +1234,7 @@ hc_status hc_add_taxel_sensor(hc_context* c, int geom_id, int n_taxels, const do
                               int* out_sensor) {
   if (hc_status st = need(c)) return st;
   if (!c->geoms.count(geom_id)) return fail(HC_ERR_INVALID_ARG, "sensor geom has no cs:: properties");
-  if (n_taxels <= 0 || n_taxels > 1024 || !taxels) return fail(HC_ERR_INVALID_ARG, "1 to 1024 taxels are needed");
+  if (n_taxels <= 0 || n_taxels > (1 << 20) || !taxels) return fail(HC_ERR_INVALID_ARG, "1 to 2^20 taxels are needed");
   if (method < HC_TAXEL_CLOSEST || method > HC_TAXEL_SQUARED) return fail(HC_ERR_INVALID_ARG, "bad taxel method");
   if (sample_method != HC_SAMPLE_DEFAULT && sample_method != HC_SAMPLE_AREA_IMPORTANCE)
     return fail(HC_ERR_INVALID_ARG, "bad sample method");
@@ -1257,12 +1277,32 @@ hc_status hc_get_taxel_sensor_values(hc_context* c, int sensor, float* out) {
   int cnt[8];
   HC_CUDA(cudaMemcpy(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
   if (cnt[kCntStatus] & 16)
-    return fail(HC_ERR_OVERFLOW, "a taxel sensor's geom had more than 1024 contact polygons in the last step");
+    return fail(HC_ERR_OVERFLOW, "a taxel sensor exceeded its sample limit in the last step (4096 grid steps per "
+                                 "triangle side, 2^20 samples per fan triangle): the sample resolution is too fine");
   int off = 0;
   for (int k = 0; k < sensor; ++k) off += (int)c->tsens_h[k].taxels.size();
   const size_t n = c->tsens_h[sensor].taxels.size();
   if (c->taxel_val.n < (size_t)off + n) return fail(HC_ERR_NOT_READY, "taxel sensor not set up (call hc_set_pairs)");
   HC_CUDA(cudaMemcpy(out, c->taxel_val.p + off, n * sizeof(float), cudaMemcpyDeviceToHost));
+  return HC_OK;
+}
+
+hc_status hc_get_all_taxel_sensor_values(hc_context* c, float* out, size_t capacity) {
+  if (hc_status st = need(c)) return st;
+  size_t total = 0;
+  for (const TaxelHost& h : c->tsens_h) total += h.taxels.size();
+  if (!out || capacity < total) return fail(HC_ERR_INVALID_ARG, "output smaller than the total taxel count");
+  if (total == 0) return HC_OK;
+  if (!c->stepped) return fail(HC_ERR_NOT_READY, "no step has run");
+  HC_CUDA(cudaSetDevice(c->device));
+  if (hc_status st = finish_step(c)) return st;
+  int cnt[8];
+  HC_CUDA(cudaMemcpy(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
+  if (cnt[kCntStatus] & 16)
+    return fail(HC_ERR_OVERFLOW, "a taxel sensor exceeded its sample limit in the last step (4096 grid steps per "
+                                 "triangle side, 2^20 samples per fan triangle): the sample resolution is too fine");
+  if (c->taxel_val.n < total) return fail(HC_ERR_NOT_READY, "taxel sensors not set up (call hc_set_pairs)");
+  HC_CUDA(cudaMemcpy(out, c->taxel_val.p, total * sizeof(float), cudaMemcpyDeviceToHost));
   return HC_OK;
 }
 

@@ -97,6 +97,11 @@ struct StepArgs {
   const int* tsens_enabled;  // per sensor: update in this step
   const float4* taxel_pos;   // geom frame
   float* taxel_val;          // values (kept between updates)
+  const int* tpairs;         // the pairs any taxel sensor reads (each once)
+  int n_tpairs;
+  int* tsort;                // per record slot of those pairs: the slot in polygon order
+  unsigned long long* tkey;  // sort scratch (pairs of more than 2048 polygons)
+  int* tidx;
 };
 
 constexpr int kBpBlock = 256;

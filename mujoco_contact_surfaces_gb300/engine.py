@@ -99,6 +99,12 @@ class Engine:
         L.check(self.lib.hc_get_taxel_sensor_values(self.ctx, sensor, L.fptr(out)))
         return out
 
+    def all_taxel_sensor_values(self) -> np.ndarray:
+        """Every taxel sensor's values, concatenated in sensor order (one copy)."""
+        out = np.zeros(sum(self.taxel_sensors.values()), np.float32)
+        L.check(self.lib.hc_get_all_taxel_sensor_values(self.ctx, L.fptr(out), out.size))
+        return out
+
     # -- per step --------------------------------------------------------------
     def set_poses(self, xpos, xmat, vel=None):
         xpos = np.ascontiguousarray(xpos, np.float64)

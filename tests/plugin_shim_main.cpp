@@ -35,10 +35,12 @@ struct FakeModel {
   int* mesh_faceadr = nullptr;
   int* mesh_facenum = nullptr;
   int* mesh_face = nullptr;
+  double* geom_pos = nullptr;
+  double* geom_quat = nullptr;
   // storage
   std::vector<std::string> geom_names, numeric_names, text_names;
   std::vector<int> v_type, v_body, v_dataid, v_nadr, v_nsize, v_tadr, v_tsize;
-  std::vector<double> v_size, v_ndata;
+  std::vector<double> v_size, v_ndata, v_pos, v_quat;
   std::vector<char> v_tdata;
 
   int add_geom(const std::string& name, int type, double sx, double sy, double sz, int body) {
@@ -47,6 +49,8 @@ struct FakeModel {
     v_size.insert(v_size.end(), {sx, sy, sz});
     v_body.push_back(body);
     v_dataid.push_back(-1);
+    v_pos.insert(v_pos.end(), {0, 0, 0});
+    v_quat.insert(v_quat.end(), {1, 0, 0, 0});
     return (int)geom_names.size() - 1;
   }
   void add_numeric(const std::string& name, std::vector<double> vals) {
@@ -68,6 +72,8 @@ struct FakeModel {
     geom_size = v_size.data();
     geom_bodyid = v_body.data();
     geom_dataid = v_dataid.data();
+    geom_pos = v_pos.data();
+    geom_quat = v_quat.data();
     nnumeric = (int)numeric_names.size();
     numeric_adr = v_nadr.data();
     numeric_size = v_nsize.data();
@@ -96,6 +102,7 @@ struct FakeApi {
   using Contact = FakeContact;
   using Real = double;
   static constexpr int kObjGeom = 5, kObjNumeric = 18, kObjText = 19;
+  static constexpr bool kGeomLocalPose = true;  // the model has geom_pos / geom_quat
   static int name2id(const Model* m, int type, const char* name) {
     const std::vector<std::string>* v = type == kObjGeom ? &m->geom_names
                                         : type == kObjNumeric ? &m->numeric_names
@@ -175,6 +182,16 @@ int main(int argc, char** argv) {
     m.add_text("cs::HydroelasticContactRepresentation", "kPolygon please");
     m.finalize();
     printf("repr2 %d\n", hc_plugin::parse_custom_fields<FakeApi>(&m).representation);
+    // taxels of a mesh geom with a local pose move by the inverse pose
+    const double p0[3] = {0.1, -0.2, 0.3};
+    const double h = std::sqrt(0.5), q0[4] = {h, 0, 0, h};  // 90 degrees about z
+    std::vector<double> t = {1.0, 2.0, 3.0, 0.1, -0.2, 0.3};
+    hc_plugin::apply_inverse_pose(p0, q0, t);
+    printf("invpose %.17g %.17g %.17g %.17g %.17g %.17g\n", t[0], t[1], t[2], t[3], t[4], t[5]);
+    const double pi[3] = {0, 0, 0}, qi[4] = {1, 0, 0, 0};
+    std::vector<double> u = {1.0, 2.0, 3.0};
+    hc_plugin::apply_inverse_pose(pi, qi, u);
+    printf("identity %.17g %.17g %.17g\n", u[0], u[1], u[2]);
     return 0;
   }
   // step: ball pressed into the plate, cube resting on the floor, stick
@@ -206,6 +223,28 @@ int main(int argc, char** argv) {
   auto sensor = std::make_unique<hc_plugin::FlatTactileSensor<FakeApi>>(sc);
   hc_plugin::FlatTactileSensor<FakeApi>* sp = sensor.get();
   plugin.add_plugin(std::move(sensor));
+  // taxel sensors on the plate's top face: a 5 x 5 grid, squared-distance
+  // ("mean" falls through to it) and closest with visualisation
+  hc_plugin::TaxelSensorConfig tc;
+  tc.sensor_name = "plate_taxels";
+  tc.geom_name = "plate";
+  tc.update_rate = 50.0;
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 5; ++j) tc.taxels.push_back({-0.01 + 0.005 * i, -0.01 + 0.005 * j, 0.005});
+  tc.method = "mean";
+  tc.include_margin = 0.004;
+  tc.sample_resolution = 0.002;
+  auto taxel = std::make_unique<hc_plugin::TaxelSensor<FakeApi>>(tc);
+  hc_plugin::TaxelSensor<FakeApi>* tp = taxel.get();
+  plugin.add_plugin(std::move(taxel));
+  tc.sensor_name = "plate_closest";
+  tc.method = "closest";
+  tc.visualize = true;
+  tc.sample_method = "area_importance";
+  tc.sample_resolution = 0.01;
+  auto closest = std::make_unique<hc_plugin::TaxelSensor<FakeApi>>(tc);
+  hc_plugin::TaxelSensor<FakeApi>* cp = closest.get();
+  plugin.add_plugin(std::move(closest));
   if (!plugin.load(&m, &d)) {
     printf("load_failed %s\n", Plugin::last_error().c_str());
     return 1;
@@ -225,8 +264,8 @@ int main(int argc, char** argv) {
       (void)r;
     }
     plugin.passiveCallback(&m, &d);
-    printf("step %d ok %d applies %d sensor_updates %d\n", step, plugin.last_step_ok() ? 1 : 0, d.n_apply,
-           sp->n_updates());
+    printf("step %d ok %d applies %d sensor_updates %d taxel_updates %d %d\n", step, plugin.last_step_ok() ? 1 : 0,
+           d.n_apply, sp->n_updates(), tp->n_updates(), cp->n_updates());
   }
   printf("counts default %d surface %d\n", n_default, n_surface);
   const std::vector<double>& w = plugin.last_wrenches();
@@ -243,6 +282,11 @@ int main(int argc, char** argv) {
     tmax = std::max(tmax, (double)v);
   }
   printf("taxels %d %d %.9g %.9g\n", sp->cx(), sp->cy(), tsum, tmax);
+  printf("taxel_values");
+  for (float v : tp->values()) printf(" %.9g", v);
+  printf("\nclosest_values");
+  for (float v : cp->values()) printf(" %.9g", v);
+  printf("\n");
   // geom resize: the ball grows, next step sees a deeper contact
   m.v_size[0] = 0.031;
   m.finalize();

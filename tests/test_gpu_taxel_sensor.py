@@ -71,6 +71,9 @@ def test_taxel_sensor_matches_oracle(gpu):
             prev[(plate, ci)] = ref
             if step == 0 and plate == s.g2[0]:
                 assert np.count_nonzero(ref) > 0
+        # one bulk copy of every sensor equals the per-sensor reads
+        each = np.concatenate([eng.taxel_sensor_values(sid) for sid in sorted(sensors.values())])
+        np.testing.assert_array_equal(eng.all_taxel_sensor_values(), each)
         if step == 1:
             assert all(np.all(prev[(s.g2[0], ci)] == 0.0) for ci in range(len(CONFIGS)))
     eng.close()
@@ -94,3 +97,33 @@ def test_disabled_sensor_keeps_values(gpu):
     v2 = eng.taxel_sensor_values(sid)
     eng.close()
     assert np.count_nonzero(v0) > 0 and np.array_equal(v0, v1) and np.all(v2 == 0)
+
+
+def test_large_surface_and_taxel_groups(gpu):
+    """One half-space contact of ~28k polygons (the polygon order is sorted in
+    14 chunks and ranked across them) read by 1089 taxels (two passes of 1024
+    taxels over the samples), against the oracle; area-importance samples
+    depend on that order through the shared random stream."""
+    s = scenes.Scene()
+    ground = s.add_geom(L.GEOM_PLANE, [0, 0, 1], [0, 1.0, 0, 0.5, 0.5])
+    box = s.add_geom(L.GEOM_BOX, [0.05, 0.05, 0.01], [2e5, 1.0, 0.0015, 0.5, 0.5])
+    s.g1.append(box); s.g2.append(ground); s.scene_of_pair.append(0)
+    scenes._alloc(s)
+    s.xpos[box] = [0.0013, -0.0007, 0.01 - 0.0043]
+    s.xmat[box] = scenes.rot_axis([0, 0, 1], 0.3).reshape(9)
+    eng = scenes.build_engine(s)
+    g = np.linspace(-0.06, 0.06, 33)
+    tx = np.array([[x, y, 0.0] for x in g for y in g])
+    cfgs = [(L.TAXEL_SQUARED, L.SAMPLE_DEFAULT, 0.004, 0, 0.003),
+            (L.TAXEL_CLOSEST, L.SAMPLE_AREA_IMPORTANCE, 0.0005, 1, 0.004)]
+    sids = [eng.add_taxel_sensor(ground, tx, m, mg, res, sm, bool(vis)) for (m, sm, res, vis, mg) in cfgs]
+    eng.set_pairs(s.g1, s.g2)
+    eng.step()
+    srf = _surfaces(eng, s, ground)
+    assert len(srf[0]["poly_offset"]) - 1 > 4 * 2048
+    for sid, (m, sm, res, vis, mg) in zip(sids, cfgs):
+        got = eng.taxel_sensor_values(sid).astype(np.float64)
+        ref = oracle.taxel_sensor(tx, m, mg, res, sm, vis, srf, values=np.zeros(len(tx)))
+        assert np.count_nonzero(ref) > 100
+        _check(got, ref, max(np.abs(ref).max(), 1e-12), (m, sm))
+    eng.close()

@@ -48,6 +48,11 @@ def test_parse_custom_fields(tmp_path):
     assert [int(g[1]) for g in geoms] == [0, 1, 2, 4]
     assert [float(x) for x in geoms[0][3:]] == [2e5, 1.0, 0.006, 0.5, 0.5]
     assert [ln for ln in out if ln[0] == "repr2"][0][1] == "1"
+    # taxels of a mesh geom with a local pose (p0, 90 degrees about z) move by
+    # the inverse pose: R^T (t - p0) (taxel_sensor.cpp:121-147)
+    inv = np.array([float(x) for x in [ln for ln in out if ln[0] == "invpose"][0][1:]])
+    np.testing.assert_allclose(inv, [2.2, -0.9, 2.7, 0, 0, 0], atol=1e-12)
+    assert [ln for ln in out if ln[0] == "identity"][0][1:] == ["1", "2", "3"]
 
 
 @pytest.mark.gpu
@@ -57,6 +62,9 @@ def test_plugin_cycle_matches_engine(gpu, tmp_path):
     assert [ln[3] for ln in steps] == ["1", "1", "1"]            # step ok
     assert [ln[5] for ln in steps] == ["4", "4", "4"]            # two surface pairs x 2 bodies
     assert [ln[7] for ln in steps] == ["1", "1", "2"]            # 50 Hz sensor at t = 0, 0.01, 0.02
+    assert [ln[9:11] for ln in steps] == [["1", "1"], ["1", "1"], ["2", "2"]]  # 50 Hz taxel sensors
+    tv = np.array([float(x) for x in [ln for ln in out if ln[0] == "taxel_values"][0][1:]], np.float32)
+    cv = np.array([float(x) for x in [ln for ln in out if ln[0] == "closest_values"][0][1:]], np.float32)
     counts = [ln for ln in out if ln[0] == "counts"][0]
     assert counts == ["counts", "default", "6", "surface", "6"]
     w = np.array([[float(x) for x in ln[2:]] for ln in out if ln[0] == "wrench"])
@@ -72,6 +80,9 @@ def test_plugin_cycle_matches_engine(gpu, tmp_path):
     eng.add_geom(2, L.GEOM_PLANE, [0, 0, 1], [0, 1.0, 0, 0.6, 0.6])
     eng.add_geom(4, L.GEOM_BOX, [0.02, 0.02, 0.02], [1e5, 0.5, 0.01, 0.3, 0.3])
     eng.add_flat_sensor(1, 0.005, 5, L.WINDOW_NONE, -1.0)
+    grid = [[-0.01 + 0.005 * i, -0.01 + 0.005 * j, 0.005] for i in range(5) for j in range(5)]
+    ts = eng.add_taxel_sensor(1, grid, L.TAXEL_MEAN, 0.004, 0.002, L.SAMPLE_DEFAULT, False)
+    tcl = eng.add_taxel_sensor(1, grid, L.TAXEL_CLOSEST, 0.004, 0.01, L.SAMPLE_AREA_IMPORTANCE, True)
     eng.set_pairs([1, 4], [0, 2])
     xpos = np.zeros((5, 3))
     xpos[0] = [0.004, -0.003, 0.005 + 0.03 - 0.002]
@@ -87,7 +98,11 @@ def test_plugin_cycle_matches_engine(gpu, tmp_path):
     we = eng.wrenches()
     _, m, n = eng.pair_order()
     te = eng.taxels(0)
+    tve, cve = eng.taxel_sensor_values(ts), eng.taxel_sensor_values(tcl)
     eng.close()
+    np.testing.assert_array_equal(tv, tve)
+    np.testing.assert_array_equal(cv, cve)
+    assert (tv > 0).sum() >= 2 and (cv > 0).sum() >= 1
     assert list(m) == [0, 2] and list(n) == [1, 4]
     assert np.array_equal(w, we)
     assert np.linalg.norm(we[0, :3]) > 0 and np.linalg.norm(we[1, :3]) > 0
