@@ -413,6 +413,11 @@ cudaError_t init_kernel_attributes() {
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(taxel_sensor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTaxelSmemBytes);
   if (e != cudaSuccess) return e;
+  // the taxel sensors' grid-count table (a pure function of the step count)
+  grid_table_kernel<<<(kTaxMaxSt + 256) / 256, 256>>>();
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
+  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(adjoint_sr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
 }
 

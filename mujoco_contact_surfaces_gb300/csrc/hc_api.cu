@@ -218,9 +218,11 @@ struct hc_context {
   DevBuf<int> tsens_pairs, tsens_enabled;
   DevBuf<float4> taxel_pos;
   DevBuf<float> taxel_val;
-  DevBuf<int> tpairs, tsort, tidx;   // taxel-sensor pairs; polygon order per record slot
+  DevBuf<int> tpairs, tpair_ai, tsort, tidx;   // taxel-sensor pairs; polygon order per record slot
   DevBuf<unsigned long long> tkey;
+  DevBuf<double> tat;                           // running fan areas (area-importance sensors)
   int n_tpairs = 0;
+  bool tsens_ai = false;
   int n_taxel_total = 0;
   DevBuf<float> rec_grad;
   DevBuf<int> item_poly_off, poly_block_sum;
@@ -409,6 +411,12 @@ hc_status ensure_recs(hc_context* c, int cap) {
     HC_CUDA(c->tkey.reserve(c->rec_cap));
     invalidate_graph(c);
   }
+  bool ai = false;
+  for (const TaxelHost& h : c->tsens_h) ai = ai || h.sample_method == HC_SAMPLE_AREA_IMPORTANCE;
+  if (ai && c->tat.n < (size_t)c->rec_cap * hc::kMaxPolyV) {
+    HC_CUDA(c->tat.reserve((size_t)c->rec_cap * hc::kMaxPolyV));
+    invalidate_graph(c);
+  }
   return ensure_rec_offsets(c);
 }
 
@@ -574,7 +582,9 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
     a.taxel_pos = c->taxel_pos.p;
     a.taxel_val = c->taxel_val.p;
     a.tpairs = c->tpairs.p;
+    a.tpair_ai = c->tpair_ai.p;
     a.n_tpairs = c->n_tpairs;
+    a.tat = c->tat.p;
     a.tsort = c->tsort.p;
     a.tkey = c->tkey.p;
     a.tidx = c->tidx.p;
@@ -1057,8 +1067,18 @@ hc_status hc_set_pairs(hc_context* c, int n_pair, const int* g1, const int* g2, 
     std::sort(up.begin(), up.end());
     up.erase(std::unique(up.begin(), up.end()), up.end());
     c->n_tpairs = (int)up.size();
-    if (up.empty()) up.push_back(0);
+    // pairs read by an area-importance sensor get their running fan areas
+    std::vector<int> uai(up.size(), 0);
+    for (size_t k = 0; k < td.size(); ++k) {
+      if (td[k].sample_method != HC_SAMPLE_AREA_IMPORTANCE) continue;
+      for (int j = 0; j < td[k].n_pairs; ++j) {
+        const int pr = tp[td[k].pair_off + j];
+        uai[std::lower_bound(up.begin(), up.end(), pr) - up.begin()] = 1;
+      }
+    }
+    if (up.empty()) { up.push_back(0); uai.push_back(0); }
     HC_CUDA(c->tpairs.upload(up, s));
+    HC_CUDA(c->tpair_ai.upload(uai, s));
     if (tp.empty()) tp.push_back(0);
     HC_CUDA(c->tsens_pairs.upload(tp, s));
     HC_CUDA(c->tsens_enabled.upload(c->tsens_enabled_h, s));

@@ -98,7 +98,9 @@ struct StepArgs {
   const float4* taxel_pos;   // geom frame
   float* taxel_val;          // values (kept between updates)
   const int* tpairs;         // the pairs any taxel sensor reads (each once)
+  const int* tpair_ai;       // per such pair: read by an area-importance sensor
   int n_tpairs;
+  double* tat;               // per record slot x kMaxPolyV: running surface area (area importance)
   int* tsort;                // per record slot of those pairs: the slot in polygon order
   unsigned long long* tkey;  // sort scratch (pairs of more than 2048 polygons)
   int* tidx;

@@ -67,7 +67,7 @@ struct TaxelSmem {
   float4 vtx[kTaxChunk][kMaxPolyV];   // polygon vertices relative to the sensor origin, pressure in w
   float4 cen[kTaxChunk];              // fan centroid relative to the origin, its pressure
   TaxelTri tri[kTaxChunk][kMaxPolyV];
-  double tarea[kTaxChunk][kMaxPolyV]; // fan triangle areas (area importance)
+  double tarea[kTaxChunk][kMaxPolyV]; // running surface area after each fan triangle (area importance)
   int nv[kTaxChunk];
   int poff[kTaxChunk + 1];            // exclusive scan of the polygons' sample counts
   int wsum[kTaxWarps];
@@ -78,7 +78,9 @@ struct TaxelSmem {
   int ws[kTaxGroup];
   int cand[kTaxGroup];                // taxels within the margin of the tile
   int ncand;
-  double area, at, ares;              // area-importance walk of the current surface
+  float fRS[9], fxo[3];               // the pair's soft frame in float, relative to the sensor origin
+  float xs_tol;                       // FP64 world-coordinate error bound of the pair
+  double area, ares;                  // area-importance walk of the current surface
 };
 constexpr size_t kTaxelSmemBytes = sizeof(TaxelSmem);
 
@@ -116,6 +118,15 @@ __device__ __forceinline__ int grid_count(int st) {
   return n;
 }
 
+// grid_count(st) for st = 0..kTaxMaxSt, filled once per device.
+__device__ int g_grid_tab[kTaxMaxSt + 1];
+
+__global__ void grid_table_kernel() {
+  const int st = blockIdx.x * blockDim.x + threadIdx.x;
+  if (st >= 1 && st <= kTaxMaxSt) g_grid_tab[st] = grid_count(st);
+  if (st == 0) g_grid_tab[0] = 0;
+}
+
 // Park-Miller minstd_rand0 (seed 1): state after `n` draws.
 __device__ __forceinline__ unsigned long long mod31(unsigned long long p) {
   const unsigned long long M = 0x7fffffffull;
@@ -148,6 +159,55 @@ __device__ __forceinline__ void pair_slots(const StepArgs& a, const PairDev& P, 
   *e = a.item_poly_off[min(a.unit_off[P.unit_end], total_items)];
 }
 
+// Fan of one kept polygon in FP64, as the host restatement forms it: world
+// vertices, the area-weighted centroid and its pressure.  Returns false for a
+// polygon of zero signed area (no fan).
+struct FanD {
+  double w[kMaxPolyV][3];
+  double c[3], pc;
+  int nv;
+};
+
+__device__ bool fan_fp64(const StepArgs& a, const AdjPoly& R, FanD& f) {
+  const FrameDev& F = a.frames[R.pair];
+  const PairDev& P = a.pairs[R.pair];
+  const int nv = R.nv;
+  f.nv = nv;
+  for (int i = 0; i < nv; ++i) world_vertex(R, i, F, f.w[i]);
+  // world normal of the contact (out of N into M), for the signed areas
+  const double sg = P.s_is_m ? 1.0 : -1.0;
+  const double nl[3] = {R.n[0] * sg, R.n[1] * sg, R.n[2] * sg};
+  double nw[3];
+  for (int c = 0; c < 3; ++c)
+    nw[c] = dadd(dadd(dmul(F.RS[3 * c], (double)(float)nl[0]), dmul(F.RS[3 * c + 1], (double)(float)nl[1])),
+                 dmul(F.RS[3 * c + 2], (double)(float)nl[2]));
+  double A = 0, Sx[3] = {0, 0, 0}, Pp = 0;
+  for (int i = 1; i + 1 < nv; ++i) {
+    double e1[3], e2[3], cr[3];
+    for (int c = 0; c < 3; ++c) { e1[c] = dsub(f.w[i][c], f.w[0][c]); e2[c] = dsub(f.w[i + 1][c], f.w[0][c]); }
+    dcross(e1, e2, cr);
+    const double ai = dmul(0.5, dadd(dadd(dmul(cr[0], nw[0]), dmul(cr[1], nw[1])), dmul(cr[2], nw[2])));
+    A = dadd(A, ai);
+    const double a3 = __ddiv_rn(ai, 3.0);
+    for (int c = 0; c < 3; ++c) Sx[c] = dadd(Sx[c], dmul(dadd(dadd(f.w[0][c], f.w[i][c]), f.w[i + 1][c]), a3));
+    Pp = dadd(Pp, __ddiv_rn(dmul(ai, dadd(dadd((double)R.v[0][3], (double)R.v[i][3]), (double)R.v[i + 1][3])), 3.0));
+  }
+  if (A == 0) return false;
+  for (int k = 0; k < 3; ++k) f.c[k] = __ddiv_rn(Sx[k], A);
+  f.pc = __ddiv_rn(Pp, A);
+  return true;
+}
+
+// Area of fan triangle k, (v_k, v_{k+1}, c), in FP64.
+__device__ __forceinline__ double fan_area_fp64(const FanD& f, int k) {
+  const double* w0 = f.w[k];
+  const double* w1 = f.w[k + 1 == f.nv ? 0 : k + 1];
+  double e1[3], e2[3], cr[3];
+  for (int m = 0; m < 3; ++m) { e1[m] = dsub(w1[m], w0[m]); e2[m] = dsub(f.c[m], w0[m]); }
+  dcross(e1, e2, cr);
+  return dmul(0.5, sqrt(dadd(dadd(dmul(cr[0], cr[0]), dmul(cr[1], cr[1])), dmul(cr[2], cr[2]))));
+}
+
 // ---------------------------------------------------------------------------
 // Polygon order of the pairs the taxel sensors read.
 
@@ -164,6 +224,37 @@ __device__ __forceinline__ int sorted_count(const unsigned long long* key, int n
     if (m < k || (upper && m == k)) lo = mid + 1; else hi = mid;
   }
   return lo;
+}
+
+// For a pair read by an area-importance sensor: the running surface area
+// after every fan triangle, in polygon order (FP64, summed in order as the
+// reference sums it), into tat[slot * kMaxPolyV + k].  The areas are formed
+// by all threads, the running sum by one.
+__device__ void fan_prefix(const StepArgs& a, int b, int n) {
+  if (!a.tpair_ai[blockIdx.x]) return;
+  __syncthreads();   // tsort of the pair is complete
+  for (int i = threadIdx.x; i < n; i += kTaxThreads) {
+    FanD f;
+    const AdjPoly& R = a.recs[a.rec_perm[a.tsort[b + i]]];
+    const bool ok = fan_fp64(a, R, f);
+    double* dst = a.tat + (size_t)(b + i) * kMaxPolyV;
+    for (int k = 0; k < kMaxPolyV; ++k) dst[k] = (ok && k < f.nv) ? fan_area_fp64(f, k) : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double run = 0;
+    for (int i = 0; i < n; ++i) {
+      double* dst = a.tat + (size_t)(b + i) * kMaxPolyV;
+      double ar[kMaxPolyV];
+#pragma unroll
+      for (int k = 0; k < kMaxPolyV; ++k) ar[k] = dst[k];
+#pragma unroll
+      for (int k = 0; k < kMaxPolyV; ++k) {
+        if (__double_as_longlong(ar[k]) != 0) run = dadd(run, ar[k]);
+        dst[k] = run;
+      }
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kTaxThreads) taxel_order_kernel(StepArgs a) {
@@ -219,7 +310,10 @@ __global__ void __launch_bounds__(kTaxThreads) taxel_order_kernel(StepArgs a) {
     }
     __syncthreads();
   }
-  if (nch == 1) return;
+  if (nch == 1) {
+    fan_prefix(a, b, n);
+    return;
+  }
   // rank across the sorted chunks: equal keys keep the index order (chunks
   // before this one hold smaller indices, chunks after it larger ones)
   for (int i = tid; i < n; i += kTaxThreads) {
@@ -233,77 +327,131 @@ __global__ void __launch_bounds__(kTaxThreads) taxel_order_kernel(StepArgs a) {
     }
     a.tsort[b + rank] = b + a.tidx[b + i];
   }
+  fan_prefix(a, b, n);
 }
 
 // ---------------------------------------------------------------------------
 // The sensor.
 
-// Fan of one kept polygon (FP64) into chunk position q: vertices and
-// centroid relative to the sensor origin o, and per fan triangle either the
-// default-grid sample counts (`counts`) or the area.  A polygon of zero area
-// has no fan (all counts and areas 0).
-__device__ void taxel_polygon(const StepArgs& a, const TaxelSensorDev& T, const AdjPoly& R, const double* o,
-                              TaxelSmem& S, int q, bool counts) {
-  const FrameDev& F = a.frames[R.pair];
+// Default-grid sample counts of fan triangle k from the FP64 side lengths.
+__device__ __forceinline__ TaxelTri grid_tri_fp64(const StepArgs& a, const FanD& f, int k, double res) {
+  const double* w0 = f.w[k];
+  const double* w1 = f.w[k + 1 == f.nv ? 0 : k + 1];
+  TaxelTri t;
+  t.cnt = 0; t.kb = 1; t.inc_a = t.inc_b = 0.f;
+  const double x0 = __ddiv_rn(dnorm3(w1, w0), res), x1 = __ddiv_rn(dnorm3(f.c, w0), res);
+  if (!(x0 < kTaxMaxSt) || !(x1 < kTaxMaxSt)) {
+    atomicOr(a.status, 16);   // resolution too fine for this triangle: no samples
+    return t;
+  }
+  const int st1 = (int)x1 + 1, st = max((int)x0 + 1, st1);
+  const int na = g_grid_tab[st], nb = g_grid_tab[st1];
+  t.kb = nb;
+  t.inc_a = 1.f / (float)st;
+  t.inc_b = 1.f / (float)st1;
+  t.cnt = min(na * nb, kTaxMaxTriSamples);
+  if (na * nb > kTaxMaxTriSamples) atomicOr(a.status, 16);
+  return t;
+}
+
+// FP64 fan of a polygon into chunk position q (the exact path): vertices and
+// centroid relative to the sensor origin o, and with `counts` the grid
+// sample counts of its triangles.
+__device__ void taxel_polygon_fp64(const StepArgs& a, const TaxelSensorDev& T, const AdjPoly& R, const double* o,
+                                   TaxelSmem& S, int q, bool counts) {
+  FanD f;
+  const bool ok = fan_fp64(a, R, f);
+  for (int k = 0; k < kMaxPolyV; ++k) S.tri[q][k].cnt = 0;
+  S.nv[q] = f.nv;
+  if (!ok) return;
+  S.cen[q] = make_float4((float)(f.c[0] - o[0]), (float)(f.c[1] - o[1]), (float)(f.c[2] - o[2]), (float)f.pc);
+  for (int k = 0; k < f.nv; ++k)
+    S.vtx[q][k] = make_float4((float)(f.w[k][0] - o[0]), (float)(f.w[k][1] - o[1]), (float)(f.w[k][2] - o[2]),
+                              R.v[k][3]);
+  if (counts)
+    for (int k = 0; k < f.nv; ++k) S.tri[q][k] = grid_tri_fp64(a, f, k, T.res);
+}
+
+// True when the FP32 value x may lie on the other side of an integer
+// boundary than its exact value, given |x_float - x_exact| < tol.
+__device__ __forceinline__ bool near_integer(float x, float tol) {
+  const float fl = floorf(x), fr = x - fl;
+  return fr > 1.f - tol || (fl > 0.f && fr < tol);
+}
+
+// FP32 fan of a polygon into chunk position q, in the soft frame relative to
+// vertex 0, then placed relative to the sensor origin with the pair's float
+// frame (S.fRS, S.fxo).  With `counts`, the grid sample counts of its
+// triangles — unless a side length over the resolution lies within the FP32
+// error bound of an integer, a count exceeds the limits, or the signed area
+// is too small to tell from zero: then it returns false and the FP64 path
+// decides.  The bound: the vertices are the same floats the FP64 path starts
+// from; a side length taken in FP32 from them is within 3e-7 relative of the
+// exact length, the centroid offset within 2e-6 of the largest vertex offset,
+// and the FP64 path's own error is below 1e-15 of the world coordinates.
+__device__ bool taxel_polygon_f32(const StepArgs& a, const TaxelSensorDev& T, const AdjPoly& R, TaxelSmem& S, int q,
+                                  bool counts, float inv_res, float xs_scale) {
   const PairDev& P = a.pairs[R.pair];
   const int nv = R.nv;
-  double w[kMaxPolyV][3];
-  for (int i = 0; i < nv; ++i) world_vertex(R, i, F, w[i]);
-  // world normal of the contact (out of N into M), for the signed areas
-  const double sg = P.s_is_m ? 1.0 : -1.0;
-  const double nl[3] = {R.n[0] * sg, R.n[1] * sg, R.n[2] * sg};
-  double nw[3];
-  for (int c = 0; c < 3; ++c)
-    nw[c] = dadd(dadd(dmul(F.RS[3 * c], (double)(float)nl[0]), dmul(F.RS[3 * c + 1], (double)(float)nl[1])),
-                 dmul(F.RS[3 * c + 2], (double)(float)nl[2]));
-  double A = 0, Sx[3] = {0, 0, 0}, Pp = 0;
-  for (int i = 1; i + 1 < nv; ++i) {
-    double e1[3], e2[3], cr[3];
-    for (int c = 0; c < 3; ++c) { e1[c] = dsub(w[i][c], w[0][c]); e2[c] = dsub(w[i + 1][c], w[0][c]); }
-    dcross(e1, e2, cr);
-    const double ai = dmul(0.5, dadd(dadd(dmul(cr[0], nw[0]), dmul(cr[1], nw[1])), dmul(cr[2], nw[2])));
-    A = dadd(A, ai);
-    const double a3 = __ddiv_rn(ai, 3.0);
-    for (int c = 0; c < 3; ++c) Sx[c] = dadd(Sx[c], dmul(dadd(dadd(w[0][c], w[i][c]), w[i + 1][c]), a3));
-    Pp = dadd(Pp, __ddiv_rn(dmul(ai, dadd(dadd((double)R.v[0][3], (double)R.v[i][3]), (double)R.v[i + 1][3])), 3.0));
+  float p[kMaxPolyV][3];
+  for (int i = 0; i < nv; ++i) {
+    const float4 v = *reinterpret_cast<const float4*>(R.v[i]);
+    p[i][0] = R.anc[0] + v.x; p[i][1] = R.anc[1] + v.y; p[i][2] = R.anc[2] + v.z;
   }
-  for (int k = 0; k < kMaxPolyV; ++k) {
-    S.tri[q][k].cnt = 0;
-    S.tarea[q][k] = 0;
+  const float sg = P.s_is_m ? 1.f : -1.f;
+  const float nl[3] = {R.n[0] * sg, R.n[1] * sg, R.n[2] * sg};
+  float A = 0.f, co[3] = {0.f, 0.f, 0.f}, Pp = 0.f, maxd = 0.f;
+  for (int i = 1; i + 1 < nv; ++i) {
+    const float d1[3] = {p[i][0] - p[0][0], p[i][1] - p[0][1], p[i][2] - p[0][2]};
+    const float d2[3] = {p[i + 1][0] - p[0][0], p[i + 1][1] - p[0][1], p[i + 1][2] - p[0][2]};
+    const float cr[3] = {d1[1] * d2[2] - d1[2] * d2[1], d1[2] * d2[0] - d1[0] * d2[2], d1[0] * d2[1] - d1[1] * d2[0]};
+    const float ai = 0.5f * (cr[0] * nl[0] + cr[1] * nl[1] + cr[2] * nl[2]);
+    A += ai;
+    for (int c = 0; c < 3; ++c) co[c] += (d1[c] + d2[c]) * ai;
+    Pp += ai * (R.v[0][3] + R.v[i][3] + R.v[i + 1][3]);
+    maxd = fmaxf(maxd, fmaxf(fabsf(d1[0]) + fabsf(d1[1]) + fabsf(d1[2]), fabsf(d2[0]) + fabsf(d2[1]) + fabsf(d2[2])));
   }
   S.nv[q] = nv;
-  if (A == 0) return;
-  double c[3];
-  for (int k = 0; k < 3; ++k) c[k] = __ddiv_rn(Sx[k], A);
-  const double pc = __ddiv_rn(Pp, A);
-  S.cen[q] = make_float4((float)(c[0] - o[0]), (float)(c[1] - o[1]), (float)(c[2] - o[2]), (float)pc);
-  for (int k = 0; k < nv; ++k)
-    S.vtx[q][k] = make_float4((float)(w[k][0] - o[0]), (float)(w[k][1] - o[1]), (float)(w[k][2] - o[2]), R.v[k][3]);
+  if (!(fabsf(A) > 1e-5f * maxd * maxd)) return false;
+  const float inv3A = 1.f / (3.f * A);
+  for (int c = 0; c < 3; ++c) co[c] *= inv3A;
+  const float pc = Pp * inv3A;
   for (int k = 0; k < nv; ++k) {
-    const double* w0 = w[k];
-    const double* w1 = w[k + 1 == nv ? 0 : k + 1];
-    if (counts) {
-      const double x0 = __ddiv_rn(dnorm3(w1, w0), T.res), x1 = __ddiv_rn(dnorm3(c, w0), T.res);
-      if (!(x0 < kTaxMaxSt) || !(x1 < kTaxMaxSt)) {
-        atomicOr(a.status, 16);   // resolution too fine for this triangle: no samples
-        continue;
-      }
-      const int st1 = (int)x1 + 1, st = max((int)x0 + 1, st1);
-      const int na = grid_count(st), nb = grid_count(st1);
-      TaxelTri t;
-      t.kb = nb;
-      t.inc_a = (float)__ddiv_rn(1.0, (double)st);
-      t.inc_b = (float)__ddiv_rn(1.0, (double)st1);
-      t.cnt = min(na * nb, kTaxMaxTriSamples);
-      if (na * nb > kTaxMaxTriSamples) atomicOr(a.status, 16);
-      S.tri[q][k] = t;
-    } else {
-      double e1[3], e2[3], cr[3];
-      for (int m = 0; m < 3; ++m) { e1[m] = dsub(w1[m], w0[m]); e2[m] = dsub(c[m], w0[m]); }
-      dcross(e1, e2, cr);
-      S.tarea[q][k] = dmul(0.5, sqrt(dadd(dadd(dmul(cr[0], cr[0]), dmul(cr[1], cr[1])), dmul(cr[2], cr[2]))));
-    }
+    float w[3];
+    for (int r = 0; r < 3; ++r) w[r] = S.fRS[3 * r] * p[k][0] + S.fRS[3 * r + 1] * p[k][1] + S.fRS[3 * r + 2] * p[k][2] + S.fxo[r];
+    S.vtx[q][k] = make_float4(w[0], w[1], w[2], R.v[k][3]);
   }
+  {
+    const float c[3] = {p[0][0] + co[0], p[0][1] + co[1], p[0][2] + co[2]};
+    float w[3];
+    for (int r = 0; r < 3; ++r) w[r] = S.fRS[3 * r] * c[0] + S.fRS[3 * r + 1] * c[1] + S.fRS[3 * r + 2] * c[2] + S.fxo[r];
+    S.cen[q] = make_float4(w[0], w[1], w[2], pc);
+  }
+  if (!counts) return true;
+  const float abs_tol = (4e-6f * maxd + xs_scale) * inv_res + 1e-6f;
+  TaxelTri tt[kMaxPolyV];
+  for (int k = 0; k < nv; ++k) {
+    const int j = k + 1 == nv ? 0 : k + 1;
+    const float e[3] = {p[j][0] - p[k][0], p[j][1] - p[k][1], p[j][2] - p[k][2]};
+    const float dk[3] = {p[k][0] - p[0][0], p[k][1] - p[0][1], p[k][2] - p[0][2]};
+    const float ce[3] = {co[0] - dk[0], co[1] - dk[1], co[2] - dk[2]};
+    const float x0 = sqrtf(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) * inv_res;
+    const float x1 = sqrtf(ce[0] * ce[0] + ce[1] * ce[1] + ce[2] * ce[2]) * inv_res;
+    if (!(x0 < kTaxMaxSt - 2) || !(x1 < kTaxMaxSt - 2)) return false;
+    if (near_integer(x0, 1e-6f * x0 + abs_tol) || near_integer(x1, 1e-6f * x1 + abs_tol)) return false;
+    const int st1 = (int)x1 + 1, st = max((int)x0 + 1, st1);
+    const int na = g_grid_tab[st], nb = g_grid_tab[st1];
+    if (na * nb > kTaxMaxTriSamples) return false;
+    tt[k].cnt = na * nb;
+    tt[k].kb = nb;
+    tt[k].inc_a = 1.f / (float)st;
+    tt[k].inc_b = 1.f / (float)st1;
+  }
+  for (int k = 0; k < kMaxPolyV; ++k) {
+    if (k < nv) S.tri[q][k] = tt[k];
+    else S.tri[q][k].cnt = 0;
+  }
+  return true;
 }
 
 // Squared distance from taxel t to a box stored as (min, -max).
@@ -351,6 +499,7 @@ __global__ void __launch_bounds__(kTaxThreads, 3) taxel_sensor_kernel(StepArgs a
   const float margin = (float)T.margin;
   const float r2 = margin * margin;
   const float r2_cull = r2 * 1.0001f;
+  const float inv_res = (float)(1.0 / T.res);
 
   for (int tbase = 0; tbase < T.n_taxels; tbase += kTaxGroup) {
     const int ng = min(kTaxGroup, T.n_taxels - tbase);
@@ -366,52 +515,58 @@ __global__ void __launch_bounds__(kTaxThreads, 3) taxel_sensor_kernel(StepArgs a
     }
     long long g_base = 0;   // samples so far (the area-importance draws follow it)
     for (int k = 0; k < T.n_pairs; ++k) {
-      const PairDev& P = a.pairs[a.tsens_pairs[T.pair_off + k]];
+      const int pair = a.tsens_pairs[T.pair_off + k];
       int b, e;
-      pair_slots(a, P, total_items, &b, &e);
+      pair_slots(a, a.pairs[pair], total_items, &b, &e);
       if (e <= b) continue;
-      if (area_imp) {
-        // the surface's total area, summed in order
-        double total = 0;
-        for (int c0 = b; c0 < e; c0 += kTaxChunk) {
-          const int nq = min(kTaxChunk, e - c0);
-          if (tid < nq) taxel_polygon(a, T, a.recs[a.rec_perm[a.tsort[c0 + tid]]], o, S, tid, false);
-          __syncthreads();
-          if (tid == 0)
-            for (int q = 0; q < nq; ++q)
-              for (int t = 0; t < kMaxPolyV; ++t) total = dadd(total, S.tarea[q][t]);
-          __syncthreads();
+      if (tid == 0) {
+        const FrameDev& F = a.frames[pair];
+        for (int i = 0; i < 9; ++i) S.fRS[i] = (float)F.RS[i];
+        double xm = 0;
+        for (int r = 0; r < 3; ++r) {
+          S.fxo[r] = (float)(F.xS[r] - o[r]);
+          xm = fmax(xm, fabs(F.xS[r]));
         }
-        if (tid == 0) {
-          S.ares = dmul(T.res, total);
+        S.xs_tol = 1e-14f * ((float)xm + 1.f);
+        if (area_imp) {
+          // one sample per res * (the surface's total area) of running area
+          S.ares = dmul(T.res, a.tat[(size_t)(e - 1) * kMaxPolyV + kMaxPolyV - 1]);
           S.area = 0;
-          S.at = 0;
         }
-        __syncthreads();
       }
+      __syncthreads();
+      const float xs_tol = S.xs_tol;
       for (int c0 = b; c0 < e; c0 += kTaxChunk) {
         const int nq = min(kTaxChunk, e - c0);
-        if (tid < nq) taxel_polygon(a, T, a.recs[a.rec_perm[a.tsort[c0 + tid]]], o, S, tid, !area_imp);
+        if (tid < nq) {
+          const AdjPoly& R = a.recs[a.rec_perm[a.tsort[c0 + tid]]];
+          if (!taxel_polygon_f32(a, T, R, S, tid, !area_imp, inv_res, xs_tol))
+            taxel_polygon_fp64(a, T, R, o, S, tid, !area_imp);
+          if (area_imp)
+            for (int t = 0; t < kMaxPolyV; ++t) S.tarea[tid][t] = a.tat[(size_t)(c0 + tid) * kMaxPolyV + t];
+        }
         __syncthreads();
         if (area_imp && tid == 0) {
-          // one sample per area step of running area (missing and zero-area
-          // triangles add no area and take no sample)
-          double area = S.area, at = S.at;
+          // the walk: fan triangle t takes a sample while the running sample
+          // area is below the running surface area after t
+          double area = S.area;
           const double ares = S.ares;
           for (int q = 0; q < nq; ++q) {
+            const int nv = S.nv[q];
             for (int t = 0; t < kMaxPolyV; ++t) {
-              at = dadd(at, S.tarea[q][t]);
               int cnt = 0;
-              while (area < at && cnt < kTaxMaxTriSamples) {
-                area = dadd(area, ares);
-                ++cnt;
+              if (t < nv) {
+                const double at = S.tarea[q][t];
+                while (area < at && cnt < kTaxMaxTriSamples) {
+                  area = dadd(area, ares);
+                  ++cnt;
+                }
+                if (area < at) atomicOr(a.status, 16);
               }
-              if (area < at) atomicOr(a.status, 16);
               S.tri[q][t].cnt = cnt;
             }
           }
           S.area = area;
-          S.at = at;
         }
         __syncthreads();
         chunk_scan(S, tid, nq);
