@@ -305,6 +305,42 @@ HC_API hc_status hc_get_taxel_sensor_values(hc_context* ctx, int sensor, float* 
  * must hold the total taxel count).  Synchronises the context stream.      */
 HC_API hc_status hc_get_all_taxel_sensor_values(hc_context* ctx, float* out, size_t capacity);
 
+/* ---- curved sensor ------------------------------------------------------
+ * Replaces CurvedSensor::load / internal_update (mujoco_contact_surface_
+ * sensors/src/curved_sensor.cpp:111-365, 367-466).
+ *
+ * hc_sample_surface: blue-noise points on a triangle mesh (n_vert x 3
+ * doubles, n_face x 3 indices, counter-clockwise outward), with the unit
+ * normal of each point's triangle — the load-time surface sampling, which
+ * the reference does with vcglib's Poisson-disk sampler (:260-268; not
+ * reproduced: the points differ, their spacing is alike).  At most
+ * `n_samples` points (the reference asks for (int)sample_resolution *
+ * area); deterministic for a `seed`.  *out_n receives the count; the
+ * outputs (capacity x 3 doubles each) must hold it.  Needs no context.      */
+HC_API hc_status hc_sample_surface(int n_vert, const double* vert, int n_face, const int* face, int n_samples,
+                                   uint64_t seed, int capacity, double* out_points, double* out_normals,
+                                   int* out_n);
+/* A curved sensor on geom_id: n_taxels points fixed in the geom's frame
+ * (n x 3 doubles) with optional normals (NULL, or n x 3; normalised; a zero
+ * normal means none), and n_points surface points with unit normals (geom
+ * frame; e.g. from hc_sample_surface).  As the reference: surface point j
+ * serves taxel i when their squared distance is below include_margin^2 and
+ * (the taxel has no normal or the normals are less than 45 degrees apart),
+ * with weight max(0, include_margin - distance)^2; each step, the ray of
+ * point j from p_j + 1e-8 n_j along -n_j takes the pressure of the nearest
+ * contact surface it meets at 0 < t < include_margin, and taxel i's value is
+ * the sum of weight x pressure over its points (0 without contact).
+ * Soft-rigid and half-space contacts.                                       */
+HC_API hc_status hc_add_curved_sensor(hc_context* ctx, int geom_id, int n_taxels, const double* taxels,
+                                      const double* taxel_normals, double include_margin, int n_points,
+                                      const double* points, const double* point_normals, int* out_sensor);
+/* Whether the next steps update the sensor (the update-rate gate); a
+ * disabled sensor keeps its values.                                          */
+HC_API hc_status hc_set_curved_sensor_enabled(hc_context* ctx, int sensor, int on);
+/* The sensor's values after the last step (n_taxels floats, taxel order).
+ * Synchronises the context stream.                                          */
+HC_API hc_status hc_get_curved_sensor_values(hc_context* ctx, int sensor, float* out);
+
 /* ---- adjoint -------------------------------------------------------------
  * Gradient of L with respect to both geoms' 6-DoF poses (twist
  * [dtheta; dx], world frame, applied as X <- exp(dtheta) X, x <- x + dx)

@@ -115,6 +115,10 @@ SIGNATURES = {
     "hc_set_taxel_sensor_enabled": (C.c_int, [_P, C.c_int, C.c_int]),
     "hc_get_taxel_sensor_values": (C.c_int, [_P, C.c_int, _fp]),
     "hc_get_all_taxel_sensor_values": (C.c_int, [_P, _fp, C.c_size_t]),
+    "hc_sample_surface": (C.c_int, [C.c_int, _dp, C.c_int, _ip, C.c_int, C.c_uint64, C.c_int, _dp, _dp, _ip]),
+    "hc_add_curved_sensor": (C.c_int, [_P, C.c_int, C.c_int, _dp, _dp, C.c_double, C.c_int, _dp, _dp, _ip]),
+    "hc_set_curved_sensor_enabled": (C.c_int, [_P, C.c_int, C.c_int]),
+    "hc_get_curved_sensor_values": (C.c_int, [_P, C.c_int, _fp]),
 }
 
 _lib = None
@@ -159,6 +163,21 @@ def iptr(a: np.ndarray):
 
 def fptr(a: np.ndarray):
     return a.ctypes.data_as(_fp) if a is not None else None
+
+
+def sample_surface(mesh_vert, mesh_face, n_samples: int, seed: int = 42):
+    """Blue-noise points on a triangle mesh with their triangles' unit
+    normals (hc_sample_surface; host only).  Returns (points, normals)."""
+    lib = load()
+    v = np.ascontiguousarray(mesh_vert, dtype=np.float64).reshape(-1, 3)
+    f = np.ascontiguousarray(mesh_face, dtype=np.int32).reshape(-1, 3)
+    cap = max(1, int(n_samples))
+    pts = np.zeros((cap, 3))
+    nrm = np.zeros((cap, 3))
+    n = C.c_int()
+    check(lib.hc_sample_surface(v.shape[0], dptr(v), f.shape[0], iptr(f), int(n_samples), int(seed), cap, dptr(pts),
+                                dptr(nrm), C.byref(n)))
+    return pts[:n.value].copy(), nrm[:n.value].copy()
 
 
 def generate_mesh(gtype: int, size, cs5, mesh_vert=None, mesh_face=None):

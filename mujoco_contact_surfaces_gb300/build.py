@@ -19,7 +19,7 @@ LIB = os.path.join(BUILD, "libhc.so")
 
 SOURCES = ["contact.cu", "hc_api.cu", "noalloc.cu", "meshgen.cpp"]
 HEADERS = ["clip.cuh", "geom_math.cuh", "narrow.cuh", "adjoint.cuh", "hc_internal.h", "kernels.h", "meshgen.h",
-           "noalloc.h", "taxel_sensor.cuh"]
+           "noalloc.h", "taxel_sensor.cuh", "curved_sensor.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

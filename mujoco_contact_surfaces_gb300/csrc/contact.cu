@@ -313,6 +313,7 @@ __global__ void bp_emit_kernel(StepArgs a) {
 #include "narrow.cuh"
 #include "adjoint.cuh"
 #include "taxel_sensor.cuh"
+#include "curved_sensor.cuh"
 
 // ---------------------------------------------------------------------------
 // per-pair reduction (fixed order, FP64) and the world-frame wrench
@@ -482,6 +483,9 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
         taxel_order_kernel<<<a.n_tpairs, kTaxThreads, 0, s>>>(a); ++n;
       }
       taxel_sensor_kernel<<<a.n_tsens, kTaxThreads, kTaxelSmemBytes, s>>>(a); ++n;
+    }
+    if (a.n_csens > 0) {
+      curved_sensor_kernel<<<a.n_csens, kCurvThreads, 0, s>>>(a); ++n;
     }
   }
   if (ev) cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal);

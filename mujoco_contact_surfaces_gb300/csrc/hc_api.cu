@@ -79,6 +79,15 @@ struct TaxelHost {
   std::vector<float4> taxels;   // geom frame
 };
 
+struct CurvedHost {
+  int geom;
+  double margin;
+  int n_taxels;
+  std::vector<float4> points, normals;   // the surface points some taxel uses (geom frame)
+  std::vector<int> off, pt;              // per taxel: its points (local index) in point order
+  std::vector<float> w;                  // and their weights
+};
+
 struct SensorHost {
   int geom;
   double resolution;
@@ -222,6 +231,13 @@ struct hc_context {
   DevBuf<unsigned long long> tkey;
   DevBuf<double> tat;                           // running fan areas (area-importance sensors)
   int n_tpairs = 0;
+  // curved sensors
+  std::vector<CurvedHost> csens_h;
+  std::vector<int> csens_enabled_h;
+  DevBuf<hc::CurvedSensorDev> csens;
+  DevBuf<int> csens_pairs, csens_enabled, clist_off, clist_pt;
+  DevBuf<float4> cpoints, cnormals;
+  DevBuf<float> clist_w, chit, cvalues;
   bool tsens_ai = false;
   int n_taxel_total = 0;
   DevBuf<float> rec_grad;
@@ -377,6 +393,12 @@ hc_status ensure_items(hc_context* c, int cap) {
 
 // Capacity of the polygon records (kept by steps with sensors or in adjoint
 // mode).
+// Polygons are kept as records (rays cast and sensors sampled from them, the
+// adjoint reads them) in adjoint mode and whenever sensors are attached.
+bool keeps_polygons(const hc_context* c) {
+  return c->adjoint_mode || c->n_cells > 0 || !c->tsens_h.empty() || !c->csens_h.empty();
+}
+
 int initial_rec_cap(const hc_context* c) {
   return c->cfg.face_capacity > 0 ? (int)std::min<int64_t>(c->cfg.face_capacity, 1 << 30)
                                   : std::max(1 << 15, 4 * c->item_cap);
@@ -565,7 +587,7 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
   a.rec_count = c->counters.p + kCntRec;
   // polygons are kept as records (rays cast and taxels sampled from them,
   // the adjoint reads them) in adjoint mode and whenever sensors are attached
-  if ((c->adjoint_mode || c->n_cells > 0 || !c->tsens_h.empty()) && c->rec_cap > 0) {
+  if (keeps_polygons(c) && c->rec_cap > 0) {
     a.recs = c->recs.p;
     a.rec_key = c->rec_key.p;
     a.rec_cap = c->rec_cap;
@@ -585,6 +607,17 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
     a.tpair_ai = c->tpair_ai.p;
     a.n_tpairs = c->n_tpairs;
     a.tat = c->tat.p;
+    a.csens = c->csens.p;
+    a.n_csens = (int)c->csens_h.size();
+    a.csens_pairs = c->csens_pairs.p;
+    a.csens_enabled = c->csens_enabled.p;
+    a.cpoints = c->cpoints.p;
+    a.cnormals = c->cnormals.p;
+    a.clist_off = c->clist_off.p;
+    a.clist_pt = c->clist_pt.p;
+    a.clist_w = c->clist_w.p;
+    a.chit = c->chit.p;
+    a.cvalues = c->cvalues.p;
     a.tsort = c->tsort.p;
     a.tkey = c->tkey.p;
     a.tidx = c->tidx.p;
@@ -1035,8 +1068,53 @@ hc_status hc_set_pairs(hc_context* c, int n_pair, const int* g1, const int* g2, 
   HC_CUDA(c->block_sum.reserve(c->n_bp_blocks));
   int want = c->cfg.item_capacity > 0 ? (int)c->cfg.item_capacity : std::max(1 << 16, 64 * n_pair);
   if (hc_status st = ensure_items(c, want)) return st;
-  if (c->n_cells > 0 || c->adjoint_mode || !c->tsens_h.empty())
+  if (keeps_polygons(c))
     if (hc_status st = ensure_recs(c, initial_rec_cap(c))) return st;
+  // curved sensors: the soft-rigid and half-space pairs of each sensor geom
+  if (!c->csens_h.empty()) {
+    std::vector<hc::CurvedSensorDev> cd;
+    std::vector<int> cp, loff(1, 0), lpt;
+    std::vector<float4> pts, nrm;
+    std::vector<float> lw;
+    for (const CurvedHost& h : c->csens_h) {
+      hc::CurvedSensorDev d;
+      d.geom = h.geom;
+      d.n_taxels = h.n_taxels;
+      d.taxel_off = (int)loff.size() - 1;
+      d.n_points = (int)h.points.size();
+      d.point_off = (int)pts.size();
+      d.margin = (float)h.margin;
+      d.pair_off = (int)cp.size();
+      for (int i = 0; i < n_pair; ++i)
+        if ((P[i].query == HC_QUERY_SOFT_RIGID || P[i].query == HC_QUERY_SOFT_HALFSPACE) &&
+            (g1[i] == h.geom || g2[i] == h.geom))
+          cp.push_back(i);
+      d.n_pairs = (int)cp.size() - d.pair_off;
+      const int base = loff.back();
+      for (int i = 0; i < h.n_taxels; ++i) loff.push_back(base + h.off[(size_t)i + 1]);
+      lpt.insert(lpt.end(), h.pt.begin(), h.pt.end());
+      lw.insert(lw.end(), h.w.begin(), h.w.end());
+      pts.insert(pts.end(), h.points.begin(), h.points.end());
+      nrm.insert(nrm.end(), h.normals.begin(), h.normals.end());
+      cd.push_back(d);
+    }
+    if (cp.empty()) cp.push_back(0);
+    if (lpt.empty()) { lpt.push_back(0); lw.push_back(0.f); }
+    if (pts.empty()) { pts.push_back(make_float4(0, 0, 0, 0)); nrm.push_back(make_float4(0, 0, 0, 0)); }
+    HC_CUDA(c->csens.upload(cd, s));
+    HC_CUDA(c->csens_pairs.upload(cp, s));
+    HC_CUDA(c->csens_enabled.upload(c->csens_enabled_h, s));
+    HC_CUDA(c->clist_off.upload(loff, s));
+    HC_CUDA(c->clist_pt.upload(lpt, s));
+    HC_CUDA(c->clist_w.upload(lw, s));
+    HC_CUDA(c->cpoints.upload(pts, s));
+    HC_CUDA(c->cnormals.upload(nrm, s));
+    HC_CUDA(c->chit.reserve(pts.size()));
+    if (c->cvalues.n < (size_t)loff.size() - 1 || c->cvalues.p == nullptr) {
+      HC_CUDA(c->cvalues.reserve(std::max<size_t>(1, loff.size() - 1)));
+      HC_CUDA(cudaMemsetAsync(c->cvalues.p, 0, c->cvalues.n * sizeof(float), s));
+    }
+  }
   // taxel-point sensors: the soft-rigid and half-space pairs of each sensor
   // geom, in pair order
   if (!c->tsens_h.empty()) {
@@ -1323,6 +1401,124 @@ hc_status hc_get_all_taxel_sensor_values(hc_context* c, float* out, size_t capac
                                  "triangle side, 2^20 samples per fan triangle): the sample resolution is too fine");
   if (c->taxel_val.n < total) return fail(HC_ERR_NOT_READY, "taxel sensors not set up (call hc_set_pairs)");
   HC_CUDA(cudaMemcpy(out, c->taxel_val.p, total * sizeof(float), cudaMemcpyDeviceToHost));
+  return HC_OK;
+}
+
+hc_status hc_sample_surface(int n_vert, const double* vert, int n_face, const int* face, int n_samples,
+                            uint64_t seed, int capacity, double* out_points, double* out_normals, int* out_n) {
+  if (n_vert <= 0 || n_face <= 0 || !vert || !face || n_samples < 0 || !out_n)
+    return fail(HC_ERR_INVALID_ARG, "a mesh with vertices and faces and an output count are needed");
+  if (!finite_all(vert, 3 * (size_t)n_vert)) return fail(HC_ERR_INVALID_ARG, "non-finite mesh vertex");
+  for (int i = 0; i < 3 * n_face; ++i)
+    if (face[i] < 0 || face[i] >= n_vert) return fail(HC_ERR_INVALID_ARG, "face index out of range");
+  std::vector<double> p, n;
+  const int got = hc::sample_surface(vert, n_vert, face, n_face, std::min(n_samples, 1 << 22), seed, &p, &n, nullptr);
+  *out_n = got;
+  if (got > capacity || (got > 0 && (!out_points || !out_normals)))
+    return fail(HC_ERR_INVALID_ARG, "output capacity smaller than the sample count (see out_n)");
+  if (got > 0) {
+    std::copy(p.begin(), p.end(), out_points);
+    std::copy(n.begin(), n.end(), out_normals);
+  }
+  return HC_OK;
+}
+
+hc_status hc_add_curved_sensor(hc_context* c, int geom_id, int n_taxels, const double* taxels,
+                               const double* taxel_normals, double include_margin, int n_points,
+                               const double* points, const double* point_normals, int* out_sensor) {
+  if (hc_status st = need(c)) return st;
+  if (!c->geoms.count(geom_id)) return fail(HC_ERR_INVALID_ARG, "sensor geom has no cs:: properties");
+  if (n_taxels <= 0 || n_taxels > (1 << 20) || !taxels) return fail(HC_ERR_INVALID_ARG, "1 to 2^20 taxels are needed");
+  if (n_points < 0 || n_points > (1 << 24) || (n_points > 0 && (!points || !point_normals)))
+    return fail(HC_ERR_INVALID_ARG, "0 to 2^24 surface points with normals are needed");
+  if (!(include_margin > 0) || !std::isfinite(include_margin) || !finite_all(taxels, 3 * (size_t)n_taxels) ||
+      (taxel_normals && !finite_all(taxel_normals, 3 * (size_t)n_taxels)) ||
+      (n_points > 0 && (!finite_all(points, 3 * (size_t)n_points) || !finite_all(point_normals, 3 * (size_t)n_points))))
+    return fail(HC_ERR_INVALID_ARG, "bad margin, taxel, normal or surface point");
+  // the taxels' normals, normalised (curved_sensor.cpp:174-189); none = zero
+  std::vector<double> tn(3 * (size_t)n_taxels, 0.0);
+  if (taxel_normals)
+    for (int i = 0; i < n_taxels; ++i) {
+      const double* v = taxel_normals + 3 * (size_t)i;
+      const double z = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+      for (int k = 0; k < 3; ++k) tn[3 * (size_t)i + k] = z > 0 ? v[k] / std::sqrt(z) : 0.0;
+    }
+  // points near each taxel (curved_sensor.cpp:318-347): the distance-matrix
+  // expression, the margin, the 45-degree normal test; weights
+  // max(0, margin - d)^2; points kept in order of first use
+  const double m2 = include_margin * include_margin, lim = 45 * 3.141592653589793 / 180.;
+  std::vector<std::vector<std::pair<int, float>>> lists((size_t)n_taxels);
+  std::vector<int> used;
+  for (int j = 0; j < n_points; ++j) {
+    const double* s = points + 3 * (size_t)j;
+    const double* sn = point_normals + 3 * (size_t)j;
+    const double ss = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
+    bool added = false;
+    for (int i = 0; i < n_taxels; ++i) {
+      const double* t = taxels + 3 * (size_t)i;
+      const double tt = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
+      const double d = (-2 * (t[0] * s[0] + t[1] * s[1] + t[2] * s[2]) + tt) + ss;
+      if (!(d < m2)) continue;
+      const double* nt = &tn[3 * (size_t)i];
+      if (nt[0] * nt[0] + nt[1] * nt[1] + nt[2] * nt[2] != 0 &&
+          !(std::acos(nt[0] * sn[0] + nt[1] * sn[1] + nt[2] * sn[2]) < lim))
+        continue;
+      if (!added) {
+        used.push_back(j);
+        added = true;
+      }
+      const double r = include_margin - std::sqrt(d);
+      lists[(size_t)i].push_back({(int)used.size() - 1, (float)(r > 0 ? r * r : 0.0)});
+    }
+  }
+  CurvedHost h;
+  h.geom = geom_id;
+  h.margin = include_margin;
+  h.n_taxels = n_taxels;
+  for (int j : used) {
+    const double* s = points + 3 * (size_t)j;
+    const double* sn = point_normals + 3 * (size_t)j;
+    h.points.push_back(make_float4((float)s[0], (float)s[1], (float)s[2], 0.f));
+    h.normals.push_back(make_float4((float)sn[0], (float)sn[1], (float)sn[2], 0.f));
+  }
+  h.off.push_back(0);
+  for (const auto& l : lists) {
+    for (const auto& e : l) {
+      h.pt.push_back(e.first);
+      h.w.push_back(e.second);
+    }
+    h.off.push_back((int)h.pt.size());
+  }
+  c->csens_h.push_back(std::move(h));
+  c->csens_enabled_h.push_back(1);
+  c->sensors_dirty = true;   // pairs are dispatched again before the next step
+  if (out_sensor) *out_sensor = (int)c->csens_h.size() - 1;
+  return HC_OK;
+}
+
+hc_status hc_set_curved_sensor_enabled(hc_context* c, int sensor, int on) {
+  if (hc_status st = need(c)) return st;
+  if (sensor < 0 || sensor >= (int)c->csens_h.size()) return fail(HC_ERR_INVALID_ARG, "bad curved sensor");
+  c->csens_enabled_h[sensor] = on ? 1 : 0;
+  if (c->csens_enabled.n >= c->csens_enabled_h.size()) {
+    HC_CUDA(cudaSetDevice(c->device));
+    HC_CUDA(cudaMemcpyAsync(c->csens_enabled.p + sensor, &c->csens_enabled_h[sensor], sizeof(int),
+                            cudaMemcpyHostToDevice, c->stream));
+  }
+  return HC_OK;
+}
+
+hc_status hc_get_curved_sensor_values(hc_context* c, int sensor, float* out) {
+  if (hc_status st = need(c)) return st;
+  if (sensor < 0 || sensor >= (int)c->csens_h.size() || !out) return fail(HC_ERR_INVALID_ARG, "bad curved sensor");
+  if (!c->stepped) return fail(HC_ERR_NOT_READY, "no step has run");
+  HC_CUDA(cudaSetDevice(c->device));
+  if (hc_status st = finish_step(c)) return st;
+  int off = 0;
+  for (int k = 0; k < sensor; ++k) off += c->csens_h[k].n_taxels;
+  const size_t n = (size_t)c->csens_h[sensor].n_taxels;
+  if (c->cvalues.n < (size_t)off + n) return fail(HC_ERR_NOT_READY, "curved sensor not set up (call hc_set_pairs)");
+  HC_CUDA(cudaMemcpy(out, c->cvalues.p + off, n * sizeof(float), cudaMemcpyDeviceToHost));
   return HC_OK;
 }
 

@@ -128,6 +128,16 @@ struct TaxelSensorDev {
   double margin, res;          // as given (the sample counts use res in double)
 };
 
+// Curved sensor (device): rays from points on the geom's surface into the
+// contact surfaces; each taxel sums weight x hit pressure over its points.
+struct CurvedSensorDev {
+  int geom;
+  int n_taxels, taxel_off;     // values; per-taxel lists at list offsets [taxel_off + i]
+  int n_points, point_off;     // the points some taxel uses (geom frame) and their hit pressures
+  int pair_off, n_pairs;       // the soft-rigid and half-space pairs of the geom, in pair order
+  float margin;                // rays count hits with 0 < t < margin
+};
+
 // Forces of one kept polygon (soft frame), in the pair-ordered record slot.
 struct alignas(16) RecOut {
   float F[3], T[3], area, fn0;

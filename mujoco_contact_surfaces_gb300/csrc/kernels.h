@@ -101,6 +101,18 @@ struct StepArgs {
   const int* tpair_ai;       // per such pair: read by an area-importance sensor
   int n_tpairs;
   double* tat;               // per record slot x kMaxPolyV: running surface area (area importance)
+  // curved sensors
+  const CurvedSensorDev* csens;
+  int n_csens;
+  const int* csens_pairs;
+  const int* csens_enabled;
+  const float4* cpoints;     // geom frame
+  const float4* cnormals;    // geom frame, unit
+  const int* clist_off;      // per taxel (all curved sensors' taxels back to back) + 1
+  const int* clist_pt;       // point index within the sensor
+  const float* clist_w;      // weight
+  float* chit;               // per point: hit pressure of its ray (0: no hit)
+  float* cvalues;
   int* tsort;                // per record slot of those pairs: the slot in polygon order
   unsigned long long* tkey;  // sort scratch (pairs of more than 2048 polygons)
   int* tidx;

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <unordered_map>
 #include <utility>
 
 #include "../../include/hc/hc.h"
@@ -356,6 +357,119 @@ void round_to_float(SoftMesh* m) {
 
 void round_to_float(RigidMesh* m) {
   for (double& x : m->v) x = (double)(float)x;
+}
+
+namespace {
+
+// splitmix64: a seedable 64-bit generator (Steele, Lea and Flood 2014).
+struct Split64 {
+  uint64_t s;
+  uint64_t next() {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  }
+  double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }   // [0, 1)
+};
+
+struct Candidate {
+  double x[3];
+  int face;
+};
+
+// Greedy thinning in candidate order with a hash grid of cell size r.
+int thin(const std::vector<Candidate>& c, double r, int want, std::vector<int>* kept) {
+  kept->clear();
+  std::unordered_map<int64_t, std::vector<int>> grid;
+  const double r2 = r * r;
+  auto key = [](int64_t i, int64_t j, int64_t k) { return (i * 73856093) ^ (j * 19349663) ^ (k * 83492791); };
+  for (int idx = 0; idx < (int)c.size(); ++idx) {
+    const double* p = c[idx].x;
+    const int64_t ci = (int64_t)std::floor(p[0] / r), cj = (int64_t)std::floor(p[1] / r),
+                  ck = (int64_t)std::floor(p[2] / r);
+    bool ok = true;
+    for (int64_t di = -1; di <= 1 && ok; ++di)
+      for (int64_t dj = -1; dj <= 1 && ok; ++dj)
+        for (int64_t dk = -1; dk <= 1 && ok; ++dk) {
+          auto it = grid.find(key(ci + di, cj + dj, ck + dk));
+          if (it == grid.end()) continue;
+          for (int o : it->second) {
+            const double* q = c[o].x;
+            const double d0 = p[0] - q[0], d1 = p[1] - q[1], d2 = p[2] - q[2];
+            if (d0 * d0 + d1 * d1 + d2 * d2 < r2) { ok = false; break; }
+          }
+        }
+    if (!ok) continue;
+    grid[key(ci, cj, ck)].push_back(idx);
+    kept->push_back(idx);
+    if (want > 0 && (int)kept->size() >= want) break;
+  }
+  return (int)kept->size();
+}
+
+}  // namespace
+
+int sample_surface(const double* v, int nv, const int* f, int nf, int n, uint64_t seed, std::vector<double>* pts,
+                   std::vector<double>* nrm, double* radius) {
+  pts->clear();
+  nrm->clear();
+  if (radius) *radius = 0;
+  if (n <= 0 || nf <= 0 || nv <= 0) return 0;
+  std::vector<double> cdf((size_t)nf + 1, 0.0), fn(3 * (size_t)nf, 0.0);
+  for (int t = 0; t < nf; ++t) {
+    double a = 0;
+    const int i0 = f[3 * t], i1 = f[3 * t + 1], i2 = f[3 * t + 2];
+    if (i0 >= 0 && i1 >= 0 && i2 >= 0 && i0 < nv && i1 < nv && i2 < nv) {
+      const double* p0 = v + 3 * i0;
+      const double* p1 = v + 3 * i1;
+      const double* p2 = v + 3 * i2;
+      const double e1[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+      const double e2[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+      const double cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                            e1[0] * e2[1] - e1[1] * e2[0]};
+      const double len = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+      a = 0.5 * len;
+      if (len > 0)
+        for (int k = 0; k < 3; ++k) fn[3 * (size_t)t + k] = cr[k] / len;
+    }
+    cdf[(size_t)t + 1] = cdf[t] + a;
+  }
+  const double A = cdf[nf];
+  if (!(A > 0) || !std::isfinite(A)) return 0;
+  // candidates, uniform by area: face by the area CDF, point by the
+  // square-root warp of two uniforms
+  const int64_t n_cand = std::min<int64_t>(std::max<int64_t>(32 * (int64_t)n, 1024), 1 << 23);
+  std::vector<Candidate> cand((size_t)n_cand);
+  Split64 rng{seed};
+  for (int64_t k = 0; k < n_cand; ++k) {
+    const double u = rng.uniform() * A;
+    int t = (int)(std::upper_bound(cdf.begin(), cdf.end(), u) - cdf.begin()) - 1;
+    t = std::max(0, std::min(nf - 1, t));
+    while (t > 0 && !(cdf[(size_t)t + 1] > cdf[t])) --t;
+    const double r1 = std::sqrt(rng.uniform()), r2 = rng.uniform();
+    const double w0 = 1 - r1, w1 = r1 * (1 - r2), w2 = r1 * r2;
+    const double* p0 = v + 3 * f[3 * t];
+    const double* p1 = v + 3 * f[3 * t + 1];
+    const double* p2 = v + 3 * f[3 * t + 2];
+    for (int c = 0; c < 3; ++c) cand[(size_t)k].x[c] = w0 * p0[c] + w1 * p1[c] + w2 * p2[c];
+    cand[(size_t)k].face = t;
+  }
+  // radius: start at the spacing of a hexagonal packing of n points (an
+  // upper bound) and shrink until n points survive the thinning
+  double r = std::sqrt(2.0 * A / (std::sqrt(3.0) * n));
+  std::vector<int> kept;
+  for (int it = 0; it < 40; ++it) {
+    const int got = thin(cand, r, n, &kept);
+    if (got >= n) break;
+    r *= std::max(0.5, std::sqrt((double)std::max(got, 1) / n) * 0.98);
+  }
+  if (radius) *radius = r;
+  for (int idx : kept) {
+    for (int c = 0; c < 3; ++c) pts->push_back(cand[(size_t)idx].x[c]);
+    for (int c = 0; c < 3; ++c) nrm->push_back(fn[3 * (size_t)cand[(size_t)idx].face + c]);
+  }
+  return (int)kept.size();
 }
 
 }  // namespace hc

@@ -10,6 +10,7 @@
 // our own; the pressure field is E * extent with extent 0 on the surface and 1
 // on the deepest interior points, linear inside each tetrahedron.
 #pragma once
+#include <cstdint>
 #include <string>
 #include <vector>
 
@@ -42,5 +43,16 @@ void round_to_float(RigidMesh* m);
 
 // Signed volume of tet (a, b, c, d): (b-a).((c-a)x(d-a)) / 6.
 double tet_volume(const double* a, const double* b, const double* c, const double* d);
+
+// Blue-noise points on a triangle mesh surface, for the curved sensor (the
+// reference draws them with vcglib's Poisson-disk sampler at load,
+// curved_sensor.cpp:260-268, which is not reproduced): `n` candidates
+// spread uniformly by area are thinned greedily so that no two kept points
+// are closer than a radius, and the radius is shrunk until at least n points
+// survive; the first n are kept.  Each point carries the unit normal of its
+// triangle (outward for counter-clockwise faces).  Deterministic for a seed
+// on every host.  Returns the number of points (<= n).
+int sample_surface(const double* v, int nv, const int* f, int nf, int n, uint64_t seed, std::vector<double>* pts,
+                   std::vector<double>* nrm, double* radius);
 
 }  // namespace hc

@@ -31,6 +31,7 @@ class Engine:
         self.n_pair = 0
         self.sensors = {}   # sensor index -> (cx, cy)
         self.taxel_sensors = {}   # taxel sensor index -> number of taxels
+        self.curved_sensors = {}  # curved sensor index -> number of taxels
 
     def close(self):
         if self.ctx:
@@ -97,6 +98,29 @@ class Engine:
     def taxel_sensor_values(self, sensor: int) -> np.ndarray:
         out = np.zeros(self.taxel_sensors[sensor], np.float32)
         L.check(self.lib.hc_get_taxel_sensor_values(self.ctx, sensor, L.fptr(out)))
+        return out
+
+    def add_curved_sensor(self, geom_id: int, taxels, include_margin: float, points, point_normals,
+                          taxel_normals=None) -> int:
+        """Curved sensor (hc_add_curved_sensor): taxels and surface points
+        with unit normals in the geom frame."""
+        t = np.ascontiguousarray(taxels, np.float64).reshape(-1, 3)
+        tn = None if taxel_normals is None else np.ascontiguousarray(taxel_normals, np.float64).reshape(-1, 3)
+        p = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+        pn = np.ascontiguousarray(point_normals, np.float64).reshape(-1, 3)
+        sid = C.c_int()
+        L.check(self.lib.hc_add_curved_sensor(self.ctx, geom_id, t.shape[0], L.dptr(t), L.dptr(tn),
+                                              float(include_margin), p.shape[0], L.dptr(p), L.dptr(pn),
+                                              C.byref(sid)))
+        self.curved_sensors[sid.value] = t.shape[0]
+        return sid.value
+
+    def set_curved_sensor_enabled(self, sensor: int, on: bool = True):
+        L.check(self.lib.hc_set_curved_sensor_enabled(self.ctx, sensor, int(on)))
+
+    def curved_sensor_values(self, sensor: int) -> np.ndarray:
+        out = np.zeros(self.curved_sensors[sensor], np.float32)
+        L.check(self.lib.hc_get_curved_sensor_values(self.ctx, sensor, L.fptr(out)))
         return out
 
     def all_taxel_sensor_values(self) -> np.ndarray:

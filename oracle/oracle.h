@@ -106,6 +106,21 @@ void or_taxel_sensor(const or_taxel_cfg* cfg, int n_surf, const int* surf_poly_o
 uint64_t or_minstd_nth(int n);
 double or_uniform_nth(int n);
 
+/* Curved sensor (curved.c; CurvedSensor, mujoco_contact_surface_sensors/
+ * src/curved_sensor.cpp).  Selection at load: taxels and surface points in
+ * the geom frame (3 doubles each), taxel_normals NULL or unit vectors (zero =
+ * none), point_normals unit; per taxel i its points pt[off[i]..off[i+1]) in
+ * point order with weights w (off: n_taxels+1; pt, w: n_taxels * n_points
+ * at most).  Returns the number of (taxel, point) entries.                 */
+int or_curved_select(int n_taxels, const double* taxels, const double* taxel_normals, double margin, int n_points,
+                     const double* points, const double* point_normals, int* off, int* pt, double* w);
+/* Update: points and normals in the world frame; surfaces as for
+ * or_taxel_sensor; values: n_taxels (every value is written).               */
+void or_curved_update(int n_taxels, const int* off, const int* pt, const double* w, int n_points,
+                      const double* points, const double* normals, double margin, int n_surf,
+                      const int* surf_poly_off, const int* poly_vert_off, const double* vert, const double* vert_p,
+                      const double* normal, double* values);
+
 #ifdef __cplusplus
 }
 #endif

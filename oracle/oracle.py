@@ -17,7 +17,7 @@ LIB = os.path.join(HERE, "_build", "liboracle.so")
 
 
 def build(force: bool = False) -> str:
-    src = [os.path.join(HERE, f) for f in ("oracle.c", "taxel.c", "oracle.h", "Makefile")]
+    src = [os.path.join(HERE, f) for f in ("oracle.c", "taxel.c", "curved.c", "oracle.h", "Makefile")]
     if force or not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in src):
         r = subprocess.run(["make", "-s", "-C", HERE, "-B" if force else "-s"], capture_output=True, text=True)
         if r.returncode != 0:
@@ -81,6 +81,10 @@ def load():
         lib.or_minstd_nth.argtypes = [C.c_int]
         lib.or_uniform_nth.restype = C.c_double
         lib.or_uniform_nth.argtypes = [C.c_int]
+        lib.or_curved_select.restype = C.c_int
+        lib.or_curved_select.argtypes = [C.c_int, dp, dp, C.c_double, C.c_int, dp, dp, ip, ip, dp]
+        lib.or_curved_update.argtypes = [C.c_int, ip, ip, dp, C.c_int, dp, dp, C.c_double, C.c_int, ip, ip, dp,
+                                         dp, dp, dp]
         _lib = lib
     return _lib
 
@@ -252,4 +256,55 @@ def taxel_sensor(taxels_world, method, include_margin, sample_resolution, sample
     cfg = or_taxel_cfg(n, _dp(tx), int(method), float(include_margin), float(sample_resolution), int(sample_method),
                        int(visualize))
     lib.or_taxel_sensor(C.byref(cfg), len(surfaces), _ip(so), _ip(vo), _dp(V), _dp(P), _dp(N), _dp(out))
+    return out
+
+
+def _surface_arrays(surfaces):
+    surf_off, vert_off, verts, vps, nrms = [0], [0], [], [], []
+    for srf in surfaces:
+        po = np.asarray(srf["poly_offset"], np.int64)
+        for k in range(len(po) - 1):
+            vert_off.append(vert_off[-1] + int(po[k + 1] - po[k]))
+        surf_off.append(surf_off[-1] + len(po) - 1)
+        verts.append(np.asarray(srf["vert"], np.float64).reshape(-1, 3))
+        vps.append(np.asarray(srf["vert_pressure"], np.float64).reshape(-1))
+        nrms.append(np.asarray(srf["normal"], np.float64).reshape(-1, 3))
+    so = np.asarray(surf_off, np.int32)
+    vo = np.asarray(vert_off, np.int32)
+    V = np.ascontiguousarray(np.concatenate(verts) if verts else np.zeros((0, 3)))
+    P = np.ascontiguousarray(np.concatenate(vps) if vps else np.zeros(0))
+    N = np.ascontiguousarray(np.concatenate(nrms) if nrms else np.zeros((0, 3)))
+    return so, vo, V, P, N
+
+
+def curved_select(taxels, taxel_normals, include_margin, points, point_normals):
+    """Per-taxel surface-point lists and weights (or_curved_select), all in
+    the geom frame; returns (off, pt, w)."""
+    lib = load()
+    tx = np.ascontiguousarray(taxels, np.float64).reshape(-1, 3)
+    pts = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+    pn = np.ascontiguousarray(point_normals, np.float64).reshape(-1, 3)
+    tn = None if taxel_normals is None else np.ascontiguousarray(taxel_normals, np.float64).reshape(-1, 3)
+    n, m = tx.shape[0], pts.shape[0]
+    off = np.zeros(n + 1, np.int32)
+    pt = np.zeros(max(1, n * m), np.int32)
+    w = np.zeros(max(1, n * m))
+    k = lib.or_curved_select(n, _dp(tx), _dp(tn) if tn is not None else None, float(include_margin), m, _dp(pts),
+                             _dp(pn), _ip(off), _ip(pt), _dp(w))
+    return off, pt[:k].copy(), w[:k].copy()
+
+
+def curved_update(off, pt, w, points_world, normals_world, include_margin, surfaces):
+    """Curved-sensor values (or_curved_update) for the given lists, world
+    points and normals, on the given contact surfaces (as taxel_sensor)."""
+    lib = load()
+    off = np.ascontiguousarray(off, np.int32)
+    pt = np.ascontiguousarray(pt, np.int32)
+    w = np.ascontiguousarray(w, np.float64)
+    pts = np.ascontiguousarray(points_world, np.float64).reshape(-1, 3)
+    nrm = np.ascontiguousarray(normals_world, np.float64).reshape(-1, 3)
+    so, vo, V, P, N = _surface_arrays(surfaces)
+    out = np.zeros(len(off) - 1)
+    lib.or_curved_update(len(off) - 1, _ip(off), _ip(pt), _dp(w), pts.shape[0], _dp(pts), _dp(nrm),
+                         float(include_margin), len(surfaces), _ip(so), _ip(vo), _dp(V), _dp(P), _dp(N), _dp(out))
     return out

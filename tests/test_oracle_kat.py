@@ -195,3 +195,39 @@ def test_taxel_sensor_kat():
         assert np.array_equal(w[0], w[1]) and np.array_equal(w[1], w[2])   # fall-through
         assert w[2][0] > w[2][1] > 0 and w[2][2] == 7.0
     assert list(oracle.taxel_sensor(tx, 3, 0.002, 0.001, 0, 0, [], values=prev)) == [0.0, 0.0, 0.0]
+
+
+def test_curved_sensor_kat():
+    """Curved-sensor restatement (curved_sensor.cpp): the selection's margin,
+    weights and 45-degree normal test, and rays into a uniform-pressure
+    square below the sensor surface (t < margin counts, t >= margin not)."""
+    import oracle
+    g = np.linspace(-0.004, 0.004, 9)
+    pts = np.array([[x, y, 0.0] for x in g for y in g])
+    pn = np.tile([0.0, 0.0, 1.0], (len(pts), 1))
+    tx = np.array([[0.0, 0.0, 0.0], [0.002, 0.0, 0.0], [0.0, 0.0, 0.0], [0.1, 0.0, 0.0]])
+    tn = np.array([[0, 0, 0], [0, 0, 2.0], [1.0, 0, 1.0 / np.sqrt(3.0)], [0, 0, 0]], float)
+    tn_unit = tn / np.maximum(np.linalg.norm(tn, axis=1, keepdims=True), 1e-300)
+    margin = 0.003
+    off, pt, w = oracle.curved_select(tx, tn_unit, margin, pts, pn)
+    for i in range(len(tx)):
+        d = np.linalg.norm(pts - tx[i], axis=1)
+        cos = tn_unit[i] @ np.array([0, 0, 1.0])
+        want = np.nonzero((d < margin) & ((np.linalg.norm(tn[i]) == 0) | (np.arccos(np.clip(cos, -1, 1)) < np.pi / 4)))[0]
+        assert list(pt[off[i]:off[i + 1]]) == list(want)
+        np.testing.assert_allclose(w[off[i]:off[i + 1]], np.maximum(0, margin - d[want]) ** 2, rtol=1e-12, atol=1e-18)
+    assert off[3] - off[2] == 0 and off[4] - off[3] == 0     # 60 degrees off; out of reach
+    sq = dict(poly_offset=[0, 4], vert=[[-0.01, -0.01, -0.001], [0.01, -0.01, -0.001], [0.01, 0.01, -0.001],
+                                        [-0.01, 0.01, -0.001]], vert_pressure=[5.0] * 4, normal=[[0, 0, 1]])
+    v = oracle.curved_update(off, pt, w, pts, pn, margin, [sq])
+    for i in range(len(tx)):
+        assert v[i] == pytest.approx(5.0 * w[off[i]:off[i + 1]].sum(), rel=1e-12)
+    assert v[0] > 0 and v[1] > 0
+    # a surface deeper than the margin is not reached; no surface: zeros
+    deep = dict(sq, vert=[[x, y, -0.004] for x, y, _ in sq["vert"]])
+    assert np.all(oracle.curved_update(off, pt, w, pts, pn, margin, [deep]) == 0)
+    assert np.all(oracle.curved_update(off, pt, w, pts, pn, margin, []) == 0)
+    # the nearest of two surfaces along the ray counts
+    sq2 = dict(sq, vert=[[x, y, -0.0005] for x, y, _ in sq["vert"]], vert_pressure=[3.0] * 4)
+    v2 = oracle.curved_update(off, pt, w, pts, pn, margin, [sq, sq2])
+    assert v2[0] == pytest.approx(3.0 * w[off[0]:off[1]].sum(), rel=1e-12)
