@@ -14,6 +14,7 @@
 //   TactileSensorBase::update          mujoco_contact_surface_sensors/src/tactile_sensor_base.cpp:89-120
 //   FlatTactileSensor::load            mujoco_contact_surface_sensors/src/flat_tactile_sensor.cpp:127-214
 //   TaxelSensor::load                  mujoco_contact_surface_sensors/src/taxel_sensor.cpp:46-156
+//   CurvedSensor::load                 mujoco_contact_surface_sensors/src/curved_sensor.cpp:111-365
 //
 // The class is a template over an `Api` traits type that names the MuJoCo
 // types and the four MuJoCo calls the plugin needs, so it compiles against
@@ -294,6 +295,125 @@ class TaxelSensor : public SurfacePlugin<Api> {
   TaxelSensorConfig cfg_;
   hc_context* ctx_ = nullptr;
   int sensor_ = -1, n_updates_ = 0;
+  bool due_ = false;
+  double period_ = 0.0, last_update_ = -1e300;
+  std::vector<float> values_;
+};
+
+// Curved sensor (curved_sensor.cpp:111-365 load, 367-466 update): taxels
+// (with optional normals) on a mesh geom, valued from rays cast from points
+// sampled on the mesh surface at load (hc_sample_surface replaces vcglib's
+// Poisson-disk sampler; the reference asks it for (int)sample_resolution *
+// area points, the integer cast binding to sample_resolution, and so does
+// this class).  Mesh geoms only, as the reference.  `method` and
+// `sample_method` are checked as the reference checks them; the values do
+// not depend on them.  The update-rate gate switches the device update on
+// for the steps it reports.
+struct CurvedSensorConfig {
+  std::string sensor_name;
+  std::string geom_name;
+  double update_rate = 100.0;
+  std::vector<std::array<double, 3>> taxels;
+  std::vector<std::array<double, 3>> normals;   // empty, or up to one per taxel (missing: none)
+  std::string method = "closest";
+  double include_margin = 0.0;
+  double sample_resolution = 0.0;               // surface points per square metre
+  std::string sample_method = "default";
+  uint64_t seed = 42;
+};
+
+template <class Api>
+class CurvedSensor : public SurfacePlugin<Api> {
+ public:
+  explicit CurvedSensor(CurvedSensorConfig cfg) : cfg_(std::move(cfg)) {}
+
+  bool load(const typename Api::Model* m, typename Api::Data*, hc_context* ctx) override {
+    ctx_ = ctx;
+    const int g = Api::name2id(m, Api::kObjGeom, cfg_.geom_name.c_str());
+    if (g < 0 || cfg_.taxels.empty() || cfg_.update_rate <= 0 || cfg_.normals.size() > cfg_.taxels.size())
+      return false;
+    if (cfg_.method != "closest" && cfg_.method != "weighted" && cfg_.method != "mean" && cfg_.method != "squared")
+      return false;
+    if (cfg_.sample_method != "default" && cfg_.sample_method != "area_importance") return false;
+    if (m->geom_type[g] != HC_GEOM_MESH || m->geom_dataid[g] < 0) return false;
+    const int mesh = m->geom_dataid[g];
+    const int va = m->mesh_vertadr[mesh], vn = m->mesh_vertnum[mesh];
+    const int fa = m->mesh_faceadr[mesh], fn = m->mesh_facenum[mesh];
+    if (vn <= 0 || fn <= 0 || va < 0 || fa < 0) return false;
+    std::vector<double> mv(m->mesh_vert + 3 * (size_t)va, m->mesh_vert + 3 * (size_t)(va + vn));
+    std::vector<int> mf(m->mesh_face + 3 * (size_t)fa, m->mesh_face + 3 * (size_t)(fa + fn));
+    double area = 0;
+    for (int f = 0; f < fn; ++f) {
+      const double* a = &mv[3 * (size_t)mf[3 * (size_t)f]];
+      const double* b = &mv[3 * (size_t)mf[3 * (size_t)f + 1]];
+      const double* c = &mv[3 * (size_t)mf[3 * (size_t)f + 2]];
+      const double e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+      const double cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+      area += 0.5 * std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    }
+    const int n_samples = (int)((double)(int)cfg_.sample_resolution * area);
+    std::vector<double> pts(3 * (size_t)std::max(n_samples, 1)), nrm(pts.size());
+    int got = 0;
+    if (n_samples > 0 &&
+        hc_sample_surface(vn, mv.data(), fn, mf.data(), n_samples, cfg_.seed, n_samples, pts.data(), nrm.data(),
+                          &got) != HC_OK)
+      return false;
+    std::vector<double> t, tn(3 * cfg_.taxels.size(), 0.0);
+    for (const auto& p : cfg_.taxels) t.insert(t.end(), p.begin(), p.end());
+    for (size_t i = 0; i < cfg_.normals.size(); ++i)
+      for (int k = 0; k < 3; ++k) tn[3 * i + k] = cfg_.normals[i][k];
+    move_to_geom_frame(m, g, t, tn);
+    if (hc_add_curved_sensor(ctx, g, (int)cfg_.taxels.size(), t.data(), tn.data(), cfg_.include_margin, got,
+                             pts.data(), nrm.data(), &sensor_) != HC_OK)
+      return false;
+    n_points_ = got;
+    values_.assign(cfg_.taxels.size(), 0.f);
+    period_ = 1.0 / cfg_.update_rate;
+    last_update_ = -1e300;
+    return true;
+  }
+
+  void reset() override { last_update_ = -1e300; }
+
+  void before_step(const typename Api::Model*, typename Api::Data* d) override {
+    due_ = d->time < last_update_ || d->time - last_update_ >= period_;
+    hc_set_curved_sensor_enabled(ctx_, sensor_, due_ ? 1 : 0);
+  }
+
+  void update(const typename Api::Model*, typename Api::Data* d, const StepView&) override {
+    if (!due_) return;
+    last_update_ = d->time;
+    if (hc_get_curved_sensor_values(ctx_, sensor_, values_.data()) == HC_OK) ++n_updates_;
+  }
+
+  const std::vector<float>& values() const { return values_; }
+  const std::string& name() const { return cfg_.sensor_name; }
+  int n_updates() const { return n_updates_; }
+  int n_surface_points() const { return n_points_; }
+
+ private:
+  template <class A = Api>
+  static auto local_pose(const typename A::Model* m, int g, double p[3], double q[4])
+      -> decltype(A::kGeomLocalPose, void()) {
+    for (int k = 0; k < 3; ++k) p[k] = m->geom_pos[3 * g + k];
+    for (int k = 0; k < 4; ++k) q[k] = m->geom_quat[4 * g + k];
+  }
+  static void local_pose(...) {}
+
+  // Taxels by the inverse local pose, normals by its rotation
+  // (curved_sensor.cpp:193-226).
+  void move_to_geom_frame(const typename Api::Model* m, int g, std::vector<double>& t, std::vector<double>& tn) const {
+    double p[3] = {0, 0, 0}, q[4] = {1, 0, 0, 0};
+    local_pose(m, g, p, q);
+    apply_inverse_pose(p, q, t);
+    const double zero[3] = {0, 0, 0};
+    if (p[0] != 0 || p[1] != 0 || p[2] != 0 || q[0] != 1 || q[1] != 0 || q[2] != 0 || q[3] != 0)
+      apply_inverse_pose(zero, q, tn);
+  }
+
+  CurvedSensorConfig cfg_;
+  hc_context* ctx_ = nullptr;
+  int sensor_ = -1, n_updates_ = 0, n_points_ = 0;
   bool due_ = false;
   double period_ = 0.0, last_update_ = -1e300;
   std::vector<float> values_;

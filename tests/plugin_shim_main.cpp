@@ -41,6 +41,8 @@ struct FakeModel {
   std::vector<std::string> geom_names, numeric_names, text_names;
   std::vector<int> v_type, v_body, v_dataid, v_nadr, v_nsize, v_tadr, v_tsize;
   std::vector<double> v_size, v_ndata, v_pos, v_quat;
+  std::vector<int> v_mvadr, v_mvnum, v_mfadr, v_mfnum, v_mface;
+  std::vector<float> v_mvert;
   std::vector<char> v_tdata;
 
   int add_geom(const std::string& name, int type, double sx, double sy, double sz, int body) {
@@ -52,6 +54,18 @@ struct FakeModel {
     v_pos.insert(v_pos.end(), {0, 0, 0});
     v_quat.insert(v_quat.end(), {1, 0, 0, 0});
     return (int)geom_names.size() - 1;
+  }
+  // A mesh geom: vertices (3 floats each) and faces (3 indices each).
+  int add_mesh_geom(const std::string& name, const std::vector<float>& vert, const std::vector<int>& face, int body) {
+    const int g = add_geom(name, 7, 0, 0, 0, body);
+    v_dataid[(size_t)g] = (int)v_mvadr.size();
+    v_mvadr.push_back((int)v_mvert.size() / 3);
+    v_mvnum.push_back((int)vert.size() / 3);
+    v_mfadr.push_back((int)v_mface.size() / 3);
+    v_mfnum.push_back((int)face.size() / 3);
+    v_mvert.insert(v_mvert.end(), vert.begin(), vert.end());
+    v_mface.insert(v_mface.end(), face.begin(), face.end());
+    return g;
   }
   void add_numeric(const std::string& name, std::vector<double> vals) {
     numeric_names.push_back(name);
@@ -74,6 +88,12 @@ struct FakeModel {
     geom_dataid = v_dataid.data();
     geom_pos = v_pos.data();
     geom_quat = v_quat.data();
+    mesh_vertadr = v_mvadr.data();
+    mesh_vertnum = v_mvnum.data();
+    mesh_vert = v_mvert.data();
+    mesh_faceadr = v_mfadr.data();
+    mesh_facenum = v_mfnum.data();
+    mesh_face = v_mface.data();
     nnumeric = (int)numeric_names.size();
     numeric_adr = v_nadr.data();
     numeric_size = v_nsize.data();
@@ -165,8 +185,73 @@ static void set_pose(FakeData& d, int g, double x, double y, double z) {
   for (int k = 0; k < 9; ++k) d.xmat[9 * g + k] = (k % 4 == 0) ? 1.0 : 0.0;
 }
 
+// A soft box mesh pressed into the floor, read by a curved sensor on its
+// bottom face (50 Hz, three steps at 100 Hz).
+static int run_curved() {
+  FakeModel m;
+  m.add_geom("floor", 0, 0, 0, 1, 0);
+  const float hx = 0.02f, hy = 0.02f, hz = 0.01f;
+  std::vector<float> vert;
+  for (int sx = -1; sx <= 1; sx += 2)
+    for (int sy = -1; sy <= 1; sy += 2)
+      for (int sz = -1; sz <= 1; sz += 2) vert.insert(vert.end(), {sx * hx, sy * hy, sz * hz});
+  const std::vector<int> face = {0, 1, 3, 0, 3, 2, 4, 6, 7, 4, 7, 5, 0, 4, 5, 0, 5, 1,
+                                 2, 3, 7, 2, 7, 6, 0, 2, 6, 0, 6, 4, 1, 5, 7, 1, 7, 3};
+  const int tip = m.add_mesh_geom("tip", vert, face, 1);
+  m.add_text("cs::HydroelasticContactRepresentation", "kTriangle");
+  m.add_numeric("cs::floor", {0, 1.0, 0, 0.5, 0.5});
+  m.add_numeric("cs::tip", {1e5, 1.0, 0.004, 0.5, 0.5});
+  m.finalize();
+  FakeData d;
+  d.xpos.assign(3 * (size_t)m.ngeom, 0.0);
+  d.xmat.assign(9 * (size_t)m.ngeom, 0.0);
+  d.vel.assign(6 * (size_t)m.ngeom, 0.0);
+  d.qfrc.assign(8, 0.0);
+  d.body_wrench.assign(6 * 2, 0.0);
+  set_pose(d, 0, 0, 0, 0);
+  set_pose(d, tip, 0.001, -0.002, hz - 0.002);
+  d.geom_xpos = d.xpos.data();
+  d.geom_xmat = d.xmat.data();
+  d.qfrc_passive = d.qfrc.data();
+  Plugin plugin(0);
+  hc_plugin::CurvedSensorConfig cc;
+  cc.sensor_name = "tip_skin";
+  cc.geom_name = "tip";
+  cc.update_rate = 50.0;
+  for (int i = -1; i <= 1; ++i)
+    for (int j = -1; j <= 1; ++j) cc.taxels.push_back({0.006 * i, 0.006 * j, -hz});
+  cc.normals = {{0, 0, -1}, {0, 0, 0}, {0, 0, -3}};
+  cc.include_margin = 0.004;
+  cc.sample_resolution = 200000.7;   // the integer part counts
+  auto cs = std::make_unique<hc_plugin::CurvedSensor<FakeApi>>(cc);
+  hc_plugin::CurvedSensor<FakeApi>* cp = cs.get();
+  plugin.add_plugin(std::move(cs));
+  if (!plugin.load(&m, &d)) {
+    printf("load_failed %s\n", Plugin::last_error().c_str());
+    return 1;
+  }
+  FakeContact con[1];
+  for (int step = 0; step < 3; ++step) {
+    d.time = 0.01 * step;
+    plugin.collision_cb(&m, &d, con, tip, 0, 0.0, default_collision);
+    plugin.passiveCallback(&m, &d);
+    printf("cstep %d ok %d updates %d\n", step, plugin.last_step_ok() ? 1 : 0, cp->n_updates());
+  }
+  printf("points %d\n", cp->n_surface_points());
+  printf("curved_values");
+  for (float v : cp->values()) printf(" %.9g", v);
+  printf("\n");
+  // a primitive geom is rejected, as the reference rejects it
+  hc_plugin::CurvedSensorConfig bad = cc;
+  bad.geom_name = "floor";
+  hc_plugin::CurvedSensor<FakeApi> reject(bad);
+  printf("reject_primitive %d\n", reject.load(&m, &d, nullptr) ? 0 : 1);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   const std::string mode = argc > 1 ? argv[1] : "parse";
+  if (mode == "curved") return run_curved();
   if (mode == "parse") {
     for (int force = 0; force < 2; ++force) {
       FakeModel m;

@@ -116,3 +116,48 @@ def test_plugin_cycle_matches_engine(gpu, tmp_path):
     assert int(tax[1]) == 16 and int(tax[2]) == 16
     assert float(tax[3]) == pytest.approx(float(te.sum()), rel=1e-6) and float(tax[4]) > 0
     assert resized[2] == "1" and float(resized[4]) > we[0, 2] > 0
+
+
+@pytest.mark.gpu
+def test_curved_sensor_plugin_matches_engine(gpu, tmp_path):
+    """The CurvedSensor plugin class on a soft box mesh pressed into the
+    floor: its 50 Hz gate, the (int)sample_resolution * area point count,
+    and its values against the Engine given the same points."""
+    out = _run(_compile(tmp_path), "curved")
+    steps = [ln for ln in out if ln[0] == "cstep"]
+    assert [ln[3] for ln in steps] == ["1", "1", "1"]
+    assert [ln[5] for ln in steps] == ["1", "1", "2"]
+    n_pts = int([ln for ln in out if ln[0] == "points"][0][1])
+    vals = np.array([float(x) for x in [ln for ln in out if ln[0] == "curved_values"][0][1:]], np.float32)
+    assert [ln for ln in out if ln[0] == "reject_primitive"][0][1] == "1"
+
+    from mujoco_contact_surfaces_gb300.engine import Engine
+    hx, hy, hz = np.float32(0.02), np.float32(0.02), np.float32(0.01)
+    vert = np.array([[sx * hx, sy * hy, sz * hz] for sx in (-1, 1) for sy in (-1, 1) for sz in (-1, 1)],
+                    np.float32).astype(np.float64)
+    face = np.array([0, 1, 3, 0, 3, 2, 4, 6, 7, 4, 7, 5, 0, 4, 5, 0, 5, 1, 2, 3, 7, 2, 7, 6, 0, 2, 6, 0, 6, 4,
+                     1, 5, 7, 1, 7, 3], np.int32).reshape(-1, 3)
+    area = 0.0
+    for a, b, c in face:
+        cr = np.cross(vert[b] - vert[a], vert[c] - vert[a])
+        area += 0.5 * np.sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2])
+    n_want = int(200000 * area)
+    assert n_pts == n_want
+    pts, nrm = L.sample_surface(vert, face, n_want, seed=42)
+    taxels = [[0.006 * i, 0.006 * j, -float(hz)] for i in (-1, 0, 1) for j in (-1, 0, 1)]
+    tn = np.zeros((9, 3))
+    tn[0] = [0, 0, -1]
+    tn[2] = [0, 0, -3]
+    eng = Engine()
+    eng.add_geom(0, L.GEOM_PLANE, [0, 0, 1], [0, 1.0, 0, 0.5, 0.5])
+    eng.add_geom(1, L.GEOM_MESH, [0, 0, 0], [1e5, 1.0, 0.004, 0.5, 0.5], vert, face)
+    sid = eng.add_curved_sensor(1, taxels, 0.004, pts, nrm, tn)
+    eng.set_pairs([1], [0])
+    xpos = np.array([[0, 0, 0], [0.001, -0.002, float(hz) - 0.002]])
+    xmat = np.tile(np.eye(3).reshape(1, 9), (2, 1))
+    eng.set_poses(xpos, xmat, np.zeros((2, 6)))
+    eng.step()
+    ve = eng.curved_sensor_values(sid)
+    eng.close()
+    np.testing.assert_array_equal(vals, ve)
+    assert np.count_nonzero(ve) >= 5
