@@ -121,7 +121,14 @@ int even_count(double extent, double hint, int min_n) {
 void soft_box(const double h[3], double E, double hint, SoftMesh* out) {
   // Even cell counts put a vertex layer on every mid-plane, so the extent
   // field min_i(h_i - |x_i|) / min_i(h_i) is captured exactly in the
-  // thinnest direction.
+  // thinnest direction.  Each cell's Kuhn diagonal starts at the cell corner
+  // nearest the centre (the cell is mirrored in every axis where it lies in
+  // the lower half), which is strictly inside the box: every tet then has a
+  // vertex of positive pressure, also along the box's edges and corners
+  // (with one diagonal direction for all cells, some tets there have all
+  // four vertices on the surface and carry no pressure).  Cells on either
+  // side of a mid-plane are mirror images, so their shared faces are cut
+  // alike.
   int n[3];
   for (int a = 0; a < 3; ++a) n[a] = even_count(2 * h[a], hint, 2);
   auto id = [&](int i, int j, int k) { return (k * (n[1] + 1) + j) * (n[0] + 1) + i; };
@@ -140,8 +147,11 @@ void soft_box(const double h[3], double E, double hint, SoftMesh* out) {
   out->t.clear();
   for (int k = 0; k < n[2]; ++k)
     for (int j = 0; j < n[1]; ++j)
-      for (int i = 0; i < n[0]; ++i)
-        kuhn_cell([&](int a, int b, int c) { return id(i + a, j + b, k + c); }, &out->t);
+      for (int i = 0; i < n[0]; ++i) {
+        const bool fi = 2 * i < n[0], fj = 2 * j < n[1], fk = 2 * k < n[2];
+        kuhn_cell([&](int a, int b, int c) { return id(i + (fi ? 1 - a : a), j + (fj ? 1 - b : b), k + (fk ? 1 - c : c)); },
+                  &out->t);
+      }
   orient_tets(out);
 }
 
@@ -170,11 +180,17 @@ void soft_cylinder(double R, double hl, double E, double hint, SoftMesh* out) {
       }
     }
   }
+  // Each cell's Kuhn diagonal starts at its inner ring and at the layer
+  // nearer the mid-plane (cells of the lower half mirrored in z): that
+  // corner is inside the cylinder, so every tet carries pressure, also where
+  // the mantle meets the caps.
   out->t.clear();
-  for (int k = 0; k < nz; ++k)
+  for (int k = 0; k < nz; ++k) {
+    const bool fk = 2 * k < nz;
     for (int j = 0; j < ns; ++j)
       for (int i = 0; i < nr; ++i)
-        kuhn_cell([&](int a, int b, int c) { return id(i + a, j + b, k + c); }, &out->t);
+        kuhn_cell([&](int a, int b, int c) { return id(i + a, j + b, k + (fk ? 1 - c : c)); }, &out->t);
+  }
   orient_tets(out);
 }
 

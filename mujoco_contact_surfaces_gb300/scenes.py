@@ -269,20 +269,65 @@ def soft_soft(n_pairs=1024, seed=SEED_SOFTSOFT, tet_range=(2000, 50000)) -> Scen
     _alloc(s)
     for (a, b) in place:
         Ra, Rb = random_rotation(rng), random_rotation(rng)
-        # distance between centres along z: sum of supports minus overlap
-        def support(body, R):
-            _, t, h, _ = body
-            if t == L.GEOM_SPHERE:
-                return h[0]
-            return float(np.sum(np.abs(R[2, :]) * np.asarray(h)))
+        # b below a, its centre offset sideways; lowered until the bodies
+        # touch along the vertical, then raised by the overlap
         ov = rng.uniform(0, 0.08) * min(a[3], b[3])
-        d = support(a, Ra) + support(b, Rb) - ov
+        off = rng.uniform(-0.2, 0.2, 2) * min(a[3], b[3])
         s.xmat[a[0]] = Ra.reshape(9)
         s.xmat[b[0]] = Rb.reshape(9)
         s.xpos[a[0]] = [0, 0, 0]
-        off = rng.uniform(-0.2, 0.2, 2) * min(a[3], b[3])
-        s.xpos[b[0]] = [off[0], off[1], -d]
+        zb = _touch_height(a, Ra, np.zeros(2), b, Rb, off)
+        s.xpos[b[0]] = [off[0], off[1], zb + ov]
     return s
+
+
+def _vertical_extent(body, R, c_xy, x, y):
+    """The body (centre (c_xy, 0), rotation R) along the vertical lines
+    through (x, y): (z_low, z_high), NaN where the line misses it."""
+    _, t, h, _ = body
+    dx, dy = x - c_xy[0], y - c_xy[1]
+    if t == L.GEOM_SPHERE:
+        r2 = h[0] ** 2 - dx * dx - dy * dy
+        hz = np.sqrt(np.where(r2 >= 0, r2, np.nan))
+        return -hz, hz
+    lo = np.full(x.shape, -np.inf)
+    hi = np.full(x.shape, np.inf)
+    for i in range(3):   # |R[:, i].(p - c)| <= h_i along p = (x, y, z)
+        u = R[0, i] * dx + R[1, i] * dy
+        w = R[2, i]
+        if abs(w) < 1e-12:
+            bad = np.abs(u) > h[i]
+            lo = np.where(bad, np.nan, lo)
+            continue
+        z1, z2 = (-h[i] - u) / w, (h[i] - u) / w
+        lo = np.maximum(lo, np.minimum(z1, z2))
+        hi = np.minimum(hi, np.maximum(z1, z2))
+    empty = ~(lo <= hi)
+    return np.where(empty, np.nan, lo), np.where(empty, np.nan, hi)
+
+
+def _touch_height(a, Ra, ca, b, Rb, cb, n=48, rounds=8):
+    """Centre height of b (below a, a's centre at height 0) at which the two
+    bodies touch when b rises vertically: the smallest gap between a's lower
+    and b's upper envelope over vertical lines.  The gap is convex in (x, y)
+    for convex bodies, so a grid is zoomed in around its minimum."""
+    r = 2.0 * max(max(a[2]), max(b[2]))
+    cx, cy = float(ca[0]), float(ca[1])
+    best = None
+    for _ in range(rounds):
+        g = np.linspace(-r, r, n)
+        x, y = np.meshgrid(g + cx, g + cy)
+        a_lo, _ = _vertical_extent(a, Ra, ca, x, y)
+        _, b_hi = _vertical_extent(b, Rb, cb, x, y)
+        gap = a_lo - b_hi
+        if not np.any(np.isfinite(gap)):
+            break
+        k = int(np.nanargmin(gap))
+        v = float(gap.flat[k])
+        best = v if best is None else min(best, v)
+        cx, cy = float(x.flat[k]), float(y.flat[k])
+        r *= 4.0 / n * 2.0   # a window of a few cells around the minimum
+    return best if best is not None else -(max(a[2]) + max(b[2]))
 
 
 def halfspace(n_pairs=8, seed=SEED_SINGLE + 500) -> Scene:

@@ -51,6 +51,9 @@ def test_soft_mesh_is_a_valid_tetrahedralisation(gtype, size, hint, vol):
     assert np.all(p[bverts] == 0)
     assert p.max() == pytest.approx(1e5, rel=1e-6)
     assert p.min() >= 0
+    # every tet carries pressure: a vertex off the surface (a tet with all
+    # four vertices on the surface would be a zero-pressure shell element)
+    assert np.all(p[e].max(axis=1) > 0), f"{int(np.sum(p[e].max(axis=1) == 0))} tets without pressure"
 
 
 def test_sphere_levels_and_tet_counts():
