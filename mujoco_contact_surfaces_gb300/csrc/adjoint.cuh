@@ -545,6 +545,95 @@ __device__ __forceinline__ void rec_forces_part(const StepArgs& a, const AdjPoly
   }
 }
 
+// raster_prepare for a kept polygon, shared by its group of kGroup lanes:
+// lane k transforms vertex k into the sensor frame and the group exchanges
+// them by shuffles (the group's lanes follow one control path, so the
+// shuffles name only the group's lanes); divisions are reciprocal products.
+// The forward and the adjoint both prepare through it, so they compute the
+// same sample keys.
+__device__ __forceinline__ bool raster_prepare_group(const StepArgs& a, const SensorDev& S, const float* Rl,
+                                                     const float* tl, const AdjPoly& R, V3<float> anc,
+                                                     V3<float> g_soft, int sub, RasterPoly& rp) {
+  const int nv = R.nv;
+  const int base = (threadIdx.x & 31) & ~(kGroup - 1);
+  const unsigned gm = 0xFFu << base;
+  float mx = 0.f, my = 0.f, mz = 0.f, mp = 0.f;
+  if (sub < nv) {
+    const float4 v = rec_vtx(R, sub);
+    const float X = __fadd_rn(anc.x, v.x), Y = __fadd_rn(anc.y, v.y), Z = __fadd_rn(anc.z, v.z);
+    mx = __fadd_rn(dot3_rn(Rl, X, Y, Z), tl[0]);
+    my = __fadd_rn(dot3_rn(Rl + 3, X, Y, Z), tl[1]);
+    mz = __fadd_rn(dot3_rn(Rl + 6, X, Y, Z), tl[2]);
+    mp = v.w;
+  }
+  float lz[kMaxPolyV];
+  float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
+#pragma unroll
+  for (int i = 0; i < kMaxPolyV; ++i) {
+    rp.lx[i] = __shfl_sync(gm, mx, base + i);
+    rp.ly[i] = __shfl_sync(gm, my, base + i);
+    lz[i] = __shfl_sync(gm, mz, base + i);
+    if (i < nv) {
+      mnx = fminf(mnx, rp.lx[i]); mxx = fmaxf(mxx, rp.lx[i]);
+      mny = fminf(mny, rp.ly[i]); mxy = fmaxf(mxy, rp.ly[i]);
+    }
+  }
+  rp.p0 = __shfl_sync(gm, mp, base);
+  float A2 = 0.f;
+#pragma unroll
+  for (int i = 1; i + 1 < kMaxPolyV; ++i)
+    if (i + 1 < nv)
+      A2 = __fadd_rn(A2, __fsub_rn(__fmul_rn(__fsub_rn(rp.lx[i], rp.lx[0]), __fsub_rn(rp.ly[i + 1], rp.ly[0])),
+                                   __fmul_rn(__fsub_rn(rp.ly[i], rp.ly[0]), __fsub_rn(rp.lx[i + 1], rp.lx[0]))));
+  if (!(fabsf(A2) >= 1e-10f)) return false;
+  rp.pos = A2 > 0.f;
+  const float e1x = __fsub_rn(rp.lx[1], rp.lx[0]), e1y = __fsub_rn(rp.ly[1], rp.ly[0]), e1z = __fsub_rn(lz[1], lz[0]);
+  float nx = 0.f, ny = 0.f, nz = 0.f;
+#pragma unroll
+  for (int i = 2; i < kMaxPolyV; ++i) {
+    if (i < nv) {
+      const float fx = __fsub_rn(rp.lx[i], rp.lx[0]), fy = __fsub_rn(rp.ly[i], rp.ly[0]), fz = __fsub_rn(lz[i], lz[0]);
+      nx = __fadd_rn(nx, __fsub_rn(__fmul_rn(e1y, fz), __fmul_rn(e1z, fy)));
+      ny = __fadd_rn(ny, __fsub_rn(__fmul_rn(e1z, fx), __fmul_rn(e1x, fz)));
+      nz = __fadd_rn(nz, __fsub_rn(__fmul_rn(e1x, fy), __fmul_rn(e1y, fx)));
+    }
+  }
+  if (!(fabsf(nz) > 0.f)) return false;
+  const float inz = __frcp_rn(nz);
+  rp.zx = __fmul_rn(-nx, inz);   // dz/dx, dz/dy on the plane
+  rp.zy = __fmul_rn(-ny, inz);
+  const float glx = dot3_rn(Rl, g_soft.x, g_soft.y, g_soft.z);
+  const float gly = dot3_rn(Rl + 3, g_soft.x, g_soft.y, g_soft.z);
+  const float glz = dot3_rn(Rl + 6, g_soft.x, g_soft.y, g_soft.z);
+  rp.px = __fadd_rn(glx, __fmul_rn(glz, rp.zx));   // dp/dx, dp/dy on the plane
+  rp.py = __fadd_rn(gly, __fmul_rn(glz, rp.zy));
+  rp.lz0 = lz[0];
+  const float* sx = a.samp_coord + S.samp_off_x;
+  const float* sy = a.samp_coord + S.samp_off_y;
+  const float x0 = sx[0], dx = S.nx > 1 ? __fsub_rn(sx[1], sx[0]) : 1.f;
+  const float y0 = sy[0], dy = S.ny > 1 ? __fsub_rn(sy[1], sy[0]) : 1.f;
+  const float idx = __frcp_rn(dx), idy = __frcp_rn(dy);
+  // the sample box, widened by 1e-3 of a sample step (a conservative bound:
+  // inclusion is decided by the probe)
+  const float fx0 = ceilf(__fsub_rn(__fmul_rn(__fsub_rn(mnx, x0), idx), 1e-3f));
+  const float fx1 = floorf(__fadd_rn(__fmul_rn(__fsub_rn(mxx, x0), idx), 1e-3f));
+  const float fy0 = ceilf(__fsub_rn(__fmul_rn(__fsub_rn(mny, y0), idy), 1e-3f));
+  const float fy1 = floorf(__fadd_rn(__fmul_rn(__fsub_rn(mxy, y0), idy), 1e-3f));
+  if (!(fx1 >= 0.f && fy1 >= 0.f && fx0 <= (float)(S.nx - 1) && fy0 <= (float)(S.ny - 1))) return false;
+  rp.X0 = max(0, (int)fx0); rp.X1 = min(S.nx - 1, (int)fx1);
+  rp.Y0 = max(0, (int)fy0); rp.Y1 = min(S.ny - 1, (int)fy1);
+  rp.nv = nv;
+#pragma unroll
+  for (int i = 0; i < kMaxPolyV; ++i) {
+    const bool last = i + 1 >= nv;
+    const float nxv = last ? rp.lx[0] : rp.lx[i + 1 < kMaxPolyV ? i + 1 : 0];
+    const float nyv = last ? rp.ly[0] : rp.ly[i + 1 < kMaxPolyV ? i + 1 : 0];
+    rp.ex[i] = __fsub_rn(nxv, rp.lx[i]);
+    rp.ey[i] = __fsub_rn(nyv, rp.ly[i]);
+  }
+  return true;
+}
+
 // The lane's share of a kept polygon's ray samples on one sensor (side 0:
 // the pair's sensor0, 1: sensor1): binning with slot keys (G null; lane 0
 // also stores the polygon's pressure model for the taxel pass) or the
@@ -556,7 +645,7 @@ __device__ __forceinline__ void rec_rays_part(const StepArgs& a, const AdjPoly& 
   const V3<float> anc = mk(R.anc[0], R.anc[1], R.anc[2]);
   const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
   RasterPoly rp;
-  if (!raster_prepare(a, S, Rl, tl, R.nv, anc, g, [&](int i) { return rec_vtx(R, i); }, rp)) return;
+  if (!raster_prepare_group(a, S, Rl, tl, R, anc, g, sub, rp)) return;
   if (!G && sub == 0) {
     a.slot_press[4 * (size_t)dst + 2 * side] = make_float4(rp.lx[0], rp.ly[0], rp.p0, rp.px);
     a.slot_press[4 * (size_t)dst + 2 * side + 1] = make_float4(rp.py, 0.f, 0.f, 0.f);
@@ -566,17 +655,24 @@ __device__ __forceinline__ void rec_rays_part(const StepArgs& a, const AdjPoly& 
   const float* sy = a.samp_coord + S.samp_off_y;
   const int nY = rp.Y1 - rp.Y0 + 1;
   const int cnt = (rp.X1 - rp.X0 + 1) * nY;
-  for (int idx = sub; idx < cnt; idx += kGroup) {
-    const int X = rp.X0 + idx / nY, Y = rp.Y0 + idx % nY;
+  if (nY <= 0 || cnt <= 0) return;   // the box holds no sample
+  // the low word of a slot key names the polygon (and sensor side) that won
+  // the sample, so the adjoint probes only the samples this polygon won
+  const unsigned own = (unsigned)key_slot(0.f, dst, side);
+  // sample idx = sub, sub + kGroup, ... of the box, row-major in (X, Y):
+  // one division up front, then stepped
+  const int dq = kGroup / nY, dr = kGroup % nY;
+  int X = rp.X0 + sub / nY, Y = rp.Y0 + sub % nY;
+  for (int idx = sub; idx < cnt; idx += kGroup, X += dq, Y += dr) {
+    if (Y > rp.Y1) { Y -= nY; ++X; }
+    const size_t si = (size_t)X * S.ny + Y;
+    if (G && (unsigned)smp[si] != own) continue;   // won by another polygon, or missed
     float t, z, pr;
     if (!raster_probe(rp, S, sx[X], sy[Y], t, z, pr)) continue;
-    const unsigned long long key = key_slot(t, dst, side);
-    const size_t si = (size_t)X * S.ny + Y;
     if (!G) {
-      atomicMin(&smp[si], key);
+      atomicMin(&smp[si], key_slot(t, dst, side));
       continue;
     }
-    if (smp[si] != key) continue;   // won by another polygon (keys are unique)
     sample_adjoint(a, S, Rl, tl, sx[X], sy[Y], z, pr, X, Y, g, mk(R.n[0], R.n[1], R.n[2]), soft_is_sensor, *G);
   }
 }
@@ -623,6 +719,7 @@ __global__ void __launch_bounds__(128, 4) rec_forward_kernel(StepArgs a) {
       o.pad[0] = o.pad[1] = o.pad[2] = 0;
       a.rec_out[dst] = o;
     }
+    __syncwarp();   // the groups enter the shuffled ray preparation together
     if (on) rec_rays(a, R, dst, sub, nullptr);
   }
 }
@@ -783,6 +880,7 @@ __global__ void __launch_bounds__(128, 4) adjoint_rec_kernel(StepArgs a) {
     const AdjPoly& R = a.recs[on ? r : base];
     AdjAcc G;
     adj_zero(G);
+    __syncwarp();   // the groups enter the shuffled ray preparation together
     if (taxel && on) rec_rays(a, R, dst, sub, &G);
     __syncwarp();
     if (wrench) rec_wrench_group(a, R, on, lane, sub, G);

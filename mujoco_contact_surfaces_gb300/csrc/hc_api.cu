@@ -207,6 +207,7 @@ struct hc_context {
   hc_timings last_timings = {};
   int launches_per_step = 0;
   int narrow_block = 128, narrow_ctas_per_sm = 8, narrow_chunk = 4;
+  int rec_fwd_ctas = 4, rec_adj_ctas = 4;   // resident CTAs per SM of the kept-polygon kernels
   int n_sm = 0;
   // adjoint
   bool adjoint_mode = false;   // steps keep the won taxel samples
@@ -400,7 +401,7 @@ bool keeps_polygons(const hc_context* c) {
 }
 
 int initial_rec_cap(const hc_context* c) {
-  return c->cfg.face_capacity > 0 ? (int)std::min<int64_t>(c->cfg.face_capacity, 1 << 30)
+  return c->cfg.face_capacity > 0 ? (int)std::min<int64_t>(c->cfg.face_capacity, (1 << 30) - 1)
                                   : std::max(1 << 15, 4 * c->item_cap);
 }
 
@@ -416,7 +417,9 @@ hc_status ensure_rec_offsets(hc_context* c) {
 }
 
 hc_status ensure_recs(hc_context* c, int cap) {
-  cap = std::min(cap, 1 << 30);   // record slots are 30-bit fields of the sample keys
+  // record slots are 30-bit fields of the sample keys; the all-ones field is
+  // the empty sample's, so the largest slot is 2^30 - 2
+  cap = std::min(cap, (1 << 30) - 1);
   if (cap > c->rec_cap) {
     HC_CUDA(c->recs.reserve(cap));
     HC_CUDA(c->rec_key.reserve(cap));
@@ -582,6 +585,8 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
   a.want_pair = want_pair;
   a.narrow_block = c->narrow_block;
   a.narrow_grid = std::max(1, c->n_sm * c->narrow_ctas_per_sm);
+  a.rec_fwd_grid = std::max(1, c->n_sm * c->rec_fwd_ctas);
+  a.rec_adj_grid = std::max(1, c->n_sm * c->rec_adj_ctas);
   a.chunk = std::max(1, c->narrow_chunk);
   a.keep_samples = c->adjoint_mode ? 1 : 0;
   a.rec_count = c->counters.p + kCntRec;
@@ -732,6 +737,7 @@ hc_status hc_context_create(const hc_config* cfg, hc_context** out) {
   cudaDeviceProp prop;
   cudaGetDeviceProperties(&prop, c0.device);
   c->n_sm = prop.multiProcessorCount;
+  hc::record_ctas_per_sm(&c->rec_fwd_ctas, &c->rec_adj_ctas);
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return fail(HC_ERR_CUDA, "stream create failed");

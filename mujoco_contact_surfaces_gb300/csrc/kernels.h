@@ -68,6 +68,8 @@ struct StepArgs {
   // launch shape of the narrow phase
   int narrow_block;
   int narrow_grid;
+  int rec_fwd_grid;   // the kept-polygon kernels: every CTA resident at once
+  int rec_adj_grid;
   int chunk;          // consecutive items a soft-rigid warp takes at once
   // adjoint
   int keep_samples;          // taxel pass leaves the won samples for the adjoint
@@ -127,6 +129,11 @@ void launch_refit(const float4* elems, int verts_per_elem, float4* nodes, const 
 
 // Kernel attributes (large dynamic shared memory); once per device.
 cudaError_t init_kernel_attributes();
+
+// CTAs of 128 threads that fit on one SM for the forward and adjoint passes
+// over the kept polygons (their work is split evenly over the grid, so the
+// grid is sized to be resident in one wave).
+void record_ctas_per_sm(int* fwd, int* adj);
 
 // One step: frames, broadphase, narrow phase, per-pair reduce, taxels.
 // Returns the number of kernels launched.

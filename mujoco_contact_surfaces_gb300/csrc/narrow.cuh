@@ -193,16 +193,13 @@ __device__ __forceinline__ float raster_pressure(float lx0, float ly0, float p0,
 // and the pressure there.
 __device__ __forceinline__ bool raster_probe(const RasterPoly& rp, const SensorDev& S, float qx, float qy,
                                              float& t, float& z, float& pr) {
-  bool in = true;
 #pragma unroll
   for (int i = 0; i < kMaxPolyV; ++i) {
-    if (i < rp.nv) {
-      const float e = __fsub_rn(__fmul_rn(rp.ex[i], __fsub_rn(qy, rp.ly[i])),
-                                __fmul_rn(rp.ey[i], __fsub_rn(qx, rp.lx[i])));
-      in &= rp.pos ? e >= 0.f : e <= 0.f;
-    }
+    if (i >= rp.nv) break;
+    const float e = __fsub_rn(__fmul_rn(rp.ex[i], __fsub_rn(qy, rp.ly[i])),
+                              __fmul_rn(rp.ey[i], __fsub_rn(qx, rp.lx[i])));
+    if (rp.pos ? e < 0.f : e > 0.f) return false;   // outside this edge
   }
-  if (!in) return false;
   const float ddx = __fsub_rn(qx, rp.lx[0]), ddy = __fsub_rn(qy, rp.ly[0]);
   z = __fadd_rn(__fadd_rn(rp.lz0, __fmul_rn(rp.zx, ddx)), __fmul_rn(rp.zy, ddy));
   t = __fsub_rn(__fadd_rn(S.zs15, 1e-8f), z);
