@@ -635,20 +635,23 @@ __device__ __forceinline__ bool raster_prepare_group(const StepArgs& a, const Se
 }
 
 // The lane's share of a kept polygon's ray samples on one sensor (side 0:
-// the pair's sensor0, 1: sensor1): binning with slot keys (G null; lane 0
-// also stores the polygon's pressure model for the taxel pass) or the
-// adjoint of the samples it won.
-__device__ __forceinline__ void rec_rays_part(const StepArgs& a, const AdjPoly& R, int dst, int side, int sid,
-                                              const float* Rl, const float* tl, int soft_is_sensor, int sub,
-                                              AdjAcc* G) {
+// the pair's sensor0, 1: sensor1), forward: binning with slot keys; lane 0
+// keeps the polygon's plane, pressure model and sample box for the taxel
+// pass and the adjoint.
+__device__ __forceinline__ void rec_rays_fwd(const StepArgs& a, const AdjPoly& R, int dst, int side, int sid,
+                                             const float* Rl, const float* tl, int sub) {
   const SensorDev S = a.sensors[sid];
-  const V3<float> anc = mk(R.anc[0], R.anc[1], R.anc[2]);
-  const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
   RasterPoly rp;
-  if (!raster_prepare_group(a, S, Rl, tl, R, anc, g, sub, rp)) return;
-  if (!G && sub == 0) {
-    a.slot_press[4 * (size_t)dst + 2 * side] = make_float4(rp.lx[0], rp.ly[0], rp.p0, rp.px);
-    a.slot_press[4 * (size_t)dst + 2 * side + 1] = make_float4(rp.py, 0.f, 0.f, 0.f);
+  float4* sp = a.slot_press + 6 * (size_t)dst + 3 * side;
+  if (!raster_prepare_group(a, S, Rl, tl, R, mk(R.anc[0], R.anc[1], R.anc[2]), mk(R.g[0], R.g[1], R.g[2]), sub,
+                            rp)) {
+    if (sub == 0) sp[2] = make_float4(__int_as_float(1), __int_as_float(0), __int_as_float(1), __int_as_float(0));
+    return;
+  }
+  if (sub == 0) {
+    sp[0] = make_float4(rp.lx[0], rp.ly[0], rp.p0, rp.px);
+    sp[1] = make_float4(rp.py, rp.lz0, rp.zx, rp.zy);
+    sp[2] = make_float4(__int_as_float(rp.X0), __int_as_float(rp.X1), __int_as_float(rp.Y0), __int_as_float(rp.Y1));
   }
   unsigned long long* smp = a.samples + S.sample_off;
   const float* sx = a.samp_coord + S.samp_off_x;
@@ -656,34 +659,61 @@ __device__ __forceinline__ void rec_rays_part(const StepArgs& a, const AdjPoly& 
   const int nY = rp.Y1 - rp.Y0 + 1;
   const int cnt = (rp.X1 - rp.X0 + 1) * nY;
   if (nY <= 0 || cnt <= 0) return;   // the box holds no sample
-  // the low word of a slot key names the polygon (and sensor side) that won
-  // the sample, so the adjoint probes only the samples this polygon won
-  const unsigned own = (unsigned)key_slot(0.f, dst, side);
   // sample idx = sub, sub + kGroup, ... of the box, row-major in (X, Y):
   // one division up front, then stepped
   const int dq = kGroup / nY, dr = kGroup % nY;
   int X = rp.X0 + sub / nY, Y = rp.Y0 + sub % nY;
   for (int idx = sub; idx < cnt; idx += kGroup, X += dq, Y += dr) {
     if (Y > rp.Y1) { Y -= nY; ++X; }
-    const size_t si = (size_t)X * S.ny + Y;
-    if (G && (unsigned)smp[si] != own) continue;   // won by another polygon, or missed
     float t, z, pr;
-    if (!raster_probe(rp, S, sx[X], sy[Y], t, z, pr)) continue;
-    if (!G) {
-      atomicMin(&smp[si], key_slot(t, dst, side));
-      continue;
-    }
-    sample_adjoint(a, S, Rl, tl, sx[X], sy[Y], z, pr, X, Y, g, mk(R.n[0], R.n[1], R.n[2]), soft_is_sensor, *G);
+    if (raster_probe(rp, S, sx[X], sy[Y], t, z, pr)) atomicMin(&smp[(size_t)X * S.ny + Y], key_slot(t, dst, side));
+  }
+}
+
+// Adjoint of the samples a kept polygon won on one sensor: the forward's
+// plane and box; the won samples are known by their keys (the low word names
+// the polygon and side), so no inside test is needed.
+__device__ __forceinline__ void rec_rays_adj(const StepArgs& a, const AdjPoly& R, int dst, int side, int sid,
+                                             const float* Rl, const float* tl, int soft_is_sensor, int sub,
+                                             AdjAcc& G) {
+  const float4* sp = a.slot_press + 6 * (size_t)dst + 3 * side;
+  const float4 bx = sp[2];
+  const int X0 = __float_as_int(bx.x), X1 = __float_as_int(bx.y), Y0 = __float_as_int(bx.z),
+            Y1 = __float_as_int(bx.w);
+  const int nY = Y1 - Y0 + 1;
+  const int cnt = (X1 - X0 + 1) * nY;
+  if (X0 > X1 || nY <= 0 || cnt <= 0) return;
+  const SensorDev S = a.sensors[sid];
+  const float4 m0 = sp[0], m1 = sp[1];
+  const unsigned long long* smp = a.samples + S.sample_off;
+  const float* sx = a.samp_coord + S.samp_off_x;
+  const float* sy = a.samp_coord + S.samp_off_y;
+  const unsigned own = (unsigned)key_slot(0.f, dst, side);
+  const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
+  const int dq = kGroup / nY, dr = kGroup % nY;
+  int X = X0 + sub / nY, Y = Y0 + sub % nY;
+  for (int idx = sub; idx < cnt; idx += kGroup, X += dq, Y += dr) {
+    if (Y > Y1) { Y -= nY; ++X; }
+    if ((unsigned)smp[(size_t)X * S.ny + Y] != own) continue;   // won by another polygon, or missed
+    const float qx = sx[X], qy = sy[Y];
+    const float z = raster_height(m0.x, m0.y, m1.y, m1.z, m1.w, qx, qy);
+    const float pr = raster_pressure(m0.x, m0.y, m0.z, m0.w, m1.x, qx, qy);
+    sample_adjoint(a, S, Rl, tl, qx, qy, z, pr, X, Y, g, mk(R.n[0], R.n[1], R.n[2]), soft_is_sensor, G);
   }
 }
 
 __device__ __forceinline__ void rec_rays(const StepArgs& a, const AdjPoly& R, int dst, int sub, AdjAcc* G) {
   const PairDev& P = a.pairs[R.pair];
   const FrameDev& F = a.frames[R.pair];
+  if (!G) {
+    if (P.sensor0 >= 0) rec_rays_fwd(a, R, dst, 0, P.sensor0, F.Rl, F.tl, sub);
+    if (P.sensor1 >= 0) rec_rays_fwd(a, R, dst, 1, P.sensor1, F.Rl1, F.tl1, sub);
+    return;
+  }
   if (P.sensor0 >= 0)
-    rec_rays_part(a, R, dst, 0, P.sensor0, F.Rl, F.tl, a.sensors[P.sensor0].geom == P.gs, sub, G);
+    rec_rays_adj(a, R, dst, 0, P.sensor0, F.Rl, F.tl, a.sensors[P.sensor0].geom == P.gs, sub, *G);
   if (P.sensor1 >= 0)
-    rec_rays_part(a, R, dst, 1, P.sensor1, F.Rl1, F.tl1, a.sensors[P.sensor1].geom == P.gs, sub, G);
+    rec_rays_adj(a, R, dst, 1, P.sensor1, F.Rl1, F.tl1, a.sensors[P.sensor1].geom == P.gs, sub, *G);
 }
 
 // Forward pass over the kept polygons: forces into the polygon's pair-ordered

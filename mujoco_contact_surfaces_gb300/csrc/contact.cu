@@ -394,8 +394,8 @@ __global__ void taxel_kernel(StepArgs a) {
           // won by a kept polygon: its pressure model for this sensor
           const int slot = (int)(lo & ~(kSlotTag | kSideBit));
           const int side = (lo & kSideBit) ? 1 : 0;
-          const float4 m0 = a.slot_press[4 * (size_t)slot + 2 * side];
-          const float4 m1 = a.slot_press[4 * (size_t)slot + 2 * side + 1];
+          const float4 m0 = a.slot_press[6 * (size_t)slot + 3 * side];
+          const float4 m1 = a.slot_press[6 * (size_t)slot + 3 * side + 1];
           pr = raster_pressure(m0.x, m0.y, m0.z, m0.w, m1.x, a.samp_coord[S.samp_off_x + X],
                                a.samp_coord[S.samp_off_y + Y]);
         }

@@ -424,7 +424,7 @@ hc_status ensure_recs(hc_context* c, int cap) {
     HC_CUDA(c->recs.reserve(cap));
     HC_CUDA(c->rec_key.reserve(cap));
     HC_CUDA(c->rec_out.reserve(cap));
-    HC_CUDA(c->slot_press.reserve(4 * (size_t)cap));
+    HC_CUDA(c->slot_press.reserve(6 * (size_t)cap));
     HC_CUDA(c->rec_perm.reserve(cap));
     HC_CUDA(c->rec_grad.reserve(16 * (size_t)cap));
     c->rec_cap = cap;

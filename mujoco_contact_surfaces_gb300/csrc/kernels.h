@@ -89,8 +89,10 @@ struct StepArgs {
   int n_item_blocks;         // item_cap / kBpBlock rounded up
   float* rec_grad;           // per record in pair order: 13 gradient terms (stride 16)
   RecOut* rec_out;           // per record in pair order: forces (forward)
-  float4* slot_press;        // per record slot and sensor side (2): the linear
-                             // pressure model (lx0, ly0, p0, px), (py, -, -, -)
+  float4* slot_press;        // per record slot and sensor side (2), three float4:
+                             // the linear pressure model (lx0, ly0, p0, px), then
+                             // (py, lz0, zx, zy) of the polygon's plane, then its
+                             // sample box (X0, X1, Y0, Y1 as ints; X0 > X1: none)
   int* rec_perm;             // per record slot: the record index
   // taxel-point sensors
   const TaxelSensorDev* tsens;

@@ -181,6 +181,13 @@ __device__ __forceinline__ unsigned long long key_slot(float t, int slot, int si
          (unsigned long long)(kSlotTag | (side ? kSideBit : 0u) | (unsigned)slot);
 }
 
+// Height of a prepared polygon's plane at (qx, qy).
+__device__ __forceinline__ float raster_height(float lx0, float ly0, float lz0, float zx, float zy, float qx,
+                                               float qy) {
+  const float ddx = __fsub_rn(qx, lx0), ddy = __fsub_rn(qy, ly0);
+  return __fadd_rn(__fadd_rn(lz0, __fmul_rn(zx, ddx)), __fmul_rn(zy, ddy));
+}
+
 // Pressure of a prepared polygon's linear model at (qx, qy).
 __device__ __forceinline__ float raster_pressure(float lx0, float ly0, float p0, float px, float py, float qx,
                                                  float qy) {
@@ -200,8 +207,7 @@ __device__ __forceinline__ bool raster_probe(const RasterPoly& rp, const SensorD
                               __fmul_rn(rp.ey[i], __fsub_rn(qx, rp.lx[i])));
     if (rp.pos ? e < 0.f : e > 0.f) return false;   // outside this edge
   }
-  const float ddx = __fsub_rn(qx, rp.lx[0]), ddy = __fsub_rn(qy, rp.ly[0]);
-  z = __fadd_rn(__fadd_rn(rp.lz0, __fmul_rn(rp.zx, ddx)), __fmul_rn(rp.zy, ddy));
+  z = raster_height(rp.lx[0], rp.ly[0], rp.lz0, rp.zx, rp.zy, qx, qy);
   t = __fsub_rn(__fadd_rn(S.zs15, 1e-8f), z);
   if (!(t > 0.f && t < S.zs15)) return false;
   pr = raster_pressure(rp.lx[0], rp.ly[0], rp.p0, rp.px, rp.py, qx, qy);
