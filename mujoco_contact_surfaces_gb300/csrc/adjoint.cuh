@@ -489,38 +489,38 @@ __device__ __forceinline__ V3<float> rec_pos(const AdjPoly& R, int i) {
 }
 
 // Polygon sums of the quadrature: signed area A, the
-// area-weighted centroid c and the pressure pc there (every lane of the
-// group computes them).
-__device__ __forceinline__ void rec_fan(const AdjPoly& R, int nv, V3<float> n, float& A, V3<float>& c, float& pc) {
-  A = 0.f;
-  pc = 0.f;
-  c = mk(0.f, 0.f, 0.f);
-  const float4 v0 = rec_vtx(R, 0);
-  const V3<float> x0 = mk(v0.x, v0.y, v0.z);
-#pragma unroll
-  for (int i = 1; i + 1 < kMaxPolyV; ++i) {
-    if (i + 1 < nv) {
-      const float4 vi = rec_vtx(R, i), vj = rec_vtx(R, i + 1);
-      const V3<float> xi = mk(vi.x, vi.y, vi.z), xj = mk(vj.x, vj.y, vj.z);
-      const float ai = 0.5f * dot(cross(xi - x0, xj - x0), n);
-      A += ai;
-      c = c + (x0 + xi + xj) * (ai * (1.f / 3.f));
-      pc += ai * (v0.w + vi.w + vj.w) * (1.f / 3.f);
-    }
+// area-weighted centroid c and the pressure pc there, shared by the group:
+// lane t adds fan triangle (0, t, t+1); fixed-order shuffle sums.  Every
+// lane of the warp calls it.
+__device__ __forceinline__ void rec_fan_group(const AdjPoly& R, int nv, V3<float> n, int sub, float& A, V3<float>& c,
+                                              float& pc) {
+  float ai = 0.f, pp = 0.f;
+  V3<float> cc = mk(0.f, 0.f, 0.f);
+  if (sub >= 1 && sub + 1 < nv) {
+    const float4 v0 = rec_vtx(R, 0), vi = rec_vtx(R, sub), vj = rec_vtx(R, sub + 1);
+    const V3<float> x0 = mk(v0.x, v0.y, v0.z), xi = mk(vi.x, vi.y, vi.z), xj = mk(vj.x, vj.y, vj.z);
+    ai = 0.5f * dot(cross(xi - x0, xj - x0), n);
+    cc = (x0 + xi + xj) * (ai * (1.f / 3.f));
+    pp = ai * (v0.w + vi.w + vj.w) * (1.f / 3.f);
   }
+  A = gsum(ai);
+  c = gsum3(cc);
+  pc = gsum(pp);
 }
 
 // The lane's share of a kept polygon's forces (its quadrature point).
-__device__ __forceinline__ void rec_forces_part(const StepArgs& a, const AdjPoly& R, int sub, Acc& ac) {
+// Every lane of the warp calls it (shuffles); `on`: the group holds a polygon.
+__device__ __forceinline__ void rec_forces_part(const StepArgs& a, const AdjPoly& R, int sub, bool on, Acc& ac) {
   const PairDev& P = a.pairs[R.pair];
   const FrameDev& F = a.frames[R.pair];
-  const int nv = R.nv;
+  const int nv = on ? R.nv : 0;
   const V3<float> anc = mk(R.anc[0], R.anc[1], R.anc[2]);
   const V3<float> nc = mk(R.n[0], R.n[1], R.n[2]) * (P.s_is_m ? 1.f : -1.f);
   const float gM = P.s_is_m ? R.gint : INFINITY, gN = P.s_is_m ? INFINITY : R.gint;
   float A, pcen;
   V3<float> c;
-  rec_fan(R, nv, nc, A, c, pcen);
+  rec_fan_group(R, nv, nc, sub, A, c, pcen);
+  if (!on) return;
   if (A != 0.f) {
     c = c * (1.f / A);
     pcen /= A;
@@ -736,7 +736,7 @@ __global__ void __launch_bounds__(128, 4) rec_forward_kernel(StepArgs a) {
     const AdjPoly& R = a.recs[on ? r : base];
     Acc ac;
     acc_zero(ac);
-    if (on) rec_forces_part(a, R, sub, ac);
+    rec_forces_part(a, R, sub, on, ac);
     float v[9] = {ac.F[0], ac.F[1], ac.F[2], ac.T[0], ac.T[1], ac.T[2], ac.area, ac.fn0, (float)ac.n_faces};
 #pragma unroll
     for (int k = 0; k < 9; ++k) v[k] = gsum(v[k]);
@@ -773,7 +773,7 @@ __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPol
   const V3<float> gFv = mk(gF[0], gF[1], gF[2]), gTv = mk(gF[3], gF[4], gF[5]);
   float A = 0.f, pc = 0.f;
   V3<float> c = mk(0.f, 0.f, 0.f);
-  if (on) rec_fan(R, nv, ns, A, c, pc);
+  rec_fan_group(R, nv, ns, sub, A, c, pc);
   const bool live = on && A != 0.f;
   const float iA = live ? 1.f / A : 0.f;
   c = c * iA;
@@ -836,28 +836,39 @@ __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPol
   const V3<float> Scb = cbar * iA;
   const float Spb = pcbar * iA;
   Abar -= (dot(cbar, c) + pcbar * pc) * iA;
-  if (live) {
-    const float4 v0 = rec_vtx(R, 0);
-    const V3<float> x0 = mk(v0.x, v0.y, v0.z);
-#pragma unroll
-    for (int i = 1; i + 1 < kMaxPolyV; ++i) {
-      if (i + 1 < nv) {
-        const float4 vi = rec_vtx(R, i), vj = rec_vtx(R, i + 1);
-        const V3<float> xi = mk(vi.x, vi.y, vi.z), xj = mk(vj.x, vj.y, vj.z);
-        const V3<float> e1 = xi - x0, e2 = xj - x0;
-        const V3<float> cr = cross(e1, e2);
-        const float ai = 0.5f * dot(cr, ns);
-        const float aib = Abar + dot(Scb, x0 + xi + xj) * (1.f / 3.f) + Spb * (v0.w + vi.w + vj.w) * (1.f / 3.f);
-        const V3<float> sx = Scb * (ai * (1.f / 3.f));
-        const float sp = Spb * ai * (1.f / 3.f);
-        // a_i = n . (e1 x e2) / 2
-        nbar = nbar + cr * (0.5f * aib);
-        const V3<float> e1b = cross(e2, ns) * (0.5f * aib), e2b = cross(ns, e1) * (0.5f * aib);
-        if (sub == 0) { xb = xb + sx - e1b - e2b; pb += sp; }
-        if (sub == i) { xb = xb + sx + e1b; pb += sp; }
-        if (sub == i + 1) { xb = xb + sx + e2b; pb += sp; }
-      }
+  {
+    // fan triangle t = sub reversed by its lane: its shares go to vertex 0
+    // (a group sum), vertex t (this lane) and vertex t+1 (the next lane)
+    V3<float> nb = mk(0.f, 0.f, 0.f), to0 = nb, to_next = nb;
+    float p_to0 = 0.f, p_next = 0.f;
+    if (live && sub >= 1 && sub + 1 < nv) {
+      const float4 v0 = rec_vtx(R, 0), vi = rec_vtx(R, sub), vj = rec_vtx(R, sub + 1);
+      const V3<float> x0 = mk(v0.x, v0.y, v0.z), xi = mk(vi.x, vi.y, vi.z), xj = mk(vj.x, vj.y, vj.z);
+      const V3<float> e1 = xi - x0, e2 = xj - x0;
+      const V3<float> cr = cross(e1, e2);
+      const float ai = 0.5f * dot(cr, ns);
+      const float aib = Abar + dot(Scb, x0 + xi + xj) * (1.f / 3.f) + Spb * (v0.w + vi.w + vj.w) * (1.f / 3.f);
+      const V3<float> sx = Scb * (ai * (1.f / 3.f));
+      const float sp = Spb * ai * (1.f / 3.f);
+      // a_t = n . (e1 x e2) / 2
+      nb = cr * (0.5f * aib);
+      const V3<float> e1b = cross(e2, ns) * (0.5f * aib), e2b = cross(ns, e1) * (0.5f * aib);
+      to0 = sx - e1b - e2b;
+      p_to0 = sp;
+      xb = xb + sx + e1b;
+      pb += sp;
+      to_next = sx + e2b;
+      p_next = sp;
     }
+    const int prev = (lane & ~(kGroup - 1)) | (sub == 0 ? 0 : sub - 1);
+    const V3<float> in = mk(__shfl_sync(0xffffffffu, to_next.x, prev), __shfl_sync(0xffffffffu, to_next.y, prev),
+                            __shfl_sync(0xffffffffu, to_next.z, prev));
+    const float pin = __shfl_sync(0xffffffffu, p_next, prev);
+    if (sub > 0) { xb = xb + in; pb += pin; }
+    const V3<float> s0 = gsum3(to0);
+    const float ps0 = gsum(p_to0);
+    if (sub == 0) { xb = xb + s0; pb += ps0; }
+    nbar = nbar + gsum3(nb);
   }
   // contraction with the tangents of the lane's vertex
   V3<float> rot = mk(0.f, 0.f, 0.f), tr = rot;
