@@ -290,11 +290,12 @@ __global__ void __launch_bounds__(128, 4) adjoint_sr_kernel(StepArgs a) {
       const int i = e & 31, j = e >> 5;
       const TetStage& TS = W.tet[i];
       const TriStage& T = W.tri[j];
-      double s[4];
+      float s[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) s[q] = plane64(T.n64, T.o64, TS.X[q][0], TS.X[q][1], TS.X[q][2]);
-      const bool allp = s[0] > kNearTol && s[1] > kNearTol && s[2] > kNearTol && s[3] > kNearTol;
-      const bool alln = s[0] < -kNearTol && s[1] < -kNearTol && s[2] < -kNearTol && s[3] < -kNearTol;
+      for (int q = 0; q < 4; ++q) s[q] = plane_df(T.n, T.nl, T.o, T.ol, TS.X[q][0], TS.X[q][1], TS.X[q][2]);
+      constexpr float tol = (float)kNearTol;
+      const bool allp = s[0] > tol && s[1] > tol && s[2] > tol && s[3] > tol;
+      const bool alln = s[0] < -tol && s[1] < -tol && s[2] < -tol && s[3] < -tol;
       if (allp || alln) continue;
       TetIn<float> t;
       unstage_tet(TS, t);
@@ -308,10 +309,14 @@ __global__ void __launch_bounds__(128, 4) adjoint_sr_kernel(StepArgs a) {
       float gint = 0.f;
       if (dc.unc) {
         bool near;
-        nv = sr_fp64(a, T, tet_idx, s, anc, poly, near, gint);
+        nv = sr_fp64(a, T, tet_idx, anc, poly, near, gint);
       } else if (nv >= 3) {
         gint = dot(t.g, n);
-        if (fabsf(gint) <= 1e-5f * t.gl) gint = grad_along64(a, tet_idx, T.n64[0], T.n64[1], T.n64[2]);
+        if (fabsf(gint) <= 1e-5f * t.gl) {
+          double n64[3], o64;
+          tri_plane64(T, n64, o64);
+          gint = grad_along64(a, tet_idx, n64[0], n64[1], n64[2]);
+        }
       }
       if (nv < 3) continue;
       // taxel adjoint on the forward polygon

@@ -88,19 +88,20 @@ __device__ __forceinline__ void check(Decide& dc, R v, R tol) {
   }
 }
 
-// Section of a tet by s = 0 (s given in FP64 for the four vertices).
+// Section of a tet by s = 0 (s for the four vertices: FP64, or the FP32 head
+// of a double-float value, whose sign it has whenever it is not near zero).
 // Output: triangle or quad in cyclic order (marching-tetrahedron pattern),
 // each vertex interpolated from the endpoint with the smaller |s|.
-template <class R, int ND>
-__device__ __forceinline__ int tet_section(const PV<R, ND> tv[4], const double s[4], Decide& dc, PV<R, ND> out[4]) {
+template <class R, int ND, class S>
+__device__ __forceinline__ int tet_section(const PV<R, ND> tv[4], const S s[4], Decide& dc, PV<R, ND> out[4]) {
   int pos = 0;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    if (fabs(s[k]) < kNearTol) {
+    if (abs_r(s[k]) < (S)kNearTol) {
       if (sizeof(R) == 4) dc.unc = true;
       else dc.near = true;
     }
-    pos |= (s[k] > 0.0) << k;
+    pos |= (s[k] > (S)0) << k;
   }
   const int np = __popc(pos);
   if (np == 0 || np == 4) return 0;
@@ -128,7 +129,7 @@ __device__ __forceinline__ int tet_section(const PV<R, ND> tv[4], const double s
       // the tet edge (a, b) lies on the faces opposite the two other vertices
       const int other = 0xF & ~((1 << a) | (1 << b));
       const int c = __ffs(other) - 1, d = __ffs(other & ~(1 << c)) - 1;
-      if (fabs(s[a]) > fabs(s[b])) { int t = a; a = b; b = t; }
+      if (abs_r(s[a]) > abs_r(s[b])) { int t = a; a = b; b = t; }
       const R sa = (R)s[a], sb = (R)s[b];
       out[i] = pv_lerp(tv[a], tv[b], sa / (sa - sb));
       out[i].lab = c | (d << 4);

@@ -447,11 +447,12 @@ __device__ __forceinline__ void unstage_tet(const TetStage& S, TetIn<float>& t) 
 }
 
 // Index of the tet vertex nearest the section plane.
-__device__ __forceinline__ int nearest_vertex(const double s[4]) {
+template <class S>
+__device__ __forceinline__ int nearest_vertex(const S s[4]) {
   int k = 0;
 #pragma unroll
   for (int i = 1; i < 4; ++i)
-    if (fabs(s[i]) < fabs(s[k])) k = i;
+    if (abs_r(s[i]) < abs_r(s[k])) k = i;
   return k;
 }
 
@@ -668,12 +669,12 @@ constexpr int kNarrowWarps = 4;
 // soft-rigid
 // ============================================================================
 struct TriStage {
-  double n64[3], o64;  // FP64 plane (unit normal out of the rigid body, offset)
-  double en64[3][3];   // FP64 in-plane inward edge planes
-  double eo64[3];
-  float n[3], o;       // float copies
-  float en[3][3];
+  float n[3], o;       // plane (unit normal out of the rigid body, offset): FP32 head
+  float en[3][3];      // in-plane inward edge planes: FP32 head
   float eo[3];
+  float nl[3], ol;     // FP32 tails: head + tail is the FP64 plane to 2^-48
+  float enl[3][3];
+  float eol[3];
   float lo[3], hi[3];
   float M, h, Lt;      // coordinate magnitude, min altitude, max edge
   int orig, valid;
@@ -689,9 +690,10 @@ __device__ __noinline__ void stage_tri(const StepArgs& a, const PairDev& P, cons
   // plane: n = R n_body, o = o_body + n . t (FP64)
   const V3<double> nd = mat_mul<double>(F.R, mk(pl.x, pl.y, pl.z));
   const double od = pl.w + nd.x * F.t[0] + nd.y * F.t[1] + nd.z * F.t[2];
-  S.n64[0] = nd.x; S.n64[1] = nd.y; S.n64[2] = nd.z; S.o64 = od;
   const V3<float> n = mk((float)nd.x, (float)nd.y, (float)nd.z);
   S.n[0] = n.x; S.n[1] = n.y; S.n[2] = n.z; S.o = (float)od;
+  S.nl[0] = (float)(nd.x - (double)n.x); S.nl[1] = (float)(nd.y - (double)n.y);
+  S.nl[2] = (float)(nd.z - (double)n.z); S.ol = (float)(od - (double)S.o);
   V3<float> Y[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -704,8 +706,9 @@ __device__ __noinline__ void stage_tri(const StepArgs& a, const PairDev& P, cons
     const Dbl4 ep = a.tri_edges[3 * (size_t)idx + j];
     const V3<double> m = mat_mul<double>(F.R, mk(ep.x, ep.y, ep.z));
     const double eo = ep.w + m.x * F.t[0] + m.y * F.t[1] + m.z * F.t[2];
-    S.en64[j][0] = m.x; S.en64[j][1] = m.y; S.en64[j][2] = m.z; S.eo64[j] = eo;
     S.en[j][0] = (float)m.x; S.en[j][1] = (float)m.y; S.en[j][2] = (float)m.z; S.eo[j] = (float)eo;
+    S.enl[j][0] = (float)(m.x - (double)S.en[j][0]); S.enl[j][1] = (float)(m.y - (double)S.en[j][1]);
+    S.enl[j][2] = (float)(m.z - (double)S.en[j][2]); S.eol[j] = (float)(eo - (double)S.eo[j]);
   }
   const float M = fmaxf(meta.z, fmaxf(fabsf(F.tf[0]), fmaxf(fabsf(F.tf[1]), fabsf(F.tf[2]))));
   const float pad = 1e-5f * (M + meta.y) + 1e-7f;
@@ -719,13 +722,44 @@ __device__ __noinline__ void stage_tri(const StepArgs& a, const PairDev& P, cons
   S.valid = meta.x > 0.f ? 1 : 0;
 }
 
+// The staged FP64 planes, head + tail.
+__device__ __forceinline__ void tri_plane64(const TriStage& T, double n[3], double& o) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) n[k] = (double)T.n[k] + (double)T.nl[k];
+  o = (double)T.o + (double)T.ol;
+}
+__device__ __forceinline__ void tri_edge64(const TriStage& T, int j, double m[3], double& o) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) m[k] = (double)T.en[j][k] + (double)T.enl[j][k];
+  o = (double)T.eo[j] + (double)T.eol[j];
+}
+
+// n.x - o for a float point x and a double-float plane (heads nh, oh; tails
+// nl, ol), on the FP32 pipe: the head products are split exactly by FMA and
+// the sums carried by TwoSum, so the result (returned rounded to float) is
+// within 2^-44 of the terms' magnitude of the FP64 value; a head within
+// 1e-12 of zero sends the element pair to the FP64 path.
+__device__ __forceinline__ float plane_df(const float* nh, const float* nl, float oh, float ol, float x, float y,
+                                          float z) {
+  const float p0 = __fmul_rn(nh[0], x), p1 = __fmul_rn(nh[1], y), p2 = __fmul_rn(nh[2], z);
+  const float e0 = __fmaf_rn(nh[0], x, -p0), e1 = __fmaf_rn(nh[1], y, -p1), e2 = __fmaf_rn(nh[2], z, -p2);
+  float s, t1, t2, t3;
+  two_sum(p0, p1, s, t1);
+  two_sum(s, p2, s, t2);
+  two_sum(s, -oh, s, t3);
+  const float tl = __fadd_rn(__fadd_rn(__fmul_rn(nl[0], x), __fmul_rn(nl[1], y)), __fmul_rn(nl[2], z));
+  const float lo = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(e0, e1), e2), __fadd_rn(__fadd_rn(t1, t2), t3)),
+                             __fsub_rn(ol, tl));
+  return __fadd_rn(s, lo);
+}
+
 // Soft-rigid polygon: tet section by the triangle plane (FP64 values s),
 // clipped by the three edge planes.  In FP32 an edge plane whose four tet
 // distances are all certainly positive is inactive (no clip); an active
 // plane's distances are evaluated in FP64 (its position matters to the
 // area), then carried in FP32 and interpolated with the vertices.
-template <class R>
-__device__ int sr_polygon(const TetIn<R>& t, const double s[4], const TriStage& T, V3<R> n, R M, Decide& dc,
+template <class R, class S>
+__device__ int sr_polygon(const TetIn<R>& t, const S s[4], const TriStage& T, V3<R> n, R M, Decide& dc,
                           int& anc, PV<R, 3>* out, PV<R, 3>* tmp) {
   if (!(t.gl > (R)0)) return 0;
   const R cg = dot(n, t.g) / t.gl;
@@ -755,12 +789,22 @@ __device__ int sr_polygon(const TetIn<R>& t, const double s[4], const TriStage& 
     }
     dmax[j] = 0;
     if (active[j]) {
+      if (sizeof(R) == 4) {
+        // double-float: the plane's position matters to the area
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        tv[k].d[j] = (R)(fma(T.en64[j][2], (double)t.X[k].z,
-                             fma(T.en64[j][1], (double)t.X[k].y, T.en64[j][0] * (double)t.X[k].x)) -
-                         T.eo64[j]);
-        dmax[j] = fmax(dmax[j], abs_r(tv[k].d[j]));
+        for (int k = 0; k < 4; ++k) {
+          tv[k].d[j] = (R)plane_df(T.en[j], T.enl[j], T.eo[j], T.eol[j], (float)t.X[k].x, (float)t.X[k].y,
+                                   (float)t.X[k].z);
+          dmax[j] = fmax(dmax[j], abs_r(tv[k].d[j]));
+        }
+      } else {
+        double m[3], eo;
+        tri_edge64(T, j, m, eo);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          tv[k].d[j] = (R)(fma(m[2], (double)t.X[k].z, fma(m[1], (double)t.X[k].y, m[0] * (double)t.X[k].x)) - eo);
+          dmax[j] = fmax(dmax[j], abs_r(tv[k].d[j]));
+        }
       }
     }
   }
@@ -781,13 +825,19 @@ __device__ int sr_polygon(const TetIn<R>& t, const double s[4], const TriStage& 
 }
 
 // Exact-decision fallback of one soft-rigid element pair in FP64 from the
-// stored inputs; returns the vertex count and sets near/gint.
-__device__ __noinline__ int sr_fp64(const StepArgs& a, const TriStage& T, int tet_idx, const double s[4], int& anc,
+// stored inputs (the section values too); returns the vertex count and sets
+// near/gint.
+__device__ __noinline__ int sr_fp64(const StepArgs& a, const TriStage& T, int tet_idx, int& anc,
                                     PV<float, 3>* poly, bool& near, float& gint) {
   TetIn<double> td;
   load_tet(a.tets, tet_idx, td);
   tet_prepare(td);
-  const V3<double> n = mk(T.n64[0], T.n64[1], T.n64[2]);
+  double n64[3], o64;
+  tri_plane64(T, n64, o64);
+  double s[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) s[q] = fma(n64[2], td.X[q].z, fma(n64[1], td.X[q].y, n64[0] * td.X[q].x)) - o64;
+  const V3<double> n = mk(n64[0], n64[1], n64[2]);
   Decide dd;
   PV<double, 3> pd[kMaxPolyV], tmp[kMaxPolyV];
   const int nv = sr_polygon<double>(td, s, T, n, 0.0, dd, anc, pd, tmp);
@@ -799,7 +849,7 @@ __device__ __noinline__ int sr_fp64(const StepArgs& a, const TriStage& T, int te
 
 // FP32 soft-rigid polygon (inlined: its inputs and outputs stay out of
 // local memory where the compiler can keep them in registers).
-__device__ __forceinline__ int sr_poly_f(const TetIn<float>& t, const double* s, const TriStage& T, V3<float> n,
+__device__ __forceinline__ int sr_poly_f(const TetIn<float>& t, const float* s, const TriStage& T, V3<float> n,
                                       float M, Decide& dc, int& anc, PV<float, 3>* out) {
   PV<float, 3> tmp[kMaxPolyV];
   return sr_polygon<float>(t, s, T, n, M, dc, anc, out, tmp);
@@ -875,11 +925,12 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
         jt = j;
         const TetStage& TS = W.tet[i];
         const TriStage& T = W.tri[j];
-        double s[4];
+        float s[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) s[q] = plane64(T.n64, T.o64, TS.X[q][0], TS.X[q][1], TS.X[q][2]);
-        const bool allp = s[0] > kNearTol && s[1] > kNearTol && s[2] > kNearTol && s[3] > kNearTol;
-        const bool alln = s[0] < -kNearTol && s[1] < -kNearTol && s[2] < -kNearTol && s[3] < -kNearTol;
+        for (int q = 0; q < 4; ++q) s[q] = plane_df(T.n, T.nl, T.o, T.ol, TS.X[q][0], TS.X[q][1], TS.X[q][2]);
+        constexpr float tol = (float)kNearTol;
+        const bool allp = s[0] > tol && s[1] > tol && s[2] > tol && s[3] > tol;
+        const bool alln = s[0] < -tol && s[1] < -tol && s[2] < -tol && s[3] < -tol;
         if (allp || alln) break;
         unstage_tet(TS, t);
         n = mk(T.n[0], T.n[1], T.n[2]);
@@ -888,11 +939,15 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
         const int tet_idx = P.s_elem_off + sl * kCluster + i;
         if (dc.unc) {
           bool near;
-          nv = sr_fp64(a, T, tet_idx, s, anc, poly, near, gint);
+          nv = sr_fp64(a, T, tet_idx, anc, poly, near, gint);
           flags = near ? 1 : 0;
         } else if (nv >= 3) {
           gint = dot(t.g, n);
-          if (fabsf(gint) <= 1e-5f * t.gl) gint = grad_along64(a, tet_idx, T.n64[0], T.n64[1], T.n64[2]);
+          if (fabsf(gint) <= 1e-5f * t.gl) {
+            double n64[3], o64;
+            tri_plane64(T, n64, o64);
+            gint = grad_along64(a, tet_idx, n64[0], n64[1], n64[2]);
+          }
         }
         if (nv < 3) break;
         ac.n_poly += 1;
