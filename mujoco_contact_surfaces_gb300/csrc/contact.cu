@@ -100,8 +100,14 @@ __global__ void frames_kernel(StepArgs a) {
     F.xM[i] = a.xpos[3 * P.gm + i];
     F.xN[i] = a.xpos[3 * P.gn + i];
   }
-  for (int i = 0; i < 9; ++i) F.Rf[i] = (float)F.R[i];
-  for (int i = 0; i < 3; ++i) F.tf[i] = (float)F.t[i];
+  for (int i = 0; i < 9; ++i) {
+    F.Rf[i] = (float)F.R[i];
+    F.Rlo[i] = (float)(F.R[i] - (double)F.Rf[i]);
+  }
+  for (int i = 0; i < 3; ++i) {
+    F.tf[i] = (float)F.t[i];
+    F.tlo[i] = (float)(F.t[i] - (double)F.tf[i]);
+  }
   // velocity field v_M - v_N = c + w x p (world), in the soft frame
   V3<double> wM = mk(0.0, 0.0, 0.0), vM = wM, wN = wM, vN = wM;
   if (a.vel) {

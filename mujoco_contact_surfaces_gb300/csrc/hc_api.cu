@@ -180,7 +180,7 @@ struct hc_context {
   int item_cap = 0;
   DevBuf<int> counters;  // see kCnt* below
   int type_units[3][2] = {{0, 0}, {0, 0}, {0, 0}};  // unit ranges per query type
-  DevBuf<hc::Dbl4> tri_plane, tri_edges;
+  DevBuf<hc::DfPlane> tri_plane, tri_edges;
   DevBuf<float4> tri_meta;
   DevBuf<hc::PairOut> pair_out;
   // sensors
@@ -347,8 +347,23 @@ hc_status build_pools(hc_context* c) {
   HC_CUDA(c->tris.upload(tris, s));
   HC_CUDA(c->tet_orig.upload(tet_orig, s));
   HC_CUDA(c->tri_orig.upload(tri_orig, s));
-  HC_CUDA(c->tri_plane.upload(tri_plane, s));
-  HC_CUDA(c->tri_edges.upload(tri_edges, s));
+  // planes as FP32 head and tail (the device rotates them in double-float)
+  auto split = [](const std::vector<hc::Dbl4>& in) {
+    std::vector<hc::DfPlane> out(in.size());
+    for (size_t i = 0; i < in.size(); ++i) {
+      const double d[4] = {in[i].x, in[i].y, in[i].z, in[i].w};
+      float h[4], l[4];
+      for (int k = 0; k < 4; ++k) {
+        h[k] = (float)d[k];
+        l[k] = (float)(d[k] - (double)h[k]);
+      }
+      out[i].hi = make_float4(h[0], h[1], h[2], h[3]);
+      out[i].lo = make_float4(l[0], l[1], l[2], l[3]);
+    }
+    return out;
+  };
+  HC_CUDA(c->tri_plane.upload(split(tri_plane), s));
+  HC_CUDA(c->tri_edges.upload(split(tri_edges), s));
   HC_CUDA(c->tri_meta.upload(tri_meta, s));
   // two float4 (lo, hi) per node
   HC_CUDA(c->nodes.reserve(2 * (size_t)std::max(1, node_total)));

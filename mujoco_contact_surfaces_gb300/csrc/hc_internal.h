@@ -17,6 +17,12 @@
 namespace hc {
 
 // Four doubles, 32-byte aligned (one 32 B load).
+// An FP64 plane (x, y, z, w) as FP32 head and tail per component: head + tail
+// is the double to 2^-48 relative.
+struct alignas(32) DfPlane {
+  float4 hi, lo;
+};
+
 struct alignas(32) Dbl4 {
   double x, y, z, w;
 };
@@ -49,8 +55,10 @@ struct FrameDev {
   double xN[3];         // N origin (world)
   float lin[3];         // relative velocity field in the soft frame:
   float ang[3];         //   v_M - v_N at p = lin + ang x p
-  float Rf[9];          // float copies of R, t
+  float Rf[9];          // float copies of R, t (heads)
   float tf[3];
+  float Rlo[9];         // tails: R - Rf, t - tf (double-float R, t)
+  float tlo[3];
   float Rl[9];          // soft -> sensor0 local frame (rotation, translation)
   float tl[3];
   float Rl1[9];         // soft -> sensor1 local frame

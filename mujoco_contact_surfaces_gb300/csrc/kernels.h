@@ -20,8 +20,8 @@ struct StepArgs {
   const float4* tets;
   const int* tet_orig;
   const float4* tris;
-  const Dbl4* tri_plane;   // body-frame unit normal and offset (FP64)
-  const Dbl4* tri_edges;   // 3 per triangle: body-frame edge planes (FP64)
+  const DfPlane* tri_plane;   // body-frame unit normal and offset (FP64 as head and tail)
+  const DfPlane* tri_edges;   // 3 per triangle: body-frame edge planes
   const float4* tri_meta;     // (min altitude, max edge, max |vertex|, 0)
   const int* tri_orig;
   const float4* nodes;

@@ -680,36 +680,64 @@ struct TriStage {
   int orig, valid;
 };
 
+// Double-float product of two (head, tail) values (the tail-tail product,
+// below 2^-48 of the result, is dropped; unnormalised) and sum (normalised).
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& h, float& l) {
+  h = __fmul_rn(ah, bh);
+  l = __fadd_rn(__fmaf_rn(ah, bh, -h), __fadd_rn(__fmul_rn(ah, bl), __fmul_rn(al, bh)));
+}
+__device__ __forceinline__ void df_sum(float ah, float al, float bh, float bl, float& h, float& l) {
+  float s, e;
+  two_sum(ah, bh, s, e);
+  e = __fadd_rn(e, __fadd_rn(al, bl));
+  h = __fadd_rn(s, e);
+  l = __fsub_rn(e, __fsub_rn(h, s));
+}
+
+// A body-frame plane of the other body moved into the soft frame with the
+// pair's transform: n = R n_b, o = o_b + n . t, in double-float arithmetic
+// on the FP32 pipe (head and tail out).
+__device__ __forceinline__ void df_plane_rotate(const FrameDev& F, const DfPlane& pb, float nh[3], float nl[3],
+                                                float& oh, float& ol) {
+  const float bh[3] = {pb.hi.x, pb.hi.y, pb.hi.z}, bl[3] = {pb.lo.x, pb.lo.y, pb.lo.z};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float h, l, h2, l2;
+    df_mul(F.Rf[3 * k], F.Rlo[3 * k], bh[0], bl[0], h, l);
+    df_mul(F.Rf[3 * k + 1], F.Rlo[3 * k + 1], bh[1], bl[1], h2, l2);
+    df_sum(h, l, h2, l2, h, l);
+    df_mul(F.Rf[3 * k + 2], F.Rlo[3 * k + 2], bh[2], bl[2], h2, l2);
+    df_sum(h, l, h2, l2, nh[k], nl[k]);
+  }
+  float h = pb.hi.w, l = pb.lo.w;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float h2, l2;
+    df_mul(nh[k], nl[k], F.tf[k], F.tlo[k], h2, l2);
+    df_sum(h, l, h2, l2, h, l);
+  }
+  oh = h;
+  ol = l;
+}
+
 __device__ __noinline__ void stage_tri(const StepArgs& a, const PairDev& P, const FrameDev& F, int tj,
                                           TriStage& S) {
   S.valid = 0;
   if (tj >= P.o_n_elem) return;
   const int idx = P.o_elem_off + tj;
-  const Dbl4 pl = a.tri_plane[idx];
   const float4 meta = a.tri_meta[idx];
-  // plane: n = R n_body, o = o_body + n . t (FP64)
-  const V3<double> nd = mat_mul<double>(F.R, mk(pl.x, pl.y, pl.z));
-  const double od = pl.w + nd.x * F.t[0] + nd.y * F.t[1] + nd.z * F.t[2];
-  const V3<float> n = mk((float)nd.x, (float)nd.y, (float)nd.z);
-  S.n[0] = n.x; S.n[1] = n.y; S.n[2] = n.z; S.o = (float)od;
-  S.nl[0] = (float)(nd.x - (double)n.x); S.nl[1] = (float)(nd.y - (double)n.y);
-  S.nl[2] = (float)(nd.z - (double)n.z); S.ol = (float)(od - (double)S.o);
+  // plane: n = R n_body, o = o_body + n . t, in double-float (FP32 pipe)
+  df_plane_rotate(F, a.tri_plane[idx], S.n, S.nl, S.o, S.ol);
+  const V3<float> n = mk(S.n[0], S.n[1], S.n[2]);
   V3<float> Y[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const float4 r = a.tris[3 * (size_t)idx + k];
     Y[k] = mat_mul<float>(F.Rf, mk(r.x, r.y, r.z)) + mk(F.tf[0], F.tf[1], F.tf[2]);
   }
-  // edge planes: en = R en_body, eo = eo_body + en . t (FP64)
+  // edge planes: en = R en_body, eo = eo_body + en . t, in double-float
 #pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    const Dbl4 ep = a.tri_edges[3 * (size_t)idx + j];
-    const V3<double> m = mat_mul<double>(F.R, mk(ep.x, ep.y, ep.z));
-    const double eo = ep.w + m.x * F.t[0] + m.y * F.t[1] + m.z * F.t[2];
-    S.en[j][0] = (float)m.x; S.en[j][1] = (float)m.y; S.en[j][2] = (float)m.z; S.eo[j] = (float)eo;
-    S.enl[j][0] = (float)(m.x - (double)S.en[j][0]); S.enl[j][1] = (float)(m.y - (double)S.en[j][1]);
-    S.enl[j][2] = (float)(m.z - (double)S.en[j][2]); S.eol[j] = (float)(eo - (double)S.eo[j]);
-  }
+  for (int j = 0; j < 3; ++j) df_plane_rotate(F, a.tri_edges[3 * (size_t)idx + j], S.en[j], S.enl[j], S.eo[j], S.eol[j]);
   const float M = fmaxf(meta.z, fmaxf(fabsf(F.tf[0]), fmaxf(fabsf(F.tf[1]), fabsf(F.tf[2]))));
   const float pad = 1e-5f * (M + meta.y) + 1e-7f;
 #pragma unroll
