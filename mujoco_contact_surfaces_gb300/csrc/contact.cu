@@ -196,25 +196,6 @@ __device__ QueryBox make_query(const StepArgs& a, const PairDev& P, const FrameD
   return q;
 }
 
-// Stackless pre-order walk of the heap-numbered tree; calls emit(leaf).
-template <class Emit>
-__device__ __forceinline__ void walk(const float4* nd, int L, int ncl, const QueryBox& q, Emit emit) {
-  int k = 1;
-  while (true) {
-    if (box_test(q, nd[2 * k], nd[2 * k + 1])) {
-      if (k >= L) {
-        if (k - L < ncl) emit(k - L);
-      } else {
-        k = 2 * k;
-        continue;
-      }
-    }
-    while (k & 1) k >>= 1;
-    if (k == 0) break;
-    k += 1;
-  }
-}
-
 __device__ __forceinline__ int warp_incl_scan(int v) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
@@ -245,29 +226,67 @@ __device__ __forceinline__ int block_excl_scan(int v, int* total) {
   return r;
 }
 
+// Stackless pre-order walk of the subtree rooted at r (heap numbering);
+// calls emit(leaf) for the leaves whose boxes pass, left to right.
+template <class Emit>
+__device__ __forceinline__ void walk_sub(const float4* nd, int L, int ncl, const QueryBox& q, int r, Emit emit) {
+  int k = r;
+  while (true) {
+    if (box_test(q, nd[2 * k], nd[2 * k + 1])) {
+      if (k >= L) {
+        if (k - L < ncl) emit(k - L);
+      } else {
+        k = 2 * k;
+        continue;
+      }
+    }
+    while (k != r && (k & 1)) k >>= 1;
+    if (k == r) break;
+    k += 1;
+  }
+}
+
+// A unit's tree is walked by a warp: lane i takes the i-th subtree of the
+// level with min(32, L) nodes (L, the leaf count, is a power of two); the
+// lanes' leaves in lane order are the leaves of a whole pre-order walk.
+__device__ __forceinline__ int lane_root(int L, int lane) {
+  const int w = L < 32 ? L : 32;
+  return lane < w ? w + lane : 0;
+}
+
+constexpr int kBpUnits = kBpBlock / 32;   // units per broadphase block (a warp each)
+
 __global__ void bp_count_kernel(StepArgs a) {
-  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int u = blockIdx.x * kBpUnits + wid;
   int cnt = 0;
   if (u < a.n_units) {
     const int p = a.unit_pair[u];
     const PairDev& P = a.pairs[p];
     const FrameDev& F = a.frames[p];
     if (F.valid) {
-      QueryBox q = make_query(a, P, F, a.unit_cl[u]);
+      const QueryBox q = make_query(a, P, F, a.unit_cl[u]);
       const float4* nd = a.nodes + 2 * (size_t)P.s_node_off;
-      int ncl = (P.s_n_elem + kCluster - 1) / kCluster;
-      walk(nd, P.s_leaves, ncl, q, [&](int) { ++cnt; });
+      const int ncl = (P.s_n_elem + kCluster - 1) / kCluster;
+      const int r = lane_root(P.s_leaves, lane);
+      if (r) walk_sub(nd, P.s_leaves, ncl, q, r, [&](int) { ++cnt; });
     }
-    a.unit_count[u] = cnt;
   }
-  __shared__ int total;
-  int dummy = block_excl_scan(cnt, &total);
-  (void)dummy;
-  if (threadIdx.x == 0) a.block_sum[blockIdx.x] = total;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  __shared__ int wsum[kBpUnits];
+  if (lane == 0) {
+    if (u < a.n_units) a.unit_count[u] = cnt;
+    wsum[wid] = u < a.n_units ? cnt : 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < kBpUnits; ++w) t += wsum[w];
+    a.block_sum[blockIdx.x] = t;
+  }
 }
 
-// Single CTA: exclusive scan of the block sums, total item count, overflow
-// flag, and the work counter reset for the narrow phase.
 __global__ void bp_scan_kernel(StepArgs a) {
   __shared__ int carry;
   __shared__ int tot;
@@ -295,25 +314,33 @@ __global__ void bp_scan_kernel(StepArgs a) {
 }
 
 __global__ void bp_emit_kernel(StepArgs a) {
-  const int u = blockIdx.x * blockDim.x + threadIdx.x;
-  int cnt = u < a.n_units ? a.unit_count[u] : 0;
-  __shared__ int total;
-  int off = block_excl_scan(cnt, &total) + a.block_sum[blockIdx.x];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int u = blockIdx.x * kBpUnits + wid;
+  __shared__ int ucnt[kBpUnits];
+  if (lane == 0) ucnt[wid] = u < a.n_units ? a.unit_count[u] : 0;
+  __syncthreads();
   if (u >= a.n_units) return;
-  a.unit_off[u] = off;
-  if (!cnt) return;
+  int off = a.block_sum[blockIdx.x];
+  for (int w = 0; w < wid; ++w) off += ucnt[w];
+  if (lane == 0) a.unit_off[u] = off;
+  if (!ucnt[wid]) return;
   const int p = a.unit_pair[u];
   const PairDev& P = a.pairs[p];
   const FrameDev& F = a.frames[p];
   const int cl = a.unit_cl[u];
-  QueryBox q = make_query(a, P, F, cl);
+  const QueryBox q = make_query(a, P, F, cl);
   const float4* nd = a.nodes + 2 * (size_t)P.s_node_off;
-  int ncl = (P.s_n_elem + kCluster - 1) / kCluster;
-  int k = off;
-  walk(nd, P.s_leaves, ncl, q, [&](int leaf) {
-    if (k < a.item_cap) a.items[k] = make_int4(p, leaf, cl, 0);
-    ++k;
-  });
+  const int ncl = (P.s_n_elem + kCluster - 1) / kCluster;
+  const int r = lane_root(P.s_leaves, lane);
+  // this lane's leaves follow those of the lanes before it
+  int cnt = 0;
+  if (r) walk_sub(nd, P.s_leaves, ncl, q, r, [&](int) { ++cnt; });
+  int k = off + warp_incl_scan(cnt) - cnt;
+  if (r)
+    walk_sub(nd, P.s_leaves, ncl, q, r, [&](int leaf) {
+      if (k < a.item_cap) a.items[k] = make_int4(p, leaf, cl, 0);
+      ++k;
+    });
 }
 
 #include "narrow.cuh"

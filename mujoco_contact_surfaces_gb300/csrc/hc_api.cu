@@ -1081,7 +1081,8 @@ hc_status hc_set_pairs(hc_context* c, int n_pair, const int* g1, const int* g2, 
   HC_CUDA(c->frames.reserve(std::max(1, n_pair)));
   HC_CUDA(c->pair_out.reserve(std::max(1, n_pair)));
   c->n_units = (int)upair.size();
-  c->n_bp_blocks = std::max(1, (c->n_units + hc::kBpBlock - 1) / hc::kBpBlock);
+  // broadphase: a warp per unit, kBpBlock / 32 units per block
+  c->n_bp_blocks = std::max(1, (c->n_units + hc::kBpBlock / 32 - 1) / (hc::kBpBlock / 32));
   HC_CUDA(c->unit_pair.upload(upair, s));
   HC_CUDA(c->unit_cl.upload(ucl, s));
   HC_CUDA(c->unit_count.reserve(std::max(1, c->n_units)));
