@@ -974,30 +974,42 @@ __global__ void adjoint_reduce_kernel(StepArgs a) {
   const PairDev& P = a.pairs[p];
   const int total = *a.item_total;
   const int b = min(a.unit_off[P.unit_begin], total), e = min(a.unit_off[P.unit_end], total);
-  double v[13];
+  // double-float sums on the FP32 pipe, in a fixed order (lane-strided, then
+  // a fixed butterfly); FP64 from there on
+  float vh[13], vl[13];
 #pragma unroll
-  for (int k = 0; k < 13; ++k) v[k] = 0.0;
+  for (int k = 0; k < 13; ++k) vh[k] = vl[k] = 0.f;
   if (recs_valid(a)) {
     // the pair's records, in pair order
     const int rb = a.item_poly_off[b], re = a.item_poly_off[e];
     for (int i = rb + lane; i < re; i += 32) {
       const float4* g = reinterpret_cast<const float4*>(a.rec_grad + 16 * (size_t)i);
       const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3];
-      v[0] += g0.x; v[1] += g0.y; v[2] += g0.z; v[3] += g0.w;
-      v[4] += g1.x; v[5] += g1.y; v[6] += g1.z; v[7] += g1.w;
-      v[8] += g2.x; v[9] += g2.y; v[10] += g2.z; v[11] += g2.w;
-      v[12] += g3.x;
+      const float x[13] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w, g2.x, g2.y, g2.z, g2.w, g3.x};
+#pragma unroll
+      for (int k = 0; k < 13; ++k) df_add(vh[k], vl[k], x[k], 0.f);
     }
   } else {
-    for (int i = b + lane; i < e; i += 32)
+    for (int i = b + lane; i < e; i += 32) {
+      const double* x = a.adj_item + (size_t)i * 16;
 #pragma unroll
-      for (int k = 0; k < 13; ++k) v[k] += a.adj_item[(size_t)i * 16 + k];
+      for (int k = 0; k < 13; ++k) {
+        const float h = (float)x[k];
+        df_add(vh[k], vl[k], h, (float)(x[k] - (double)h));
+      }
+    }
   }
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1)
 #pragma unroll
-    for (int k = 0; k < 13; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    for (int k = 0; k < 13; ++k) {
+      const float h2 = __shfl_xor_sync(0xffffffffu, vh[k], o), l2 = __shfl_xor_sync(0xffffffffu, vl[k], o);
+      df_add(vh[k], vl[k], h2, l2);
+    }
   if (lane) return;
+  double v[13];
+#pragma unroll
+  for (int k = 0; k < 13; ++k) v[k] = (double)vh[k] + (double)vl[k];
   double* out = a.adj_out + 14 * (size_t)p;   // [M twist 6, N twist 6, dE_M, dE_N]
   for (int k = 0; k < 14; ++k) out[k] = 0.0;
   const FrameDev& F = a.frames[p];

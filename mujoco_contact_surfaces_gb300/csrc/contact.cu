@@ -358,11 +358,14 @@ __global__ void reduce_kernel(StepArgs a) {
   const PairDev& P = a.pairs[p];
   const int total = *a.item_total;
   int b = min(a.unit_off[P.unit_begin], total), e = min(a.unit_off[P.unit_end], total);
-  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // double-float sums on the FP32 pipe (FP64 runs at 1/64 of its rate), in a
+  // fixed order: lane-strided, then a fixed butterfly
+  float vh[8] = {0, 0, 0, 0, 0, 0, 0, 0}, vl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int c[3] = {0, 0, 0};
   for (int i = b + lane; i < e; i += 32) {
     const ItemOut& r = a.item_out[i];
-    for (int k = 0; k < 8; ++k) v[k] += (double)r.hi[k] + (double)r.lo[k];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) df_add(vh[k], vl[k], r.hi[k], r.lo[k]);
     c[0] += r.n_poly; c[1] += r.n_faces; c[2] += r.n_near;
   }
   if (rec_ok(a)) {
@@ -370,20 +373,26 @@ __global__ void reduce_kernel(StepArgs a) {
     const int rb = a.item_poly_off[b], re = a.item_poly_off[e];
     for (int i = rb + lane; i < re; i += 32) {
       const RecOut& r = a.rec_out[i];
-      v[0] += r.F[0]; v[1] += r.F[1]; v[2] += r.F[2];
-      v[3] += r.T[0]; v[4] += r.T[1]; v[5] += r.T[2];
-      v[6] += r.area; v[7] += r.fn0;
+      const float x[8] = {r.F[0], r.F[1], r.F[2], r.T[0], r.T[1], r.T[2], r.area, r.fn0};
+#pragma unroll
+      for (int k = 0; k < 8; ++k) df_add(vh[k], vl[k], x[k], 0.f);
       c[1] += r.n_faces;
     }
   }
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    for (int k = 0; k < 8; ++k) {
+      const float h2 = __shfl_xor_sync(0xffffffffu, vh[k], o), l2 = __shfl_xor_sync(0xffffffffu, vl[k], o);
+      df_add(vh[k], vl[k], h2, l2);
+    }
 #pragma unroll
     for (int k = 0; k < 3; ++k) c[k] += __shfl_xor_sync(0xffffffffu, c[k], o);
   }
   if (lane) return;
+  double v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = (double)vh[k] + (double)vl[k];
   const FrameDev& F = a.frames[p];
   PairOut o;
   V3<double> Fs = mk(v[0], v[1], v[2]), Ts = mk(v[3], v[4], v[5]);
