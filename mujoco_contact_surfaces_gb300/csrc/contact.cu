@@ -452,7 +452,10 @@ __global__ void taxel_kernel(StepArgs a) {
 
 // ---------------------------------------------------------------------------
 cudaError_t init_kernel_attributes() {
-  cudaError_t e = cudaFuncSetAttribute(narrow_sr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
+  cudaError_t e =
+      cudaFuncSetAttribute(narrow_sr_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(narrow_sr_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(taxel_sensor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTaxelSmemBytes);
   if (e != cudaSuccess) return e;
@@ -512,10 +515,14 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   }
   if (ev) cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal);
   if (a.type_unit_end[0] > a.type_unit_begin[0]) {
-    narrow_sr_kernel<<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a); ++n;
+    if (a.recs) narrow_sr_kernel<true><<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a);
+    else narrow_sr_kernel<false><<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a);
+    ++n;
   }
   if (a.type_unit_end[1] > a.type_unit_begin[1]) {
-    narrow_hs_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
+    if (a.recs) narrow_hs_kernel<true><<<a.narrow_grid, 128, 0, s>>>(a);
+    else narrow_hs_kernel<false><<<a.narrow_grid, 128, 0, s>>>(a);
+    ++n;
   }
   if (a.type_unit_end[2] > a.type_unit_begin[2]) {
     narrow_ss_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;

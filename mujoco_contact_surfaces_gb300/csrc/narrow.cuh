@@ -890,6 +890,10 @@ struct SrWarpSmem {
   unsigned short q[kCluster * kCluster];
 };
 
+// kKeep: polygons are kept as records (forces and rays come later from the
+// records) rather than integrated and cast inline; each launch carries only
+// its own output path.
+template <bool kKeep>
 __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -991,14 +995,16 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
         const float gM = P.s_is_m ? gint : INFINITY;
         const float gN = P.s_is_m ? INFINITY : gint;
         // with kept polygons the forces are integrated by rec_forward_kernel
-        if (!a.recs) integrate_forces<3>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN);
+        if constexpr (!kKeep) integrate_forces<3>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN);
         record<3>(a, it.x, poly, nv, t.X[anc], nc, orig_a, orig_b, flags);
       }
       __syncwarp();
       // with kept polygons the rays are cast by rec_forward_kernel
-      if (have && !a.recs) raster_polygon<3>(a, P, F, poly, nv, t.X[anc], nc, t.g);
+      if constexpr (!kKeep) {
+        if (have) raster_polygon<3>(a, P, F, poly, nv, t.X[anc], nc, t.g);
+      }
       __syncwarp();
-      if (a.recs)
+      if constexpr (kKeep)
         keep_polygon<3>(a, have, item, seq, lane, it.x, 0, poly, nv, t.X[have ? anc : 0], n, t.g, gint, t.X,
                         W.tri[jt].en, orig_a, orig_b);
     }
@@ -1048,6 +1054,7 @@ __device__ __noinline__ int hs_fp64(const StepArgs& a, const FrameDev& F, int te
   return nv;
 }
 
+template <bool kKeep>
 __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
   __shared__ TetStage s_tet[kNarrowWarps][kCluster];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1116,13 +1123,15 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
     if (have) {
       const float gM = P.s_is_m ? gint : INFINITY;
       const float gN = P.s_is_m ? INFINITY : gint;
-      if (!a.recs) integrate_forces<1>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN);
+      if constexpr (!kKeep) integrate_forces<1>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN);
       record<1>(a, it.x, poly, nv, t.X[anc], nc, orig_a, -1, flags);
     }
     __syncwarp();
-    if (have && !a.recs) raster_polygon<1>(a, P, F, poly, nv, t.X[anc], nc, t.g);
+    if constexpr (!kKeep) {
+      if (have) raster_polygon<1>(a, P, F, poly, nv, t.X[anc], nc, t.g);
+    }
     __syncwarp();
-    if (a.recs) {
+    if constexpr (kKeep) {
       int seq = 0;
       keep_polygon<1>(a, have, item, seq, lane, it.x, 1, poly, nv, t.X[have ? anc : 0], n, t.g, gint, t.X, nullptr,
                       orig_a, -1);
