@@ -452,11 +452,12 @@ __global__ void taxel_kernel(StepArgs a) {
 
 // ---------------------------------------------------------------------------
 cudaError_t init_kernel_attributes() {
-  cudaError_t e =
-      cudaFuncSetAttribute(narrow_sr_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(narrow_sr_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
-  if (e != cudaSuccess) return e;
+  cudaError_t e = cudaSuccess;
+  for (const void* k : {(const void*)narrow_sr_kernel<true, false>, (const void*)narrow_sr_kernel<false, false>,
+                        (const void*)narrow_sr_kernel<true, true>, (const void*)narrow_sr_kernel<false, true>}) {
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
+    if (e != cudaSuccess) return e;
+  }
   e = cudaFuncSetAttribute(taxel_sensor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTaxelSmemBytes);
   if (e != cudaSuccess) return e;
   // the taxel sensors' grid-count table (a pure function of the step count)
@@ -515,13 +516,25 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   }
   if (ev) cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal);
   if (a.type_unit_end[0] > a.type_unit_begin[0]) {
-    if (a.recs) narrow_sr_kernel<true><<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a);
-    else narrow_sr_kernel<false><<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a);
+    const bool diag = (a.debug & 1) || a.want_polys;
+    if (a.recs) {
+      if (diag) narrow_sr_kernel<true, true><<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a);
+      else narrow_sr_kernel<true, false><<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a);
+    } else {
+      if (diag) narrow_sr_kernel<false, true><<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a);
+      else narrow_sr_kernel<false, false><<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a);
+    }
     ++n;
   }
   if (a.type_unit_end[1] > a.type_unit_begin[1]) {
-    if (a.recs) narrow_hs_kernel<true><<<a.narrow_grid, 128, 0, s>>>(a);
-    else narrow_hs_kernel<false><<<a.narrow_grid, 128, 0, s>>>(a);
+    const bool diag = (a.debug & 1) || a.want_polys;
+    if (a.recs) {
+      if (diag) narrow_hs_kernel<true, true><<<a.narrow_grid, 128, 0, s>>>(a);
+      else narrow_hs_kernel<true, false><<<a.narrow_grid, 128, 0, s>>>(a);
+    } else {
+      if (diag) narrow_hs_kernel<false, true><<<a.narrow_grid, 128, 0, s>>>(a);
+      else narrow_hs_kernel<false, false><<<a.narrow_grid, 128, 0, s>>>(a);
+    }
     ++n;
   }
   if (a.type_unit_end[2] > a.type_unit_begin[2]) {

@@ -891,9 +891,10 @@ struct SrWarpSmem {
 };
 
 // kKeep: polygons are kept as records (forces and rays come later from the
-// records) rather than integrated and cast inline; each launch carries only
-// its own output path.
-template <bool kKeep>
+// records) rather than integrated and cast inline; kDiag: candidate or
+// surface recording is on (hc_get_surface, debug).  Each launch carries only
+// its own output paths.
+template <bool kKeep, bool kDiag>
 __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -996,7 +997,7 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
         const float gN = P.s_is_m ? INFINITY : gint;
         // with kept polygons the forces are integrated by rec_forward_kernel
         if constexpr (!kKeep) integrate_forces<3>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN);
-        record<3>(a, it.x, poly, nv, t.X[anc], nc, orig_a, orig_b, flags);
+        if constexpr (kDiag) record<3>(a, it.x, poly, nv, t.X[anc], nc, orig_a, orig_b, flags);
       }
       __syncwarp();
       // with kept polygons the rays are cast by rec_forward_kernel
@@ -1054,7 +1055,7 @@ __device__ __noinline__ int hs_fp64(const StepArgs& a, const FrameDev& F, int te
   return nv;
 }
 
-template <bool kKeep>
+template <bool kKeep, bool kDiag>
 __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
   __shared__ TetStage s_tet[kNarrowWarps][kCluster];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1124,7 +1125,7 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
       const float gM = P.s_is_m ? gint : INFINITY;
       const float gN = P.s_is_m ? INFINITY : gint;
       if constexpr (!kKeep) integrate_forces<1>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN);
-      record<1>(a, it.x, poly, nv, t.X[anc], nc, orig_a, -1, flags);
+      if constexpr (kDiag) record<1>(a, it.x, poly, nv, t.X[anc], nc, orig_a, -1, flags);
     }
     __syncwarp();
     if constexpr (!kKeep) {
