@@ -707,23 +707,25 @@ __device__ __forceinline__ void rec_rays_adj(const StepArgs& a, const AdjPoly& R
   }
 }
 
+// The pair's sensors (one per geom at most), a side at a time (one copy of
+// the ray code).
 __device__ __forceinline__ void rec_rays(const StepArgs& a, const AdjPoly& R, int dst, int sub, AdjAcc* G) {
   const PairDev& P = a.pairs[R.pair];
   const FrameDev& F = a.frames[R.pair];
-  if (!G) {
-    if (P.sensor0 >= 0) rec_rays_fwd(a, R, dst, 0, P.sensor0, F.Rl, F.tl, sub);
-    if (P.sensor1 >= 0) rec_rays_fwd(a, R, dst, 1, P.sensor1, F.Rl1, F.tl1, sub);
-    return;
+#pragma unroll 1
+  for (int side = 0; side < 2; ++side) {
+    const int sid = side ? P.sensor1 : P.sensor0;
+    if (sid < 0) continue;
+    const float* Rl = side ? F.Rl1 : F.Rl;
+    const float* tl = side ? F.tl1 : F.tl;
+    if (!G) rec_rays_fwd(a, R, dst, side, sid, Rl, tl, sub);
+    else rec_rays_adj(a, R, dst, side, sid, Rl, tl, a.sensors[sid].geom == P.gs, sub, *G);
   }
-  if (P.sensor0 >= 0)
-    rec_rays_adj(a, R, dst, 0, P.sensor0, F.Rl, F.tl, a.sensors[P.sensor0].geom == P.gs, sub, *G);
-  if (P.sensor1 >= 0)
-    rec_rays_adj(a, R, dst, 1, P.sensor1, F.Rl1, F.tl1, a.sensors[P.sensor1].geom == P.gs, sub, *G);
 }
 
 // Forward pass over the kept polygons: forces into the polygon's pair-ordered
 // slot, then the sensors' rays.
-__global__ void __launch_bounds__(128, 4) rec_forward_kernel(StepArgs a) {
+__global__ void __launch_bounds__(128, 5) rec_forward_kernel(StepArgs a) {
   if (!rec_ok(a)) return;   // records incomplete: the step is re-run after growth
   const int n = min(*a.rec_count, a.rec_cap);
   const int lane = threadIdx.x & 31, sub = lane & (kGroup - 1), grp = lane / kGroup;
