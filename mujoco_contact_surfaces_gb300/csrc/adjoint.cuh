@@ -515,6 +515,7 @@ __device__ __forceinline__ void rec_fan_group(const AdjPoly& R, int nv, V3<float
 
 // The lane's share of a kept polygon's forces (its quadrature point).
 // Every lane of the warp calls it (shuffles); `on`: the group holds a polygon.
+template <int kRepr>
 __device__ __forceinline__ void rec_forces_part(const StepArgs& a, const AdjPoly& R, int sub, bool on, Acc& ac) {
   const PairDev& P = a.pairs[R.pair];
   const FrameDev& F = a.frames[R.pair];
@@ -537,7 +538,7 @@ __device__ __forceinline__ void rec_forces_part(const StepArgs& a, const AdjPoly
       pcen += rec_vtx(R, i).w / nv;
     }
   }
-  if (a.repr == 1) {
+  if constexpr (kRepr == 1) {
     if (sub == 0) point_force(ac, F, P.damping, P.mu, a.apply_forces, fabsf(A), anc + c, nc, gM, gN, pcen);
   } else if (sub < nv) {
     const int j = sub + 1 == nv ? 0 : sub + 1;
@@ -725,6 +726,8 @@ __device__ __forceinline__ void rec_rays(const StepArgs& a, const AdjPoly& R, in
 
 // Forward pass over the kept polygons: forces into the polygon's pair-ordered
 // slot, then the sensors' rays.
+// kRepr: the quadrature (0 kTriangle, 1 kPolygon), fixed per launch.
+template <int kRepr>
 __global__ void __launch_bounds__(128, 5) rec_forward_kernel(StepArgs a) {
   if (!rec_ok(a)) return;   // records incomplete: the step is re-run after growth
   const int n = min(*a.rec_count, a.rec_cap);
@@ -743,7 +746,7 @@ __global__ void __launch_bounds__(128, 5) rec_forward_kernel(StepArgs a) {
     const AdjPoly& R = a.recs[on ? r : base];
     Acc ac;
     acc_zero(ac);
-    rec_forces_part(a, R, sub, on, ac);
+    rec_forces_part<kRepr>(a, R, sub, on, ac);
     float v[9] = {ac.F[0], ac.F[1], ac.F[2], ac.T[0], ac.T[1], ac.T[2], ac.area, ac.fn0, (float)ac.n_faces};
 #pragma unroll
     for (int k = 0; k < 9; ++k) v[k] = gsum(v[k]);
@@ -765,6 +768,7 @@ __global__ void __launch_bounds__(128, 5) rec_forward_kernel(StepArgs a) {
 // serial form is wrench_adjoint): lane k reverses the quadrature point of
 // fan triangle k, lane v owns vertex v for the fan reverse and the
 // constraint contraction.  Every lane of the warp calls it (shuffles).
+template <int kRepr>
 __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPoly& R, bool on, int lane, int sub,
                                                  AdjAcc& G) {
   const int nv = on ? R.nv : 0;
@@ -791,7 +795,7 @@ __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPol
   float pbi = 0.f, pbj = 0.f, gbar = 0.f, pcbar = 0.f, Abar = 0.f;
   PointBar b;
   if (live) {
-    if (a.repr == 1) {
+    if constexpr (kRepr == 1) {
       if (sub == 0 && point_reverse(G, F, P.damping, P.mu, gFv, gTv, fabsf(A), anc + c, ns, gMv, gNv, pc, b)) {
         Abar += A < 0.f ? -b.A : b.A;
         cbar = cbar + b.p;
@@ -909,6 +913,7 @@ __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPol
   G.gx[3] += tr.x; G.gx[4] += tr.y; G.gx[5] += tr.z;
 }
 
+template <int kRepr>
 __global__ void __launch_bounds__(128, 4) adjoint_rec_kernel(StepArgs a) {
   if (!recs_valid(a)) return;
   const int n = min(*a.rec_count, a.rec_cap);
@@ -931,7 +936,7 @@ __global__ void __launch_bounds__(128, 4) adjoint_rec_kernel(StepArgs a) {
     __syncwarp();   // the groups enter the shuffled ray preparation together
     if (taxel && on) rec_rays(a, R, dst, sub, &G);
     __syncwarp();
-    if (wrench) rec_wrench_group(a, R, on, lane, sub, G);
+    if (wrench) rec_wrench_group<kRepr>(a, R, on, lane, sub, G);
     float v[13] = {G.gx[0], G.gx[1], G.gx[2], G.gx[3], G.gx[4], G.gx[5], G.glin[0], G.glin[1], G.glin[2],
                    G.gang[0], G.gang[1], G.gang[2], G.gE};
 #pragma unroll

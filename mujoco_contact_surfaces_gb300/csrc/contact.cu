@@ -469,9 +469,9 @@ cudaError_t init_kernel_attributes() {
 }
 
 void record_ctas_per_sm(int* fwd, int* adj) {
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(fwd, rec_forward_kernel, 128, 0) != cudaSuccess || *fwd < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(fwd, rec_forward_kernel<0>, 128, 0) != cudaSuccess || *fwd < 1)
     *fwd = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(adj, adjoint_rec_kernel, 128, 0) != cudaSuccess || *adj < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(adj, adjoint_rec_kernel<0>, 128, 0) != cudaSuccess || *adj < 1)
     *adj = 1;
 }
 
@@ -488,7 +488,9 @@ int launch_adjoint(const StepArgs& a, cudaStream_t s) {
   if (a.use_recs) {
     // kept polygons, in the slots the forward assigned (returns at once if
     // the records overflowed)
-    adjoint_rec_kernel<<<a.rec_adj_grid, 128, 0, s>>>(a); ++n;
+    if (a.repr == 1) adjoint_rec_kernel<1><<<a.rec_adj_grid, 128, 0, s>>>(a);
+    else adjoint_rec_kernel<0><<<a.rec_adj_grid, 128, 0, s>>>(a);
+    ++n;
   }
   if (a.type_unit_end[0] > a.type_unit_begin[0]) {
     adjoint_sr_kernel<<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a); ++n;
@@ -546,7 +548,9 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
     poly_count_kernel<<<a.n_item_blocks, kBpBlock, 0, s>>>(a); ++n;
     poly_scan_kernel<<<1, kBpBlock, 0, s>>>(a); ++n;
     poly_emit_kernel<<<a.n_item_blocks, kBpBlock, 0, s>>>(a); ++n;
-    rec_forward_kernel<<<a.rec_fwd_grid, 128, 0, s>>>(a); ++n;
+    if (a.repr == 1) rec_forward_kernel<1><<<a.rec_fwd_grid, 128, 0, s>>>(a);
+    else rec_forward_kernel<0><<<a.rec_fwd_grid, 128, 0, s>>>(a);
+    ++n;
     if (a.n_tsens > 0) {
       if (a.n_tpairs > 0) {
         taxel_order_kernel<<<a.n_tpairs, kTaxThreads, 0, s>>>(a); ++n;
