@@ -271,10 +271,12 @@ __global__ void __launch_bounds__(128, 4) adjoint_sr_kernel(StepArgs a) {
     unsigned mask = 0;
     const TetStage& me = W.tet[lane];
     if (me.valid) {
+      float mlo[3], mhi[3];
+      tet_box(me, mlo, mhi);
       const int n_o = min(kCluster, P.o_n_elem - oc * kCluster);
       for (int j = 0; j < n_o; ++j) {
         const TriStage& T = W.tri[j];
-        if (!T.valid || !aabb_overlap(me.lo, me.hi, T.lo, T.hi)) continue;
+        if (!T.valid || !aabb_overlap(mlo, mhi, T.lo, T.hi)) continue;
         const float margin = 4e-6f * (me.xmax + fabsf(T.o) + T.Lt);
         if (one_sided32(me.X, T.n, T.o, margin)) continue;
         mask |= 1u << j;

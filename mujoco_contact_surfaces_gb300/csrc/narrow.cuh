@@ -404,9 +404,21 @@ struct TetStage {
   float P[4];
   float g[3];
   float gl, kappa, xmax, pmax;
-  float lo[3], hi[3];
   int orig, valid;
 };
+
+// The padded box of a staged tet (computed where it is needed, by the lane
+// that staged the tet, rather than kept in shared memory).
+__device__ __forceinline__ void tet_box(const TetStage& S, float lo[3], float hi[3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float l = fminf(fminf(S.X[0][i], S.X[1][i]), fminf(S.X[2][i], S.X[3][i]));
+    const float h = fmaxf(fmaxf(S.X[0][i], S.X[1][i]), fmaxf(S.X[2][i], S.X[3][i]));
+    const float pad = 1e-5f * (fabsf(l) + fabsf(h)) + 1e-7f;
+    lo[i] = l - pad;
+    hi[i] = h + pad;
+  }
+}
 
 // (not inlined: the forward and adjoint kernels share one compiled body, so
 // the staged values are bit-identical in both)
@@ -423,14 +435,6 @@ __device__ __noinline__ void stage_tet(const StepArgs& a, const PairDev& P, int 
   }
   S.g[0] = t.g.x; S.g[1] = t.g.y; S.g[2] = t.g.z;
   S.gl = t.gl; S.kappa = t.kappa; S.xmax = t.xmax; S.pmax = t.pmax;
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const float lo = fminf(fminf(S.X[0][i], S.X[1][i]), fminf(S.X[2][i], S.X[3][i]));
-    const float hi = fmaxf(fmaxf(S.X[0][i], S.X[1][i]), fmaxf(S.X[2][i], S.X[3][i]));
-    const float pad = 1e-5f * (fabsf(lo) + fabsf(hi)) + 1e-7f;
-    S.lo[i] = lo - pad;
-    S.hi[i] = hi + pad;
-  }
   S.orig = a.tet_orig[P.s_elem_off + ti];
   S.valid = t.hmin > 0.f ? 1 : 0;
 }
@@ -895,7 +899,7 @@ struct SrWarpSmem {
 // surface recording is on (hc_get_surface, debug).  Each launch carries only
 // its own output paths.
 template <bool kKeep, bool kDiag>
-__global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
+__global__ void __launch_bounds__(128, 5) narrow_sr_kernel(StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   SrWarpSmem& W = reinterpret_cast<SrWarpSmem*>(smem_raw)[wid];
@@ -930,10 +934,12 @@ __global__ void __launch_bounds__(128, 4) narrow_sr_kernel(StepArgs a) {
     unsigned mask = 0;
     const TetStage& me = W.tet[lane];
     if (me.valid) {
+      float mlo[3], mhi[3];
+      tet_box(me, mlo, mhi);
       const int n_o = min(kCluster, P.o_n_elem - oc * kCluster);
       for (int j = 0; j < n_o; ++j) {
         const TriStage& T = W.tri[j];
-        if (!T.valid || !aabb_overlap(me.lo, me.hi, T.lo, T.hi)) continue;
+        if (!T.valid || !aabb_overlap(mlo, mhi, T.lo, T.hi)) continue;
         const float margin = 4e-6f * (me.xmax + fabsf(T.o) + T.Lt);
         if (one_sided32(me.X, T.n, T.o, margin)) continue;
         mask |= 1u << j;
@@ -1302,10 +1308,12 @@ __global__ void __launch_bounds__(128, 4) narrow_ss_kernel(StepArgs a) {
     unsigned mask = 0;
     const TetStage& me = s_tet[wid][lane];
     if (me.valid) {
+      float mlo[3], mhi[3];
+      tet_box(me, mlo, mhi);
       const int n_o = min(kCluster, P.o_n_elem - oc * kCluster);
       for (int j = 0; j < n_o; ++j) {
         const TetBStage& B = s_tb[wid][j];
-        if (B.valid && aabb_overlap(me.lo, me.hi, B.lo, B.hi)) mask |= 1u << j;
+        if (B.valid && aabb_overlap(mlo, mhi, B.lo, B.hi)) mask |= 1u << j;
       }
     }
     const int total = build_queue(mask, s_q[wid], lane);
