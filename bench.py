@@ -314,6 +314,13 @@ def run_gb300(args):
     h2d = hx.nbytes + hm.nbytes + hv.nbytes + hw.nbytes + ht.nbytes
     d2h = n_pair * 6 * 8 + len(s.sensors) * 256 * 4 + n_pair * 14 * 8
     d2h += len(s.sensors) * args.taxel_sensors ** 2 * 4
+    # results land in page-locked host arrays the caller owns (direct copies)
+    pinned = lambda shape, dt: torch.zeros(shape, dtype=dt).pin_memory().numpy()
+    ow = pinned((n_pair, 6), torch.float64)
+    otx = pinned((len(s.sensors) * 256,), torch.float32)
+    ots = pinned((len(s.sensors) * args.taxel_sensors ** 2,), torch.float32)
+    odp = pinned((n_pair, 2, 6), torch.float64)
+    odE = pinned((n_pair, 2), torch.float64)
     e2e_ms = []
     for _ in range(max(3, args.steps // 2)):
         with torch.cuda.stream(stream):
@@ -322,11 +329,11 @@ def run_gb300(args):
         t0 = time.perf_counter()
         eng.set_poses(hx, hm, hv)
         eng.step()
-        eng.wrenches()
-        eng.all_taxels()
+        eng.wrenches(out=ow)
+        eng.all_taxels(out=otx)
         if args.taxel_sensors > 0:
-            eng.all_taxel_sensor_values()
-        eng.adjoint(hw, ht)
+            eng.all_taxel_sensor_values(out=ots)
+        eng.adjoint(hw, ht, out=(odp, odE))
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e = n_pair * world / (max_over_ranks(statistics.median(e2e_ms), world) * 1e-3)
 

@@ -356,7 +356,9 @@ HC_API hc_status hc_set_adjoint_mode(hc_context* ctx, int on);
 /* hc_adjoint on device buffers, asynchronous on the context stream.  The
  * result is n_pair x 14 doubles: [dL/dtwist M (6), N (6), dL/dE_M, dL/dE_N],
  * valid until the next adjoint.  A taxel adjoint needs adjoint mode on
- * before the step.  Covers soft-rigid and half-space pairs.                */
+ * before the step, and where polygons are recomputed (none kept, or
+ * soft-soft pairs) it takes the step's ray samples: one taxel adjoint per
+ * step (hc_adjoint re-runs the step for a second one).                   */
 HC_API hc_status hc_adjoint_device(hc_context* ctx, const double* d_dL_dwrench, const float* d_dL_dtaxel,
                                    const double** d_grad);
 /* Kernels the last adjoint launched. */

@@ -12,7 +12,10 @@ On a soft-rigid or soft-half-space pair the wrench and the taxel pressures
 are exactly linear in the soft modulus (pressure = E * extent, the damping
 and stiffness terms scale with it too: mujoco_contact_surfaces_plugin.cpp:
 394-402, 458), so the modulus enters as a scale of the step at the moduli
-the geoms were registered with.  The backward pass is the engine's
+the geoms were registered with.  On a soft-soft pair the moduli move the
+equal-pressure surface itself, so they are not a scale: the geoms of such
+pairs keep their registered moduli (a different E raises) and the gradient
+in E is the adjoint's exact dL/dE_M, dL/dE_N.  The backward pass is the engine's
 hand-written adjoint (hc_adjoint): twists [dtheta; dx] of both geoms of every
 pair, mapped to ``xpos`` by summing dx over the pairs a geom takes part in
 and to ``rot`` through the left Jacobian of SO(3) at ``rot``.
@@ -73,8 +76,11 @@ class ContactModel:
             km = engine.geom_info(int(m[p])).kind
             soft.append(int(m[p]) if km == 1 else int(n[p]))
         self.soft = torch.as_tensor(np.asarray(soft, np.int64))
-        if any(int(x) == 3 for x in q):
-            raise ValueError("the modulus enters as a scale only on soft-rigid and half-space pairs")
+        # soft-soft pairs: the moduli move the equal-pressure surface, so they
+        # are not a scale; those geoms keep their registered modulus and the
+        # adjoint gives dL/dE of both
+        self.ss = torch.as_tensor(np.asarray([int(x) == 3 for x in q], bool))
+        self.ss_geoms = sorted({int(g) for p in range(engine.n_pair) if self.ss[p] for g in (m[p], n[p])})
         self.n_sensor = len(engine.sensors)
         self.sensor_cells = [engine.sensors[k][0] * engine.sensors[k][1] for k in range(self.n_sensor)]
         self.sensor_pair = list(sensor_pair) if sensor_pair is not None else []
@@ -109,7 +115,10 @@ class ContactFunction(torch.autograd.Function):
         eng.step()
         w = torch.as_tensor(eng.wrenches())
         t = torch.as_tensor(eng.all_taxels().astype(np.float64)) if model.n_sensor else torch.zeros(0, dtype=torch.float64)
-        scale = (E.detach().cpu() / model.E0)[model.soft]           # per pair
+        Ed = E.detach().cpu()
+        if model.ss_geoms and not torch.equal(Ed[model.ss_geoms], model.E0[model.ss_geoms]):
+            raise ValueError("geoms of soft-soft pairs keep their registered modulus")
+        scale = torch.where(model.ss, torch.ones(()), (Ed / model.E0)[model.soft])   # per pair
         w = w * scale[:, None]
         tscale = torch.cat([scale[p].repeat(c) for p, c in zip(model.sensor_pair, model.sensor_cells)]) \
             if model.n_sensor else torch.zeros(0, dtype=torch.float64)
@@ -137,6 +146,10 @@ class ContactFunction(torch.autograd.Function):
             for b, g in enumerate((int(model.m[p]), int(model.n[p]))):
                 gth[g] += dpose[p, b, :3]
                 gx[g] += dpose[p, b, 3:]
+            if model.ss[p]:   # dL/dE_M and dL/dE_N at the registered moduli
+                gE[int(model.m[p])] += dE[p, 0]
+                gE[int(model.n[p])] += dE[p, 1]
+                continue
             # dL/dE = (dL/dout . out(E0)) / E0; the adjoint ran with the
             # upstream scaled by E/E0, so its dE carries that scale
             s = int(model.soft[p])

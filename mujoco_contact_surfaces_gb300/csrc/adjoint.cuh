@@ -18,7 +18,7 @@
 // P:361-368).  upstream: fbar = gF + gT x p (force and torque about the soft
 // origin).
 struct PointBar {
-  float A, p0, gM, gN;
+  float A, p0, gM, gN, d;   // d: dL/d(damping)
   V3<float> p, n;
 };
 
@@ -61,6 +61,7 @@ __device__ __forceinline__ bool point_reverse(AdjAcc& G, const FrameDev& F, floa
   nbar = nbar - vtbar * vn;
   // fn = hp (fn0 - 0.001 k vn)
   const float hbar = h > 0.f ? Lfn * fnb : 0.f;
+  b.d = -hbar * vn;
   const float fn0bar = Lfn * hp;
   const float kbar = -Lfn * hp * 0.001f * vn;
   vnbar += -Lfn * hp * 0.001f * k - damping * hbar;
@@ -218,6 +219,142 @@ __device__ __noinline__ void wrench_adjoint(AdjAcc& G, const StepArgs& a, const 
   }
   G.gx[0] += rot.x; G.gx[1] += rot.y; G.gx[2] += rot.z;
   G.gx[3] += tr.x; G.gx[4] += tr.y; G.gx[5] += tr.z;
+}
+
+// Wrench adjoint of one soft-soft polygon (soft frame = M's; the twist moves
+// N).  The quadrature and force law reverse as in wrench_adjoint; the
+// contraction differs where the section is not a rigid plane:
+//   section row p_M(x) - p_N(x) = 0, m = g_M - g_N, n = m / |m|: under the
+//     twist N's field moves, p_N(y) <- p_N(y - (w x y + v)), so the vertex
+//     obeys n . dx = -g_N . (w x x + v) / |m| and the row adds
+//     -b_0 g_N / |m| to B (b_0 = xbar . a_0 / det as for the other rows);
+//     the moduli enter as n . dx = (-p / E_M dE_M + p / E_N dE_N) / |m|;
+//   faces of tet M fixed, faces of tet N (clip planes) moving rigidly;
+//   normal: dm = -(w x g_N) + g_M dE_M / E_M - g_N dE_N / E_N, and
+//     dn = (I - n n^T) dm / |m|;
+//   gM = g_M . n, gN = -g_N . n (g_N turns with N, both scale with E);
+//   vertex pressure p_M(x): dp = g_M . dx + p dE_M / E_M;
+//   damping d(E_M, E_N) of the combined dissipation: dL/dd summed in ss.gD.
+__device__ __noinline__ void wrench_adjoint_ss(AdjAcc& G, SsAdj& ss, const StepArgs& a, const PairDev& P,
+                                               const FrameDev& F, const float* gF, const float* gT,
+                                               const PV<float, 4>* poly, int nv, V3<float> anc, V3<float> n,
+                                               const V3<float>* face, const V3<float>* clipn, float gMv, float gNv) {
+  V3<float> x[kMaxPolyV], xb[kMaxPolyV];
+  float pv[kMaxPolyV], pb[kMaxPolyV];
+  for (int i = 0; i < nv; ++i) {
+    x[i] = pv_pos(poly[i]);
+    pv[i] = poly[i].p;
+    xb[i] = mk(0.f, 0.f, 0.f);
+    pb[i] = 0.f;
+  }
+  const V3<float> gFv = mk(gF[0], gF[1], gF[2]), gTv = mk(gT[0], gT[1], gT[2]);
+  float A = 0.f, Sp = 0.f;
+  V3<float> Sc = mk(0.f, 0.f, 0.f);
+  for (int i = 1; i + 1 < nv; ++i) {
+    const float ai = 0.5f * dot(cross(x[i] - x[0], x[i + 1] - x[0]), n);
+    A += ai;
+    Sc = Sc + (x[0] + x[i] + x[i + 1]) * (ai * (1.f / 3.f));
+    Sp += ai * (pv[0] + pv[i] + pv[i + 1]) * (1.f / 3.f);
+  }
+  if (A == 0.f) return;
+  const float iA = 1.f / A;
+  const V3<float> c = Sc * iA;
+  const float pc = Sp * iA;
+  V3<float> nbar = mk(0.f, 0.f, 0.f), cbar = mk(0.f, 0.f, 0.f);
+  float gMbar = 0.f, gNbar = 0.f, pcbar = 0.f, Abar = 0.f;
+  PointBar b;
+  if (a.repr == 1) {
+    if (point_reverse(G, F, P.damping, P.mu, gFv, gTv, fabsf(A), anc + c, n, gMv, gNv, pc, b)) {
+      Abar += A < 0.f ? -b.A : b.A;
+      cbar = cbar + b.p;
+      pcbar += b.p0;
+      nbar = nbar + b.n;
+      gMbar += b.gM;
+      gNbar += b.gN;
+      ss.gD += b.d;
+    }
+  } else {
+    for (int i = 0; i < nv; ++i) {
+      const int j = i + 1 == nv ? 0 : i + 1;
+      const V3<float> u = x[i] - c, w = x[j] - c;
+      const V3<float> cr = cross(u, w);
+      const float len = norm(cr);
+      const V3<float> cen = anc + (c + x[i] + x[j]) * (1.f / 3.f);
+      const float p0 = pc / 3.f + pv[i] / 3.f + pv[j] / 3.f;
+      if (!point_reverse(G, F, P.damping, P.mu, gFv, gTv, 0.5f * len, cen, n, gMv, gNv, p0, b)) continue;
+      nbar = nbar + b.n;
+      gMbar += b.gM;
+      gNbar += b.gN;
+      ss.gD += b.d;
+      if (len > 0.f) {
+        const V3<float> crb = cr * (0.5f * b.A / len);
+        const V3<float> ub = cross(w, crb), wb = cross(crb, u);
+        xb[i] = xb[i] + ub;
+        xb[j] = xb[j] + wb;
+        cbar = cbar - ub - wb;
+      }
+      const V3<float> c3 = b.p * (1.f / 3.f);
+      cbar = cbar + c3;
+      xb[i] = xb[i] + c3;
+      xb[j] = xb[j] + c3;
+      const float p3 = b.p0 * (1.f / 3.f);
+      pcbar += p3;
+      pb[i] += p3;
+      pb[j] += p3;
+    }
+  }
+  const V3<float> Scb = cbar * iA;
+  const float Spb = pcbar * iA;
+  Abar -= (dot(cbar, c) + pcbar * pc) * iA;
+  for (int i = 1; i + 1 < nv; ++i) {
+    const V3<float> e1 = x[i] - x[0], e2 = x[i + 1] - x[0];
+    const V3<float> cr = cross(e1, e2);
+    const float ai = 0.5f * dot(cr, n);
+    const float aib = Abar + dot(Scb, x[0] + x[i] + x[i + 1]) * (1.f / 3.f) +
+                      Spb * (pv[0] + pv[i] + pv[i + 1]) * (1.f / 3.f);
+    const V3<float> sx = Scb * (ai * (1.f / 3.f));
+    const float sp = Spb * ai * (1.f / 3.f);
+    xb[0] = xb[0] + sx; xb[i] = xb[i] + sx; xb[i + 1] = xb[i + 1] + sx;
+    pb[0] += sp; pb[i] += sp; pb[i + 1] += sp;
+    nbar = nbar + cr * (0.5f * aib);
+    const V3<float> e1b = cross(e2, n) * (0.5f * aib), e2b = cross(n, e1) * (0.5f * aib);
+    xb[i] = xb[i] + e1b;
+    xb[i + 1] = xb[i + 1] + e2b;
+    xb[0] = xb[0] - e1b - e2b;
+  }
+  // normal and gradient terms
+  nbar = nbar + ss.ga * gMbar - ss.gb * gNbar;
+  const V3<float> np = nbar - n * dot(nbar, n);
+  const float il = 1.f / ss.lm;
+  V3<float> rot = cross(np, ss.gb) * il + cross(n, ss.gb) * gNbar, tr = mk(0.f, 0.f, 0.f);
+  float gEa = (dot(np, ss.ga) * il + gMbar * gMv) * ss.iEa;
+  float gEb = (gNbar * gNv - dot(np, ss.gb) * il) * ss.iEb;
+  for (int v = 0; v < nv; ++v) {
+    const V3<float> xe = xb[v] + ss.ga * pb[v];
+    gEa += pb[v] * pv[v] * ss.iEa;
+    const V3<float> X = anc + x[v];
+    const int l0 = poly[v].lab & 15, l1 = poly[v].lab >> 4;
+    const V3<float> r0 = n;
+    const V3<float> r1 = l0 < 4 ? face[l0] : clipn[l0 - 4];
+    const V3<float> r2 = l1 < 4 ? face[l1] : clipn[l1 - 4];
+    const V3<float> a0 = cross(r1, r2), a1 = cross(r2, r0), a2 = cross(r0, r1);
+    const float det = dot(r0, a0);
+    const float sc = norm(r0) * norm(r1) * norm(r2);
+    if (!(fabsf(det) > 1e-12f * sc)) continue;
+    const float id = 1.f / det;
+    const float b0 = dot(xe, a0) * id;
+    V3<float> B = ss.gb * (-b0 * il);
+    if (l0 >= 4) B = B + r1 * (dot(xe, a1) * id);
+    if (l1 >= 4) B = B + r2 * (dot(xe, a2) * id);
+    tr = tr + B;
+    rot = rot + cross(X, B);
+    gEa -= b0 * pv[v] * il * ss.iEa;
+    gEb += b0 * pv[v] * il * ss.iEb;
+  }
+  G.gx[0] += rot.x; G.gx[1] += rot.y; G.gx[2] += rot.z;
+  G.gx[3] += tr.x; G.gx[4] += tr.y; G.gx[5] += tr.z;
+  G.gE += gEa;
+  ss.gEb += gEb;
 }
 
 __device__ __forceinline__ void adj_reduce_store(const StepArgs& a, const AdjAcc& G, int item, int lane) {
@@ -414,6 +551,81 @@ __global__ void __launch_bounds__(128, 4) adjoint_hs_kernel(StepArgs a) {
     }
     __syncwarp();
     adj_reduce_store(a, G, item, lane);
+  }
+}
+
+// Soft-soft pairs (no records are kept for them): one warp per item repeats
+// the forward's staging and clipping and reverses each polygon.  The item's
+// sums go to adj_item: the 13 of adj_reduce_store, then dL/dE_N and
+// dL/d(damping); here entry 12 is dL/dE_M itself.
+__global__ void __launch_bounds__(128, 2) adjoint_ss_kernel(StepArgs a) {
+  __shared__ TetBStage s_tb[kNarrowWarps][kCluster];
+  __shared__ TetStage s_tet[kNarrowWarps][kCluster];
+  __shared__ unsigned short s_q[kNarrowWarps][kCluster * kCluster];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  while (true) {
+    int ie;
+    const int item = next_item(a, 2, lane, ie);
+    if (item >= ie) break;
+    const int4 it = a.items[item];
+    const PairDev& P = a.pairs[it.x];
+    const FrameDev& F = a.frames[it.x];
+    const float* gF = a.adj_pair + 8 * (size_t)it.x;
+    const float* gT = gF + 3;
+    AdjAcc G;
+    adj_zero(G);
+    SsAdj ss;
+    ss.gEb = ss.gD = 0.f;
+    ss.iEa = 1.f / P.E_s;
+    ss.iEb = 1.f / P.E_o;
+    const int sl = it.y, oc = it.z;
+    const int total = ss_stage_item(a, P, F, sl, oc, s_tb[wid], s_tet[wid], s_q[wid], lane);
+    for (int base = 0; base < total; base += 32) {
+      const int k = base + lane;
+      if (k >= total) continue;
+      const int e = s_q[wid][k];
+      const int i = e & 31, j = e >> 5;
+      const TetStage& TS = s_tet[wid][i];
+      const TetBStage& B = s_tb[wid][j];
+      TetIn<float> t;
+      unstage_tet(TS, t);
+      PV<float, 4> poly[kMaxPolyV];
+      int anc = 0, flags = 0;
+      V3<float> nrm;
+      float gM, gN;
+      const int ta_idx = P.s_elem_off + sl * kCluster + i, tb_idx = P.o_elem_off + oc * kCluster + j;
+      const int nv = ss_element_pair(a, F, t, B, ta_idx, tb_idx, poly, anc, nrm, gM, gN, flags);
+      if (nv < 3) continue;
+      ss.ga = t.g;
+      ss.gb = mk(B.g[0], B.g[1], B.g[2]);
+      ss.lm = norm(ss.ga - ss.gb);
+      // taxel adjoint on the forward polygon (same keys as the forward's)
+      if (a.adj_taxel) {
+        if (P.sensor0 >= 0)
+          raster_keys<4, true>(a, P.sensor0, F.Rl, F.tl, poly, nv, t.X[anc], t.g, nrm,
+                               a.sensors[P.sensor0].geom == P.gs, &G, &ss);
+        if (P.sensor1 >= 0)
+          raster_keys<4, true>(a, P.sensor1, F.Rl1, F.tl1, poly, nv, t.X[anc], t.g, nrm,
+                               a.sensors[P.sensor1].geom == P.gs, &G, &ss);
+      }
+      if (!a.adj_wrench || !a.apply_forces) continue;
+      V3<float> face[4];
+      tet_face_normals(t.X, face);
+      const V3<float> clipn[4] = {mk(B.pn[0][0], B.pn[0][1], B.pn[0][2]), mk(B.pn[1][0], B.pn[1][1], B.pn[1][2]),
+                                  mk(B.pn[2][0], B.pn[2][1], B.pn[2][2]), mk(B.pn[3][0], B.pn[3][1], B.pn[3][2])};
+      wrench_adjoint_ss(G, ss, a, P, F, gF, gT, poly, nv, t.X[anc], nrm, face, clipn, gM, gN);
+    }
+    __syncwarp();
+    adj_reduce_store(a, G, item, lane);
+    float v[2] = {ss.gEb, ss.gD};
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+    if (lane == 0) {
+      a.adj_item[(size_t)item * 16 + 13] = v[0];
+      a.adj_item[(size_t)item * 16 + 14] = v[1];
+    }
   }
 }
 
@@ -706,7 +918,8 @@ __device__ __forceinline__ void rec_rays_adj(const StepArgs& a, const AdjPoly& R
     const float qx = sx[X], qy = sy[Y];
     const float z = raster_height(m0.x, m0.y, m1.y, m1.z, m1.w, qx, qy);
     const float pr = raster_pressure(m0.x, m0.y, m0.z, m0.w, m1.x, qx, qy);
-    sample_adjoint(a, S, Rl, tl, qx, qy, z, pr, X, Y, g, mk(R.n[0], R.n[1], R.n[2]), soft_is_sensor, G);
+    sample_adjoint<false>(a, S, Rl, tl, qx, qy, z, pr, X, Y, g, mk(R.n[0], R.n[1], R.n[2]), soft_is_sensor, G,
+                          nullptr);
   }
 }
 
@@ -985,10 +1198,11 @@ __global__ void adjoint_reduce_kernel(StepArgs a) {
   const int b = min(a.unit_off[P.unit_begin], total), e = min(a.unit_off[P.unit_end], total);
   // double-float sums on the FP32 pipe, in a fixed order (lane-strided, then
   // a fixed butterfly); FP64 from there on
-  float vh[13], vl[13];
+  float vh[15], vl[15];
 #pragma unroll
-  for (int k = 0; k < 13; ++k) vh[k] = vl[k] = 0.f;
-  if (recs_valid(a)) {
+  for (int k = 0; k < 15; ++k) vh[k] = vl[k] = 0.f;
+  const bool ssp = P.query == 3;   // soft-soft: dL/dE_M, dL/dE_N, dL/d(damping) in entries 12-14
+  if (recs_valid(a) && !ssp) {
     // the pair's records, in pair order
     const int rb = a.item_poly_off[b], re = a.item_poly_off[e];
     for (int i = rb + lane; i < re; i += 32) {
@@ -1002,7 +1216,8 @@ __global__ void adjoint_reduce_kernel(StepArgs a) {
     for (int i = b + lane; i < e; i += 32) {
       const double* x = a.adj_item + (size_t)i * 16;
 #pragma unroll
-      for (int k = 0; k < 13; ++k) {
+      for (int k = 0; k < 15; ++k) {
+        if (k >= 13 && !ssp) break;
         const float h = (float)x[k];
         df_add(vh[k], vl[k], h, (float)(x[k] - (double)h));
       }
@@ -1011,14 +1226,14 @@ __global__ void adjoint_reduce_kernel(StepArgs a) {
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1)
 #pragma unroll
-    for (int k = 0; k < 13; ++k) {
+    for (int k = 0; k < 15; ++k) {
       const float h2 = __shfl_xor_sync(0xffffffffu, vh[k], o), l2 = __shfl_xor_sync(0xffffffffu, vl[k], o);
       df_add(vh[k], vl[k], h2, l2);
     }
   if (lane) return;
-  double v[13];
+  double v[15];
 #pragma unroll
-  for (int k = 0; k < 13; ++k) v[k] = (double)vh[k] + (double)vl[k];
+  for (int k = 0; k < 15; ++k) v[k] = (double)vh[k] + (double)vl[k];
   double* out = a.adj_out + 14 * (size_t)p;   // [M twist 6, N twist 6, dE_M, dE_N]
   for (int k = 0; k < 14; ++k) out[k] = 0.0;
   const FrameDev& F = a.frames[p];
@@ -1068,8 +1283,15 @@ __global__ void adjoint_reduce_kernel(StepArgs a) {
   go[0] += thO.x; go[1] += thO.y; go[2] += thO.z; go[3] += xO.x; go[4] += xO.y; go[5] += xO.z;
   gm[3] += xM.x; gm[4] += xM.y; gm[5] += xM.z;
   gn[3] += xN.x; gn[4] += xN.y; gn[5] += xN.z;
-  // modulus: soft-rigid / half-space wrench and taxels are linear in E_s
-  if (P.query != 3 && P.E_s > 0.f) {
+  // modulus: soft-soft sums hold dL/dE_M and dL/dE_N themselves, plus the
+  // damping term (d = (E_N d_M + E_M d_N) / (E_M + E_N))
+  if (ssp) {
+    out[12] = v[12] + v[14] * (double)P.dd_dEs;
+    out[13] = v[13] + v[14] * (double)P.dd_dEo;
+    return;
+  }
+  // soft-rigid / half-space wrench and taxels are linear in E_s
+  if (P.E_s > 0.f) {
     double dE = v[12];
     if (a.adj_wrench) {
       const double* aw = a.adj_wrench + 6 * (size_t)p;

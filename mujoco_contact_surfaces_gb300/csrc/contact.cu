@@ -498,6 +498,9 @@ int launch_adjoint(const StepArgs& a, cudaStream_t s) {
   if (a.type_unit_end[1] > a.type_unit_begin[1]) {
     adjoint_hs_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
   }
+  if (a.type_unit_end[2] > a.type_unit_begin[2]) {
+    adjoint_ss_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
+  }
   adjoint_reduce_kernel<<<(a.n_pair * 32 + 127) / 128, 128, 0, s>>>(a); ++n;
   return n;
 }

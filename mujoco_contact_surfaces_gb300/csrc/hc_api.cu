@@ -212,6 +212,9 @@ struct hc_context {
   // adjoint
   bool adjoint_mode = false;   // steps keep the won taxel samples
   bool samples_dirty = false;  // the sample buffer holds a kept step's hits
+  bool step_checked = false;  // the last step's status word was read and clean
+  bool samples_used = false;   // a taxel adjoint consumed some of them (recomputed
+                               // polygons take their samples once: exact ties)
   DevBuf<float> adj_pair, adj_taxel;
   DevBuf<double> adj_item, adj_out, adj_wrench;
   int adj_launches = 0;
@@ -653,6 +656,7 @@ hc_status run_step(hc_context* c, int want_polys, int want_pair) {
   }
   hc::StepArgs a = make_args(c, want_polys, want_pair);
   c->recs_step = a.recs != nullptr;
+  c->step_checked = false;
   HC_CUDA(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(int), c->stream));
   // samples kept by an earlier step and not consumed by an adjoint
   if (c->samples_dirty && c->samples.n) {
@@ -660,6 +664,7 @@ hc_status run_step(hc_context* c, int want_polys, int want_pair) {
     c->samples_dirty = false;
   }
   if (c->adjoint_mode && c->n_cells > 0) c->samples_dirty = true;
+  c->samples_used = false;
   // With timing on, event records between the stages are part of the
   // launch sequence (and of the captured graph).
   cudaEvent_t* ev = c->timing && !want_polys ? c->ev : nullptr;
@@ -685,12 +690,17 @@ hc_status run_step(hc_context* c, int want_polys, int want_pair) {
 }
 
 // Check the status word; on item overflow grow the capacity and re-run.
+// Once a step has checked clean, later calls return at once.
 hc_status finish_step(hc_context* c) {
+  if (c->step_checked) return HC_OK;
   for (int attempt = 0; attempt < 4; ++attempt) {
     int cnt[8];
     HC_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
     HC_CUDA(cudaStreamSynchronize(c->stream));
-    if (!(cnt[kCntStatus] & 9)) return HC_OK;
+    if (!(cnt[kCntStatus] & 9)) {
+      c->step_checked = true;
+      return HC_OK;
+    }
     if (cnt[kCntStatus] & 8) {
       // too many polygons for the records (rays and adjoint): grow, re-run
       const int want = std::max(2 * c->rec_cap, cnt[kCntRec] + cnt[kCntRec] / 4 + 1024);
@@ -1041,6 +1051,11 @@ hc_status hc_set_pairs(hc_context* c, int n_pair, const int* g1, const int* g2, 
       p.mu = (float)(ma + mb == 0 ? 0.0 : 2 * ma * mb / (ma + mb));
       p.E_s = (float)S->cs5[0];
       p.E_o = O->kind == HC_SOFT ? (float)O->cs5[0] : 0.f;
+      if (p.query == HC_QUERY_SOFT_SOFT) {   // S = M, O = N
+        const double den = (EM + EN) * (EM + EN);
+        p.dd_dEs = (float)(EN * (dN - dM) / den);
+        p.dd_dEo = (float)(EM * (dM - dN) / den);
+      }
       int ns = 0;
       for (size_t k = 0; k < c->sensors.size() && ns < 2; ++k)
         if (c->sensors[k].geom == g1[i] || c->sensors[k].geom == g2[i]) {
@@ -1221,9 +1236,10 @@ hc_status hc_get_wrenches(hc_context* c, double* wrench) {
   if (hc_status st = finish_step(c)) return st;
   size_t n = c->pairs_h.size();
   if (!wrench || !n) return HC_OK;
-  std::vector<hc::PairOut> o(n);
-  HC_CUDA(cudaMemcpy(o.data(), c->pair_out.p, n * sizeof(hc::PairOut), cudaMemcpyDeviceToHost));
-  for (size_t i = 0; i < n; ++i) memcpy(wrench + 6 * i, o[i].wrench, 6 * sizeof(double));
+  // the wrench of each pair record, straight into the caller's rows
+  HC_CUDA(cudaMemcpy2DAsync(wrench, 6 * sizeof(double), c->pair_out.p, sizeof(hc::PairOut), 6 * sizeof(double), n,
+                            cudaMemcpyDeviceToHost, c->stream));
+  HC_CUDA(cudaStreamSynchronize(c->stream));
   return HC_OK;
 }
 
@@ -1595,8 +1611,10 @@ hc_status hc_get_taxels_all(hc_context* c, float* out, int64_t n_floats) {
   if (c->stepped) {
     if (hc_status st = finish_step(c)) return st;
   }
-  if (c->n_cells)
-    HC_CUDA(cudaMemcpy(out, c->taxels.p, (size_t)c->n_cells * sizeof(float), cudaMemcpyDeviceToHost));
+  if (c->n_cells) {
+    HC_CUDA(cudaMemcpyAsync(out, c->taxels.p, (size_t)c->n_cells * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+  }
   return HC_OK;
 }
 
@@ -1726,8 +1744,6 @@ hc_status hc_set_adjoint_mode(hc_context* c, int on) {
 
 // Launch the adjoint on device inputs; leaves n_pair x 14 doubles in adj_out.
 static hc_status adjoint_launch(hc_context* c, const double* d_dw, const float* d_dt) {
-  for (const auto& p : c->pairs_h)
-    if (p.query == HC_QUERY_SOFT_SOFT) return fail(HC_ERR_UNSUPPORTED, "the adjoint covers soft-rigid and half-space pairs");
   if (!c->stepped) return fail(HC_ERR_NOT_READY, "no step has run");
   HC_CUDA(cudaSetDevice(c->device));
   const int n_pair = (int)c->pairs_h.size();
@@ -1758,14 +1774,18 @@ static hc_status adjoint_launch(hc_context* c, const double* d_dw, const float* 
   }
   c->adj_launches = hc::launch_adjoint(a, c->stream);
   HC_CUDA(cudaGetLastError());
-  // the samples stay as the step left them (the next step clears them)
+  // Kept polygons find their samples by slot key and leave them as the step
+  // left them (the next step clears them); recomputed ones (no polygons
+  // kept, soft-soft pairs) take each won sample once, so a further taxel
+  // adjoint of this step needs the step again.
+  if (a.adj_taxel && (!c->recs_step || c->type_units[2][1] > c->type_units[2][0])) c->samples_used = true;
   return HC_OK;
 }
 
 // Make sure the last step's won samples are available for a taxel adjoint.
 static hc_status ensure_kept_samples(hc_context* c) {
   if (hc_status st = finish_step(c)) return st;
-  if (c->samples_dirty || c->n_cells == 0) return HC_OK;
+  if ((c->samples_dirty && !c->samples_used) || c->n_cells == 0) return HC_OK;
   bool was = c->adjoint_mode;
   c->adjoint_mode = true;
   invalidate_graph(c);
@@ -1802,15 +1822,15 @@ hc_status hc_adjoint(hc_context* c, const double* dL_dwrench, const float* dL_dt
     d_dt = c->adj_taxel.p;
   }
   if (hc_status st = adjoint_launch(c, d_dw, d_dt)) return st;
-  std::vector<double> out(14 * (size_t)std::max(1, n_pair));
-  if (n_pair)
-    HC_CUDA(cudaMemcpyAsync(out.data(), c->adj_out.p, 14 * (size_t)n_pair * sizeof(double), cudaMemcpyDeviceToHost,
-                            c->stream));
+  // rows of 14 doubles per pair: the 12 twist terms and the 2 moduli terms
+  // straight into the caller's arrays
+  if (n_pair && dL_dpose)
+    HC_CUDA(cudaMemcpy2DAsync(dL_dpose, 12 * sizeof(double), c->adj_out.p, 14 * sizeof(double), 12 * sizeof(double),
+                              n_pair, cudaMemcpyDeviceToHost, c->stream));
+  if (n_pair && dL_dE)
+    HC_CUDA(cudaMemcpy2DAsync(dL_dE, 2 * sizeof(double), c->adj_out.p + 12, 14 * sizeof(double), 2 * sizeof(double),
+                              n_pair, cudaMemcpyDeviceToHost, c->stream));
   HC_CUDA(cudaStreamSynchronize(c->stream));
-  for (int p = 0; p < n_pair; ++p) {
-    if (dL_dpose) memcpy(dL_dpose + 12 * (size_t)p, &out[14 * (size_t)p], 12 * sizeof(double));
-    if (dL_dE) dL_dE[2 * p] = out[14 * (size_t)p + 12], dL_dE[2 * p + 1] = out[14 * (size_t)p + 13];
-  }
   return HC_OK;
 }
 
@@ -1819,6 +1839,9 @@ hc_status hc_adjoint_device(hc_context* c, const double* d_dL_dwrench, const flo
   if (hc_status st = need(c)) return st;
   if (d_dL_dtaxel && !c->samples_dirty && c->n_cells > 0)
     return fail(HC_ERR_NOT_READY, "taxel adjoint needs hc_set_adjoint_mode(ctx, 1) before the step");
+  if (d_dL_dtaxel && c->samples_used && c->n_cells > 0)
+    return fail(HC_ERR_NOT_READY, "a taxel adjoint of this step already took the samples of its recomputed polygons; "
+                                  "step again (hc_adjoint does so itself)");
   if (hc_status st = adjoint_launch(c, d_dL_dwrench, d_dL_dtaxel)) return st;
   if (d_grad) *d_grad = c->adj_out.p;
   return HC_OK;

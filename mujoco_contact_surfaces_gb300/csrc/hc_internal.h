@@ -43,6 +43,7 @@ struct PairDev {
   int unit_begin, unit_end;                         // broadphase units
   float damping, mu;
   float E_s, E_o;       // moduli (E_o = 0 for rigid)
+  float dd_dEs, dd_dEo; // soft-soft: derivatives of the combined damping by E_s, E_o
 };
 
 // Per-step frame data of one pair (computed on the device from the poses).

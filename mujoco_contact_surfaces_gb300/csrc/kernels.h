@@ -141,7 +141,7 @@ void record_ctas_per_sm(int* fwd, int* adj);
 // Returns the number of kernels launched.
 int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev /* 7 or null */);
 
-// Adjoint of the last step (soft-rigid and half-space pairs).  Returns the
+// Adjoint of the last step (all query types).  Returns the
 // number of kernels launched.
 int launch_adjoint(const StepArgs& a, cudaStream_t s);
 

@@ -70,7 +70,18 @@ struct AdjAcc {
   float gx[6];     // dL/dxi: twist (w, v) of the other body in the soft frame
   float glin[3];   // dL/dlin of the velocity field v = lin + ang x p
   float gang[3];   // dL/dang
-  float gE;        // sum of dL/dp * p over won samples (taxel part of dL/dE * E)
+  float gE;        // sum of dL/dp * p over won samples (taxel part of dL/dE * E);
+                   // soft-soft: dL/dE_M itself
+};
+
+// Soft-soft terms of the adjoint.  The section plane p_M = p_N moves with
+// N's field and with both moduli, so the adjoint needs both gradients (soft
+// frame, M's), |g_M - g_N|, 1/E of both geoms; it sums dL/dE_N and
+// dL/d(damping) here (the combined dissipation depends on E_M / E_N).
+struct SsAdj {
+  V3<float> ga, gb;
+  float lm, iEa, iEb;
+  float gEb, gD;
 };
 
 // One polygon prepared for ray binning on one sensor (sensor frame): vertex
@@ -216,15 +227,34 @@ __device__ __forceinline__ bool raster_probe(const RasterPoly& rp, const SensorD
 
 // Adjoint of one won sample: dL/dp = pbar at the hit (qx, qy, z) of the
 // sensor frame.
+template <bool kSS>
 __device__ __forceinline__ void sample_adjoint(const StepArgs& a, const SensorDev& S, const float* Rl,
                                                const float* tl, float qx, float qy, float z, float pr, int X, int Y,
-                                               V3<float> g_soft, V3<float> n_tri, int soft_is_sensor, AdjAcc& G) {
+                                               V3<float> g_soft, V3<float> n_tri, int soft_is_sensor, AdjAcc& G,
+                                               SsAdj* ss) {
   // dL/dp at this sample: cell (X / sr, Y / sr), window weight of (X % sr, Y % sr)
   const float w = a.weights[S.weight_off + (X % S.sr) * S.sr + (Y % S.sr)];
   const float pbar = a.adj_taxel[S.taxel_off + X / S.sr + S.cy * (Y / S.sr)] * w * S.rmean;
   if (pbar == 0.f) return;
-  G.gE += pbar * pr;
   const V3<float> xs = mat_tmul<float>(Rl, mk(qx, qy, z) - mk(tl[0], tl[1], tl[2]));   // hit point, soft frame
+  if (kSS) {
+    // hit x = o + t D on p_M - p_N = 0 (m = g_M - g_N), reading p = p_M(x).
+    // Rays on N (move with it): dp = kb g_M . (w x x + v); rays on M:
+    // dp = -ka g_N . (w x x + v), with ka = g_M.D / m.D, kb = -g_N.D / m.D
+    // (ka + kb = 1).  Moduli: dp/dE_M = kb p / E_M, dp/dE_N = ka p / E_N.
+    const V3<float> D = mk(-Rl[6], -Rl[7], -Rl[8]);
+    const float mD = dot(ss->ga - ss->gb, D);
+    if (!(fabsf(mD) > 0.f)) return;
+    const float ka = dot(ss->ga, D) / mD, kb = -dot(ss->gb, D) / mD;
+    G.gE += pbar * pr * kb * ss->iEa;
+    ss->gEb += pbar * pr * ka * ss->iEb;
+    const V3<float> gv = soft_is_sensor ? ss->gb * (-ka) : ss->ga * kb;
+    const V3<float> wx = cross(xs, gv);
+    G.gx[0] += pbar * wx.x; G.gx[1] += pbar * wx.y; G.gx[2] += pbar * wx.z;
+    G.gx[3] += pbar * gv.x; G.gx[4] += pbar * gv.y; G.gx[5] += pbar * gv.z;
+    return;
+  }
+  G.gE += pbar * pr;
   if (!soft_is_sensor) {
     // rays and plane move with the other body: dp = g . (w x x + v)
     const V3<float> wx = cross(xs, g_soft);
@@ -243,10 +273,10 @@ __device__ __forceinline__ void sample_adjoint(const StepArgs& a, const SensorDe
   }
 }
 
-template <int ND>
+template <int ND, bool kSS = false>
 __device__ __noinline__ void raster_keys(const StepArgs& a, int sid, const float* Rl, const float* tl,
                                          const PV<float, ND>* v, int nv, V3<float> anc, V3<float> g_soft,
-                                         V3<float> n_tri, int soft_is_sensor, AdjAcc* G) {
+                                         V3<float> n_tri, int soft_is_sensor, AdjAcc* G, SsAdj* ss = nullptr) {
   const SensorDev S = a.sensors[sid];
   RasterPoly rp;
   if (!raster_prepare(a, S, Rl, tl, nv, anc, g_soft,
@@ -267,7 +297,7 @@ __device__ __noinline__ void raster_keys(const StepArgs& a, int sid, const float
         continue;
       }
       if (atomicCAS(&smp[si], key, ~0ull) != key) continue;
-      sample_adjoint(a, S, Rl, tl, qx, sy[Y], z, pr, X, Y, g_soft, n_tri, soft_is_sensor, *G);
+      sample_adjoint<kSS>(a, S, Rl, tl, qx, sy[Y], z, pr, X, Y, g_soft, n_tri, soft_is_sensor, *G, ss);
     }
   }
 }
@@ -1282,6 +1312,75 @@ __device__ __noinline__ int ss_fp64(const StepArgs& a, const FrameDev& F, int ta
   return nv;
 }
 
+// One soft-soft element pair: tet A (soft frame) against the staged tet B.
+// Its polygon relative to A's vertex `anc`, the unit normal (g_A - g_B) / |.|
+// (out of N into M), gM = g_A . n and gN = -g_B . n, with the FP64 pass where
+// the FP32 decisions or gradient terms are uncertain (`flags` 1: a value
+// was near zero in FP64).  The adjoint recomputes the forward's polygons
+// (and so its ray keys) with this same code.  Returns the vertex count.
+__device__ __forceinline__ int ss_element_pair(const StepArgs& a, const FrameDev& F, const TetIn<float>& t,
+                                               const TetBStage& B, int ta_idx, int tb_idx, PV<float, 4>* poly,
+                                               int& anc, V3<float>& nrm, float& gM, float& gN, int& flags) {
+  const V3<float> gb = mk(B.g[0], B.g[1], B.g[2]);
+  const V3<float> m = t.g - gb;
+  const float lm = norm(m);
+  if (!(lm > 0.f) || !(t.gl > 0.f) || !(B.gl > 0.f)) return 0;
+  double s[4];
+  const double il = 1.0 / (double)lm;
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    s[q] = ((double)t.P[q] - (fma(B.g64[2], (double)t.X[q].z, fma(B.g64[1], (double)t.X[q].y, B.g64[0] * (double)t.X[q].x)) +
+                              B.c64)) * il;
+  const bool allp = s[0] > kNearTol && s[1] > kNearTol && s[2] > kNearTol && s[3] > kNearTol;
+  const bool alln = s[0] < -kNearTol && s[1] < -kNearTol && s[2] < -kNearTol && s[3] < -kNearTol;
+  if (allp || alln) return 0;
+  const V3<float> pn[4] = {mk(B.pn[0][0], B.pn[0][1], B.pn[0][2]), mk(B.pn[1][0], B.pn[1][1], B.pn[1][2]),
+                           mk(B.pn[2][0], B.pn[2][1], B.pn[2][2]), mk(B.pn[3][0], B.pn[3][1], B.pn[3][2])};
+  nrm = m * (1.f / lm);
+  PV<float, 4> tmp[kMaxPolyV];
+  Decide dc;
+  anc = 0;
+  int nv = ss_polygon<float>(t, s, gb, B.gl, nrm, lm, pn, B.po, B.M, B.h, B.kappa, dc, anc, poly, tmp);
+  gM = dot(t.g, nrm);
+  gN = -dot(gb, nrm);
+  flags = 0;
+  if (dc.unc || (nv >= 3 && (fabsf(gM) <= 1e-5f * t.gl || fabsf(gN) <= 1e-5f * B.gl))) {
+    bool near;
+    nv = ss_fp64(a, F, ta_idx, tb_idx, s, dc.unc, anc, poly, near, nrm, gM, gN, nv);
+    flags = near ? 1 : 0;
+  }
+  return nv;
+}
+
+// Stages one soft-soft item in the warp's shared memory (its 32 A tets and,
+// in A's frame, 32 B tets) and queues the element pairs whose boxes
+// overlap.  Returns the queue length (the warp is synchronised).
+__device__ __forceinline__ int ss_stage_item(const StepArgs& a, const PairDev& P, const FrameDev& F, int sl, int oc,
+                                             TetBStage* tb, TetStage* tet, unsigned short* q, int lane) {
+  if (F.valid) {
+    stage_tetb(a, P, F, oc * kCluster + lane, tb[lane]);
+    stage_tet(a, P, sl * kCluster + lane, tet[lane]);
+  } else {
+    tb[lane].valid = 0;
+    tet[lane].valid = 0;
+  }
+  __syncwarp();
+  unsigned mask = 0;
+  const TetStage& me = tet[lane];
+  if (me.valid) {
+    float mlo[3], mhi[3];
+    tet_box(me, mlo, mhi);
+    const int n_o = min(kCluster, P.o_n_elem - oc * kCluster);
+    for (int j = 0; j < n_o; ++j) {
+      const TetBStage& B = tb[j];
+      if (B.valid && aabb_overlap(mlo, mhi, B.lo, B.hi)) mask |= 1u << j;
+    }
+  }
+  const int total = build_queue(mask, q, lane);
+  __syncwarp();
+  return total;
+}
+
 __global__ void __launch_bounds__(128, 4) narrow_ss_kernel(StepArgs a) {
   __shared__ TetBStage s_tb[kNarrowWarps][kCluster];
   __shared__ TetStage s_tet[kNarrowWarps][kCluster];
@@ -1297,27 +1396,7 @@ __global__ void __launch_bounds__(128, 4) narrow_ss_kernel(StepArgs a) {
     Acc ac;
     acc_zero(ac);
     const int sl = it.y, oc = it.z;
-    if (F.valid) {
-      stage_tetb(a, P, F, oc * kCluster + lane, s_tb[wid][lane]);
-      stage_tet(a, P, sl * kCluster + lane, s_tet[wid][lane]);
-    } else {
-      s_tb[wid][lane].valid = 0;
-      s_tet[wid][lane].valid = 0;
-    }
-    __syncwarp();
-    unsigned mask = 0;
-    const TetStage& me = s_tet[wid][lane];
-    if (me.valid) {
-      float mlo[3], mhi[3];
-      tet_box(me, mlo, mhi);
-      const int n_o = min(kCluster, P.o_n_elem - oc * kCluster);
-      for (int j = 0; j < n_o; ++j) {
-        const TetBStage& B = s_tb[wid][j];
-        if (B.valid && aabb_overlap(mlo, mhi, B.lo, B.hi)) mask |= 1u << j;
-      }
-    }
-    const int total = build_queue(mask, s_q[wid], lane);
-    __syncwarp();
+    const int total = ss_stage_item(a, P, F, sl, oc, s_tb[wid], s_tet[wid], s_q[wid], lane);
     for (int base = 0; base < total; base += 32) {
       const int k = base + lane;
       if (k >= total) continue;
@@ -1327,35 +1406,12 @@ __global__ void __launch_bounds__(128, 4) narrow_ss_kernel(StepArgs a) {
       const TetBStage& B = s_tb[wid][j];
       TetIn<float> t;
       unstage_tet(TS, t);
-      const V3<float> gb = mk(B.g[0], B.g[1], B.g[2]);
-      const V3<float> m = t.g - gb;
-      const float lm = norm(m);
-      if (!(lm > 0.f) || !(t.gl > 0.f) || !(B.gl > 0.f)) continue;
-      double s[4];
-      const double il = 1.0 / (double)lm;
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        s[q] = ((double)t.P[q] - (fma(B.g64[2], (double)t.X[q].z,
-                                      fma(B.g64[1], (double)t.X[q].y, B.g64[0] * (double)t.X[q].x)) +
-                                  B.c64)) * il;
-      const bool allp = s[0] > kNearTol && s[1] > kNearTol && s[2] > kNearTol && s[3] > kNearTol;
-      const bool alln = s[0] < -kNearTol && s[1] < -kNearTol && s[2] < -kNearTol && s[3] < -kNearTol;
-      if (allp || alln) continue;
-      const V3<float> pn[4] = {mk(B.pn[0][0], B.pn[0][1], B.pn[0][2]), mk(B.pn[1][0], B.pn[1][1], B.pn[1][2]),
-                               mk(B.pn[2][0], B.pn[2][1], B.pn[2][2]), mk(B.pn[3][0], B.pn[3][1], B.pn[3][2])};
-      V3<float> nrm = m * (1.f / lm);
-      PV<float, 4> poly[kMaxPolyV], tmp[kMaxPolyV];
-      Decide dc;
-      int anc = 0;
-      int nv = ss_polygon<float>(t, s, gb, B.gl, nrm, lm, pn, B.po, B.M, B.h, B.kappa, dc, anc, poly, tmp);
-      float gM = dot(t.g, nrm), gN = -dot(gb, nrm);
-      int flags = 0;
+      PV<float, 4> poly[kMaxPolyV];
+      int anc = 0, flags = 0;
+      V3<float> nrm;
+      float gM, gN;
       const int ta_idx = P.s_elem_off + sl * kCluster + i, tb_idx = P.o_elem_off + oc * kCluster + j;
-      if (dc.unc || (nv >= 3 && (fabsf(gM) <= 1e-5f * t.gl || fabsf(gN) <= 1e-5f * B.gl))) {
-        bool near;
-        nv = ss_fp64(a, F, ta_idx, tb_idx, s, dc.unc, anc, poly, near, nrm, gM, gN, nv);
-        flags = near ? 1 : 0;
-      }
+      const int nv = ss_element_pair(a, F, t, B, ta_idx, tb_idx, poly, anc, nrm, gM, gN, flags);
       if (nv < 3) continue;
       ac.n_poly += 1;
       ac.n_near += flags;

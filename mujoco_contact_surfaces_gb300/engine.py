@@ -13,6 +13,15 @@ import numpy as np
 from . import _lib as L
 
 
+def _out(out, shape, dtype):
+    """A new zeroed array, or the caller's (right dtype and size, C-contiguous)."""
+    if out is None:
+        return np.zeros(shape, dtype)
+    if out.dtype != dtype or out.size != int(np.prod(shape)) or not out.flags.c_contiguous:
+        raise ValueError(f"out must be a C-contiguous {np.dtype(dtype).name} array of {int(np.prod(shape))} elements")
+    return out
+
+
 class Engine:
     def __init__(self, device: int = 0, representation: int = L.REPR_TRIANGLE, apply_forces: bool = True,
                  use_graph: bool = True, item_capacity: int = 0,
@@ -123,9 +132,9 @@ class Engine:
         L.check(self.lib.hc_get_curved_sensor_values(self.ctx, sensor, L.fptr(out)))
         return out
 
-    def all_taxel_sensor_values(self) -> np.ndarray:
+    def all_taxel_sensor_values(self, out=None) -> np.ndarray:
         """Every taxel sensor's values, concatenated in sensor order (one copy)."""
-        out = np.zeros(sum(self.taxel_sensors.values()), np.float32)
+        out = _out(out, (sum(self.taxel_sensors.values()),), np.float32)
         L.check(self.lib.hc_get_all_taxel_sensor_values(self.ctx, L.fptr(out), out.size))
         return out
 
@@ -153,8 +162,10 @@ class Engine:
     def step(self):
         L.check(self.lib.hc_step(self.ctx))
 
-    def wrenches(self) -> np.ndarray:
-        w = np.zeros((self.n_pair, 6), np.float64)
+    def wrenches(self, out=None) -> np.ndarray:
+        """Per-pair world wrenches (n_pair x 6).  ``out``: a caller's array to
+        fill (page-locked host memory makes the read a direct copy)."""
+        w = _out(out, (self.n_pair, 6), np.float64)
         L.check(self.lib.hc_get_wrenches(self.ctx, L.dptr(w)))
         return w
 
@@ -176,9 +187,9 @@ class Engine:
         L.check(self.lib.hc_get_taxels(self.ctx, sensor, L.fptr(out)))
         return out
 
-    def all_taxels(self) -> np.ndarray:
+    def all_taxels(self, out=None) -> np.ndarray:
         n = sum(cx * cy for cx, cy in self.sensors.values())
-        out = np.zeros(n, np.float32)
+        out = _out(out, (n,), np.float32)
         L.check(self.lib.hc_get_taxels_all(self.ctx, L.fptr(out), n))
         return out
 
@@ -256,10 +267,12 @@ class Engine:
         L.check(self.lib.hc_get_adjoint_launch_count(self.ctx, C.byref(n)))
         return n.value
 
-    def adjoint(self, dL_dwrench=None, dL_dtaxel=None):
+    def adjoint(self, dL_dwrench=None, dL_dtaxel=None, out=None):
+        """(dL/dpose n_pair x 2 x 6, dL/dE n_pair x 2); ``out``: a pair of
+        caller's arrays to fill."""
         dw = np.ascontiguousarray(dL_dwrench, np.float64) if dL_dwrench is not None else None
         dt = np.ascontiguousarray(dL_dtaxel, np.float32) if dL_dtaxel is not None else None
-        dpose = np.zeros((self.n_pair, 2, 6), np.float64)
-        dE = np.zeros((self.n_pair, 2), np.float64)
+        dpose = _out(out[0] if out is not None else None, (self.n_pair, 2, 6), np.float64)
+        dE = _out(out[1] if out is not None else None, (self.n_pair, 2), np.float64)
         L.check(self.lib.hc_adjoint(self.ctx, L.dptr(dw), L.fptr(dt), L.dptr(dpose), L.dptr(dE)))
         return dpose, dE

@@ -281,6 +281,48 @@ def soft_soft(n_pairs=1024, seed=SEED_SOFTSOFT, tet_range=(2000, 50000)) -> Scen
     return s
 
 
+def soft_soft_pressed(n_pairs=4, seed=SEED_ADJOINT + 100, velocities=True, min_pen=1.5e-3) -> Scene:
+    """A soft sphere pressed into the top face of a soft box that carries a
+    16x16 flat taxel grid, one pair per scene (the soft-soft adjoint cases).
+
+    Moduli E U[5e4,5e5] and dissipations 1.0 (box) / 0.4 (sphere), so the
+    combined damping depends on both moduli; the box is registered first
+    (M, the sensor on the soft frame's geom) in even scenes and second in odd
+    ones.  Penetration U[min_pen, 4 mm] split between the bodies by the
+    equal-pressure surface; the box is 0.3 mm longer in x than in y so that
+    no ray sample sits exactly on a face of its tet grid."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene()
+    box_h = [0.0403, 0.04, 0.012]
+    spec = []
+    for k in range(n_pairs):
+        R = rng.uniform(0.02, 0.03)
+        Eb, Ea = rng.uniform(5e4, 5e5, 2)
+        mk_box = lambda: s.add_geom(L.GEOM_BOX, box_h, [Eb, 1.0, 0.006, 0.5, 0.5])
+        mk_sph = lambda: s.add_geom(L.GEOM_SPHERE, [R, 0, 0], [Ea, 0.4, sphere_hint(R, 4), 0.5, 0.5])
+        if k % 2 == 0:
+            b = mk_box(); a = mk_sph()
+            s.g1.append(b); s.g2.append(a)
+        else:
+            a = mk_sph(); b = mk_box()
+            s.g1.append(a); s.g2.append(b)
+        s.scene_of_pair.append(k)
+        s.sensors.append(dict(geom=b, resolution=0.005, sr=5, window=L.WINDOW_NONE, sigma=-1.0))
+        spec.append((a, b, R))
+    _alloc(s)
+    for (a, b, R) in spec:
+        pen = rng.uniform(min_pen, 0.004)
+        off = rng.uniform(-0.015, 0.015, 2)
+        s.xmat[b] = rot_axis([0, 0, 1], rng.uniform(0, 2 * math.pi)).reshape(9)
+        s.xmat[a] = random_rotation(rng).reshape(9)
+        s.xpos[b] = [0.0, 0.0, 0.0]
+        s.xpos[a] = [off[0], off[1], box_h[2] + R - pen]
+        if velocities:
+            s.vel[a] = rng.uniform(-0.1, 0.1, 6)
+            s.vel[b] = rng.uniform(-0.1, 0.1, 6)
+    return s
+
+
 def _vertical_extent(body, R, c_xy, x, y):
     """The body (centre (c_xy, 0), rotation R) along the vertical lines
     through (x, y): (z_low, z_high), NaN where the line misses it."""

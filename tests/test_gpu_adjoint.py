@@ -12,6 +12,8 @@ with the square of the penetration near first touch), and the taxel maps,
 piecewise linear in the pose with kinks where a ray crosses a tet face, are
 differenced at 1e-7 so that few of the 6400 rays per sensor straddle a kink.
 """
+import copy
+
 import numpy as np
 import pytest
 
@@ -178,3 +180,86 @@ def test_adjoint_is_deterministic(gpu):
     a = run_adjoint(s, dLdw, dLdt)
     b = run_adjoint(s, dLdw, dLdt)
     assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3])
+
+
+def _scaled_moduli(s, geoms, f):
+    st = copy.deepcopy(s)
+    for g in geoms:
+        st.geoms[g]["cs5"] = np.array(st.geoms[g]["cs5"], np.float64)
+        st.geoms[g]["cs5"][0] *= f
+    return st
+
+
+def _pair_losses(s, dLdw, dLdt):
+    r = Oracle(s).collide(taxels64=True)
+    return np.array([np.dot(dLdw[p], r["wrench"][p]) + np.dot(dLdt[p], r["taxels64"][p]) for p in range(len(s.g1))])
+
+
+def test_soft_soft_gradient_poses_and_moduli(gpu):
+    # soft sphere pressed into a soft box carrying the taxel grid; the box
+    # is M in even scenes (sensor on the soft frame's geom) and N in odd
+    # ones.  The equal-pressure surface moves with N's field and with both
+    # moduli; the dissipations differ, so the combined damping depends on
+    # E_M / E_N too.
+    s = scenes.soft_soft_pressed(4)
+    rng = np.random.default_rng(13)
+    dLdw = rng.normal(size=(len(s.g1), 6))
+    dLdt = [rng.normal(size=256) * 1e-3 for _ in s.sensors]
+    w, tax, dpose, dE = run_adjoint(s, dLdw, dLdt)
+    orc = Oracle(s)
+    r0 = orc.collide(taxels64=True)
+    assert np.all(r0["query"] == 3)
+    # forward: wrenches and the soft box's taxel maps (16x16 each)
+    tax = tax.reshape(len(s.sensors), -1)
+    for p in range(len(s.g1)):
+        assert np.linalg.norm(w[p] - r0["wrench"][p]) <= 1e-5 * np.linalg.norm(r0["wrench"][p])
+        t_ref = r0["taxels64"][p]
+        assert np.max(np.abs(tax[p] - t_ref)) <= 1e-4 * np.max(np.abs(t_ref))
+    # poses: central differences of the oracle
+    for p in range(len(s.g1)):
+        ref = fd_gradient(orc, s, p, dLdw, dLdt, h=1e-7)
+        got = dpose[p].reshape(12)
+        err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
+        assert err <= GRAD_RTOL, f"pair {p}: rel err {err:.2e}\n{got}\n{ref}"
+    # moduli: central differences in E_M (all pairs at once; pairs are
+    # independent), then in E_N.  Mesh pressures are E x extent rounded to
+    # FP32 (relative noise ~6e-8 per vertex), which swamps steps below ~1e-4;
+    # at relative step 1e-3 the difference is smooth to ~1e-5.
+    h = 1e-3
+    ref = np.zeros((len(s.g1), 2))
+    for b, geoms in enumerate((r0["m"], r0["n"])):
+        lp = _pair_losses(_scaled_moduli(s, geoms, 1 + h), dLdw, dLdt)
+        lm = _pair_losses(_scaled_moduli(s, geoms, 1 - h), dLdw, dLdt)
+        E = np.array([s.geoms[g]["cs5"][0] for g in geoms])
+        ref[:, b] = (lp - lm) / (2 * h * E)
+    L0 = _pair_losses(s, dLdw, dLdt)
+    for p in range(len(s.g1)):
+        err = np.linalg.norm(dE[p] - ref[p]) / max(np.linalg.norm(ref[p]), 1e-30)
+        assert err <= GRAD_RTOL, f"pair {p}: dE rel err {err:.2e}\n{dE[p]}\n{ref[p]}"
+        # wrench and taxels are homogeneous of degree 1 in (E_M, E_N)
+        EM, EN = s.geoms[r0["m"][p]]["cs5"][0], s.geoms[r0["n"][p]]["cs5"][0]
+        assert abs(EM * dE[p, 0] + EN * dE[p, 1] - L0[p]) <= 1e-4 * abs(L0[p]), (p, dE[p], L0[p])
+
+
+def test_second_taxel_adjoint_of_a_step(gpu):
+    # recomputed polygons (soft-soft) take their won ray samples once; a
+    # second hc_adjoint of the same step re-runs the step and repeats the
+    # first result bit for bit, and the device entry point refuses instead
+    s = scenes.soft_soft_pressed(2)
+    rng = np.random.default_rng(17)
+    dLdw = rng.normal(size=(len(s.g1), 6))
+    dt = np.concatenate([rng.normal(size=256) for _ in s.sensors]).astype(np.float32)
+    eng = scenes.build_engine(s)
+    eng.set_adjoint_mode(True)
+    eng.step()
+    d1, e1 = eng.adjoint(dLdw, dt)
+    d2, e2 = eng.adjoint(dLdw, dt)
+    assert np.array_equal(d1, d2) and np.array_equal(e1, e2)
+    assert np.any(e1 != 0.0)
+    import torch
+    gw = torch.tensor(dLdw, dtype=torch.float64, device="cuda")
+    gt = torch.tensor(dt, device="cuda")
+    torch.cuda.synchronize()
+    with pytest.raises(RuntimeError):
+        eng.adjoint_device(gw.data_ptr(), gt.data_ptr())
+    eng.close()

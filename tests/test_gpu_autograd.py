@@ -103,3 +103,33 @@ def test_modulus_identification_64_maps(gpu):
     rel = np.abs(E.numpy()[soft] - E_true[soft]) / E_true[soft]
     assert hist[-1] < 1e-8 * max(hist[0], 1e-30) + 1e-12, hist
     assert rel.max() < 1e-3, rel.max()
+
+
+def test_autograd_soft_soft_pairs(gpu):
+    # soft-soft pairs: the moduli move the equal-pressure surface, so the
+    # wrapper keeps them at the registered values and returns the adjoint's
+    # exact dL/dE_M, dL/dE_N; pose gradients map as for the other pairs.
+    torch = pytest.importorskip("torch")
+    from mujoco_contact_surfaces_gb300.autograd import ContactModel, contact
+    s = scenes.soft_soft_pressed(2)
+    rng = np.random.default_rng(5)
+    dLdw = rng.normal(size=(len(s.g1), 6))
+    dLdt = [rng.normal(size=256) * 1e-3 for _ in s.sensors]
+    model = ContactModel.from_scene(s)
+    xpos = torch.tensor(s.xpos, dtype=torch.float64, requires_grad=True)
+    rot = torch.zeros(s.n_geom, 3, dtype=torch.float64, requires_grad=True)
+    E0 = torch.tensor([g["cs5"][0] for g in s.geoms], dtype=torch.float64, requires_grad=True)
+    w, t = contact(model, xpos, rot, E0)
+    L = torch.sum(torch.tensor(dLdw) * w) + torch.sum(torch.tensor(np.concatenate(dLdt)) * t)
+    L.backward()
+    eng = model.engine
+    dpose, dE = eng.adjoint(dLdw, np.concatenate(dLdt).astype(np.float32))
+    q, m, n = eng.pair_order()
+    assert np.all(np.asarray(q) == 3)
+    for p in range(len(s.g1)):
+        assert E0.grad[int(m[p])].item() == dE[p, 0] and E0.grad[int(n[p])].item() == dE[p, 1]
+        np.testing.assert_allclose(xpos.grad[int(m[p])].numpy(), dpose[p, 0, 3:], rtol=1e-12, atol=0)
+        np.testing.assert_allclose(xpos.grad[int(n[p])].numpy(), dpose[p, 1, 3:], rtol=1e-12, atol=0)
+    with pytest.raises(ValueError):
+        contact(model, xpos, rot, E0.detach() * 1.5)
+    eng.close()
