@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(128, 4) adjoint_sr_kernel(StepArgs a) {
         const TriStage& T = W.tri[j];
         if (!T.valid || !aabb_overlap(mlo, mhi, T.lo, T.hi)) continue;
         const float margin = 4e-6f * (me.xmax + fabsf(T.o) + T.Lt);
-        if (one_sided32(me.X, T.n, T.o, margin)) continue;
+        if (one_sided32(me.X, T.n, T.o, margin) || edge_outside32(me.X, T, me.xmax)) continue;
         mask |= 1u << j;
       }
     }

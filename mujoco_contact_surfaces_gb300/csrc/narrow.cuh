@@ -714,6 +714,26 @@ struct TriStage {
   int orig, valid;
 };
 
+// True when the tet lies beyond one of the triangle's edge planes by more
+// than the FP32 margin (all four vertices outside): its section would be
+// clipped away whole.  sr_polygon makes the same test with the same values;
+// here it keeps such pairs out of the candidate queue.
+__device__ __forceinline__ bool edge_outside32(const float X[4][3], const TriStage& T, float xmax) {
+  bool out = false;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const float tol = 4e-6f * (xmax + fabsf(T.eo[j]));
+    bool all_out = true;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float d = T.en[j][0] * X[k][0] + T.en[j][1] * X[k][1] + T.en[j][2] * X[k][2] - T.eo[j];
+      all_out &= d < -tol;
+    }
+    out |= all_out;
+  }
+  return out;
+}
+
 // Double-float product of two (head, tail) values (the tail-tail product,
 // below 2^-48 of the result, is dropped; unnormalised) and sum (normalised).
 __device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& h, float& l) {
@@ -971,7 +991,7 @@ __global__ void __launch_bounds__(128, 5) narrow_sr_kernel(StepArgs a) {
         const TriStage& T = W.tri[j];
         if (!T.valid || !aabb_overlap(mlo, mhi, T.lo, T.hi)) continue;
         const float margin = 4e-6f * (me.xmax + fabsf(T.o) + T.Lt);
-        if (one_sided32(me.X, T.n, T.o, margin)) continue;
+        if (one_sided32(me.X, T.n, T.o, margin) || edge_outside32(me.X, T, me.xmax)) continue;
         mask |= 1u << j;
       }
     }
