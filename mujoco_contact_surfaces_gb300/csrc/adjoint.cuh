@@ -423,9 +423,10 @@ __global__ void __launch_bounds__(128, 4) adjoint_sr_kernel(StepArgs a) {
     __syncwarp();
     const float sgn = P.s_is_m ? 1.f : -1.f;
     for (int base = 0; base < total; base += 32) {
+      queue_window(mask, W.q, lane, base);
       const int k = base + lane;
       if (k >= total) continue;
-      const int e = W.q[k];
+      const int e = W.q[k % kQCap];
       const int i = e & 31, j = e >> 5;
       const TetStage& TS = W.tet[i];
       const TriStage& T = W.tri[j];
@@ -561,7 +562,7 @@ __global__ void __launch_bounds__(128, 4) adjoint_hs_kernel(StepArgs a) {
 __global__ void __launch_bounds__(128, 2) adjoint_ss_kernel(StepArgs a) {
   __shared__ TetBStage s_tb[kNarrowWarps][kCluster];
   __shared__ TetStage s_tet[kNarrowWarps][kCluster];
-  __shared__ unsigned short s_q[kNarrowWarps][kCluster * kCluster];
+  __shared__ unsigned short s_q[kNarrowWarps][kQCap];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   while (true) {
     int ie;
@@ -579,11 +580,13 @@ __global__ void __launch_bounds__(128, 2) adjoint_ss_kernel(StepArgs a) {
     ss.iEa = 1.f / P.E_s;
     ss.iEb = 1.f / P.E_o;
     const int sl = it.y, oc = it.z;
-    const int total = ss_stage_item(a, P, F, sl, oc, s_tb[wid], s_tet[wid], s_q[wid], lane);
+    unsigned mask;
+    const int total = ss_stage_item(a, P, F, sl, oc, s_tb[wid], s_tet[wid], s_q[wid], lane, mask);
     for (int base = 0; base < total; base += 32) {
+      queue_window(mask, s_q[wid], lane, base);
       const int k = base + lane;
       if (k >= total) continue;
-      const int e = s_q[wid][k];
+      const int e = s_q[wid][k % kQCap];
       const int i = e & 31, j = e >> 5;
       const TetStage& TS = s_tet[wid][i];
       const TetBStage& B = s_tb[wid][j];

@@ -612,9 +612,18 @@ __device__ __forceinline__ int next_chunk(const StepArgs& a, int q, int lane, in
   return ib + __shfl_sync(0xffffffffu, c, 0);
 }
 
+// Candidate queue entries held per warp at once.  A warp's item has up to
+// 32 x 32 candidates but typically a few dozen; the queue is a window of the
+// lane-major order, refilled from the lanes' masks when the rounds reach its
+// end (kQCap is a multiple of 32, so a round never straddles two windows).
+// Holding 256 instead of 1024 entries leaves 6 KB more of each SM's L1 to the
+// narrow kernels' per-lane polygon arrays.
+constexpr int kQCap = 256;
+
 // Compact the warp's candidate masks (bit j of lane i: element pair (i, j))
-// into a queue of (i | j << 5) entries in lane-major order.
-__device__ __forceinline__ int build_queue(unsigned mask, unsigned short* q, int lane) {
+// into queue entries (i | j << 5) in lane-major order; the entries at
+// positions [from, from + kQCap) go to q.  Returns the total count.
+__device__ __forceinline__ int build_queue(unsigned mask, unsigned short* q, int lane, int from = 0) {
   const int cnt = __popc(mask);
   int incl = cnt;
 #pragma unroll
@@ -623,12 +632,26 @@ __device__ __forceinline__ int build_queue(unsigned mask, unsigned short* q, int
     if (lane >= o) incl += u;
   }
   int w = incl - cnt;
-  while (mask) {
-    const int j = __ffs(mask) - 1;
-    mask &= mask - 1;
-    q[w++] = (unsigned short)(lane | (j << 5));
+  const int end = from + kQCap;
+  if (w < end && incl > from) {
+    while (mask) {
+      const int j = __ffs(mask) - 1;
+      mask &= mask - 1;
+      if (w >= from && w < end) q[w - from] = (unsigned short)(lane | (j << 5));
+      ++w;
+    }
   }
   return __shfl_sync(0xffffffffu, incl, 31);
+}
+
+// Queue entry k of the warp's candidates: the round starting at `base`
+// (a multiple of 32) first refills the window when it starts a new one.
+__device__ __forceinline__ void queue_window(unsigned mask, unsigned short* q, int lane, int base) {
+  if (base > 0 && base % kQCap == 0) {
+    __syncwarp();
+    build_queue(mask, q, lane, base);
+    __syncwarp();
+  }
 }
 
 // Unnormalised normals of the four faces of a tet (face k opposite vertex k).
@@ -941,7 +964,7 @@ __device__ __forceinline__ int sr_poly_f(const TetIn<float>& t, const float* s, 
 struct SrWarpSmem {
   TriStage tri[kCluster];
   TetStage tet[kCluster];
-  unsigned short q[kCluster * kCluster];
+  unsigned short q[kQCap];
 };
 
 // kKeep: polygons are kept as records (forces and rays come later from the
@@ -1000,6 +1023,7 @@ __global__ void __launch_bounds__(128, 5) narrow_sr_kernel(StepArgs a) {
     const float sgn = P.s_is_m ? 1.f : -1.f;
     int seq = 0;
     for (int base = 0; base < total; base += 32) {
+      queue_window(mask, W.q, lane, base);
       const int k = base + lane;
       bool have = false;
       PV<float, 3> poly[kMaxPolyV];
@@ -1009,7 +1033,7 @@ __global__ void __launch_bounds__(128, 5) narrow_sr_kernel(StepArgs a) {
       float gint = 0.f;
       do {
         if (k >= total) break;
-        const int e = W.q[k];
+        const int e = W.q[k % kQCap];
         const int i = e & 31, j = e >> 5;
         jt = j;
         const TetStage& TS = W.tet[i];
@@ -1376,7 +1400,8 @@ __device__ __forceinline__ int ss_element_pair(const StepArgs& a, const FrameDev
 // in A's frame, 32 B tets) and queues the element pairs whose boxes
 // overlap.  Returns the queue length (the warp is synchronised).
 __device__ __forceinline__ int ss_stage_item(const StepArgs& a, const PairDev& P, const FrameDev& F, int sl, int oc,
-                                             TetBStage* tb, TetStage* tet, unsigned short* q, int lane) {
+                                             TetBStage* tb, TetStage* tet, unsigned short* q, int lane,
+                                             unsigned& mask) {
   if (F.valid) {
     stage_tetb(a, P, F, oc * kCluster + lane, tb[lane]);
     stage_tet(a, P, sl * kCluster + lane, tet[lane]);
@@ -1385,7 +1410,7 @@ __device__ __forceinline__ int ss_stage_item(const StepArgs& a, const PairDev& P
     tet[lane].valid = 0;
   }
   __syncwarp();
-  unsigned mask = 0;
+  mask = 0;
   const TetStage& me = tet[lane];
   if (me.valid) {
     float mlo[3], mhi[3];
@@ -1404,7 +1429,7 @@ __device__ __forceinline__ int ss_stage_item(const StepArgs& a, const PairDev& P
 __global__ void __launch_bounds__(128, 4) narrow_ss_kernel(StepArgs a) {
   __shared__ TetBStage s_tb[kNarrowWarps][kCluster];
   __shared__ TetStage s_tet[kNarrowWarps][kCluster];
-  __shared__ unsigned short s_q[kNarrowWarps][kCluster * kCluster];
+  __shared__ unsigned short s_q[kNarrowWarps][kQCap];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   while (true) {
     int ie;
@@ -1416,11 +1441,13 @@ __global__ void __launch_bounds__(128, 4) narrow_ss_kernel(StepArgs a) {
     Acc ac;
     acc_zero(ac);
     const int sl = it.y, oc = it.z;
-    const int total = ss_stage_item(a, P, F, sl, oc, s_tb[wid], s_tet[wid], s_q[wid], lane);
+    unsigned mask;
+    const int total = ss_stage_item(a, P, F, sl, oc, s_tb[wid], s_tet[wid], s_q[wid], lane, mask);
     for (int base = 0; base < total; base += 32) {
+      queue_window(mask, s_q[wid], lane, base);
       const int k = base + lane;
       if (k >= total) continue;
-      const int e = s_q[wid][k];
+      const int e = s_q[wid][k % kQCap];
       const int i = e & 31, j = e >> 5;
       const TetStage& TS = s_tet[wid][i];
       const TetBStage& B = s_tb[wid][j];
