@@ -689,20 +689,26 @@ __global__ void poly_emit_kernel(StepArgs a) {
   if (i < end) a.item_poly_off[i] = ex;
 }
 
-// ---- record kernels: a group of kGroup lanes per kept polygon -------------
+// ---- record kernels: a group of G lanes per kept polygon ------------------
 // The lanes of a group share the polygon's work: its quadrature points
 // (kTriangle: one fan triangle per lane), its ray samples (strided over the
-// bounding box), and in the adjoint one vertex per lane.  Group sums use a
-// fixed shuffle order, so results are deterministic.
-constexpr int kGroup = 8;
+// bounding box), and in the adjoint one vertex per lane.  Polygons of up to
+// 4 vertices (triangles and quads, about 99 % of them) take groups of 4
+// lanes, larger ones groups of 8.  Group sums use a fixed shuffle order, so
+// results are deterministic; a polygon's sums are the same in either group
+// size (the lanes past its vertices add zeros).
+constexpr int kGroup = 8;        // lanes per polygon of more than 4 vertices
+constexpr int kGroupSmall = 4;   // lanes per polygon of at most 4 vertices
 
+template <int G>
 __device__ __forceinline__ float gsum(float v) {
-  v += __shfl_xor_sync(0xffffffffu, v, 4);
+  if constexpr (G >= 8) v += __shfl_xor_sync(0xffffffffu, v, 4);
   v += __shfl_xor_sync(0xffffffffu, v, 2);
   v += __shfl_xor_sync(0xffffffffu, v, 1);
   return v;
 }
-__device__ __forceinline__ V3<float> gsum3(V3<float> v) { return mk(gsum(v.x), gsum(v.y), gsum(v.z)); }
+template <int G>
+__device__ __forceinline__ V3<float> gsum3(V3<float> v) { return mk(gsum<G>(v.x), gsum<G>(v.y), gsum<G>(v.z)); }
 
 __device__ __forceinline__ float4 rec_vtx(const AdjPoly& R, int i) { return *reinterpret_cast<const float4*>(R.v[i]); }
 __device__ __forceinline__ V3<float> rec_pos(const AdjPoly& R, int i) {
@@ -714,6 +720,7 @@ __device__ __forceinline__ V3<float> rec_pos(const AdjPoly& R, int i) {
 // area-weighted centroid c and the pressure pc there, shared by the group:
 // lane t adds fan triangle (0, t, t+1); fixed-order shuffle sums.  Every
 // lane of the warp calls it.
+template <int G>
 __device__ __forceinline__ void rec_fan_group(const AdjPoly& R, int nv, V3<float> n, int sub, float& A, V3<float>& c,
                                               float& pc) {
   float ai = 0.f, pp = 0.f;
@@ -725,14 +732,14 @@ __device__ __forceinline__ void rec_fan_group(const AdjPoly& R, int nv, V3<float
     cc = (x0 + xi + xj) * (ai * (1.f / 3.f));
     pp = ai * (v0.w + vi.w + vj.w) * (1.f / 3.f);
   }
-  A = gsum(ai);
-  c = gsum3(cc);
-  pc = gsum(pp);
+  A = gsum<G>(ai);
+  c = gsum3<G>(cc);
+  pc = gsum<G>(pp);
 }
 
 // The lane's share of a kept polygon's forces (its quadrature point).
 // Every lane of the warp calls it (shuffles); `on`: the group holds a polygon.
-template <int kRepr>
+template <int G, int kRepr>
 __device__ __forceinline__ void rec_forces_part(const StepArgs& a, const AdjPoly& R, int sub, bool on, Acc& ac) {
   const PairDev& P = a.pairs[R.pair];
   const FrameDev& F = a.frames[R.pair];
@@ -742,7 +749,7 @@ __device__ __forceinline__ void rec_forces_part(const StepArgs& a, const AdjPoly
   const float gM = P.s_is_m ? R.gint : INFINITY, gN = P.s_is_m ? INFINITY : R.gint;
   float A, pcen;
   V3<float> c;
-  rec_fan_group(R, nv, nc, sub, A, c, pcen);
+  rec_fan_group<G>(R, nv, nc, sub, A, c, pcen);
   if (!on) return;
   if (A != 0.f) {
     c = c * (1.f / A);
@@ -768,18 +775,19 @@ __device__ __forceinline__ void rec_forces_part(const StepArgs& a, const AdjPoly
   }
 }
 
-// raster_prepare for a kept polygon, shared by its group of kGroup lanes:
+// raster_prepare for a kept polygon, shared by its group of G lanes:
 // lane k transforms vertex k into the sensor frame and the group exchanges
 // them by shuffles (the group's lanes follow one control path, so the
 // shuffles name only the group's lanes); divisions are reciprocal products.
 // The forward and the adjoint both prepare through it, so they compute the
 // same sample keys.
+template <int G>
 __device__ __forceinline__ bool raster_prepare_group(const StepArgs& a, const SensorDev& S, const float* Rl,
                                                      const float* tl, const AdjPoly& R, V3<float> anc,
                                                      V3<float> g_soft, int sub, RasterPoly& rp) {
   const int nv = R.nv;
-  const int base = (threadIdx.x & 31) & ~(kGroup - 1);
-  const unsigned gm = 0xFFu << base;
+  const int base = (threadIdx.x & 31) & ~(G - 1);
+  const unsigned gm = ((1u << G) - 1u) << base;
   float mx = 0.f, my = 0.f, mz = 0.f, mp = 0.f;
   if (sub < nv) {
     const float4 v = rec_vtx(R, sub);
@@ -793,9 +801,9 @@ __device__ __forceinline__ bool raster_prepare_group(const StepArgs& a, const Se
   float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
 #pragma unroll
   for (int i = 0; i < kMaxPolyV; ++i) {
-    rp.lx[i] = __shfl_sync(gm, mx, base + i);
-    rp.ly[i] = __shfl_sync(gm, my, base + i);
-    lz[i] = __shfl_sync(gm, mz, base + i);
+    rp.lx[i] = i < G ? __shfl_sync(gm, mx, base + i) : 0.f;
+    rp.ly[i] = i < G ? __shfl_sync(gm, my, base + i) : 0.f;
+    lz[i] = i < G ? __shfl_sync(gm, mz, base + i) : 0.f;
     if (i < nv) {
       mnx = fminf(mnx, rp.lx[i]); mxx = fmaxf(mxx, rp.lx[i]);
       mny = fminf(mny, rp.ly[i]); mxy = fmaxf(mxy, rp.ly[i]);
@@ -861,13 +869,14 @@ __device__ __forceinline__ bool raster_prepare_group(const StepArgs& a, const Se
 // the pair's sensor0, 1: sensor1), forward: binning with slot keys; lane 0
 // keeps the polygon's plane, pressure model and sample box for the taxel
 // pass and the adjoint.
+template <int G>
 __device__ __forceinline__ void rec_rays_fwd(const StepArgs& a, const AdjPoly& R, int dst, int side, int sid,
                                              const float* Rl, const float* tl, int sub) {
   const SensorDev S = a.sensors[sid];
   RasterPoly rp;
   float4* sp = a.slot_press + 6 * (size_t)dst + 3 * side;
-  if (!raster_prepare_group(a, S, Rl, tl, R, mk(R.anc[0], R.anc[1], R.anc[2]), mk(R.g[0], R.g[1], R.g[2]), sub,
-                            rp)) {
+  if (!raster_prepare_group<G>(a, S, Rl, tl, R, mk(R.anc[0], R.anc[1], R.anc[2]), mk(R.g[0], R.g[1], R.g[2]), sub,
+                               rp)) {
     if (sub == 0) sp[2] = make_float4(__int_as_float(1), __int_as_float(0), __int_as_float(1), __int_as_float(0));
     return;
   }
@@ -882,11 +891,11 @@ __device__ __forceinline__ void rec_rays_fwd(const StepArgs& a, const AdjPoly& R
   const int nY = rp.Y1 - rp.Y0 + 1;
   const int cnt = (rp.X1 - rp.X0 + 1) * nY;
   if (nY <= 0 || cnt <= 0) return;   // the box holds no sample
-  // sample idx = sub, sub + kGroup, ... of the box, row-major in (X, Y):
+  // sample idx = sub, sub + G, ... of the box, row-major in (X, Y):
   // one division up front, then stepped
-  const int dq = kGroup / nY, dr = kGroup % nY;
+  const int dq = G / nY, dr = G % nY;
   int X = rp.X0 + sub / nY, Y = rp.Y0 + sub % nY;
-  for (int idx = sub; idx < cnt; idx += kGroup, X += dq, Y += dr) {
+  for (int idx = sub; idx < cnt; idx += G, X += dq, Y += dr) {
     if (Y > rp.Y1) { Y -= nY; ++X; }
     float t, z, pr;
     if (raster_probe(rp, S, sx[X], sy[Y], t, z, pr)) atomicMin(&smp[(size_t)X * S.ny + Y], key_slot(t, dst, side));
@@ -896,6 +905,7 @@ __device__ __forceinline__ void rec_rays_fwd(const StepArgs& a, const AdjPoly& R
 // Adjoint of the samples a kept polygon won on one sensor: the forward's
 // plane and box; the won samples are known by their keys (the low word names
 // the polygon and side), so no inside test is needed.
+template <int Gs>
 __device__ __forceinline__ void rec_rays_adj(const StepArgs& a, const AdjPoly& R, int dst, int side, int sid,
                                              const float* Rl, const float* tl, int soft_is_sensor, int sub,
                                              AdjAcc& G) {
@@ -913,9 +923,9 @@ __device__ __forceinline__ void rec_rays_adj(const StepArgs& a, const AdjPoly& R
   const float* sy = a.samp_coord + S.samp_off_y;
   const unsigned own = (unsigned)key_slot(0.f, dst, side);
   const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
-  const int dq = kGroup / nY, dr = kGroup % nY;
+  const int dq = Gs / nY, dr = Gs % nY;
   int X = X0 + sub / nY, Y = Y0 + sub % nY;
-  for (int idx = sub; idx < cnt; idx += kGroup, X += dq, Y += dr) {
+  for (int idx = sub; idx < cnt; idx += Gs, X += dq, Y += dr) {
     if (Y > Y1) { Y -= nY; ++X; }
     if ((unsigned)smp[(size_t)X * S.ny + Y] != own) continue;   // won by another polygon, or missed
     const float qx = sx[X], qy = sy[Y];
@@ -928,6 +938,7 @@ __device__ __forceinline__ void rec_rays_adj(const StepArgs& a, const AdjPoly& R
 
 // The pair's sensors (one per geom at most), a side at a time (one copy of
 // the ray code).
+template <int Gs>
 __device__ __forceinline__ void rec_rays(const StepArgs& a, const AdjPoly& R, int dst, int sub, AdjAcc* G) {
   const PairDev& P = a.pairs[R.pair];
   const FrameDev& F = a.frames[R.pair];
@@ -937,48 +948,82 @@ __device__ __forceinline__ void rec_rays(const StepArgs& a, const AdjPoly& R, in
     if (sid < 0) continue;
     const float* Rl = side ? F.Rl1 : F.Rl;
     const float* tl = side ? F.tl1 : F.tl;
-    if (!G) rec_rays_fwd(a, R, dst, side, sid, Rl, tl, sub);
-    else rec_rays_adj(a, R, dst, side, sid, Rl, tl, a.sensors[sid].geom == P.gs, sub, *G);
+    if (!G) rec_rays_fwd<Gs>(a, R, dst, side, sid, Rl, tl, sub);
+    else rec_rays_adj<Gs>(a, R, dst, side, sid, Rl, tl, a.sensors[sid].geom == P.gs, sub, *G);
   }
 }
 
-// Forward pass over the kept polygons: forces into the polygon's pair-ordered
-// slot, then the sensors' rays.
+// Record r's pair-ordered slot (-1: none).
+__device__ __forceinline__ int rec_slot(const StepArgs& a, int r, int n) {
+  if (r >= n) return -1;
+  const int2 key = a.rec_key[r];
+  const int dst = a.item_poly_off[key.x] + key.y;
+  return dst >= 0 && dst < a.rec_cap ? dst : -1;
+}
+
+// The larger polygons among a warp's kPer8 records of one round: lane 4k
+// flags record k (`flag`); the 8-lane groups take them four at a time in
+// record order.  Calls body(r, dst, on, sub) for each turn.  Every lane of
+// the warp calls it.
+template <class Body>
+__device__ __forceinline__ void rec_large_turns(bool flag, int base, int dst, int lane, Body body) {
+  unsigned big = __ballot_sync(0xffffffffu, flag);
+  while (big) {
+    unsigned m = big;
+    for (int q = 0; q < (lane >> 3); ++q) m &= m - 1;
+    const int pick = m ? __ffs(m) - 1 : 0;
+    const bool on = m != 0;
+    const int dst8 = __shfl_sync(0xffffffffu, dst, pick);
+    body(base + (pick >> 2), dst8, on, lane & (kGroup - 1));
+#pragma unroll
+    for (int q = 0; q < 32 / kGroup; ++q) big &= big - 1;
+  }
+}
+
+// The forward pass over one kept polygon by a group of G lanes: forces into
+// its pair-ordered slot, then the sensors' rays.
+template <int G, int kRepr>
+__device__ __forceinline__ void rec_fwd_one(const StepArgs& a, int r, int dst, bool on, int sub) {
+  const AdjPoly& R = a.recs[on ? r : 0];
+  Acc ac;
+  acc_zero(ac);
+  rec_forces_part<G, kRepr>(a, R, sub, on, ac);
+  float v[9] = {ac.F[0], ac.F[1], ac.F[2], ac.T[0], ac.T[1], ac.T[2], ac.area, ac.fn0, (float)ac.n_faces};
+#pragma unroll
+  for (int k = 0; k < 9; ++k) v[k] = gsum<G>(v[k]);
+  if (on && sub == 0) {
+    a.rec_perm[dst] = r;
+    RecOut o;
+    o.F[0] = v[0]; o.F[1] = v[1]; o.F[2] = v[2];
+    o.T[0] = v[3]; o.T[1] = v[4]; o.T[2] = v[5];
+    o.area = v[6]; o.fn0 = v[7]; o.n_faces = (int)v[8];
+    o.pad[0] = o.pad[1] = o.pad[2] = 0;
+    a.rec_out[dst] = o;
+  }
+  __syncwarp();   // the groups enter the shuffled ray preparation together
+  if (on) rec_rays<G>(a, R, dst, sub, nullptr);
+}
+
+// Forward pass over the kept polygons, eight records per warp and round:
+// those of up to 4 vertices in groups of 4 lanes, the rest after them in
+// groups of 8.
 // kRepr: the quadrature (0 kTriangle, 1 kPolygon), fixed per launch.
 template <int kRepr>
 __global__ void __launch_bounds__(128, 5) rec_forward_kernel(StepArgs a) {
   if (!rec_ok(a)) return;   // records incomplete: the step is re-run after growth
   const int n = min(*a.rec_count, a.rec_cap);
-  const int lane = threadIdx.x & 31, sub = lane & (kGroup - 1), grp = lane / kGroup;
+  const int lane = threadIdx.x & 31, sub = lane & (kGroupSmall - 1), grp = lane / kGroupSmall;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
-  constexpr int kPer = 32 / kGroup;
+  constexpr int kPer = 32 / kGroupSmall;
   for (int base = warp * kPer; base < n; base += n_warps * kPer) {
     const int r = base + grp;
-    int dst = -1;
-    if (r < n) {
-      const int2 key = a.rec_key[r];
-      dst = a.item_poly_off[key.x] + key.y;
-    }
-    const bool on = r < n && dst >= 0 && dst < a.rec_cap;
-    const AdjPoly& R = a.recs[on ? r : base];
-    Acc ac;
-    acc_zero(ac);
-    rec_forces_part<kRepr>(a, R, sub, on, ac);
-    float v[9] = {ac.F[0], ac.F[1], ac.F[2], ac.T[0], ac.T[1], ac.T[2], ac.area, ac.fn0, (float)ac.n_faces};
-#pragma unroll
-    for (int k = 0; k < 9; ++k) v[k] = gsum(v[k]);
-    if (on && sub == 0) {
-      a.rec_perm[dst] = r;
-      RecOut o;
-      o.F[0] = v[0]; o.F[1] = v[1]; o.F[2] = v[2];
-      o.T[0] = v[3]; o.T[1] = v[4]; o.T[2] = v[5];
-      o.area = v[6]; o.fn0 = v[7]; o.n_faces = (int)v[8];
-      o.pad[0] = o.pad[1] = o.pad[2] = 0;
-      a.rec_out[dst] = o;
-    }
-    __syncwarp();   // the groups enter the shuffled ray preparation together
-    if (on) rec_rays(a, R, dst, sub, nullptr);
+    const int dst = rec_slot(a, r, n);
+    const int nv = dst >= 0 ? a.recs[r].nv : 0;
+    rec_fwd_one<kGroupSmall, kRepr>(a, r, dst, dst >= 0 && nv <= kGroupSmall, sub);
+    __syncwarp();
+    rec_large_turns(dst >= 0 && nv > kGroupSmall && sub == 0, base, dst, lane,
+                    [&](int r8, int dst8, bool on8, int sub8) { rec_fwd_one<kGroup, kRepr>(a, r8, dst8, on8, sub8); });
   }
 }
 
@@ -986,7 +1031,7 @@ __global__ void __launch_bounds__(128, 5) rec_forward_kernel(StepArgs a) {
 // serial form is wrench_adjoint): lane k reverses the quadrature point of
 // fan triangle k, lane v owns vertex v for the fan reverse and the
 // constraint contraction.  Every lane of the warp calls it (shuffles).
-template <int kRepr>
+template <int Gs, int kRepr>
 __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPoly& R, bool on, int lane, int sub,
                                                  AdjAcc& G) {
   const int nv = on ? R.nv : 0;
@@ -1002,7 +1047,7 @@ __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPol
   const V3<float> gFv = mk(gF[0], gF[1], gF[2]), gTv = mk(gF[3], gF[4], gF[5]);
   float A = 0.f, pc = 0.f;
   V3<float> c = mk(0.f, 0.f, 0.f);
-  rec_fan_group(R, nv, ns, sub, A, c, pc);
+  rec_fan_group<Gs>(R, nv, ns, sub, A, c, pc);
   const bool live = on && A != 0.f;
   const float iA = live ? 1.f / A : 0.f;
   c = c * iA;
@@ -1051,13 +1096,13 @@ __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPol
       }
     }
   }
-  nbar = gsum3(nbar);
-  cbar = gsum3(cbar);
-  gbar = gsum(gbar);
-  pcbar = gsum(pcbar);
-  Abar = gsum(Abar);
+  nbar = gsum3<Gs>(nbar);
+  cbar = gsum3<Gs>(cbar);
+  gbar = gsum<Gs>(gbar);
+  pcbar = gsum<Gs>(pcbar);
+  Abar = gsum<Gs>(Abar);
   // vertex v collects its share as "i" (own lane) and as "j" (lane v - 1)
-  const int src = (lane & ~(kGroup - 1)) | (sub == 0 ? (nv > 0 ? nv - 1 : 0) : sub - 1);
+  const int src = (lane & ~(Gs - 1)) | (sub == 0 ? (nv > 0 ? nv - 1 : 0) : sub - 1);
   V3<float> xb = xbi + mk(__shfl_sync(0xffffffffu, xbj.x, src), __shfl_sync(0xffffffffu, xbj.y, src),
                           __shfl_sync(0xffffffffu, xbj.z, src));
   float pb = pbi + __shfl_sync(0xffffffffu, pbj, src);
@@ -1089,15 +1134,15 @@ __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPol
       to_next = sx + e2b;
       p_next = sp;
     }
-    const int prev = (lane & ~(kGroup - 1)) | (sub == 0 ? 0 : sub - 1);
+    const int prev = (lane & ~(Gs - 1)) | (sub == 0 ? 0 : sub - 1);
     const V3<float> in = mk(__shfl_sync(0xffffffffu, to_next.x, prev), __shfl_sync(0xffffffffu, to_next.y, prev),
                             __shfl_sync(0xffffffffu, to_next.z, prev));
     const float pin = __shfl_sync(0xffffffffu, p_next, prev);
     if (sub > 0) { xb = xb + in; pb += pin; }
-    const V3<float> s0 = gsum3(to0);
-    const float ps0 = gsum(p_to0);
+    const V3<float> s0 = gsum3<Gs>(to0);
+    const float ps0 = gsum<Gs>(p_to0);
     if (sub == 0) { xb = xb + s0; pb += ps0; }
-    nbar = nbar + gsum3(nb);
+    nbar = nbar + gsum3<Gs>(nb);
   }
   // contraction with the tangents of the lane's vertex
   V3<float> rot = mk(0.f, 0.f, 0.f), tr = rot;
@@ -1131,41 +1176,48 @@ __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPol
   G.gx[3] += tr.x; G.gx[4] += tr.y; G.gx[5] += tr.z;
 }
 
+// The reverse pass over one kept polygon by a group of G lanes: the taxel
+// samples it won, then the wrench; its 13 gradient terms into its slot.
+template <int G, int kRepr>
+__device__ __forceinline__ void rec_adj_one(const StepArgs& a, int r, int dst, bool on, int lane, int sub) {
+  const AdjPoly& R = a.recs[on ? r : 0];
+  AdjAcc G_;
+  adj_zero(G_);
+  __syncwarp();   // the groups enter the shuffled ray preparation together
+  if (a.adj_taxel != nullptr && on) rec_rays<G>(a, R, dst, sub, &G_);
+  __syncwarp();
+  if (a.adj_wrench != nullptr && a.apply_forces) rec_wrench_group<G, kRepr>(a, R, on, lane, sub, G_);
+  float v[13] = {G_.gx[0], G_.gx[1], G_.gx[2], G_.gx[3], G_.gx[4], G_.gx[5], G_.glin[0], G_.glin[1], G_.glin[2],
+                 G_.gang[0], G_.gang[1], G_.gang[2], G_.gE};
+#pragma unroll
+  for (int k = 0; k < 13; ++k) v[k] = gsum<G>(v[k]);
+  if (on && sub == 0) {
+    float4* o = reinterpret_cast<float4*>(a.rec_grad + 16 * (size_t)dst);
+    o[0] = make_float4(v[0], v[1], v[2], v[3]);
+    o[1] = make_float4(v[4], v[5], v[6], v[7]);
+    o[2] = make_float4(v[8], v[9], v[10], v[11]);
+    o[3] = make_float4(v[12], 0.f, 0.f, 0.f);
+  }
+}
+
+// Reverse pass over the kept polygons, eight records per warp and round (as
+// rec_forward_kernel: groups of 4 lanes, then groups of 8 for the larger).
 template <int kRepr>
 __global__ void __launch_bounds__(128, 4) adjoint_rec_kernel(StepArgs a) {
   if (!recs_valid(a)) return;
   const int n = min(*a.rec_count, a.rec_cap);
-  const int lane = threadIdx.x & 31, sub = lane & (kGroup - 1), grp = lane / kGroup;
+  const int lane = threadIdx.x & 31, sub = lane & (kGroupSmall - 1), grp = lane / kGroupSmall;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
-  constexpr int kPer = 32 / kGroup;
-  const bool taxel = a.adj_taxel != nullptr, wrench = a.adj_wrench != nullptr && a.apply_forces;
+  constexpr int kPer = 32 / kGroupSmall;
   for (int base = warp * kPer; base < n; base += n_warps * kPer) {
     const int r = base + grp;
-    int dst = -1;
-    if (r < n) {
-      const int2 key = a.rec_key[r];
-      dst = a.item_poly_off[key.x] + key.y;
-    }
-    const bool on = r < n && dst >= 0 && dst < a.rec_cap;
-    const AdjPoly& R = a.recs[on ? r : base];
-    AdjAcc G;
-    adj_zero(G);
-    __syncwarp();   // the groups enter the shuffled ray preparation together
-    if (taxel && on) rec_rays(a, R, dst, sub, &G);
+    const int dst = rec_slot(a, r, n);
+    const int nv = dst >= 0 ? a.recs[r].nv : 0;
+    rec_adj_one<kGroupSmall, kRepr>(a, r, dst, dst >= 0 && nv <= kGroupSmall, lane, sub);
     __syncwarp();
-    if (wrench) rec_wrench_group<kRepr>(a, R, on, lane, sub, G);
-    float v[13] = {G.gx[0], G.gx[1], G.gx[2], G.gx[3], G.gx[4], G.gx[5], G.glin[0], G.glin[1], G.glin[2],
-                   G.gang[0], G.gang[1], G.gang[2], G.gE};
-#pragma unroll
-    for (int k = 0; k < 13; ++k) v[k] = gsum(v[k]);
-    if (on && sub == 0) {
-      float4* o = reinterpret_cast<float4*>(a.rec_grad + 16 * (size_t)dst);
-      o[0] = make_float4(v[0], v[1], v[2], v[3]);
-      o[1] = make_float4(v[4], v[5], v[6], v[7]);
-      o[2] = make_float4(v[8], v[9], v[10], v[11]);
-      o[3] = make_float4(v[12], 0.f, 0.f, 0.f);
-    }
+    rec_large_turns(dst >= 0 && nv > kGroupSmall && sub == 0, base, dst, lane,
+                    [&](int r8, int dst8, bool on8, int sub8) { rec_adj_one<kGroup, kRepr>(a, r8, dst8, on8, lane, sub8); });
   }
 }
 
