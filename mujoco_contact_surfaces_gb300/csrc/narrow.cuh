@@ -563,7 +563,23 @@ __device__ __forceinline__ void df_add(float& hi, float& lo, float h2, float l2)
 // Fixed-order butterfly of the lanes' sums in double-float arithmetic (on
 // the FP32 pipe; FP64 runs at 1/64 of the FP32 rate on this part); lane 0
 // stores the item's (hi, lo) pairs.
+// kKeep: the item's polygons were kept as records (their forces come from
+// the records later), so only the counts are summed; the force sums stored
+// are zero.
+template <bool kKeep = false>
 __device__ __forceinline__ void warp_reduce_store(const StepArgs& a, const Acc& ac, int item, int lane) {
+  if constexpr (kKeep) {
+    const int n_poly = __reduce_add_sync(0xffffffffu, ac.n_poly);
+    const int n_near = __reduce_add_sync(0xffffffffu, ac.n_near);
+    if (lane == 0) {
+      ItemOut r;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) r.hi[i] = r.lo[i] = 0.f;
+      r.n_poly = n_poly; r.n_faces = 0; r.n_near = n_near; r.pad = 0;
+      a.item_out[item] = r;
+    }
+    return;
+  }
   float hi[8] = {ac.F[0], ac.F[1], ac.F[2], ac.T[0], ac.T[1], ac.T[2], ac.area, ac.fn0};
   float lo[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   int c3[3] = {ac.n_poly, ac.n_faces, ac.n_near};
@@ -1090,7 +1106,7 @@ __global__ void __launch_bounds__(128, 5) narrow_sr_kernel(StepArgs a) {
                         W.tri[jt].en, orig_a, orig_b);
     }
     __syncwarp();
-    warp_reduce_store(a, ac, item, lane);
+    warp_reduce_store<kKeep>(a, ac, item, lane);
   }
   }
 }
@@ -1218,7 +1234,7 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
                       orig_a, -1);
     }
     __syncwarp();
-    warp_reduce_store(a, ac, item, lane);
+    warp_reduce_store<kKeep>(a, ac, item, lane);
   }
 }
 
