@@ -368,8 +368,9 @@ __global__ void reduce_kernel(StepArgs a) {
     for (int k = 0; k < 8; ++k) df_add(vh[k], vl[k], r.hi[k], r.lo[k]);
     c[0] += r.n_poly; c[1] += r.n_faces; c[2] += r.n_near;
   }
-  if (rec_ok(a)) {
-    // forces of the kept polygons, in pair order
+  if (rec_ok(a) && P.query != 3) {
+    // forces of the kept polygons, in pair order (soft-soft pairs keep none,
+    // and a step of soft-soft pairs alone runs no record scan)
     const int rb = a.item_poly_off[b], re = a.item_poly_off[e];
     for (int i = rb + lane; i < re; i += 32) {
       const RecOut& r = a.rec_out[i];
@@ -448,6 +449,10 @@ __global__ void taxel_kernel(StepArgs a) {
     }
   }
   a.taxels[S.taxel_off + x + S.cy * y] = avg;
+}
+
+void launch_tet_props(const float4* tets, float4* props, int n_tets, cudaStream_t s) {
+  if (n_tets > 0) tet_props_kernel<<<(n_tets + 255) / 256, 256, 0, s>>>(tets, props, n_tets);
 }
 
 // ---------------------------------------------------------------------------

@@ -33,10 +33,15 @@ hc_status fail(hc_status st, const std::string& msg) {
     if (e_ != cudaSuccess) return fail(HC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
+// A device array owned by the context (freed with it).
 template <class T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;  // capacity in elements
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
   cudaError_t reserve(size_t want) {
     if (want <= n && p) return cudaSuccess;
     if (p) cudaFree(p);
@@ -162,6 +167,7 @@ struct hc_context {
   int max_geom_id = -1;
   // pools
   DevBuf<float4> tets, tris, nodes;
+  DevBuf<float4> tet_props;   // two per tet: the constants of its field
   DevBuf<int> tet_orig, tri_orig;
   // inputs
   DevBuf<double> xpos, xmat, vel;
@@ -347,6 +353,9 @@ hc_status build_pools(hc_context* c) {
   }
   cudaStream_t s = c->stream;
   HC_CUDA(c->tets.upload(tets, s));
+  HC_CUDA(c->tet_props.reserve(std::max<size_t>(2, tets.size() / 2)));
+  hc::launch_tet_props(c->tets.p, c->tet_props.p, (int)(tets.size() / 4), s);
+  HC_CUDA(cudaGetLastError());
   HC_CUDA(c->tris.upload(tris, s));
   HC_CUDA(c->tet_orig.upload(tet_orig, s));
   HC_CUDA(c->tri_orig.upload(tri_orig, s));
@@ -556,6 +565,7 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
   a.n_pair = (int)c->pairs_h.size();
   a.frames = c->frames.p;
   a.tets = c->tets.p;
+  a.tet_props = c->tet_props.p;
   a.tet_orig = c->tet_orig.p;
   a.tris = c->tris.p;
   a.tri_orig = c->tri_orig.p;
@@ -782,19 +792,9 @@ hc_status hc_context_destroy(hc_context* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   invalidate_graph(c);
-  c->tets.release(); c->tris.release(); c->nodes.release(); c->tet_orig.release(); c->tri_orig.release();
-  c->tri_plane.release(); c->tri_edges.release(); c->tri_meta.release();
-  c->xpos.release(); c->xmat.release(); c->vel.release();
-  c->pairs.release(); c->frames.release(); c->unit_pair.release(); c->unit_cl.release();
-  c->unit_count.release(); c->unit_off.release(); c->block_sum.release(); c->items.release();
-  c->item_out.release(); c->counters.release(); c->pair_out.release(); c->sensors_d.release();
-  c->samples.release(); c->taxels.release(); c->weights.release(); c->samp_coord.release();
-  c->cell_sensor.release(); c->cell_first.release(); c->cand.release(); c->polys.release();
-  c->adj_pair.release(); c->adj_taxel.release(); c->adj_item.release(); c->adj_out.release();
-  c->adj_wrench.release();
   for (auto& ev : c->ev) cudaEventDestroy(ev);
   cudaStreamDestroy(c->stream);
-  delete c;
+  delete c;   // every device array is freed by its destructor
   return HC_OK;
 }
 

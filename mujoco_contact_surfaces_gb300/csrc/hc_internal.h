@@ -4,6 +4,9 @@
 //   tet pool   : float4[4] per tet, vertices (x, y, z, pressure) in the soft
 //                geom's body frame, tets in Morton order of their centroids.
 //                64 B per tet, read as four 16 B vector loads.
+//   tet props  : float4[2] per tet, (g.xyz, |g|) and (kappa, xmax, pmax, hmin)
+//                of its linear pressure field, computed on the device once
+//                per pool build (constant in the body frame).
 //   tri pool   : float4[3] per triangle, vertices (x, y, z, 0) in the rigid
 //                geom's body frame, Morton order.  48 B per triangle.
 //   node pool  : float4[2] per node (lo.xyz, hi.xyz) of each geom's implicit

@@ -18,6 +18,7 @@ struct StepArgs {
   FrameDev* frames;
   // geometry pools
   const float4* tets;
+  const float4* tet_props;   // per tet: (g.xyz, |g|), (kappa, xmax, pmax, hmin) of its field
   const int* tet_orig;
   const float4* tris;
   const DfPlane* tri_plane;   // body-frame unit normal and offset (FP64 as head and tail)
@@ -128,6 +129,11 @@ constexpr int kBpBlock = 256;
 void launch_refit(const float4* elems, int verts_per_elem, float4* nodes, const int* geom_elem_off,
                   const int* geom_n_elem, const int* geom_node_off, const int* geom_leaves,
                   int n_geoms, cudaStream_t s);
+
+// Per-tet constants of the soft tets (pressure gradient and its norm,
+// conditioning, coordinate and pressure magnitudes, minimum height), all in
+// the soft body frame: computed once when the pool is built.
+void launch_tet_props(const float4* tets, float4* props, int n_tets, cudaStream_t s);
 
 // Kernel attributes (large dynamic shared memory); once per device.
 cudaError_t init_kernel_attributes();

@@ -455,18 +455,32 @@ __device__ __forceinline__ void tet_box(const TetStage& S, float lo[3], float hi
 __device__ __noinline__ void stage_tet(const StepArgs& a, const PairDev& P, int ti, TetStage& S) {
   S.valid = 0;
   if (ti >= P.s_n_elem) return;
+  const int idx = P.s_elem_off + ti;
   TetIn<float> t;
-  load_tet(a.tets, P.s_elem_off + ti, t);
-  tet_prepare(t);
+  load_tet(a.tets, idx, t);
+  // the field's constants, computed when the pool was built (tet_props_kernel)
+  const float4 p0 = a.tet_props[2 * (size_t)idx], p1 = a.tet_props[2 * (size_t)idx + 1];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     S.X[k][0] = t.X[k].x; S.X[k][1] = t.X[k].y; S.X[k][2] = t.X[k].z;
     S.P[k] = t.P[k];
   }
-  S.g[0] = t.g.x; S.g[1] = t.g.y; S.g[2] = t.g.z;
-  S.gl = t.gl; S.kappa = t.kappa; S.xmax = t.xmax; S.pmax = t.pmax;
-  S.orig = a.tet_orig[P.s_elem_off + ti];
-  S.valid = t.hmin > 0.f ? 1 : 0;
+  S.g[0] = p0.x; S.g[1] = p0.y; S.g[2] = p0.z;
+  S.gl = p0.w; S.kappa = p1.x; S.xmax = p1.y; S.pmax = p1.z;
+  S.orig = a.tet_orig[idx];
+  S.valid = p1.w > 0.f ? 1 : 0;
+}
+
+// The constants of each soft tet's field (what tet_prepare derives), once
+// per pool build.
+__global__ void tet_props_kernel(const float4* tets, float4* props, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  TetIn<float> t;
+  load_tet(tets, i, t);
+  tet_prepare(t);
+  props[2 * (size_t)i] = make_float4(t.g.x, t.g.y, t.g.z, t.gl);
+  props[2 * (size_t)i + 1] = make_float4(t.kappa, t.xmax, t.pmax, t.hmin);
 }
 
 __device__ __forceinline__ void unstage_tet(const TetStage& S, TetIn<float>& t) {

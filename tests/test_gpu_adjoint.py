@@ -263,3 +263,25 @@ def test_second_taxel_adjoint_of_a_step(gpu):
     with pytest.raises(RuntimeError):
         eng.adjoint_device(gw.data_ptr(), gt.data_ptr())
     eng.close()
+
+
+def test_soft_soft_only_step_with_records_after_another_engine(gpu):
+    # a step of soft-soft pairs alone runs no record scan (they keep no
+    # polygons); its per-pair reduction must not read record offsets, which
+    # then hold whatever the device memory held (here: an earlier engine's
+    # records, freed before this engine allocates its own)
+    t = scenes.tactile(64, velocities=True)
+    eng = scenes.build_engine(t)
+    eng.set_adjoint_mode(True)
+    eng.step()
+    eng.wrenches()
+    eng.close()
+    s = scenes.soft_soft_pressed(4)
+    eng = scenes.build_engine(s)
+    eng.set_adjoint_mode(True)
+    eng.step()
+    w = eng.wrenches()
+    eng.close()
+    ref = Oracle(s).collide()["wrench"]
+    for p in range(len(s.g1)):
+        assert np.linalg.norm(w[p] - ref[p]) <= 1e-5 * np.linalg.norm(ref[p]), (p, w[p], ref[p])
