@@ -1009,7 +1009,7 @@ __device__ __forceinline__ void rec_fwd_one(const StepArgs& a, int r, int dst, b
 // groups of 8.
 // kRepr: the quadrature (0 kTriangle, 1 kPolygon), fixed per launch.
 template <int kRepr>
-__global__ void __launch_bounds__(128, 6) rec_forward_kernel(StepArgs a) {
+__global__ void __launch_bounds__(128, 7) rec_forward_kernel(StepArgs a) {
   if (!rec_ok(a)) return;   // records incomplete: the step is re-run after growth
   const int n = min(*a.rec_count, a.rec_cap);
   const int lane = threadIdx.x & 31, sub = lane & (kGroupSmall - 1), grp = lane / kGroupSmall;
