@@ -26,6 +26,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -52,6 +53,9 @@ def parse():
     ap.add_argument("--plain-sample", type=int, default=64, help="scenes timed on the plain path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--launch-shape", default=None,
+                    help="CTAS,CHUNK: use this launch shape instead of autotuning (e.g. the shape an earlier "
+                         "run chose, for a profiler run whose own timings would mislead the autotuner)")
     ap.add_argument("--taxel-sensors", type=int, default=0,
                     help="K: also attach a taxel-point sensor with a KxK taxel grid to every plate")
     return ap.parse_args()
@@ -118,7 +122,10 @@ class Clocks:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # the raw samples (the JSON line carries their summary): HC_CLOCKS_DIR
+        # or the system's temporary directory
+        out_dir = os.environ.get("HC_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out_dir, f"clocks_{os.getpid()}.csv")
 
     def start(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
@@ -250,7 +257,11 @@ def run_gb300(args):
         extra["taxel_sensors"] = {"per_plate": k * k, "method": "squared", "include_margin": 0.002,
                                   "sample_resolution": 0.0015, "sample_method": "default"}
     eng.set_adjoint_mode(True)
-    tuned_ctas, tuned_chunk = eng.autotune()       # launch shape, before any timing
+    if args.launch_shape:
+        tuned_ctas, tuned_chunk = (int(x) for x in args.launch_shape.split(","))
+        eng.set_launch_shape(tuned_ctas, tuned_chunk)
+    else:
+        tuned_ctas, tuned_chunk = eng.autotune()   # launch shape, before any timing
     eng.enable_timing(True)
     ab = algorithmic_bytes(eng, n_pair, len(s.sensors))
     dLdw_h, dLdt_h = upstream(s)

@@ -109,6 +109,7 @@ SIGNATURES = {
     "hc_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "hc_get_launch_count": (C.c_int, [_P, _ip]),
     "hc_autotune": (C.c_int, [_P, _ip, _ip]),
+    "hc_set_launch_shape": (C.c_int, [_P, C.c_int, C.c_int]),
     "hc_step_noalloc": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _P, _P]),
     "hc_add_taxel_sensor": (C.c_int, [_P, C.c_int, C.c_int, _dp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
                                       _ip]),

@@ -1731,6 +1731,16 @@ hc_status hc_autotune(hc_context* c, int* chosen_ctas_per_sm, int* chosen_chunk)
   return HC_OK;
 }
 
+hc_status hc_set_launch_shape(hc_context* c, int ctas_per_sm, int chunk) {
+  if (hc_status st = need(c)) return st;
+  if (ctas_per_sm < 1 || ctas_per_sm > 8 || chunk < 1 || chunk > 8)
+    return fail(HC_ERR_INVALID_ARG, "ctas_per_sm and chunk must be in 1-8");
+  if (ctas_per_sm != c->narrow_ctas_per_sm || chunk != c->narrow_chunk) invalidate_graph(c);
+  c->narrow_ctas_per_sm = ctas_per_sm;
+  c->narrow_chunk = chunk;
+  return HC_OK;
+}
+
 hc_status hc_set_adjoint_mode(hc_context* c, int on) {
   if (hc_status st = need(c)) return st;
   if ((on != 0) != c->adjoint_mode) invalidate_graph(c);

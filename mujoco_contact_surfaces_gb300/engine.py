@@ -241,6 +241,10 @@ class Engine:
         L.check(self.lib.hc_autotune(self.ctx, C.byref(ct), C.byref(ch)))
         return ct.value, ch.value
 
+    def set_launch_shape(self, ctas_per_sm: int, chunk: int):
+        """Set the persistent kernels' grid and the work-queue chunk directly."""
+        L.check(self.lib.hc_set_launch_shape(self.ctx, int(ctas_per_sm), int(chunk)))
+
     def launch_count(self) -> int:
         n = C.c_int()
         L.check(self.lib.hc_get_launch_count(self.ctx, C.byref(n)))
