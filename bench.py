@@ -39,7 +39,7 @@ METRIC = "contact pairs/s fwd+adjoint, batched vs plain GPU path at 1e-5 rel wre
 # DRAM bytes of one narrow_sr_kernel launch (dram__bytes_read.sum +
 # dram__bytes_write.sum) from an ncu capture of this workload at 1024 scenes,
 # scaled by the scenes processed (items and polygons grow in proportion).
-NARROW_SR_DRAM_BYTES_PER_SCENE = 108.2e6 / 1024
+NARROW_SR_DRAM_BYTES_PER_SCENE = 240.1e6 / 1024
 
 
 def parse():
