@@ -362,7 +362,11 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (fp64 section values, plane offsets and wrench sums)",
         "data": "synthetic (seeded PCG64 scenes; no dataset exists)",
-        "config": config_dict(args, world, {"pairs": n_pair, "polygons": ab["polygons"], "tets_touched": ab["tets"],
+        "config": config_dict(args, world, {"pairs": n_pair, "polygons": ab["polygons"],
+                                            # secondary figure: non-empty element pairs (polygons)
+                                            # through forward and adjoint, per second, all ranks
+                                            "element_pairs_per_s": ab["polygons"] * world / (t_step * 1e-3),
+                                            "tets_touched": ab["tets"],
                                             "tris_touched": ab["tris"], "ms_forward": t_step - adj_avg,
                                             "ms_adjoint": adj_avg, "ms_narrow_kernel": narrow_avg,
                                             "ms_kept_polygons_pass": kept_avg,

@@ -8,6 +8,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 from mujoco_contact_surfaces_gb300 import _lib as L
 
@@ -86,3 +87,23 @@ def test_generated_values_are_float_representable():
     k, v, p, e = L.generate_mesh(L.GEOM_SPHERE, [0.05, 0, 0], [1e5, 1, 0.01, 0.5, 0.5])
     assert np.array_equal(v, v.astype(np.float32).astype(np.float64))
     assert np.array_equal(p, p.astype(np.float32).astype(np.float64))
+
+
+def test_caller_output_arrays_are_checked():
+    # Engine outputs go into the caller's arrays (e.g. page-locked ones) when
+    # given: right dtype, size and C order, else a ValueError before any call
+    from mujoco_contact_surfaces_gb300.engine import _out
+    a = np.zeros((4, 6))
+    assert _out(a, (4, 6), np.float64) is a
+    assert _out(None, (4, 6), np.float64).shape == (4, 6)
+    with pytest.raises(ValueError):
+        _out(np.zeros((4, 6), np.float32), (4, 6), np.float64)
+    with pytest.raises(ValueError):
+        _out(np.zeros((4, 5)), (4, 6), np.float64)
+    with pytest.raises(ValueError):
+        _out(np.zeros((6, 4)).T, (4, 6), np.float64)
+
+
+def test_launch_shape_rejects_null_context():
+    lib = L.load()
+    assert lib.hc_set_launch_shape(None, 6, 8) == L.HC_ERR_INVALID_ARG
