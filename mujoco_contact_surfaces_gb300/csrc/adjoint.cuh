@@ -961,10 +961,13 @@ __device__ __forceinline__ int rec_slot(const StepArgs& a, int r, int n) {
   return dst >= 0 && dst < a.rec_cap ? dst : -1;
 }
 
-// The larger polygons among a warp's kPer8 records of one round: lane 4k
-// flags record k (`flag`); the 8-lane groups take them four at a time in
-// record order.  Calls body(r, dst, on, sub) for each turn.  Every lane of
-// the warp calls it.
+// The polygons of more than 4 vertices among a warp's 8 records of one
+// round (records base .. base + 7, record k held by lanes 4k .. 4k + 3):
+// lane 4k flags record k (`flag`) and holds its slot (`dst`); the warp's
+// four 8-lane groups take the flagged records four at a time in record
+// order.  Calls body(r, dst, on, sub) once per turn on every lane (`on`:
+// the lane's group holds a record this turn).  Every lane of the warp calls
+// it.
 template <class Body>
 __device__ __forceinline__ void rec_large_turns(bool flag, int base, int dst, int lane, Body body) {
   unsigned big = __ballot_sync(0xffffffffu, flag);
