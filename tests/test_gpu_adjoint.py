@@ -37,12 +37,13 @@ def perturb(xpos, xmat, g, comp, h):
     return xp, xm
 
 
-def fd_gradient(orc, s, p, dLdw, dLdt, h=1e-6):
+def fd_gradient(orc, s, p, dLdw, dLdt, h=1e-6, representation=0):
     """Central differences of L for pair p: 12 components (M then N)."""
     m, n = orc.collide(pairs=[p], sensors=False)["m"][0], orc.collide(pairs=[p], sensors=False)["n"][0]
 
     def L(xp, xm):
-        r = orc.collide(pairs=[p], xpos=xp, xmat=xm, sensors=dLdt is not None, taxels64=dLdt is not None)
+        r = orc.collide(representation=representation, pairs=[p], xpos=xp, xmat=xm, sensors=dLdt is not None,
+                        taxels64=dLdt is not None)
         v = float(np.dot(dLdw[p], r["wrench"][0]))
         if dLdt is not None:
             v += sum(float(np.dot(dLdt[k], r["taxels64"][k])) for k in range(len(s.sensors)))
@@ -59,8 +60,8 @@ def fd_gradient(orc, s, p, dLdw, dLdt, h=1e-6):
     return g
 
 
-def run_adjoint(s, dLdw, dLdt, adjoint_mode=True):
-    eng = scenes.build_engine(s)
+def run_adjoint(s, dLdw, dLdt, adjoint_mode=True, **engine_kw):
+    eng = scenes.build_engine(s, **engine_kw)
     if adjoint_mode:
         eng.lib.hc_set_adjoint_mode(eng.ctx, 1)
     eng.step()
@@ -285,3 +286,21 @@ def test_soft_soft_only_step_with_records_after_another_engine(gpu):
     ref = Oracle(s).collide()["wrench"]
     for p in range(len(s.g1)):
         assert np.linalg.norm(w[p] - ref[p]) <= 1e-5 * np.linalg.norm(ref[p]), (p, w[p], ref[p])
+
+
+def test_gradient_polygon_quadrature_soft_rigid(gpu):
+    # kPolygon: one quadrature point per polygon (its centroid) instead of
+    # one per fan triangle; the adjoint reverses that point from the kept
+    # polygons (wrench upstream: the taxel maps do not depend on the
+    # quadrature)
+    from mujoco_contact_surfaces_gb300 import _lib as L
+    s = scenes.single_pair(4, velocities=True, min_pen=1e-3)
+    rng = np.random.default_rng(23)
+    dLdw = rng.normal(size=(len(s.g1), 6))
+    _, _, dpose, _ = run_adjoint(s, dLdw, None, representation=L.REPR_POLYGON)
+    orc = Oracle(s)
+    for p in range(len(s.g1)):
+        ref = fd_gradient(orc, s, p, dLdw, None, representation=1)
+        got = dpose[p].reshape(12)
+        err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
+        assert err <= GRAD_RTOL, f"pair {p}: rel err {err:.2e}\n{got}\n{ref}"
