@@ -83,6 +83,16 @@ __device__ __forceinline__ bool point_reverse(AdjAcc& G, const FrameDev& F, floa
   return true;
 }
 
+// A polygon vertex whose three constraint rows are linearly dependent
+// (normalised |det| below kDetTol) is not fixed by them and is left out of
+// the contraction.  Soft-soft polygons have such vertices where an edge on
+// one body's surface meets the other's surface: both pressures vanish there,
+// so the section plane p_M = p_N and the two surface planes share a line.
+// In FP32 the determinant of a dependent triple is rounding noise (~1e-7
+// relative), not zero, so the tolerance sits far above that and far below
+// the vertices of well-formed polygons (0.06 and up on the test scenes).
+constexpr float kDetTol = 1e-4f;
+
 __device__ __forceinline__ void adj_zero(AdjAcc& g) {
 #pragma unroll
   for (int i = 0; i < 6; ++i) g.gx[i] = 0.f;
@@ -209,7 +219,7 @@ __device__ __noinline__ void wrench_adjoint(AdjAcc& G, const StepArgs& a, const 
     const V3<float> a0 = cross(r1, r2), a1 = cross(r2, r0), a2 = cross(r0, r1);
     const float det = dot(r0, a0);
     const float sc = norm(r0) * norm(r1) * norm(r2);
-    if (!(fabsf(det) > 1e-12f * sc)) continue;
+    if (!(fabsf(det) > kDetTol * sc)) continue;
     const float id = 1.f / det;
     V3<float> B = r0 * (dot(xe, a0) * id);
     if (l0 >= 4) B = B + r1 * (dot(xe, a1) * id);
@@ -340,7 +350,7 @@ __device__ __noinline__ void wrench_adjoint_ss(AdjAcc& G, SsAdj& ss, const StepA
     const V3<float> a0 = cross(r1, r2), a1 = cross(r2, r0), a2 = cross(r0, r1);
     const float det = dot(r0, a0);
     const float sc = norm(r0) * norm(r1) * norm(r2);
-    if (!(fabsf(det) > 1e-12f * sc)) continue;
+    if (!(fabsf(det) > kDetTol * sc)) continue;
     const float id = 1.f / det;
     const float b0 = dot(xe, a0) * id;
     V3<float> B = ss.gb * (-b0 * il);
@@ -1162,7 +1172,7 @@ __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPol
     const V3<float> a0 = cross(r1, r2), a1 = cross(r2, r0), a2 = cross(r0, r1);
     const float det = dot(r0, a0);
     const float sc = norm(r0) * norm(r1) * norm(r2);
-    if (fabsf(det) > 1e-12f * sc) {
+    if (fabsf(det) > kDetTol * sc) {
       const float id = 1.f / det;
       V3<float> B = r0 * (dot(xe, a0) * id);
       if (l0 >= 4) B = B + r1 * (dot(xe, a1) * id);
