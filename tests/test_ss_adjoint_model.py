@@ -1,0 +1,124 @@
+"""The soft-soft wrench reverse, restated in FP64 (tests/ss_adjoint_model.py),
+against the oracle and against central differences (CPU).
+
+The pair is the sphere-on-soft-box pair the GPU adjoint tests use
+(`soft_soft_pressed(2)`, pair 1, the sphere registered first).  Its contact
+boundary has vertices whose three constraint rows are linearly dependent
+(an edge on one body's surface meets the other body's surface: both
+pressures vanish, so the section plane and the two surface planes share a
+line).  Such a vertex is not fixed by its rows and the reverse leaves it out;
+in FP32 the determinant of a dependent triple is rounding noise, so the
+guard must sit well above it (the device's kDetTol = 1e-4), which the FP32
+emulation here shows.
+"""
+import numpy as np
+import pytest
+
+from mujoco_contact_surfaces_gb300 import _lib as L
+from mujoco_contact_surfaces_gb300 import scenes
+from oracle import Oracle
+from tests import ss_adjoint_model as M
+
+
+def _rotation(w):
+    th = np.linalg.norm(w)
+    if th == 0:
+        return np.eye(3)
+    k = w / th
+    K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+    return np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * K @ K
+
+
+@pytest.fixture(scope="module")
+def pair():
+    s = scenes.soft_soft_pressed(2)
+    p = 1
+    ga, gb = s.g1[p], s.g2[p]
+    mesh = {}
+    for g in (ga, gb):
+        G = s.geoms[g]
+        _, v, pr, e = L.generate_mesh(G["type"], G["size"], G["cs5"], G["mesh_v"], G["mesh_f"])
+        mesh[g] = (np.asarray(v, float).reshape(-1, 3), np.asarray(pr, float), np.asarray(e, int).reshape(-1, 4))
+    RA, tA = s.xmat[ga].reshape(3, 3), s.xpos[ga]
+    RB, tB = s.xmat[gb].reshape(3, 3), s.xpos[gb]
+    vA, pA, eA = mesh[ga]
+    vB0, pB, eB = mesh[gb]
+    vB = ((RB @ vB0.T).T + tB - tA) @ RA          # B in A's frame
+    EM, EN = s.geoms[ga]["cs5"][0], s.geoms[gb]["cs5"][0]
+    dM, dN = s.geoms[ga]["cs5"][1], s.geoms[gb]["cs5"][1]
+    ma, mb = s.geoms[ga]["cs5"][4], s.geoms[gb]["cs5"][4]
+    wM, vM = s.vel[ga][:3], s.vel[ga][3:]
+    wN, vN = s.vel[gb][:3], s.vel[gb][3:]
+    # relative velocity field v_M - v_N in A's frame: lin + ang x p
+    lin = RA.T @ ((vM - vN) - np.cross(wM, tA) + np.cross(wN, tB) + np.cross(wM - wN, tA))
+    vf = (lin, RA.T @ (wM - wN), (EN * dM + EM * dN) / (EM + EN), 2 * ma * mb / (ma + mb))
+    XA, XB = vA[eA], vB[eB]
+    ov = np.all((XA.min(1)[:, None] <= XB.max(1)[None]) & (XB.min(1)[None] <= XA.max(1)[:, None]), axis=2)
+    polys = {}
+    for ta, tb in np.argwhere(ov):
+        P = M.element_polygon(vA[eA[ta]], pA[eA[ta]], vB[eB[tb]], pB[eB[tb]])
+        if P is not None:
+            polys[(int(ta), int(tb))] = P
+
+    def loss(vb, gF, gT, repr_):
+        tot = 0.0
+        for ta, tb in polys:   # element pairs without a polygon enter at second order
+            P = M.element_polygon(vA[eA[ta]], pA[eA[ta]], vb[eB[tb]], pB[eB[tb]])
+            if P is not None:
+                f, t = M.polygon_wrench(P, vf, repr_)
+                tot += gF @ f + gT @ t
+        return tot
+
+    def central_differences(gF, gT, repr_, h=1e-7):
+        fd = np.zeros(6)
+        for c in range(6):
+            w, v = np.zeros(3), np.zeros(3)
+            if c < 3:
+                w[c] = h
+            else:
+                v[c - 3] = h
+            lp = loss((_rotation(w) @ vB.T).T + v, gF, gT, repr_)
+            lm = loss((_rotation(-w) @ vB.T).T - v, gF, gT, repr_)
+            fd[c] = (lp - lm) / (2 * h)
+        return fd
+
+    orc = Oracle(s)
+    return dict(s=s, p=p, RA=RA, vf=vf, polys=polys, fd=central_differences, oracle=orc)
+
+
+@pytest.mark.parametrize("repr_", [0, 1])
+def test_model_forward_matches_oracle(pair, repr_):
+    F, T = np.zeros(3), np.zeros(3)
+    for P in pair["polys"].values():
+        f, t = M.polygon_wrench(P, pair["vf"], repr_)
+        F += f
+        T += t
+    ref = pair["oracle"].collide(representation=repr_, pairs=[pair["p"]], sensors=False)
+    assert len(pair["polys"]) == ref["n_polygons"][0]
+    w = np.concatenate([pair["RA"] @ F, pair["RA"] @ T])
+    assert np.linalg.norm(w - ref["wrench"][0]) <= 1e-9 * np.linalg.norm(ref["wrench"][0])
+
+
+@pytest.mark.parametrize("repr_", [0, 1])
+def test_reverse_matches_central_differences_and_needs_an_fp32_guard(pair, repr_):
+    rng = np.random.default_rng(5)
+    gF, gT = rng.normal(size=3), rng.normal(size=3) * 0.05
+    fd = pair["fd"](gF, gT, repr_)
+    vf = pair["vf"]
+    g64 = sum(M.polygon_reverse(P, gF, gT, vf, repr_) for P in pair["polys"].values())
+    err = lambda g: np.linalg.norm(g - fd) / np.linalg.norm(fd)
+    assert err(g64) <= 1e-3
+    vf32 = tuple(np.float32(x) for x in vf)
+
+    def fp32(tol):
+        tot = np.zeros(6)
+        for P in pair["polys"].values():
+            Q, anc = M.as_float32(P)
+            tot += np.asarray(M.polygon_reverse(Q, np.float32(gF), np.float32(gT), vf32, repr_, anc,
+                                                np.float32(tol)), np.float64)
+        return tot
+
+    # the FP64 guard lets the dependent vertices' rounding-noise determinants
+    # through in FP32; the device's tolerance does not
+    assert err(fp32(1e-12)) > 2e-3
+    assert err(fp32(1e-4)) <= 1e-3
