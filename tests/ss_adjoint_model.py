@@ -208,13 +208,15 @@ def _point_reverse(gF, gT, A, p, n, gM, gN, p0, vf):
     nbar = nbar + v * vnbar
     gbar = kbar * A
     return dict(A=kbar * g + fn0bar * p0, p0=fn0bar * A, gM=gbar * (g / gM) ** 2, gN=gbar * (g / gN) ** 2,
-                p=np.cross(vbar, ang) + np.cross(f, gT), n=nbar)
+                p=np.cross(vbar, ang) + np.cross(f, gT), n=nbar, d=-hbar * vn)
 
 
-def polygon_reverse(P, gF, gT, vf, repr_=0, anc=None, det_tol=1e-12):
+def polygon_reverse(P, gF, gT, vf, repr_=0, anc=None, det_tol=1e-12, moduli=None):
     """dL/d(w, v) of one polygon for L = gF . F + gT . T (the device's
     wrench_adjoint_ss).  With `anc`, the vertices are relative to it (the
-    device keeps them so in FP32); det_tol: the dependent-rows guard."""
+    device keeps them so in FP32); det_tol: the dependent-rows guard.  With
+    moduli = (E_A, E_B), returns (dL/d(w, v), dL/dE_A, dL/dE_B, dL/d(damping))
+    instead, the moduli's own terms at fixed damping."""
     x, n = list(P['x']), P['n']
     anc = np.zeros(3) if anc is None else anc
     ga, gb, lm = P['gA'], P['gB'], P['lm']
@@ -228,7 +230,7 @@ def polygon_reverse(P, gF, gT, vf, repr_=0, anc=None, det_tol=1e-12):
     iA = 1.0 / A
     c, pc = Sc * iA, Sp * iA
     nbar, cbar = np.zeros(3), np.zeros(3)
-    gMbar = gNbar = pcbar = Abar = 0.0
+    gMbar = gNbar = pcbar = Abar = gD = 0.0
     if repr_ == 1:
         b = _point_reverse(gF, gT, abs(A), anc + c, n, P['gM'], P['gN'], pc, vf)
         if b is not None:
@@ -238,6 +240,7 @@ def polygon_reverse(P, gF, gT, vf, repr_=0, anc=None, det_tol=1e-12):
             nbar = nbar + b['n']
             gMbar += b['gM']
             gNbar += b['gN']
+            gD += b['d']
     for i in range(nv if repr_ == 0 else 0):
         j = (i + 1) % nv
         u, w = x[i] - c, x[j] - c
@@ -250,6 +253,7 @@ def polygon_reverse(P, gF, gT, vf, repr_=0, anc=None, det_tol=1e-12):
         nbar = nbar + b['n']
         gMbar += b['gM']
         gNbar += b['gN']
+        gD += b['d']
         if ln > 0:
             crb = cr * (0.5 * b['A'] / ln)
             ub, wb = np.cross(w, crb), np.cross(crb, u)
@@ -283,8 +287,12 @@ def polygon_reverse(P, gF, gT, vf, repr_=0, anc=None, det_tol=1e-12):
     npp = nbar - n * (nbar @ n)
     rot = np.cross(npp, gb) / lm + np.cross(n, gb) * gNbar
     tr = np.zeros(3)
+    iEa, iEb = (1.0 / moduli[0], 1.0 / moduli[1]) if moduli is not None else (0.0, 0.0)
+    gEa = (npp @ ga / lm + gMbar * P['gM']) * iEa
+    gEb = (gNbar * P['gN'] - npp @ gb / lm) * iEb
     for v in range(nv):
         xe = xb[v] + ga * pb[v]
+        gEa += pb[v] * pv[v] * iEa
         l0, l1 = P['lab'][v]
         r1 = P['faceA'][l0] if l0 < 4 else P['pnB'][l0 - 4]
         r2 = P['faceA'][l1] if l1 < 4 else P['pnB'][l1 - 4]
@@ -300,6 +308,10 @@ def polygon_reverse(P, gF, gT, vf, repr_=0, anc=None, det_tol=1e-12):
             B = B + r2 * (xe @ a2 / det)
         tr = tr + B
         rot = rot + np.cross(anc + x[v], B)
+        gEa -= b0 * pv[v] / lm * iEa
+        gEb += b0 * pv[v] / lm * iEb
+    if moduli is not None:
+        return np.concatenate([rot, tr]), gEa, gEb, gD
     return np.concatenate([rot, tr])
 
 

@@ -82,8 +82,21 @@ def pair():
             fd[c] = (lp - lm) / (2 * h)
         return fd
 
+    def loss_moduli(fa, fb, gF, gT, repr_):
+        """L with E_A scaled by fa and E_B by fb (pressures and damping)."""
+        ea, eb = EM * fa, EN * fb
+        vfe = (vf[0], vf[1], (eb * dM + ea * dN) / (ea + eb), vf[3])
+        tot = 0.0
+        for ta, tb in polys:
+            P = M.element_polygon(vA[eA[ta]], pA[eA[ta]] * fa, vB[eB[tb]], pB[eB[tb]] * fb)
+            if P is not None:
+                f, t = M.polygon_wrench(P, vfe, repr_)
+                tot += gF @ f + gT @ t
+        return tot
+
     orc = Oracle(s)
-    return dict(s=s, p=p, RA=RA, vf=vf, polys=polys, fd=central_differences, oracle=orc)
+    return dict(s=s, p=p, RA=RA, vf=vf, polys=polys, fd=central_differences, oracle=orc,
+                moduli=(EM, EN), dissipation=(dM, dN), loss_moduli=loss_moduli)
 
 
 @pytest.mark.parametrize("repr_", [0, 1])
@@ -122,3 +135,32 @@ def test_reverse_matches_central_differences_and_needs_an_fp32_guard(pair, repr_
     # through in FP32; the device's tolerance does not
     assert err(fp32(1e-12)) > 2e-3
     assert err(fp32(1e-4)) <= 1e-3
+
+
+@pytest.mark.parametrize("repr_", [0, 1])
+def test_reverse_modulus_terms(pair, repr_):
+    # dL/dE_A and dL/dE_B of the reverse (the equal-pressure plane moves with
+    # both moduli; the combined damping d = (E_B d_A + E_A d_B)/(E_A + E_B)
+    # depends on their ratio) against central differences at relative step
+    # 1e-6, and Euler's identity E_A dL/dE_A + E_B dL/dE_B = L
+    rng = np.random.default_rng(6)
+    gF, gT = rng.normal(size=3), rng.normal(size=3) * 0.05
+    EA, EB = pair["moduli"]
+    dA, dB = pair["dissipation"]
+    gEa = gEb = gD = 0.0
+    for P in pair["polys"].values():
+        _, a, b, d = M.polygon_reverse(P, gF, gT, pair["vf"], repr_, moduli=(EA, EB))
+        gEa += a
+        gEb += b
+        gD += d
+    den = (EA + EB) ** 2
+    dEa = gEa + gD * EB * (dB - dA) / den
+    dEb = gEb + gD * EA * (dA - dB) / den
+    h = 1e-6
+    L = pair["loss_moduli"]
+    ref_a = (L(1 + h, 1, gF, gT, repr_) - L(1 - h, 1, gF, gT, repr_)) / (2 * h * EA)
+    ref_b = (L(1, 1 + h, gF, gT, repr_) - L(1, 1 - h, gF, gT, repr_)) / (2 * h * EB)
+    got, ref = np.array([dEa, dEb]), np.array([ref_a, ref_b])
+    assert np.linalg.norm(got - ref) <= 1e-3 * np.linalg.norm(ref), (got, ref)
+    L0 = L(1, 1, gF, gT, repr_)
+    assert abs(EA * dEa + EB * dEb - L0) <= 1e-9 * abs(L0) + 1e-12, (EA * dEa + EB * dEb, L0)
