@@ -164,3 +164,48 @@ def test_reverse_modulus_terms(pair, repr_):
     assert np.linalg.norm(got - ref) <= 1e-3 * np.linalg.norm(ref), (got, ref)
     L0 = L(1, 1, gF, gT, repr_)
     assert abs(EA * dEa + EB * dEb - L0) <= 1e-9 * abs(L0) + 1e-12, (EA * dEa + EB * dEb, L0)
+
+
+@pytest.mark.parametrize("sensor_on_b", [False, True])
+def test_ray_hit_pressure_derivatives(sensor_on_b):
+    # The soft-soft sample adjoint (sample_adjoint, kSS): a ray o + t D hits
+    # p_A = p_B and reads p = p_A(x).  With m = g_A - g_B, ka = g_A.D / m.D and
+    # kb = -g_B.D / m.D: rays on B move with it, dp = kb g_A.(w x x + v);
+    # rays on A are fixed, dp = -ka g_B.(w x x + v); dp/dE_A = kb p / E_A,
+    # dp/dE_B = ka p / E_B.  Central differences of the exact hit.
+    rng = np.random.default_rng(31)
+    EA, EB = 2e5, 3e5
+    ga_u, gb_u = rng.normal(size=3), rng.normal(size=3)
+    ga_u[2], gb_u[2] = 1.0 + abs(ga_u[2]), -1.0 - abs(gb_u[2])   # fields facing each other along z
+    ca_u, cb_u = 0.3, 0.5
+    o, D = np.array([0.01, -0.02, 0.3]), np.array([0.05, -0.03, -1.0])
+
+    def hit(R, v, fa=1.0, fb=1.0):
+        ga, ca = EA * fa * ga_u, EA * fa * ca_u
+        gb, cb = EB * fb * gb_u, EB * fb * cb_u
+        # B moved by (R, v): p_B'(y) = p_B(R^T (y - v))
+        gbm, cbm = R @ gb, cb - (R @ gb) @ v
+        oo, DD = (R @ o + v, R @ D) if sensor_on_b else (o, D)
+        m, mc = ga - gbm, ca - cbm
+        t = -(m @ oo + mc) / (m @ DD)
+        x = oo + t * DD
+        return ga @ x + ca, x
+
+    p0, x0 = hit(np.eye(3), np.zeros(3))
+    ga, gb = EA * ga_u, EB * gb_u
+    mD = (ga - gb) @ D
+    ka, kb = ga @ D / mD, -(gb @ D) / mD
+    gv = gb * (-ka) if not sensor_on_b else ga * kb
+    want = np.concatenate([np.cross(x0, gv), gv, [kb * p0 / EA, ka * p0 / EB]])
+    h = 1e-7
+    got = np.zeros(8)
+    for c in range(6):
+        w, v = np.zeros(3), np.zeros(3)
+        if c < 3:
+            w[c] = h
+        else:
+            v[c - 3] = h
+        got[c] = (hit(_rotation(w), v)[0] - hit(_rotation(-w), -v)[0]) / (2 * h)
+    got[6] = (hit(np.eye(3), np.zeros(3), fa=1 + h)[0] - hit(np.eye(3), np.zeros(3), fa=1 - h)[0]) / (2 * h * EA)
+    got[7] = (hit(np.eye(3), np.zeros(3), fb=1 + h)[0] - hit(np.eye(3), np.zeros(3), fb=1 - h)[0]) / (2 * h * EB)
+    assert np.allclose(got, want, rtol=1e-6, atol=1e-9 * np.abs(want).max()), (got, want)
