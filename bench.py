@@ -79,8 +79,35 @@ def max_over_ranks(x: float, world: int) -> float:
 
 
 def workload(n_scenes, rank):
+    """The tactile scenes; the plate is 0.1 mm wider in x than in y so that no
+    ray sample lies exactly on its top face's diagonal (where any two ray
+    casters may disagree by one sample)."""
     from mujoco_contact_surfaces_gb300 import scenes
-    return scenes.tactile(n_scenes, seed=scenes.SEED_ADJOINT + rank, velocities=True)
+    return scenes.tactile(n_scenes, seed=scenes.SEED_ADJOINT + rank, velocities=True,
+                          plate_half=(0.0401, 0.04, 0.005))
+
+
+def sample_pairs(n_pair, n_sample):
+    """Evenly spaced pairs of the workload: the CPU legs' bounded sample."""
+    n = min(n_sample, n_pair)
+    return sorted({int(round(k * (n_pair - 1) / max(1, n - 1))) for k in range(n)})
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
 
 
 def upstream(s, seed=17):
@@ -99,12 +126,17 @@ def config_dict(args, world, extra=None):
     return c
 
 
-def cpu_baseline(n_sample, rank, reps=3):
-    """FP64 oracle, OpenMP over pairs, all host cores, on a bounded sample
-    (forward only: the reference has no adjoint)."""
+def cpu_sample_scene(s, n_sample):
+    from mujoco_contact_surfaces_gb300 import scenes
+    pairs = sample_pairs(len(s.g1), n_sample)
+    return pairs, scenes.subscene(s, pairs)
+
+
+def cpu_baseline(sub, n_pairs, reps=3):
+    """FP64 oracle, OpenMP over pairs, all host cores, on a bounded sample of
+    the workload's pairs (forward only: the reference path has no adjoint)."""
     import oracle
-    s = workload(n_sample, rank)
-    o = oracle.Oracle(s)
+    o = oracle.Oracle(sub)
     o.collide()
     ts = []
     for _ in range(reps):
@@ -113,9 +145,48 @@ def cpu_baseline(n_sample, rank, reps=3):
         ts.append(time.perf_counter() - t0)
     o.close()
     t = statistics.median(ts)
-    return {"value": n_sample / t, "unit": "pairs/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{n_sample} scenes of the same workload, forward only (the reference path has no "
-                      f"adjoint), median of {reps}"}
+    return {"value": n_pairs / t, "unit": "pairs/s", "cores": os.cpu_count(), "cpu_model": cpu_model(),
+            "kind": "port",
+            "sample": f"{n_pairs} evenly spaced scenes of the timed workload (one pair and one 16x16 sensor each), "
+                      f"forward only (the reference path has no adjoint), FP64, OpenMP over pairs, median of {reps}"}
+
+
+def accuracy(sub, pairs, w, stats, taxels):
+    """The timed step's wrenches, contact areas and taxel maps of the sampled
+    pairs against the FP64 oracle on the same pairs (outside the timed
+    region).  Taxel errors are relative to each map's largest value."""
+    import oracle
+    o = oracle.Oracle(sub)
+    ref = o.collide()
+    o.close()
+    F, Fo = w[pairs, :3], ref["wrench"][:, :3]
+    T, To = w[pairs, 3:], ref["wrench"][:, 3:]
+    fo = np.linalg.norm(Fo, axis=1)
+    area_ref = ref["area"]
+    ef = np.linalg.norm(F - Fo, axis=1) / np.maximum(fo, 1e-9)
+    et = np.linalg.norm(T - To, axis=1) / np.maximum(np.linalg.norm(To, axis=1) + fo * np.sqrt(area_ref), 1e-12)
+    area = np.array([stats[p].area for p in pairs])
+    nz = area_ref > 0
+    ea = np.abs(area[nz] - area_ref[nz]) / area_ref[nz]
+    # a cell may differ by one ray sample (a ray within float rounding of a
+    # contact-polygon edge is hit or missed by either caster); one sample
+    # weighs p / 25 and is bounded by twice the map's largest value / 25
+    t_err, t_all, one = 0.0, 0.0, 0
+    one_sample = 2.0 / 25.0 * 1.001 + 1e-5
+    for j, p in enumerate(pairs):
+        to = ref["taxels"][j].astype(np.float64)
+        scale = max(float(np.abs(to).max()), 1e-12)
+        d = np.abs(taxels[p].astype(np.float64) - to) / scale
+        sample_off = (d > 1e-5) & (d <= one_sample)
+        one += int(np.sum(sample_off))
+        t_err = max(t_err, float(d[~sample_off].max(initial=0.0)))
+        t_all = max(t_all, float(d.max()))
+    return {"n_pairs": len(pairs), "n_touching": int(np.sum(nz)), "max_rel_wrench_err": float(max(ef.max(), et.max())),
+            "max_rel_force_err": float(ef.max()), "max_rel_torque_err": float(et.max()),
+            "max_rel_area_err": float(ea.max(initial=0.0)), "max_taxel_err_frac": t_err,
+            "taxel_cells_one_ray_sample_off": one, "max_taxel_err_frac_incl_those": t_all,
+            "taxel_cells": 256 * len(pairs),
+            "oracle": "FP64 CPU restatement (oracle/), same pairs, same poses"}
 
 
 class Clocks:
@@ -177,12 +248,13 @@ def algorithmic_bytes(eng, n_pair, n_sensor_pairs):
     eng.step()
     cand = eng.candidates()
     eng.set_debug(0)
-    tets = len({(int(r[0]), int(r[1])) for r in cand})
-    tris = len({(int(r[0]), int(r[2])) for r in cand if r[2] >= 0})
+    tets = len(np.unique(cand[:, 0] * (1 << 32) + cand[:, 1]))
+    rig = cand[cand[:, 2] >= 0]
+    tris = len(np.unique(rig[:, 0] * (1 << 32) + rig[:, 2]))
     elem = 80 * tets + 48 * tris
     fwd = elem + (96 + 48) * n_pair + 1024 * n_sensor_pairs
     adj = fwd + (48 + 104) * n_pair + 1024 * n_sensor_pairs
-    return dict(elem=elem, fwd=fwd, adj=adj, tets=tets, tris=tris, polygons=len(cand))
+    return dict(elem=elem, fwd=fwd, adj=adj, step=fwd + adj, tets=tets, tris=tris, polygons=len(cand))
 
 
 def plain_path(s_full, n_sample, dLdw, dLdt, local):
@@ -368,6 +440,8 @@ def run_gb300(args):
                                             "element_pairs_per_s": ab["polygons"] * world / (t_step * 1e-3),
                                             "tets_touched": ab["tets"],
                                             "tris_touched": ab["tris"], "ms_forward": t_step - adj_avg,
+                                            # forward alone (like for like with the CPU legs)
+                                            "forward_pairs_per_s": n_pair * world / ((t_step - adj_avg) * 1e-3),
                                             "ms_adjoint": adj_avg, "ms_narrow_kernel": narrow_avg,
                                             "ms_kept_polygons_pass": kept_avg,
                                             "autotuned": {"ctas_per_sm": tuned_ctas, "chunk": tuned_chunk},
@@ -378,18 +452,31 @@ def run_gb300(args):
                      "frac": achieved / hbm_peak, "traffic": traffic,
                      "traffic_source": "ncu dram bytes of one launch at 1024 scenes, scaled by scenes",
                      "kernel": kname, "kernel_ms": kms,
-                     "algorithmic_bytes": kbytes, "step_algorithmic_bytes": ab["adj"],
-                     "step_achieved_gbs": ab["adj"] / (t_step * 1e-3) / 1e9, "peak_source": peak_src},
+                     "algorithmic_bytes": kbytes,
+                     # the whole step by the per-pair formula: B_fwd + B_adj, the
+                     # adjoint reading the elements again
+                     "step_algorithmic_bytes": ab["step"],
+                     "step_achieved_gbs": ab["step"] / (t_step * 1e-3) / 1e9,
+                     "step_frac": ab["step"] / (t_step * 1e-3) / 1e9 / hbm_peak, "peak_source": peak_src},
         "clocks": clk,
     }
+    # accuracy of the timed step on a sample of its pairs (outside the timed
+    # region): the last step's outputs against the FP64 oracle
+    w_last = eng.wrenches()
+    stats = eng.pair_stats()
+    tax = eng.all_taxels().reshape(len(s.sensors), -1)
+    pairs, sub = cpu_sample_scene(s, args.cpu_sample)
+    line["accuracy"] = accuracy(sub, pairs, w_last, stats, tax)
+    eng.close()
     if rank == 0 and not args.no_plain:
         pv, pl = plain_path(s, min(args.plain_sample, len(s.g1)), dLdw_h, dLdt_h, local)
         line["config"]["plain_pairs_per_s"] = pv
+        # device-timed batched over host-timed plain, and host over host
         line["config"]["batched_over_plain"] = value / world / pv
+        line["config"]["e2e_over_plain"] = e2e / world / pv
         line["config"]["plain_launches_per_scene"] = pl
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args.cpu_sample, rank)
-    eng.close()
+        line["cpu_baseline"] = cpu_baseline(sub, len(pairs))
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -401,8 +488,8 @@ def run_reference(args):
     if rank != 0:
         return
     import oracle
-    n = args.cpu_sample
-    s = workload(n, 0)
+    pairs, s = cpu_sample_scene(workload(args.scenes, 0), args.cpu_sample)
+    n = len(pairs)
     o = oracle.Oracle(s)
     for _ in range(args.warmup):
         o.collide()
@@ -419,8 +506,10 @@ def run_reference(args):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64 scenes)", "impl": "reference",
             "config": config_dict(args, world, {"scenes_per_step": n, "pass": "forward only (the reference path "
                                                                             "has no adjoint)"}),
-            "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": f"{n} scenes of the workload per step (FP64 oracle, OpenMP over pairs)"},
+            "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": os.cpu_count(), "cpu_model": cpu_model(),
+                             "kind": "port",
+                             "sample": f"{n} evenly spaced scenes of the {args.scenes}-scene workload per step "
+                                       f"(FP64 oracle, OpenMP over pairs, all host threads)"},
             "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

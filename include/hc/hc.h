@@ -408,8 +408,11 @@ HC_API hc_status hc_set_launch_shape(hc_context* ctx, int ctas_per_sm, int chunk
  *   n_geom, d_xpos, d_xmat, d_vel: device poses and velocities for geom ids
  *       [0, n_geom), in the layout of hc_set_poses (d_vel may be NULL);
  *   d_wrench: device output, n_pair x 6 doubles, as hc_get_wrenches;
- *   d_taxels: device output, all sensors' taxel maps, as
+ *   d_taxels: device output, all flat sensors' taxel maps, as
  *       hc_get_taxels_device (NULL allowed when the context has no sensor);
+ *       a context with taxel-point (hc_add_taxel_sensor) or curved
+ *       (hc_add_curved_sensor) sensors is refused with HC_ERR_UNSUPPORTED:
+ *       those sensors read kept polygons, which this step does not keep;
  *   stream: the cudaStream_t to run on, or NULL for the context's stream.
  *
  * The context must be ready: hc_set_pairs called after the last change of

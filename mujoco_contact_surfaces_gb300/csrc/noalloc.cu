@@ -91,6 +91,12 @@ extern "C" HC_API hc_status hc_step_noalloc(hc_context* ctx, int n_geom, const d
     if (!d_xpos || !d_xmat) return hc::set_last_error(HC_ERR_INVALID_ARG, "d_xpos and d_xmat are required");
     if (!d_wrench) return hc::set_last_error(HC_ERR_INVALID_ARG, "d_wrench is required");
   }
+  // Taxel-point and curved sensors read the polygons a step keeps, which
+  // this step does not keep: refuse rather than leave their values stale.
+  if (a.n_tsens > 0 || a.n_csens > 0)
+    return hc::set_last_error(HC_ERR_UNSUPPORTED,
+                              "hc_step_noalloc evaluates flat sensors only; the context has taxel-point or curved "
+                              "sensors (use hc_step)");
   if (a.n_cells_total > 0 && !d_taxels) return hc::set_last_error(HC_ERR_INVALID_ARG, "d_taxels is required (the context has sensors)");
   if (n_pair == 0 && a.n_cells_total == 0) return HC_OK;
 

@@ -199,13 +199,10 @@ class Engine:
     def candidates(self) -> np.ndarray:
         n = C.c_int64()
         L.check(self.lib.hc_get_candidates(self.ctx, None, 0, C.byref(n)))
-        arr = (L.hc_candidate * max(1, n.value))()
-        L.check(self.lib.hc_get_candidates(self.ctx, arr, n.value, C.byref(n)))
-        out = np.zeros((n.value, 5), np.int64)
-        for i in range(n.value):
-            r = arr[i]
-            out[i] = (r.pair, r.elem_a, r.elem_b, r.n_vert, r.flags)
-        return out
+        buf = np.zeros((max(1, n.value), 5), np.int32)   # hc_candidate: five int32 fields
+        L.check(self.lib.hc_get_candidates(self.ctx, buf.ctypes.data_as(C.POINTER(L.hc_candidate)), n.value,
+                                           C.byref(n)))
+        return buf[:n.value].astype(np.int64)
 
     def surface(self, pair: int):
         v = L.hc_surface_view()

@@ -372,8 +372,9 @@ def _touch_height(a, Ra, ca, b, Rb, cb, n=48, rounds=8):
     return best if best is not None else -(max(a[2]) + max(b[2]))
 
 
-def halfspace(n_pairs=8, seed=SEED_SINGLE + 500) -> Scene:
-    """Soft primitives resting on a rigid ground plane (plane geom)."""
+def halfspace(n_pairs=8, seed=SEED_SINGLE + 500, min_frac=0.0) -> Scene:
+    """Soft primitives resting on a rigid ground plane (plane geom), sunk by
+    U[min_frac, 0.1] of their extent."""
     rng = np.random.Generator(np.random.PCG64(seed))
     s = Scene()
     ground = s.add_geom(L.GEOM_PLANE, [0, 0, 1], [0, 1.0, 0, 0.5, 0.5])
@@ -396,9 +397,37 @@ def halfspace(n_pairs=8, seed=SEED_SINGLE + 500) -> Scene:
             r, hl = ssize[0], ssize[1]
             low = float(r * math.sqrt(max(0.0, 1 - Rs[2, 2] ** 2)) + hl * abs(Rs[2, 2]))
         s.xmat[g] = Rs.reshape(9)
-        s.xpos[g] = [rng.uniform(-1, 1), rng.uniform(-1, 1), low - rng.uniform(0, 0.1) * sext]
+        s.xpos[g] = [rng.uniform(-1, 1), rng.uniform(-1, 1), low - rng.uniform(min_frac, 0.1) * sext]
         s.vel[g] = rng.uniform(-0.1, 0.1, 6)
     return s
+
+
+def subscene(s: Scene, pairs) -> Scene:
+    """The geoms, poses, sensors and pairs of the given pair indices of `s`,
+    geoms registered in their original relative order (so each pair's M/N
+    order is the one it has in `s`); pair k of the result is pairs[k] in
+    sorted order, and a sensor is kept when its geom is."""
+    pairs = sorted(int(p) for p in pairs)
+    keep = sorted({s.g1[p] for p in pairs} | {s.g2[p] for p in pairs})
+    remap = {g: i for i, g in enumerate(keep)}
+    t = Scene()
+    for g in keep:
+        d = s.geoms[g]
+        t.add_geom(d["type"], d["size"], d["cs5"], d["mesh_v"], d["mesh_f"])
+    _alloc(t)
+    for g in keep:
+        t.xpos[remap[g]] = s.xpos[g]
+        t.xmat[remap[g]] = s.xmat[g]
+        t.vel[remap[g]] = s.vel[g]
+    for p in pairs:
+        t.g1.append(remap[s.g1[p]]); t.g2.append(remap[s.g2[p]])
+        t.scene_of_pair.append(s.scene_of_pair[p] if s.scene_of_pair else 0)
+    for sn in s.sensors:
+        if sn["geom"] in remap:
+            d = dict(sn)
+            d["geom"] = remap[sn["geom"]]
+            t.sensors.append(d)
+    return t
 
 
 def build_engine(scene: Scene, **engine_kw):

@@ -16,8 +16,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 
 
+MESHGEN = [os.path.join(HERE, "..", "mujoco_contact_surfaces_gb300", "csrc", f) for f in ("meshgen.cpp", "meshgen.h")]
+
+
 def build(force: bool = False) -> str:
-    src = [os.path.join(HERE, f) for f in ("oracle.c", "taxel.c", "curved.c", "oracle.h", "Makefile")]
+    src = [os.path.join(HERE, f) for f in ("oracle.c", "taxel.c", "curved.c", "oracle.h", "or_mesh.cpp", "Makefile")]
+    src += MESHGEN
     if force or not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in src):
         r = subprocess.run(["make", "-s", "-C", HERE, "-B" if force else "-s"], capture_output=True, text=True)
         if r.returncode != 0:
@@ -85,6 +89,9 @@ def load():
         lib.or_curved_select.argtypes = [C.c_int, dp, dp, C.c_double, C.c_int, dp, dp, ip, ip, dp]
         lib.or_curved_update.argtypes = [C.c_int, ip, ip, dp, C.c_int, dp, dp, C.c_double, C.c_int, ip, ip, dp,
                                          dp, dp, dp]
+        lib.or_generate_mesh.restype = C.c_int
+        lib.or_generate_mesh.argtypes = [C.c_int, dp, dp, dp, C.c_int, ip, C.c_int, ip, ip, ip, dp, dp, ip,
+                                         C.c_char_p, C.c_int]
         _lib = lib
     return _lib
 
@@ -95,6 +102,31 @@ def _dp(a):
 
 def _ip(a):
     return a.ctypes.data_as(C.POINTER(C.c_int)) if a is not None else None
+
+
+def generate_mesh(gtype: int, size, cs5, mesh_vert=None, mesh_face=None):
+    """The scene mesh of one geom from the package's generator source,
+    compiled into this library (or_mesh.cpp): (kind, verts, pressures or
+    None, elems), the same arrays as the engine's hc_generate_mesh."""
+    lib = load()
+    size = np.ascontiguousarray(size, np.float64)
+    cs5 = np.ascontiguousarray(cs5, np.float64)
+    mv = np.ascontiguousarray(mesh_vert, np.float64).reshape(-1) if mesh_vert is not None else None
+    mf = np.ascontiguousarray(mesh_face, np.int32).reshape(-1) if mesh_face is not None else None
+    nv_in = 0 if mv is None else len(mv) // 3
+    nf_in = 0 if mf is None else len(mf) // 3
+    kind, nv, ne = C.c_int(), C.c_int(), C.c_int()
+    err = C.create_string_buffer(256)
+    if lib.or_generate_mesh(gtype, _dp(size), _dp(cs5), _dp(mv), nv_in, _ip(mf), nf_in, C.byref(kind), C.byref(nv),
+                            C.byref(ne), None, None, None, err, 256):
+        raise ValueError(f"mesh generation failed: {err.value.decode()}")
+    npe = 4 if kind.value == 1 else 3
+    v = np.zeros((nv.value, 3), np.float64)
+    e = np.zeros((ne.value, npe), np.int32)
+    p = np.zeros(nv.value, np.float64) if kind.value == 1 else None
+    lib.or_generate_mesh(gtype, _dp(size), _dp(cs5), _dp(mv), nv_in, _ip(mf), nf_in, C.byref(kind), C.byref(nv),
+                         C.byref(ne), _dp(v), _dp(p), _ip(e), err, 256)
+    return kind.value, v, p, e
 
 
 class Oracle:
@@ -110,7 +142,7 @@ class Oracle:
         self.meshes = meshes or {}
         for i, g in enumerate(scene.geoms):
             if g["id"] not in self.meshes:
-                self.meshes[g["id"]] = L.generate_mesh(g["type"], g["size"], g["cs5"], g["mesh_v"], g["mesh_f"])
+                self.meshes[g["id"]] = generate_mesh(g["type"], g["size"], g["cs5"], g["mesh_v"], g["mesh_f"])
             kind, v, p, e = self.meshes[g["id"]]
             v = np.ascontiguousarray(v, np.float64)
             e = np.ascontiguousarray(e, np.int32)
@@ -203,11 +235,8 @@ class Oracle:
             taxels64=t64,
         )
         if candidates:
-            c = np.zeros((ncand.value, 5), np.int64)
-            for i in range(ncand.value):
-                r = cand[i]
-                c[i] = (r.pair, r.elem_a, r.elem_b, r.n_vert, r.flags)
-            res["candidates"] = c
+            res["candidates"] = np.ctypeslib.as_array(
+                C.cast(cand, C.POINTER(C.c_int32)), shape=(max(1, cap), 5))[:ncand.value].astype(np.int64)
         return res
 
     def surface(self, g1, g2, xpos=None, xmat=None):

@@ -191,9 +191,10 @@ def _scaled_moduli(s, geoms, f):
     return st
 
 
-def _pair_losses(s, dLdw, dLdt):
-    r = Oracle(s).collide(taxels64=True)
-    return np.array([np.dot(dLdw[p], r["wrench"][p]) + np.dot(dLdt[p], r["taxels64"][p]) for p in range(len(s.g1))])
+def _pair_losses(s, dLdw, dLdt, representation=0):
+    r = Oracle(s).collide(representation=representation, taxels64=dLdt is not None, sensors=dLdt is not None)
+    return np.array([np.dot(dLdw[p], r["wrench"][p]) + (np.dot(dLdt[p], r["taxels64"][p]) if dLdt is not None else 0.0)
+                     for p in range(len(s.g1))])
 
 
 def test_soft_soft_gradient_poses_and_moduli(gpu):
@@ -304,3 +305,61 @@ def test_gradient_polygon_quadrature_soft_rigid(gpu):
         got = dpose[p].reshape(12)
         err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
         assert err <= GRAD_RTOL, f"pair {p}: rel err {err:.2e}\n{got}\n{ref}"
+
+
+@pytest.mark.parametrize("adjoint_mode", [True, False])
+def test_halfspace_gradient_poses_and_modulus(gpu, adjoint_mode):
+    # soft primitives on a rigid ground plane (the half-space query).  In
+    # adjoint mode the reverse reads the polygons the step kept; without it
+    # (and without sensors) the half-space adjoint kernel recomputes them.
+    # Poses against central differences of the oracle; the wrench is linear
+    # in the soft modulus, so dL/dE = L / E.
+    s = scenes.halfspace(4, min_frac=0.03)
+    rng = np.random.default_rng(29)
+    dLdw = rng.normal(size=(len(s.g1), 6))
+    w, _, dpose, dE = run_adjoint(s, dLdw, None, adjoint_mode=adjoint_mode)
+    orc = Oracle(s)
+    r0 = orc.collide()
+    assert np.all(r0["query"] == 2)
+    for p in range(len(s.g1)):
+        assert np.linalg.norm(w[p] - r0["wrench"][p]) <= 1e-5 * np.linalg.norm(r0["wrench"][p])
+        ref = fd_gradient(orc, s, p, dLdw, None)
+        got = dpose[p].reshape(12)
+        err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
+        assert err <= GRAD_RTOL, f"pair {p}: rel err {err:.2e}\n{got}\n{ref}"
+        soft = 0 if s.geoms[r0["m"][p]]["cs5"][0] > 0 else 1
+        E = s.geoms[(r0["m"], r0["n"])[soft][p]]["cs5"][0]
+        L0 = float(np.dot(dLdw[p], r0["wrench"][p]))
+        assert dE[p, 1 - soft] == 0.0
+        assert abs(dE[p, soft] - L0 / E) <= 1e-4 * abs(L0 / E), (p, dE[p], L0 / E)
+
+
+def test_soft_soft_gradient_polygon_quadrature(gpu):
+    # kPolygon on soft-soft pairs: one quadrature point per polygon, the
+    # polygon recomputed in the reverse with its equal-pressure plane moving
+    # with N's field and with both moduli (wrench upstream: the taxel maps do
+    # not depend on the quadrature).  Poses and both moduli against central
+    # differences of the oracle with the same quadrature.
+    from mujoco_contact_surfaces_gb300 import _lib as L
+    s = scenes.soft_soft_pressed(4)
+    rng = np.random.default_rng(31)
+    dLdw = rng.normal(size=(len(s.g1), 6))
+    w, _, dpose, dE = run_adjoint(s, dLdw, None, representation=L.REPR_POLYGON)
+    orc = Oracle(s)
+    r0 = orc.collide(representation=1, sensors=False)
+    for p in range(len(s.g1)):
+        assert np.linalg.norm(w[p] - r0["wrench"][p]) <= 1e-5 * np.linalg.norm(r0["wrench"][p])
+        ref = fd_gradient(orc, s, p, dLdw, None, representation=1)
+        got = dpose[p].reshape(12)
+        err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
+        assert err <= GRAD_RTOL, f"pair {p}: rel err {err:.2e}\n{got}\n{ref}"
+    h = 1e-3
+    ref = np.zeros((len(s.g1), 2))
+    for b, geoms in enumerate((r0["m"], r0["n"])):
+        lp = _pair_losses(_scaled_moduli(s, geoms, 1 + h), dLdw, None, representation=1)
+        lm = _pair_losses(_scaled_moduli(s, geoms, 1 - h), dLdw, None, representation=1)
+        E = np.array([s.geoms[g]["cs5"][0] for g in geoms])
+        ref[:, b] = (lp - lm) / (2 * h * E)
+    for p in range(len(s.g1)):
+        err = np.linalg.norm(dE[p] - ref[p]) / max(np.linalg.norm(ref[p]), 1e-30)
+        assert err <= GRAD_RTOL, f"pair {p}: dE rel err {err:.2e}\n{dE[p]}\n{ref[p]}"

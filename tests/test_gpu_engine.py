@@ -112,3 +112,41 @@ def test_update_geom_size_matches_fresh_engine(gpu):
     ref = _outputs(fresh, s)
     fresh.close()
     _same(ref, got)
+
+
+@pytest.mark.parametrize("which", ["soft", "rigid"])
+def test_update_geom_size_matches_oracle(gpu, which):
+    # hc_update_geom_size (the reference's onGeomChanged) regenerates the
+    # geom's mesh, field and LBVH; the next step must equal the FP64 oracle
+    # run on the resized primitive (candidates, counts, area, wrench, taxels)
+    from oracle import Oracle
+    from tests.test_gpu_parity import check_pairs
+    from tests._parity import taxel_check
+    if which == "soft":
+        s = scenes.tactile(6, velocities=True, plate_half=(0.0401, 0.04, 0.005), min_pen=5e-4)
+    else:
+        s = scenes.single_pair(6, velocities=True)
+    eng = scenes.build_engine(s)
+    eng.set_debug(1)
+    eng.step()
+    for p in range(len(s.g1)):
+        g = s.g1[p] if which == "soft" else s.g2[p]
+        size = np.array(s.geoms[g]["size"], np.float64)
+        if which == "soft":
+            size = size * 1.04                     # every half-size and radius
+        else:
+            size[:2] *= 0.6 + 0.1 * p              # a smaller box top, same height
+        eng.update_geom_size(g, size)
+        s.geoms[g]["size"] = size
+    eng.step()
+    out = dict(wrench=eng.wrenches(), stats=eng.pair_stats(), cand=eng.candidates(), order=eng.pair_order(),
+               taxels=[eng.taxels(k) for k in range(len(s.sensors))])
+    eng.close()
+    orc = Oracle(s)
+    ref = orc.collide(candidates=True)
+    orc.close()
+    check_pairs(out, ref, min_polys=200)
+    for k in range(len(s.sensors)):
+        tg, to = out["taxels"][k], ref["taxels"][k]
+        bad, one = taxel_check(tg, to, float(np.abs(to).max()) / 25.0 * 2.0)
+        assert bad == 0 and one <= 2, (k, bad, one)

@@ -1,43 +1,62 @@
-"""The batched workloads at their full sizes, through properties that do not
-depend on size (the oracle checks element-level parity on the smaller
-scenes of test_gpu_parity):
+"""The batched workloads at their full sizes against the FP64 oracle:
 
 * 4096 independent scenes of 1-8 soft-rigid pairs, soft meshes of 500-20000
   tets and rigid meshes of 12-5000 triangles (18402 pairs, ~170M elements);
-* 1024 soft-soft pairs of 2k-50k tets each.
+* 1024 soft-soft pairs of 2k-50k tets each, E ratio 0.1-10.
 
-Properties: a repeated step is bit-identical; every pair's wrench, and (soft-
-rigid) its adjoint, is bit-identical to that pair computed alone in its own
-context — the batch changes the scheduling, never a pair's arithmetic; the
-forces are finite and the contacts non-trivial."""
+The whole batch runs as one step.  A sample of its pairs (the largest
+contacts and random others) is compared with the oracle on exactly those
+pairs: candidate element-pair sets and per-pair polygon counts equal after a
+canonical sort (near-degenerate pairs counted and reported), area and wrench
+within 1e-5.  Properties that hold at any size are checked on the whole
+batch: a repeated step is bit-identical, and sampled pairs computed alone in
+their own context give the batch's wrench and adjoint bit for bit (the batch
+changes the scheduling, never a pair's arithmetic)."""
 import numpy as np
 import pytest
 
 from mujoco_contact_surfaces_gb300 import scenes
+from oracle import Oracle
+from tests._parity import AREA_RTOL, WRENCH_RTOL, compare_candidates, wrench_errors
 
 pytestmark = pytest.mark.gpu
 
 
-def subscene(s, pairs):
-    """The geoms, poses and pairs of the given pair indices, registered in
-    their original relative order (so M/N stay as in the batch)."""
-    keep = sorted({s.g1[p] for p in pairs} | {s.g2[p] for p in pairs})
-    remap = {g: i for i, g in enumerate(keep)}
-    t = scenes.Scene()
-    for g in keep:
-        d = s.geoms[g]
-        t.add_geom(d["type"], d["size"], d["cs5"], d["mesh_v"], d["mesh_f"])
-    scenes._alloc(t)
-    for g in keep:
-        t.xpos[remap[g]] = s.xpos[g]
-        t.xmat[remap[g]] = s.xmat[g]
-        t.vel[remap[g]] = s.vel[g]
-    for p in pairs:
-        t.g1.append(remap[s.g1[p]]); t.g2.append(remap[s.g2[p]]); t.scene_of_pair.append(0)
-    return t
+def _sample(npoly, n_sample, rng):
+    n_pair = len(npoly)
+    big = list(np.argsort(-npoly)[:n_sample // 4])
+    rest = rng.choice(n_pair, n_sample, replace=False)
+    return sorted(list(dict.fromkeys(int(x) for x in big + list(rest)))[:n_sample])
 
 
-def _check(s, n_sample, adjoint, seed):
+def _oracle_parity(s, pairs, w, stats, cand):
+    """The batch's outputs of `pairs` against the oracle on those pairs."""
+    sub = scenes.subscene(s, pairs)
+    orc = Oracle(sub)
+    ref = orc.collide(candidates=True)
+    orc.close()
+    pos = {p: k for k, p in enumerate(pairs)}
+    sel = np.isin(cand[:, 0], pairs)
+    mine = cand[sel].copy()
+    mine[:, 0] = [pos[int(p)] for p in mine[:, 0]]
+    bad, near, common = compare_candidates(mine, ref["candidates"])
+    assert not bad, f"{len(bad)} candidate mismatches (first: {bad[:5]}), {near} near-degenerate"
+    npoly = np.array([stats[p].n_polygons for p in pairs])
+    if near == 0:
+        assert np.array_equal(npoly, ref["n_polygons"])
+    area = np.array([stats[p].area for p in pairs])
+    nz = ref["area"] > 0
+    ea = np.abs(area[nz] - ref["area"][nz]) / ref["area"][nz]
+    assert ea.max(initial=0) <= AREA_RTOL, f"area rel err {ea.max():.3e}"
+    ef, et = wrench_errors(w[pairs], ref["wrench"], ref["area"])
+    assert ef.max() <= WRENCH_RTOL, f"force rel err {ef.max():.3e}"
+    assert et.max() <= WRENCH_RTOL, f"torque rel err {et.max():.3e}"
+    print(f"{len(pairs)} pairs, {common} polygons in common, {near} near-degenerate element pairs, "
+          f"max rel err: force {ef.max():.2e}, torque {et.max():.2e}, area {ea.max(initial=0):.2e}")
+    return common
+
+
+def _check(s, n_oracle, n_alone, adjoint, seed, min_polys):
     rng = np.random.Generator(np.random.PCG64(seed))
     n_pair = len(s.g1)
     eng = scenes.build_engine(s)
@@ -56,13 +75,18 @@ def _check(s, n_sample, adjoint, seed):
         dpose, dE = eng.adjoint(up)
         assert np.all(np.isfinite(dpose)) and np.all(np.isfinite(dE))
     stats = eng.pair_stats()
+    # the same step with candidate recording: the candidate list of every pair
+    eng.set_debug(1)
+    eng.step()
+    cand = eng.candidates()
+    assert np.allclose(eng.wrenches(), w1, rtol=1e-9, atol=0)
     eng.close()
-    # the sample: the largest contacts and random others
     npoly = np.array([st.n_polygons for st in stats])
-    pick = list(np.argsort(-npoly)[:n_sample // 2]) + list(rng.choice(n_pair, n_sample - n_sample // 2,
-                                                                       replace=False))
-    for p in dict.fromkeys(int(x) for x in pick):
-        e = scenes.build_engine(subscene(s, [p]))
+    pairs = _sample(npoly, n_oracle, rng)
+    assert _oracle_parity(s, pairs, w1, stats, cand) >= min_polys
+    # a few pairs computed alone in their own context
+    for p in pairs[:n_alone // 2] + [int(x) for x in np.argsort(-npoly)[:n_alone - n_alone // 2]]:
+        e = scenes.build_engine(scenes.subscene(s, [p]))
         if adjoint:
             e.set_adjoint_mode(True)
         e.step()
@@ -77,9 +101,9 @@ def _check(s, n_sample, adjoint, seed):
 def test_batched_4096_scenes(gpu):
     s = scenes.batched(4096)
     assert len(s.g1) > 16000
-    _check(s, 16, adjoint=True, seed=3)
+    _check(s, n_oracle=384, n_alone=8, adjoint=True, seed=3, min_polys=20000)
 
 
 def test_soft_soft_1024_pairs(gpu):
     s = scenes.soft_soft(1024)
-    _check(s, 12, adjoint=False, seed=4)
+    _check(s, n_oracle=128, n_alone=6, adjoint=False, seed=4, min_polys=20000)

@@ -1,7 +1,7 @@
 """Taxel-point sensor (hc_add_taxel_sensor) against the oracle's restatement
-of TaxelSensor::internal_update, evaluated on the engine's own contact
-surfaces (hc_get_surface: the polygons are checked against the oracle by the
-parity tests).  Two steps: the second moves one soft body out of contact
+of TaxelSensor::internal_update, evaluated both on the engine's own contact
+surfaces (hc_get_surface: the sensor alone) and on the oracle's surfaces (end
+to end).  Two steps: the second moves one soft body out of contact
 and shifts another, so kept values and the empty case are exercised."""
 import numpy as np
 import pytest
@@ -37,6 +37,19 @@ def _surfaces(eng, s, geom):
     return out
 
 
+def _oracle_surfaces(orc, s, geom, xpos):
+    """The oracle's own contact surfaces of the pairs that touch `geom`, in
+    collision order (world frame, polygons in (soft element, other element)
+    order): the sensor checked end to end, surfaces included."""
+    out = []
+    for p in range(len(s.g1)):
+        if geom in (s.g1[p], s.g2[p]):
+            srf = orc.surface(s.g1[p], s.g2[p], xpos=xpos)
+            out.append(dict(poly_offset=srf["offset"], vert=srf["vert"], vert_pressure=srf["pressure"],
+                            normal=srf["normal"]))
+    return out
+
+
 def _check(got, ref, scale, what):
     bad = np.abs(got - ref) > 1e-4 * scale + 1e-9
     assert bad.sum() == 0, (what, np.where(bad), got[bad], ref[bad], scale)
@@ -53,6 +66,8 @@ def test_taxel_sensor_matches_oracle(gpu):
             sensors[(plate, ci)] = eng.add_taxel_sensor(plate, tx, m, MARGIN, res, sm, bool(vis))
     eng.set_pairs(s.g1, s.g2)
     prev = {k: np.zeros(len(tx)) for k in sensors}
+    prev_e2e = {k: np.zeros(len(tx)) for k in sensors}
+    orc = oracle.Oracle(s)
     xpos = s.xpos.copy()
     for step in range(2):
         if step == 1:
@@ -69,6 +84,11 @@ def test_taxel_sensor_matches_oracle(gpu):
             scale = max(np.abs(ref).max(), 1e-12)
             _check(got, ref, scale, (step, plate, CONFIGS[ci]))
             prev[(plate, ci)] = ref
+            # end to end: the oracle's sensor on the oracle's surfaces
+            ref2 = oracle.taxel_sensor(tw, m, MARGIN, res, sm, vis, _oracle_surfaces(orc, s, plate, xpos),
+                                       values=prev_e2e[(plate, ci)])
+            _check(got, ref2, max(np.abs(ref2).max(), 1e-12), ("oracle surfaces", step, plate, CONFIGS[ci]))
+            prev_e2e[(plate, ci)] = ref2
             if step == 0 and plate == s.g2[0]:
                 assert np.count_nonzero(ref) > 0
         # one bulk copy of every sensor equals the per-sensor reads
@@ -77,6 +97,7 @@ def test_taxel_sensor_matches_oracle(gpu):
         if step == 1:
             assert all(np.all(prev[(s.g2[0], ci)] == 0.0) for ci in range(len(CONFIGS)))
     eng.close()
+    orc.close()
 
 
 def test_disabled_sensor_keeps_values(gpu):

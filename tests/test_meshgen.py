@@ -115,3 +115,25 @@ def test_convex_mesh_soft_is_centroid_fan():
     c = sv[np.argmax(sp)]
     np.testing.assert_allclose(c, 0, atol=1e-7)
     assert tet_vol(sv, se).sum() == pytest.approx(1.0, rel=1e-6)
+
+
+def test_oracle_builds_the_same_meshes():
+    # the oracle library compiles the generator source itself (so the CPU
+    # baseline loads no engine library); its meshes must be the engine's,
+    # bit for bit, for every primitive and kind the workloads use
+    import oracle
+    from mujoco_contact_surfaces_gb300 import scenes
+    cases = [(L.GEOM_SPHERE, [0.05, 0, 0], [1e5, 1, 0.01, 0.5, 0.5]),
+             (L.GEOM_ELLIPSOID, [0.04, 0.03, 0.02], [2e5, 1, sphere_hint(0.04, 4), 0.5, 0.5]),
+             (L.GEOM_CYLINDER, [0.03, 0.03, 0], [3e5, 1, 0.0075, 0.5, 0.5]),
+             (L.GEOM_BOX, [0.02, 0.03, 0.01], [1e5, 1, 0.005, 0.5, 0.5]),
+             (L.GEOM_BOX, [0.1, 0.1, 0.01], [0, 1, 0, 0.5, 0.5]),
+             (L.GEOM_PLANE, [0, 0, 1], [0, 1, 0, 0.5, 0.5])]
+    s = scenes.batched(6)
+    cases += [(g["type"], g["size"], g["cs5"]) for g in s.geoms]
+    for gtype, size, cs5 in cases:
+        a = L.generate_mesh(gtype, size, cs5)
+        b = oracle.generate_mesh(gtype, size, cs5)
+        assert a[0] == b[0]
+        for x, y in zip(a[1:], b[1:]):
+            assert (x is None and y is None) or np.array_equal(x, y)

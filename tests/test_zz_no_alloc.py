@@ -111,3 +111,28 @@ def test_noalloc_rejects_oversized_step(gpu):
         _check(w_ref, np.zeros(0), area, w, np.zeros(0))
     finally:
         eng.close()
+
+
+def test_noalloc_refuses_taxel_point_and_curved_sensors(gpu):
+    torch = pytest.importorskip("torch")
+    # taxel-point and curved sensors read the polygons hc_step keeps; the
+    # allocation-free step keeps none, so it refuses such a context instead
+    # of returning with their values untouched
+    scene = scenes.tactile(2, velocities=True)
+    grid = np.array([[x, y, 0.005] for x in (-0.01, 0.0, 0.01) for y in (-0.01, 0.0, 0.01)])
+    for kind in ("taxel", "curved"):
+        eng = scenes.build_engine(scene)
+        try:
+            plate = scene.sensors[0]["geom"]
+            if kind == "taxel":
+                eng.add_taxel_sensor(plate, grid, L.TAXEL_SQUARED, 0.002, 0.0015)
+            else:
+                pts = grid.copy()
+                nrm = np.tile([0.0, 0.0, 1.0], (len(pts), 1))
+                eng.add_curved_sensor(plate, grid, 0.005, pts, nrm)
+            eng.set_pairs(scene.g1, scene.g2)
+            with pytest.raises(L.HCError) as ei:
+                _noalloc(eng, torch, scene.xpos, scene.xmat, scene.vel, 256 * len(scene.sensors))
+            assert ei.value.status == L.HC_ERR_UNSUPPORTED and "flat sensors only" in str(ei.value)
+        finally:
+            eng.close()
