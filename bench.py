@@ -11,9 +11,10 @@ friction, per-pair wrenches, taxel binning, then the adjoint of the wrenches
 and taxel maps with respect to both bodies' poses and the modulus (seeded
 upstream gradients).  Synthetic seeded inputs: no dataset exists.
 
-`value` is timed with inputs resident in HBM; `e2e` goes through the C ABI
-with host buffers (poses and upstream gradients in, wrenches, taxel maps and
-gradients out every step).  The plain path (one scene per launch sequence,
+`value` is timed with inputs resident in HBM, each step one CUDA graph of
+the forward step and its adjoint (hc_step_adjoint_device); `e2e` goes through
+the C ABI with host buffers (hc_step_adjoint: poses and upstream gradients in,
+wrenches, taxel maps and gradients out every step, one wait).  The plain path (one scene per launch sequence,
 no graph) is timed on a sample for the batched/plain ratio.  `--impl
 reference` times the CPU path (the FP64 restatement in oracle/, OpenMP over
 pairs, all host threads) on a bounded sample of the same workload.
@@ -350,9 +351,9 @@ def run_gb300(args):
     torch.cuda.synchronize()
 
     def device_step():
+        # forward step and adjoint: one graph launch
         eng.set_poses_device(n_geom, xpos.data_ptr(), xmat.data_ptr(), vel.data_ptr())
-        eng.step()
-        eng.adjoint_device(dLdw.data_ptr(), dLdt.data_ptr())
+        eng.step_adjoint_device(dLdw.data_ptr(), dLdt.data_ptr())
 
     for _ in range(args.warmup):
         device_step()
@@ -364,22 +365,18 @@ def run_gb300(args):
     clocks = Clocks(local)
     clocks.start()
     step_ms, narrow_ms, kept_ms, adj_ms = [], [], [], []
-    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.fill_(1)
             e0.record(stream)
-        eng.set_poses_device(n_geom, xpos.data_ptr(), xmat.data_ptr(), vel.data_ptr())
-        eng.step()
-        with torch.cuda.stream(stream):
-            e1.record(stream)
-        eng.adjoint_device(dLdw.data_ptr(), dLdt.data_ptr())
+        device_step()
         with torch.cuda.stream(stream):
             e2.record(stream)
         e2.synchronize()
         step_ms.append(e0.elapsed_time(e2))
-        adj_ms.append(e1.elapsed_time(e2))
-        tm = eng.timings()
+        tm = eng.timings()   # the engine's stage events inside the graph
+        adj_ms.append(tm.ms_adjoint)
         narrow_ms.append(tm.ms_narrowphase)
         kept_ms.append(tm.ms_kept_polygons)
     torch.cuda.synchronize()
@@ -410,13 +407,11 @@ def run_gb300(args):
             flush.fill_(1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        eng.set_poses(hx, hm, hv)
-        eng.step()
-        eng.wrenches(out=ow)
-        eng.all_taxels(out=otx)
+        # poses and upstream gradients in, wrenches, taxel maps and gradients
+        # out: one call, one wait (hc_step_adjoint)
+        eng.step_adjoint(hx, hm, hv, hw, ht, out=(ow, otx, odp, odE))
         if args.taxel_sensors > 0:
             eng.all_taxel_sensor_values(out=ots)
-        eng.adjoint(hw, ht, out=(odp, odE))
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e = n_pair * world / (max_over_ranks(statistics.median(e2e_ms), world) * 1e-3)
 
@@ -448,6 +443,7 @@ def run_gb300(args):
                                             **extra}),
         "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches * args.steps,
+        "launches_per_step": launches, "graphs_per_step": 1,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
                      "traffic_source": "ncu dram bytes of one launch at 1024 scenes, scaled by scenes",

@@ -345,9 +345,10 @@ HC_API hc_status hc_get_curved_sensor_values(hc_context* ctx, int sensor, float*
  * Gradient of L with respect to both geoms' 6-DoF poses (twist
  * [dtheta; dx], world frame, applied as X <- exp(dtheta) X, x <- x + dx)
  * and the soft moduli, given dL/dwrench (n_pair x 6 doubles, may be NULL)
- * and dL/dtaxel (all sensors' maps, may be NULL).  Recomputes the clip
- * polygons instead of storing them.  Outputs: dL_dpose n_pair x 2 x 6
- * (M then N), dL_dE n_pair x 2 (M then N; 0 for a rigid geom).          */
+ * and dL/dtaxel (all sensors' maps, may be NULL).  Reads the polygons the
+ * step kept (adjoint mode, or sensors attached) and otherwise recomputes
+ * them.  Outputs: dL_dpose n_pair x 2 x 6 (M then N), dL_dE n_pair x 2 (M
+ * then N; 0 for a rigid geom).                                            */
 HC_API hc_status hc_adjoint(hc_context* ctx, const double* dL_dwrench, const float* dL_dtaxel,
                             double* dL_dpose, double* dL_dE);
 /* Keep each step's ray-sample hits for a following taxel adjoint (without
@@ -363,6 +364,29 @@ HC_API hc_status hc_adjoint_device(hc_context* ctx, const double* d_dL_dwrench, 
                                    const double** d_grad);
 /* Kernels the last adjoint launched. */
 HC_API hc_status hc_get_adjoint_launch_count(hc_context* ctx, int* n);
+/* Forward step and adjoint as one graph launch with one wait: the
+ * training-style step of a caller that knows dL/dwrench and dL/dtaxel before
+ * the step (a fixed linear loss, identification against target maps).  The
+ * reference has no gradient; this replaces the sequence hc_set_poses,
+ * hc_step, hc_get_wrenches, hc_get_taxels_all, hc_adjoint with identical
+ * results.  Inputs as hc_set_poses and hc_adjoint (host arrays; page-locked
+ * memory makes the copies direct); outputs (each may be NULL): wrench
+ * n_pair x 6, taxels (all flat sensors' maps), dL_dpose n_pair x 2 x 6,
+ * dL_dE n_pair x 2.  Turns adjoint mode on if it is off.  A step whose
+ * work items or kept polygons overflow grows the capacity and runs again
+ * before the call returns.                                                 */
+HC_API hc_status hc_step_adjoint(hc_context* ctx, int n_geom, const double* xpos, const double* xmat,
+                                 const double* vel, const double* dL_dwrench, const float* dL_dtaxel,
+                                 double* wrench, float* taxels, double* dL_dpose, double* dL_dE);
+/* The same on device buffers, asynchronous on the context stream: poses as
+ * last set (hc_set_poses / hc_set_poses_device), upstream gradients as
+ * hc_adjoint_device (either may be NULL), *d_grad as hc_adjoint_device.
+ * Needs adjoint mode on.  The graph is kept while the upstream pointers stay
+ * the same.  An overflowing step is found by the next synchronising call
+ * (hc_get_wrenches, ...), which grows the capacity and re-runs the forward
+ * step alone: call this again for its gradient.                             */
+HC_API hc_status hc_step_adjoint_device(hc_context* ctx, const double* d_dL_dwrench, const float* d_dL_dtaxel,
+                                        const double** d_grad);
 
 /* ---- measurement --------------------------------------------------------*/
 typedef struct {
@@ -371,6 +395,8 @@ typedef struct {
                                the narrow-phase stage, not of ms_narrowphase) */
   int64_t n_items;
   int64_t n_polygons;
+  float ms_adjoint;         /* the adjoint of a fused step (hc_step_adjoint*),
+                               else 0                                        */
 } hc_timings;
 /* Enable CUDA-event timing of the stages of hc_step (the event records
  * become part of the captured graph).                                    */

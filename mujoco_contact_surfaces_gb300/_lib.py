@@ -63,7 +63,8 @@ class hc_candidate(C.Structure):
 class hc_timings(C.Structure):
     _fields_ = [("ms_setup", C.c_float), ("ms_broadphase", C.c_float), ("ms_narrowphase", C.c_float),
                 ("ms_reduce", C.c_float), ("ms_taxels", C.c_float), ("ms_total", C.c_float),
-                ("ms_kept_polygons", C.c_float), ("n_items", C.c_int64), ("n_polygons", C.c_int64)]
+                ("ms_kept_polygons", C.c_float), ("n_items", C.c_int64), ("n_polygons", C.c_int64),
+                ("ms_adjoint", C.c_float)]
 
 
 _P = C.c_void_p
@@ -104,6 +105,8 @@ SIGNATURES = {
     "hc_set_adjoint_mode": (C.c_int, [_P, C.c_int]),
     "hc_adjoint_device": (C.c_int, [_P, _P, _P, C.POINTER(_P)]),
     "hc_get_adjoint_launch_count": (C.c_int, [_P, _ip]),
+    "hc_step_adjoint": (C.c_int, [_P, C.c_int, _dp, _dp, _dp, _dp, _fp, _dp, _fp, _dp, _dp]),
+    "hc_step_adjoint_device": (C.c_int, [_P, _P, _P, C.POINTER(_P)]),
     "hc_enable_timing": (C.c_int, [_P, C.c_int]),
     "hc_get_timings": (C.c_int, [_P, C.POINTER(hc_timings)]),
     "hc_get_stream": (C.c_int, [_P, C.POINTER(_P)]),

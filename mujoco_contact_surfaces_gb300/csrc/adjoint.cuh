@@ -84,13 +84,17 @@ __device__ __forceinline__ bool point_reverse(AdjAcc& G, const FrameDev& F, floa
 }
 
 // A polygon vertex whose three constraint rows are linearly dependent
-// (normalised |det| below kDetTol) is not fixed by them and is left out of
-// the contraction.  Soft-soft polygons have such vertices where an edge on
-// one body's surface meets the other's surface: both pressures vanish there,
-// so the section plane p_M = p_N and the two surface planes share a line.
-// In FP32 the determinant of a dependent triple is rounding noise (~1e-7
-// relative), not zero, so the tolerance sits far above that and far below
-// the vertices of well-formed polygons (0.06 and up on the test scenes).
+// (normalised |det| below kDetTol) is not fixed by them.  Soft-soft polygons
+// have such vertices wherever an edge on one body's surface meets the other
+// body's surface: both pressures vanish there, so the section plane
+// p_M = p_N contains the line where the two surface faces meet, and a
+// vertex recorded on those two faces lies on that line.  Its motion is the
+// line's, carried by the two face rows alone (wrench_adjoint_ss); in the
+// soft-rigid and half-space contractions such a triple is accidental and
+// the vertex is left out.  In FP32 the determinant of a dependent triple is
+// rounding noise (~1e-7 relative), not zero, so the tolerance sits far above
+// that and far below the vertices of well-formed polygons (0.008 and up on
+// the soft-soft test scenes).
 constexpr float kDetTol = 1e-4f;
 
 __device__ __forceinline__ void adj_zero(AdjAcc& g) {
@@ -350,7 +354,22 @@ __device__ __noinline__ void wrench_adjoint_ss(AdjAcc& G, SsAdj& ss, const StepA
     const V3<float> a0 = cross(r1, r2), a1 = cross(r2, r0), a2 = cross(r0, r1);
     const float det = dot(r0, a0);
     const float sc = norm(r0) * norm(r1) * norm(r2);
-    if (!(fabsf(det) > kDetTol * sc)) continue;
+    if (!(fabsf(det) > kDetTol * sc)) {
+      // dependent rows (an edge on both bodies' surfaces): the vertex lies on
+      // the line where the two faces meet, which the section contains; the
+      // two face rows alone carry its motion (minimum norm: no slide along
+      // the line, where its position is set by rounding in the clip)
+      const float g11 = dot(r1, r1), g12 = dot(r1, r2), g22 = dot(r2, r2);
+      const float gd = g11 * g22 - g12 * g12;
+      if (!(gd > kDetTol * g11 * g22)) continue;
+      const float q1 = dot(r1, xe), q2 = dot(r2, xe), igd = 1.f / gd;
+      V3<float> B = mk(0.f, 0.f, 0.f);
+      if (l0 >= 4) B = B + r1 * ((g22 * q1 - g12 * q2) * igd);
+      if (l1 >= 4) B = B + r2 * ((g11 * q2 - g12 * q1) * igd);
+      tr = tr + B;
+      rot = rot + cross(X, B);
+      continue;
+    }
     const float id = 1.f / det;
     const float b0 = dot(xe, a0) * id;
     V3<float> B = ss.gb * (-b0 * il);

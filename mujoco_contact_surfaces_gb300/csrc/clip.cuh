@@ -132,6 +132,14 @@ __device__ __forceinline__ int tet_section(const PV<R, ND> tv[4], const S s[4], 
       if (abs_r(s[a]) > abs_r(s[b])) { int t = a; a = b; b = t; }
       const R sa = (R)s[a], sb = (R)s[b];
       out[i] = pv_lerp(tv[a], tv[b], sa / (sa - sb));
+      if (sizeof(S) == 8 && sizeof(R) == 4) {
+        // FP64 section values: the pressure there in FP64 too.  The tet's
+        // vertex pressures are of the order of E while a contact near first
+        // touch sees pressures thousands of times smaller; interpolated in
+        // FP32 those would keep only a few digits.
+        const double ta = (double)s[a] / ((double)s[a] - (double)s[b]);
+        out[i].p = (R)((double)tv[a].p + ta * ((double)tv[b].p - (double)tv[a].p));
+      }
       out[i].lab = c | (d << 4);
     }
   }
@@ -139,29 +147,62 @@ __device__ __forceinline__ int tet_section(const PV<R, ND> tv[4], const S s[4], 
 }
 
 // Sutherland-Hodgman clip of a convex polygon by d_j >= 0 (carried
-// distances).  tol: FP32 margin of the plane distances.
+// distances), in place.  A convex polygon crosses a plane at most twice, so
+// the output never runs more than one vertex ahead of the input: the write
+// index m stays at most i + 1 while vertex i is processed, and at m = i + 1
+// vertex i is outside (writes only the crossing, at i + 1).  Each next
+// vertex is read before the writes of its turn, and the first vertex is kept
+// aside for the closing edge, so no vertex is overwritten before it is read.
+// The arithmetic is that of a clip into a second array.  Rounding can give
+// a sign pattern with more than two changes (every vertex within noise of
+// the plane); that polygon is clipped through a copy.  n >= 1.  tol: FP32
+// margin of the plane distances.
 template <class R, int ND>
-__device__ __forceinline__ int clip_dist(const PV<R, ND>* in, int n, int j, R tol, Decide& dc, PV<R, ND>* out) {
+__device__ __forceinline__ int clip_step(const PV<R, ND>& a, const PV<R, ND>& b, int j, PV<R, ND>* out, int m) {
+  const R di = a.d[j], dk = b.d[j];
+  const bool ii = di >= (R)0, ik = dk >= (R)0;
+  if (ii && m < kMaxPolyV) out[m++] = a;
+  if (ii != ik && m < kMaxPolyV) {
+    out[m] = abs_r(di) <= abs_r(dk) ? pv_lerp(a, b, di / (di - dk)) : pv_lerp(b, a, dk / (dk - di));
+    out[m].lab = shared_label(a.lab, b.lab) | ((4 + j) << 4);
+    ++m;
+  }
+  return m;
+}
+
+// The same clip through a copy of the input: for sign patterns with more
+// than two changes around the polygon (rounding, every vertex within noise
+// of the plane), where clipping in place could overwrite an unread vertex.
+template <class R, int ND>
+__device__ __noinline__ int clip_dist_copy(PV<R, ND>* p, int n, int j) {
+  PV<R, ND> in[kMaxPolyV];
+  for (int i = 0; i < n; ++i) in[i] = p[i];
+  int m = 0;
+  for (int i = 0; i < n; ++i) m = clip_step(in[i], in[i + 1 == n ? 0 : i + 1], j, p, m);
+  return m;
+}
+
+template <class R, int ND>
+__device__ __forceinline__ int clip_dist(PV<R, ND>* p, int n, int j, R tol, Decide& dc) {
   bool all_in = true;
+  int changes = 0;
+  bool prev = p[n - 1].d[j] >= (R)0;
   for (int i = 0; i < n; ++i) {
-    check(dc, in[i].d[j], tol);
-    all_in &= in[i].d[j] >= (R)0;
+    check(dc, p[i].d[j], tol);
+    const bool in = p[i].d[j] >= (R)0;
+    all_in &= in;
+    changes += in != prev;
+    prev = in;
   }
-  if (all_in) {
-    for (int i = 0; i < n; ++i) out[i] = in[i];
-    return n;
-  }
+  if (all_in) return n;
+  if (changes > 2) return clip_dist_copy(p, n, j);
+  const PV<R, ND> first = p[0];
+  PV<R, ND> cur = first;
   int m = 0;
   for (int i = 0; i < n; ++i) {
-    const int k = i + 1 == n ? 0 : i + 1;
-    const R di = in[i].d[j], dk = in[k].d[j];
-    const bool ii = di >= (R)0, ik = dk >= (R)0;
-    if (ii && m < kMaxPolyV) out[m++] = in[i];
-    if (ii != ik && m < kMaxPolyV) {
-      out[m] = abs_r(di) <= abs_r(dk) ? pv_lerp(in[i], in[k], di / (di - dk)) : pv_lerp(in[k], in[i], dk / (dk - di));
-      out[m].lab = shared_label(in[i].lab, in[k].lab) | ((4 + j) << 4);
-      ++m;
-    }
+    const PV<R, ND> nxt = i + 1 < n ? p[i + 1] : first;
+    m = clip_step(cur, nxt, j, p, m);
+    cur = nxt;
   }
   return m;
 }

@@ -209,7 +209,14 @@ struct hc_context {
   bool graph_valid = false;
   bool stepped = false;
   bool timing = false;
-  cudaEvent_t ev[7] = {};   // stage boundaries; ev[6]: narrow kernels | kept polygons
+  cudaEvent_t ev[8] = {};   // stage boundaries; ev[6]: narrow kernels | kept polygons;
+                            // ev[7]: end of the adjoint (fused step)
+  // forward step and adjoint captured as one graph (hc_step_adjoint*)
+  cudaGraph_t fused_graph = nullptr;
+  cudaGraphExec_t fused_exec = nullptr;
+  bool fused_valid = false;
+  const void* fused_key[5] = {};   // upstream and adjoint buffers it was captured with
+  bool last_fused = false;         // the last step ran as the fused graph
   hc_timings last_timings = {};
   int launches_per_step = 0;
   int narrow_block = 128, narrow_ctas_per_sm = 8, narrow_chunk = 4;
@@ -264,6 +271,11 @@ void invalidate_graph(hc_context* c) {
   c->graph_exec = nullptr;
   c->graph = nullptr;
   c->graph_valid = false;
+  if (c->fused_exec) cudaGraphExecDestroy(c->fused_exec);
+  if (c->fused_graph) cudaGraphDestroy(c->fused_graph);
+  c->fused_exec = nullptr;
+  c->fused_graph = nullptr;
+  c->fused_valid = false;
 }
 
 hc_status build_pools(hc_context* c) {
@@ -667,6 +679,7 @@ hc_status run_step(hc_context* c, int want_polys, int want_pair) {
   hc::StepArgs a = make_args(c, want_polys, want_pair);
   c->recs_step = a.recs != nullptr;
   c->step_checked = false;
+  c->last_fused = false;
   HC_CUDA(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(int), c->stream));
   // samples kept by an earlier step and not consumed by an adjoint
   if (c->samples_dirty && c->samples.n) {
@@ -1653,6 +1666,11 @@ hc_status hc_get_timings(hc_context* c, hc_timings* out) {
   out->ms_reduce = t[3];
   out->ms_taxels = t[4];
   cudaEventElapsedTime(&out->ms_total, c->ev[0], c->ev[5]);
+  out->ms_adjoint = 0.f;
+  if (c->last_fused) {
+    HC_CUDA(cudaEventSynchronize(c->ev[7]));
+    cudaEventElapsedTime(&out->ms_adjoint, c->ev[5], c->ev[7]);
+  }
   int cnt[8];
   HC_CUDA(cudaMemcpy(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost));
   out->n_items = cnt[kCntTotal];
@@ -1804,6 +1822,149 @@ static hc_status ensure_kept_samples(hc_context* c) {
   invalidate_graph(c);
   if (st) return st;
   return finish_step(c);
+}
+
+// The forward step and its adjoint as one graph on the context stream: the
+// counters and kept samples cleared, the step's kernels, then the adjoint's
+// on the upstream gradients at d_dw / d_dt (device; either may be null).
+// Adjoint mode must be on.  The adjoint kernels read the step's status on the
+// device (records that overflowed are not read; work items never exceed the
+// capacity), so nothing waits between the two; the caller checks the status.
+static hc_status run_fused(hc_context* c, const double* d_dw, const float* d_dt) {
+  const int n_pair = (int)c->pairs_h.size();
+  if (n_pair == 0 && c->sensors.empty()) {
+    c->stepped = true;
+    return HC_OK;
+  }
+  HC_CUDA(c->adj_pair.reserve(8 * (size_t)std::max(1, n_pair)));
+  HC_CUDA(c->adj_out.reserve(14 * (size_t)std::max(1, n_pair)));
+  HC_CUDA(c->adj_item.reserve(16 * (size_t)std::max(1, c->item_cap)));
+  hc::StepArgs a = make_args(c, 0, -1);
+  hc::StepArgs b = a;
+  b.adj_wrench = d_dw;
+  b.adj_taxel = d_dt && c->n_cells > 0 ? d_dt : nullptr;
+  b.adj_pair = c->adj_pair.p;
+  b.adj_item = c->adj_item.p;
+  b.adj_out = c->adj_out.p;
+  if (a.recs) {
+    b.n_item_blocks = std::max(1, (c->item_cap + hc::kBpBlock - 1) / hc::kBpBlock);
+    b.use_recs = 1;
+    b.rec_grad = c->rec_grad.p;
+  }
+  c->recs_step = a.recs != nullptr;
+  c->step_checked = false;
+  const void* key[5] = {d_dw, b.adj_taxel, c->adj_pair.p, c->adj_item.p, c->adj_out.p};
+  if (c->fused_valid && memcmp(key, c->fused_key, sizeof(key)) != 0) invalidate_graph(c);
+  if (!c->fused_valid) {
+    invalidate_graph(c);
+    cudaEvent_t* ev = c->timing ? c->ev : nullptr;
+    HC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(int), c->stream);
+    if (a.keep_samples && c->samples.n)
+      cudaMemsetAsync(c->samples.p, 0xFF, c->samples.n * sizeof(unsigned long long), c->stream);
+    c->launches_per_step = hc::launch_step(a, c->stream, ev);
+    c->adj_launches = hc::launch_adjoint(b, c->stream);
+    if (ev) cudaEventRecordWithFlags(ev[7], c->stream, cudaEventRecordExternal);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &c->fused_graph);
+    if (e != cudaSuccess) return fail(HC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    HC_CUDA(cudaGraphInstantiate(&c->fused_exec, c->fused_graph, 0));
+    memcpy(c->fused_key, key, sizeof(key));
+    c->fused_valid = true;
+  }
+  HC_CUDA(cudaGraphLaunch(c->fused_exec, c->stream));
+  c->stepped = true;
+  c->last_fused = true;
+  // the step kept its samples (cleared in the graph itself; a later hc_step
+  // clears them again); recomputed polygons took theirs
+  c->samples_dirty = a.keep_samples && c->n_cells > 0;
+  c->samples_used = b.adj_taxel && (!c->recs_step || c->type_units[2][1] > c->type_units[2][0]);
+  return HC_OK;
+}
+
+// Preconditions of a fused step; turns adjoint mode on when `enable` is set.
+static hc_status fused_ready(hc_context* c, bool enable) {
+  if (!c->adjoint_mode) {
+    if (!enable) return fail(HC_ERR_NOT_READY, "the fused step needs hc_set_adjoint_mode(ctx, 1)");
+    if (hc_status st = hc_set_adjoint_mode(c, 1)) return st;
+  }
+  if (c->pools_dirty || c->sensors_dirty) {
+    std::vector<int> g1 = c->g1_h, g2 = c->g2_h;
+    if (hc_status st = hc_set_pairs(c, (int)g1.size(), g1.data(), g2.data(), nullptr, nullptr)) return st;
+  }
+  if (!c->poses_set && !c->pairs_h.empty()) return fail(HC_ERR_NOT_READY, "poses not set");
+  if ((size_t)c->n_pose * 3 > c->xpos.n || c->n_pose <= c->max_geom_id)
+    return fail(HC_ERR_NOT_READY, "poses do not cover every registered geom");
+  return HC_OK;
+}
+
+hc_status hc_step_adjoint(hc_context* c, int n_geom, const double* xpos, const double* xmat, const double* vel,
+                          const double* dL_dwrench, const float* dL_dtaxel, double* wrench, float* taxels,
+                          double* dL_dpose, double* dL_dE) {
+  if (hc_status st = need(c)) return st;
+  HC_CUDA(cudaSetDevice(c->device));
+  if (hc_status st = hc_set_poses(c, n_geom, xpos, xmat, vel)) return st;
+  if (hc_status st = fused_ready(c, true)) return st;
+  const int n_pair = (int)c->pairs_h.size();
+  const double* d_dw = nullptr;
+  const float* d_dt = nullptr;
+  if (dL_dwrench && n_pair) {
+    HC_CUDA(c->adj_wrench.reserve(6 * (size_t)n_pair));
+    HC_CUDA(cudaMemcpyAsync(c->adj_wrench.p, dL_dwrench, 6 * (size_t)n_pair * sizeof(double), cudaMemcpyHostToDevice,
+                            c->stream));
+    d_dw = c->adj_wrench.p;
+  }
+  if (dL_dtaxel && c->n_cells) {
+    HC_CUDA(c->adj_taxel.reserve(c->n_cells));
+    HC_CUDA(cudaMemcpyAsync(c->adj_taxel.p, dL_dtaxel, (size_t)c->n_cells * sizeof(float), cudaMemcpyHostToDevice,
+                            c->stream));
+    d_dt = c->adj_taxel.p;
+  }
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    if (hc_status st = run_fused(c, d_dw, d_dt)) return st;
+    if (n_pair == 0 && c->sensors.empty()) return HC_OK;
+    // results straight into the caller's arrays, then the status word; one
+    // wait for all of it
+    if (n_pair && wrench)
+      HC_CUDA(cudaMemcpy2DAsync(wrench, 6 * sizeof(double), c->pair_out.p, sizeof(hc::PairOut), 6 * sizeof(double),
+                                n_pair, cudaMemcpyDeviceToHost, c->stream));
+    if (c->n_cells && taxels)
+      HC_CUDA(cudaMemcpyAsync(taxels, c->taxels.p, (size_t)c->n_cells * sizeof(float), cudaMemcpyDeviceToHost,
+                              c->stream));
+    if (n_pair && dL_dpose)
+      HC_CUDA(cudaMemcpy2DAsync(dL_dpose, 12 * sizeof(double), c->adj_out.p, 14 * sizeof(double),
+                                12 * sizeof(double), n_pair, cudaMemcpyDeviceToHost, c->stream));
+    if (n_pair && dL_dE)
+      HC_CUDA(cudaMemcpy2DAsync(dL_dE, 2 * sizeof(double), c->adj_out.p + 12, 14 * sizeof(double),
+                                2 * sizeof(double), n_pair, cudaMemcpyDeviceToHost, c->stream));
+    int cnt[8];
+    HC_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    if (!(cnt[kCntStatus] & 9)) {
+      c->step_checked = true;
+      return HC_OK;
+    }
+    // a capacity overflowed: grow it and run the whole step again
+    if (cnt[kCntStatus] & 8) {
+      const int want = std::max(2 * c->rec_cap, cnt[kCntRec] + cnt[kCntRec] / 4 + 1024);
+      if (hc_status st = ensure_recs(c, want)) return st;
+    }
+    if (cnt[kCntStatus] & 1) {
+      int total = 0;
+      HC_CUDA(cudaMemcpy(&total, c->unit_off.p + c->n_units, sizeof(int), cudaMemcpyDeviceToHost));
+      if (hc_status st = ensure_items(c, std::max(2 * c->item_cap, total + total / 4 + 1024))) return st;
+    }
+  }
+  return fail(HC_ERR_OVERFLOW, "work-item or polygon-record capacity overflow persisted");
+}
+
+hc_status hc_step_adjoint_device(hc_context* c, const double* d_dL_dwrench, const float* d_dL_dtaxel,
+                                 const double** d_grad) {
+  if (hc_status st = need(c)) return st;
+  HC_CUDA(cudaSetDevice(c->device));
+  if (hc_status st = fused_ready(c, false)) return st;
+  if (hc_status st = run_fused(c, d_dL_dwrench, d_dL_dtaxel)) return st;
+  if (d_grad) *d_grad = c->adj_out.p;
+  return HC_OK;
 }
 
 hc_status hc_adjoint(hc_context* c, const double* dL_dwrench, const float* dL_dtaxel, double* dL_dpose,

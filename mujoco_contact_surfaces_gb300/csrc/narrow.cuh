@@ -895,7 +895,7 @@ __device__ __forceinline__ float plane_df(const float* nh, const float* nl, floa
 // area), then carried in FP32 and interpolated with the vertices.
 template <class R, class S>
 __device__ int sr_polygon(const TetIn<R>& t, const S s[4], const TriStage& T, V3<R> n, R M, Decide& dc,
-                          int& anc, PV<R, 3>* out, PV<R, 3>* tmp) {
+                          int& anc, PV<R, 3>* out) {
   if (!(t.gl > (R)0)) return 0;
   const R cg = dot(n, t.g) / t.gl;
   check(dc, cg - (R)kCosAlphaD, (R)kFilt * ((R)1 + M / (R)T.h + t.kappa));
@@ -945,17 +945,12 @@ __device__ int sr_polygon(const TetIn<R>& t, const S s[4], const TriStage& T, V3
   }
   int nv = tet_section(tv, s, dc, out);
   if (nv == 0) return 0;
-  PV<R, 3>* src = out;
-  PV<R, 3>* dst = tmp;
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
     if (!active[j]) continue;
-    nv = clip_dist(src, nv, j, (R)kFiltRel * dmax[j], dc, dst);
-    PV<R, 3>* sw = src; src = dst; dst = sw;
+    nv = clip_dist(out, nv, j, (R)kFiltRel * dmax[j], dc);
     if (nv == 0) return 0;
   }
-  if (src != out)
-    for (int i = 0; i < nv; ++i) out[i] = src[i];
   return nv;
 }
 
@@ -974,8 +969,8 @@ __device__ __noinline__ int sr_fp64(const StepArgs& a, const TriStage& T, int te
   for (int q = 0; q < 4; ++q) s[q] = fma(n64[2], td.X[q].z, fma(n64[1], td.X[q].y, n64[0] * td.X[q].x)) - o64;
   const V3<double> n = mk(n64[0], n64[1], n64[2]);
   Decide dd;
-  PV<double, 3> pd[kMaxPolyV], tmp[kMaxPolyV];
-  const int nv = sr_polygon<double>(td, s, T, n, 0.0, dd, anc, pd, tmp);
+  PV<double, 3> pd[kMaxPolyV];
+  const int nv = sr_polygon<double>(td, s, T, n, 0.0, dd, anc, pd);
   to_f(pd, nv, poly);
   near = dd.near;
   gint = grad_noise_rule(dot(td.g, n), td.gl);
@@ -986,8 +981,7 @@ __device__ __noinline__ int sr_fp64(const StepArgs& a, const TriStage& T, int te
 // local memory where the compiler can keep them in registers).
 __device__ __forceinline__ int sr_poly_f(const TetIn<float>& t, const float* s, const TriStage& T, V3<float> n,
                                       float M, Decide& dc, int& anc, PV<float, 3>* out) {
-  PV<float, 3> tmp[kMaxPolyV];
-  return sr_polygon<float>(t, s, T, n, M, dc, anc, out, tmp);
+  return sr_polygon<float>(t, s, T, n, M, dc, anc, out);
 }
 
 // shared memory of one warp of the soft-rigid kernel
@@ -1318,8 +1312,7 @@ __device__ __forceinline__ void stage_tetb(const StepArgs& a, const PairDev& P, 
 // clipped by tet B's faces.
 template <class R>
 __device__ int ss_polygon(const TetIn<R>& ta, const double s[4], V3<R> gb, R glb, V3<R> nrm, R lm,
-                          const V3<R> pn[4], const R po[4], R Mb, R hb, R kb, Decide& dc, int& anc, PV<R, 4>* out,
-                          PV<R, 4>* tmp) {
+                          const V3<R> pn[4], const R po[4], R Mb, R hb, R kb, Decide& dc, int& anc, PV<R, 4>* out) {
   const R cond = (((R)1 + ta.kappa) * ta.gl + ((R)1 + kb + Mb / hb) * glb) / lm;
   const R tol_c = (R)kFilt * cond;
   const R ca = dot(nrm, ta.g) / ta.gl;
@@ -1342,16 +1335,11 @@ __device__ int ss_polygon(const TetIn<R>& ta, const double s[4], V3<R> gb, R glb
   if (nv == 0) return 0;
   const R D = ta.xmax + Mb;
   const R tol_p = (R)kFilt * (Mb * ((R)1 + D / hb) + D);
-  PV<R, 4>* src = out;
-  PV<R, 4>* dst = tmp;
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    nv = clip_dist(src, nv, j, tol_p + (R)kFiltRel * dmax[j], dc, dst);
-    PV<R, 4>* sw = src; src = dst; dst = sw;
+    nv = clip_dist(out, nv, j, tol_p + (R)kFiltRel * dmax[j], dc);
     if (nv == 0) return 0;
   }
-  if (src != out)
-    for (int i = 0; i < nv; ++i) out[i] = src[i];
   return nv;
 }
 
@@ -1375,8 +1363,8 @@ __device__ __noinline__ int ss_fp64(const StepArgs& a, const FrameDev& F, int ta
     double pod[4];
     tet_planes(tbd.X, pnd, pod);
     Decide dd;
-    PV<double, 4> pd[kMaxPolyV], tmp[kMaxPolyV];
-    nv = ss_polygon<double>(td, s, tbd.g, tbd.gl, nrmd, lmd, pnd, pod, 0.0, 1.0, 0.0, dd, anc, pd, tmp);
+    PV<double, 4> pd[kMaxPolyV];
+    nv = ss_polygon<double>(td, s, tbd.g, tbd.gl, nrmd, lmd, pnd, pod, 0.0, 1.0, 0.0, dd, anc, pd);
     to_f(pd, nv, poly);
     near = dd.near;
     nrm = mk((float)nrmd.x, (float)nrmd.y, (float)nrmd.z);
@@ -1411,10 +1399,9 @@ __device__ __forceinline__ int ss_element_pair(const StepArgs& a, const FrameDev
   const V3<float> pn[4] = {mk(B.pn[0][0], B.pn[0][1], B.pn[0][2]), mk(B.pn[1][0], B.pn[1][1], B.pn[1][2]),
                            mk(B.pn[2][0], B.pn[2][1], B.pn[2][2]), mk(B.pn[3][0], B.pn[3][1], B.pn[3][2])};
   nrm = m * (1.f / lm);
-  PV<float, 4> tmp[kMaxPolyV];
   Decide dc;
   anc = 0;
-  int nv = ss_polygon<float>(t, s, gb, B.gl, nrm, lm, pn, B.po, B.M, B.h, B.kappa, dc, anc, poly, tmp);
+  int nv = ss_polygon<float>(t, s, gb, B.gl, nrm, lm, pn, B.po, B.M, B.h, B.kappa, dc, anc, poly);
   gM = dot(t.g, nrm);
   gN = -dot(gb, nrm);
   flags = 0;

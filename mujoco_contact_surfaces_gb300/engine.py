@@ -268,6 +268,35 @@ class Engine:
         L.check(self.lib.hc_get_adjoint_launch_count(self.ctx, C.byref(n)))
         return n.value
 
+    def step_adjoint(self, xpos, xmat, vel, dL_dwrench=None, dL_dtaxel=None, out=None):
+        """Forward step and adjoint with one wait (hc_step_adjoint): returns
+        (wrenches n_pair x 6, all flat taxel maps, dL/dpose n_pair x 2 x 6,
+        dL/dE n_pair x 2).  ``out``: a 4-tuple of the caller's arrays."""
+        xpos = np.ascontiguousarray(xpos, np.float64)
+        xmat = np.ascontiguousarray(xmat, np.float64)
+        v = np.ascontiguousarray(vel, np.float64) if vel is not None else None
+        dw = np.ascontiguousarray(dL_dwrench, np.float64) if dL_dwrench is not None else None
+        dt = np.ascontiguousarray(dL_dtaxel, np.float32) if dL_dtaxel is not None else None
+        n_cells = sum(cx * cy for cx, cy in self.sensors.values())
+        o = out if out is not None else (None,) * 4
+        w = _out(o[0], (self.n_pair, 6), np.float64)
+        t = _out(o[1], (n_cells,), np.float32)
+        dpose = _out(o[2], (self.n_pair, 2, 6), np.float64)
+        dE = _out(o[3], (self.n_pair, 2), np.float64)
+        L.check(self.lib.hc_step_adjoint(self.ctx, xpos.size // 3, L.dptr(xpos), L.dptr(xmat), L.dptr(v), L.dptr(dw),
+                                         L.fptr(dt), L.dptr(w), L.fptr(t) if n_cells else None, L.dptr(dpose),
+                                         L.dptr(dE)))
+        return w, t, dpose, dE
+
+    def step_adjoint_device(self, d_dL_dwrench: int | None, d_dL_dtaxel: int | None) -> int:
+        """Forward step and adjoint as one graph on device buffers
+        (hc_step_adjoint_device, asynchronous); returns the device pointer of
+        the n_pair x 14 result."""
+        out = C.c_void_p()
+        L.check(self.lib.hc_step_adjoint_device(self.ctx, C.c_void_p(d_dL_dwrench) if d_dL_dwrench else None,
+                                                C.c_void_p(d_dL_dtaxel) if d_dL_dtaxel else None, C.byref(out)))
+        return out.value or 0
+
     def adjoint(self, dL_dwrench=None, dL_dtaxel=None, out=None):
         """(dL/dpose n_pair x 2 x 6, dL/dE n_pair x 2); ``out``: a pair of
         caller's arrays to fill."""

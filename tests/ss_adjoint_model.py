@@ -299,6 +299,22 @@ def polygon_reverse(P, gF, gT, vf, repr_=0, anc=None, det_tol=1e-12, moduli=None
         a0, a1, a2 = np.cross(r1, r2), np.cross(r2, n), np.cross(n, r1)
         det = n @ a0
         if not abs(det) > det_tol * np.linalg.norm(n) * np.linalg.norm(r1) * np.linalg.norm(r2):
+            # dependent rows: the vertex lies on the line r1 = r2 = 0, which
+            # the section contains (both pressures vanish there); the two
+            # face rows alone carry its motion (minimum norm: no slide along
+            # the line)
+            g11, g12, g22 = r1 @ r1, r1 @ r2, r2 @ r2
+            gd = g11 * g22 - g12 * g12
+            if not gd > det_tol * g11 * g22:
+                continue
+            q1, q2 = r1 @ xe, r2 @ xe
+            B = np.zeros(3)
+            if l0 >= 4:
+                B = B + r1 * ((g22 * q1 - g12 * q2) / gd)
+            if l1 >= 4:
+                B = B + r2 * ((g11 * q2 - g12 * q1) / gd)
+            tr = tr + B
+            rot = rot + np.cross(anc + x[v], B)
             continue
         b0 = xe @ a0 / det
         B = gb * (-b0 / lm)

@@ -49,6 +49,9 @@ def _oracle_parity(s, pairs, w, stats, cand):
     ea = np.abs(area[nz] - ref["area"][nz]) / ref["area"][nz]
     assert ea.max(initial=0) <= AREA_RTOL, f"area rel err {ea.max():.3e}"
     ef, et = wrench_errors(w[pairs], ref["wrench"], ref["area"])
+    for k in np.argsort(-ef)[:3]:
+        print(f"pair {pairs[k]}: force rel err {ef[k]:.2e}, torque {et[k]:.2e}, |F| "
+              f"{np.linalg.norm(ref['wrench'][k, :3]):.3e}, area {ref['area'][k]:.3e}, {ref['n_polygons'][k]} polygons")
     assert ef.max() <= WRENCH_RTOL, f"force rel err {ef.max():.3e}"
     assert et.max() <= WRENCH_RTOL, f"torque rel err {et.max():.3e}"
     print(f"{len(pairs)} pairs, {common} polygons in common, {near} near-degenerate element pairs, "
