@@ -913,6 +913,7 @@ __device__ __forceinline__ void rec_rays_fwd(const StepArgs& a, const AdjPoly& R
     sp[0] = make_float4(rp.lx[0], rp.ly[0], rp.p0, rp.px);
     sp[1] = make_float4(rp.py, rp.lz0, rp.zx, rp.zy);
     sp[2] = make_float4(__int_as_float(rp.X0), __int_as_float(rp.X1), __int_as_float(rp.Y0), __int_as_float(rp.Y1));
+    if (a.sens_box && rp.X0 <= rp.X1 && rp.Y0 <= rp.Y1) grow_box(a.sens_box + sid, rp.X0, rp.X1, rp.Y0, rp.Y1);
   }
   unsigned long long* smp = a.samples + S.sample_off;
   const float* sx = a.samp_coord + S.samp_off_x;

@@ -422,6 +422,15 @@ __global__ void taxel_kernel(StepArgs a) {
   const SensorDev S = a.sensors[sid];
   const int cell = gc - a.cell_first[sid];
   const int x = cell / S.cy, y = cell % S.cy;
+  if (a.sens_box) {
+    // a cell whose samples lie outside every box this step's rays touched
+    // holds no hit: its value is 0 and its samples are already clear
+    const int4 b = a.sens_box[sid];
+    if (x * S.sr > b.y || x * S.sr + S.sr - 1 < b.x || y * S.sr > b.w || y * S.sr + S.sr - 1 < b.z) {
+      a.taxels[S.taxel_off + x + S.cy * y] = 0.f;
+      return;
+    }
+  }
   unsigned long long* smp = a.samples + S.sample_off;
   const float* w = a.weights + S.weight_off;
   float avg = 0.f;
@@ -480,6 +489,24 @@ void record_ctas_per_sm(int* fwd, int* adj) {
     *adj = 1;
 }
 
+// Start of a step: every flat sensor's samples inside the box the last step
+// touched go back to "no hit" (the taxel pass clears what it reads unless the
+// samples are kept for the adjoint), and the box is emptied.  A block per
+// sensor, rows of the box across its threads.
+__global__ void clear_boxes_kernel(StepArgs a) {
+  const int sid = blockIdx.x;
+  const SensorDev S = a.sensors[sid];
+  const int4 b = a.sens_box[sid];
+  if (b.x <= b.y && b.z <= b.w) {
+    unsigned long long* smp = a.samples + S.sample_off;
+    const int nY = b.w - b.z + 1, cnt = (b.y - b.x + 1) * nY;
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x)
+      smp[(size_t)(b.x + i / nY) * S.ny + b.z + i % nY] = ~0ull;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) a.sens_box[sid] = make_int4(0x7fffffff, -1, 0x7fffffff, -1);
+}
+
 // Work counters of the adjoint pass reuse the narrow-phase ones.
 __global__ void reset_next_kernel(StepArgs a) {
   if (threadIdx.x < 3) a.item_next[threadIdx.x] = 0;
@@ -513,6 +540,9 @@ int launch_adjoint(const StepArgs& a, cudaStream_t s) {
 int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   int n = 0;
   if (ev) cudaEventRecordWithFlags(ev[0], s, cudaEventRecordExternal);
+  if (a.sens_box && a.n_sensor > 0) {
+    clear_boxes_kernel<<<a.n_sensor, 256, 0, s>>>(a); ++n;
+  }
   if (a.n_pair > 0) {
     frames_kernel<<<(a.n_pair + 127) / 128, 128, 0, s>>>(a); ++n;
   }

@@ -193,6 +193,7 @@ struct hc_context {
   std::vector<SensorHost> sensors;
   DevBuf<hc::SensorDev> sensors_d;
   DevBuf<unsigned long long> samples;
+  DevBuf<int4> sens_box;   // per flat sensor: the sample box the last step touched
   DevBuf<float> taxels, weights, samp_coord;
   DevBuf<int> cell_sensor, cell_first;
   int n_cells = 0;
@@ -215,7 +216,9 @@ struct hc_context {
   cudaGraph_t fused_graph = nullptr;
   cudaGraphExec_t fused_exec = nullptr;
   bool fused_valid = false;
-  const void* fused_key[5] = {};   // upstream and adjoint buffers it was captured with
+  const void* fused_key[6] = {};   // upstream, adjoint and result buffers it was captured with
+  DevBuf<double> out_stage;        // fused step's results back to back: wrenches n x 6,
+                                   // pose gradients n x 12, moduli gradients n x 2
   bool last_fused = false;         // the last step ran as the fused graph
   hc_timings last_timings = {};
   int launches_per_step = 0;
@@ -560,6 +563,12 @@ hc_status build_sensors(hc_context* c) {
   HC_CUDA(c->taxels.reserve(std::max(1, cells)));
   HC_CUDA(c->samples.reserve(std::max<int64_t>(1, smp)));
   if (smp > 0) HC_CUDA(cudaMemsetAsync(c->samples.p, 0xFF, smp * sizeof(unsigned long long), s));
+  {
+    // every sensor's touched box starts empty (X0 > X1)
+    std::vector<int4> empty(std::max<size_t>(1, c->sensors.size()), make_int4(0x7fffffff, -1, 0x7fffffff, -1));
+    HC_CUDA(c->sens_box.reserve(empty.size()));
+    HC_CUDA(cudaMemcpyAsync(c->sens_box.p, empty.data(), empty.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  }
   if (cells > 0) HC_CUDA(cudaMemsetAsync(c->taxels.p, 0, cells * sizeof(float), s));
   c->n_cells = cells;
   c->sensors_dirty = false;
@@ -608,6 +617,7 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
   a.sensors = c->sensors_d.p;
   a.n_sensor = (int)c->sensors.size();
   a.samples = c->samples.p;
+  a.sens_box = c->sens_box.p;
   a.taxels = c->taxels.p;
   a.weights = c->weights.p;
   a.samp_coord = c->samp_coord.p;
@@ -681,12 +691,9 @@ hc_status run_step(hc_context* c, int want_polys, int want_pair) {
   c->step_checked = false;
   c->last_fused = false;
   HC_CUDA(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(int), c->stream));
-  // samples kept by an earlier step and not consumed by an adjoint
-  if (c->samples_dirty && c->samples.n) {
-    HC_CUDA(cudaMemsetAsync(c->samples.p, 0xFF, c->samples.n * sizeof(unsigned long long), c->stream));
-    c->samples_dirty = false;
-  }
-  if (c->adjoint_mode && c->n_cells > 0) c->samples_dirty = true;
+  // samples an earlier step kept lie inside that step's touched boxes: the
+  // step's first kernel clears those boxes (launch_step)
+  c->samples_dirty = c->adjoint_mode && c->n_cells > 0;
   c->samples_used = false;
   // With timing on, event records between the stages are part of the
   // launch sequence (and of the captured graph).
@@ -828,9 +835,10 @@ hc_status hc_generate_mesh(int type, const double size[3], const double cs5[5], 
     std::string err = hc::make_soft_mesh(type, size, E, hint, mesh_vert, nvert, mesh_face, nface, &m);
     if (!err.empty()) {
       bool unsup = type == HC_GEOM_PLANE || type == HC_GEOM_HFIELD || type == HC_GEOM_CAPSULE;
-      return fail(unsup ? HC_ERR_UNSUPPORTED : HC_ERR_INVALID_ARG, err);
+      return fail(unsup ? HC_ERR_UNSUPPORTED : hc::is_degenerate(err) ? HC_ERR_DEGENERATE : HC_ERR_INVALID_ARG, err);
     }
     hc::round_to_float(&m);
+    if (std::string d = hc::degenerate_soft(m); !d.empty()) return fail(HC_ERR_DEGENERATE, d);
     if (out_kind) *out_kind = HC_SOFT;
     if (out_nvert) *out_nvert = (int)(m.v.size() / 3);
     if (out_nelem) *out_nelem = (int)(m.t.size() / 4);
@@ -843,9 +851,10 @@ hc_status hc_generate_mesh(int type, const double size[3], const double cs5[5], 
   std::string err = hc::make_rigid_mesh(type, size, hint, mesh_vert, nvert, mesh_face, nface, &m);
   if (!err.empty()) {
     bool unsup = type == HC_GEOM_HFIELD || type == HC_GEOM_CAPSULE;
-    return fail(unsup ? HC_ERR_UNSUPPORTED : HC_ERR_INVALID_ARG, err);
+    return fail(unsup ? HC_ERR_UNSUPPORTED : hc::is_degenerate(err) ? HC_ERR_DEGENERATE : HC_ERR_INVALID_ARG, err);
   }
   hc::round_to_float(&m);
+  if (std::string d = hc::degenerate_rigid(m, type == HC_GEOM_PLANE); !d.empty()) return fail(HC_ERR_DEGENERATE, d);
   if (out_kind) *out_kind = HC_RIGID;
   if (out_nvert) *out_nvert = (int)(m.v.size() / 3);
   if (out_nelem) *out_nelem = (int)(m.f.size() / 3);
@@ -861,13 +870,16 @@ static hc_status make_geom_mesh(GeomHost* g) {
   int nv = (int)(g->mesh_v.size() / 3), nf = (int)(g->mesh_f.size() / 3);
   if (E > 0) {
     std::string err = hc::make_soft_mesh(g->type, g->size, E, hint, mv, nv, mf, nf, &g->soft);
-    if (!err.empty()) return fail(HC_ERR_INVALID_ARG, err);
+    if (!err.empty()) return fail(hc::is_degenerate(err) ? HC_ERR_DEGENERATE : HC_ERR_INVALID_ARG, err);
     hc::round_to_float(&g->soft);
+    if (std::string d = hc::degenerate_soft(g->soft); !d.empty()) return fail(HC_ERR_DEGENERATE, d);
     g->kind = HC_SOFT;
   } else {
     std::string err = hc::make_rigid_mesh(g->type, g->size, hint, mv, nv, mf, nf, &g->rigid);
-    if (!err.empty()) return fail(HC_ERR_INVALID_ARG, err);
+    if (!err.empty()) return fail(hc::is_degenerate(err) ? HC_ERR_DEGENERATE : HC_ERR_INVALID_ARG, err);
     hc::round_to_float(&g->rigid);
+    if (std::string d = hc::degenerate_rigid(g->rigid, g->type == HC_GEOM_PLANE); !d.empty())
+      return fail(HC_ERR_DEGENERATE, d);
     g->kind = HC_RIGID;
     g->is_plane = g->type == HC_GEOM_PLANE;
   }
@@ -1824,6 +1836,23 @@ static hc_status ensure_kept_samples(hc_context* c) {
   return finish_step(c);
 }
 
+// The fused step's per-pair results back to back (one contiguous read each
+// for the host instead of strided rows): wrench (6), dL/dpose (12), dL/dE (2).
+__global__ void pack_results_kernel(const hc::PairOut* __restrict__ po, const double* __restrict__ adj, int n_pair,
+                                    double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 20 * n_pair) return;
+  if (i < 6 * n_pair) {
+    out[i] = po[i / 6].wrench[i % 6];
+  } else if (i < 18 * n_pair) {
+    const int k = i - 6 * n_pair;
+    out[i] = adj[14 * (k / 12) + k % 12];
+  } else {
+    const int k = i - 18 * n_pair;
+    out[i] = adj[14 * (k / 2) + 12 + k % 2];
+  }
+}
+
 // The forward step and its adjoint as one graph on the context stream: the
 // counters and kept samples cleared, the step's kernels, then the adjoint's
 // on the upstream gradients at d_dw / d_dt (device; either may be null).
@@ -1839,6 +1868,7 @@ static hc_status run_fused(hc_context* c, const double* d_dw, const float* d_dt)
   HC_CUDA(c->adj_pair.reserve(8 * (size_t)std::max(1, n_pair)));
   HC_CUDA(c->adj_out.reserve(14 * (size_t)std::max(1, n_pair)));
   HC_CUDA(c->adj_item.reserve(16 * (size_t)std::max(1, c->item_cap)));
+  HC_CUDA(c->out_stage.reserve(20 * (size_t)std::max(1, n_pair)));
   hc::StepArgs a = make_args(c, 0, -1);
   hc::StepArgs b = a;
   b.adj_wrench = d_dw;
@@ -1853,17 +1883,20 @@ static hc_status run_fused(hc_context* c, const double* d_dw, const float* d_dt)
   }
   c->recs_step = a.recs != nullptr;
   c->step_checked = false;
-  const void* key[5] = {d_dw, b.adj_taxel, c->adj_pair.p, c->adj_item.p, c->adj_out.p};
+  const void* key[6] = {d_dw, b.adj_taxel, c->adj_pair.p, c->adj_item.p, c->adj_out.p, c->out_stage.p};
   if (c->fused_valid && memcmp(key, c->fused_key, sizeof(key)) != 0) invalidate_graph(c);
   if (!c->fused_valid) {
     invalidate_graph(c);
     cudaEvent_t* ev = c->timing ? c->ev : nullptr;
     HC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(int), c->stream);
-    if (a.keep_samples && c->samples.n)
-      cudaMemsetAsync(c->samples.p, 0xFF, c->samples.n * sizeof(unsigned long long), c->stream);
     c->launches_per_step = hc::launch_step(a, c->stream, ev);
     c->adj_launches = hc::launch_adjoint(b, c->stream);
+    if (n_pair > 0) {
+      pack_results_kernel<<<(20 * n_pair + 255) / 256, 256, 0, c->stream>>>(c->pair_out.p, c->adj_out.p, n_pair,
+                                                                             c->out_stage.p);
+      ++c->adj_launches;
+    }
     if (ev) cudaEventRecordWithFlags(ev[7], c->stream, cudaEventRecordExternal);
     cudaError_t e = cudaStreamEndCapture(c->stream, &c->fused_graph);
     if (e != cudaSuccess) return fail(HC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
@@ -1874,8 +1907,8 @@ static hc_status run_fused(hc_context* c, const double* d_dw, const float* d_dt)
   HC_CUDA(cudaGraphLaunch(c->fused_exec, c->stream));
   c->stepped = true;
   c->last_fused = true;
-  // the step kept its samples (cleared in the graph itself; a later hc_step
-  // clears them again); recomputed polygons took theirs
+  // the step kept its samples (the next step's first kernel clears them);
+  // recomputed polygons took theirs
   c->samples_dirty = a.keep_samples && c->n_cells > 0;
   c->samples_used = b.adj_taxel && (!c->recs_step || c->type_units[2][1] > c->type_units[2][0]);
   return HC_OK;
@@ -1922,20 +1955,20 @@ hc_status hc_step_adjoint(hc_context* c, int n_geom, const double* xpos, const d
   for (int attempt = 0; attempt < 4; ++attempt) {
     if (hc_status st = run_fused(c, d_dw, d_dt)) return st;
     if (n_pair == 0 && c->sensors.empty()) return HC_OK;
-    // results straight into the caller's arrays, then the status word; one
-    // wait for all of it
+    // results straight into the caller's arrays (each one contiguous copy
+    // from the packed results), then the status word; one wait for all of it
+    const double* st = c->out_stage.p;
     if (n_pair && wrench)
-      HC_CUDA(cudaMemcpy2DAsync(wrench, 6 * sizeof(double), c->pair_out.p, sizeof(hc::PairOut), 6 * sizeof(double),
-                                n_pair, cudaMemcpyDeviceToHost, c->stream));
+      HC_CUDA(cudaMemcpyAsync(wrench, st, 6 * (size_t)n_pair * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     if (c->n_cells && taxels)
       HC_CUDA(cudaMemcpyAsync(taxels, c->taxels.p, (size_t)c->n_cells * sizeof(float), cudaMemcpyDeviceToHost,
                               c->stream));
     if (n_pair && dL_dpose)
-      HC_CUDA(cudaMemcpy2DAsync(dL_dpose, 12 * sizeof(double), c->adj_out.p, 14 * sizeof(double),
-                                12 * sizeof(double), n_pair, cudaMemcpyDeviceToHost, c->stream));
+      HC_CUDA(cudaMemcpyAsync(dL_dpose, st + 6 * (size_t)n_pair, 12 * (size_t)n_pair * sizeof(double),
+                              cudaMemcpyDeviceToHost, c->stream));
     if (n_pair && dL_dE)
-      HC_CUDA(cudaMemcpy2DAsync(dL_dE, 2 * sizeof(double), c->adj_out.p + 12, 14 * sizeof(double),
-                                2 * sizeof(double), n_pair, cudaMemcpyDeviceToHost, c->stream));
+      HC_CUDA(cudaMemcpyAsync(dL_dE, st + 18 * (size_t)n_pair, 2 * (size_t)n_pair * sizeof(double),
+                              cudaMemcpyDeviceToHost, c->stream));
     int cnt[8];
     HC_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
     HC_CUDA(cudaStreamSynchronize(c->stream));

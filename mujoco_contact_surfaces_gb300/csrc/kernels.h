@@ -48,6 +48,9 @@ struct StepArgs {
   const SensorDev* sensors;
   int n_sensor;
   unsigned long long* samples;
+  int4* sens_box;     // per flat sensor: the sample box (X0, X1, Y0, Y1) this
+                      // step's rays can touch (X0 > X1: none); null: every
+                      // sample may be set (the taxel pass reads them all)
   float* taxels;
   const float* weights;
   const float* samp_coord;

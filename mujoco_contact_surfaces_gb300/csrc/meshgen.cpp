@@ -311,11 +311,12 @@ std::string make_soft_mesh(int type, const double size[3], double E, double hint
       return "";
     }
     case HC_GEOM_MESH: {
-      if (!mesh_v || !mesh_f || nv < 4 || nf < 4) return "mesh geom needs vertices and faces";
+      if (!mesh_v || !mesh_f) return "mesh geom needs vertices and faces";
+      if (nv < 4 || nf < 4) return std::string(kDegenerate) + "a soft mesh needs at least 4 vertices and 4 faces";
       for (int i = 0; i < 3 * nf; ++i)
         if (mesh_f[i] < 0 || mesh_f[i] >= nv) return "mesh face index out of range";
       double c[3];
-      if (!enclosed_centroid(mesh_v, mesh_f, nf, c)) return "mesh encloses zero volume";
+      if (!enclosed_centroid(mesh_v, mesh_f, nf, c)) return std::string(kDegenerate) + "mesh encloses zero volume";
       std::vector<double> sv(mesh_v, mesh_v + 3 * nv);
       std::vector<int> sf(mesh_f, mesh_f + 3 * nf);
       fan_soft(sv, sf, c, E, out);
@@ -352,7 +353,8 @@ std::string make_rigid_mesh(int type, const double size[3], double hint, const d
       rigid_cylinder(size[0], size[1], hint, out);
       return "";
     case HC_GEOM_MESH:
-      if (!mesh_v || !mesh_f || nv < 3 || nf < 1) return "mesh geom needs vertices and faces";
+      if (!mesh_v || !mesh_f) return "mesh geom needs vertices and faces";
+      if (nv < 3 || nf < 1) return std::string(kDegenerate) + "empty rigid mesh";
       for (int i = 0; i < 3 * nf; ++i)
         if (mesh_f[i] < 0 || mesh_f[i] >= nv) return "mesh face index out of range";
       out->v.assign(mesh_v, mesh_v + 3 * nv);
@@ -486,6 +488,49 @@ int sample_surface(const double* v, int nv, const int* f, int nf, int n, uint64_
     for (int c = 0; c < 3; ++c) nrm->push_back(fn[3 * (size_t)cand[(size_t)idx].face + c]);
   }
   return (int)kept.size();
+}
+
+}  // namespace hc
+
+namespace hc {
+
+namespace {
+double extent(const std::vector<double>& v) {
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (size_t i = 0; i < v.size(); ++i) {
+    lo[i % 3] = std::min(lo[i % 3], v[i]);
+    hi[i % 3] = std::max(hi[i % 3], v[i]);
+  }
+  return std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+}
+}  // namespace
+
+std::string degenerate_soft(const SoftMesh& m) {
+  const size_t n = m.t.size() / 4;
+  if (n == 0) return std::string(kDegenerate) + "soft mesh without tetrahedra";
+  const double L = extent(m.v), tol = 1e-12 * L * L * L;
+  for (size_t k = 0; k < n; ++k) {
+    const int* t = &m.t[4 * k];
+    const double vol = tet_volume(&m.v[3 * t[0]], &m.v[3 * t[1]], &m.v[3 * t[2]], &m.v[3 * t[3]]);
+    if (!(std::fabs(vol) > tol)) return std::string(kDegenerate) + "zero-volume tetrahedron " + std::to_string(k);
+  }
+  return "";
+}
+
+std::string degenerate_rigid(const RigidMesh& m, bool plane) {
+  const size_t n = m.f.size() / 3;
+  if (plane) return "";
+  if (n == 0) return std::string(kDegenerate) + "rigid mesh without triangles";
+  const double L = extent(m.v), tol = 1e-12 * L * L;
+  for (size_t k = 0; k < n; ++k) {
+    const double* a = &m.v[3 * m.f[3 * k]];
+    const double* b = &m.v[3 * m.f[3 * k + 1]];
+    const double* c = &m.v[3 * m.f[3 * k + 2]];
+    const double e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+    const double x = e1[1] * e2[2] - e1[2] * e2[1], y = e1[2] * e2[0] - e1[0] * e2[2], z = e1[0] * e2[1] - e1[1] * e2[0];
+    if (!(std::sqrt(x * x + y * y + z * z) > tol)) return std::string(kDegenerate) + "zero-area triangle " + std::to_string(k);
+  }
+  return "";
 }
 
 }  // namespace hc

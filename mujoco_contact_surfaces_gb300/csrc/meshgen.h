@@ -41,6 +41,17 @@ std::string make_rigid_mesh(int type, const double size[3], double hint, const d
 void round_to_float(SoftMesh* m);
 void round_to_float(RigidMesh* m);
 
+// Messages that start with kDegenerate report degenerate input geometry
+// (the API's HC_ERR_DEGENERATE), all others invalid arguments.
+constexpr const char* kDegenerate = "degenerate: ";
+inline bool is_degenerate(const std::string& err) { return err.rfind(kDegenerate, 0) == 0; }
+
+// Degenerate generated meshes, checked after rounding to float: no elements,
+// a tetrahedron of volume at most 1e-12 L^3 or a triangle of area at most
+// 1e-12 L^2 (L: the mesh's largest extent).  "" when none.
+std::string degenerate_soft(const SoftMesh& m);
+std::string degenerate_rigid(const RigidMesh& m, bool plane);
+
 // Signed volume of tet (a, b, c, d): (b-a).((c-a)x(d-a)) / 6.
 double tet_volume(const double* a, const double* b, const double* c, const double* d);
 

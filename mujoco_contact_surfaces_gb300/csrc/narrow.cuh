@@ -273,6 +273,17 @@ __device__ __forceinline__ void sample_adjoint(const StepArgs& a, const SensorDe
   }
 }
 
+// Grow a sensor's touched sample box to hold (X0..X1, Y0..Y1).  The box is
+// read from L2 first (it changes only during the step, and a stale value
+// can only be looser), so most polygons issue no atomic at all.
+__device__ __forceinline__ void grow_box(int4* b, int X0, int X1, int Y0, int Y1) {
+  const int4 c = __ldcg(b);
+  if (X0 < c.x) atomicMin(&b->x, X0);
+  if (X1 > c.y) atomicMax(&b->y, X1);
+  if (Y0 < c.z) atomicMin(&b->z, Y0);
+  if (Y1 > c.w) atomicMax(&b->w, Y1);
+}
+
 template <int ND, bool kSS = false>
 __device__ __noinline__ void raster_keys(const StepArgs& a, int sid, const float* Rl, const float* tl,
                                          const PV<float, ND>* v, int nv, V3<float> anc, V3<float> g_soft,
@@ -285,6 +296,7 @@ __device__ __noinline__ void raster_keys(const StepArgs& a, int sid, const float
   unsigned long long* smp = a.samples + S.sample_off;
   const float* sx = a.samp_coord + S.samp_off_x;
   const float* sy = a.samp_coord + S.samp_off_y;
+  if (!G && a.sens_box && rp.X0 <= rp.X1 && rp.Y0 <= rp.Y1) grow_box(a.sens_box + sid, rp.X0, rp.X1, rp.Y0, rp.Y1);
   for (int X = rp.X0; X <= rp.X1; ++X) {
     const float qx = sx[X];
     for (int Y = rp.Y0; Y <= rp.Y1; ++Y) {

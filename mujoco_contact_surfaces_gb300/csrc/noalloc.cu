@@ -114,6 +114,7 @@ extern "C" HC_API hc_status hc_step_noalloc(hc_context* ctx, int n_geom, const d
   a.unit_off = cv.take<int>((size_t)a.n_units + 1);
   a.block_sum = cv.take<int>(a.n_bp_blocks > 0 ? a.n_bp_blocks : 1);
   a.samples = cv.take<unsigned long long>(v.n_samples > 0 ? v.n_samples : 1);
+  a.sens_box = nullptr;   // the whole sample array is cleared below and read
   if (!words || !a.frames || !a.pair_out || !a.unit_count || !a.unit_off || !a.block_sum || !a.samples) {
     char msg[240];
     snprintf(msg, sizeof(msg),

@@ -28,6 +28,9 @@ int or_generate_mesh(int type, const double size[3], const double cs5[5], const 
     e = hc::make_soft_mesh(type, size, E, hint, mesh_vert, nvert, mesh_face, nface, &m);
     if (e.empty()) {
       hc::round_to_float(&m);
+      e = hc::degenerate_soft(m);
+    }
+    if (e.empty()) {
       *out_kind = 1;
       *out_nvert = (int)(m.v.size() / 3);
       *out_nelem = (int)(m.t.size() / 4);
@@ -41,6 +44,9 @@ int or_generate_mesh(int type, const double size[3], const double cs5[5], const 
     e = hc::make_rigid_mesh(type, size, hint, mesh_vert, nvert, mesh_face, nface, &m);
     if (e.empty()) {
       hc::round_to_float(&m);
+      e = hc::degenerate_rigid(m, type == 0);
+    }
+    if (e.empty()) {
       *out_kind = 0;
       *out_nvert = (int)(m.v.size() / 3);
       *out_nelem = (int)(m.f.size() / 3);

@@ -72,7 +72,7 @@ class _DevArray:
     """A view of n doubles at a device address (for torch.as_tensor)."""
 
     def __init__(self, ptr, n):
-        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, True), "version": 3}
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 3}
 
 
 def test_fused_device_matches(gpu):

@@ -137,3 +137,35 @@ def test_oracle_builds_the_same_meshes():
         assert a[0] == b[0]
         for x, y in zip(a[1:], b[1:]):
             assert (x is None and y is None) or np.array_equal(x, y)
+
+
+def _degenerate(gtype, size, cs5, v=None, f=None):
+    with pytest.raises(L.HCError) as ei:
+        L.generate_mesh(gtype, size, cs5, v, f)
+    assert ei.value.status == L.HC_ERR_DEGENERATE, str(ei.value)
+    return str(ei.value)
+
+
+def test_degenerate_meshes_are_rejected():
+    # Host-side checks of the input geometry (the engine's hc_add_geom runs
+    # the same generator and checks): a flat soft mesh encloses no volume, a
+    # closed mesh with a zero-area face gives a zero-volume tet in its
+    # centroid fan, an empty or zero-area rigid mesh has nothing to clip.
+    soft, rigid = [1e5, 1.0, 0.0, 0.5, 0.5], [0, 1.0, 0.0, 0.5, 0.5]
+    flat_v = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], float) * 0.05
+    flat_f = np.array([[0, 1, 2], [0, 2, 3], [0, 2, 1], [0, 3, 2]], np.int32)
+    assert "zero volume" in _degenerate(L.GEOM_MESH, [0, 0, 0], soft, flat_v, flat_f)
+    # a tetrahedron whose fourth face is split by a vertex on its edge: the
+    # split leaves a zero-area sliver face
+    tv = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [0.5, 0.5, 0]], float) * 0.05
+    tf = np.array([[0, 2, 1], [0, 1, 3], [0, 3, 2], [1, 2, 3], [1, 4, 2]], np.int32)
+    assert "zero-volume" in _degenerate(L.GEOM_MESH, [0, 0, 0], soft, tv, tf)
+    rv = np.array([[0, 0, 0], [1, 0, 0], [2, 0, 0], [0, 1, 0]], float)
+    assert "zero-area" in _degenerate(L.GEOM_MESH, [0, 0, 0], rigid, rv, np.array([[0, 3, 1], [0, 1, 2]], np.int32))
+    assert "empty" in _degenerate(L.GEOM_MESH, [0, 0, 0], rigid, rv, np.zeros((0, 3), np.int32))
+    # the same rules in the oracle's copy of the generator
+    import oracle
+    with pytest.raises(ValueError):
+        oracle.generate_mesh(L.GEOM_MESH, [0, 0, 0], soft, flat_v, flat_f)
+    # well-formed meshes pass
+    assert L.generate_mesh(L.GEOM_MESH, [0, 0, 0], soft, tv[:4], tf[:4])[0] == L.SOFT
