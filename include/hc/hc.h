@@ -155,6 +155,13 @@ typedef struct {
 } hc_geom_info;
 HC_API hc_status hc_get_geom_info(hc_context* ctx, int geom_id, hc_geom_info* out);
 
+/* The geom's elements in the order of its LBVH leaves (built on the device:
+ * the Morton curve of their centroids in the geom's bounding box): order[k]
+ * is the index, in the geom's mesh, of the k-th element (n_elements ints).
+ * A diagnostic of the LBVH build; builds the element pools if needed.  No
+ * counterpart in the reference (its BVHs live inside Drake).               */
+HC_API hc_status hc_get_element_order(hc_context* ctx, int geom_id, int* order);
+
 /* Copy the geom's mesh as stored (vertices rounded to float, body frame).
  * Soft: elems = 4 ints per tet, pressure = one value per vertex.
  * Rigid: elems = 3 ints per triangle, pressure untouched.  Pass NULL

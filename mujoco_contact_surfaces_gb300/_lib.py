@@ -84,6 +84,7 @@ SIGNATURES = {
     "hc_update_geom_size": (C.c_int, [_P, C.c_int, _dp]),
     "hc_get_geom_info": (C.c_int, [_P, C.c_int, C.POINTER(hc_geom_info)]),
     "hc_get_geom_mesh": (C.c_int, [_P, C.c_int, _dp, _dp, _ip]),
+    "hc_get_element_order": (C.c_int, [_P, C.c_int, _ip]),
     "hc_generate_mesh": (C.c_int, [C.c_int, _dp, _dp, _dp, C.c_int, _ip, C.c_int, _ip, _ip, _ip, _dp, _dp, _ip]),
     "hc_set_poses": (C.c_int, [_P, C.c_int, _dp, _dp, _dp]),
     "hc_set_poses_device": (C.c_int, [_P, C.c_int, _P, _P, _P]),

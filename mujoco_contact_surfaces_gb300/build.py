@@ -17,7 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libhc.so")
 
-SOURCES = ["contact.cu", "hc_api.cu", "noalloc.cu", "meshgen.cpp"]
+SOURCES = ["contact.cu", "hc_api.cu", "noalloc.cu", "lbvh.cu", "meshgen.cpp"]
 HEADERS = ["clip.cuh", "geom_math.cuh", "narrow.cuh", "adjoint.cuh", "hc_internal.h", "kernels.h", "meshgen.h",
            "noalloc.h", "taxel_sensor.cuh", "curved_sensor.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -16,7 +16,19 @@
 #include "hc_internal.h"
 #include "kernels.h"
 #include "meshgen.h"
+#include <nvtx3/nvToolsExt.h>
 #include "noalloc.h"
+
+namespace {
+// A named range on the profiler timeline (NVTX) for the span of a host call;
+// without a profiler attached it costs a call and a branch.
+struct HostRange {
+  explicit HostRange(const char* name) { nvtxRangePushA(name); }
+  ~HostRange() { nvtxRangePop(); }
+  HostRange(const HostRange&) = delete;
+  HostRange& operator=(const HostRange&) = delete;
+};
+}  // namespace
 
 namespace {
 
@@ -74,7 +86,6 @@ struct GeomHost {
   std::vector<int> mesh_f;
   // device placement
   int elem_off = 0, n_elem = 0, node_off = 0, leaves = 1;
-  std::vector<int> perm;       // Morton position -> original element
 };
 
 struct TaxelHost {
@@ -101,39 +112,6 @@ struct SensorHost {
   int cx, cy;
   hc::SensorDev dev;
 };
-
-uint32_t expand_bits(uint32_t v) {
-  v = (v * 0x00010001u) & 0xFF0000FFu;
-  v = (v * 0x00000101u) & 0x0F00F00Fu;
-  v = (v * 0x00000011u) & 0xC30C30C3u;
-  v = (v * 0x00000005u) & 0x49249249u;
-  return v;
-}
-
-// Morton order of element centroids inside the mesh's bounding box.
-std::vector<int> morton_order(const std::vector<double>& v, const std::vector<int>& e, int npe) {
-  int ne = (int)(e.size() / npe);
-  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-  for (size_t i = 0; i < v.size(); i += 3)
-    for (int a = 0; a < 3; ++a) lo[a] = std::min(lo[a], v[i + a]), hi[a] = std::max(hi[a], v[i + a]);
-  std::vector<std::pair<uint32_t, int>> key(ne);
-  for (int i = 0; i < ne; ++i) {
-    double c[3] = {0, 0, 0};
-    for (int k = 0; k < npe; ++k)
-      for (int a = 0; a < 3; ++a) c[a] += v[3 * e[npe * i + k] + a] / npe;
-    uint32_t q[3];
-    for (int a = 0; a < 3; ++a) {
-      double ext = hi[a] - lo[a];
-      double f = ext > 0 ? (c[a] - lo[a]) / ext : 0.5;
-      q[a] = (uint32_t)std::min(1023.0, std::max(0.0, f * 1024.0));
-    }
-    key[i] = {(expand_bits(q[0]) << 2) | (expand_bits(q[1]) << 1) | expand_bits(q[2]), i};
-  }
-  std::stable_sort(key.begin(), key.end());
-  std::vector<int> perm(ne);
-  for (int i = 0; i < ne; ++i) perm[i] = key[i].second;
-  return perm;
-}
 
 // Device counter words of a context.
 constexpr int kCntTotal = 0;   // work items of the step (clamped to capacity)
@@ -286,9 +264,25 @@ hc_status build_pools(hc_context* c) {
   std::vector<GeomHost*> order;
   for (auto& kv : c->geoms) order.push_back(&kv.second);
   std::sort(order.begin(), order.end(), [](GeomHost* a, GeomHost* b) { return a->order < b->order; });
+  // every element in its geom's original order; the device orders each geom
+  // along its Morton curve (launch_lbvh_order)
   std::vector<float4> tets, tris, tri_meta;
   std::vector<hc::Dbl4> tri_plane, tri_edges;
-  std::vector<int> tet_orig, tri_orig;
+  std::vector<hc::LbvhSeg> sseg, rseg;
+  std::vector<int> s_chunk_seg, r_chunk_seg;
+  const int chunk = hc::lbvh_sort_chunk();
+  auto segment = [&](std::vector<hc::LbvhSeg>& segs, std::vector<int>& chunk_seg, const std::vector<double>& v,
+                     int off, int n) {
+    hc::LbvhSeg g{};
+    g.off = off;
+    g.n = n;
+    g.chunk_off = (int)chunk_seg.size();
+    for (int a = 0; a < 3; ++a) g.lo[a] = 1e300, g.hi[a] = -1e300;
+    for (size_t i = 0; i < v.size(); i += 3)
+      for (int a = 0; a < 3; ++a) g.lo[a] = std::min(g.lo[a], v[i + a]), g.hi[a] = std::max(g.hi[a], v[i + a]);
+    for (int k = 0; k < (n + chunk - 1) / chunk; ++k) chunk_seg.push_back((int)segs.size());
+    segs.push_back(g);
+  };
   int node_total = 0;
   std::vector<int> s_eoff, s_ne, s_noff, s_L, r_eoff, r_ne, r_noff, r_L;
   for (GeomHost* g : order) {
@@ -297,33 +291,28 @@ hc_status build_pools(hc_context* c) {
     if (g->kind == HC_SOFT) {
       const auto& m = g->soft;
       int ne = (int)(m.t.size() / 4);
-      g->perm = morton_order(m.v, m.t, 4);
       g->elem_off = (int)(tets.size() / 4);
       g->n_elem = ne;
-      for (int i = 0; i < ne; ++i) {
-        int t = g->perm[i];
+      for (int t = 0; t < ne; ++t) {
         for (int k = 0; k < 4; ++k) {
           int vi = m.t[4 * t + k];
           tets.push_back(make_float4((float)m.v[3 * vi], (float)m.v[3 * vi + 1], (float)m.v[3 * vi + 2], (float)m.p[vi]));
         }
-        tet_orig.push_back(t);
       }
+      segment(sseg, s_chunk_seg, m.v, g->elem_off, ne);
       s_eoff.push_back(g->elem_off); s_ne.push_back(ne);
     } else if (g->kind == HC_RIGID && !g->is_plane) {
       const auto& m = g->rigid;
       int ne = (int)(m.f.size() / 3);
-      g->perm = morton_order(m.v, m.f, 3);
       g->elem_off = (int)(tris.size() / 3);
       g->n_elem = ne;
-      for (int i = 0; i < ne; ++i) {
-        int t = g->perm[i];
+      for (int t = 0; t < ne; ++t) {
         const double* r[3];
         for (int k = 0; k < 3; ++k) {
           int vi = m.f[3 * t + k];
           r[k] = &m.v[3 * vi];
           tris.push_back(make_float4((float)m.v[3 * vi], (float)m.v[3 * vi + 1], (float)m.v[3 * vi + 2], 0.f));
         }
-        tri_orig.push_back(t);
         // FP64 plane of the triangle in its body frame (from the stored
         // float vertices), min altitude, max edge and coordinate magnitude
         double e1[3], e2[3], N[3];
@@ -355,6 +344,7 @@ hc_status build_pools(hc_context* c) {
         }
         tri_meta.push_back(make_float4(ln > 0 && le > 0 ? (float)(ln / le) : 0.f, (float)le, (float)mag, 0.f));
       }
+      segment(rseg, r_chunk_seg, m.v, g->elem_off, ne);
       r_eoff.push_back(g->elem_off); r_ne.push_back(ne);
     } else {
       continue;
@@ -367,13 +357,11 @@ hc_status build_pools(hc_context* c) {
     else { r_noff.push_back(g->node_off); r_L.push_back(g->leaves); }
   }
   cudaStream_t s = c->stream;
-  HC_CUDA(c->tets.upload(tets, s));
-  HC_CUDA(c->tet_props.reserve(std::max<size_t>(2, tets.size() / 2)));
-  hc::launch_tet_props(c->tets.p, c->tet_props.p, (int)(tets.size() / 4), s);
-  HC_CUDA(cudaGetLastError());
-  HC_CUDA(c->tris.upload(tris, s));
-  HC_CUDA(c->tet_orig.upload(tet_orig, s));
-  HC_CUDA(c->tri_orig.upload(tri_orig, s));
+  const size_t n_tet = tets.size() / 4, n_tri = tris.size() / 3;
+  HC_CUDA(c->tets.reserve(std::max<size_t>(4, tets.size())));
+  HC_CUDA(c->tris.reserve(std::max<size_t>(3, tris.size())));
+  HC_CUDA(c->tet_orig.reserve(std::max<size_t>(1, n_tet)));
+  HC_CUDA(c->tri_orig.reserve(std::max<size_t>(1, n_tri)));
   // planes as FP32 head and tail (the device rotates them in double-float)
   auto split = [](const std::vector<hc::Dbl4>& in) {
     std::vector<hc::DfPlane> out(in.size());
@@ -389,9 +377,44 @@ hc_status build_pools(hc_context* c) {
     }
     return out;
   };
-  HC_CUDA(c->tri_plane.upload(split(tri_plane), s));
-  HC_CUDA(c->tri_edges.upload(split(tri_edges), s));
-  HC_CUDA(c->tri_meta.upload(tri_meta, s));
+  HC_CUDA(c->tri_plane.reserve(std::max<size_t>(1, n_tri)));
+  HC_CUDA(c->tri_edges.reserve(std::max<size_t>(3, 3 * n_tri)));
+  HC_CUDA(c->tri_meta.reserve(std::max<size_t>(1, n_tri)));
+  {
+    // the LBVH element order on the device: Morton keys, sort, gather
+    DevBuf<float4> raw, meta_raw;
+    DevBuf<hc::DfPlane> plane_raw, edge_raw;
+    DevBuf<hc::LbvhSeg> segs;
+    DevBuf<int> chunk_seg, perm;
+    DevBuf<unsigned long long> keys;
+    HC_CUDA(keys.reserve(std::max<size_t>(1, std::max(n_tet, n_tri))));
+    HC_CUDA(perm.reserve(std::max<size_t>(1, std::max(n_tet, n_tri))));
+    if (!sseg.empty()) {
+      HC_CUDA(raw.upload(tets, s));
+      HC_CUDA(segs.upload(sseg, s));
+      HC_CUDA(chunk_seg.upload(s_chunk_seg, s));
+      hc::launch_lbvh_order(raw.p, 4, segs.p, (int)sseg.size(), chunk_seg.p, (int)s_chunk_seg.size(), keys.p, perm.p,
+                            c->tets.p, c->tet_orig.p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, s);
+      HC_CUDA(cudaGetLastError());
+    }
+    if (!rseg.empty()) {
+      HC_CUDA(raw.upload(tris, s));
+      HC_CUDA(segs.upload(rseg, s));
+      HC_CUDA(chunk_seg.upload(r_chunk_seg, s));
+      HC_CUDA(plane_raw.upload(split(tri_plane), s));
+      HC_CUDA(edge_raw.upload(split(tri_edges), s));
+      HC_CUDA(meta_raw.upload(tri_meta, s));
+      hc::launch_lbvh_order(raw.p, 3, segs.p, (int)rseg.size(), chunk_seg.p, (int)r_chunk_seg.size(), keys.p, perm.p,
+                            c->tris.p, c->tri_orig.p, plane_raw.p, c->tri_plane.p, edge_raw.p, c->tri_edges.p,
+                            meta_raw.p, c->tri_meta.p, s);
+      HC_CUDA(cudaGetLastError());
+    }
+    // the scratch is freed when the order is done
+    HC_CUDA(cudaStreamSynchronize(s));
+  }
+  HC_CUDA(c->tet_props.reserve(std::max<size_t>(2, tets.size() / 2)));
+  hc::launch_tet_props(c->tets.p, c->tet_props.p, (int)n_tet, s);
+  HC_CUDA(cudaGetLastError());
   // two float4 (lo, hi) per node
   HC_CUDA(c->nodes.reserve(2 * (size_t)std::max(1, node_total)));
   // LBVH node boxes on the device
@@ -723,6 +746,7 @@ hc_status run_step(hc_context* c, int want_polys, int want_pair) {
 // Once a step has checked clean, later calls return at once.
 hc_status finish_step(hc_context* c) {
   if (c->step_checked) return HC_OK;
+  HostRange range_("wait for the step");
   for (int attempt = 0; attempt < 4; ++attempt) {
     int cnt[8];
     HC_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
@@ -888,6 +912,7 @@ static hc_status make_geom_mesh(GeomHost* g) {
 
 hc_status hc_add_geom(hc_context* c, int geom_id, int type, const double size[3], const double cs5[5],
                       const double* mesh_vert, int nvert, const int* mesh_face, int nface, int* out_kind) {
+  HostRange range_("hc_add_geom");
   if (hc_status st = need(c)) return st;
   if (out_kind) *out_kind = -1;
   if (geom_id < 0) return fail(HC_ERR_INVALID_ARG, "negative geom id");
@@ -919,6 +944,7 @@ hc_status hc_add_geom(hc_context* c, int geom_id, int type, const double size[3]
 }
 
 hc_status hc_update_geom_size(hc_context* c, int geom_id, const double size[3]) {
+  HostRange range_("hc_update_geom_size");
   if (hc_status st = need(c)) return st;
   auto it = c->geoms.find(geom_id);
   if (it == c->geoms.end()) return fail(HC_ERR_INVALID_ARG, "unknown geom id");
@@ -953,6 +979,21 @@ hc_status hc_get_geom_info(hc_context* c, int geom_id, hc_geom_info* out) {
   out->n_vertices = g.kind == HC_SOFT ? (int)(g.soft.v.size() / 3) : (int)(g.rigid.v.size() / 3);
   out->E = g.cs5[0]; out->dissipation = g.cs5[1]; out->resolution_hint = g.cs5[2];
   out->mu_static = g.cs5[3]; out->mu_dynamic = g.cs5[4];
+  return HC_OK;
+}
+
+hc_status hc_get_element_order(hc_context* c, int geom_id, int* order) {
+  if (hc_status st = need(c)) return st;
+  auto it = c->geoms.find(geom_id);
+  if (it == c->geoms.end()) return fail(HC_ERR_INVALID_ARG, "unknown geom id");
+  if (!order) return fail(HC_ERR_INVALID_ARG, "null output");
+  HC_CUDA(cudaSetDevice(c->device));
+  if (hc_status st = build_pools(c)) return st;
+  const GeomHost& g = it->second;
+  if (g.n_elem == 0) return HC_OK;
+  const int* src = g.kind == HC_SOFT ? c->tet_orig.p : c->tri_orig.p;
+  HC_CUDA(cudaStreamSynchronize(c->stream));
+  HC_CUDA(cudaMemcpy(order, src + g.elem_off, (size_t)g.n_elem * sizeof(int), cudaMemcpyDeviceToHost));
   return HC_OK;
 }
 
@@ -1019,6 +1060,7 @@ hc_status hc_set_poses_device(hc_context* c, int n_geom, const double* d_xpos, c
 
 hc_status hc_set_pairs(hc_context* c, int n_pair, const int* g1, const int* g2, int* per_pair_status,
                        int* per_pair_query) {
+  HostRange range_("hc_set_pairs");
   if (hc_status st = need(c)) return st;
   if (n_pair < 0 || (n_pair > 0 && (!g1 || !g2))) return fail(HC_ERR_INVALID_ARG, "bad pair arrays");
   HC_CUDA(cudaSetDevice(c->device));
@@ -1237,6 +1279,7 @@ hc_status hc_set_pairs(hc_context* c, int n_pair, const int* g1, const int* g2, 
 }
 
 hc_status hc_step(hc_context* c) {
+  HostRange range_("hc_step");
   if (hc_status st = need(c)) return st;
   if (!c->poses_set && !c->pairs_h.empty()) return fail(HC_ERR_NOT_READY, "poses not set");
   HC_CUDA(cudaSetDevice(c->device));
@@ -1255,6 +1298,7 @@ hc_status hc_collide_pairs(hc_context* c, int n_pair, const int* g1, const int* 
 }
 
 hc_status hc_get_wrenches(hc_context* c, double* wrench) {
+  HostRange range_("hc_get_wrenches");
   if (hc_status st = need(c)) return st;
   if (!c->stepped) return fail(HC_ERR_NOT_READY, "no step has run");
   HC_CUDA(cudaSetDevice(c->device));
@@ -1340,6 +1384,7 @@ hc_status hc_get_candidates(hc_context* c, hc_candidate* out, int64_t capacity, 
 }
 
 hc_status hc_get_surface(hc_context* c, int pair, hc_surface_view* view) {
+  HostRange range_("hc_get_surface");
   if (hc_status st = need(c)) return st;
   if (!view || pair < 0 || pair >= (int)c->pairs_h.size()) return fail(HC_ERR_INVALID_ARG, "bad pair or view");
   if (!c->stepped) return fail(HC_ERR_NOT_READY, "no step has run");
@@ -1393,6 +1438,7 @@ hc_status hc_get_surface(hc_context* c, int pair, hc_surface_view* view) {
 hc_status hc_add_taxel_sensor(hc_context* c, int geom_id, int n_taxels, const double* taxels, int method,
                               double include_margin, double sample_resolution, int sample_method, int visualize,
                               int* out_sensor) {
+  HostRange range_("hc_add_taxel_sensor");
   if (hc_status st = need(c)) return st;
   if (!c->geoms.count(geom_id)) return fail(HC_ERR_INVALID_ARG, "sensor geom has no cs:: properties");
   if (n_taxels <= 0 || n_taxels > (1 << 20) || !taxels) return fail(HC_ERR_INVALID_ARG, "1 to 2^20 taxels are needed");
@@ -1489,6 +1535,7 @@ hc_status hc_sample_surface(int n_vert, const double* vert, int n_face, const in
 hc_status hc_add_curved_sensor(hc_context* c, int geom_id, int n_taxels, const double* taxels,
                                const double* taxel_normals, double include_margin, int n_points,
                                const double* points, const double* point_normals, int* out_sensor) {
+  HostRange range_("hc_add_curved_sensor");
   if (hc_status st = need(c)) return st;
   if (!c->geoms.count(geom_id)) return fail(HC_ERR_INVALID_ARG, "sensor geom has no cs:: properties");
   if (n_taxels <= 0 || n_taxels > (1 << 20) || !taxels) return fail(HC_ERR_INVALID_ARG, "1 to 2^20 taxels are needed");
@@ -1587,6 +1634,7 @@ hc_status hc_get_curved_sensor_values(hc_context* c, int sensor, float* out) {
 
 hc_status hc_add_flat_sensor(hc_context* c, int geom_id, double resolution, int sampling_resolution, int window,
                              double sigma, int* out_sensor, int* out_cx, int* out_cy) {
+  HostRange range_("hc_add_flat_sensor");
   if (hc_status st = need(c)) return st;
   auto it = c->geoms.find(geom_id);
   if (it == c->geoms.end()) return fail(HC_ERR_INVALID_ARG, "sensor geom has no cs:: properties");
@@ -1629,6 +1677,7 @@ hc_status hc_get_taxels(hc_context* c, int sensor, float* out) {
 }
 
 hc_status hc_get_taxels_all(hc_context* c, float* out, int64_t n_floats) {
+  HostRange range_("hc_get_taxels_all");
   if (hc_status st = need(c)) return st;
   if (!out || n_floats < c->n_cells) return fail(HC_ERR_INVALID_ARG, "output too small");
   if (c->sensors_dirty) return fail(HC_ERR_NOT_READY, "sensors not built; run a step first");
@@ -1709,6 +1758,7 @@ hc_status hc_get_launch_count(hc_context* c, int* n) {
 // fastest step wins.  Results do not depend on the shape (per-item sums are
 // deterministic and reduced in a fixed order).
 hc_status hc_autotune(hc_context* c, int* chosen_ctas_per_sm, int* chosen_chunk) {
+  HostRange range_("hc_autotune");
   if (hc_status st = need(c)) return st;
   if (!c->poses_set || c->pairs_h.empty()) return fail(HC_ERR_NOT_READY, "set pairs and poses before autotuning");
   HC_CUDA(cudaSetDevice(c->device));
@@ -1933,6 +1983,7 @@ static hc_status fused_ready(hc_context* c, bool enable) {
 hc_status hc_step_adjoint(hc_context* c, int n_geom, const double* xpos, const double* xmat, const double* vel,
                           const double* dL_dwrench, const float* dL_dtaxel, double* wrench, float* taxels,
                           double* dL_dpose, double* dL_dE) {
+  HostRange range_("hc_step_adjoint");
   if (hc_status st = need(c)) return st;
   HC_CUDA(cudaSetDevice(c->device));
   if (hc_status st = hc_set_poses(c, n_geom, xpos, xmat, vel)) return st;
@@ -1992,6 +2043,7 @@ hc_status hc_step_adjoint(hc_context* c, int n_geom, const double* xpos, const d
 
 hc_status hc_step_adjoint_device(hc_context* c, const double* d_dL_dwrench, const float* d_dL_dtaxel,
                                  const double** d_grad) {
+  HostRange range_("hc_step_adjoint_device");
   if (hc_status st = need(c)) return st;
   HC_CUDA(cudaSetDevice(c->device));
   if (hc_status st = fused_ready(c, false)) return st;
@@ -2002,6 +2054,7 @@ hc_status hc_step_adjoint_device(hc_context* c, const double* d_dL_dwrench, cons
 
 hc_status hc_adjoint(hc_context* c, const double* dL_dwrench, const float* dL_dtaxel, double* dL_dpose,
                      double* dL_dE) {
+  HostRange range_("hc_adjoint");
   if (hc_status st = need(c)) return st;
   if (!c->stepped) return fail(HC_ERR_NOT_READY, "no step has run");
   HC_CUDA(cudaSetDevice(c->device));
@@ -2040,6 +2093,7 @@ hc_status hc_adjoint(hc_context* c, const double* dL_dwrench, const float* dL_dt
 
 hc_status hc_adjoint_device(hc_context* c, const double* d_dL_dwrench, const float* d_dL_dtaxel,
                             const double** d_grad) {
+  HostRange range_("hc_adjoint_device");
   if (hc_status st = need(c)) return st;
   if (d_dL_dtaxel && !c->samples_dirty && c->n_cells > 0)
     return fail(HC_ERR_NOT_READY, "taxel adjoint needs hc_set_adjoint_mode(ctx, 1) before the step");

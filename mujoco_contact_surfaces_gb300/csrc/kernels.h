@@ -128,6 +128,27 @@ struct StepArgs {
 
 constexpr int kBpBlock = 256;
 
+// LBVH build, element order: one geom's elements in the element pools
+// (the same offset in the unsorted input and in the pools).
+struct LbvhSeg {
+  int off;         // first element
+  int n;           // elements
+  int chunk_off;   // first sort chunk of the geom
+  int pad;
+  double lo[3], hi[3];   // bounding box of the geom's vertices
+};
+// Orders each geom's elements (npe float4 each, unsorted in `raw`) along the
+// Morton curve of their centroids and gathers them into `out`; orig gets each
+// pool element's index in its geom.  Rigid triangles also carry their planes,
+// edge planes and metadata (plane_raw / edge_raw / meta_raw; null for tets).
+// chunk_seg: the geom of every sort chunk of lbvh_sort_chunk() keys; keys and
+// perm: scratch of one entry per element.
+void launch_lbvh_order(const float4* raw, int npe, const LbvhSeg* segs, int n_segs, const int* chunk_seg,
+                       int n_chunks, unsigned long long* keys, int* perm, float4* out, int* orig,
+                       const DfPlane* plane_raw, DfPlane* plane, const DfPlane* edge_raw, DfPlane* edge,
+                       const float4* meta_raw, float4* meta, cudaStream_t s);
+int lbvh_sort_chunk();
+
 // LBVH build/refit: node boxes of the implicit trees of `n_geoms` geoms.
 void launch_refit(const float4* elems, int verts_per_elem, float4* nodes, const int* geom_elem_off,
                   const int* geom_n_elem, const int* geom_node_off, const int* geom_leaves,

@@ -79,6 +79,12 @@ class Engine:
         L.check(self.lib.hc_get_geom_mesh(self.ctx, geom_id, L.dptr(v), L.dptr(p), L.iptr(e)))
         return v, p, e
 
+    def element_order(self, geom_id: int) -> np.ndarray:
+        """The geom's elements in LBVH leaf order (hc_get_element_order)."""
+        out = np.zeros(self.geom_info(geom_id).n_elements, np.int32)
+        L.check(self.lib.hc_get_element_order(self.ctx, geom_id, L.iptr(out)))
+        return out
+
     def update_geom_size(self, geom_id: int, size):
         size = np.ascontiguousarray(size, np.float64)
         L.check(self.lib.hc_update_geom_size(self.ctx, geom_id, L.dptr(size)))
