@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(128, 4) adjoint_sr_kernel(StepArgs a) {
       unstage_tet(TS, t);
       const V3<float> n = mk(T.n[0], T.n[1], T.n[2]);
       // forward polygon (the taxel keys must equal the forward's)
-      PV<float, 3> poly[kMaxPolyV];
+      PV<float, 0> poly[kMaxPolyV];
       Decide dc;
       int anc = 0;
       int nv = sr_poly_f(t, s, T, n, fmaxf(T.M, t.xmax), dc, anc, poly);
@@ -491,10 +491,10 @@ __global__ void __launch_bounds__(128, 4) adjoint_sr_kernel(StepArgs a) {
       // taxel adjoint on the forward polygon
       if (a.adj_taxel) {
         if (P.sensor0 >= 0)
-          raster_keys<3>(a, P.sensor0, F.Rl, F.tl, poly, nv, t.X[anc], t.g, n, a.sensors[P.sensor0].geom == P.gs,
+          raster_keys<0>(a, P.sensor0, F.Rl, F.tl, poly, nv, t.X[anc], t.g, n, a.sensors[P.sensor0].geom == P.gs,
                          &G);
         if (P.sensor1 >= 0)
-          raster_keys<3>(a, P.sensor1, F.Rl1, F.tl1, poly, nv, t.X[anc], t.g, n, a.sensors[P.sensor1].geom == P.gs,
+          raster_keys<0>(a, P.sensor1, F.Rl1, F.tl1, poly, nv, t.X[anc], t.g, n, a.sensors[P.sensor1].geom == P.gs,
                          &G);
       }
       if (!a.adj_wrench || !a.apply_forces) continue;
@@ -502,7 +502,7 @@ __global__ void __launch_bounds__(128, 4) adjoint_sr_kernel(StepArgs a) {
       tet_face_normals(t.X, face);
       const V3<float> clipn[3] = {mk(T.en[0][0], T.en[0][1], T.en[0][2]), mk(T.en[1][0], T.en[1][1], T.en[1][2]),
                                   mk(T.en[2][0], T.en[2][1], T.en[2][2])};
-      wrench_adjoint<3>(G, a, P, F, gF, gT, poly, nv, t.X[anc], n, sgn, face, clipn, t.g, gint);
+      wrench_adjoint<0>(G, a, P, F, gF, gT, poly, nv, t.X[anc], n, sgn, face, clipn, t.g, gint);
     }
     __syncwarp();
     adj_reduce_store(a, G, item, lane);

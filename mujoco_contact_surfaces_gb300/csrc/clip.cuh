@@ -49,6 +49,13 @@ struct PV {
   R d[ND];
   int lab;
 };
+// A vertex without carried distances (the FP32 soft-rigid polygon: each
+// clip plane's distance is evaluated from the position when it is needed).
+template <class R>
+struct PV<R, 0> {
+  R x, y, z, p;
+  int lab;
+};
 
 template <class R, int ND>
 __device__ __forceinline__ PV<R, ND> pv_lerp(const PV<R, ND>& a, const PV<R, ND>& b, R t) {
@@ -57,8 +64,10 @@ __device__ __forceinline__ PV<R, ND> pv_lerp(const PV<R, ND>& a, const PV<R, ND>
   o.y = a.y + t * (b.y - a.y);
   o.z = a.z + t * (b.z - a.z);
   o.p = a.p + t * (b.p - a.p);
+  if constexpr (ND > 0) {
 #pragma unroll
-  for (int j = 0; j < ND; ++j) o.d[j] = a.d[j] + t * (b.d[j] - a.d[j]);
+    for (int j = 0; j < ND; ++j) o.d[j] = a.d[j] + t * (b.d[j] - a.d[j]);
+  }
   o.lab = a.lab;
   return o;
 }
@@ -71,6 +80,17 @@ __device__ __forceinline__ int shared_label(int la, int lb) {
 
 template <class R, int ND>
 __device__ __forceinline__ V3<R> pv_pos(const PV<R, ND>& a) { return mk(a.x, a.y, a.z); }
+
+// v[i] for a lane-varying i in 0..3 with static indices only, so that a
+// four-entry array stays in registers (the values are those of v[i]).
+template <class T>
+__device__ __forceinline__ T sel4(const T v[4], int i) {
+  T r = v[0];
+  r = i == 1 ? v[1] : r;
+  r = i == 2 ? v[2] : r;
+  r = i == 3 ? v[3] : r;
+  return r;
+}
 
 // FP32 passes set `unc` when a decision is inside its margin; FP64 passes
 // set `near` when a value is within kNearTol.
@@ -129,16 +149,21 @@ __device__ __forceinline__ int tet_section(const PV<R, ND> tv[4], const S s[4], 
       // the tet edge (a, b) lies on the faces opposite the two other vertices
       const int other = 0xF & ~((1 << a) | (1 << b));
       const int c = __ffs(other) - 1, d = __ffs(other & ~(1 << c)) - 1;
-      if (abs_r(s[a]) > abs_r(s[b])) { int t = a; a = b; b = t; }
-      const R sa = (R)s[a], sb = (R)s[b];
-      out[i] = pv_lerp(tv[a], tv[b], sa / (sa - sb));
+      S s_a = sel4(s, a), s_b = sel4(s, b);
+      if (abs_r(s_a) > abs_r(s_b)) {
+        int t = a; a = b; b = t;
+        S u = s_a; s_a = s_b; s_b = u;
+      }
+      const PV<R, ND> va = sel4(tv, a), vb = sel4(tv, b);
+      const R sa = (R)s_a, sb = (R)s_b;
+      out[i] = pv_lerp(va, vb, sa / (sa - sb));
       if (sizeof(S) == 8 && sizeof(R) == 4) {
         // FP64 section values: the pressure there in FP64 too.  The tet's
         // vertex pressures are of the order of E while a contact near first
         // touch sees pressures thousands of times smaller; interpolated in
         // FP32 those would keep only a few digits.
-        const double ta = (double)s[a] / ((double)s[a] - (double)s[b]);
-        out[i].p = (R)((double)tv[a].p + ta * ((double)tv[b].p - (double)tv[a].p));
+        const double ta = (double)s_a / ((double)s_a - (double)s_b);
+        out[i].p = (R)((double)va.p + ta * ((double)vb.p - (double)va.p));
       }
       out[i].lab = c | (d << 4);
     }
@@ -203,6 +228,67 @@ __device__ __forceinline__ int clip_dist(PV<R, ND>* p, int n, int j, R tol, Deci
     const PV<R, ND> nxt = i + 1 < n ? p[i + 1] : first;
     m = clip_step(cur, nxt, j, p, m);
     cur = nxt;
+  }
+  return m;
+}
+
+// Signed distance of a vertex to the plane e.x + c = 0 (x relative to the
+// polygon's anchor; c: the plane's value at the anchor).
+__device__ __forceinline__ float pos_dist(const PV<float, 0>& v, const float* e, float c) {
+  return fmaf(e[2], v.z, fmaf(e[1], v.y, fmaf(e[0], v.x, c)));
+}
+
+__device__ __forceinline__ int clip_step_pos(const PV<float, 0>& a, const PV<float, 0>& b, float da, float db, int j,
+                                             PV<float, 0>* out, int m) {
+  const bool ii = da >= 0.f, ik = db >= 0.f;
+  if (ii && m < kMaxPolyV) out[m++] = a;
+  if (ii != ik && m < kMaxPolyV) {
+    out[m] = fabsf(da) <= fabsf(db) ? pv_lerp(a, b, da / (da - db)) : pv_lerp(b, a, db / (db - da));
+    out[m].lab = shared_label(a.lab, b.lab) | ((4 + j) << 4);
+    ++m;
+  }
+  return m;
+}
+
+__device__ __noinline__ int clip_pos_copy(PV<float, 0>* p, int n, int j, const float* e, float c) {
+  PV<float, 0> in[kMaxPolyV];
+  for (int i = 0; i < n; ++i) in[i] = p[i];
+  int m = 0;
+  for (int i = 0; i < n; ++i) {
+    const PV<float, 0>& b = in[i + 1 == n ? 0 : i + 1];
+    m = clip_step_pos(in[i], b, pos_dist(in[i], e, c), pos_dist(b, e, c), j, p, m);
+  }
+  return m;
+}
+
+// clip_dist for vertices without carried distances: the distance to clip
+// plane j is e.x + c from each vertex's position, in place as clip_dist.
+__device__ __forceinline__ int clip_pos(PV<float, 0>* p, int n, int j, const float* e, float c, float tol,
+                                        Decide& dc) {
+  bool all_in = true;
+  int changes = 0;
+  bool prev = pos_dist(p[n - 1], e, c) >= 0.f;
+  for (int i = 0; i < n; ++i) {
+    const float d = pos_dist(p[i], e, c);
+    check(dc, d, tol);
+    const bool in = d >= 0.f;
+    all_in &= in;
+    changes += in != prev;
+    prev = in;
+  }
+  if (all_in) return n;
+  if (changes > 2) return clip_pos_copy(p, n, j, e, c);
+  const PV<float, 0> first = p[0];
+  const float d_first = pos_dist(first, e, c);
+  PV<float, 0> cur = first;
+  float d_cur = d_first;
+  int m = 0;
+  for (int i = 0; i < n; ++i) {
+    const PV<float, 0> nxt = i + 1 < n ? p[i + 1] : first;
+    const float d_nxt = i + 1 < n ? pos_dist(nxt, e, c) : d_first;
+    m = clip_step_pos(cur, nxt, d_cur, d_nxt, j, p, m);
+    cur = nxt;
+    d_cur = d_nxt;
   }
   return m;
 }

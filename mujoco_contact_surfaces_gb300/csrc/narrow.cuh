@@ -510,19 +510,24 @@ __device__ __forceinline__ void unstage_tet(const TetStage& S, TetIn<float>& t) 
 template <class S>
 __device__ __forceinline__ int nearest_vertex(const S s[4]) {
   int k = 0;
+  S best = abs_r(s[0]);
 #pragma unroll
   for (int i = 1; i < 4; ++i)
-    if (abs_r(s[i]) < abs_r(s[k])) k = i;
+    if (abs_r(s[i]) < best) {
+      best = abs_r(s[i]);
+      k = i;
+    }
   return k;
 }
 
 template <class R, int ND>
 __device__ __forceinline__ void tet_local(const TetIn<R>& t, int anc, PV<R, ND> tv[4]) {
+  const V3<R> xa = sel4(t.X, anc);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    tv[k].x = t.X[k].x - t.X[anc].x;
-    tv[k].y = t.X[k].y - t.X[anc].y;
-    tv[k].z = t.X[k].z - t.X[anc].z;
+    tv[k].x = t.X[k].x - xa.x;
+    tv[k].y = t.X[k].y - xa.y;
+    tv[k].z = t.X[k].z - xa.z;
     tv[k].p = t.P[k];
   }
 }
@@ -560,13 +565,15 @@ __device__ __forceinline__ bool aabb_overlap(const float* alo, const float* ahi,
          ahi[2] >= blo[2];
 }
 
-template <int ND>
-__device__ __forceinline__ void to_f(const PV<double, ND>* in, int n, PV<float, ND>* out) {
+template <int ND, int MD>
+__device__ __forceinline__ void to_f(const PV<double, ND>* in, int n, PV<float, MD>* out) {
   for (int i = 0; i < n; ++i) {
     out[i].x = (float)in[i].x; out[i].y = (float)in[i].y; out[i].z = (float)in[i].z; out[i].p = (float)in[i].p;
     out[i].lab = in[i].lab;
+    if constexpr (MD > 0) {
 #pragma unroll
-    for (int j = 0; j < ND; ++j) out[i].d[j] = (float)in[i].d[j];
+      for (int j = 0; j < MD; ++j) out[i].d[j] = (float)in[i].d[j];
+    }
   }
 }
 
@@ -966,11 +973,69 @@ __device__ int sr_polygon(const TetIn<R>& t, const S s[4], const TriStage& T, V3
   return nv;
 }
 
+// The FP32 soft-rigid polygon: as sr_polygon, with vertices that carry no
+// clip distances.  An active edge plane's distance is its double-float value
+// at the anchor vertex plus the FP32 plane normal times the vertex's offset
+// from the anchor; its margin covers that product's rounding (relative to
+// the anchored tet's extent) as well as the distances' own, so every
+// decision inside it still goes to the FP64 fallback.
+__device__ __forceinline__ int sr_polygon_f(const TetIn<float>& t, const float s[4], const TriStage& T, V3<float> n,
+                                            float M, Decide& dc, int& anc, PV<float, 0>* out) {
+  if (!(t.gl > 0.f)) return 0;
+  const float cg = dot(n, t.g) / t.gl;
+  check(dc, cg - (float)kCosAlphaD, kFilt * (1.f + M / T.h + t.kappa));
+  if (!dc.unc && !(cg > (float)kCosAlphaD)) return 0;
+  anc = nearest_vertex(s);
+  PV<float, 0> tv[4];
+  tet_local(t, anc, tv);
+  float xr = 0.f;   // the anchored tet's extent
+#pragma unroll
+  for (int k = 0; k < 4; ++k) xr = fmaxf(xr, fmaxf(fabsf(tv[k].x), fmaxf(fabsf(tv[k].y), fabsf(tv[k].z))));
+  bool active[3];
+  float tol[3], c[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const float tj = 4e-6f * (t.xmax + fabsf(T.eo[j]));
+    bool all_in = true, all_out = true;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float d = T.en[j][0] * t.X[k].x + T.en[j][1] * t.X[k].y + T.en[j][2] * t.X[k].z - T.eo[j];
+      all_in &= d > tj;
+      all_out &= d < -tj;
+    }
+    if (all_out) return 0;
+    active[j] = !all_in;
+    tol[j] = 0.f;
+    c[j] = 0.f;
+    if (active[j]) {
+      // double-float at the four vertices: the plane's position matters to
+      // the area; the anchor's value is the plane's offset for the clip
+      float dmax = 0.f;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float d = plane_df(T.en[j], T.enl[j], T.eo[j], T.eol[j], t.X[k].x, t.X[k].y, t.X[k].z);
+        dmax = fmaxf(dmax, fabsf(d));
+        if (k == anc) c[j] = d;
+      }
+      tol[j] = (float)kFiltRel * (dmax + xr);
+    }
+  }
+  int nv = tet_section(tv, s, dc, out);
+  if (nv == 0) return 0;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    if (!active[j]) continue;
+    nv = clip_pos(out, nv, j, T.en[j], c[j], tol[j], dc);
+    if (nv == 0) return 0;
+  }
+  return nv;
+}
+
 // Exact-decision fallback of one soft-rigid element pair in FP64 from the
 // stored inputs (the section values too); returns the vertex count and sets
 // near/gint.
 __device__ __noinline__ int sr_fp64(const StepArgs& a, const TriStage& T, int tet_idx, int& anc,
-                                    PV<float, 3>* poly, bool& near, float& gint) {
+                                    PV<float, 0>* poly, bool& near, float& gint) {
   TetIn<double> td;
   load_tet(a.tets, tet_idx, td);
   tet_prepare(td);
@@ -992,8 +1057,8 @@ __device__ __noinline__ int sr_fp64(const StepArgs& a, const TriStage& T, int te
 // FP32 soft-rigid polygon (inlined: its inputs and outputs stay out of
 // local memory where the compiler can keep them in registers).
 __device__ __forceinline__ int sr_poly_f(const TetIn<float>& t, const float* s, const TriStage& T, V3<float> n,
-                                      float M, Decide& dc, int& anc, PV<float, 3>* out) {
-  return sr_polygon<float>(t, s, T, n, M, dc, anc, out);
+                                      float M, Decide& dc, int& anc, PV<float, 0>* out) {
+  return sr_polygon_f(t, s, T, n, M, dc, anc, out);
 }
 
 // shared memory of one warp of the soft-rigid kernel
@@ -1062,7 +1127,7 @@ __global__ void __launch_bounds__(128, 5) narrow_sr_kernel(StepArgs a) {
       queue_window(mask, W.q, lane, base);
       const int k = base + lane;
       bool have = false;
-      PV<float, 3> poly[kMaxPolyV];
+      PV<float, 0> poly[kMaxPolyV];
       TetIn<float> t;
       V3<float> n = mk(0.f, 0.f, 0.f);
       int nv = 0, anc = 0, jt = 0, orig_a = 0, orig_b = 0, flags = 0;
@@ -1112,17 +1177,17 @@ __global__ void __launch_bounds__(128, 5) narrow_sr_kernel(StepArgs a) {
         const float gM = P.s_is_m ? gint : INFINITY;
         const float gN = P.s_is_m ? INFINITY : gint;
         // with kept polygons the forces are integrated by rec_forward_kernel
-        if constexpr (!kKeep) integrate_forces<3>(a, P, F, ac, poly, nv, t.X[anc], nc, gM, gN);
-        if constexpr (kDiag) record<3>(a, it.x, poly, nv, t.X[anc], nc, orig_a, orig_b, flags);
+        if constexpr (!kKeep) integrate_forces<0>(a, P, F, ac, poly, nv, sel4(t.X, anc), nc, gM, gN);
+        if constexpr (kDiag) record<0>(a, it.x, poly, nv, sel4(t.X, anc), nc, orig_a, orig_b, flags);
       }
       __syncwarp();
       // with kept polygons the rays are cast by rec_forward_kernel
       if constexpr (!kKeep) {
-        if (have) raster_polygon<3>(a, P, F, poly, nv, t.X[anc], nc, t.g);
+        if (have) raster_polygon<0>(a, P, F, poly, nv, sel4(t.X, anc), nc, t.g);
       }
       __syncwarp();
       if constexpr (kKeep)
-        keep_polygon<3>(a, have, item, seq, lane, it.x, 0, poly, nv, t.X[have ? anc : 0], n, t.g, gint, t.X,
+        keep_polygon<0>(a, have, item, seq, lane, it.x, 0, poly, nv, sel4(t.X, have ? anc : 0), n, t.g, gint, t.X,
                         W.tri[jt].en, orig_a, orig_b);
     }
     __syncwarp();
@@ -1264,7 +1329,8 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
 struct TetBStage {
   double g64[3], c64;  // FP64 field of the B tet in A's frame
   float g[3], gl;
-  float pn[4][3], po[4];
+  float pn[4][3], po[4];     // face planes (inward unit normal, offset) in A's frame: FP32 head
+  float pnl[4][3], pol[4];   // and tail (head + tail: the FP64 plane to 2^-48)
   float lo[3], hi[3];
   float M, h, kappa;
   int orig, valid;
@@ -1299,14 +1365,24 @@ __device__ __forceinline__ void stage_tetb(const StepArgs& a, const PairDev& P, 
   }
   M = fmaxf(M, fmaxf(fabsf(F.tf[0]), fmaxf(fabsf(F.tf[1]), fabsf(F.tf[2]))));
   tet_prepare(tb);
-  V3<float> pn[4];
-  float po[4];
-  tet_planes(tb.X, pn, po);
+  // the face planes in FP64 from the FP64 vertices, kept as FP32 head and
+  // tail: a plane offset of the order of the body's size rounded to FP32
+  // would misplace the clip of a first-touch contact by a sizeable share of
+  // its width
+  V3<double> pn[4];
+  double po[4];
+  tet_planes(bd.X, pn, po);
   S.g64[0] = bd.g.x; S.g64[1] = bd.g.y; S.g64[2] = bd.g.z; S.c64 = bd.c;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    S.pn[k][0] = pn[k].x; S.pn[k][1] = pn[k].y; S.pn[k][2] = pn[k].z;
-    S.po[k] = po[k];
+    const double d[4] = {pn[k].x, pn[k].y, pn[k].z, po[k]};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      S.pn[k][c] = (float)d[c];
+      S.pnl[k][c] = (float)(d[c] - (double)S.pn[k][c]);
+    }
+    S.po[k] = (float)d[3];
+    S.pol[k] = (float)(d[3] - (double)S.po[k]);
   }
   S.g[0] = tb.g.x; S.g[1] = tb.g.y; S.g[2] = tb.g.z; S.gl = tb.gl;
   const float pad = 1e-5f * M + 1e-7f;
@@ -1324,7 +1400,8 @@ __device__ __forceinline__ void stage_tetb(const StepArgs& a, const PairDev& P, 
 // clipped by tet B's faces.
 template <class R>
 __device__ int ss_polygon(const TetIn<R>& ta, const double s[4], V3<R> gb, R glb, V3<R> nrm, R lm,
-                          const V3<R> pn[4], const R po[4], R Mb, R hb, R kb, Decide& dc, int& anc, PV<R, 4>* out) {
+                          const V3<R> pn[4], const R po[4], R Mb, R hb, R kb, Decide& dc, int& anc, PV<R, 4>* out,
+                          const TetBStage* B = nullptr) {
   const R cond = (((R)1 + ta.kappa) * ta.gl + ((R)1 + kb + Mb / hb) * glb) / lm;
   const R tol_c = (R)kFilt * cond;
   const R ca = dot(nrm, ta.g) / ta.gl;
@@ -1340,7 +1417,11 @@ __device__ int ss_polygon(const TetIn<R>& ta, const double s[4], V3<R> gb, R glb
   for (int k = 0; k < 4; ++k)
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      tv[k].d[j] = dot(pn[j], ta.X[k]) - po[j];
+      if (sizeof(R) == 4 && B)   // staged planes: double-float on the FP32 pipe
+        tv[k].d[j] = (R)plane_df(B->pn[j], B->pnl[j], B->po[j], B->pol[j], (float)ta.X[k].x, (float)ta.X[k].y,
+                                 (float)ta.X[k].z);
+      else
+        tv[k].d[j] = dot(pn[j], ta.X[k]) - po[j];
       dmax[j] = fmax(dmax[j], abs_r(tv[k].d[j]));
     }
   int nv = tet_section(tv, s, dc, out);
@@ -1413,7 +1494,7 @@ __device__ __forceinline__ int ss_element_pair(const StepArgs& a, const FrameDev
   nrm = m * (1.f / lm);
   Decide dc;
   anc = 0;
-  int nv = ss_polygon<float>(t, s, gb, B.gl, nrm, lm, pn, B.po, B.M, B.h, B.kappa, dc, anc, poly);
+  int nv = ss_polygon<float>(t, s, gb, B.gl, nrm, lm, pn, B.po, B.M, B.h, B.kappa, dc, anc, poly, &B);
   gM = dot(t.g, nrm);
   gN = -dot(gb, nrm);
   flags = 0;
