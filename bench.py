@@ -40,7 +40,7 @@ METRIC = "contact pairs/s fwd+adjoint, batched vs plain GPU path at 1e-5 rel wre
 # DRAM bytes of one narrow_sr_kernel launch (dram__bytes_read.sum +
 # dram__bytes_write.sum) from an ncu capture of this workload at 1024 scenes,
 # scaled by the scenes processed (items and polygons grow in proportion).
-NARROW_SR_DRAM_BYTES_PER_SCENE = 240.1e6 / 1024
+NARROW_SR_DRAM_BYTES_PER_SCENE = (75.16e6 + 44.28e6) / 1024
 
 
 def parse():
@@ -161,7 +161,10 @@ def accuracy(sub, pairs, w, stats, taxels):
     ref = o.collide()
     o.close()
     F, Fo = w[pairs, :3], ref["wrench"][:, :3]
-    T, To = w[pairs, 3:], ref["wrench"][:, 3:]
+    # torques about the contact centroid (a reference-point-free error)
+    arm = ref["centroid"] - ref["xm"]
+    T = w[pairs, 3:] - np.cross(arm, F)
+    To = ref["wrench"][:, 3:] - np.cross(arm, Fo)
     fo = np.linalg.norm(Fo, axis=1)
     area_ref = ref["area"]
     ef = np.linalg.norm(F - Fo, axis=1) / np.maximum(fo, 1e-9)

@@ -39,6 +39,8 @@ class Engine:
         L.check(self.lib.hc_context_create(C.byref(cfg), C.byref(self.ctx)))
         self.n_pair = 0
         self.sensors = {}   # sensor index -> (cx, cy)
+        self.n_cells = 0    # taxels of all flat sensors (kept as sensors are added)
+        self.n_taxel_values = 0   # taxels of all taxel-point sensors
         self.taxel_sensors = {}   # taxel sensor index -> number of taxels
         self.curved_sensors = {}  # curved sensor index -> number of taxels
 
@@ -95,6 +97,7 @@ class Engine:
         L.check(self.lib.hc_add_flat_sensor(self.ctx, geom_id, resolution, sampling_resolution, window, sigma,
                                             C.byref(sid), C.byref(cx), C.byref(cy)))
         self.sensors[sid.value] = (cx.value, cy.value)
+        self.n_cells += cx.value * cy.value
         return sid.value
 
     def add_taxel_sensor(self, geom_id: int, taxels, method: int, include_margin: float, sample_resolution: float,
@@ -105,6 +108,7 @@ class Engine:
                                              float(include_margin), float(sample_resolution), int(sample_method),
                                              int(visualize), C.byref(sid)))
         self.taxel_sensors[sid.value] = t.shape[0]
+        self.n_taxel_values += t.shape[0]
         return sid.value
 
     def set_taxel_sensor_enabled(self, sensor: int, on: bool = True):
@@ -140,7 +144,7 @@ class Engine:
 
     def all_taxel_sensor_values(self, out=None) -> np.ndarray:
         """Every taxel sensor's values, concatenated in sensor order (one copy)."""
-        out = _out(out, (sum(self.taxel_sensors.values()),), np.float32)
+        out = _out(out, (self.n_taxel_values,), np.float32)
         L.check(self.lib.hc_get_all_taxel_sensor_values(self.ctx, L.fptr(out), out.size))
         return out
 
@@ -194,7 +198,7 @@ class Engine:
         return out
 
     def all_taxels(self, out=None) -> np.ndarray:
-        n = sum(cx * cy for cx, cy in self.sensors.values())
+        n = self.n_cells
         out = _out(out, (n,), np.float32)
         L.check(self.lib.hc_get_taxels_all(self.ctx, L.fptr(out), n))
         return out
@@ -283,7 +287,7 @@ class Engine:
         v = np.ascontiguousarray(vel, np.float64) if vel is not None else None
         dw = np.ascontiguousarray(dL_dwrench, np.float64) if dL_dwrench is not None else None
         dt = np.ascontiguousarray(dL_dtaxel, np.float32) if dL_dtaxel is not None else None
-        n_cells = sum(cx * cy for cx, cy in self.sensors.values())
+        n_cells = self.n_cells
         o = out if out is not None else (None,) * 4
         w = _out(o[0], (self.n_pair, 6), np.float64)
         t = _out(o[1], (n_cells,), np.float32)

@@ -982,10 +982,24 @@ int or_collide(or_ctx* c, const double* xpos, const double* xmat, const double* 
     ac.damping = combined_d(GM, GN);
     ac.mu = combined_mu(GM->mu_d, GN->mu_d);
     ac.apply = opt->apply_forces;
+    double sa = 0.0, sc[3] = {0.0, 0.0, 0.0};
     for (int k = 0; k < lists[i].n; ++k) {
-      integrate_polygon(&ac, &lists[i].p[k], opt->representation);
-      if (lists[i].p[k].flags & 1) r->n_near_degenerate++;
+      const poly* pg = &lists[i].p[k];
+      integrate_polygon(&ac, pg, opt->representation);
+      if (pg->flags & 1) r->n_near_degenerate++;
+      double A = 0.0;
+      for (int q = 1; q + 1 < pg->nv; ++q) {
+        double e1[3], e2[3], cr[3];
+        v_sub(pg->x[q], pg->x[0], e1);
+        v_sub(pg->x[q + 1], pg->x[0], e2);
+        v_cross(e1, e2, cr);
+        A += 0.5 * v_dot(cr, pg->n);
+      }
+      A = fabs(A);
+      sa += A;
+      for (int a = 0; a < 3; ++a) sc[a] += A * pg->c[a];
     }
+    for (int a = 0; a < 3; ++a) r->centroid[a] = sa > 0.0 ? sc[a] / sa : 0.0;
     r->n_polygons = lists[i].n;
     r->n_faces = ac.n_faces;
     r->area = ac.area;

@@ -46,6 +46,8 @@ typedef struct {
   double wrench[6];       /* force on M, torque about x_M, world              */
   int n_polygons, n_faces, n_near_degenerate;
   double area, total_fn0;
+  double centroid[3];     /* area-weighted centroid of the surface, world (the
+                             point a reference-free torque error is taken at) */
 } or_pair_result;
 
 typedef struct {

@@ -49,7 +49,7 @@ class or_options(C.Structure):
 class or_pair_result(C.Structure):
     _fields_ = [("query", C.c_int), ("m", C.c_int), ("n", C.c_int), ("wrench", C.c_double * 6),
                 ("n_polygons", C.c_int), ("n_faces", C.c_int), ("n_near_degenerate", C.c_int),
-                ("area", C.c_double), ("total_fn0", C.c_double)]
+                ("area", C.c_double), ("total_fn0", C.c_double), ("centroid", C.c_double * 3)]
 
 
 class or_candidate(C.Structure):
@@ -231,6 +231,8 @@ class Oracle:
             n_near=np.array([out[i].n_near_degenerate for i in range(npair)]),
             area=np.array([out[i].area for i in range(npair)]),
             total_fn0=np.array([out[i].total_fn0 for i in range(npair)]),
+            centroid=np.array([list(out[i].centroid) for i in range(npair)]).reshape(npair, 3),
+            xm=xpos.reshape(-1, 3)[np.array([out[i].m for i in range(npair)], dtype=np.int64)].reshape(npair, 3),
             taxels=taxels,
             taxels64=t64,
         )

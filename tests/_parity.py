@@ -4,7 +4,8 @@ from __future__ import annotations
 import numpy as np
 
 # Tolerances (FP32 GPU vs FP64 oracle).
-WRENCH_RTOL = 1e-5     # force: |dF| <= 1e-5 |F|; torque: |dT| <= 1e-5 (|T| + |F| sqrt(area))
+WRENCH_RTOL = 1e-5     # force: |dF| <= 1e-5 |F|; torque about the contact
+                       # centroid: |dT_c| <= 1e-5 (|T_c| + |F| sqrt(area))
 AREA_RTOL = 1e-5
 TAXEL_RTOL = 1e-5      # relative to the largest taxel of the map
 
@@ -32,8 +33,17 @@ def compare_candidates(gpu: np.ndarray, orc: np.ndarray):
     return bad, near, len(set(g) & set(o))
 
 
-def wrench_errors(wg: np.ndarray, wo: np.ndarray, area: np.ndarray):
+def wrench_errors(wg: np.ndarray, wo: np.ndarray, area: np.ndarray, centroid=None, xm=None):
+    """Relative force and torque errors per pair.  The wrenches hold the
+    torque about M's origin; with the oracle's contact centroid and M's
+    origin given, both torques are moved to the centroid first, so the torque
+    error does not grow with the lever arm from M's origin to the contact
+    (which would only repeat the force error)."""
     Fg, Fo, Tg, To = wg[:, :3], wo[:, :3], wg[:, 3:], wo[:, 3:]
+    if centroid is not None and xm is not None:
+        r = np.asarray(centroid) - np.asarray(xm)
+        Tg = Tg - np.cross(r, Fg)
+        To = To - np.cross(r, Fo)
     fo = np.linalg.norm(Fo, axis=1)
     ef = np.linalg.norm(Fg - Fo, axis=1) / np.maximum(fo, 1e-9)
     et = np.linalg.norm(Tg - To, axis=1) / np.maximum(np.linalg.norm(To, axis=1) + fo * np.sqrt(area), 1e-12)

@@ -48,7 +48,7 @@ def _oracle_parity(s, pairs, w, stats, cand):
     nz = ref["area"] > 0
     ea = np.abs(area[nz] - ref["area"][nz]) / ref["area"][nz]
     assert ea.max(initial=0) <= AREA_RTOL, f"area rel err {ea.max():.3e}"
-    ef, et = wrench_errors(w[pairs], ref["wrench"], ref["area"])
+    ef, et = wrench_errors(w[pairs], ref["wrench"], ref["area"], ref["centroid"], ref["xm"])
     for k in np.argsort(-ef)[:3]:
         print(f"pair {pairs[k]}: force rel err {ef[k]:.2e}, torque {et[k]:.2e}, |F| "
               f"{np.linalg.norm(ref['wrench'][k, :3]):.3e}, area {ref['area'][k]:.3e}, {ref['n_polygons'][k]} polygons")

@@ -40,7 +40,7 @@ def check_pairs(out, ref, min_polys=1):
     area = np.array([s.area for s in out["stats"]])
     nz = ref["area"] > 0
     assert np.all(np.abs(area[nz] - ref["area"][nz]) <= AREA_RTOL * ref["area"][nz])
-    ef, et = wrench_errors(out["wrench"], ref["wrench"], ref["area"])
+    ef, et = wrench_errors(out["wrench"], ref["wrench"], ref["area"], ref["centroid"], ref["xm"])
     assert ef.max() <= WRENCH_RTOL, f"force rel err {ef.max():.3e}"
     assert et.max() <= WRENCH_RTOL, f"torque rel err {et.max():.3e}"
     return near
@@ -132,7 +132,7 @@ def test_items_beyond_one_candidate_window(gpu):
         eng = scenes.build_engine(s)
         eng.set_adjoint_mode(adjoint_mode)
         eng.step()
-        ef, et = wrench_errors(eng.wrenches(), ref["wrench"], ref["area"])
+        ef, et = wrench_errors(eng.wrenches(), ref["wrench"], ref["area"], ref["centroid"], ref["xm"])
         assert ef.max() <= WRENCH_RTOL and et.max() <= WRENCH_RTOL, (adjoint_mode, ef, et)
         # the adjoint reads the kept polygons (adjoint mode) or recomputes
         # them through the same windows; the two agree to float rounding
