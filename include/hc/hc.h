@@ -371,6 +371,14 @@ HC_API hc_status hc_adjoint_device(hc_context* ctx, const double* d_dL_dwrench, 
                                    const double** d_grad);
 /* Kernels the last adjoint launched. */
 HC_API hc_status hc_get_adjoint_launch_count(hc_context* ctx, int* n);
+/* Diagnostic (needs HC_DEBUG_CANDIDATES): polygon vertices the last adjoint
+ * left out of its contraction because their three constraint rows were
+ * linearly dependent (normalised determinant below 1e-4; soft-soft vertices
+ * on the line where both surfaces meet are carried by their two face rows
+ * instead and are not counted), and the smallest normalised determinant it
+ * met (+infinity when none).  Either output may be NULL.  No counterpart in
+ * the reference.                                                          */
+HC_API hc_status hc_get_adjoint_skipped(hc_context* ctx, int* n, float* min_det);
 /* Forward step and adjoint as one graph launch with one wait: the
  * training-style step of a caller that knows dL/dwrench and dL/dtaxel before
  * the step (a fixed linear loss, identification against target maps).  The

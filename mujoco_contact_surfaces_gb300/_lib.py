@@ -106,6 +106,7 @@ SIGNATURES = {
     "hc_set_adjoint_mode": (C.c_int, [_P, C.c_int]),
     "hc_adjoint_device": (C.c_int, [_P, _P, _P, C.POINTER(_P)]),
     "hc_get_adjoint_launch_count": (C.c_int, [_P, _ip]),
+    "hc_get_adjoint_skipped": (C.c_int, [_P, _ip, _fp]),
     "hc_step_adjoint": (C.c_int, [_P, C.c_int, _dp, _dp, _dp, _dp, _fp, _dp, _fp, _dp, _dp]),
     "hc_step_adjoint_device": (C.c_int, [_P, _P, _P, C.POINTER(_P)]),
     "hc_enable_timing": (C.c_int, [_P, C.c_int]),

@@ -97,6 +97,15 @@ __device__ __forceinline__ bool point_reverse(AdjAcc& G, const FrameDev& F, floa
 // the soft-soft test scenes).
 constexpr float kDetTol = 1e-4f;
 
+// Debug statistics of the contraction (StepArgs::adj_skip: [0] vertices left
+// out, [1] the smallest normalised |det| seen, as the bits of a non-negative
+// float, so an integer minimum orders them).
+__device__ __forceinline__ void det_stat(const StepArgs& a, float det, float sc) {
+  if (!a.adj_skip) return;
+  const float r = sc > 0.f ? fabsf(det) / sc : 0.f;
+  atomicMin(a.adj_skip + 1, __float_as_int(r));
+}
+
 __device__ __forceinline__ void adj_zero(AdjAcc& g) {
 #pragma unroll
   for (int i = 0; i < 6; ++i) g.gx[i] = 0.f;
@@ -223,7 +232,11 @@ __device__ __noinline__ void wrench_adjoint(AdjAcc& G, const StepArgs& a, const 
     const V3<float> a0 = cross(r1, r2), a1 = cross(r2, r0), a2 = cross(r0, r1);
     const float det = dot(r0, a0);
     const float sc = norm(r0) * norm(r1) * norm(r2);
-    if (!(fabsf(det) > kDetTol * sc)) continue;
+    det_stat(a, det, sc);
+    if (!(fabsf(det) > kDetTol * sc)) {
+      if (a.adj_skip) atomicAdd(a.adj_skip, 1);
+      continue;
+    }
     const float id = 1.f / det;
     V3<float> B = r0 * (dot(xe, a0) * id);
     if (l0 >= 4) B = B + r1 * (dot(xe, a1) * id);
@@ -361,7 +374,10 @@ __device__ __noinline__ void wrench_adjoint_ss(AdjAcc& G, SsAdj& ss, const StepA
       // the line, where its position is set by rounding in the clip)
       const float g11 = dot(r1, r1), g12 = dot(r1, r2), g22 = dot(r2, r2);
       const float gd = g11 * g22 - g12 * g12;
-      if (!(gd > kDetTol * g11 * g22)) continue;
+      if (!(gd > kDetTol * g11 * g22)) {
+        if (a.adj_skip) atomicAdd(a.adj_skip, 1);
+        continue;
+      }
       const float q1 = dot(r1, xe), q2 = dot(r2, xe), igd = 1.f / gd;
       V3<float> B = mk(0.f, 0.f, 0.f);
       if (l0 >= 4) B = B + r1 * ((g22 * q1 - g12 * q2) * igd);
@@ -1192,6 +1208,7 @@ __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPol
     const V3<float> a0 = cross(r1, r2), a1 = cross(r2, r0), a2 = cross(r0, r1);
     const float det = dot(r0, a0);
     const float sc = norm(r0) * norm(r1) * norm(r2);
+    det_stat(a, det, sc);
     if (fabsf(det) > kDetTol * sc) {
       const float id = 1.f / det;
       V3<float> B = r0 * (dot(xe, a0) * id);
@@ -1199,6 +1216,8 @@ __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPol
       if (l1 >= 4) B = B + r2 * (dot(xe, a2) * id);
       tr = B;
       rot = cross(X, B);
+    } else if (a.adj_skip) {
+      atomicAdd(a.adj_skip, 1);
     }
   }
   if (live && sub == 0) {

@@ -510,6 +510,10 @@ __global__ void clear_boxes_kernel(StepArgs a) {
 // Work counters of the adjoint pass reuse the narrow-phase ones.
 __global__ void reset_next_kernel(StepArgs a) {
   if (threadIdx.x < 3) a.item_next[threadIdx.x] = 0;
+  if (threadIdx.x == 3 && a.adj_skip) {
+    a.adj_skip[0] = 0;
+    a.adj_skip[1] = 0x7f800000;   // +infinity
+  }
 }
 
 int launch_adjoint(const StepArgs& a, cudaStream_t s) {

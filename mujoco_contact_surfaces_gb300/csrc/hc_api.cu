@@ -120,6 +120,8 @@ constexpr int kCntCand = 2;    // candidate records written
 constexpr int kCntPoly = 3;    // polygon records written
 constexpr int kCntNext = 4;    // three work counters, one per query type
 constexpr int kCntRec = 7;     // adjoint records kept (may exceed the capacity)
+constexpr int kCntAdjSkip = 8; // two words: adjoint vertices left out, smallest |det| (debug)
+constexpr int kCntWords = 16;
 
 int next_pow2(int n) {
   int p = 1;
@@ -663,6 +665,7 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
   a.chunk = std::max(1, c->narrow_chunk);
   a.keep_samples = c->adjoint_mode ? 1 : 0;
   a.rec_count = c->counters.p + kCntRec;
+  a.adj_skip = (c->debug & HC_DEBUG_CANDIDATES) ? c->counters.p + kCntAdjSkip : nullptr;
   // polygons are kept as records (rays cast and taxels sampled from them,
   // the adjoint reads them) in adjoint mode and whenever sensors are attached
   if (keeps_polygons(c) && c->rec_cap > 0) {
@@ -822,11 +825,11 @@ hc_status hc_context_create(const hc_config* cfg, hc_context** out) {
     return fail(HC_ERR_CUDA, "stream create failed");
   }
   for (auto& ev : c->ev) cudaEventCreate(&ev);
-  if (c->counters.reserve(8) != cudaSuccess) {
+  if (c->counters.reserve(kCntWords) != cudaSuccess) {
     delete c;
     return fail(HC_ERR_CUDA, "counter alloc failed");
   }
-  cudaMemset(c->counters.p, 0, 8 * sizeof(int));
+  cudaMemset(c->counters.p, 0, kCntWords * sizeof(int));
   *out = c;
   return HC_OK;
 }
@@ -2102,6 +2105,18 @@ hc_status hc_adjoint_device(hc_context* c, const double* d_dL_dwrench, const flo
                                   "step again (hc_adjoint does so itself)");
   if (hc_status st = adjoint_launch(c, d_dL_dwrench, d_dL_dtaxel)) return st;
   if (d_grad) *d_grad = c->adj_out.p;
+  return HC_OK;
+}
+
+hc_status hc_get_adjoint_skipped(hc_context* c, int* n, float* min_det) {
+  if (hc_status st = need(c)) return st;
+  if (!(c->debug & HC_DEBUG_CANDIDATES)) return fail(HC_ERR_NOT_READY, "needs debug recording (hc_set_debug)");
+  HC_CUDA(cudaSetDevice(c->device));
+  HC_CUDA(cudaStreamSynchronize(c->stream));
+  int w[2];
+  HC_CUDA(cudaMemcpy(w, c->counters.p + kCntAdjSkip, sizeof(w), cudaMemcpyDeviceToHost));
+  if (n) *n = w[0];
+  if (min_det) memcpy(min_det, &w[1], sizeof(float));
   return HC_OK;
 }
 

@@ -87,6 +87,8 @@ struct StepArgs {
   int2* rec_key;             // (item, sequence number within the item)
   int rec_cap;
   int* rec_count;
+  int* adj_skip;             // with debug recording: [0] adjoint polygon vertices left out
+                             // of the contraction, [1] the smallest normalised |det| (bits), else null
   int use_recs;              // the adjoint reads the kept polygons (when none overflowed)
   int* item_poly_off;        // per item: first record of the item in pair order (item_cap + 1)
   int* poly_block_sum;       // one per kBpBlock items

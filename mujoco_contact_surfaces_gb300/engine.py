@@ -273,6 +273,13 @@ class Engine:
                                            C.c_void_p(d_dL_dtaxel) if d_dL_dtaxel else None, C.byref(out)))
         return out.value or 0
 
+    def adjoint_skipped(self):
+        """(vertices the last adjoint left out of its contraction, smallest
+        normalised determinant it met); needs debug recording, set_debug(1)."""
+        n, d = C.c_int(), C.c_float()
+        L.check(self.lib.hc_get_adjoint_skipped(self.ctx, C.byref(n), C.byref(d)))
+        return n.value, d.value
+
     def adjoint_launch_count(self) -> int:
         n = C.c_int()
         L.check(self.lib.hc_get_adjoint_launch_count(self.ctx, C.byref(n)))

@@ -363,3 +363,44 @@ def test_soft_soft_gradient_polygon_quadrature(gpu):
     for p in range(len(s.g1)):
         err = np.linalg.norm(dE[p] - ref[p]) / max(np.linalg.norm(ref[p]), 1e-30)
         assert err <= GRAD_RTOL, f"pair {p}: dE rel err {err:.2e}\n{dE[p]}\n{ref[p]}"
+
+
+def _grazing_box_scene(tilt):
+    """A soft box (5 layers of 4 mm) pressed into a rigid plate so that the
+    plate's top plane lies on one of the box mesh's horizontal layers,
+    tilted by `tilt` rad: tet edges in that layer cross the plane at about
+    `tilt` rad."""
+    from mujoco_contact_surfaces_gb300 import _lib as L
+    s = scenes.Scene()
+    b = s.add_geom(L.GEOM_BOX, [0.02, 0.02, 0.01], [1e5, 1.0, 0.004, 0.5, 0.5])
+    p = s.add_geom(L.GEOM_BOX, [0.1, 0.1, 0.01], [0, 1.0, 0, 0.5, 0.5])
+    s.g1.append(b); s.g2.append(p); s.scene_of_pair.append(0)
+    scenes._alloc(s)
+    s.xpos[b] = [0.0013, -0.0021, 0.01 + 0.01 - 0.004]
+    s.xmat[b] = rot_axis([1, 0.3, 0], tilt).reshape(9)
+    s.vel[b] = [0.01, -0.02, 0.01, 0.02, 0.01, -0.03]
+    return s
+
+
+@pytest.mark.parametrize("adjoint_mode", [True, False])
+def test_soft_rigid_contraction_leaves_no_vertex_out(gpu, adjoint_mode):
+    # The dependent-rows guard of the soft-rigid and half-space contractions
+    # (normalised |det| below 1e-4) must not drop vertices of well-formed
+    # contacts: none is left out on the test scenes, a grazing box included
+    # (tet edges crossing the contact plane at 1e-3 rad)
+    cases = {"single_pair": scenes.single_pair(16, velocities=True, min_pen=1e-3),
+             "tactile": scenes.tactile(8, velocities=True, plate_half=(0.0401, 0.04, 0.005)),
+             "halfspace": scenes.halfspace(4, min_frac=0.03),
+             "grazing": _grazing_box_scene(1e-3)}
+    for name, s in cases.items():
+        rng = np.random.default_rng(3)
+        eng = scenes.build_engine(s)
+        eng.set_adjoint_mode(adjoint_mode)
+        eng.set_debug(1)
+        eng.step()
+        assert np.any(eng.wrenches() != 0)
+        eng.adjoint(rng.normal(size=(len(s.g1), 6)), None)
+        n, dmin = eng.adjoint_skipped()
+        eng.close()
+        print(f"{name} (adjoint mode {adjoint_mode}): {n} vertices left out, smallest normalised det {dmin:.3e}")
+        assert n == 0, (name, n, dmin)
