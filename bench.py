@@ -161,14 +161,15 @@ def accuracy(sub, pairs, w, stats, taxels):
     ref = o.collide()
     o.close()
     F, Fo = w[pairs, :3], ref["wrench"][:, :3]
-    # torques about the contact centroid (a reference-point-free error)
-    arm = ref["centroid"] - ref["xm"]
-    T = w[pairs, 3:] - np.cross(arm, F)
-    To = ref["wrench"][:, 3:] - np.cross(arm, Fo)
+    T, To = w[pairs, 3:], ref["wrench"][:, 3:]
     fo = np.linalg.norm(Fo, axis=1)
     area_ref = ref["area"]
+    # torque scale: |T| + |F| (sqrt(area) + lever arm from M's origin to the
+    # oracle's contact centroid)
+    arm = np.linalg.norm(ref["centroid"] - ref["xm"], axis=1)
     ef = np.linalg.norm(F - Fo, axis=1) / np.maximum(fo, 1e-9)
-    et = np.linalg.norm(T - To, axis=1) / np.maximum(np.linalg.norm(To, axis=1) + fo * np.sqrt(area_ref), 1e-12)
+    et = np.linalg.norm(T - To, axis=1) / np.maximum(np.linalg.norm(To, axis=1) + fo * (np.sqrt(area_ref) + arm),
+                                                     1e-12)
     area = np.array([stats[p].area for p in pairs])
     nz = area_ref > 0
     ea = np.abs(area[nz] - area_ref[nz]) / area_ref[nz]

@@ -4,8 +4,9 @@ from __future__ import annotations
 import numpy as np
 
 # Tolerances (FP32 GPU vs FP64 oracle).
-WRENCH_RTOL = 1e-5     # force: |dF| <= 1e-5 |F|; torque about the contact
-                       # centroid: |dT_c| <= 1e-5 (|T_c| + |F| sqrt(area))
+WRENCH_RTOL = 1e-5     # force: |dF| <= 1e-5 |F|; torque (about M's origin, as
+                       # reported): |dT| <= 1e-5 (|T| + |F| (sqrt(area) + arm)),
+                       # arm = distance from M's origin to the contact centroid
 AREA_RTOL = 1e-5
 TAXEL_RTOL = 1e-5      # relative to the largest taxel of the map
 
@@ -34,19 +35,19 @@ def compare_candidates(gpu: np.ndarray, orc: np.ndarray):
 
 
 def wrench_errors(wg: np.ndarray, wo: np.ndarray, area: np.ndarray, centroid=None, xm=None):
-    """Relative force and torque errors per pair.  The wrenches hold the
-    torque about M's origin; with the oracle's contact centroid and M's
-    origin given, both torques are moved to the centroid first, so the torque
-    error does not grow with the lever arm from M's origin to the contact
-    (which would only repeat the force error)."""
+    """Relative force and torque errors per pair.  The torque is the reported
+    one (about M's origin); its scale is |T| + |F| (sqrt(area) + arm), the
+    force times the lever arm from M's origin to the oracle's contact centroid
+    plus the contact's size, so that neither a torque that nearly vanishes
+    about M's origin (a force through it) nor one about a far origin sets a
+    scale the force's own rounding does not have."""
     Fg, Fo, Tg, To = wg[:, :3], wo[:, :3], wg[:, 3:], wo[:, 3:]
-    if centroid is not None and xm is not None:
-        r = np.asarray(centroid) - np.asarray(xm)
-        Tg = Tg - np.cross(r, Fg)
-        To = To - np.cross(r, Fo)
     fo = np.linalg.norm(Fo, axis=1)
+    arm = np.zeros(len(fo)) if centroid is None or xm is None else np.linalg.norm(
+        np.asarray(centroid) - np.asarray(xm), axis=1)
     ef = np.linalg.norm(Fg - Fo, axis=1) / np.maximum(fo, 1e-9)
-    et = np.linalg.norm(Tg - To, axis=1) / np.maximum(np.linalg.norm(To, axis=1) + fo * np.sqrt(area), 1e-12)
+    et = np.linalg.norm(Tg - To, axis=1) / np.maximum(np.linalg.norm(To, axis=1) + fo * (np.sqrt(area) + arm),
+                                                      1e-12)
     return ef, et
 
 
