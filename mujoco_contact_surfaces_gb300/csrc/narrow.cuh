@@ -1329,8 +1329,8 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
 struct TetBStage {
   double g64[3], c64;  // FP64 field of the B tet in A's frame
   float g[3], gl;
-  float pn[4][3], po[4];     // face planes (inward unit normal, offset) in A's frame: FP32 head
-  float pnl[4][3], pol[4];   // and tail (head + tail: the FP64 plane to 2^-48)
+  float pn[4][3], po[4];     // face planes (inward unit normal, offset) in A's frame, from
+                             // the FP64 vertices, rounded to FP32
   float lo[3], hi[3];
   float M, h, kappa;
   int orig, valid;
@@ -1365,24 +1365,16 @@ __device__ __forceinline__ void stage_tetb(const StepArgs& a, const PairDev& P, 
   }
   M = fmaxf(M, fmaxf(fabsf(F.tf[0]), fmaxf(fabsf(F.tf[1]), fabsf(F.tf[2]))));
   tet_prepare(tb);
-  // the face planes in FP64 from the FP64 vertices, kept as FP32 head and
-  // tail: a plane offset of the order of the body's size rounded to FP32
-  // would misplace the clip of a first-touch contact by a sizeable share of
-  // its width
+  // the face planes in FP64 from the FP64 vertices (not from the vertices
+  // rounded to FP32), then rounded
   V3<double> pn[4];
   double po[4];
   tet_planes(bd.X, pn, po);
   S.g64[0] = bd.g.x; S.g64[1] = bd.g.y; S.g64[2] = bd.g.z; S.c64 = bd.c;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const double d[4] = {pn[k].x, pn[k].y, pn[k].z, po[k]};
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      S.pn[k][c] = (float)d[c];
-      S.pnl[k][c] = (float)(d[c] - (double)S.pn[k][c]);
-    }
-    S.po[k] = (float)d[3];
-    S.pol[k] = (float)(d[3] - (double)S.po[k]);
+    S.pn[k][0] = (float)pn[k].x; S.pn[k][1] = (float)pn[k].y; S.pn[k][2] = (float)pn[k].z;
+    S.po[k] = (float)po[k];
   }
   S.g[0] = tb.g.x; S.g[1] = tb.g.y; S.g[2] = tb.g.z; S.gl = tb.gl;
   const float pad = 1e-5f * M + 1e-7f;
@@ -1400,8 +1392,7 @@ __device__ __forceinline__ void stage_tetb(const StepArgs& a, const PairDev& P, 
 // clipped by tet B's faces.
 template <class R>
 __device__ int ss_polygon(const TetIn<R>& ta, const double s[4], V3<R> gb, R glb, V3<R> nrm, R lm,
-                          const V3<R> pn[4], const R po[4], R Mb, R hb, R kb, Decide& dc, int& anc, PV<R, 4>* out,
-                          const TetBStage* B = nullptr) {
+                          const V3<R> pn[4], const R po[4], R Mb, R hb, R kb, Decide& dc, int& anc, PV<R, 4>* out) {
   const R cond = (((R)1 + ta.kappa) * ta.gl + ((R)1 + kb + Mb / hb) * glb) / lm;
   const R tol_c = (R)kFilt * cond;
   const R ca = dot(nrm, ta.g) / ta.gl;
@@ -1417,11 +1408,7 @@ __device__ int ss_polygon(const TetIn<R>& ta, const double s[4], V3<R> gb, R glb
   for (int k = 0; k < 4; ++k)
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      if (sizeof(R) == 4 && B)   // staged planes: double-float on the FP32 pipe
-        tv[k].d[j] = (R)plane_df(B->pn[j], B->pnl[j], B->po[j], B->pol[j], (float)ta.X[k].x, (float)ta.X[k].y,
-                                 (float)ta.X[k].z);
-      else
-        tv[k].d[j] = dot(pn[j], ta.X[k]) - po[j];
+      tv[k].d[j] = dot(pn[j], ta.X[k]) - po[j];
       dmax[j] = fmax(dmax[j], abs_r(tv[k].d[j]));
     }
   int nv = tet_section(tv, s, dc, out);
@@ -1494,7 +1481,7 @@ __device__ __forceinline__ int ss_element_pair(const StepArgs& a, const FrameDev
   nrm = m * (1.f / lm);
   Decide dc;
   anc = 0;
-  int nv = ss_polygon<float>(t, s, gb, B.gl, nrm, lm, pn, B.po, B.M, B.h, B.kappa, dc, anc, poly, &B);
+  int nv = ss_polygon<float>(t, s, gb, B.gl, nrm, lm, pn, B.po, B.M, B.h, B.kappa, dc, anc, poly);
   gM = dot(t.g, nrm);
   gN = -dot(gb, nrm);
   flags = 0;

