@@ -8,8 +8,7 @@ The whole batch runs as one step.  A sample of its pairs (the largest
 contacts and random others) is compared with the oracle on exactly those
 pairs: candidate element-pair sets and per-pair polygon counts equal after a
 canonical sort (near-degenerate pairs counted and reported), area and wrench
-within 1e-5 (a pair made only of near-degenerate polygons is reported, not
-held to the wrench bar).  Properties that hold at any size are checked on the whole
+within 1e-5 (a pair made only of near-degenerate polygons within 5e-5).  Properties that hold at any size are checked on the whole
 batch: a repeated step is bit-identical, and sampled pairs computed alone in
 their own context give the batch's wrench and adjoint bit for bit (the batch
 changes the scheduling, never a pair's arithmetic)."""
@@ -19,6 +18,8 @@ import pytest
 from mujoco_contact_surfaces_gb300 import scenes
 from oracle import Oracle
 from tests._parity import AREA_RTOL, WRENCH_RTOL, compare_candidates, wrench_errors
+
+NEAR_RTOL = 5 * WRENCH_RTOL   # pairs made only of near-degenerate polygons
 
 pytestmark = pytest.mark.gpu
 
@@ -55,7 +56,8 @@ def _oracle_parity(s, pairs, w, stats, cand):
               f"{np.linalg.norm(ref['wrench'][k, :3]):.3e}, area {ref['area'][k]:.3e}, {ref['n_polygons'][k]} polygons")
     # A pair whose every polygon is near-degenerate on either side (a value
     # within 1e-12 of a clip threshold) is decided by rounding in either
-    # formulation, as its candidates are: reported, not held to the bar.
+    # formulation, as its candidates are: such pairs are tiny slivers (areas
+    # near 1e-9 m^2) and are held to five times the bar.
     ref_c = ref["candidates"]
     all_near = np.array([
         np.all(ref_c[ref_c[:, 0] == k, 4] & 1) or np.all(mine[mine[:, 0] == k, 4] & 1) if np.any(ref_c[:, 0] == k)
@@ -65,6 +67,8 @@ def _oracle_parity(s, pairs, w, stats, cand):
     held = ~all_near
     assert ef[held].max(initial=0) <= WRENCH_RTOL, f"force rel err {ef[held].max():.3e}"
     assert et[held].max(initial=0) <= WRENCH_RTOL, f"torque rel err {et[held].max():.3e}"
+    assert ef[all_near].max(initial=0) <= NEAR_RTOL, f"force rel err {ef[all_near].max():.3e} (near-degenerate)"
+    assert et[all_near].max(initial=0) <= NEAR_RTOL, f"torque rel err {et[all_near].max():.3e} (near-degenerate)"
     print(f"{len(pairs)} pairs, {common} polygons in common, {near} near-degenerate element pairs, "
           f"max rel err: force {ef.max():.2e}, torque {et.max():.2e}, area {ea.max(initial=0):.2e}")
     return common

@@ -90,10 +90,12 @@ def test_taxel_sensor_matches_oracle(gpu):
             # counts are decided by its side lengths over the resolution;
             # where a length lies within the surfaces' FP32 rounding of a
             # multiple of it, the two sides place a different grid on that
-            # triangle, which moves the taxels near it by up to that
-            # triangle's share (closest: the pressure change over one grid
-            # step, where the closest sample moves): nine in ten taxels agree
-            # at 1e-4 of the map maximum, every one within 1e-1.
+            # triangle.  Closest: a taxel whose closest sample moves takes the
+            # pressure change over one grid step, the others are unchanged:
+            # nine in ten taxels agree at 1e-4 of the map maximum, every one
+            # within 1e-1.  Squared: every taxel within the margin of that
+            # triangle averages over its samples, so several taxels move, each
+            # by a fraction of one sample's share: every one within 1e-2.
             # Area-importance samples are draws that
             # walk the running area of all fan triangles; surfaces that differ
             # by rounding move a draw into a neighbouring triangle, and a
@@ -104,8 +106,10 @@ def test_taxel_sensor_matches_oracle(gpu):
             sc2 = max(np.abs(ref2).max(), 1e-12)
             d2 = np.abs(got - ref2) / sc2
             e2e_stats.append((step, plate, ci, float(d2.max()), float(np.mean(d2 <= 1e-4))))
-            if sm == L.SAMPLE_DEFAULT:
+            if sm == L.SAMPLE_DEFAULT and m == L.TAXEL_CLOSEST:
                 assert d2.max() <= 1e-1 and np.mean(d2 <= 1e-4) >= 0.9, ("oracle surfaces", e2e_stats[-1])
+            elif sm == L.SAMPLE_DEFAULT:
+                assert d2.max() <= 1e-2, ("oracle surfaces", e2e_stats[-1])
             prev_e2e[(plate, ci)] = ref2
             if step == 0 and plate == s.g2[0]:
                 assert np.count_nonzero(ref) > 0
