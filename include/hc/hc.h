@@ -424,11 +424,11 @@ HC_API hc_status hc_get_stream(hc_context* ctx, void** stream);
 HC_API hc_status hc_get_launch_count(hc_context* ctx, int* n);
 /* Autotune the launch shape on the current pairs and poses: the grid of the
  * persistent kernels (CTAs per SM, 2-8) and the soft-rigid work-queue chunk
- * (consecutive work items a warp takes, 1-8), timed over three steps each;
+ * (consecutive work items a warp takes, 1-16), timed over three steps each;
  * the fastest is kept for later steps.  Outputs may be NULL.              */
 HC_API hc_status hc_autotune(hc_context* ctx, int* chosen_ctas_per_sm, int* chosen_chunk);
-/* Set the launch shape directly (CTAs per SM and work-queue chunk, each
- * 1-8), e.g. to a shape an earlier hc_autotune chose.                     */
+/* Set the launch shape directly (CTAs per SM 1-8, work-queue chunk 1-16),
+ * e.g. to a shape an earlier hc_autotune chose.                           */
 HC_API hc_status hc_set_launch_shape(hc_context* ctx, int ctas_per_sm, int chunk);
 
 /* ---- step without device allocation -------------------------------------

@@ -467,7 +467,7 @@ void launch_tet_props(const float4* tets, float4* props, int n_tets, cudaStream_
 // ---------------------------------------------------------------------------
 cudaError_t init_kernel_attributes() {
   cudaError_t e = cudaSuccess;
-  for (const void* k : {(const void*)narrow_sr_kernel<true, false>, (const void*)narrow_sr_kernel<false, false>,
+  for (const void* k : {(const void*)narrow_sr_keep_kernel<kSrKeepCtas>, (const void*)narrow_sr_kernel<false, false>,
                         (const void*)narrow_sr_kernel<true, true>, (const void*)narrow_sr_kernel<false, true>}) {
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
     if (e != cudaSuccess) return e;
@@ -563,7 +563,7 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
     const bool diag = (a.debug & 1) || a.want_polys;
     if (a.recs) {
       if (diag) narrow_sr_kernel<true, true><<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a);
-      else narrow_sr_kernel<true, false><<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a);
+      else narrow_sr_keep_kernel<kSrKeepCtas><<<a.narrow_grid, 128, kSrKeepSmemBytes, s>>>(a);
     } else {
       if (diag) narrow_sr_kernel<false, true><<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a);
       else narrow_sr_kernel<false, false><<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a);

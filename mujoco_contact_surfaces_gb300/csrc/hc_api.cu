@@ -1771,7 +1771,7 @@ hc_status hc_autotune(hc_context* c, int* chosen_ctas_per_sm, int* chosen_chunk)
   const int old_ctas = c->narrow_ctas_per_sm, old_chunk = c->narrow_chunk;
   c->timing = true;
   static const int kCtas[] = {2, 3, 4, 6, 8};
-  static const int kChunks[] = {1, 2, 4, 8};
+  static const int kChunks[] = {1, 2, 4, 8, 16};
   float best = INFINITY;
   int best_ctas = old_ctas, best_chunk = old_chunk;
   for (int ct : kCtas) {
@@ -1816,8 +1816,8 @@ hc_status hc_autotune(hc_context* c, int* chosen_ctas_per_sm, int* chosen_chunk)
 
 hc_status hc_set_launch_shape(hc_context* c, int ctas_per_sm, int chunk) {
   if (hc_status st = need(c)) return st;
-  if (ctas_per_sm < 1 || ctas_per_sm > 8 || chunk < 1 || chunk > 8)
-    return fail(HC_ERR_INVALID_ARG, "ctas_per_sm and chunk must be in 1-8");
+  if (ctas_per_sm < 1 || ctas_per_sm > 8 || chunk < 1 || chunk > 16)
+    return fail(HC_ERR_INVALID_ARG, "ctas_per_sm must be in 1-8 and chunk in 1-16");
   if (ctas_per_sm != c->narrow_ctas_per_sm || chunk != c->narrow_chunk) invalidate_graph(c);
   c->narrow_ctas_per_sm = ctas_per_sm;
   c->narrow_chunk = chunk;

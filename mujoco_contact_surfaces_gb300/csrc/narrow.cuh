@@ -714,31 +714,13 @@ __device__ __forceinline__ void tet_face_normals(const V3<float> X[4], V3<float>
   }
 }
 
-// Keeps this lane's polygon as an adjoint record.  All lanes of the warp
-// call it together once per round (`have` marks a polygon); the record's key
-// is (item, seq), seq being the polygon's rank among the item's polygons in
-// processing order (rounds, then lanes), so the keys do not depend on the
-// order in which warps reach the counter.
+// Writes record r of a kept polygon, keyed (item, seq).
 template <int ND>
-__device__ __forceinline__ void keep_polygon(const StepArgs& a, bool have, int item, int& seq, int lane, int pair,
-                                             int kind, const PV<float, ND>* poly, int nv, V3<float> anc,
-                                             V3<float> n, V3<float> g, float gint, const V3<float>* X,
-                                             const float (*clip)[3], int elem_a, int elem_b) {
-  const unsigned b = __ballot_sync(0xffffffffu, have);
-  if (!b) return;
-  int base = 0;
-  if (lane == 0) base = atomicAdd(a.rec_count, __popc(b));
-  base = __shfl_sync(0xffffffffu, base, 0);
-  const int rank = __popc(b & ((1u << lane) - 1u));
-  const int seq0 = seq;
-  seq += __popc(b);
-  if (!have) return;
-  const int r = base + rank;
-  if (r >= a.rec_cap) {
-    atomicOr(a.status, 8);
-    return;
-  }
-  a.rec_key[r] = make_int2(item, seq0 + rank);
+__device__ __forceinline__ void write_record(const StepArgs& a, int r, int item, int seq, int pair, int kind,
+                                             const PV<float, ND>* poly, int nv, V3<float> anc, V3<float> n,
+                                             V3<float> g, float gint, const V3<float>* X, const float (*clip)[3],
+                                             int elem_a, int elem_b) {
+  a.rec_key[r] = make_int2(item, seq);
   AdjPoly& R = a.recs[r];
   int l0 = 0, l1 = 0;
   for (int i = 0; i < kMaxPolyV; ++i) {
@@ -767,6 +749,33 @@ __device__ __forceinline__ void keep_polygon(const StepArgs& a, bool have, int i
   R.kind = kind;
   R.elem_a = elem_a;
   R.elem_b = elem_b;
+}
+
+// Keeps this lane's polygon as an adjoint record.  All lanes of the warp
+// call it together once per round (`have` marks a polygon); the record's key
+// is (item, seq), seq being the polygon's rank among the item's polygons in
+// processing order (rounds, then lanes), so the keys do not depend on the
+// order in which warps reach the counter.
+template <int ND>
+__device__ __forceinline__ void keep_polygon(const StepArgs& a, bool have, int item, int& seq, int lane, int pair,
+                                             int kind, const PV<float, ND>* poly, int nv, V3<float> anc,
+                                             V3<float> n, V3<float> g, float gint, const V3<float>* X,
+                                             const float (*clip)[3], int elem_a, int elem_b) {
+  const unsigned b = __ballot_sync(0xffffffffu, have);
+  if (!b) return;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(a.rec_count, __popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  const int rank = __popc(b & ((1u << lane) - 1u));
+  const int seq0 = seq;
+  seq += __popc(b);
+  if (!have) return;
+  const int r = base + rank;
+  if (r >= a.rec_cap) {
+    atomicOr(a.status, 8);
+    return;
+  }
+  write_record<ND>(a, r, item, seq0 + rank, pair, kind, poly, nv, anc, n, g, gint, X, clip, elem_a, elem_b);
 }
 
 constexpr int kNarrowWarps = 4;
@@ -1198,6 +1207,307 @@ __global__ void __launch_bounds__(128, 5) narrow_sr_kernel(StepArgs a) {
 
 constexpr size_t kSrSmemBytes = sizeof(SrWarpSmem) * kNarrowWarps;
 
+// ---- soft-rigid, polygons kept as records: rounds across items ------------
+//
+// The adjoint step's forward soft-rigid narrow phase.  An item (32 tets of
+// the soft body against a staged cluster of 32 triangles) typically holds
+// well under 32 candidate element pairs, so a round per item leaves most
+// lanes idle.  Here the candidates of consecutive items that share a pair
+// and a triangle cluster go into one circular queue per warp, and a round
+// takes the next 32 of them whatever their item.  A lane loads its
+// candidate's tet from global memory (the filter phase has just read it, so
+// the lines are in L1 or L2); nothing but the triangles is staged.  A record
+// is keyed (item, rank of the polygon among its item's polygons in
+// candidate order), the key narrow_sr_kernel gives it, so both kernels keep
+// the same records in the same slots.
+
+constexpr int kRing = 32;     // items with candidates pending in a warp's queue
+constexpr int kRQCap = 256;   // queue entries per warp (a power of two)
+
+// An item whose candidates are in the queue: its tets' base index, the
+// polygons and near-degenerate polygons it has so far, the candidates left.
+struct RingItem {
+  int item, tet_base, seq, near, left;
+};
+
+struct SrKeepWarpSmem {
+  TriStage tri[kCluster];
+  RingItem ring[kRing];
+  unsigned short q[kRQCap];   // ring slot | tet lane << 5 | triangle << 10
+};
+
+constexpr size_t kSrKeepSmemBytes = sizeof(SrKeepWarpSmem) * kNarrowWarps;
+
+// CTAs per SM narrow_sr_keep_kernel is compiled for (its register budget).
+#ifndef HC_SR_KEEP_CTAS
+#define HC_SR_KEEP_CTAS 6
+#endif
+constexpr int kSrKeepCtas = HC_SR_KEEP_CTAS;
+
+// The item's counts (its forces come from the records later).
+__device__ __forceinline__ void store_item_counts(const StepArgs& a, int item, int n_poly, int n_near) {
+  ItemOut r;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r.hi[i] = r.lo[i] = 0.f;
+  r.n_poly = n_poly; r.n_faces = 0; r.n_near = n_near; r.pad = 0;
+  a.item_out[item] = r;
+}
+
+// One round of up to 32 queued candidates (nr of them, from queue position
+// head): polygon, record, then the item bookkeeping.  Every lane calls it.
+__device__ __forceinline__ void sr_keep_round(const StepArgs& a, SrKeepWarpSmem& W, int pair, int head, int nr,
+                                              int lane) {
+  const bool on = lane < nr;
+  const int e = on ? W.q[(head + lane) & (kRQCap - 1)] : 0;
+  const int slot = e & 31, i = (e >> 5) & 31, j = e >> 10;
+  const int item = W.ring[slot].item, seq0 = W.ring[slot].seq;
+  const int tet_idx = W.ring[slot].tet_base + i;
+  bool have = false;
+  PV<float, 0> poly[kMaxPolyV];
+  TetIn<float> t;
+  V3<float> n = mk(0.f, 0.f, 0.f);
+  int nv = 0, anc = 0, orig_a = 0, orig_b = 0, flags = 0;
+  float gint = 0.f;
+  do {
+    if (!on) break;
+    const TriStage& T = W.tri[j];
+    load_tet(a.tets, tet_idx, t);
+    const float4 p0 = a.tet_props[2 * (size_t)tet_idx], p1 = a.tet_props[2 * (size_t)tet_idx + 1];
+    t.g = mk(p0.x, p0.y, p0.z);
+    t.gl = p0.w; t.kappa = p1.x; t.xmax = p1.y; t.pmax = p1.z;
+    t.c = 0.f; t.hmin = 0.f;
+    float s[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) s[q] = plane_df(T.n, T.nl, T.o, T.ol, t.X[q].x, t.X[q].y, t.X[q].z);
+    constexpr float tol = (float)kNearTol;
+    const bool allp = s[0] > tol && s[1] > tol && s[2] > tol && s[3] > tol;
+    const bool alln = s[0] < -tol && s[1] < -tol && s[2] < -tol && s[3] < -tol;
+    if (allp || alln) break;
+    n = mk(T.n[0], T.n[1], T.n[2]);
+    Decide dc;
+    nv = sr_poly_f(t, s, T, n, fmaxf(T.M, t.xmax), dc, anc, poly);
+    if (dc.unc) {
+      bool near;
+      nv = sr_fp64(a, T, tet_idx, anc, poly, near, gint);
+      flags = near ? 1 : 0;
+    } else if (nv >= 3) {
+      gint = dot(t.g, n);
+      if (fabsf(gint) <= 1e-5f * t.gl) {
+        double n64[3], o64;
+        tri_plane64(T, n64, o64);
+        gint = grad_along64(a, tet_idx, n64[0], n64[1], n64[2]);
+      }
+    }
+    if (nv < 3) break;
+    orig_a = a.tet_orig[tet_idx];
+    orig_b = T.orig;
+    have = true;
+  } while (0);
+  __syncwarp();
+  // the polygon's rank among its item's: the item's earlier polygons plus
+  // this round's on lower lanes of the same item
+  const unsigned hv = __ballot_sync(0xffffffffu, have);
+  const unsigned nm = __ballot_sync(0xffffffffu, have && flags);
+  const unsigned same = __match_any_sync(0xffffffffu, on ? slot : 32 + lane);
+  const unsigned lt = (1u << lane) - 1u;
+  if (hv) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(a.rec_count, __popc(hv));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (have) {
+      const int r = base + __popc(hv & lt);
+      if (r >= a.rec_cap) atomicOr(a.status, 8);
+      else
+        write_record<0>(a, r, item, seq0 + __popc(same & hv & lt), pair, 0, poly, nv, sel4(t.X, anc), n, t.g, gint,
+                        t.X, W.tri[j].en, orig_a, orig_b);
+    }
+  }
+  // the highest lane of each item's run updates the item; an item whose
+  // last candidate this was stores its counts
+  if (on && (same >> lane) == 1u) {
+    RingItem& R = W.ring[slot];
+    R.seq += __popc(same & hv);
+    R.near += __popc(same & nm);
+    R.left -= __popc(same);
+    if (R.left == 0) store_item_counts(a, R.item, R.seq, R.near);
+  }
+  __syncwarp();
+}
+
+// A float's bits as an int of the same order (for warp min/max reductions).
+__device__ __forceinline__ int ordered_bits(float f) {
+  const int i = __float_as_int(f);
+  return i ^ ((i >> 31) & 0x7fffffff);
+}
+
+// The tet at idx against the staged triangles that can reach the warp's
+// tets (tmask, from the union of their boxes): narrow_sr_kernel's per-pair
+// tests on the same values.  Returns the candidate mask.
+__device__ __forceinline__ unsigned sr_filter(const StepArgs& a, const SrKeepWarpSmem& W, int idx, bool in,
+                                              int n_o, int lane) {
+  float X[4][3];
+  float mlo[3], mhi[3], xmax = 0.f;
+  bool tv = false;
+  if (in) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float4 v = a.tets[4 * (size_t)idx + k];
+      X[k][0] = v.x; X[k][1] = v.y; X[k][2] = v.z;
+    }
+    const float4 p1 = a.tet_props[2 * (size_t)idx + 1];
+    tv = p1.w > 0.f;
+    xmax = p1.y;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    mlo[c] = INFINITY;
+    mhi[c] = -INFINITY;
+    if (tv) {
+      const float l = fminf(fminf(X[0][c], X[1][c]), fminf(X[2][c], X[3][c]));
+      const float h = fmaxf(fmaxf(X[0][c], X[1][c]), fmaxf(X[2][c], X[3][c]));
+      const float pad = 1e-5f * (fabsf(l) + fabsf(h)) + 1e-7f;
+      mlo[c] = l - pad;
+      mhi[c] = h + pad;
+    }
+  }
+  // the triangles whose box meets the union of the tets' boxes (a triangle
+  // that misses the union misses every tet's box): lane j tests triangle j
+  float clo[3], chi[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const int lo = __reduce_min_sync(0xffffffffu, ordered_bits(mlo[c]));
+    const int hi = __reduce_max_sync(0xffffffffu, ordered_bits(mhi[c]));
+    clo[c] = __int_as_float(lo ^ ((lo >> 31) & 0x7fffffff));
+    chi[c] = __int_as_float(hi ^ ((hi >> 31) & 0x7fffffff));
+  }
+  bool reach = false;
+  if (lane < n_o) {
+    const TriStage& T = W.tri[lane];
+    reach = T.valid && aabb_overlap(clo, chi, T.lo, T.hi);
+  }
+  unsigned tmask = __ballot_sync(0xffffffffu, reach);
+  unsigned mask = 0;
+  if (!tv) return 0;
+  while (tmask) {
+    const int jj = __ffs(tmask) - 1;
+    tmask &= tmask - 1;
+    const TriStage& T = W.tri[jj];
+    if (!aabb_overlap(mlo, mhi, T.lo, T.hi)) continue;
+    const float margin = 4e-6f * (xmax + fabsf(T.o) + T.Lt);
+    if (one_sided32(X, T.n, T.o, margin) || edge_outside32(X, T, xmax)) continue;
+    mask |= 1u << jj;
+  }
+  return mask;
+}
+
+// One loop step does one of: a round of queued candidates, a window of the
+// current item's candidates into the queue, or the next item (staging its
+// triangles, filtering its tets).  The round has one call site.
+template <int kMinCtas>
+__global__ void __launch_bounds__(128, kMinCtas) narrow_sr_keep_kernel(StepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  SrKeepWarpSmem& W = reinterpret_cast<SrKeepWarpSmem*>(smem_raw)[wid];
+  int staged_pair = -1, staged_oc = -1;
+  int head = 0, pending = 0, ring_ctr = 0;   // queue state, the same on every lane
+  int nxt = 0, end = 0;                      // the warp's chunk of items
+  int held = -1;                             // an item waiting for the queue to drain
+  bool drain = false, finished = false;
+  int from = 0, total = 0, slot = 0, w0 = 0; // the item being appended
+  unsigned mask = 0;
+  while (true) {
+    if (pending >= 32 || (pending > 0 && drain)) {
+      const int nr = min(32, pending);
+      sr_keep_round(a, W, staged_pair, head, nr, lane);
+      head += nr;
+      pending -= nr;
+      continue;
+    }
+    if (from < total) {
+      // the next window of the item's lane-major candidates
+      const int nput = min(total - from, kRQCap - pending);
+      const int tail = head + pending;
+      int w = w0;
+      const int incl = w0 + __popc(mask);
+      if (w < from + nput && incl > from) {
+        unsigned m = mask;
+        while (m) {
+          const int jj = __ffs(m) - 1;
+          m &= m - 1;
+          if (w >= from && w < from + nput)
+            W.q[(tail + w - from) & (kRQCap - 1)] = (unsigned short)(slot | (lane << 5) | (jj << 10));
+          ++w;
+        }
+      }
+      from += nput;
+      pending += nput;
+      __syncwarp();
+      continue;
+    }
+    drain = false;
+    int item = held;
+    if (item < 0) {
+      if (nxt >= end) {
+        if (finished) break;
+        int ie;
+        const int c0 = next_chunk(a, 0, lane, ie);
+        if (c0 >= ie) {
+          finished = true;
+          drain = true;
+          continue;
+        }
+        nxt = c0;
+        end = min(c0 + a.chunk, ie);
+      }
+      item = nxt++;
+    }
+    held = -1;
+    const int4 it = a.items[item];
+    const PairDev& P = a.pairs[it.x];
+    const FrameDev& F = a.frames[it.x];
+    const int sl = it.y, oc = it.z;
+    if (!F.valid) {
+      if (lane == 0) store_item_counts(a, item, 0, 0);
+      continue;
+    }
+    if (it.x != staged_pair || oc != staged_oc) {
+      if (pending > 0) {
+        // the queued candidates read the staged triangles: finish them first
+        held = item;
+        drain = true;
+        continue;
+      }
+      __syncwarp();
+      stage_tri(a, P, F, oc * kCluster + lane, W.tri[lane]);
+      staged_pair = it.x;
+      staged_oc = oc;
+      __syncwarp();
+    }
+    const int ti = sl * kCluster + lane;
+    mask = sr_filter(a, W, P.s_elem_off + ti, ti < P.s_n_elem, min(kCluster, P.o_n_elem - oc * kCluster), lane);
+    // lane-major positions of this lane's candidates
+    const int cnt = __popc(mask);
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    w0 = incl - cnt;
+    total = __shfl_sync(0xffffffffu, incl, 31);
+    from = 0;
+    if (total == 0) {
+      if (lane == 0) store_item_counts(a, item, 0, 0);
+      continue;
+    }
+    slot = ring_ctr & (kRing - 1);
+    ++ring_ctr;
+    if (lane == 0) {
+      RingItem& R = W.ring[slot];
+      R.item = item; R.tet_base = P.s_elem_off + sl * kCluster; R.seq = 0; R.near = 0; R.left = total;
+    }
+  }
+}
 
 // ============================================================================
 // soft vs rigid half-space

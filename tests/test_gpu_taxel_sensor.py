@@ -94,8 +94,10 @@ def test_taxel_sensor_matches_oracle(gpu):
             # pressure change over one grid step, the others are unchanged:
             # nine in ten taxels agree at 1e-4 of the map maximum, every one
             # within 1e-1.  Squared: every taxel within the margin of that
-            # triangle averages over its samples, so several taxels move, each
-            # by a fraction of one sample's share: every one within 1e-2.
+            # triangle sums over its samples, about five of them here (margin
+            # 2 mm, resolution 1.5 mm), so several taxels move, each by the
+            # weight of the samples that moved: the map's L1 difference within
+            # 5e-2 of its L1 norm, every taxel within 1e-1 of the map maximum.
             # Area-importance samples are draws that
             # walk the running area of all fan triangles; surfaces that differ
             # by rounding move a draw into a neighbouring triangle, and a
@@ -109,7 +111,8 @@ def test_taxel_sensor_matches_oracle(gpu):
             if sm == L.SAMPLE_DEFAULT and m == L.TAXEL_CLOSEST:
                 assert d2.max() <= 1e-1 and np.mean(d2 <= 1e-4) >= 0.9, ("oracle surfaces", e2e_stats[-1])
             elif sm == L.SAMPLE_DEFAULT:
-                assert d2.max() <= 1e-2, ("oracle surfaces", e2e_stats[-1])
+                l1 = np.abs(got - ref2).sum() / max(np.abs(ref2).sum(), 1e-12)
+                assert d2.max() <= 1e-1 and l1 <= 5e-2, ("oracle surfaces", e2e_stats[-1], l1)
             prev_e2e[(plate, ci)] = ref2
             if step == 0 and plate == s.g2[0]:
                 assert np.count_nonzero(ref) > 0
