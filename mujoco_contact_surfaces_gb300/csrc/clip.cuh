@@ -111,7 +111,9 @@ __device__ __forceinline__ void check(Decide& dc, R v, R tol) {
 // Section of a tet by s = 0 (s for the four vertices: FP64, or the FP32 head
 // of a double-float value, whose sign it has whenever it is not near zero).
 // Output: triangle or quad in cyclic order (marching-tetrahedron pattern),
-// each vertex interpolated from the endpoint with the smaller |s|.
+// each vertex interpolated from the endpoint with the smaller |s|.  The
+// winding of that order depends on the tet's parity and on which side holds
+// the single vertex; orient_ccw sets the finished polygon's.
 template <class R, int ND, class S>
 __device__ __forceinline__ int tet_section(const PV<R, ND> tv[4], const S s[4], Decide& dc, PV<R, ND> out[4]) {
   int pos = 0;
@@ -291,6 +293,37 @@ __device__ __forceinline__ int clip_pos(PV<float, 0>* p, int n, int j, const flo
     d_cur = d_nxt;
   }
   return m;
+}
+
+// Winds a finished polygon counter-clockwise about `up` (the direction in
+// which the section value grows: the contact plane's normal), as the
+// reference's contact polygons are wound: when the fan area vector from the
+// first vertex points against up, the order is reversed (first vertex
+// kept).  Clipping keeps a winding, so this is applied once per polygon, to
+// the FP32 result or to the FP64 pass's.  Each product and sum is rounded on
+// its own, so every kernel that builds the polygon decides the same way on
+// a sliver whose area is near zero.
+template <int ND>
+__device__ __forceinline__ void orient_ccw(PV<float, ND>* p, int nv, V3<float> up) {
+  if (nv < 3) return;
+  float w = 0.f;
+  const float x0 = p[0].x, y0 = p[0].y, z0 = p[0].z;
+  float ax = __fsub_rn(p[1].x, x0), ay = __fsub_rn(p[1].y, y0), az = __fsub_rn(p[1].z, z0);
+  for (int i = 2; i < nv; ++i) {
+    const float bx = __fsub_rn(p[i].x, x0), by = __fsub_rn(p[i].y, y0), bz = __fsub_rn(p[i].z, z0);
+    const float cx = __fsub_rn(__fmul_rn(ay, bz), __fmul_rn(az, by));
+    const float cy = __fsub_rn(__fmul_rn(az, bx), __fmul_rn(ax, bz));
+    const float cz = __fsub_rn(__fmul_rn(ax, by), __fmul_rn(ay, bx));
+    w = __fadd_rn(w, __fadd_rn(__fadd_rn(__fmul_rn(cx, up.x), __fmul_rn(cy, up.y)), __fmul_rn(cz, up.z)));
+    ax = bx; ay = by; az = bz;
+  }
+  if (w < 0.f) {
+    for (int i = 1, k = nv - 1; i < k; ++i, --k) {
+      const PV<float, ND> tmp = p[i];
+      p[i] = p[k];
+      p[k] = tmp;
+    }
+  }
 }
 
 // Linear field of a tet from its vertex values: p(x) = g.x + c; also the

@@ -195,6 +195,12 @@ struct hc_context {
   // forward step and adjoint captured as one graph (hc_step_adjoint*)
   cudaGraph_t fused_graph = nullptr;
   cudaGraphExec_t fused_exec = nullptr;
+  // host copies beside the fused graph (hc_step_adjoint): the upstream
+  // gradients go in and the taxel maps come out on copy_stream while the
+  // graph computes; xev[0] upstream in (the graph's adjoint waits on it),
+  // xev[1] forward done (recorded by the graph), xev[2] taxel maps out
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t xev[3] = {};
   bool fused_valid = false;
   const void* fused_key[6] = {};   // upstream, adjoint and result buffers it was captured with
   DevBuf<double> out_stage;        // fused step's results back to back: wrenches n x 6,
@@ -825,6 +831,12 @@ hc_status hc_context_create(const hc_config* cfg, hc_context** out) {
     return fail(HC_ERR_CUDA, "stream create failed");
   }
   for (auto& ev : c->ev) cudaEventCreate(&ev);
+  if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return fail(HC_ERR_CUDA, "stream create failed");
+  }
+  for (auto& ev : c->xev) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
   if (c->counters.reserve(kCntWords) != cudaSuccess) {
     delete c;
     return fail(HC_ERR_CUDA, "counter alloc failed");
@@ -839,8 +851,11 @@ hc_status hc_context_destroy(hc_context* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   invalidate_graph(c);
+  cudaStreamSynchronize(c->copy_stream);
   for (auto& ev : c->ev) cudaEventDestroy(ev);
+  for (auto& ev : c->xev) cudaEventDestroy(ev);
   cudaStreamDestroy(c->stream);
+  cudaStreamDestroy(c->copy_stream);
   delete c;   // every device array is freed by its destructor
   return HC_OK;
 }
@@ -1944,6 +1959,10 @@ static hc_status run_fused(hc_context* c, const double* d_dw, const float* d_dt)
     HC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(int), c->stream);
     c->launches_per_step = hc::launch_step(a, c->stream, ev);
+    // the forward's results are final here (the taxel maps may leave on
+    // the copy stream); the adjoint needs the upstream gradients in
+    cudaEventRecordWithFlags(c->xev[1], c->stream, cudaEventRecordExternal);
+    cudaStreamWaitEvent(c->stream, c->xev[0], cudaEventWaitExternal);
     c->adj_launches = hc::launch_adjoint(b, c->stream);
     if (n_pair > 0) {
       pack_results_kernel<<<(20 * n_pair + 255) / 256, 256, 0, c->stream>>>(c->pair_out.p, c->adj_out.p, n_pair,
@@ -1994,29 +2013,39 @@ hc_status hc_step_adjoint(hc_context* c, int n_geom, const double* xpos, const d
   const int n_pair = (int)c->pairs_h.size();
   const double* d_dw = nullptr;
   const float* d_dt = nullptr;
+  // the upstream gradients go in on the copy stream while the forward runs
+  // (the adjoint part of the graph waits for xev[0]); the buffers are free:
+  // the previous call waited for its graph
   if (dL_dwrench && n_pair) {
     HC_CUDA(c->adj_wrench.reserve(6 * (size_t)n_pair));
     HC_CUDA(cudaMemcpyAsync(c->adj_wrench.p, dL_dwrench, 6 * (size_t)n_pair * sizeof(double), cudaMemcpyHostToDevice,
-                            c->stream));
+                            c->copy_stream));
     d_dw = c->adj_wrench.p;
   }
   if (dL_dtaxel && c->n_cells) {
     HC_CUDA(c->adj_taxel.reserve(c->n_cells));
     HC_CUDA(cudaMemcpyAsync(c->adj_taxel.p, dL_dtaxel, (size_t)c->n_cells * sizeof(float), cudaMemcpyHostToDevice,
-                            c->stream));
+                            c->copy_stream));
     d_dt = c->adj_taxel.p;
   }
+  HC_CUDA(cudaEventRecord(c->xev[0], c->copy_stream));
   for (int attempt = 0; attempt < 4; ++attempt) {
     if (hc_status st = run_fused(c, d_dw, d_dt)) return st;
     if (n_pair == 0 && c->sensors.empty()) return HC_OK;
-    // results straight into the caller's arrays (each one contiguous copy
-    // from the packed results), then the status word; one wait for all of it
+    // the taxel maps leave on the copy stream once the forward is done,
+    // while the adjoint runs; the other results straight into the caller's
+    // arrays (each one contiguous copy from the packed results), then the
+    // status word; one wait for all of it
+    if (c->n_cells && taxels) {
+      HC_CUDA(cudaStreamWaitEvent(c->copy_stream, c->xev[1], 0));
+      HC_CUDA(cudaMemcpyAsync(taxels, c->taxels.p, (size_t)c->n_cells * sizeof(float), cudaMemcpyDeviceToHost,
+                              c->copy_stream));
+    }
+    HC_CUDA(cudaEventRecord(c->xev[2], c->copy_stream));
+    HC_CUDA(cudaStreamWaitEvent(c->stream, c->xev[2], 0));
     const double* st = c->out_stage.p;
     if (n_pair && wrench)
       HC_CUDA(cudaMemcpyAsync(wrench, st, 6 * (size_t)n_pair * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    if (c->n_cells && taxels)
-      HC_CUDA(cudaMemcpyAsync(taxels, c->taxels.p, (size_t)c->n_cells * sizeof(float), cudaMemcpyDeviceToHost,
-                              c->stream));
     if (n_pair && dL_dpose)
       HC_CUDA(cudaMemcpyAsync(dL_dpose, st + 6 * (size_t)n_pair, 12 * (size_t)n_pair * sizeof(double),
                               cudaMemcpyDeviceToHost, c->stream));
@@ -2050,6 +2079,9 @@ hc_status hc_step_adjoint_device(hc_context* c, const double* d_dL_dwrench, cons
   if (hc_status st = need(c)) return st;
   HC_CUDA(cudaSetDevice(c->device));
   if (hc_status st = fused_ready(c, false)) return st;
+  // the caller's upstream arrays are ordered on the context's stream: the
+  // graph's wait for upstream copies is met at once
+  HC_CUDA(cudaEventRecord(c->xev[0], c->stream));
   if (hc_status st = run_fused(c, d_dL_dwrench, d_dL_dtaxel)) return st;
   if (d_grad) *d_grad = c->adj_out.p;
   return HC_OK;

@@ -1173,6 +1173,7 @@ __global__ void __launch_bounds__(128, 5) narrow_sr_kernel(StepArgs a) {
           }
         }
         if (nv < 3) break;
+        orient_ccw(poly, nv, n);
         ac.n_poly += 1;
         ac.n_near += flags;
         orig_a = TS.orig;
@@ -1299,6 +1300,7 @@ __device__ __forceinline__ void sr_keep_round(const StepArgs& a, SrKeepWarpSmem&
       }
     }
     if (nv < 3) break;
+    orient_ccw(poly, nv, n);
     orig_a = a.tet_orig[tet_idx];
     orig_b = T.orig;
     have = true;
@@ -1603,6 +1605,7 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
         if (fabsf(gint) <= 1e-5f * t.gl) gint = grad_along64(a, tet_idx, n64[0], n64[1], n64[2]);
       }
       if (nv >= 3) {
+        orient_ccw(poly, nv, n);
         ac.n_poly += 1;
         ac.n_near += flags;
         orig_a = TS.orig;
@@ -1800,6 +1803,7 @@ __device__ __forceinline__ int ss_element_pair(const StepArgs& a, const FrameDev
     nv = ss_fp64(a, F, ta_idx, tb_idx, s, dc.unc, anc, poly, near, nrm, gM, gN, nv);
     flags = near ? 1 : 0;
   }
+  orient_ccw(poly, nv, nrm);
   return nv;
 }
 

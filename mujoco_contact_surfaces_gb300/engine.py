@@ -17,9 +17,31 @@ def _out(out, shape, dtype):
     """A new zeroed array, or the caller's (right dtype and size, C-contiguous)."""
     if out is None:
         return np.zeros(shape, dtype)
-    if out.dtype != dtype or out.size != int(np.prod(shape)) or not out.flags.c_contiguous:
-        raise ValueError(f"out must be a C-contiguous {np.dtype(dtype).name} array of {int(np.prod(shape))} elements")
+    size = 1
+    for s in shape:
+        size *= s
+    if out.dtype != dtype or out.size != size or not out.flags.c_contiguous:
+        raise ValueError(f"out must be a C-contiguous {np.dtype(dtype).name} array of {size} elements")
     return out
+
+
+class _Ptrs:
+    """ctypes pointers of the arrays a per-step call was last given: a call
+    that passes the same arrays again (a simulation loop's buffers) reuses
+    them instead of converting each array again.  Holds a reference to each
+    array, so an entry's pointer stays valid while it is kept."""
+
+    def __init__(self, n):
+        self.arr = [None] * n
+        self.ptr = [None] * n
+
+    def get(self, k, a, conv):
+        if a is None:
+            return None
+        if self.arr[k] is not a:
+            self.arr[k] = a
+            self.ptr[k] = conv(a)
+        return self.ptr[k]
 
 
 class Engine:
@@ -43,6 +65,7 @@ class Engine:
         self.n_taxel_values = 0   # taxels of all taxel-point sensors
         self.taxel_sensors = {}   # taxel sensor index -> number of taxels
         self.curved_sensors = {}  # curved sensor index -> number of taxels
+        self._step_ptrs = _Ptrs(9)
 
     def close(self):
         if self.ctx:
@@ -300,9 +323,11 @@ class Engine:
         t = _out(o[1], (n_cells,), np.float32)
         dpose = _out(o[2], (self.n_pair, 2, 6), np.float64)
         dE = _out(o[3], (self.n_pair, 2), np.float64)
-        L.check(self.lib.hc_step_adjoint(self.ctx, xpos.size // 3, L.dptr(xpos), L.dptr(xmat), L.dptr(v), L.dptr(dw),
-                                         L.fptr(dt), L.dptr(w), L.fptr(t) if n_cells else None, L.dptr(dpose),
-                                         L.dptr(dE)))
+        p = self._step_ptrs
+        L.check(self.lib.hc_step_adjoint(self.ctx, xpos.size // 3, p.get(0, xpos, L.dptr), p.get(1, xmat, L.dptr),
+                                         p.get(2, v, L.dptr), p.get(3, dw, L.dptr), p.get(4, dt, L.fptr),
+                                         p.get(5, w, L.dptr), p.get(6, t, L.fptr) if n_cells else None,
+                                         p.get(7, dpose, L.dptr), p.get(8, dE, L.dptr)))
         return w, t, dpose, dE
 
     def step_adjoint_device(self, d_dL_dwrench: int | None, d_dL_dtaxel: int | None) -> int:

@@ -75,6 +75,15 @@ def tet_section(X, s):
     return out, near
 
 
+def orient_ccw(poly, up):
+    """The finished polygon wound counter-clockwise about up (the direction in
+    which the section value grows), first vertex kept, as the device's
+    orient_ccw."""
+    x = [v for v, _ in poly]
+    w = sum(np.cross(x[i - 1] - x[0], x[i] - x[0]) @ up for i in range(2, len(x)))
+    return [poly[0]] + poly[1:][::-1] if w < 0 else poly
+
+
 def _shared(la, lb):
     return la[0] if la[0] in lb else la[1]
 
@@ -119,6 +128,7 @@ def element_polygon(XA, PA, XB, PB):
         near = near or nj
         if len(poly) < 3:
             return None
+    poly = orient_ccw(poly, n)
     return dict(x=[x for x, _ in poly], lab=[lab for _, lab in poly], n=n, gA=gA, cA=cA, gB=gB, lm=lm,
                 gM=gA @ n, gN=-(gB @ n), faceA=face_normals(XA), pnB=pn, near=near)
 

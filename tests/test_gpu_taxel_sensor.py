@@ -86,33 +86,22 @@ def test_taxel_sensor_matches_oracle(gpu):
             _check(got, ref, scale, (step, plate, CONFIGS[ci]))
             prev[(plate, ci)] = ref
             # end to end: the oracle's sensor on the oracle's surfaces.  With
-            # the default grid, the samples of a fan triangle are a grid whose
-            # counts are decided by its side lengths over the resolution;
-            # where a length lies within the surfaces' FP32 rounding of a
-            # multiple of it, the two sides place a different grid on that
-            # triangle.  Closest: a taxel whose closest sample moves takes the
-            # pressure change over one grid step, the others are unchanged:
-            # nine in ten taxels agree at 1e-4 of the map maximum, every one
-            # within 1e-1.  Squared: every taxel within the margin of that
-            # triangle sums over its samples, about five of them here (margin
-            # 2 mm, resolution 1.5 mm), so several taxels move, each by the
-            # weight of the samples that moved: the map's L1 difference within
-            # 5e-2 of its L1 norm, every taxel within 1e-1 of the map maximum.
-            # Area-importance samples are draws that
-            # walk the running area of all fan triangles; surfaces that differ
-            # by rounding move a draw into a neighbouring triangle, and a
-            # closest or weighted taxel then follows a different sample, so
-            # only the statistics are reported for those.
+            # the default grid the samples of a polygon depend on its vertex
+            # set and winding (each fan triangle's grid starts at the first
+            # vertex of its polygon edge), which the engine's surfaces share
+            # with the oracle's: every taxel within 1e-4 of the map maximum.
+            # Area-importance draws walk the running area of the fan
+            # triangles in order, which also depends on the vertex each
+            # polygon starts at (the oracle's Sutherland-Hodgman clip of the
+            # triangle starts elsewhere than the engine's clipped section),
+            # so only the statistics are reported for those.
             ref2 = oracle.taxel_sensor(tw, m, MARGIN, res, sm, vis, _oracle_surfaces(orc, s, plate, xpos),
                                        values=prev_e2e[(plate, ci)])
             sc2 = max(np.abs(ref2).max(), 1e-12)
             d2 = np.abs(got - ref2) / sc2
             e2e_stats.append((step, plate, ci, float(d2.max()), float(np.mean(d2 <= 1e-4))))
-            if sm == L.SAMPLE_DEFAULT and m == L.TAXEL_CLOSEST:
-                assert d2.max() <= 1e-1 and np.mean(d2 <= 1e-4) >= 0.9, ("oracle surfaces", e2e_stats[-1])
-            elif sm == L.SAMPLE_DEFAULT:
-                l1 = np.abs(got - ref2).sum() / max(np.abs(ref2).sum(), 1e-12)
-                assert d2.max() <= 1e-1 and l1 <= 5e-2, ("oracle surfaces", e2e_stats[-1], l1)
+            if sm == L.SAMPLE_DEFAULT:
+                assert d2.max() <= 1e-4, ("oracle surfaces", e2e_stats[-1])
             prev_e2e[(plate, ci)] = ref2
             if step == 0 and plate == s.g2[0]:
                 assert np.count_nonzero(ref) > 0
