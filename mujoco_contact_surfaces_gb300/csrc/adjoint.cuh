@@ -1278,6 +1278,14 @@ __global__ void __launch_bounds__(128, 5) adjoint_rec_kernel(StepArgs a) {
 // Per pair: upstream adjoints of the soft-frame sums from dL/dwrench
 // (wrench = [R_S F_S ; R_S T_S + (x_S - x_M) x R_S F_S]).
 __global__ void adjoint_setup_kernel(StepArgs a) {
+  // the work counters of the adjoint's kernels reuse the narrow phase's
+  if (blockIdx.x == 0) {
+    if (threadIdx.x < 3) a.item_next[threadIdx.x] = 0;
+    if (threadIdx.x == 3 && a.adj_skip) {
+      a.adj_skip[0] = 0;
+      a.adj_skip[1] = 0x7f800000;   // +infinity
+    }
+  }
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= a.n_pair) return;
   const FrameDev& F = a.frames[p];
@@ -1298,10 +1306,7 @@ __global__ void adjoint_setup_kernel(StepArgs a) {
 
 // Per pair: sum of the item gradients (fixed order, FP64) and the chain rule
 // to the world twists of M and N, plus dL/dE.
-__global__ void adjoint_reduce_kernel(StepArgs a) {
-  const int lane = threadIdx.x & 31;
-  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (p >= a.n_pair) return;
+__device__ __forceinline__ void adjoint_reduce_pair(const StepArgs& a, int p, int lane) {
   const PairDev& P = a.pairs[p];
   const int total = *a.item_total;
   const int b = min(a.unit_off[P.unit_begin], total), e = min(a.unit_off[P.unit_end], total);
@@ -1409,5 +1414,23 @@ __global__ void adjoint_reduce_kernel(StepArgs a) {
     }
     dE /= (double)P.E_s;
     out[12 + (sm ? 0 : 1)] = dE;
+  }
+}
+
+// A warp per pair (adjoint_reduce_pair); in a fused step, lane 0 also packs
+// the pair's results for the host copy: its wrench, its two twist gradients
+// and its two moduli terms, each kind back to back over the pairs.
+__global__ void adjoint_reduce_kernel(StepArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (p >= a.n_pair) return;
+  adjoint_reduce_pair(a, p, lane);
+  if (lane == 0 && a.out_stage) {
+    const size_t n = (size_t)a.n_pair;
+    const double* g = a.adj_out + 14 * (size_t)p;
+    double* o = a.out_stage;
+    for (int k = 0; k < 6; ++k) o[6 * (size_t)p + k] = a.pair_out[p].wrench[k];
+    for (int k = 0; k < 12; ++k) o[6 * n + 12 * (size_t)p + k] = g[k];
+    for (int k = 0; k < 2; ++k) o[18 * n + 2 * (size_t)p + k] = g[12 + k];
   }
 }

@@ -69,9 +69,7 @@ void launch_refit(const float4* elems, int vpe, float4* nodes, const int* geom_e
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool finite_d(double x) { return isfinite(x); }
 
-__global__ void frames_kernel(StepArgs a) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= a.n_pair) return;
+__device__ __forceinline__ void pair_frame(const StepArgs& a, int p) {
   const PairDev P = a.pairs[p];
   FrameDev F;
   if (P.query == 0) {   // unsupported pair: no poses are read
@@ -146,6 +144,37 @@ __global__ void frames_kernel(StepArgs a) {
   F.valid = ok ? 1 : 0;
   F.pad = 0;
   a.frames[p] = F;
+}
+
+// Every flat sensor's samples inside the box the last step touched go back
+// to "no hit" (the taxel pass clears what it reads unless the samples are
+// kept for the adjoint), and the box is emptied.  One block, rows of the box
+// across its threads.
+__device__ __forceinline__ void clear_box(const StepArgs& a, int sid) {
+  const SensorDev S = a.sensors[sid];
+  const int4 b = a.sens_box[sid];
+  if (b.x <= b.y && b.z <= b.w) {
+    unsigned long long* smp = a.samples + S.sample_off;
+    const int nY = b.w - b.z + 1, cnt = (b.y - b.x + 1) * nY;
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x)
+      smp[(size_t)(b.x + i / nY) * S.ny + b.z + i % nY] = ~0ull;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) a.sens_box[sid] = make_int4(0x7fffffff, -1, 0x7fffffff, -1);
+}
+
+// The step's first kernel: the step counters zeroed (block 0), the pair
+// frames (a thread per pair in the first n_frame_blocks blocks) and, in the
+// blocks after them, one block per flat sensor clearing the last step's
+// touched samples.  The three are independent.
+__global__ void step_begin_kernel(StepArgs a, int n_frame_blocks) {
+  if ((int)blockIdx.x < n_frame_blocks) {
+    if (blockIdx.x == 0 && a.reset_words && threadIdx.x < kResetWords) a.reset_words[threadIdx.x] = 0;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < a.n_pair) pair_frame(a, p);
+  } else {
+    clear_box(a, blockIdx.x - n_frame_blocks);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -415,49 +444,96 @@ __global__ void reduce_kernel(StepArgs a) {
 // reference's i-major, j-minor order, weight * pressure * (1/s^2); the
 // sample slots are reset for the next step.
 // ---------------------------------------------------------------------------
-__global__ void taxel_kernel(StepArgs a) {
-  const int gc = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gc >= a.n_cells_total) return;
-  const int sid = a.cell_sensor[gc];
-  const SensorDev S = a.sensors[sid];
-  const int cell = gc - a.cell_first[sid];
-  const int x = cell / S.cy, y = cell % S.cy;
-  if (a.sens_box) {
-    // a cell whose samples lie outside every box this step's rays touched
-    // holds no hit: its value is 0 and its samples are already clear
-    const int4 b = a.sens_box[sid];
-    if (x * S.sr > b.y || x * S.sr + S.sr - 1 < b.x || y * S.sr > b.w || y * S.sr + S.sr - 1 < b.z) {
-      a.taxels[S.taxel_off + x + S.cy * y] = 0.f;
-      return;
-    }
+// The pressure a sample holds (0 when no ray hit it): the value itself, or
+// for a sample won by a kept polygon that polygon's pressure model at the
+// sample, times the sensor's 1/s^2.
+__device__ __forceinline__ float sample_pressure(const StepArgs& a, const SensorDev& S, unsigned long long k, int X,
+                                                 int Y) {
+  if (k == ~0ull) return 0.f;
+  const unsigned lo = (unsigned)(k & 0xffffffffu);
+  float pr = __uint_as_float(lo);
+  if (lo & kSlotTag) {
+    const int slot = (int)(lo & ~(kSlotTag | kSideBit));
+    const int side = (lo & kSideBit) ? 1 : 0;
+    const float4 m0 = a.slot_press[6 * (size_t)slot + 3 * side];
+    const float4 m1 = a.slot_press[6 * (size_t)slot + 3 * side + 1];
+    pr = raster_pressure(m0.x, m0.y, m0.z, m0.w, m1.x, a.samp_coord[S.samp_off_x + X], a.samp_coord[S.samp_off_y + Y]);
+  }
+  return pr * S.rmean;
+}
+
+// Samples of a touched box resolved in shared memory at once.
+constexpr int kTaxBoxSamples = 8192;
+
+// A block per sensor.  Its touched box's samples are resolved first, each by
+// its own thread (the sample, then the winning polygon's pressure model: two
+// dependent loads, issued for many samples at once), into shared memory;
+// then each cell sums its samples from there in the reference's i-major,
+// j-minor order.  Cells outside the box hold no hit (value 0).  A box larger
+// than the shared array is summed cell by cell from global memory.
+__global__ void __launch_bounds__(256) taxel_kernel(StepArgs a) {
+  __shared__ SensorDev S;
+  __shared__ int4 box;
+  __shared__ float val[kTaxBoxSamples];
+  const int sid = blockIdx.x;
+  if (threadIdx.x == 0) {
+    S = a.sensors[sid];
+    // without boxes every sample is read (the no-alloc step clears them all)
+    box = a.sens_box ? a.sens_box[sid] : make_int4(0, S.nx - 1, 0, S.ny - 1);
+    box.x = max(box.x, 0); box.y = min(box.y, S.nx - 1);
+    box.z = max(box.z, 0); box.w = min(box.w, S.ny - 1);
+  }
+  __syncthreads();
+  const int n = S.cx * S.cy;
+  float* out = a.taxels + S.taxel_off;
+  if (box.x > box.y || box.z > box.w) {
+    // no ray of this step touched the sensor: every value is 0 and its
+    // samples are already clear
+    for (int cell = threadIdx.x; cell < n; cell += blockDim.x) out[cell / S.cy + S.cy * (cell % S.cy)] = 0.f;
+    return;
   }
   unsigned long long* smp = a.samples + S.sample_off;
   const float* w = a.weights + S.weight_off;
-  float avg = 0.f;
-  for (int i = 0; i < S.sr; ++i) {
-    const int X = x * S.sr + i;
-    for (int j = 0; j < S.sr; ++j) {
-      const int Y = y * S.sr + j;
-      unsigned long long k = smp[(size_t)X * S.ny + Y];
-      if (k != ~0ull) {
-        const unsigned lo = (unsigned)(k & 0xffffffffu);
-        float pr = __uint_as_float(lo);
-        if (lo & kSlotTag) {
-          // won by a kept polygon: its pressure model for this sensor
-          const int slot = (int)(lo & ~(kSlotTag | kSideBit));
-          const int side = (lo & kSideBit) ? 1 : 0;
-          const float4 m0 = a.slot_press[6 * (size_t)slot + 3 * side];
-          const float4 m1 = a.slot_press[6 * (size_t)slot + 3 * side + 1];
-          pr = raster_pressure(m0.x, m0.y, m0.z, m0.w, m1.x, a.samp_coord[S.samp_off_x + X],
-                               a.samp_coord[S.samp_off_y + Y]);
+  const int bw = box.w - box.z + 1, nb = (box.y - box.x + 1) * bw;
+  const bool staged = nb <= kTaxBoxSamples;
+  if (staged) {
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+      const int X = box.x + i / bw, Y = box.z + i % bw;
+      unsigned long long* q = smp + (size_t)X * S.ny + Y;
+      const unsigned long long k = *q;
+      val[i] = sample_pressure(a, S, k, X, Y);
+      if (!a.keep_samples && k != ~0ull) *q = ~0ull;
+    }
+    __syncthreads();
+  }
+  for (int cell = threadIdx.x; cell < n; cell += blockDim.x) {
+    const int x = cell / S.cy, y = cell % S.cy;
+    // a cell whose samples lie outside the box this step's rays touched
+    // holds no hit: its value is 0 and its samples are already clear
+    if (x * S.sr > box.y || x * S.sr + S.sr - 1 < box.x || y * S.sr > box.w || y * S.sr + S.sr - 1 < box.z) {
+      out[x + S.cy * y] = 0.f;
+      continue;
+    }
+    float avg = 0.f;
+    for (int i = 0; i < S.sr; ++i) {
+      const int X = x * S.sr + i;
+      for (int j = 0; j < S.sr; ++j) {
+        const int Y = y * S.sr + j;
+        if (X < box.x || X > box.y || Y < box.z || Y > box.w) continue;   // no hit there
+        float raw;
+        if (staged) {
+          raw = val[(X - box.x) * bw + (Y - box.z)];
+        } else {
+          unsigned long long* q = smp + (size_t)X * S.ny + Y;
+          const unsigned long long k = *q;
+          raw = sample_pressure(a, S, k, X, Y);
+          if (!a.keep_samples && k != ~0ull) *q = ~0ull;
         }
-        float raw = pr * S.rmean;
-        avg += w[i * S.sr + j] * raw;
-        if (!a.keep_samples) smp[(size_t)X * S.ny + Y] = ~0ull;
+        avg = __fadd_rn(avg, __fmul_rn(w[i * S.sr + j], raw));
       }
     }
+    out[x + S.cy * y] = avg;
   }
-  a.taxels[S.taxel_off + x + S.cy * y] = avg;
 }
 
 void launch_tet_props(const float4* tets, float4* props, int n_tets, cudaStream_t s) {
@@ -489,37 +565,9 @@ void record_ctas_per_sm(int* fwd, int* adj) {
     *adj = 1;
 }
 
-// Start of a step: every flat sensor's samples inside the box the last step
-// touched go back to "no hit" (the taxel pass clears what it reads unless the
-// samples are kept for the adjoint), and the box is emptied.  A block per
-// sensor, rows of the box across its threads.
-__global__ void clear_boxes_kernel(StepArgs a) {
-  const int sid = blockIdx.x;
-  const SensorDev S = a.sensors[sid];
-  const int4 b = a.sens_box[sid];
-  if (b.x <= b.y && b.z <= b.w) {
-    unsigned long long* smp = a.samples + S.sample_off;
-    const int nY = b.w - b.z + 1, cnt = (b.y - b.x + 1) * nY;
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x)
-      smp[(size_t)(b.x + i / nY) * S.ny + b.z + i % nY] = ~0ull;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) a.sens_box[sid] = make_int4(0x7fffffff, -1, 0x7fffffff, -1);
-}
-
-// Work counters of the adjoint pass reuse the narrow-phase ones.
-__global__ void reset_next_kernel(StepArgs a) {
-  if (threadIdx.x < 3) a.item_next[threadIdx.x] = 0;
-  if (threadIdx.x == 3 && a.adj_skip) {
-    a.adj_skip[0] = 0;
-    a.adj_skip[1] = 0x7f800000;   // +infinity
-  }
-}
-
 int launch_adjoint(const StepArgs& a, cudaStream_t s) {
   int n = 0;
   if (a.n_pair <= 0) return 0;
-  reset_next_kernel<<<1, 32, 0, s>>>(a); ++n;
   adjoint_setup_kernel<<<(a.n_pair + 127) / 128, 128, 0, s>>>(a); ++n;
   if (a.use_recs) {
     // kept polygons, in the slots the forward assigned (returns at once if
@@ -528,10 +576,13 @@ int launch_adjoint(const StepArgs& a, cudaStream_t s) {
     else adjoint_rec_kernel<0><<<a.rec_adj_grid, 128, 0, s>>>(a);
     ++n;
   }
-  if (a.type_unit_end[0] > a.type_unit_begin[0]) {
+  // the recomputing soft-rigid and half-space adjoints (they return at once
+  // when the kept polygons are valid; a fused step re-runs on an overflow)
+  const bool recompute = !(a.use_recs && a.fused);
+  if (recompute && a.type_unit_end[0] > a.type_unit_begin[0]) {
     adjoint_sr_kernel<<<a.narrow_grid, 128, kSrSmemBytes, s>>>(a); ++n;
   }
-  if (a.type_unit_end[1] > a.type_unit_begin[1]) {
+  if (recompute && a.type_unit_end[1] > a.type_unit_begin[1]) {
     adjoint_hs_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
   }
   if (a.type_unit_end[2] > a.type_unit_begin[2]) {
@@ -544,11 +595,10 @@ int launch_adjoint(const StepArgs& a, cudaStream_t s) {
 int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   int n = 0;
   if (ev) cudaEventRecordWithFlags(ev[0], s, cudaEventRecordExternal);
-  if (a.sens_box && a.n_sensor > 0) {
-    clear_boxes_kernel<<<a.n_sensor, 256, 0, s>>>(a); ++n;
-  }
-  if (a.n_pair > 0) {
-    frames_kernel<<<(a.n_pair + 127) / 128, 128, 0, s>>>(a); ++n;
+  {
+    const int nfb = a.n_pair > 0 ? (a.n_pair + 127) / 128 : 1;
+    const int nsb = a.sens_box ? a.n_sensor : 0;
+    step_begin_kernel<<<nfb + nsb, 128, 0, s>>>(a, nfb); ++n;
   }
   if (ev) cudaEventRecordWithFlags(ev[1], s, cudaEventRecordExternal);
   if (a.n_units > 0) {
@@ -609,7 +659,7 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   }
   if (ev) cudaEventRecordWithFlags(ev[4], s, cudaEventRecordExternal);
   if (a.n_cells_total > 0) {
-    taxel_kernel<<<(a.n_cells_total + 127) / 128, 128, 0, s>>>(a); ++n;
+    taxel_kernel<<<a.n_sensor, 256, 0, s>>>(a); ++n;
   }
   if (ev) cudaEventRecordWithFlags(ev[5], s, cudaEventRecordExternal);
   return n;

@@ -122,6 +122,7 @@ constexpr int kCntNext = 4;    // three work counters, one per query type
 constexpr int kCntRec = 7;     // adjoint records kept (may exceed the capacity)
 constexpr int kCntAdjSkip = 8; // two words: adjoint vertices left out, smallest |det| (debug)
 constexpr int kCntWords = 16;
+static_assert(kCntRec < hc::kResetWords, "the step's first kernel zeroes the counters up to kCntRec");
 
 int next_pow2(int n) {
   int p = 1;
@@ -631,6 +632,7 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
   a.n_bp_blocks = c->n_bp_blocks;
   a.items = c->items.p;
   a.item_cap = c->item_cap;
+  a.reset_words = c->counters.p;   // kResetWords (8) words: total .. rec
   a.item_total = c->counters.p + kCntTotal;
   a.status = c->counters.p + kCntStatus;
   a.cand_count = c->counters.p + kCntCand;
@@ -722,7 +724,7 @@ hc_status run_step(hc_context* c, int want_polys, int want_pair) {
   c->recs_step = a.recs != nullptr;
   c->step_checked = false;
   c->last_fused = false;
-  HC_CUDA(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(int), c->stream));
+  // (the step's first kernel zeroes the counters: StepArgs::reset_words)
   // samples an earlier step kept lie inside that step's touched boxes: the
   // step's first kernel clears those boxes (launch_step)
   c->samples_dirty = c->adjoint_mode && c->n_cells > 0;
@@ -1906,20 +1908,6 @@ static hc_status ensure_kept_samples(hc_context* c) {
 
 // The fused step's per-pair results back to back (one contiguous read each
 // for the host instead of strided rows): wrench (6), dL/dpose (12), dL/dE (2).
-__global__ void pack_results_kernel(const hc::PairOut* __restrict__ po, const double* __restrict__ adj, int n_pair,
-                                    double* __restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= 20 * n_pair) return;
-  if (i < 6 * n_pair) {
-    out[i] = po[i / 6].wrench[i % 6];
-  } else if (i < 18 * n_pair) {
-    const int k = i - 6 * n_pair;
-    out[i] = adj[14 * (k / 12) + k % 12];
-  } else {
-    const int k = i - 18 * n_pair;
-    out[i] = adj[14 * (k / 2) + 12 + k % 2];
-  }
-}
 
 // The forward step and its adjoint as one graph on the context stream: the
 // counters and kept samples cleared, the step's kernels, then the adjoint's
@@ -1949,6 +1937,8 @@ static hc_status run_fused(hc_context* c, const double* d_dw, const float* d_dt)
     b.use_recs = 1;
     b.rec_grad = c->rec_grad.p;
   }
+  b.out_stage = c->out_stage.p;
+  b.fused = 1;
   c->recs_step = a.recs != nullptr;
   c->step_checked = false;
   const void* key[6] = {d_dw, b.adj_taxel, c->adj_pair.p, c->adj_item.p, c->adj_out.p, c->out_stage.p};
@@ -1957,18 +1947,12 @@ static hc_status run_fused(hc_context* c, const double* d_dw, const float* d_dt)
     invalidate_graph(c);
     cudaEvent_t* ev = c->timing ? c->ev : nullptr;
     HC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(int), c->stream);
     c->launches_per_step = hc::launch_step(a, c->stream, ev);
     // the forward's results are final here (the taxel maps may leave on
     // the copy stream); the adjoint needs the upstream gradients in
     cudaEventRecordWithFlags(c->xev[1], c->stream, cudaEventRecordExternal);
     cudaStreamWaitEvent(c->stream, c->xev[0], cudaEventWaitExternal);
     c->adj_launches = hc::launch_adjoint(b, c->stream);
-    if (n_pair > 0) {
-      pack_results_kernel<<<(20 * n_pair + 255) / 256, 256, 0, c->stream>>>(c->pair_out.p, c->adj_out.p, n_pair,
-                                                                             c->out_stage.p);
-      ++c->adj_launches;
-    }
     if (ev) cudaEventRecordWithFlags(ev[7], c->stream, cudaEventRecordExternal);
     cudaError_t e = cudaStreamEndCapture(c->stream, &c->fused_graph);
     if (e != cudaSuccess) return fail(HC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));

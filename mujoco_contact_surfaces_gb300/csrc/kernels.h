@@ -7,6 +7,9 @@
 
 namespace hc {
 
+// Step counters the step's first kernel zeroes (StepArgs::reset_words).
+constexpr int kResetWords = 8;
+
 struct StepArgs {
   // per-step inputs (device)
   const double* xpos;
@@ -90,6 +93,11 @@ struct StepArgs {
   int* adj_skip;             // with debug recording: [0] adjoint polygon vertices left out
                              // of the contraction, [1] the smallest normalised |det| (bits), else null
   int use_recs;              // the adjoint reads the kept polygons (when none overflowed)
+  int* reset_words;          // kResetWords step counters zeroed by the step's first kernel (null: none)
+  double* out_stage;         // fused step: the adjoint's last kernel packs the results here
+                             // (wrenches n x 6, twist gradients n x 12, moduli n x 2), else null
+  int fused;                 // fused step: an overflow re-runs the whole step, so the
+                             // recomputing adjoint fallbacks are left out
   int* item_poly_off;        // per item: first record of the item in pair order (item_cap + 1)
   int* poly_block_sum;       // one per kBpBlock items
   int n_item_blocks;         // item_cap / kBpBlock rounded up

@@ -135,6 +135,9 @@ extern "C" HC_API hc_status hc_step_noalloc(hc_context* ctx, int n_geom, const d
     return hc::set_last_error(HC_ERR_OVERFLOW, msg);
   }
   a.item_cap = item_cap;
+  a.reset_words = nullptr;   // zeroed below, with the samples
+  a.out_stage = nullptr;
+  a.fused = 0;
   a.item_total = words + kWTotal;
   a.status = words + kWStatus;
   a.cand_count = words + kWCand;

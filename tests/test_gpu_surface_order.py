@@ -68,15 +68,22 @@ def _check(s, min_polys):
         for i in range(len(ke)):
             ve = _dedupe(se["vert"][se["offset"][i]:se["offset"][i + 1]])
             vo = _dedupe(so["vert"][so["offset"][i]:so["offset"][i + 1]])
-            if len(ve) != len(vo):
+            r = _match(ve, vo) if len(ve) == len(vo) else None
+            if r is None:
+                # a collinear vertex that one side has (or that the two
+                # sides place at different points of the same edge)
                 ve, vo = _drop_collinear(ve), _drop_collinear(vo)
                 collinear += 1
-            assert len(ve) == len(vo), (p, ke[i], len(ve), len(vo))
-            r = _match(ve, vo)
+                assert len(ve) == len(vo), (p, ke[i], len(ve), len(vo))
+                r = _match(ve, vo)
             if r is None:
                 rev = _match(ve[::-1], vo)
+                dev = min(np.abs(np.roll(ve, k, axis=0) - vo).max() for k in range(len(ve)))
+                size = np.ptp(vo, axis=0).max()
                 raise AssertionError(f"pair {p} polygon {ke[i]}: no cyclic shift matches the oracle's "
-                                     f"({'reversed winding' if rev is not None else 'different vertices'})")
+                                     f"({'reversed winding' if rev is not None else 'different vertices'}; "
+                                     f"best shift off by {dev:.3e} m, polygon size {size:.3e} m)\n"
+                                     f"engine {np.round(ve, 9).tolist()}\noracle {np.round(vo, 9).tolist()}")
             # the unit normal: soft-soft's is the FP32 difference of two tet
             # gradients, normalised (FP64 only where a decision needs it)
             np.testing.assert_allclose(se["normal"][i], so["normal"][i], atol=1e-5)
