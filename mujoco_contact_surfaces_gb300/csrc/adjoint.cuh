@@ -495,6 +495,7 @@ __global__ void __launch_bounds__(128, 4) adjoint_sr_kernel(StepArgs a) {
       if (dc.unc) {
         bool near;
         nv = sr_fp64(a, T, tet_idx, anc, poly, near, gint);
+        orient_ccw(poly, nv, n);
       } else if (nv >= 3) {
         gint = dot(t.g, n);
         if (fabsf(gint) <= 1e-5f * t.gl) {
@@ -504,7 +505,6 @@ __global__ void __launch_bounds__(128, 4) adjoint_sr_kernel(StepArgs a) {
         }
       }
       if (nv < 3) continue;
-      orient_ccw(poly, nv, n);
       // taxel adjoint on the forward polygon
       if (a.adj_taxel) {
         if (P.sensor0 >= 0)
@@ -576,12 +576,12 @@ __global__ void __launch_bounds__(128, 4) adjoint_hs_kernel(StepArgs a) {
       if (dc.unc) {
         bool near;
         nv = hs_fp64(a, F, tet_idx, s, anc, poly, near, gint);
+        orient_ccw(poly, nv, n);
       } else if (nv >= 3) {
         gint = dot(t.g, n);
         if (fabsf(gint) <= 1e-5f * t.gl) gint = grad_along64(a, tet_idx, n64[0], n64[1], n64[2]);
       }
       if (nv >= 3) {
-        orient_ccw(poly, nv, n);
         if (a.adj_taxel) {
           if (P.sensor0 >= 0)
             raster_keys<1>(a, P.sensor0, F.Rl, F.tl, poly, nv, t.X[anc], t.g, n,

@@ -108,12 +108,32 @@ __device__ __forceinline__ void check(Decide& dc, R v, R tol) {
   }
 }
 
+// a - b and (a x b) . u with every product and sum rounded on its own.
+__device__ __forceinline__ V3<float> sub_rn(V3<float> a, V3<float> b) {
+  return mk(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+}
+__device__ __forceinline__ float winding_rn(V3<float> a, V3<float> b, V3<float> u) {
+  const float cx = __fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y));
+  const float cy = __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z));
+  const float cz = __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x));
+  return __fadd_rn(__fadd_rn(__fmul_rn(cx, u.x), __fmul_rn(cy, u.y)), __fmul_rn(cz, u.z));
+}
+
+// Sign patterns (bit k: s_k > 0) whose marching-tetrahedron section below
+// winds clockwise about grad s in a positively oriented tet, whose
+// (X1 - X0) . ((X2 - X0) x (X3 - X0)) > 0; a negatively oriented tet winds
+// every pattern the other way.
+constexpr unsigned kSectionCw = 0x32DAu;   // patterns 1, 3, 4, 6, 7, 9, 12, 13
+
 // Section of a tet by s = 0 (s for the four vertices: FP64, or the FP32 head
 // of a double-float value, whose sign it has whenever it is not near zero).
 // Output: triangle or quad in cyclic order (marching-tetrahedron pattern),
-// each vertex interpolated from the endpoint with the smaller |s|.  The
-// winding of that order depends on the tet's parity and on which side holds
-// the single vertex; orient_ccw sets the finished polygon's.
+// each vertex interpolated from the endpoint with the smaller |s|.  In FP32
+// the order is counter-clockwise about grad s (the contact plane's normal),
+// as the reference's contact polygons wind: the pattern's winding, from
+// kSectionCw and the tet's parity, decides whether the vertices after the
+// first are stored in reverse, and clipping keeps the winding.  The FP64
+// fallbacks leave the marching order; orient_ccw winds their results.
 template <class R, int ND, class S>
 __device__ __forceinline__ int tet_section(const PV<R, ND> tv[4], const S s[4], Decide& dc, PV<R, ND> out[4]) {
   int pos = 0;
@@ -127,6 +147,14 @@ __device__ __forceinline__ int tet_section(const PV<R, ND> tv[4], const S s[4], 
   }
   const int np = __popc(pos);
   if (np == 0 || np == 4) return 0;
+  bool rev = false;
+  if constexpr (sizeof(R) == 4) {
+    // the tet's parity from its anchored vertices, each operation rounded
+    // on its own so that every kernel decides alike
+    const V3<float> x0 = pv_pos(tv[0]);
+    const float det = winding_rn(sub_rn(pv_pos(tv[2]), x0), sub_rn(pv_pos(tv[3]), x0), sub_rn(pv_pos(tv[1]), x0));
+    rev = (((kSectionCw >> pos) & 1u) != 0u) != (det < 0.f);
+  }
   int ea[4], eb[4], n;
   if (np == 1 || np == 3) {
     const int single = np == 1 ? __ffs(pos) - 1 : __ffs(~pos & 0xF) - 1;
@@ -158,16 +186,17 @@ __device__ __forceinline__ int tet_section(const PV<R, ND> tv[4], const S s[4], 
       }
       const PV<R, ND> va = sel4(tv, a), vb = sel4(tv, b);
       const R sa = (R)s_a, sb = (R)s_b;
-      out[i] = pv_lerp(va, vb, sa / (sa - sb));
+      PV<R, ND>& o = out[rev && i > 0 ? n - i : i];
+      o = pv_lerp(va, vb, sa / (sa - sb));
       if (sizeof(S) == 8 && sizeof(R) == 4) {
         // FP64 section values: the pressure there in FP64 too.  The tet's
         // vertex pressures are of the order of E while a contact near first
         // touch sees pressures thousands of times smaller; interpolated in
         // FP32 those would keep only a few digits.
         const double ta = (double)s_a / ((double)s_a - (double)s_b);
-        out[i].p = (R)((double)va.p + ta * ((double)vb.p - (double)va.p));
+        o.p = (R)((double)va.p + ta * ((double)vb.p - (double)va.p));
       }
-      out[i].lab = c | (d << 4);
+      o.lab = c | (d << 4);
     }
   }
   return n;
@@ -299,10 +328,10 @@ __device__ __forceinline__ int clip_pos(PV<float, 0>* p, int n, int j, const flo
 // which the section value grows: the contact plane's normal), as the
 // reference's contact polygons are wound: when the fan area vector from the
 // first vertex points against up, the order is reversed (first vertex
-// kept).  Clipping keeps a winding, so this is applied once per polygon, to
-// the FP32 result or to the FP64 pass's.  Each product and sum is rounded on
-// its own, so every kernel that builds the polygon decides the same way on
-// a sliver whose area is near zero.
+// kept).  Applied to the FP64 fallbacks' polygons (the FP32 section is
+// wound by tet_section).  Each product and sum is rounded on its own, so
+// every kernel that builds the polygon decides the same way on a sliver
+// whose area is near zero.
 template <int ND>
 __device__ __forceinline__ void orient_ccw(PV<float, ND>* p, int nv, V3<float> up) {
   if (nv < 3) return;

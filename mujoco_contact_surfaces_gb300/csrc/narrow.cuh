@@ -1163,6 +1163,7 @@ __global__ void __launch_bounds__(128, 5) narrow_sr_kernel(StepArgs a) {
         if (dc.unc) {
           bool near;
           nv = sr_fp64(a, T, tet_idx, anc, poly, near, gint);
+          orient_ccw(poly, nv, n);
           flags = near ? 1 : 0;
         } else if (nv >= 3) {
           gint = dot(t.g, n);
@@ -1173,7 +1174,6 @@ __global__ void __launch_bounds__(128, 5) narrow_sr_kernel(StepArgs a) {
           }
         }
         if (nv < 3) break;
-        orient_ccw(poly, nv, n);
         ac.n_poly += 1;
         ac.n_near += flags;
         orig_a = TS.orig;
@@ -1290,6 +1290,7 @@ __device__ __forceinline__ void sr_keep_round(const StepArgs& a, SrKeepWarpSmem&
     if (dc.unc) {
       bool near;
       nv = sr_fp64(a, T, tet_idx, anc, poly, near, gint);
+      orient_ccw(poly, nv, n);
       flags = near ? 1 : 0;
     } else if (nv >= 3) {
       gint = dot(t.g, n);
@@ -1300,7 +1301,6 @@ __device__ __forceinline__ void sr_keep_round(const StepArgs& a, SrKeepWarpSmem&
       }
     }
     if (nv < 3) break;
-    orient_ccw(poly, nv, n);
     orig_a = a.tet_orig[tet_idx];
     orig_b = T.orig;
     have = true;
@@ -1599,13 +1599,13 @@ __global__ void __launch_bounds__(128, 4) narrow_hs_kernel(StepArgs a) {
       if (dc.unc) {
         bool near;
         nv = hs_fp64(a, F, tet_idx, s, anc, poly, near, gint);
+        orient_ccw(poly, nv, n);
         flags = near ? 1 : 0;
       } else if (nv >= 3) {
         gint = dot(t.g, n);
         if (fabsf(gint) <= 1e-5f * t.gl) gint = grad_along64(a, tet_idx, n64[0], n64[1], n64[2]);
       }
       if (nv >= 3) {
-        orient_ccw(poly, nv, n);
         ac.n_poly += 1;
         ac.n_near += flags;
         orig_a = TS.orig;
@@ -1801,9 +1801,9 @@ __device__ __forceinline__ int ss_element_pair(const StepArgs& a, const FrameDev
   if (dc.unc || (nv >= 3 && (fabsf(gM) <= 1e-5f * t.gl || fabsf(gN) <= 1e-5f * B.gl))) {
     bool near;
     nv = ss_fp64(a, F, ta_idx, tb_idx, s, dc.unc, anc, poly, near, nrm, gM, gN, nv);
+    if (dc.unc) orient_ccw(poly, nv, nrm);
     flags = near ? 1 : 0;
   }
-  orient_ccw(poly, nv, nrm);
   return nv;
 }
 

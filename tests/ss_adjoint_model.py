@@ -77,8 +77,10 @@ def tet_section(X, s):
 
 def orient_ccw(poly, up):
     """The finished polygon wound counter-clockwise about up (the direction in
-    which the section value grows), first vertex kept, as the device's
-    orient_ccw."""
+    which the section value grows), first vertex kept: the device's polygons
+    wind that way (it winds the section before clipping, which keeps the
+    winding, so its first vertex may differ; the reverse does not depend on
+    it)."""
     x = [v for v, _ in poly]
     w = sum(np.cross(x[i - 1] - x[0], x[i] - x[0]) @ up for i in range(2, len(x)))
     return [poly[0]] + poly[1:][::-1] if w < 0 else poly
