@@ -689,51 +689,46 @@ __device__ __forceinline__ int rec_items_end(const StepArgs& a) {
   return min(a.unit_off[a.type_unit_begin[2]], total);
 }
 
-__global__ void poly_count_kernel(StepArgs a) {
-  if (!rec_ok(a)) return;
-  const int end = rec_items_end(a);
-  if ((int)(blockIdx.x * blockDim.x) >= end) {
-    if (threadIdx.x == 0) a.poly_block_sum[blockIdx.x] = 0;
-    return;
-  }
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int v = i < end ? a.item_out[i].n_poly : 0;
-  __shared__ int tot;
-  block_excl_scan(v, &tot);
-  if (threadIdx.x == 0) a.poly_block_sum[blockIdx.x] = tot;
-}
+// Items per thread of the slot scan (a tile is kBpBlock x kSlotItems items).
+constexpr int kSlotItems = 4;
 
-__global__ void poly_scan_kernel(StepArgs a) {
+// Each item's first slot in one pass: a block per tile of kBpBlock x
+// kSlotItems items (tiles taken in order from a counter) scans its items'
+// polygon counts and adds the tiles before it (decoupled look-back,
+// tile_lookback).  Tiles past the last record-keeping item return at once
+// (no tile that is needed waits on them); the tile holding that item gives
+// the items from rec_items_end on (soft-soft, no records) and the end
+// sentinel the grand total.
+__global__ void poly_slots_kernel(StepArgs a) {
   if (!rec_ok(a)) return;
-  __shared__ int carry;
-  __shared__ int tot;
-  if (threadIdx.x == 0) carry = 0;
+  __shared__ int tile_s, excl_s, tot;
+  if (threadIdx.x == 0) tile_s = atomicAdd(a.tile_ctr + 1, 1);
   __syncthreads();
-  for (int base = 0; base < a.n_item_blocks; base += blockDim.x) {
-    const int i = base + threadIdx.x;
-    const int v = i < a.n_item_blocks ? a.poly_block_sum[i] : 0;
-    const int ex = block_excl_scan(v, &tot);
-    if (i < a.n_item_blocks) a.poly_block_sum[i] = ex + carry;
-    __syncthreads();
-    if (threadIdx.x == 0) carry += tot;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    // items from rec_items_end on (soft-soft) start at the total
-    const int total = *a.item_total, end = rec_items_end(a);
-    for (int i = end; i <= total; ++i) a.item_poly_off[i] = carry;
-  }
-}
-
-__global__ void poly_emit_kernel(StepArgs a) {
-  if (!rec_ok(a)) return;
+  const int tile = tile_s;
   const int end = rec_items_end(a);
-  if ((int)(blockIdx.x * blockDim.x) >= end) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int v = i < end ? a.item_out[i].n_poly : 0;
-  __shared__ int tot;
-  const int ex = block_excl_scan(v, &tot) + a.poly_block_sum[blockIdx.x];
-  if (i < end) a.item_poly_off[i] = ex;
+  constexpr int kTile = kBpBlock * kSlotItems;
+  const int last = end > 0 ? (end - 1) / kTile : 0;
+  if (tile > last) return;
+  const int i0 = tile * kTile + threadIdx.x * kSlotItems;
+  int v[kSlotItems], sum = 0;
+#pragma unroll
+  for (int j = 0; j < kSlotItems; ++j) {
+    v[j] = i0 + j < end ? a.item_out[i0 + j].n_poly : 0;
+    sum += v[j];
+  }
+  int ex = block_excl_scan(sum, &tot);
+  if (threadIdx.x == 0) excl_s = tile_lookback(a.poly_tiles, tile, tot, a.status);
+  __syncthreads();
+  ex += excl_s;
+#pragma unroll
+  for (int j = 0; j < kSlotItems; ++j) {
+    if (i0 + j < end) a.item_poly_off[i0 + j] = ex;
+    ex += v[j];
+  }
+  if (tile == last) {
+    const int total = *a.item_total, grand = excl_s + tot;
+    for (int k = end + threadIdx.x; k <= total; k += blockDim.x) a.item_poly_off[k] = grand;
+  }
 }
 
 // ---- record kernels: a group of G lanes per kept polygon ------------------

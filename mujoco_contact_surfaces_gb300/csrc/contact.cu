@@ -1,16 +1,19 @@
 // contact.cu — the per-step device pipeline of the hydroelastic contact path.
 //
-//   frames_kernel     pair setup: relative transforms (FP64), velocity field,
-//                     sensor frames (the pose/velocity fetches of
-//                     passiveCallback, mujoco_contact_surfaces_plugin.cpp:435-451)
-//   bp_count_kernel   cluster-level broadphase over the LBVH, counts
-//   bp_scan_kernel    exclusive scan of the per-block counts
-//   bp_emit_kernel    block prefix-scan compaction of work items
-//   narrow_kernel     per item: element tests, clipping, quadrature
-//                     (P:320-409), Hunt-Crossley + friction,
-//                     taxel binning (flat_tactile_sensor.cpp:262-402)
-//   reduce_kernel     deterministic FP64 per-pair wrench
-//   taxel_kernel      per-cell sums of the binned samples
+//   step_begin_kernel  counters and scan tiles zeroed; pair setup: relative
+//                      transforms (FP64), velocity field, sensor frames (the
+//                      pose/velocity fetches of passiveCallback,
+//                      mujoco_contact_surfaces_plugin.cpp:435-451); the last
+//                      step's touched samples cleared
+//   bp_kernel          cluster-level broadphase over the LBVH and the
+//                      compaction of its work items in one pass (decoupled
+//                      look-back scan)
+//   narrow kernels     per item: element tests, clipping, quadrature
+//                      (P:320-409), Hunt-Crossley + friction,
+//                      taxel binning (flat_tactile_sensor.cpp:262-402), or the
+//                      polygons kept for rec_forward_kernel and the adjoint
+//   reduce_kernel      deterministic FP64 per-pair wrench
+//   taxel_kernel       per-cell sums of the binned samples
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -163,14 +166,21 @@ __device__ __forceinline__ void clear_box(const StepArgs& a, int sid) {
   if (threadIdx.x == 0) a.sens_box[sid] = make_int4(0x7fffffff, -1, 0x7fffffff, -1);
 }
 
-// The step's first kernel: the step counters zeroed (block 0), the pair
-// frames (a thread per pair in the first n_frame_blocks blocks) and, in the
+// The step's first kernel: the step counters and the scans' tile states
+// zeroed, the pair frames (a thread per pair in the first n_frame_blocks
+// blocks) and, in the
 // blocks after them, one block per flat sensor clearing the last step's
 // touched samples.  The three are independent.
 __global__ void step_begin_kernel(StepArgs a, int n_frame_blocks) {
   if ((int)blockIdx.x < n_frame_blocks) {
     if (blockIdx.x == 0 && a.reset_words && threadIdx.x < kResetWords) a.reset_words[threadIdx.x] = 0;
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    // the single-pass scans' tile states
+    const int g = blockIdx.x * blockDim.x + threadIdx.x, stride = n_frame_blocks * blockDim.x;
+    if (a.bp_tiles)
+      for (int i = g; i < a.n_bp_blocks; i += stride) a.bp_tiles[i] = 0;
+    if (a.poly_tiles)
+      for (int i = g; i < a.n_item_blocks; i += stride) a.poly_tiles[i] = 0;
+    const int p = g;
     if (p < a.n_pair) pair_frame(a, p);
   } else {
     clear_box(a, blockIdx.x - n_frame_blocks);
@@ -285,88 +295,103 @@ __device__ __forceinline__ int lane_root(int L, int lane) {
 
 constexpr int kBpUnits = kBpBlock / 32;   // units per broadphase block (a warp each)
 
-__global__ void bp_count_kernel(StepArgs a) {
+// ---- single-pass prefix scans (decoupled look-back) ------------------------
+// A block takes the next tile from an atomic counter, so every tile it waits
+// on belongs to a block that started before it and is running; each tile
+// publishes its aggregate, then its inclusive prefix, as one 64-bit word
+// (state in the top two bits).  A wait is bounded: past the bound the
+// status word gets bit 32 and the host reports the step as failed.
+constexpr unsigned long long kTileAggregate = 1ull << 62;
+constexpr unsigned long long kTileInclusive = 2ull << 62;
+constexpr unsigned long long kTileValue = (1ull << 62) - 1;
+constexpr int kTileWaitRounds = 1 << 22;   // about 0.3 s of 64 ns sleeps
+constexpr int kStatusScanWait = 32;
+
+// The exclusive prefix of tile t given its aggregate (one thread calls it).
+__device__ __forceinline__ int tile_lookback(unsigned long long* st, int t, int agg, int* status) {
+  if (t == 0) {
+    atomicExch(st, kTileInclusive | (unsigned long long)agg);
+    return 0;
+  }
+  atomicExch(st + t, kTileAggregate | (unsigned long long)agg);
+  const volatile unsigned long long* vs = st;
+  unsigned long long excl = 0;
+  for (int k = t - 1; k >= 0; --k) {
+    unsigned long long v = vs[k];
+    for (int w = 0; v == 0; ++w) {
+      if (w == kTileWaitRounds) {
+        atomicOr(status, kStatusScanWait);
+        return 0;
+      }
+      __nanosleep(64);
+      v = vs[k];
+    }
+    excl += v & kTileValue;
+    if ((v >> 62) == 2) break;
+  }
+  atomicExch(st + t, kTileInclusive | (excl + (unsigned long long)agg));
+  return (int)excl;
+}
+
+// Broadphase in one pass: a warp per (pair, other cluster) unit walks the
+// soft tree with the cluster's box (or the plane) and counts the leaves that
+// pass; the block's units get their item offsets from the tile scan; the
+// walk is repeated to write the items (pair, soft leaf, other cluster) in
+// pre-order.  The last tile writes the item total (clamped to the capacity;
+// an overflow sets status bit 1 and leaves the full total in
+// unit_off[n_units]).
+__global__ void bp_kernel(StepArgs a) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int u = blockIdx.x * kBpUnits + wid;
-  int cnt = 0;
+  __shared__ int tile_s, excl_s;
+  __shared__ int ucnt[kBpUnits];
+  if (threadIdx.x == 0) tile_s = atomicAdd(a.tile_ctr, 1);
+  __syncthreads();
+  const int tile = tile_s;
+  const int u = tile * kBpUnits + wid;
+  int p = 0, r = 0, cnt = 0, cl = 0, ncl = 0;
+  QueryBox q;
+  const float4* nd = nullptr;
+  const PairDev* P = nullptr;
   if (u < a.n_units) {
-    const int p = a.unit_pair[u];
-    const PairDev& P = a.pairs[p];
+    p = a.unit_pair[u];
+    P = &a.pairs[p];
     const FrameDev& F = a.frames[p];
     if (F.valid) {
-      const QueryBox q = make_query(a, P, F, a.unit_cl[u]);
-      const float4* nd = a.nodes + 2 * (size_t)P.s_node_off;
-      const int ncl = (P.s_n_elem + kCluster - 1) / kCluster;
-      const int r = lane_root(P.s_leaves, lane);
-      if (r) walk_sub(nd, P.s_leaves, ncl, q, r, [&](int) { ++cnt; });
+      cl = a.unit_cl[u];
+      q = make_query(a, *P, F, cl);
+      nd = a.nodes + 2 * (size_t)P->s_node_off;
+      ncl = (P->s_n_elem + kCluster - 1) / kCluster;
+      r = lane_root(P->s_leaves, lane);
+      if (r) walk_sub(nd, P->s_leaves, ncl, q, r, [&](int) { ++cnt; });
     }
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-  __shared__ int wsum[kBpUnits];
-  if (lane == 0) {
-    if (u < a.n_units) a.unit_count[u] = cnt;
-    wsum[wid] = u < a.n_units ? cnt : 0;
-  }
+  const int lane_first = warp_incl_scan(cnt) - cnt;   // this lane's leaves follow the lanes' before it
+  const int total_u = __shfl_sync(0xffffffffu, lane_first + cnt, 31);
+  if (lane == 0) ucnt[wid] = u < a.n_units ? total_u : 0;
   __syncthreads();
   if (threadIdx.x == 0) {
-    int t = 0;
-    for (int w = 0; w < kBpUnits; ++w) t += wsum[w];
-    a.block_sum[blockIdx.x] = t;
-  }
-}
-
-__global__ void bp_scan_kernel(StepArgs a) {
-  __shared__ int carry;
-  __shared__ int tot;
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
-  for (int base = 0; base < a.n_bp_blocks; base += blockDim.x) {
-    int i = base + threadIdx.x;
-    int v = (i < a.n_bp_blocks && a.n_units > 0) ? a.block_sum[i] : 0;
-    int ex = block_excl_scan(v, &tot);
-    if (i < a.n_bp_blocks) a.block_sum[i] = ex + carry;
-    __syncthreads();
-    if (threadIdx.x == 0) carry += tot;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    int total = carry;
-    if (total > a.item_cap) {
-      atomicOr(a.status, 1);
-      total = a.item_cap;
+    int agg = 0;
+    for (int w = 0; w < kBpUnits; ++w) agg += ucnt[w];
+    excl_s = tile_lookback(a.bp_tiles, tile, agg, a.status);
+    if (tile == (int)gridDim.x - 1) {
+      int total = excl_s + agg;
+      a.unit_off[a.n_units] = total;
+      if (total > a.item_cap) {
+        atomicOr(a.status, 1);
+        total = a.item_cap;
+      }
+      *a.item_total = total;
     }
-    *a.item_total = total;
-    a.item_next[0] = a.item_next[1] = a.item_next[2] = 0;
-    a.unit_off[a.n_units] = carry;
   }
-}
-
-__global__ void bp_emit_kernel(StepArgs a) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int u = blockIdx.x * kBpUnits + wid;
-  __shared__ int ucnt[kBpUnits];
-  if (lane == 0) ucnt[wid] = u < a.n_units ? a.unit_count[u] : 0;
   __syncthreads();
   if (u >= a.n_units) return;
-  int off = a.block_sum[blockIdx.x];
+  int off = excl_s;
   for (int w = 0; w < wid; ++w) off += ucnt[w];
   if (lane == 0) a.unit_off[u] = off;
   if (!ucnt[wid]) return;
-  const int p = a.unit_pair[u];
-  const PairDev& P = a.pairs[p];
-  const FrameDev& F = a.frames[p];
-  const int cl = a.unit_cl[u];
-  const QueryBox q = make_query(a, P, F, cl);
-  const float4* nd = a.nodes + 2 * (size_t)P.s_node_off;
-  const int ncl = (P.s_n_elem + kCluster - 1) / kCluster;
-  const int r = lane_root(P.s_leaves, lane);
-  // this lane's leaves follow those of the lanes before it
-  int cnt = 0;
-  if (r) walk_sub(nd, P.s_leaves, ncl, q, r, [&](int) { ++cnt; });
-  int k = off + warp_incl_scan(cnt) - cnt;
+  int k = off + lane_first;
   if (r)
-    walk_sub(nd, P.s_leaves, ncl, q, r, [&](int leaf) {
+    walk_sub(nd, P->s_leaves, ncl, q, r, [&](int leaf) {
       if (k < a.item_cap) a.items[k] = make_int4(p, leaf, cl, 0);
       ++k;
     });
@@ -601,13 +626,8 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
     step_begin_kernel<<<nfb + nsb, 128, 0, s>>>(a, nfb); ++n;
   }
   if (ev) cudaEventRecordWithFlags(ev[1], s, cudaEventRecordExternal);
-  if (a.n_units > 0) {
-    bp_count_kernel<<<a.n_bp_blocks, kBpBlock, 0, s>>>(a); ++n;
-  }
-  bp_scan_kernel<<<1, kBpBlock, 0, s>>>(a); ++n;
-  if (a.n_units > 0) {
-    bp_emit_kernel<<<a.n_bp_blocks, kBpBlock, 0, s>>>(a); ++n;
-  }
+  // (also with no units: the last tile writes the item total)
+  bp_kernel<<<a.n_bp_blocks > 0 ? a.n_bp_blocks : 1, kBpBlock, 0, s>>>(a); ++n;
   if (ev) cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal);
   if (a.type_unit_end[0] > a.type_unit_begin[0]) {
     const bool diag = (a.debug & 1) || a.want_polys;
@@ -637,9 +657,7 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   if (ev) cudaEventRecordWithFlags(ev[6], s, cudaEventRecordExternal);
   if (a.recs && a.type_unit_end[1] > a.type_unit_begin[0]) {
     // kept polygons: pair-ordered slots, then forces and rays per polygon
-    poly_count_kernel<<<a.n_item_blocks, kBpBlock, 0, s>>>(a); ++n;
-    poly_scan_kernel<<<1, kBpBlock, 0, s>>>(a); ++n;
-    poly_emit_kernel<<<a.n_item_blocks, kBpBlock, 0, s>>>(a); ++n;
+    poly_slots_kernel<<<(a.n_item_blocks + kSlotItems - 1) / kSlotItems, kBpBlock, 0, s>>>(a); ++n;
     if (a.repr == 1) rec_forward_kernel<1><<<a.rec_fwd_grid, 128, 0, s>>>(a);
     else rec_forward_kernel<0><<<a.rec_fwd_grid, 128, 0, s>>>(a);
     ++n;

@@ -121,8 +121,10 @@ constexpr int kCntPoly = 3;    // polygon records written
 constexpr int kCntNext = 4;    // three work counters, one per query type
 constexpr int kCntRec = 7;     // adjoint records kept (may exceed the capacity)
 constexpr int kCntAdjSkip = 8; // two words: adjoint vertices left out, smallest |det| (debug)
+constexpr int kCntTile = 10;   // two words: the next tile of the broadphase and slot scans
 constexpr int kCntWords = 16;
-static_assert(kCntRec < hc::kResetWords, "the step's first kernel zeroes the counters up to kCntRec");
+constexpr int kStatusScanWaitBit = 32;   // status: a look-back wait ran out (contact.cu)
+static_assert(kCntTile + 1 < hc::kResetWords, "the step's first kernel zeroes the counters up to kCntTile + 1");
 
 int next_pow2(int n) {
   int p = 1;
@@ -160,7 +162,8 @@ struct hc_context {
   std::vector<int> g1_h, g2_h;
   DevBuf<hc::PairDev> pairs;
   DevBuf<hc::FrameDev> frames;
-  DevBuf<int> unit_pair, unit_cl, unit_count, unit_off, block_sum;
+  DevBuf<int> unit_pair, unit_cl, unit_off;
+  DevBuf<unsigned long long> bp_tiles;   // the broadphase scan's look-back state, one per block
   int n_units = 0, n_bp_blocks = 0;
   DevBuf<int4> items;
   DevBuf<hc::ItemOut> item_out;
@@ -248,7 +251,8 @@ struct hc_context {
   bool tsens_ai = false;
   int n_taxel_total = 0;
   DevBuf<float> rec_grad;
-  DevBuf<int> item_poly_off, poly_block_sum;
+  DevBuf<int> item_poly_off;
+  DevBuf<unsigned long long> poly_tiles;   // the slot scan's look-back state, one per kBpBlock items
   int rec_cap = 0;
   bool recs_step = false;  // the last step kept its polygons
 };
@@ -479,13 +483,13 @@ int initial_rec_cap(const hc_context* c) {
                                   : std::max(1 << 15, 4 * c->item_cap);
 }
 
-// Per-item record offsets: item_cap + 1 ints and one block sum per kBpBlock items.
+// Per-item record offsets: item_cap + 1 ints and one scan tile state per kBpBlock items.
 hc_status ensure_rec_offsets(hc_context* c) {
   if (c->rec_cap == 0) return HC_OK;
   const size_t blocks = (size_t)std::max(1, (c->item_cap + hc::kBpBlock - 1) / hc::kBpBlock);
-  if ((size_t)c->item_cap + 1 <= c->item_poly_off.n && blocks <= c->poly_block_sum.n) return HC_OK;
+  if ((size_t)c->item_cap + 1 <= c->item_poly_off.n && blocks <= c->poly_tiles.n) return HC_OK;
   HC_CUDA(c->item_poly_off.reserve((size_t)c->item_cap + 1));
-  HC_CUDA(c->poly_block_sum.reserve(blocks));
+  HC_CUDA(c->poly_tiles.reserve(blocks));
   invalidate_graph(c);
   return HC_OK;
 }
@@ -626,13 +630,13 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
   a.unit_pair = c->unit_pair.p;
   a.unit_cl = c->unit_cl.p;
   a.n_units = c->n_units;
-  a.unit_count = c->unit_count.p;
   a.unit_off = c->unit_off.p;
-  a.block_sum = c->block_sum.p;
+  a.bp_tiles = c->bp_tiles.p;
   a.n_bp_blocks = c->n_bp_blocks;
   a.items = c->items.p;
   a.item_cap = c->item_cap;
-  a.reset_words = c->counters.p;   // kResetWords (8) words: total .. rec
+  a.reset_words = c->counters.p;   // kResetWords (12) words: total .. the scans' tile counters
+  a.tile_ctr = c->counters.p + kCntTile;
   a.item_total = c->counters.p + kCntTotal;
   a.status = c->counters.p + kCntStatus;
   a.cand_count = c->counters.p + kCntCand;
@@ -684,7 +688,7 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
     a.slot_press = c->slot_press.p;
     a.rec_perm = c->rec_perm.p;
     a.item_poly_off = c->item_poly_off.p;
-    a.poly_block_sum = c->poly_block_sum.p;
+    a.poly_tiles = c->poly_tiles.p;
     a.n_item_blocks = std::max(1, (c->item_cap + hc::kBpBlock - 1) / hc::kBpBlock);
     a.tsens = c->tsens.p;
     a.n_tsens = (int)c->tsens_h.size();
@@ -762,6 +766,8 @@ hc_status finish_step(hc_context* c) {
     int cnt[8];
     HC_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
     HC_CUDA(cudaStreamSynchronize(c->stream));
+    if (cnt[kCntStatus] & kStatusScanWaitBit)
+      return fail(HC_ERR_CUDA, "a single-pass scan waited past its bound for an earlier tile");
     if (!(cnt[kCntStatus] & 9)) {
       c->step_checked = true;
       return HC_OK;
@@ -1187,9 +1193,8 @@ hc_status hc_set_pairs(hc_context* c, int n_pair, const int* g1, const int* g2, 
   c->n_bp_blocks = std::max(1, (c->n_units + hc::kBpBlock / 32 - 1) / (hc::kBpBlock / 32));
   HC_CUDA(c->unit_pair.upload(upair, s));
   HC_CUDA(c->unit_cl.upload(ucl, s));
-  HC_CUDA(c->unit_count.reserve(std::max(1, c->n_units)));
   HC_CUDA(c->unit_off.reserve(c->n_units + 1));
-  HC_CUDA(c->block_sum.reserve(c->n_bp_blocks));
+  HC_CUDA(c->bp_tiles.reserve(c->n_bp_blocks));
   int want = c->cfg.item_capacity > 0 ? (int)c->cfg.item_capacity : std::max(1 << 16, 64 * n_pair);
   if (hc_status st = ensure_items(c, want)) return st;
   if (keeps_polygons(c))
@@ -1875,7 +1880,7 @@ static hc_status adjoint_launch(hc_context* c, const double* d_dw, const float* 
     a.rec_cap = c->rec_cap;
     a.rec_out = c->rec_out.p;
     a.item_poly_off = c->item_poly_off.p;
-    a.poly_block_sum = c->poly_block_sum.p;
+    a.poly_tiles = c->poly_tiles.p;
     a.rec_grad = c->rec_grad.p;
   } else {
     a.recs = nullptr;
@@ -2039,6 +2044,8 @@ hc_status hc_step_adjoint(hc_context* c, int n_geom, const double* xpos, const d
     int cnt[8];
     HC_CUDA(cudaMemcpyAsync(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
     HC_CUDA(cudaStreamSynchronize(c->stream));
+    if (cnt[kCntStatus] & kStatusScanWaitBit)
+      return fail(HC_ERR_CUDA, "a single-pass scan waited past its bound for an earlier tile");
     if (!(cnt[kCntStatus] & 9)) {
       c->step_checked = true;
       return HC_OK;

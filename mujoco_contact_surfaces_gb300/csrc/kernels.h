@@ -8,7 +8,7 @@
 namespace hc {
 
 // Step counters the step's first kernel zeroes (StepArgs::reset_words).
-constexpr int kResetWords = 8;
+constexpr int kResetWords = 12;
 
 struct StepArgs {
   // per-step inputs (device)
@@ -33,9 +33,8 @@ struct StepArgs {
   const int* unit_pair;
   const int* unit_cl;
   int n_units;
-  int* unit_count;
   int* unit_off;      // n_units + 1
-  int* block_sum;     // one per broadphase block
+  unsigned long long* bp_tiles;   // per broadphase block: its decoupled look-back state
   int n_bp_blocks;
   int4* items;
   int item_cap;
@@ -99,7 +98,8 @@ struct StepArgs {
   int fused;                 // fused step: an overflow re-runs the whole step, so the
                              // recomputing adjoint fallbacks are left out
   int* item_poly_off;        // per item: first record of the item in pair order (item_cap + 1)
-  int* poly_block_sum;       // one per kBpBlock items
+  unsigned long long* poly_tiles; // per kBpBlock items: the polygon-slot scan's look-back state
+  int* tile_ctr;             // [0] broadphase, [1] polygon slots: the next tile a block takes
   int n_item_blocks;         // item_cap / kBpBlock rounded up
   float* rec_grad;           // per record in pair order: 13 gradient terms (stride 16)
   RecOut* rec_out;           // per record in pair order: forces (forward)

@@ -63,7 +63,7 @@ struct Carve {
 };
 
 // Word layout of the counter block (the same meaning as hc_step's).
-constexpr int kWTotal = 0, kWStatus = 1, kWCand = 2, kWPoly = 3, kWNext = 4, kWRec = 7, kWords = 8;
+constexpr int kWTotal = 0, kWStatus = 1, kWCand = 2, kWPoly = 3, kWNext = 4, kWRec = 7, kWTile = 8, kWords = 10;
 
 // The wrench part of the per-pair records, to the caller's n_pair x 6 array.
 __global__ void wrench_out_kernel(const hc::PairOut* __restrict__ po, int n_pair, double* __restrict__ w) {
@@ -110,12 +110,12 @@ extern "C" HC_API hc_status hc_step_noalloc(hc_context* ctx, int n_geom, const d
   int* words = cv.take<int>(kWords);
   a.frames = cv.take<hc::FrameDev>(n_pair > 0 ? n_pair : 1);
   a.pair_out = cv.take<hc::PairOut>(n_pair > 0 ? n_pair : 1);
-  a.unit_count = cv.take<int>(a.n_units > 0 ? a.n_units : 1);
   a.unit_off = cv.take<int>((size_t)a.n_units + 1);
-  a.block_sum = cv.take<int>(a.n_bp_blocks > 0 ? a.n_bp_blocks : 1);
+  a.bp_tiles = cv.take<unsigned long long>(a.n_bp_blocks > 0 ? a.n_bp_blocks : 1);   // zeroed by the first kernel
+  a.poly_tiles = nullptr;
   a.samples = cv.take<unsigned long long>(v.n_samples > 0 ? v.n_samples : 1);
   a.sens_box = nullptr;   // the whole sample array is cleared below and read
-  if (!words || !a.frames || !a.pair_out || !a.unit_count || !a.unit_off || !a.block_sum || !a.samples) {
+  if (!words || !a.frames || !a.pair_out || !a.unit_off || !a.bp_tiles || !a.samples) {
     char msg[240];
     snprintf(msg, sizeof(msg),
              "no-alloc scratch (%zu bytes) too small for %d pairs, %d broadphase units and %zu ray samples",
@@ -143,6 +143,7 @@ extern "C" HC_API hc_status hc_step_noalloc(hc_context* ctx, int n_geom, const d
   a.cand_count = words + kWCand;
   a.poly_count = words + kWPoly;
   a.item_next = words + kWNext;
+  a.tile_ctr = words + kWTile;
   // inputs and outputs of the caller
   a.xpos = d_xpos;
   a.xmat = d_xmat;
@@ -179,6 +180,7 @@ extern "C" HC_API hc_status hc_step_noalloc(hc_context* ctx, int n_geom, const d
   if ((e = cudaMemcpyAsync(&needed, a.unit_off + a.n_units, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
     return cuda_fail("cudaMemcpyAsync", e);
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail("cudaStreamSynchronize", e);
+  if (w[kWStatus] & 32) return hc::set_last_error(HC_ERR_CUDA, "a single-pass scan waited past its bound for an earlier tile");
   if (w[kWStatus] & 1) {
     char msg[200];
     snprintf(msg, sizeof(msg), "the step needs %d work items; the no-alloc scratch (%zu bytes) holds %d", needed,
