@@ -37,10 +37,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "contact pairs/s fwd+adjoint, batched vs plain GPU path at 1e-5 rel wrench err"
 
-# DRAM bytes of one narrow_sr_kernel launch (dram__bytes_read.sum +
-# dram__bytes_write.sum) from an ncu capture of this workload at 1024 scenes,
-# scaled by the scenes processed (items and polygons grow in proportion).
-NARROW_SR_DRAM_BYTES_PER_SCENE = (75.16e6 + 44.28e6) / 1024
+# DRAM bytes of one narrow_sr_keep_kernel launch (dram__bytes_read.sum +
+# dram__bytes_write.sum) from an ncu capture of this workload at 1024 scenes
+# (launch shape 6,2), scaled by the scenes processed (items and polygons
+# grow in proportion).
+NARROW_SR_DRAM_BYTES_PER_SCENE = (79.968768e6 + 62.995456e6) / 1024
 
 
 def parse():
@@ -425,7 +426,7 @@ def run_gb300(args):
     # roofline of the kernel that reads the algorithmic element bytes (the
     # soft-rigid narrow phase; the kept-polygon passes read records, which
     # are overhead by the formula)
-    kname, kms, kbytes = "narrow_sr_kernel", narrow_avg, ab["elem"]
+    kname, kms, kbytes = "narrow_sr_keep_kernel", narrow_avg, ab["elem"]
     achieved = kbytes / (kms * 1e-3) / 1e9
     traffic = NARROW_SR_DRAM_BYTES_PER_SCENE * args.scenes
     line = {
