@@ -982,6 +982,38 @@ __device__ int sr_polygon(const TetIn<R>& t, const S s[4], const TriStage& T, V3
   return nv;
 }
 
+// Edge plane j of the staged triangle against the tet (FP32 with margins):
+// -1 when all four vertices are certainly outside (no polygon), 0 when all
+// are certainly inside (the plane clips nothing), 1 when it is active; then
+// c is its double-float value at the anchor vertex (the plane's offset for
+// the clip) and tol the clip margin.
+__device__ __forceinline__ int edge_plane_f(const TetIn<float>& t, const TriStage& T, int j, int anc, float xr,
+                                            float& c, float& tol) {
+  const float tj = 4e-6f * (t.xmax + fabsf(T.eo[j]));
+  bool all_in = true, all_out = true;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float d = T.en[j][0] * t.X[k].x + T.en[j][1] * t.X[k].y + T.en[j][2] * t.X[k].z - T.eo[j];
+    all_in &= d > tj;
+    all_out &= d < -tj;
+  }
+  c = 0.f;
+  tol = 0.f;
+  if (all_out) return -1;
+  if (all_in) return 0;
+  // double-float at the four vertices: the plane's position matters to the
+  // area; the anchor's value is the plane's offset for the clip
+  float dmax = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float d = plane_df(T.en[j], T.enl[j], T.eo[j], T.eol[j], t.X[k].x, t.X[k].y, t.X[k].z);
+    dmax = fmaxf(dmax, fabsf(d));
+    if (k == anc) c = d;
+  }
+  tol = (float)kFiltRel * (dmax + xr);
+  return 1;
+}
+
 // The FP32 soft-rigid polygon: as sr_polygon, with vertices that carry no
 // clip distances.  An active edge plane's distance is its double-float value
 // at the anchor vertex plus the FP32 plane normal times the vertex's offset
@@ -1000,41 +1032,31 @@ __device__ __forceinline__ int sr_polygon_f(const TetIn<float>& t, const float s
   float xr = 0.f;   // the anchored tet's extent
 #pragma unroll
   for (int k = 0; k < 4; ++k) xr = fmaxf(xr, fmaxf(fabsf(tv[k].x), fmaxf(fabsf(tv[k].y), fabsf(tv[k].z))));
-  bool active[3];
-  float tol[3], c[3];
-#pragma unroll
+  // the three edge planes in a loop that is not unrolled (one copy of the
+  // double-float evaluation: the kernel's code, not its arithmetic, limits
+  // it through instruction fetch); the per-plane results in scalars
+  int act_mask = 0;
+  float c0 = 0.f, c1 = 0.f, c2 = 0.f, t0 = 0.f, t1 = 0.f, t2 = 0.f;
+#pragma unroll 1
   for (int j = 0; j < 3; ++j) {
-    const float tj = 4e-6f * (t.xmax + fabsf(T.eo[j]));
-    bool all_in = true, all_out = true;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const float d = T.en[j][0] * t.X[k].x + T.en[j][1] * t.X[k].y + T.en[j][2] * t.X[k].z - T.eo[j];
-      all_in &= d > tj;
-      all_out &= d < -tj;
-    }
-    if (all_out) return 0;
-    active[j] = !all_in;
-    tol[j] = 0.f;
-    c[j] = 0.f;
-    if (active[j]) {
-      // double-float at the four vertices: the plane's position matters to
-      // the area; the anchor's value is the plane's offset for the clip
-      float dmax = 0.f;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const float d = plane_df(T.en[j], T.enl[j], T.eo[j], T.eol[j], t.X[k].x, t.X[k].y, t.X[k].z);
-        dmax = fmaxf(dmax, fabsf(d));
-        if (k == anc) c[j] = d;
-      }
-      tol[j] = (float)kFiltRel * (dmax + xr);
+    float cj, tolj;
+    const int r = edge_plane_f(t, T, j, anc, xr, cj, tolj);
+    if (r < 0) return 0;
+    if (r > 0) {
+      act_mask |= 1 << j;
+      if (j == 0) { c0 = cj; t0 = tolj; }
+      else if (j == 1) { c1 = cj; t1 = tolj; }
+      else { c2 = cj; t2 = tolj; }
     }
   }
   int nv = tet_section(tv, s, dc, out);
   if (nv == 0) return 0;
-#pragma unroll
+#pragma unroll 1
   for (int j = 0; j < 3; ++j) {
-    if (!active[j]) continue;
-    nv = clip_pos(out, nv, j, T.en[j], c[j], tol[j], dc);
+    if (!((act_mask >> j) & 1)) continue;
+    const float cj = j == 0 ? c0 : (j == 1 ? c1 : c2);
+    const float tj = j == 0 ? t0 : (j == 1 ? t1 : t2);
+    nv = clip_pos(out, nv, j, T.en[j], cj, tj, dc);
     if (nv == 0) return 0;
   }
   return nv;
