@@ -172,7 +172,9 @@ __device__ __forceinline__ int tet_section(const PV<R, ND> tv[4], const S s[4], 
     ea[3] = b; eb[3] = c;
     n = 4;
   }
-#pragma unroll
+  // (loops here are not unrolled: the narrow kernels inline this code in
+  // several places and are bound by instruction fetch, not arithmetic)
+#pragma unroll 1
   for (int i = 0; i < 4; ++i) {
     if (i < n) {
       int a = ea[i], b = eb[i];
@@ -299,6 +301,7 @@ __device__ __forceinline__ int clip_pos(PV<float, 0>* p, int n, int j, const flo
   bool all_in = true;
   int changes = 0;
   bool prev = pos_dist(p[n - 1], e, c) >= 0.f;
+#pragma unroll 1
   for (int i = 0; i < n; ++i) {
     const float d = pos_dist(p[i], e, c);
     check(dc, d, tol);
@@ -314,6 +317,7 @@ __device__ __forceinline__ int clip_pos(PV<float, 0>* p, int n, int j, const flo
   PV<float, 0> cur = first;
   float d_cur = d_first;
   int m = 0;
+#pragma unroll 1
   for (int i = 0; i < n; ++i) {
     const PV<float, 0> nxt = i + 1 < n ? p[i + 1] : first;
     const float d_nxt = i + 1 < n ? pos_dist(nxt, e, c) : d_first;

@@ -723,6 +723,7 @@ __device__ __forceinline__ void write_record(const StepArgs& a, int r, int item,
   a.rec_key[r] = make_int2(item, seq);
   AdjPoly& R = a.recs[r];
   int l0 = 0, l1 = 0;
+#pragma unroll 1
   for (int i = 0; i < kMaxPolyV; ++i) {
     const bool in = i < nv;
     *reinterpret_cast<float4*>(R.v[i]) =
@@ -1004,9 +1005,10 @@ __device__ __forceinline__ int edge_plane_f(const TetIn<float>& t, const TriStag
   // double-float at the four vertices: the plane's position matters to the
   // area; the anchor's value is the plane's offset for the clip
   float dmax = 0.f;
-#pragma unroll
+#pragma unroll 1   // one copy of the evaluation (code size; sel4 keeps t.X in registers)
   for (int k = 0; k < 4; ++k) {
-    const float d = plane_df(T.en[j], T.enl[j], T.eo[j], T.eol[j], t.X[k].x, t.X[k].y, t.X[k].z);
+    const V3<float> x = sel4(t.X, k);
+    const float d = plane_df(T.en[j], T.enl[j], T.eo[j], T.eol[j], x.x, x.y, x.z);
     dmax = fmaxf(dmax, fabsf(d));
     if (k == anc) c = d;
   }
