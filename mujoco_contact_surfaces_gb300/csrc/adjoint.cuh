@@ -1050,6 +1050,19 @@ __device__ __forceinline__ void rec_fwd_one(const StepArgs& a, int r, int dst, b
   if (on) rec_rays<G>(a, R, dst, sub, nullptr);
 }
 
+// The next round's eight records (8 x 288 B: 18 lines of 128 B), one line
+// per lane, and their keys, requested into L1 before this round's work: the
+// record kernels wait on their records' loads more than on arithmetic
+// (adjoint 0.57 -> 0.54 ms; into L2 alone gained a little less).
+__device__ __forceinline__ void prefetch_records(const StepArgs& a, int base, int n, int lane) {
+  if (base >= n) return;
+  const int nrec = min(8, n - base);
+  const char* p = reinterpret_cast<const char*>(a.recs + base);
+  const int lines = (nrec * (int)sizeof(AdjPoly) + 127) / 128;
+  if (lane < lines) asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 128 * lane));
+  if (lane == 31) asm volatile("prefetch.global.L1 [%0];" ::"l"(a.rec_key + base));
+}
+
 // Forward pass over the kept polygons, eight records per warp and round:
 // those of up to 4 vertices in groups of 4 lanes, the rest after them in
 // groups of 8.
@@ -1063,6 +1076,7 @@ __global__ void __launch_bounds__(128, 7) rec_forward_kernel(StepArgs a) {
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
   constexpr int kPer = 32 / kGroupSmall;
   for (int base = warp * kPer; base < n; base += n_warps * kPer) {
+    prefetch_records(a, base + n_warps * kPer, n, lane);
     const int r = base + grp;
     const int dst = rec_slot(a, r, n);
     const int nv = dst >= 0 ? a.recs[r].nv : 0;
@@ -1260,6 +1274,7 @@ __global__ void __launch_bounds__(128, 5) adjoint_rec_kernel(StepArgs a) {
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
   constexpr int kPer = 32 / kGroupSmall;
   for (int base = warp * kPer; base < n; base += n_warps * kPer) {
+    prefetch_records(a, base + n_warps * kPer, n, lane);
     const int r = base + grp;
     const int dst = rec_slot(a, r, n);
     const int nv = dst >= 0 ? a.recs[r].nv : 0;
