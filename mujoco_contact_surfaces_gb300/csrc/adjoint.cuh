@@ -828,6 +828,9 @@ __device__ __forceinline__ bool raster_prepare_group(const StepArgs& a, const Se
                                                      const float* tl, const AdjPoly& R, V3<float> anc,
                                                      V3<float> g_soft, int sub, RasterPoly& rp) {
   const int nv = R.nv;
+  // a group of G lanes holds polygons of at most G vertices: the loops stop
+  // there (the vertices past nv add nothing)
+  constexpr int MV = G < kMaxPolyV ? G : kMaxPolyV;
   const int base = (threadIdx.x & 31) & ~(G - 1);
   const unsigned gm = ((1u << G) - 1u) << base;
   float mx = 0.f, my = 0.f, mz = 0.f, mp = 0.f;
@@ -842,10 +845,10 @@ __device__ __forceinline__ bool raster_prepare_group(const StepArgs& a, const Se
   float lz[kMaxPolyV];
   float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
 #pragma unroll
-  for (int i = 0; i < kMaxPolyV; ++i) {
-    rp.lx[i] = i < G ? __shfl_sync(gm, mx, base + i) : 0.f;
-    rp.ly[i] = i < G ? __shfl_sync(gm, my, base + i) : 0.f;
-    lz[i] = i < G ? __shfl_sync(gm, mz, base + i) : 0.f;
+  for (int i = 0; i < MV; ++i) {
+    rp.lx[i] = __shfl_sync(gm, mx, base + i);
+    rp.ly[i] = __shfl_sync(gm, my, base + i);
+    lz[i] = __shfl_sync(gm, mz, base + i);
     if (i < nv) {
       mnx = fminf(mnx, rp.lx[i]); mxx = fmaxf(mxx, rp.lx[i]);
       mny = fminf(mny, rp.ly[i]); mxy = fmaxf(mxy, rp.ly[i]);
@@ -854,7 +857,7 @@ __device__ __forceinline__ bool raster_prepare_group(const StepArgs& a, const Se
   rp.p0 = __shfl_sync(gm, mp, base);
   float A2 = 0.f;
 #pragma unroll
-  for (int i = 1; i + 1 < kMaxPolyV; ++i)
+  for (int i = 1; i + 1 < MV; ++i)
     if (i + 1 < nv)
       A2 = __fadd_rn(A2, __fsub_rn(__fmul_rn(__fsub_rn(rp.lx[i], rp.lx[0]), __fsub_rn(rp.ly[i + 1], rp.ly[0])),
                                    __fmul_rn(__fsub_rn(rp.ly[i], rp.ly[0]), __fsub_rn(rp.lx[i + 1], rp.lx[0]))));
@@ -863,7 +866,7 @@ __device__ __forceinline__ bool raster_prepare_group(const StepArgs& a, const Se
   const float e1x = __fsub_rn(rp.lx[1], rp.lx[0]), e1y = __fsub_rn(rp.ly[1], rp.ly[0]), e1z = __fsub_rn(lz[1], lz[0]);
   float nx = 0.f, ny = 0.f, nz = 0.f;
 #pragma unroll
-  for (int i = 2; i < kMaxPolyV; ++i) {
+  for (int i = 2; i < MV; ++i) {
     if (i < nv) {
       const float fx = __fsub_rn(rp.lx[i], rp.lx[0]), fy = __fsub_rn(rp.ly[i], rp.ly[0]), fz = __fsub_rn(lz[i], lz[0]);
       nx = __fadd_rn(nx, __fsub_rn(__fmul_rn(e1y, fz), __fmul_rn(e1z, fy)));
@@ -897,10 +900,10 @@ __device__ __forceinline__ bool raster_prepare_group(const StepArgs& a, const Se
   rp.Y0 = max(0, (int)fy0); rp.Y1 = min(S.ny - 1, (int)fy1);
   rp.nv = nv;
 #pragma unroll
-  for (int i = 0; i < kMaxPolyV; ++i) {
+  for (int i = 0; i < MV; ++i) {
     const bool last = i + 1 >= nv;
-    const float nxv = last ? rp.lx[0] : rp.lx[i + 1 < kMaxPolyV ? i + 1 : 0];
-    const float nyv = last ? rp.ly[0] : rp.ly[i + 1 < kMaxPolyV ? i + 1 : 0];
+    const float nxv = last ? rp.lx[0] : rp.lx[i + 1 < MV ? i + 1 : 0];
+    const float nyv = last ? rp.ly[0] : rp.ly[i + 1 < MV ? i + 1 : 0];
     rp.ex[i] = __fsub_rn(nxv, rp.lx[i]);
     rp.ey[i] = __fsub_rn(nyv, rp.ly[i]);
   }
@@ -941,7 +944,8 @@ __device__ __forceinline__ void rec_rays_fwd(const StepArgs& a, const AdjPoly& R
   for (int idx = sub; idx < cnt; idx += G, X += dq, Y += dr) {
     if (Y > rp.Y1) { Y -= nY; ++X; }
     float t, z, pr;
-    if (raster_probe(rp, S, sx[X], sy[Y], t, z, pr)) atomicMin(&smp[(size_t)X * S.ny + Y], key_slot(t, dst, side));
+    if (raster_probe<(G < kMaxPolyV ? G : kMaxPolyV)>(rp, S, sx[X], sy[Y], t, z, pr))
+      atomicMin(&smp[(size_t)X * S.ny + Y], key_slot(t, dst, side));
   }
 }
 

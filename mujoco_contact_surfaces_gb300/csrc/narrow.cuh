@@ -209,10 +209,12 @@ __device__ __forceinline__ float raster_pressure(float lx0, float ly0, float p0,
 // Sample (qx, qy) against a prepared polygon: false when the ray misses the
 // polygon or its hit lies outside 0 < t < 1.5 zs; else t, the hit height z
 // and the pressure there.
+// MV: the most vertices the polygon can have (the loop's bound).
+template <int MV = kMaxPolyV>
 __device__ __forceinline__ bool raster_probe(const RasterPoly& rp, const SensorDev& S, float qx, float qy,
                                              float& t, float& z, float& pr) {
 #pragma unroll
-  for (int i = 0; i < kMaxPolyV; ++i) {
+  for (int i = 0; i < MV; ++i) {
     if (i >= rp.nv) break;
     const float e = __fsub_rn(__fmul_rn(rp.ex[i], __fsub_rn(qy, rp.ly[i])),
                               __fmul_rn(rp.ey[i], __fsub_rn(qx, rp.lx[i])));
