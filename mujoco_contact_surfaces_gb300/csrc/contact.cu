@@ -568,11 +568,14 @@ void launch_tet_props(const float4* tets, float4* props, int n_tets, cudaStream_
 // ---------------------------------------------------------------------------
 cudaError_t init_kernel_attributes() {
   cudaError_t e = cudaSuccess;
-  for (const void* k : {(const void*)narrow_sr_keep_kernel<kSrKeepCtas>, (const void*)narrow_sr_kernel<false, false>,
-                        (const void*)narrow_sr_kernel<true, true>, (const void*)narrow_sr_kernel<false, true>}) {
+  for (const void* k : {(const void*)narrow_sr_kernel<false, false>, (const void*)narrow_sr_kernel<true, true>,
+                        (const void*)narrow_sr_kernel<false, true>}) {
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSrSmemBytes);
     if (e != cudaSuccess) return e;
   }
+  e = cudaFuncSetAttribute((const void*)narrow_sr_keep_kernel<kSrKeepCtas>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)kSrKeepSmemBytes);
+  if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(taxel_sensor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTaxelSmemBytes);
   if (e != cudaSuccess) return e;
   // the taxel sensors' grid-count table (a pure function of the step count)

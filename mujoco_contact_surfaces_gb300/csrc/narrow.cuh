@@ -1257,10 +1257,23 @@ struct RingItem {
   int item, tet_base, seq, near, left;
 };
 
+#ifndef HC_POLY_SMEM
+#define HC_POLY_SMEM 0
+#endif
+// A lane's polygon in shared memory, padded to an odd number of words so
+// that lanes at the same vertex hit different banks.
+struct LanePoly {
+  PV<float, 0> v[kMaxPolyV];
+  int pad;
+};
+
 struct SrKeepWarpSmem {
   TriStage tri[kCluster];
   RingItem ring[kRing];
   unsigned short q[kRQCap];   // ring slot | tet lane << 5 | triangle << 10
+#if HC_POLY_SMEM
+  LanePoly lp[32];
+#endif
 };
 
 constexpr size_t kSrKeepSmemBytes = sizeof(SrKeepWarpSmem) * kNarrowWarps;
@@ -1290,7 +1303,11 @@ __device__ __forceinline__ void sr_keep_round(const StepArgs& a, SrKeepWarpSmem&
   const int item = W.ring[slot].item, seq0 = W.ring[slot].seq;
   const int tet_idx = W.ring[slot].tet_base + i;
   bool have = false;
+#if HC_POLY_SMEM
+  PV<float, 0>* poly = W.lp[lane].v;
+#else
   PV<float, 0> poly[kMaxPolyV];
+#endif
   TetIn<float> t;
   V3<float> n = mk(0.f, 0.f, 0.f);
   int nv = 0, anc = 0, orig_a = 0, orig_b = 0, flags = 0;
