@@ -1257,11 +1257,10 @@ struct RingItem {
   int item, tet_base, seq, near, left;
 };
 
-#ifndef HC_POLY_SMEM
-#define HC_POLY_SMEM 0
-#endif
-// A lane's polygon in shared memory, padded to an odd number of words so
-// that lanes at the same vertex hit different banks.
+// A lane's polygon in shared memory (in local memory the 24 warps' arrays
+// outgrew the L1 beside the staging: 0.42 -> 0.39 ms at 4 CTAs per SM instead
+// of 6), padded to an odd number of words so that lanes at the same vertex
+// hit different banks.
 struct LanePoly {
   PV<float, 0> v[kMaxPolyV];
   int pad;
@@ -1271,18 +1270,14 @@ struct SrKeepWarpSmem {
   TriStage tri[kCluster];
   RingItem ring[kRing];
   unsigned short q[kRQCap];   // ring slot | tet lane << 5 | triangle << 10
-#if HC_POLY_SMEM
-  LanePoly lp[32];
-#endif
+  LanePoly lp[32];            // each lane's polygon of the round
 };
 
 constexpr size_t kSrKeepSmemBytes = sizeof(SrKeepWarpSmem) * kNarrowWarps;
 
-// CTAs per SM narrow_sr_keep_kernel is compiled for (its register budget).
-#ifndef HC_SR_KEEP_CTAS
-#define HC_SR_KEEP_CTAS 6
-#endif
-constexpr int kSrKeepCtas = HC_SR_KEEP_CTAS;
+// CTAs per SM narrow_sr_keep_kernel is compiled for (its register budget;
+// its shared memory, 47.6 KB per CTA, allows 4).
+constexpr int kSrKeepCtas = 4;
 
 // The item's counts (its forces come from the records later).
 __device__ __forceinline__ void store_item_counts(const StepArgs& a, int item, int n_poly, int n_near) {
@@ -1303,11 +1298,7 @@ __device__ __forceinline__ void sr_keep_round(const StepArgs& a, SrKeepWarpSmem&
   const int item = W.ring[slot].item, seq0 = W.ring[slot].seq;
   const int tet_idx = W.ring[slot].tet_base + i;
   bool have = false;
-#if HC_POLY_SMEM
   PV<float, 0>* poly = W.lp[lane].v;
-#else
-  PV<float, 0> poly[kMaxPolyV];
-#endif
   TetIn<float> t;
   V3<float> n = mk(0.f, 0.f, 0.f);
   int nv = 0, anc = 0, orig_a = 0, orig_b = 0, flags = 0;
