@@ -1320,13 +1320,12 @@ __global__ void adjoint_setup_kernel(StepArgs a) {
 
 // Per pair: sum of the item gradients (fixed order, FP64) and the chain rule
 // to the world twists of M and N, plus dL/dE.
-__device__ __forceinline__ void adjoint_reduce_pair(const StepArgs& a, int p, int lane) {
+// The pair's sums by one warp: double-float on the FP32 pipe, in a fixed
+// order (lane-strided, then a fixed butterfly); lane 0 holds them.
+__device__ __forceinline__ void adjoint_sums(const StepArgs& a, int p, int lane, float vh[15], float vl[15]) {
   const PairDev& P = a.pairs[p];
   const int total = *a.item_total;
   const int b = min(a.unit_off[P.unit_begin], total), e = min(a.unit_off[P.unit_end], total);
-  // double-float sums on the FP32 pipe, in a fixed order (lane-strided, then
-  // a fixed butterfly); FP64 from there on
-  float vh[15], vl[15];
 #pragma unroll
   for (int k = 0; k < 15; ++k) vh[k] = vl[k] = 0.f;
   const bool ssp = P.query == 3;   // soft-soft: dL/dE_M, dL/dE_N, dL/d(damping) in entries 12-14
@@ -1358,10 +1357,13 @@ __device__ __forceinline__ void adjoint_reduce_pair(const StepArgs& a, int p, in
       const float h2 = __shfl_xor_sync(0xffffffffu, vh[k], o), l2 = __shfl_xor_sync(0xffffffffu, vl[k], o);
       df_add(vh[k], vl[k], h2, l2);
     }
-  if (lane) return;
-  double v[15];
-#pragma unroll
-  for (int k = 0; k < 15; ++k) v[k] = (double)vh[k] + (double)vl[k];
+}
+
+// The pair's FP64 chain rule from its sums v to both world twists and dE
+// (one thread; FP64 from here on).
+__device__ __forceinline__ void adjoint_tail(const StepArgs& a, int p, const double v[15]) {
+  const PairDev& P = a.pairs[p];
+  const bool ssp = P.query == 3;
   double* out = a.adj_out + 14 * (size_t)p;   // [M twist 6, N twist 6, dE_M, dE_N]
   for (int k = 0; k < 14; ++k) out[k] = 0.0;
   const FrameDev& F = a.frames[p];
@@ -1431,15 +1433,33 @@ __device__ __forceinline__ void adjoint_reduce_pair(const StepArgs& a, int p, in
   }
 }
 
-// A warp per pair (adjoint_reduce_pair); in a fused step, lane 0 also packs
-// the pair's results for the host copy: its wrench, its two twist gradients
-// and its two moduli terms, each kind back to back over the pairs.
-__global__ void adjoint_reduce_kernel(StepArgs a) {
-  const int lane = threadIdx.x & 31;
-  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (p >= a.n_pair) return;
-  adjoint_reduce_pair(a, p, lane);
-  if (lane == 0 && a.out_stage) {
+// kReducePairs pairs per block: warp w sums pair w of the block
+// (adjoint_sums), then the first kReducePairs threads run the pairs' FP64
+// chain rules side by side (an FP64 warp instruction costs the FP64 pipe the
+// same with one active lane as with 32: one tail per warp made this kernel
+// FP64-bound).  In a fused step each also packs its pair's results for the
+// host copy: its wrench, its two twist gradients and its two moduli terms,
+// each kind back to back over the pairs.
+__global__ void __launch_bounds__(kReducePairs * 32) adjoint_reduce_kernel(StepArgs a) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __shared__ float sh[kReducePairs][15], sl[kReducePairs][15];
+  const int pw = blockIdx.x * kReducePairs + w;
+  if (pw < a.n_pair) {
+    float vh[15], vl[15];
+    adjoint_sums(a, pw, lane, vh, vl);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < 15; ++k) { sh[w][k] = vh[k]; sl[w][k] = vl[k]; }
+    }
+  }
+  __syncthreads();
+  const int p = blockIdx.x * kReducePairs + threadIdx.x;
+  if (threadIdx.x >= kReducePairs || p >= a.n_pair) return;
+  double v[15];
+#pragma unroll
+  for (int k = 0; k < 15; ++k) v[k] = (double)sh[threadIdx.x][k] + (double)sl[threadIdx.x][k];
+  adjoint_tail(a, p, v);
+  if (a.out_stage) {
     const size_t n = (size_t)a.n_pair;
     const double* g = a.adj_out + 14 * (size_t)p;
     double* o = a.out_stage;

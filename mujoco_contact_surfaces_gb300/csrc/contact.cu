@@ -405,49 +405,66 @@ __global__ void bp_kernel(StepArgs a) {
 // ---------------------------------------------------------------------------
 // per-pair reduction (fixed order, FP64) and the world-frame wrench
 // ---------------------------------------------------------------------------
-__global__ void reduce_kernel(StepArgs a) {
-  const int lane = threadIdx.x & 31;
-  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (p >= a.n_pair) return;
-  const PairDev& P = a.pairs[p];
+// kReducePairs pairs per block: warp w sums pair w of the block in
+// double-float on the FP32 pipe (FP64 runs at 1/64 of its rate) in a fixed
+// order, lane-strided, then a fixed butterfly; then the first kReducePairs
+// threads turn the pairs' sums into world wrenches side by side in FP64 (one
+// FP64 tail per warp would cost the FP64 pipe a full warp instruction per
+// operation).
+__global__ void __launch_bounds__(kReducePairs * 32) reduce_kernel(StepArgs a) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __shared__ float sh[kReducePairs][8], sl[kReducePairs][8];
+  __shared__ int sc[kReducePairs][3];
   const int total = *a.item_total;
-  int b = min(a.unit_off[P.unit_begin], total), e = min(a.unit_off[P.unit_end], total);
-  // double-float sums on the FP32 pipe (FP64 runs at 1/64 of its rate), in a
-  // fixed order: lane-strided, then a fixed butterfly
-  float vh[8] = {0, 0, 0, 0, 0, 0, 0, 0}, vl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  int c[3] = {0, 0, 0};
-  for (int i = b + lane; i < e; i += 32) {
-    const ItemOut& r = a.item_out[i];
+  const int pw = blockIdx.x * kReducePairs + w;
+  if (pw < a.n_pair) {
+    const PairDev& P = a.pairs[pw];
+    const int b = min(a.unit_off[P.unit_begin], total), e = min(a.unit_off[P.unit_end], total);
+    float vh[8] = {0, 0, 0, 0, 0, 0, 0, 0}, vl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int c[3] = {0, 0, 0};
+    for (int i = b + lane; i < e; i += 32) {
+      const ItemOut& r = a.item_out[i];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) df_add(vh[k], vl[k], r.hi[k], r.lo[k]);
-    c[0] += r.n_poly; c[1] += r.n_faces; c[2] += r.n_near;
-  }
-  if (rec_ok(a) && P.query != 3) {
-    // forces of the kept polygons, in pair order (soft-soft pairs keep none,
-    // and a step of soft-soft pairs alone runs no record scan)
-    const int rb = a.item_poly_off[b], re = a.item_poly_off[e];
-    for (int i = rb + lane; i < re; i += 32) {
-      const RecOut& r = a.rec_out[i];
-      const float x[8] = {r.F[0], r.F[1], r.F[2], r.T[0], r.T[1], r.T[2], r.area, r.fn0};
-#pragma unroll
-      for (int k = 0; k < 8; ++k) df_add(vh[k], vl[k], x[k], 0.f);
-      c[1] += r.n_faces;
+      for (int k = 0; k < 8; ++k) df_add(vh[k], vl[k], r.hi[k], r.lo[k]);
+      c[0] += r.n_poly; c[1] += r.n_faces; c[2] += r.n_near;
     }
-  }
+    if (rec_ok(a) && P.query != 3) {
+      // forces of the kept polygons, in pair order (soft-soft pairs keep none,
+      // and a step of soft-soft pairs alone runs no record scan)
+      const int rb = a.item_poly_off[b], re = a.item_poly_off[e];
+      for (int i = rb + lane; i < re; i += 32) {
+        const RecOut& r = a.rec_out[i];
+        const float x[8] = {r.F[0], r.F[1], r.F[2], r.T[0], r.T[1], r.T[2], r.area, r.fn0};
 #pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) {
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const float h2 = __shfl_xor_sync(0xffffffffu, vh[k], o), l2 = __shfl_xor_sync(0xffffffffu, vl[k], o);
-      df_add(vh[k], vl[k], h2, l2);
+        for (int k = 0; k < 8; ++k) df_add(vh[k], vl[k], x[k], 0.f);
+        c[1] += r.n_faces;
+      }
     }
 #pragma unroll
-    for (int k = 0; k < 3; ++k) c[k] += __shfl_xor_sync(0xffffffffu, c[k], o);
+    for (int o = 16; o >= 1; o >>= 1) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const float h2 = __shfl_xor_sync(0xffffffffu, vh[k], o), l2 = __shfl_xor_sync(0xffffffffu, vl[k], o);
+        df_add(vh[k], vl[k], h2, l2);
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) c[k] += __shfl_xor_sync(0xffffffffu, c[k], o);
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) { sh[w][k] = vh[k]; sl[w][k] = vl[k]; }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) sc[w][k] = c[k];
+    }
   }
-  if (lane) return;
+  __syncthreads();
+  const int p = blockIdx.x * kReducePairs + threadIdx.x;
+  if (threadIdx.x >= kReducePairs || p >= a.n_pair) return;
+  const PairDev& P = a.pairs[p];
+  const int b = min(a.unit_off[P.unit_begin], total), e = min(a.unit_off[P.unit_end], total);
   double v[8];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) v[k] = (double)vh[k] + (double)vl[k];
+  for (int k = 0; k < 8; ++k) v[k] = (double)sh[threadIdx.x][k] + (double)sl[threadIdx.x][k];
   const FrameDev& F = a.frames[p];
   PairOut o;
   V3<double> Fs = mk(v[0], v[1], v[2]), Ts = mk(v[3], v[4], v[5]);
@@ -459,7 +476,7 @@ __global__ void reduce_kernel(StepArgs a) {
   o.wrench[3] = on ? Tw.x : 0.0; o.wrench[4] = on ? Tw.y : 0.0; o.wrench[5] = on ? Tw.z : 0.0;
   o.area = v[6];
   o.total_fn0 = v[7];
-  o.n_poly = c[0]; o.n_faces = c[1]; o.n_near = c[2];
+  o.n_poly = sc[threadIdx.x][0]; o.n_faces = sc[threadIdx.x][1]; o.n_near = sc[threadIdx.x][2];
   o.n_items = e - b;
   a.pair_out[p] = o;
 }
@@ -616,7 +633,7 @@ int launch_adjoint(const StepArgs& a, cudaStream_t s) {
   if (a.type_unit_end[2] > a.type_unit_begin[2]) {
     adjoint_ss_kernel<<<a.narrow_grid, 128, 0, s>>>(a); ++n;
   }
-  adjoint_reduce_kernel<<<(a.n_pair * 32 + 127) / 128, 128, 0, s>>>(a); ++n;
+  adjoint_reduce_kernel<<<(a.n_pair + kReducePairs - 1) / kReducePairs, kReducePairs * 32, 0, s>>>(a); ++n;
   return n;
 }
 
@@ -676,7 +693,7 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   }
   if (ev) cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal);
   if (a.n_pair > 0) {
-    reduce_kernel<<<(a.n_pair * 32 + 127) / 128, 128, 0, s>>>(a); ++n;
+    reduce_kernel<<<(a.n_pair + kReducePairs - 1) / kReducePairs, kReducePairs * 32, 0, s>>>(a); ++n;
   }
   if (ev) cudaEventRecordWithFlags(ev[4], s, cudaEventRecordExternal);
   if (a.n_cells_total > 0) {

@@ -7,6 +7,9 @@
 
 namespace hc {
 
+// Pairs per block of the per-pair reductions (a warp each).
+constexpr int kReducePairs = 16;
+
 // Step counters the step's first kernel zeroes (StepArgs::reset_words).
 constexpr int kResetWords = 12;
 
