@@ -41,7 +41,7 @@ METRIC = "contact pairs/s fwd+adjoint, batched vs plain GPU path at 1e-5 rel wre
 # dram__bytes_write.sum) from an ncu capture of this workload at 1024 scenes
 # (launch shape 6,2), scaled by the scenes processed (items and polygons
 # grow in proportion).
-NARROW_SR_DRAM_BYTES_PER_SCENE = (74.477568e6 + 64.97152e6) / 1024
+NARROW_SR_DRAM_BYTES_PER_SCENE = (61.00736e6 + 30.865664e6) / 1024
 
 
 def parse():
