@@ -863,17 +863,11 @@ __device__ __forceinline__ bool raster_prepare_group(const StepArgs& a, const Se
                                    __fmul_rn(__fsub_rn(rp.ly[i], rp.ly[0]), __fsub_rn(rp.lx[i + 1], rp.lx[0]))));
   if (!(fabsf(A2) >= 1e-10f)) return false;
   rp.pos = A2 > 0.f;
-  const float e1x = __fsub_rn(rp.lx[1], rp.lx[0]), e1y = __fsub_rn(rp.ly[1], rp.ly[0]), e1z = __fsub_rn(lz[1], lz[0]);
-  float nx = 0.f, ny = 0.f, nz = 0.f;
-#pragma unroll
-  for (int i = 2; i < MV; ++i) {
-    if (i < nv) {
-      const float fx = __fsub_rn(rp.lx[i], rp.lx[0]), fy = __fsub_rn(rp.ly[i], rp.ly[0]), fz = __fsub_rn(lz[i], lz[0]);
-      nx = __fadd_rn(nx, __fsub_rn(__fmul_rn(e1y, fz), __fmul_rn(e1z, fy)));
-      ny = __fadd_rn(ny, __fsub_rn(__fmul_rn(e1z, fx), __fmul_rn(e1x, fz)));
-      nz = __fadd_rn(nz, __fsub_rn(__fmul_rn(e1x, fy), __fmul_rn(e1y, fx)));
-    }
-  }
+  // the polygon lies in its triangle's (or the half-space's) plane: the
+  // record's unit normal, in the sensor frame
+  const float nx = dot3_rn(Rl, R.n[0], R.n[1], R.n[2]);
+  const float ny = dot3_rn(Rl + 3, R.n[0], R.n[1], R.n[2]);
+  const float nz = dot3_rn(Rl + 6, R.n[0], R.n[1], R.n[2]);
   if (!(fabsf(nz) > 0.f)) return false;
   const float inz = __frcp_rn(nz);
   rp.zx = __fmul_rn(-nx, inz);   // dz/dx, dz/dy on the plane
