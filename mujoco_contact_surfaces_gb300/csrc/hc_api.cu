@@ -2021,20 +2021,22 @@ hc_status hc_step_adjoint(hc_context* c, int n_geom, const double* xpos, const d
   for (int attempt = 0; attempt < 4; ++attempt) {
     if (hc_status st = run_fused(c, d_dw, d_dt)) return st;
     if (n_pair == 0 && c->sensors.empty()) return HC_OK;
-    // the taxel maps leave on the copy stream once the forward is done,
-    // while the adjoint runs; the other results straight into the caller's
-    // arrays (each one contiguous copy from the packed results), then the
-    // status word; one wait for all of it
-    if (c->n_cells && taxels) {
-      HC_CUDA(cudaStreamWaitEvent(c->copy_stream, c->xev[1], 0));
+    // the taxel maps and wrenches leave on the copy stream once the forward
+    // is done, while the adjoint runs; the gradients straight into the
+    // caller's arrays (each one contiguous copy from the packed results),
+    // then the status word; one wait for all of it
+    if ((c->n_cells && taxels) || (n_pair && wrench)) HC_CUDA(cudaStreamWaitEvent(c->copy_stream, c->xev[1], 0));
+    if (c->n_cells && taxels)
       HC_CUDA(cudaMemcpyAsync(taxels, c->taxels.p, (size_t)c->n_cells * sizeof(float), cudaMemcpyDeviceToHost,
                               c->copy_stream));
-    }
+    // the wrenches are final with the forward too: the six leading doubles
+    // of each 10-double pair record
+    if (n_pair && wrench)
+      HC_CUDA(cudaMemcpy2DAsync(wrench, 6 * sizeof(double), c->pair_out.p, sizeof(hc::PairOut), 6 * sizeof(double),
+                                (size_t)n_pair, cudaMemcpyDeviceToHost, c->copy_stream));
     HC_CUDA(cudaEventRecord(c->xev[2], c->copy_stream));
     HC_CUDA(cudaStreamWaitEvent(c->stream, c->xev[2], 0));
     const double* st = c->out_stage.p;
-    if (n_pair && wrench)
-      HC_CUDA(cudaMemcpyAsync(wrench, st, 6 * (size_t)n_pair * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     if (n_pair && dL_dpose)
       HC_CUDA(cudaMemcpyAsync(dL_dpose, st + 6 * (size_t)n_pair, 12 * (size_t)n_pair * sizeof(double),
                               cudaMemcpyDeviceToHost, c->stream));
