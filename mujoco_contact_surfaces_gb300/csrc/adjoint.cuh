@@ -1049,16 +1049,20 @@ __device__ __forceinline__ void rec_fwd_one(const StepArgs& a, int r, int dst, b
 }
 
 // The next round's eight records (8 x 288 B: 18 lines of 128 B), one line
-// per lane, and their keys, requested into L1 before this round's work: the
-// record kernels wait on their records' loads more than on arithmetic
-// (adjoint 0.57 -> 0.54 ms; into L2 alone gained a little less).
-__device__ __forceinline__ void prefetch_records(const StepArgs& a, int base, int n, int lane) {
+// per lane, and their slot lookups (the forward's keys, the adjoint's
+// slots), requested into L1 before this round's work: the record kernels
+// wait on their records' loads more than on arithmetic (adjoint 0.57 ->
+// 0.54 ms; into L2 alone gained a little less).
+__device__ __forceinline__ void prefetch_records(const StepArgs& a, int base, int n, int lane, bool slots) {
   if (base >= n) return;
   const int nrec = min(8, n - base);
   const char* p = reinterpret_cast<const char*>(a.recs + base);
   const int lines = (nrec * (int)sizeof(AdjPoly) + 127) / 128;
   if (lane < lines) asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 128 * lane));
-  if (lane == 31) asm volatile("prefetch.global.L1 [%0];" ::"l"(a.rec_key + base));
+  if (lane == 31) {
+    const void* q = slots ? (const void*)(a.rec_dst + base) : (const void*)(a.rec_key + base);
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(q));
+  }
 }
 
 // Forward pass over the kept polygons, eight records per warp and round:
@@ -1074,9 +1078,10 @@ __global__ void __launch_bounds__(128, 7) rec_forward_kernel(StepArgs a) {
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
   constexpr int kPer = 32 / kGroupSmall;
   for (int base = warp * kPer; base < n; base += n_warps * kPer) {
-    prefetch_records(a, base + n_warps * kPer, n, lane);
+    prefetch_records(a, base + n_warps * kPer, n, lane, false);
     const int r = base + grp;
     const int dst = rec_slot(a, r, n);
+    if (r < n && sub == 0) a.rec_dst[r] = dst;   // the adjoint's lookup
     const int nv = dst >= 0 ? a.recs[r].nv : 0;
     rec_fwd_one<kGroupSmall, kRepr>(a, r, dst, dst >= 0 && nv <= kGroupSmall, sub);
     __syncwarp();
@@ -1272,9 +1277,11 @@ __global__ void __launch_bounds__(128, 5) adjoint_rec_kernel(StepArgs a) {
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
   constexpr int kPer = 32 / kGroupSmall;
   for (int base = warp * kPer; base < n; base += n_warps * kPer) {
-    prefetch_records(a, base + n_warps * kPer, n, lane);
+    prefetch_records(a, base + n_warps * kPer, n, lane, true);
     const int r = base + grp;
-    const int dst = rec_slot(a, r, n);
+    // the slot the forward record pass stored (one load where the key and
+    // the item's offset were two dependent ones: adjoint 0.523 -> 0.516 ms)
+    const int dst = r < n ? a.rec_dst[r] : -1;
     const int nv = dst >= 0 ? a.recs[r].nv : 0;
     rec_adj_one<kGroupSmall, kRepr>(a, r, dst, dst >= 0 && nv <= kGroupSmall, lane, sub);
     __syncwarp();

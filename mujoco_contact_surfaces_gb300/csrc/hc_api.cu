@@ -230,6 +230,7 @@ struct hc_context {
   DevBuf<hc::RecOut> rec_out;
   DevBuf<float4> slot_press;
   DevBuf<int> rec_perm;
+  DevBuf<int> rec_dst;
   // taxel-point sensors
   std::vector<TaxelHost> tsens_h;
   std::vector<int> tsens_enabled_h;
@@ -504,6 +505,7 @@ hc_status ensure_recs(hc_context* c, int cap) {
     HC_CUDA(c->rec_out.reserve(cap));
     HC_CUDA(c->slot_press.reserve(6 * (size_t)cap));
     HC_CUDA(c->rec_perm.reserve(cap));
+    HC_CUDA(c->rec_dst.reserve(cap));
     HC_CUDA(c->rec_grad.reserve(16 * (size_t)cap));
     c->rec_cap = cap;
     invalidate_graph(c);
@@ -687,6 +689,7 @@ hc::StepArgs make_args(hc_context* c, int want_polys, int want_pair) {
     a.rec_out = c->rec_out.p;
     a.slot_press = c->slot_press.p;
     a.rec_perm = c->rec_perm.p;
+    a.rec_dst = c->rec_dst.p;
     a.item_poly_off = c->item_poly_off.p;
     a.poly_tiles = c->poly_tiles.p;
     a.n_item_blocks = std::max(1, (c->item_cap + hc::kBpBlock - 1) / hc::kBpBlock);

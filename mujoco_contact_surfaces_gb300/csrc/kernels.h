@@ -111,6 +111,7 @@ struct StepArgs {
                              // (py, lz0, zx, zy) of the polygon's plane, then its
                              // sample box (X0, X1, Y0, Y1 as ints; X0 > X1: none)
   int* rec_perm;             // per record slot: the record index
+  int* rec_dst;              // per record: its slot (-1: none), written by the forward record pass
   // taxel-point sensors
   const TaxelSensorDev* tsens;
   int n_tsens;
