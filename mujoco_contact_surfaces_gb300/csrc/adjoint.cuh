@@ -1333,7 +1333,30 @@ __device__ __forceinline__ void adjoint_sums(const StepArgs& a, int p, int lane,
   if (recs_valid(a) && !ssp) {
     // the pair's records, in pair order
     const int rb = a.item_poly_off[b], re = a.item_poly_off[e];
-    for (int i = rb + lane; i < re; i += 32) {
+    // four records per lane in flight, then summed in the same order (with
+    // the forward's reduction batched likewise: adjoint stage 0.517 ->
+    // 0.506 ms, step 1.411 -> 1.394 ms)
+    int i = rb + lane;
+    for (; i + 96 < re; i += 128) {
+      float4 q0[4], q1[4], q2[4];
+      float q3[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float4* g = reinterpret_cast<const float4*>(a.rec_grad + 16 * (size_t)(i + 32 * u));
+        q0[u] = g[0];
+        q1[u] = g[1];
+        q2[u] = g[2];
+        q3[u] = reinterpret_cast<const float*>(g + 3)[0];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float x[13] = {q0[u].x, q0[u].y, q0[u].z, q0[u].w, q1[u].x, q1[u].y, q1[u].z, q1[u].w,
+                             q2[u].x, q2[u].y, q2[u].z, q2[u].w, q3[u]};
+#pragma unroll
+        for (int k = 0; k < 13; ++k) df_add(vh[k], vl[k], x[k], 0.f);
+      }
+    }
+    for (; i < re; i += 32) {
       const float4* g = reinterpret_cast<const float4*>(a.rec_grad + 16 * (size_t)i);
       const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3];
       const float x[13] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w, g2.x, g2.y, g2.z, g2.w, g3.x};

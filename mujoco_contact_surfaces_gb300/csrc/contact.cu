@@ -432,7 +432,28 @@ __global__ void __launch_bounds__(kReducePairs * 32) reduce_kernel(StepArgs a) {
       // forces of the kept polygons, in pair order (soft-soft pairs keep none,
       // and a step of soft-soft pairs alone runs no record scan)
       const int rb = a.item_poly_off[b], re = a.item_poly_off[e];
-      for (int i = rb + lane; i < re; i += 32) {
+      // four records per lane in flight, then summed in the same order
+      // (the loads of a plain lane-strided loop waited one by one)
+      int i = rb + lane;
+      for (; i + 96 < re; i += 128) {
+        float4 q0[4], q1[4];
+        int nf[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const float4* s = reinterpret_cast<const float4*>(a.rec_out + i + 32 * u);
+          q0[u] = s[0];
+          q1[u] = s[1];
+          nf[u] = reinterpret_cast<const int*>(s + 2)[0];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const float x[8] = {q0[u].x, q0[u].y, q0[u].z, q0[u].w, q1[u].x, q1[u].y, q1[u].z, q1[u].w};
+#pragma unroll
+          for (int k = 0; k < 8; ++k) df_add(vh[k], vl[k], x[k], 0.f);
+          c[1] += nf[u];
+        }
+      }
+      for (; i < re; i += 32) {
         const RecOut& r = a.rec_out[i];
         const float x[8] = {r.F[0], r.F[1], r.F[2], r.T[0], r.T[1], r.T[2], r.area, r.fn0};
 #pragma unroll
@@ -539,12 +560,44 @@ __global__ void __launch_bounds__(256) taxel_kernel(StepArgs a) {
   const int bw = box.w - box.z + 1, nb = (box.y - box.x + 1) * bw;
   const bool staged = nb <= kTaxBoxSamples;
   if (staged) {
-    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-      const int X = box.x + i / bw, Y = box.z + i % bw;
-      unsigned long long* q = smp + (size_t)X * S.ny + Y;
-      const unsigned long long k = *q;
-      val[i] = sample_pressure(a, S, k, X, Y);
-      if (!a.keep_samples && k != ~0ull) *q = ~0ull;
+    // two samples per thread in flight: their keys, then the winning
+    // polygons' pressure models and the sample coordinates, then the values
+    // as sample_pressure forms them (one sample at a time waited out both
+    // loads; four at a time took 57 registers, two fewer blocks per SM)
+    const int nt = blockDim.x;
+    for (int i0 = threadIdx.x; i0 < nb; i0 += 2 * nt) {
+      unsigned long long k[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int i = i0 + u * nt;
+        k[u] = i < nb ? smp[(size_t)(box.x + i / bw) * S.ny + (box.z + i % bw)] : ~0ull;
+      }
+      float4 m0[2], m1[2];
+      float sx[2], sy[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int i = i0 + u * nt;
+        const unsigned lo = (unsigned)(k[u] & 0xffffffffu);
+        m0[u] = m1[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        sx[u] = sy[u] = 0.f;
+        if (k[u] != ~0ull && (lo & kSlotTag)) {
+          const size_t b6 = 6 * (size_t)(lo & ~(kSlotTag | kSideBit)) + ((lo & kSideBit) ? 3 : 0);
+          m0[u] = a.slot_press[b6];
+          m1[u] = a.slot_press[b6 + 1];
+          sx[u] = a.samp_coord[S.samp_off_x + box.x + i / bw];
+          sy[u] = a.samp_coord[S.samp_off_y + box.z + i % bw];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int i = i0 + u * nt;
+        if (i >= nb) break;
+        const unsigned lo = (unsigned)(k[u] & 0xffffffffu);
+        const float pr = (lo & kSlotTag) ? raster_pressure(m0[u].x, m0[u].y, m0[u].z, m0[u].w, m1[u].x, sx[u], sy[u])
+                                         : __uint_as_float(lo);
+        val[i] = k[u] == ~0ull ? 0.f : pr * S.rmean;
+        if (!a.keep_samples && k[u] != ~0ull) smp[(size_t)(box.x + i / bw) * S.ny + (box.z + i % bw)] = ~0ull;
+      }
     }
     __syncthreads();
   }
