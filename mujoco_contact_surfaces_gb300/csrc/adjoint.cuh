@@ -965,15 +965,28 @@ __device__ __forceinline__ void rec_rays_adj(const StepArgs& a, const AdjPoly& R
   const unsigned own = (unsigned)key_slot(0.f, dst, side);
   const V3<float> g = mk(R.g[0], R.g[1], R.g[2]);
   const int dq = Gs / nY, dr = Gs % nY;
+  // the lane's samples two at a time: both keys in flight before either is
+  // tested (adjoint 0.506 -> 0.492 ms), one copy of the won-sample code
   int X = X0 + sub / nY, Y = Y0 + sub % nY;
-  for (int idx = sub; idx < cnt; idx += Gs, X += dq, Y += dr) {
+  for (int idx = sub; idx < cnt; idx += 2 * Gs) {
+    int Xb = X + dq, Yb = Y + dr;
+    if (Yb > Y1) { Yb -= nY; ++Xb; }
+    const bool hb = idx + Gs < cnt;
+    const unsigned ka = (unsigned)smp[(size_t)X * S.ny + Y];
+    const unsigned kb = hb ? (unsigned)smp[(size_t)Xb * S.ny + Yb] : 0u;   // own is never 0
+#pragma unroll 1
+    for (int u = 0; u < 2; ++u) {
+      if ((u ? kb : ka) != own) continue;   // won by another polygon, or missed
+      const int Xs = u ? Xb : X, Ys = u ? Yb : Y;
+      const float qx = sx[Xs], qy = sy[Ys];
+      const float z = raster_height(m0.x, m0.y, m1.y, m1.z, m1.w, qx, qy);
+      const float pr = raster_pressure(m0.x, m0.y, m0.z, m0.w, m1.x, qx, qy);
+      sample_adjoint<false>(a, S, Rl, tl, qx, qy, z, pr, Xs, Ys, g, mk(R.n[0], R.n[1], R.n[2]), soft_is_sensor, G,
+                            nullptr);
+    }
+    X = Xb + dq;
+    Y = Yb + dr;
     if (Y > Y1) { Y -= nY; ++X; }
-    if ((unsigned)smp[(size_t)X * S.ny + Y] != own) continue;   // won by another polygon, or missed
-    const float qx = sx[X], qy = sy[Y];
-    const float z = raster_height(m0.x, m0.y, m1.y, m1.z, m1.w, qx, qy);
-    const float pr = raster_pressure(m0.x, m0.y, m0.z, m0.w, m1.x, qx, qy);
-    sample_adjoint<false>(a, S, Rl, tl, qx, qy, z, pr, X, Y, g, mk(R.n[0], R.n[1], R.n[2]), soft_is_sensor, G,
-                          nullptr);
   }
 }
 
