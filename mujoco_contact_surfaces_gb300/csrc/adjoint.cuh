@@ -1062,20 +1062,58 @@ __device__ __forceinline__ void rec_fwd_one(const StepArgs& a, int r, int dst, b
 }
 
 // The next round's eight records (8 x 288 B: 18 lines of 128 B), one line
-// per lane, and their slot lookups (the forward's keys, the adjoint's
-// slots), requested into L1 before this round's work: the record kernels
-// wait on their records' loads more than on arithmetic (adjoint 0.57 ->
-// 0.54 ms; into L2 alone gained a little less).
-__device__ __forceinline__ void prefetch_records(const StepArgs& a, int base, int n, int lane, bool slots) {
+// per lane, and their keys, requested into L1 before this round's work: the
+// record kernels wait on their records' loads more than on arithmetic
+// (adjoint 0.57 -> 0.54 ms when it prefetched too; into L2 alone gained a
+// little less).
+__device__ __forceinline__ void prefetch_records(const StepArgs& a, int base, int n, int lane) {
   if (base >= n) return;
   const int nrec = min(8, n - base);
   const char* p = reinterpret_cast<const char*>(a.recs + base);
   const int lines = (nrec * (int)sizeof(AdjPoly) + 127) / 128;
   if (lane < lines) asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 128 * lane));
-  if (lane == 31) {
-    const void* q = slots ? (const void*)(a.rec_dst + base) : (const void*)(a.rec_key + base);
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(q));
+  if (lane == 31) asm volatile("prefetch.global.L1 [%0];" ::"l"(a.rec_key + base));
+}
+
+// The adjoint's round of eight records staged in shared memory instead,
+// double-buffered per warp (the next round's copies in flight while this
+// round runs).  The copies bypass L1 and are marked evict-first in L2: the
+// pass reads each record once, and what it shares with the other passes
+// (sample keys, pressure models, gradients) should stay in L2.  Adjoint
+// 0.492 -> 0.483 ms against the L1 prefetch; the forward record pass
+// measured 0.320 -> 0.323 ms with it and keeps the prefetch.
+struct RecStage {
+  AdjPoly r[2][8];
+};
+
+__device__ __forceinline__ unsigned long long evict_first_policy() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+// Records base .. base + 7 (those below n) into dst, 16 B per copy across
+// the lanes, as one commit group (empty past the end); lane 31 requests the
+// round's stored slots into L1.
+__device__ __forceinline__ void stage_round(const StepArgs& a, AdjPoly* dst, int base, int n, int lane,
+                                            unsigned long long pol) {
+  if (base < n) {
+    const int chunks = min(8, n - base) * (int)(sizeof(AdjPoly) / 16);
+    const char* src = reinterpret_cast<const char*>(a.recs + base);
+    const unsigned d0 = (unsigned)__cvta_generic_to_shared(dst);
+    for (int c = lane; c < chunks; c += 32)
+      asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(d0 + 16 * c),
+                   "l"(src + 16 * c), "l"(pol)
+                   : "memory");
+    if (lane == 31) asm volatile("prefetch.global.L1 [%0];" ::"l"(a.rec_dst + base));
   }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// This round's group complete on every lane (the next one may be in flight).
+__device__ __forceinline__ void stage_wait() {
+  asm volatile("cp.async.wait_group 1;" ::: "memory");
+  __syncwarp();
 }
 
 // Forward pass over the kept polygons, eight records per warp and round:
@@ -1091,7 +1129,7 @@ __global__ void __launch_bounds__(128, 7) rec_forward_kernel(StepArgs a) {
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
   constexpr int kPer = 32 / kGroupSmall;
   for (int base = warp * kPer; base < n; base += n_warps * kPer) {
-    prefetch_records(a, base + n_warps * kPer, n, lane, false);
+    prefetch_records(a, base + n_warps * kPer, n, lane);
     const int r = base + grp;
     const int dst = rec_slot(a, r, n);
     if (r < n && sub == 0) a.rec_dst[r] = dst;   // the adjoint's lookup
@@ -1257,9 +1295,11 @@ __device__ __forceinline__ void rec_wrench_group(const StepArgs& a, const AdjPol
 
 // The reverse pass over one kept polygon by a group of G lanes: the taxel
 // samples it won, then the wrench; its 13 gradient terms into its slot.
+// rs: the round's staged records, k: this one's index among them.
 template <int G, int kRepr>
-__device__ __forceinline__ void rec_adj_one(const StepArgs& a, int r, int dst, bool on, int lane, int sub) {
-  const AdjPoly& R = a.recs[on ? r : 0];
+__device__ __forceinline__ void rec_adj_one(const StepArgs& a, const AdjPoly* rs, int k, int dst, bool on, int lane,
+                                            int sub) {
+  const AdjPoly& R = rs[on ? k : 0];
   AdjAcc G_;
   adj_zero(G_);
   __syncwarp();   // the groups enter the shuffled ray preparation together
@@ -1289,18 +1329,28 @@ __global__ void __launch_bounds__(128, 5) adjoint_rec_kernel(StepArgs a) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n_warps = (gridDim.x * blockDim.x) >> 5;
   constexpr int kPer = 32 / kGroupSmall;
-  for (int base = warp * kPer; base < n; base += n_warps * kPer) {
-    prefetch_records(a, base + n_warps * kPer, n, lane, true);
+  __shared__ RecStage stage[4];   // per warp (128 threads)
+  RecStage& St = stage[threadIdx.x >> 5];
+  const unsigned long long pol = evict_first_policy();
+  int buf = 0;
+  stage_round(a, St.r[0], warp * kPer, n, lane, pol);
+  for (int base = warp * kPer; base < n; base += n_warps * kPer, buf ^= 1) {
+    stage_round(a, St.r[buf ^ 1], base + n_warps * kPer, n, lane, pol);
+    stage_wait();
+    const AdjPoly* rs = St.r[buf];
     const int r = base + grp;
     // the slot the forward record pass stored (one load where the key and
     // the item's offset were two dependent ones: adjoint 0.523 -> 0.516 ms)
     const int dst = r < n ? a.rec_dst[r] : -1;
-    const int nv = dst >= 0 ? a.recs[r].nv : 0;
-    rec_adj_one<kGroupSmall, kRepr>(a, r, dst, dst >= 0 && nv <= kGroupSmall, lane, sub);
+    const int nv = dst >= 0 ? rs[grp].nv : 0;
+    rec_adj_one<kGroupSmall, kRepr>(a, rs, grp, dst, dst >= 0 && nv <= kGroupSmall, lane, sub);
     __syncwarp();
-    rec_large_turns(dst >= 0 && nv > kGroupSmall && sub == 0, base, dst, lane,
-                    [&](int r8, int dst8, bool on8, int sub8) { rec_adj_one<kGroup, kRepr>(a, r8, dst8, on8, lane, sub8); });
+    rec_large_turns(dst >= 0 && nv > kGroupSmall && sub == 0, base, dst, lane, [&](int r8, int dst8, bool on8, int sub8) {
+      rec_adj_one<kGroup, kRepr>(a, rs, r8 - base, dst8, on8, lane, sub8);
+    });
+    __syncwarp();   // the round's records read before their buffer is refilled
   }
+  asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 // Per pair: upstream adjoints of the soft-frame sums from dL/dwrench
