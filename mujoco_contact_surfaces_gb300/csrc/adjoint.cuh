@@ -1037,6 +1037,50 @@ __device__ __forceinline__ void rec_large_turns(bool flag, int base, int dst, in
   }
 }
 
+// The adjoint defers the polygons of more than 4 vertices (about 1 in 100)
+// across rounds instead: lane i of the warp holds the i-th deferred
+// (record, slot), and whenever four are held the warp's four 8-lane groups
+// take them in one turn.  A turn in every round that held one (about 1
+// round in 13) left most of the warp idle (adjoint 0.483 -> 0.473 ms; the
+// forward record pass measured 0.319 -> 0.325 ms with it, at its 72-register
+// bound, and keeps the turns in the round).  Each polygon writes only its
+// own slot, so the order does not change any result.
+struct LargeQueue {
+  int r, dst, n;   // this lane's entry; entries held (the same on every lane)
+};
+
+// Appends the records whose lane 4k sets `flag` (record r, slot dst), in
+// lane order.  Every lane of the warp calls it.
+__device__ __forceinline__ void large_push(LargeQueue& q, bool flag, int r, int dst, int lane) {
+  const unsigned big = __ballot_sync(0xffffffffu, flag);
+  const int cnt = __popc(big), j = lane - q.n;
+  unsigned m = big;
+  for (int t = 0; t < j && t < cnt; ++t) m &= m - 1;
+  const bool take = j >= 0 && j < cnt;
+  const int src = take ? __ffs(m) - 1 : lane;
+  const int rr = __shfl_sync(0xffffffffu, r, src), dd = __shfl_sync(0xffffffffu, dst, src);
+  if (take) {
+    q.r = rr;
+    q.dst = dd;
+  }
+  q.n += cnt;
+}
+
+// Turns of four held polygons while four are held (all held ones when
+// `all`): body(r, dst, on, sub) on every lane, `on` when the lane's 8-lane
+// group holds one this turn.  Every lane of the warp calls it.
+template <class Body>
+__device__ __forceinline__ void large_turns(LargeQueue& q, bool all, int lane, Body body) {
+  while (q.n >= 4 || (all && q.n > 0)) {
+    const int g = lane >> 3;
+    const int r8 = __shfl_sync(0xffffffffu, q.r, g), d8 = __shfl_sync(0xffffffffu, q.dst, g);
+    body(r8, d8, g < q.n, lane & (kGroup - 1));
+    q.r = __shfl_down_sync(0xffffffffu, q.r, 4);
+    q.dst = __shfl_down_sync(0xffffffffu, q.dst, 4);
+    q.n = max(0, q.n - 4);
+  }
+}
+
 // The forward pass over one kept polygon by a group of G lanes: forces into
 // its pair-ordered slot, then the sensors' rays.
 template <int G, int kRepr>
@@ -1332,6 +1376,8 @@ __global__ void __launch_bounds__(128, 5) adjoint_rec_kernel(StepArgs a) {
   __shared__ RecStage stage[4];   // per warp (128 threads)
   RecStage& St = stage[threadIdx.x >> 5];
   const unsigned long long pol = evict_first_policy();
+  LargeQueue lq = {0, -1, 0};
+  auto large = [&](int r8, int dst8, bool on8, int sub8) { rec_adj_one<kGroup, kRepr>(a, a.recs, r8, dst8, on8, lane, sub8); };
   int buf = 0;
   stage_round(a, St.r[0], warp * kPer, n, lane, pol);
   for (int base = warp * kPer; base < n; base += n_warps * kPer, buf ^= 1) {
@@ -1344,12 +1390,13 @@ __global__ void __launch_bounds__(128, 5) adjoint_rec_kernel(StepArgs a) {
     const int dst = r < n ? a.rec_dst[r] : -1;
     const int nv = dst >= 0 ? rs[grp].nv : 0;
     rec_adj_one<kGroupSmall, kRepr>(a, rs, grp, dst, dst >= 0 && nv <= kGroupSmall, lane, sub);
-    __syncwarp();
-    rec_large_turns(dst >= 0 && nv > kGroupSmall && sub == 0, base, dst, lane, [&](int r8, int dst8, bool on8, int sub8) {
-      rec_adj_one<kGroup, kRepr>(a, rs, r8 - base, dst8, on8, lane, sub8);
-    });
     __syncwarp();   // the round's records read before their buffer is refilled
+    // the held larger polygons are read from global memory (their round's
+    // buffer is gone by the time four are held)
+    large_push(lq, dst >= 0 && nv > kGroupSmall && sub == 0, r, dst, lane);
+    large_turns(lq, false, lane, large);
   }
+  large_turns(lq, true, lane, large);
   asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
