@@ -527,6 +527,9 @@ __device__ __forceinline__ float sample_pressure(const StepArgs& a, const Sensor
 
 // Samples of a touched box resolved in shared memory at once.
 constexpr int kTaxBoxSamples = 8192;
+// Threads per sensor block: 512 resolve a touched box (about 1500 samples
+// on the bench) in fewer steps than 256 (step 1.360 -> 1.352 ms).
+constexpr int kTaxelBlock = 512;
 
 // A block per sensor.  Its touched box's samples are resolved first, each by
 // its own thread (the sample, then the winning polygon's pressure model: two
@@ -534,7 +537,7 @@ constexpr int kTaxBoxSamples = 8192;
 // then each cell sums its samples from there in the reference's i-major,
 // j-minor order.  Cells outside the box hold no hit (value 0).  A box larger
 // than the shared array is summed cell by cell from global memory.
-__global__ void __launch_bounds__(256) taxel_kernel(StepArgs a) {
+__global__ void __launch_bounds__(kTaxelBlock) taxel_kernel(StepArgs a) {
   __shared__ SensorDev S;
   __shared__ int4 box;
   __shared__ float val[kTaxBoxSamples];
@@ -750,7 +753,7 @@ int launch_step(const StepArgs& a, cudaStream_t s, cudaEvent_t* ev) {
   }
   if (ev) cudaEventRecordWithFlags(ev[4], s, cudaEventRecordExternal);
   if (a.n_cells_total > 0) {
-    taxel_kernel<<<a.n_sensor, 256, 0, s>>>(a); ++n;
+    taxel_kernel<<<a.n_sensor, kTaxelBlock, 0, s>>>(a); ++n;
   }
   if (ev) cudaEventRecordWithFlags(ev[5], s, cudaEventRecordExternal);
   return n;
