@@ -122,8 +122,12 @@ def test_taxel_gradient_without_adjoint_mode(gpu):
 def test_kept_polygons_match_recompute(gpu):
     # without sensors and without adjoint mode no polygons are kept and the
     # adjoint recomputes them; in adjoint mode it reads the kept polygons.
-    # The two paths agree to float rounding.
+    # The two paths agree to float rounding.  The scenes hold polygons of
+    # more than 4 vertices (the oracle counts them), which the kept-polygon
+    # adjoint defers to turns of 8-lane groups.
     s = scenes.single_pair(6, velocities=True, min_pen=1e-3)
+    cand = np.asarray(Oracle(s).collide(candidates=True)["candidates"])
+    assert (cand[:, 3] > 4).sum() >= 4
     rng = np.random.default_rng(9)
     dLdw = rng.normal(size=(len(s.g1), 6))
     _, _, d1, e1 = run_adjoint(s, dLdw, None, adjoint_mode=False)
