@@ -349,6 +349,12 @@ __global__ void bp_kernel(StepArgs a) {
   const int tile = tile_s;
   const int u = tile * kBpUnits + wid;
   int p = 0, r = 0, cnt = 0, cl = 0, ncl = 0;
+  // the passing leaves of the lane's subtree as bits (leaf0 + bit), when
+  // the subtree has at most 32 leaves (trees of up to 1024 leaf clusters):
+  // the items are then written from the bits instead of a second walk
+  unsigned lmask = 0;
+  int leaf0 = 0;
+  bool masked = false;
   QueryBox q;
   const float4* nd = nullptr;
   const PairDev* P = nullptr;
@@ -362,7 +368,14 @@ __global__ void bp_kernel(StepArgs a) {
       nd = a.nodes + 2 * (size_t)P->s_node_off;
       ncl = (P->s_n_elem + kCluster - 1) / kCluster;
       r = lane_root(P->s_leaves, lane);
-      if (r) walk_sub(nd, P->s_leaves, ncl, q, r, [&](int) { ++cnt; });
+      const int w = P->s_leaves < 32 ? P->s_leaves : 32, per = P->s_leaves / w;
+      masked = per <= 32;
+      leaf0 = r ? (r - w) * per : 0;
+      if (r)
+        walk_sub(nd, P->s_leaves, ncl, q, r, [&](int leaf) {
+          ++cnt;
+          if (masked) lmask |= 1u << (leaf - leaf0);
+        });
     }
   }
   const int lane_first = warp_incl_scan(cnt) - cnt;   // this lane's leaves follow the lanes' before it
@@ -390,11 +403,18 @@ __global__ void bp_kernel(StepArgs a) {
   if (lane == 0) a.unit_off[u] = off;
   if (!ucnt[wid]) return;
   int k = off + lane_first;
-  if (r)
+  if (r && masked) {
+    // ascending bits: the walk's left-to-right order
+    for (unsigned m = lmask; m; m &= m - 1) {
+      if (k < a.item_cap) a.items[k] = make_int4(p, leaf0 + __ffs(m) - 1, cl, 0);
+      ++k;
+    }
+  } else if (r) {
     walk_sub(nd, P->s_leaves, ncl, q, r, [&](int leaf) {
       if (k < a.item_cap) a.items[k] = make_int4(p, leaf, cl, 0);
       ++k;
     });
+  }
 }
 
 #include "narrow.cuh"
